@@ -1,0 +1,110 @@
+"""ctypes mirror of include/cg_erosion.h.
+
+The structs below follow the header field by field; ctypes lays them out with the C compiler's
+alignment rules, so a change to one side must be made to the other.
+"""
+import ctypes as C
+
+CG_ABI_VERSION = 1
+
+CG_OK, CG_CANCELLED, CG_TIMEOUT, CG_BAD_ARG, CG_OOM, CG_CUDA, CG_UNSUPPORTED = range(7)
+STATUS_NAMES = {
+    CG_OK: "OK", CG_CANCELLED: "CANCELLED", CG_TIMEOUT: "TIMEOUT", CG_BAD_ARG: "BAD_ARG",
+    CG_OOM: "OOM", CG_CUDA: "CUDA", CG_UNSUPPORTED: "UNSUPPORTED",
+}
+CG_MODE_REF32 = 0
+CG_PROFILE_P0, CG_PROFILE_P1, CG_PROFILE_P2 = 0, 1, 2
+
+
+class ThermalLimits(C.Structure):
+    _fields_ = [("east_west", C.c_float), ("north_south", C.c_float), ("diagonal", C.c_float)]
+
+
+class ErosionParams(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_uint32),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("mode", C.c_int32),
+        ("seed", C.c_int64),
+        ("world_width_km", C.c_double),
+        ("highest_land_metres", C.c_float),
+        ("deepest_ocean_metres", C.c_float),
+        ("years_per_hydraulic_round", C.c_double),
+        ("enabled", C.c_int32),
+        ("critical_fall_metres_per_km", C.c_float),
+        ("debris_travel_km", C.c_double),
+        ("rate", C.c_float),
+        ("hydraulic_rounds", C.c_int32),
+        ("bedrock_erodibility_per_year", C.c_float),
+        ("facet_routing", C.c_int32),
+        ("flat_potential", C.c_int32),
+        ("sea_level", C.c_float),
+        ("lowstand_metres", C.c_float),
+        ("receiver_clamp", C.c_int32),
+        ("shield_cut", C.c_int32),
+        ("profile", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class Inputs(C.Structure):
+    _fields_ = [
+        ("height", C.c_void_p),
+        ("uplift_mm_per_year", C.c_void_p),
+        ("rock_erodibility", C.c_void_p),
+        ("rainfall_mm", C.c_void_p),
+        ("vegetation_density", C.c_void_p),
+    ]
+
+
+class Basins(C.Structure):
+    _fields_ = [
+        ("capacity", C.c_int32),
+        ("count", C.c_int32),
+        ("spill", C.c_void_p),
+        ("entry", C.c_void_p),
+        ("level", C.c_void_p),
+        ("floor", C.c_void_p),
+        ("cells", C.c_void_p),
+        ("largest", C.c_int32),
+        ("largest_cells", C.c_int32),
+        ("largest_depth", C.c_float),
+        ("deepest", C.c_float),
+    ]
+
+
+class Outputs(C.Structure):
+    _fields_ = [
+        ("height", C.c_void_p),
+        ("receivers", C.c_void_p),
+        ("area", C.c_void_p),
+        ("filled", C.c_void_p),
+        ("relative", C.c_void_p),
+        ("is_land", C.c_void_p),
+        ("order", C.c_void_p),
+        ("basin_of_cell", C.c_void_p),
+        ("donors", C.c_void_p),
+        ("basins", C.POINTER(Basins)),
+    ]
+
+
+class RoundStats(C.Structure):
+    _fields_ = [
+        ("round", C.c_int32),
+        ("land_cells", C.c_int32),
+        ("shoreline", C.c_float),
+        ("basins", C.c_int32),
+        ("flats", C.c_int32),
+        ("flats_kept", C.c_int32),
+        ("raised_cells", C.c_int32),
+        ("levels", C.c_int32),
+        ("fill_ties", C.c_int64),
+        ("fill_unresolved", C.c_int64),
+        ("ms_total", C.c_double),
+    ]
+
+
+def ptr(a):
+    """Address of a numpy array's data, or None."""
+    return None if a is None else a.ctypes.data

@@ -1,0 +1,226 @@
+/*
+ * cg_erosion.h - C ABI of the GB300-native erosion stage.
+ *
+ * This library replaces Cartogenesis's per-round erosion stage on one GPU:
+ *   ErosionStage.apply -> HydraulicErosion.apply, with the thermal relaxation between rounds
+ *   (worldgen/src/commonMain/kotlin/com/cartogenesis/worldgen/pipeline/ErosionStage.kt:133-183,
+ *    .../pipeline/HydraulicErosion.kt:596-1506).
+ * The reference has exactly one device seam, ErosionAccelerator.erode
+ * (.../pipeline/ErosionAccelerator.kt:15-45); cg_thermal_sweeps keeps its contract. The hydraulic
+ * rounds have no seam in the reference, so cg_erode_stage is the new one a Kotlin
+ * `HydraulicAccelerator` binds through FFM or JNI in place of HydraulicErosion.apply.
+ *
+ * Conventions
+ *  - Every function returns a cg_status; no exception crosses the ABI.
+ *  - Buffers are caller-owned HOST memory unless a name says `_dev`. Inputs are never written.
+ *  - Grids are row-major, cell = row * width + column; x wraps east-west, y stops at the poles
+ *    (FloatField, .../model/FloatField.kt:7).
+ *  - Heights are in the height field's own 0..1 units; relative elevations are shoreline-relative,
+ *    1 = WorldScale.highestLandMetres above, -1 = deepestOceanMetres below.
+ *  - One context per thread, or serialise calls on a context. cg_cancel may be called from any
+ *    thread or a signal handler.
+ *  - No CPU fallback: if the device cannot run the job the call fails with a status.
+ */
+#ifndef CG_EROSION_H
+#define CG_EROSION_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_ABI_VERSION 1u
+
+typedef enum cg_status {
+    CG_OK = 0,
+    CG_CANCELLED = 1,   /* cg_cancel was seen between phases; outputs are not written */
+    CG_TIMEOUT = 2,     /* a bounded device-side wait ran out; the context stays usable */
+    CG_BAD_ARG = 3,     /* a size, pointer or parameter failed validation */
+    CG_OOM = 4,         /* device or pinned-host allocation failed */
+    CG_CUDA = 5,        /* a CUDA call failed; cg_last_error says which */
+    CG_UNSUPPORTED = 6  /* a switch this build does not implement (e.g. profile P2) */
+} cg_status;
+
+/* Parity mode. REF32 is the reference's own arithmetic (FP32 field, FP64 where Kotlin promotes). */
+typedef enum cg_mode { CG_MODE_REF32 = 0 } cg_mode;
+
+/*
+ * Round-tail profile. P0: uplift, percentile cut, weights, fill, routing, accumulation, incision
+ * and relaxation (climateFeed, deposition, outletIncision, flexure and the belt replay off).
+ */
+typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2 } cg_profile;
+
+/* ThermalLimits (.../pipeline/ErosionAccelerator.kt:58-65): steepest drop per neighbour kind. */
+typedef struct cg_thermal_limits {
+    float east_west;
+    float north_south;
+    float diagonal;
+} cg_thermal_limits;
+
+/*
+ * The WorldGenConfig fields the stage reads (.../model/WorldGenConfig.kt: WorldScale 32-304,
+ * ErosionConfig 2068-2496, WorldGenConfig 3236-3384, SeaConfig.lowstandMetres 1580), plus the
+ * test-only switches ErodeBlocking exposes (.../jvmMain/.../pipeline/ErodeBlocking.kt:61-104).
+ * cg_default_params fills the reference defaults.
+ */
+typedef struct cg_erosion_params {
+    uint32_t abi_version;                 /* CG_ABI_VERSION */
+    int32_t  width;                       /* cells across, a power of two */
+    int32_t  height;                      /* cells down, a power of two */
+    int32_t  mode;                        /* cg_mode */
+    int64_t  seed;                        /* WorldGenConfig.seed */
+    /* WorldScale */
+    double   world_width_km;              /* 40075 */
+    float    highest_land_metres;         /* 6000 */
+    float    deepest_ocean_metres;        /* 10000 */
+    double   years_per_hydraulic_round;   /* 336476.4 */
+    /* ErosionConfig */
+    int32_t  enabled;                     /* 1 */
+    float    critical_fall_metres_per_km; /* 60 */
+    double   debris_travel_km;            /* 1875 */
+    float    rate;                        /* 0.25 */
+    int32_t  hydraulic_rounds;            /* 12 */
+    float    bedrock_erodibility_per_year;/* 1e-6 */
+    /* WorldGenConfig top level */
+    int32_t  facet_routing;               /* 1 */
+    int32_t  flat_potential;              /* 1 */
+    float    sea_level;                   /* 0.71 */
+    float    lowstand_metres;             /* SeaConfig.lowstandMetres, 120 */
+    /* Test switches, never set by a production caller */
+    int32_t  receiver_clamp;              /* 1: HydraulicErosion.incise onlyAboveBase */
+    int32_t  shield_cut;                  /* 1: incision takes the cover's factor */
+    int32_t  profile;                     /* cg_profile; only P0 is implemented */
+    int32_t  reserved;
+} cg_erosion_params;
+
+/* Per-cell inputs of one world (ErosionTectonics + the weather the rounds cut with). */
+typedef struct cg_inputs {
+    const float* height;               /* required: uplifted terrain, field units */
+    const float* uplift_mm_per_year;   /* or NULL: ErosionTectonics.upliftRateMmPerYear */
+    const float* rock_erodibility;     /* or NULL: ErosionTectonics.rockErodibility */
+    const float* rainfall_mm;          /* or NULL (all 1): HydraulicErosion.Weather.rainfallMm */
+    const float* vegetation_density;   /* or NULL (all 0): HydraulicErosion.Weather.vegetationDensity */
+} cg_inputs;
+
+/* The last round's basins (FlowRouting.Spillways, .../pipeline/FlowRouting.kt:519-544). */
+typedef struct cg_basins {
+    int32_t  capacity;       /* entries each array below holds */
+    int32_t  count;          /* basins found (may exceed capacity: arrays then hold the first) */
+    int32_t* spill;          /* pour point or -1 */
+    int32_t* entry;          /* lowest exit, ties on index, or -1 */
+    float*   level;
+    float*   floor;
+    int32_t* cells;
+    int32_t  largest;
+    int32_t  largest_cells;
+    float    largest_depth;
+    float    deepest;
+} cg_basins;
+
+/* What cg_erode_stage hands back. Every pointer except height may be NULL. */
+typedef struct cg_outputs {
+    float*    height;          /* required: N, the stage's result (ErosionResult.height) */
+    int32_t*  receivers;       /* N: last round's flowDirections, -1 = none */
+    float*    area;            /* N: last round's accumulate */
+    float*    filled;          /* N: last round's fillDepressions */
+    float*    relative;        /* N: last round's shoreline-relative field */
+    uint8_t*  is_land;         /* N: last round's land mask */
+    int32_t*  order;           /* N: last round's drainageOrder, land cells first */
+    int32_t*  basin_of_cell;   /* N: last round's basin label of each ponded cell, else -1 */
+    int32_t*  donors;          /* N: last round's donor count (land donors into a land cell) */
+    cg_basins* basins;         /* last round's spillways */
+} cg_outputs;
+
+/* One hydraulic round's bookkeeping, an observer only (like RoundMass). */
+typedef struct cg_round_stats {
+    int32_t round;
+    int32_t land_cells;
+    float   shoreline;
+    int32_t basins;
+    int32_t flats;              /* FlatRouting.Surface.flats */
+    int32_t flats_kept;         /* FlatRouting.Surface.flatsKept */
+    int32_t raised_cells;       /* FlatRouting.Surface.raisedCells */
+    int32_t levels;             /* drainage levels (longest donor chain + 1) */
+    int64_t fill_ties;          /* cells whose fill parent was decided on a quantised-key tie */
+    int64_t fill_unresolved;    /* of those, ties the fill could not order exactly (expected 0) */
+    double  ms_total;           /* device time of the round, milliseconds */
+} cg_round_stats;
+
+typedef struct cg_ctx cg_ctx;
+
+/* Fills reference defaults (WorldGenConfig(seed, width, height), P0 switches). */
+void cg_default_params(cg_erosion_params* params, int32_t width, int32_t height, int64_t seed);
+
+/* The thermal limits and sweep count the reference derives (ErosionStage.kt:412-437). */
+cg_status cg_thermal_limits_for(const cg_erosion_params* params, cg_thermal_limits* limits,
+                                int32_t* sweeps);
+
+cg_status cg_create(cg_ctx** ctx, int32_t device);
+void      cg_destroy(cg_ctx* ctx);
+/* Async-signal-safe: sets a flag the stage polls between phases and rounds. */
+void      cg_cancel(cg_ctx* ctx);
+/* The message of the last failure on this context (static storage, never NULL). */
+const char* cg_last_error(const cg_ctx* ctx);
+
+/*
+ * ErosionAccelerator.erode (.../pipeline/ErosionAccelerator.kt:38-45; ErosionStage.kt:235-403):
+ * `passes` Musgrave sweeps over heights_in into heights_out (a separate array).
+ */
+cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t width, int32_t height, const float* heights_in,
+                            float* heights_out, cg_thermal_limits limits, int32_t passes, float rate);
+
+/*
+ * ErosionStage.apply (.../pipeline/ErosionStage.kt:133-183) with HydraulicErosion.apply
+ * (.../pipeline/HydraulicErosion.kt:596-1506): the initial thermal sweeps, then the hydraulic
+ * rounds, each relaxed by sweepsFor/rounds sweeps. `stats`, if not NULL, receives one entry per
+ * round (hydraulic_rounds entries).
+ */
+cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs,
+                         cg_outputs* outputs, cg_round_stats* stats);
+
+/* ---- The stage's routing functions, each run alone on host buffers (FlowRouting, SeaLevelStage) ---- */
+
+/* SeaLevelStage.percentileCut (.../pipeline/SeaLevelStage.kt:146-200, 579-651). */
+cg_status cg_percentile_cut(cg_ctx* ctx, int32_t width, int32_t height, const float* heights,
+                            float sea_level_fraction, float highest_land_metres,
+                            float deepest_ocean_metres, float lowstand_share_of_field,
+                            float* shoreline, uint8_t* is_land, float* relative,
+                            int32_t* land_cells);
+
+/* FlowRouting.fillDepressions (.../pipeline/FlowRouting.kt:52-111). */
+cg_status cg_fill_depressions(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
+                              const float* relative, float* filled, int64_t* ties,
+                              int64_t* unresolved);
+
+/*
+ * FlowRouting.flowDirections (.../pipeline/FlowRouting.kt:179-216) with FlatRouting.surfaceOf
+ * (.../pipeline/FlatRouting.kt:58-138). `surface` (N doubles) may be NULL; `flat_counts` may be
+ * NULL or receives {flats, flatsKept, raisedCells}.
+ */
+cg_status cg_flow_directions(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
+                             const float* relative, const float* filled, int64_t seed,
+                             double cell_height_in_cell_widths, int32_t smooth_lattice_columns,
+                             int32_t by_facet, int32_t over_potential, int32_t* receivers,
+                             double* surface, int32_t* flat_counts);
+
+/* FlowRouting.drainageOrder (.../pipeline/FlowRouting.kt:695-729); `order` holds land_cells. */
+cg_status cg_drainage_order(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
+                            const int32_t* receivers, int32_t land_cells, int32_t* order);
+
+/* FlowRouting.accumulate (.../pipeline/FlowRouting.kt:485-511) with per-cell weights. */
+cg_status cg_accumulate(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
+                        const int32_t* receivers, int32_t land_cells, const float* weights,
+                        float* area);
+
+/* FlowRouting.spillways (.../pipeline/FlowRouting.kt:573-677). */
+cg_status cg_spillways(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
+                       const float* relative, const float* filled, const int32_t* receivers,
+                       float pond_depth, int32_t* basin_of_cell, cg_basins* basins);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CG_EROSION_H */

@@ -1,0 +1,235 @@
+"""TEST INFRASTRUCTURE ONLY - the oracle.
+
+A CPU restatement of Cartogenesis's erosion stage (cg_oracle.cpp), loaded through ctypes. Only
+the tests, the smoke check and bench.py's CPU-baseline leg may use it, and only as the checker or
+the timed CPU stand-in; the product path (cartogenesis_gb300) never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from cartogenesis_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+SOURCES = [os.path.join(HERE, "cg_oracle.cpp")]
+# -ffp-contract=off: the JVM never fuses a multiply and an add, and neither may the restatement.
+CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
+
+
+def build(force=False):
+    """Compile the oracle into oracle/_build/liboracle.so (seconds)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "..", "include", "cg_erosion.h")])
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    tmp = LIB_PATH + f".{os.getpid()}.tmp"
+    subprocess.check_call(["g++", *CXXFLAGS, "-o", tmp, *SOURCES])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, i32, i64, f32, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_double
+        L.or_default_params.argtypes = [C.POINTER(abi.ErosionParams), i32, i32, i64]
+        L.or_thermal_limits.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.ThermalLimits), C.POINTER(i32)]
+        L.or_thermal_sweep.argtypes = [i32, i32, vp, vp, f32, f32, f32, i32, f32, i32]
+        L.or_percentile_cut.argtypes = [i32, i32, vp, f32, f32, f32, f32, C.POINTER(f32), vp, vp]
+        L.or_percentile_cut.restype = i32
+        L.or_fill_depressions.argtypes = [i32, i32, vp, vp, vp]
+        L.or_flow_directions.argtypes = [i32, i32, vp, vp, vp, i64, f64, i32, i32, i32, vp, vp, vp]
+        L.or_drainage_order.argtypes = [i32, i32, vp, vp, i32, vp]
+        L.or_accumulate.argtypes = [i32, i32, vp, vp, i32, vp, vp]
+        L.or_spillways.argtypes = [i32, i32, vp, vp, vp, vp, f32, vp, C.POINTER(abi.Basins)]
+        L.or_spillways.restype = i32
+        L.or_incise.argtypes = [C.POINTER(abi.ErosionParams), vp, i32, vp, vp, vp, vp, vp, f32, f32, f32, vp, vp,
+                                i32, vp]
+        L.or_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)]
+        L.or_stand_below_today.argtypes = [C.POINTER(abi.ErosionParams), i32]
+        L.or_stand_below_today.restype = f32
+        L.or_seeded_noise.argtypes = [i32, i32, i64]
+        L.or_seeded_noise.restype = f32
+        L.or_smooth_seeded_field.argtypes = [i32, i32, i32, i32, i64]
+        L.or_smooth_seeded_field.restype = f32
+        L.or_erode_stage.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), C.POINTER(abi.Outputs),
+                                     vp]
+        L.or_erode_stage.restype = i32
+        L.or_hydraulic_apply.argtypes = L.or_erode_stage.argtypes
+        L.or_hydraulic_apply.restype = i32
+        _lib = L
+    return _lib
+
+
+P = abi.ptr
+
+
+def default_params(width, height, seed=1, **overrides):
+    p = abi.ErosionParams()
+    lib().or_default_params(C.byref(p), width, height, seed)
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def thermal_limits(params):
+    lim = abi.ThermalLimits()
+    sweeps = C.c_int32()
+    lib().or_thermal_limits(C.byref(params), C.byref(lim), C.byref(sweeps))
+    return lim, sweeps.value
+
+
+def thermal_sweep(height, limits, sweeps, rate=0.25, skip=True):
+    h = np.ascontiguousarray(height, dtype=np.float32)
+    H, W = h.shape
+    out = np.empty_like(h)
+    lib().or_thermal_sweep(W, H, P(h), P(out), limits.east_west, limits.north_south, limits.diagonal, sweeps,
+                           rate, 1 if skip else 0)
+    return out
+
+
+def percentile_cut(height, sea_level, lowstand_share=0.0, highest_land=6000.0, deepest_ocean=10000.0):
+    h = np.ascontiguousarray(height, dtype=np.float32)
+    H, W = h.shape
+    is_land = np.empty((H, W), np.uint8)
+    rel = np.empty((H, W), np.float32)
+    s = C.c_float()
+    n = lib().or_percentile_cut(W, H, P(h), sea_level, highest_land, deepest_ocean, lowstand_share, C.byref(s),
+                                P(is_land), P(rel))
+    return s.value, is_land, rel, n
+
+
+def fill_depressions(is_land, relative):
+    H, W = relative.shape
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rel = np.ascontiguousarray(relative, dtype=np.float32)
+    out = np.empty_like(rel)
+    lib().or_fill_depressions(W, H, P(il), P(rel), P(out))
+    return out
+
+
+def flow_directions(is_land, relative, filled, seed, r, lattice, by_facet=True, over_potential=True,
+                    want_surface=False):
+    H, W = relative.shape
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rel = np.ascontiguousarray(relative, dtype=np.float32)
+    fil = np.ascontiguousarray(filled, dtype=np.float32)
+    rec = np.empty((H, W), np.int32)
+    surf = np.empty((H, W), np.float64) if want_surface else None
+    counts = np.zeros(3, np.int32)
+    lib().or_flow_directions(W, H, P(il), P(rel), P(fil), seed, r, lattice, int(by_facet), int(over_potential),
+                             P(rec), P(surf), P(counts))
+    return (rec, surf, counts) if want_surface else (rec, counts)
+
+
+def drainage_order(is_land, receivers, land_cells):
+    H, W = receivers.shape
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rec = np.ascontiguousarray(receivers, dtype=np.int32)
+    order = np.empty(max(land_cells, 1), np.int32)
+    lib().or_drainage_order(W, H, P(il), P(rec), land_cells, P(order))
+    return order[:land_cells]
+
+
+def accumulate(is_land, receivers, land_cells, weights):
+    H, W = receivers.shape
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rec = np.ascontiguousarray(receivers, dtype=np.int32)
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    area = np.empty((H, W), np.float32)
+    lib().or_accumulate(W, H, P(il), P(rec), land_cells, P(w), P(area))
+    return area
+
+
+def spillways(is_land, relative, filled, receivers, pond_depth):
+    H, W = relative.shape
+    N = W * H
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rel = np.ascontiguousarray(relative, dtype=np.float32)
+    fil = np.ascontiguousarray(filled, dtype=np.float32)
+    rec = np.ascontiguousarray(receivers, dtype=np.int32)
+    labels = np.empty((H, W), np.int32)
+    arrays = {k: np.empty(N, dt) for k, dt in
+              [("spill", np.int32), ("entry", np.int32), ("level", np.float32), ("floor", np.float32),
+               ("cells", np.int32)]}
+    b = abi.Basins(capacity=N, count=0, **{k: P(v) for k, v in arrays.items()})
+    n = lib().or_spillways(W, H, P(il), P(rel), P(fil), P(rec), pond_depth, P(labels), C.byref(b))
+    out = {k: v[:n].copy() for k, v in arrays.items()}
+    out.update(count=n, largest=b.largest, largest_cells=b.largest_cells, largest_depth=b.largest_depth,
+               deepest=b.deepest, labels=labels)
+    return out
+
+
+def rates(params):
+    a, b, c = C.c_float(), C.c_float(), C.c_float()
+    lib().or_rates(C.byref(params), C.byref(a), C.byref(b), C.byref(c))
+    return a.value, b.value, c.value
+
+
+def incise(params, order, directions, is_land, ground, relative, discharge, land_cells, land_range, shoreline,
+           erodibility, surface, only_above_base=True, unresolved=None):
+    """HydraulicErosion.incise; `surface` (float32, contiguous) is updated in place."""
+    dts = (np.int32, np.int32, np.uint8, np.float32, np.float32, np.float32, np.float32)
+    # Held in locals for the whole call: ctypes only sees their addresses.
+    order, directions, is_land, ground, relative, discharge, erodibility = [
+        np.ascontiguousarray(a, dtype=dt).ravel() for a, dt in
+        zip((order, directions, is_land, ground, relative, discharge, erodibility), dts)]
+    unresolved = None if unresolved is None else np.ascontiguousarray(unresolved, np.float32)
+    assert surface.dtype == np.float32 and surface.flags.c_contiguous
+    lib().or_incise(C.byref(params), P(order), len(order), P(directions), P(is_land), P(ground), P(relative),
+                    P(discharge), land_cells, land_range, shoreline, P(erodibility), P(surface),
+                    int(only_above_base), P(unresolved))
+
+
+def stand_below_today(params, round_):
+    return lib().or_stand_below_today(C.byref(params), round_)
+
+
+def seeded_noise(c, r, seed):
+    return lib().or_seeded_noise(c, r, seed)
+
+
+def erode_stage(params, height, uplift=None, rock=None, rain=None, veg=None, thermal=True, want=("receivers", "area", "filled",
+                                                                                    "relative", "is_land", "order",
+                                                                                    "basin_of_cell", "donors")):
+    H, W = params.height, params.width
+    N = W * H
+    keep = []
+
+    def f32(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+        keep.append(a)
+        return a
+
+    h, up, rk, rn, vg = map(f32, (height, uplift, rock, rain, veg))
+    inputs = abi.Inputs(P(h), P(up), P(rk), P(rn), P(vg))
+    outs = {"height": np.empty((H, W), np.float32)}
+    kinds = {"receivers": np.int32, "area": np.float32, "filled": np.float32, "relative": np.float32,
+             "is_land": np.uint8, "order": np.int32, "basin_of_cell": np.int32, "donors": np.int32}
+    for k in want:
+        outs[k] = np.empty((H, W), kinds[k])
+    basins_arrays = {k: np.empty(N, dt) for k, dt in
+                     [("spill", np.int32), ("entry", np.int32), ("level", np.float32), ("floor", np.float32),
+                      ("cells", np.int32)]}
+    basins = abi.Basins(capacity=N, count=0, **{k: P(v) for k, v in basins_arrays.items()})
+    o = abi.Outputs(**{k: P(v) for k, v in outs.items()}, basins=C.pointer(basins))
+    stats = (abi.RoundStats * max(params.hydraulic_rounds, 1))()
+    fn = lib().or_erode_stage if thermal else lib().or_hydraulic_apply
+    st = fn(C.byref(params), C.byref(inputs), C.byref(o), C.cast(stats, C.c_void_p))
+    assert st == 0, st
+    outs["basins"] = {k: v[:basins.count].copy() for k, v in basins_arrays.items()}
+    outs["basins"].update(count=basins.count, largest=basins.largest, largest_cells=basins.largest_cells,
+                          largest_depth=basins.largest_depth, deepest=basins.deepest)
+    outs["stats"] = [{f: getattr(s, f) for f, _ in abi.RoundStats._fields_} for s in stats]
+    return outs
