@@ -1,0 +1,239 @@
+"""Python mirror of the reference's entry points for the erosion stage, on libcg_erosion.so.
+
+Names, argument meanings and units follow the Kotlin (P = worldgen/src/commonMain/kotlin/com/
+cartogenesis/worldgen/pipeline):
+  GpuErosionAccelerator.erode  -> ErosionAccelerator.erode   (P/ErosionAccelerator.kt:38-45)
+  ErosionStage.apply           -> ErosionStage.apply         (P/ErosionStage.kt:110-183)
+  SeaLevelStage.percentile_cut -> SeaLevelStage.percentileCut (P/SeaLevelStage.kt:146-200)
+  FlowRouting.*                -> FlowRouting.fillDepressions, flowDirections, drainageOrder,
+                                  accumulate, spillways (P/FlowRouting.kt)
+Arrays are numpy, row-major [height, width]. Every call runs on the GPU; none falls back to a CPU.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .runtime import CgError, Context, load_library
+
+P = abi.ptr
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+@dataclass
+class ThermalLimits:
+    """ThermalLimits (P/ErosionAccelerator.kt:58-65), field units per neighbour kind."""
+    east_west: float
+    north_south: float
+    diagonal: float
+
+    def to_c(self):
+        return abi.ThermalLimits(self.east_west, self.north_south, self.diagonal)
+
+
+class ErosionConfig:
+    """The WorldGenConfig fields the stage reads, as cg_erosion_params.
+
+    ErosionConfig(width, height, seed, sea_level=0.70, hydraulic_rounds=12, ...): any field of
+    cg_erosion_params may be given by name; the rest keep the reference defaults.
+    """
+
+    def __init__(self, width, height, seed=1, **fields):
+        self.params = abi.ErosionParams()
+        load_library().cg_default_params(C.byref(self.params), width, height, seed)
+        for k, v in fields.items():
+            if not hasattr(self.params, k):
+                raise AttributeError(f"cg_erosion_params has no field {k}")
+            setattr(self.params, k, v)
+
+    def __getattr__(self, name):
+        return getattr(self.__dict__["params"], name)
+
+    @property
+    def cells(self):
+        return self.params.width * self.params.height
+
+    def thermal_limits(self):
+        lim = abi.ThermalLimits()
+        sweeps = C.c_int32()
+        st = load_library().cg_thermal_limits_for(C.byref(self.params), C.byref(lim), C.byref(sweeps))
+        if st != abi.CG_OK:
+            raise CgError(st, "cg_thermal_limits_for")
+        return ThermalLimits(lim.east_west, lim.north_south, lim.diagonal), sweeps.value
+
+
+def _f32(a, shape):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.size != shape[0] * shape[1]:
+        raise ValueError(f"array of {a.size} cells for a {shape[1]} x {shape[0]} grid")
+    return a.reshape(shape)
+
+
+class GpuErosionAccelerator:
+    """ErosionAccelerator on the GB300: the thermal sweeps alone (P/ErosionAccelerator.kt:38-45)."""
+
+    name = "GB300 (sm_103a)"
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+
+    def erode(self, width, height, heights, limits, passes, rate):
+        """`passes` sweeps; `heights` is not modified and the result is a new array."""
+        h = _f32(heights, (height, width))
+        out = np.empty_like(h)
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_thermal_sweeps(self.ctx.handle, width, height, P(h), P(out),
+                                                          limits.to_c(), passes, rate))
+        return out
+
+
+class ErosionResult:
+    """ErosionResult (P/ErosionStage.kt:11-22) plus the last round's routing the C ABI hands back."""
+
+    def __init__(self, height, **extra):
+        self.height = height
+        self.swept_on_device = True
+        self.__dict__.update(extra)
+
+
+class ErosionStage:
+    """ErosionStage.apply on the GPU (P/ErosionStage.kt:133-183 with HydraulicErosion.apply)."""
+
+    WANT = ("receivers", "area", "filled", "relative", "is_land", "order", "basin_of_cell", "donors")
+    KINDS = {"receivers": np.int32, "area": np.float32, "filled": np.float32, "relative": np.float32,
+             "is_land": np.uint8, "order": np.int32, "basin_of_cell": np.int32, "donors": np.int32}
+
+    @staticmethod
+    def apply(config, height, uplift_mm_per_year=None, rock_erodibility=None, rainfall_mm=None,
+              vegetation_density=None, want=WANT, ctx=None):
+        ctx = ctx or default_context()
+        H, W = config.params.height, config.params.width
+        keep = [_f32(a, (H, W)) for a in (height, uplift_mm_per_year, rock_erodibility, rainfall_mm,
+                                         vegetation_density)]
+        inputs = abi.Inputs(*[P(a) for a in keep])
+        outs = {"height": np.empty((H, W), np.float32)}
+        for k in want:
+            outs[k] = np.empty((H, W), ErosionStage.KINDS[k])
+        N = W * H
+        barrays = {k: np.empty(N, dt) for k, dt in [("spill", np.int32), ("entry", np.int32),
+                                                    ("level", np.float32), ("floor", np.float32),
+                                                    ("cells", np.int32)]}
+        basins = abi.Basins(capacity=N, count=0, **{k: P(v) for k, v in barrays.items()})
+        o = abi.Outputs(**{k: P(v) for k, v in outs.items()}, basins=C.pointer(basins))
+        rounds = max(config.params.hydraulic_rounds, 1)
+        stats = (abi.RoundStats * rounds)()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_erode_stage(ctx.handle, C.byref(config.params), C.byref(inputs), C.byref(o),
+                                             C.cast(stats, C.c_void_p)))
+        outs["basins"] = {k: v[:min(basins.count, N)].copy() for k, v in barrays.items()}
+        outs["basins"].update(count=basins.count, largest=basins.largest, largest_cells=basins.largest_cells,
+                              largest_depth=basins.largest_depth, deepest=basins.deepest)
+        outs["stats"] = [{f: getattr(s, f) for f, _ in abi.RoundStats._fields_} for s in stats]
+        return ErosionResult(**outs)
+
+
+class SeaLevelStage:
+    @staticmethod
+    def percentile_cut(height, sea_level_fraction, lowstand_share_of_field=0.0, highest_land_metres=6000.0,
+                       deepest_ocean_metres=10000.0, ctx=None):
+        """SeaLevelStage.percentileCut: (shoreline, is_land, relative, land_cells)."""
+        ctx = ctx or default_context()
+        h = np.ascontiguousarray(height, dtype=np.float32)
+        H, W = h.shape
+        is_land = np.empty((H, W), np.uint8)
+        rel = np.empty((H, W), np.float32)
+        s = C.c_float()
+        n = C.c_int32()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_percentile_cut(ctx.handle, W, H, P(h), sea_level_fraction, highest_land_metres,
+                                                deepest_ocean_metres, lowstand_share_of_field, C.byref(s),
+                                                P(is_land), P(rel), C.byref(n)))
+        return s.value, is_land, rel, n.value
+
+
+class FlowRouting:
+    @staticmethod
+    def fill_depressions(is_land, elevation, ctx=None, with_ties=False):
+        ctx = ctx or default_context()
+        rel = np.ascontiguousarray(elevation, dtype=np.float32)
+        H, W = rel.shape
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        out = np.empty_like(rel)
+        ties, unresolved = C.c_int64(), C.c_int64()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_fill_depressions(ctx.handle, W, H, P(il), P(rel), P(out), C.byref(ties),
+                                                  C.byref(unresolved)))
+        return (out, ties.value, unresolved.value) if with_ties else out
+
+    @staticmethod
+    def flow_directions(is_land, elevation, filled, seed, cell_height_in_cell_widths, smooth_lattice_columns,
+                        by_facet=True, over_potential=True, want_surface=False, ctx=None):
+        ctx = ctx or default_context()
+        rel = np.ascontiguousarray(elevation, dtype=np.float32)
+        H, W = rel.shape
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        fil = np.ascontiguousarray(filled, dtype=np.float32)
+        rec = np.empty((H, W), np.int32)
+        surf = np.empty((H, W), np.float64) if want_surface else None
+        counts = np.zeros(3, np.int32)
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_flow_directions(ctx.handle, W, H, P(il), P(rel), P(fil), seed,
+                                                 cell_height_in_cell_widths, smooth_lattice_columns, int(by_facet),
+                                                 int(over_potential), P(rec), P(surf), P(counts)))
+        return (rec, surf, counts) if want_surface else (rec, counts)
+
+    @staticmethod
+    def drainage_order(is_land, receivers, land_cells, ctx=None):
+        ctx = ctx or default_context()
+        rec = np.ascontiguousarray(receivers, dtype=np.int32)
+        H, W = rec.shape
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        order = np.empty(max(land_cells, 1), np.int32)
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_drainage_order(ctx.handle, W, H, P(il), P(rec), land_cells, P(order)))
+        return order[:land_cells]
+
+    @staticmethod
+    def accumulate(is_land, receivers, land_cells, weights, ctx=None):
+        ctx = ctx or default_context()
+        rec = np.ascontiguousarray(receivers, dtype=np.int32)
+        H, W = rec.shape
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        area = np.empty((H, W), np.float32)
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_accumulate(ctx.handle, W, H, P(il), P(rec), land_cells, P(w), P(area)))
+        return area
+
+    @staticmethod
+    def spillways(is_land, elevation, filled, receivers, pond_depth, ctx=None):
+        ctx = ctx or default_context()
+        rel = np.ascontiguousarray(elevation, dtype=np.float32)
+        H, W = rel.shape
+        N = W * H
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        fil = np.ascontiguousarray(filled, dtype=np.float32)
+        rec = np.ascontiguousarray(receivers, dtype=np.int32)
+        labels = np.empty((H, W), np.int32)
+        arrays = {k: np.empty(N, dt) for k, dt in [("spill", np.int32), ("entry", np.int32),
+                                                   ("level", np.float32), ("floor", np.float32),
+                                                   ("cells", np.int32)]}
+        b = abi.Basins(capacity=N, count=0, **{k: P(v) for k, v in arrays.items()})
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_spillways(ctx.handle, W, H, P(il), P(rel), P(fil), P(rec), pond_depth, P(labels),
+                                           C.byref(b)))
+        out = {k: v[:b.count].copy() for k, v in arrays.items()}
+        out.update(count=b.count, largest=b.largest, largest_cells=b.largest_cells, largest_depth=b.largest_depth,
+                   deepest=b.deepest, labels=labels)
+        return out

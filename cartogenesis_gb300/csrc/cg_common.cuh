@@ -1,0 +1,95 @@
+// Shared device helpers and the context of the GB300 erosion stage.
+//
+// Every kernel of this library is compiled with --fmad=false and IEEE division and square root:
+// the reference runs on the JVM, which never fuses a multiply and an add, and the REF32 mode
+// reproduces its float arithmetic bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/cg_erosion.h"
+
+namespace cg {
+
+constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
+
+// Neighbour order of ErosionStage's thermal sweep (ErosionStage.kt:460-461): E, W, S, N, then the
+// diagonals (+1,+1), (+1,-1), (-1,+1), (-1,-1) as (column step, row step).
+__host__ __device__ constexpr int thermal_col_step(int n) { return n == 0 ? 1 : n == 1 ? -1 : n < 4 ? 0 : (n < 6 ? 1 : -1); }
+__host__ __device__ constexpr int thermal_row_step(int n) { return n == 0 || n == 1 ? 0 : n == 2 ? 1 : n == 3 ? -1 : ((n & 1) == 0 ? 1 : -1); }
+
+__device__ __forceinline__ int wrap_col(int c, int W) {
+    int r = c % W;
+    return r < 0 ? r + W : r;
+}
+
+// Float <-> raw bits, as Float.toRawBits.
+__device__ __forceinline__ int32_t float_bits(float f) { return __float_as_int(f); }
+
+// Growable device buffer owned by the context.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Timer;
+
+}  // namespace cg
+
+// The library context (opaque in the C ABI).
+struct cg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::atomic<int> cancel{0};
+    char error[512] = {0};
+    // Named scratch buffers, grown on demand and reused across calls.
+    cg::DevBuf bufs[64];
+    // Pinned host staging.
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    int num_sms = cg::kSMs;
+    // Row-weight table of the sea-level cut, cached for the last grid shape.
+    int rw_w = 0, rw_h = 0;
+    double rw_total = 0.0;
+};
+
+namespace cg {
+
+// Buffer slots of cg_ctx::bufs.
+enum Slot {
+    S_H0, S_H1, S_GIVE, S_UPLIFT, S_ROCK, S_RAIN, S_VEG, S_RUNOFF, S_ERODE, S_LAND, S_REL, S_FILLED,
+    S_SURFACE, S_RECV, S_DONORS, S_KEY, S_ORDER, S_AREA, S_WATER, S_LABEL, S_PTR, S_PTR2, S_SCRATCH0,
+    S_SCRATCH1, S_SCRATCH2, S_SCRATCH3, S_ROWW, S_HIST, S_BRACKET, S_BRACKET2, S_SMALL, S_FLATS,
+    S_FLATIDX, S_FLATMEM, S_CG0, S_CG1, S_CG2, S_CG3, S_CG4, S_CG5, S_LEVELCNT, S_DEPTH, S_STATS,
+    S_BASIN, S_BASIN2, S_FILLQ, S_FILLF, S_FILLFLAG, S_TILEFLAG, S_SCRATCH4, S_SCRATCH5,
+    S_COUNT
+};
+
+cg_status fail(cg_ctx* ctx, cg_status st, const char* fmt, ...);
+cg_status cuda_fail(cg_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
+// Returns a device pointer of at least `bytes` for `slot`, growing it if needed.
+void* buf(cg_ctx* ctx, int slot, size_t bytes, cg_status* st);
+void* pinned(cg_ctx* ctx, size_t bytes, cg_status* st);
+
+}  // namespace cg
+
+#define CG_CUDA(ctx, call)                                                       \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) return cg::cuda_fail((ctx), e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define CG_CHECK_LAUNCH(ctx) CG_CUDA(ctx, cudaGetLastError())
+
+#define CG_BUF(T, name, ctx, slot, count)                                        \
+    T* name;                                                                     \
+    {                                                                            \
+        cg_status st_ = CG_OK;                                                   \
+        name = (T*)cg::buf((ctx), (slot), sizeof(T) * (size_t)(count), &st_);    \
+        if (st_ != CG_OK) return st_;                                            \
+    }

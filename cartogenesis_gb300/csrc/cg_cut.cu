@@ -1,0 +1,319 @@
+// SeaLevelStage.percentileCut on the device (SeaLevelStage.kt:146-200, 579-651), bit-exact.
+//
+// The reference finds the height with the asked share of the planet's area below it: a 4096-bin
+// histogram of cos(latitude) row weights brackets the answer, then the bracketing bin's cells are
+// sorted by (height bits, index) and walked until the area below reaches the target. Both sums are
+// sequential double sums in the reference, and the answer can flip on their last bit, so both are
+// reproduced exactly:
+//  - the histogram: per (row, bin) cell counts are exact integers, and each bin's sequential sum
+//    over the rows in order is rebuilt with cg::seq_repeat_add, which replays `count` additions of
+//    the row's weight exactly (csrc/cg_fpemu.h);
+//  - the bracket: its cells are sorted on the device and walked by one thread in the reference's
+//    order (a few thousand cells on the benchmark worlds).
+// min, max, the bin of a cell and the land/relative split are elementwise or exact reductions.
+#include <cmath>
+#include <vector>
+
+#include "cg_common.cuh"
+#include "cg_fpemu.h"
+#include "cg_internal.h"
+
+namespace cg {
+
+namespace {
+
+constexpr int BINS = 4096;   // SeaLevelStage.HISTOGRAM_BINS
+
+struct CutState {
+    unsigned lo_key, hi_key;   // ordered float keys for atomicMin / atomicMax
+    float lowest, highest, per;
+    int degenerate;            // 1: the answer is `lowest` (flat field or nothing below)
+    int bracket_bin;
+    int count;                 // cells in the bracket bin
+    double below_bracket;
+    float todays;              // the percentile's height, before the lowstand
+    int land_cells;
+};
+
+__device__ __forceinline__ unsigned ordered_key(float f) {
+    unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered_key(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// SeaLevelStage.sortableBits (SeaLevelStage.kt:648-651).
+__device__ __forceinline__ int sortable_bits(float v) {
+    int bits = __float_as_int(v);
+    return bits < 0 ? (bits ^ 0x7FFFFFFF) : bits;
+}
+
+__device__ __forceinline__ int bin_of(float v, float lowest, float per) {
+    float x = __fmul_rn(__fsub_rn(v, lowest), per);
+    int b = (int)x;   // Float.toInt(): truncation
+    return b < 0 ? 0 : (b > BINS - 1 ? BINS - 1 : b);
+}
+
+__global__ void k_cut_init(CutState* s) {
+    s->lo_key = 0xFFFFFFFFu;
+    s->hi_key = 0u;
+    s->count = 0;
+    s->land_cells = 0;
+    s->degenerate = 0;
+}
+
+__global__ void k_minmax(const float* __restrict__ h, size_t N, CutState* s) {
+    unsigned lo = 0xFFFFFFFFu, hi = 0u;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        unsigned k = ordered_key(h[i]);
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&s->lo_key, lo);
+        atomicMax(&s->hi_key, hi);
+    }
+}
+
+__global__ void k_cut_prepare(CutState* s, double target) {
+    float lo = from_ordered_key(s->lo_key), hi = from_ordered_key(s->hi_key);
+    s->lowest = lo;
+    s->highest = hi;
+    if (__fsub_rn(hi, lo) <= 0.0f || target <= 0.0) {
+        s->degenerate = 1;
+        s->todays = lo;
+        s->per = 0.0f;
+    } else {
+        s->per = __fdiv_rn((float)(BINS - 1), __fsub_rn(hi, lo));
+    }
+}
+
+// One CTA per row: exact cell counts of every bin in that row.
+__global__ void __launch_bounds__(512) k_row_counts(const float* __restrict__ h, int W, const CutState* s,
+                                                    unsigned* __restrict__ counts) {
+    __shared__ unsigned sh[BINS];
+    if (s->degenerate) return;
+    const float lo = s->lowest, per = s->per;
+    for (int b = threadIdx.x; b < BINS; b += blockDim.x) sh[b] = 0u;
+    __syncthreads();
+    const float* rowp = h + (size_t)blockIdx.x * W;
+    for (int c = threadIdx.x; c < W; c += blockDim.x) atomicAdd(&sh[bin_of(rowp[c], lo, per)], 1u);
+    __syncthreads();
+    unsigned* out = counts + (size_t)blockIdx.x * BINS;
+    for (int b = threadIdx.x; b < BINS; b += blockDim.x) out[b] = sh[b];
+}
+
+// One thread per bin: the reference's sequential sum `histogram[bin] += rowWeights[row]`, in cell
+// order, replayed exactly row by row.
+__global__ void k_bin_sums(const unsigned* __restrict__ counts, const double* __restrict__ w, int H,
+                           const CutState* s, double* __restrict__ hist) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= BINS || s->degenerate) return;
+    double acc = 0.0;
+    for (int r = 0; r < H; ++r) {
+        unsigned c = counts[(size_t)r * BINS + b];
+        if (c) acc = seq_repeat_add(acc, w[r], (int64_t)c);
+    }
+    hist[b] = acc;
+}
+
+// SeaLevelStage.kt:614-622: the first bin that brings the weight below up to the target.
+__global__ void k_bracket_bin(const double* __restrict__ hist, double target, CutState* s) {
+    if (s->degenerate) return;
+    double below = 0.0;
+    int bracket = BINS - 1;
+    for (int b = 0; b < BINS; ++b) {
+        if (below + hist[b] >= target) {
+            bracket = b;
+            break;
+        }
+        below += hist[b];
+    }
+    s->bracket_bin = bracket;
+    s->below_bracket = below;
+}
+
+__global__ void k_bracket_collect(const float* __restrict__ h, size_t N, CutState* s, long long* __restrict__ keys) {
+    if (s->degenerate) return;
+    const float lo = s->lowest, per = s->per;
+    const int bracket = s->bracket_bin;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        float v = h[i];
+        if (bin_of(v, lo, per) != bracket) continue;
+        int slot = atomicAdd(&s->count, 1);
+        keys[slot] = (long long)(((unsigned long long)(long long)sortable_bits(v) << 32) | (unsigned long long)i);
+    }
+}
+
+// Bitonic sort of up to 16384 keys in one CTA's shared memory (padding with the largest key).
+constexpr int SMALL_SORT = 16384;
+__global__ void __launch_bounds__(1024) k_sort_small(long long* keys, const CutState* s) {
+    extern __shared__ long long sk[];
+    int n = s->count;
+    if (s->degenerate || n <= 1 || n > SMALL_SORT) return;
+    int P2 = 1;
+    while (P2 < n) P2 <<= 1;
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) sk[i] = i < n ? keys[i] : LLONG_MAX;
+    __syncthreads();
+    for (int k = 2; k <= P2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+                int l = i ^ j;
+                if (l > i) {
+                    bool up = (i & k) == 0;
+                    long long a = sk[i], b = sk[l];
+                    if ((a > b) == up) {
+                        sk[i] = b;
+                        sk[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = sk[i];
+}
+
+// One compare-exchange stage of a global bitonic sort over P2 slots (slots >= n hold +inf).
+__global__ void k_sort_stage(long long* keys, int n, int P2, int k, int j) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
+        int l = i ^ j;
+        if (l <= i) continue;
+        long long a = i < n ? keys[i] : LLONG_MAX;
+        long long b = l < n ? keys[l] : LLONG_MAX;
+        bool up = (i & k) == 0;
+        if ((a > b) == up) {
+            if (i < n) keys[i] = b;
+            if (l < n) keys[l] = a;
+        }
+    }
+}
+
+// SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target.
+__global__ void k_bracket_walk(const float* __restrict__ h, const long long* __restrict__ keys,
+                               const double* __restrict__ w, int W, double target, CutState* s) {
+    if (s->degenerate) return;
+    int n = s->count;
+    if (n == 0) {
+        s->todays = s->highest;
+        return;
+    }
+    double below = s->below_bracket;
+    for (int i = 0; i < n; ++i) {
+        int cell = (int)(keys[i] & 0xFFFFFFFFLL);
+        if (below >= target) {
+            s->todays = h[cell];
+            return;
+        }
+        below += w[cell / W];
+    }
+    s->todays = h[(int)(keys[n - 1] & 0xFFFFFFFFLL)];
+}
+
+// SeaLevelStage.landAndWaterAt (SeaLevelStage.kt:175-200).
+__global__ void k_land_and_water(const float* __restrict__ h, size_t N, CutState* s, float lowstand,
+                                 float land_half, float sea_half, uint8_t* __restrict__ land,
+                                 float* __restrict__ rel) {
+    const float shore = __fsub_rn(s->todays, lowstand);
+    int count = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        float g = h[i];
+        float d = __fsub_rn(g, shore);
+        if (g >= shore) {
+            land[i] = 1;
+            rel[i] = __fdiv_rn(d, land_half);
+            ++count;
+        } else {
+            land[i] = 0;
+            rel[i] = __fdiv_rn(d, sea_half);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xFFFFFFFFu, count, o);
+    if ((threadIdx.x & 31) == 0 && count) atomicAdd(&s->land_cells, count);
+}
+
+}  // namespace
+
+cg_status row_weights_dev(cg_ctx* ctx, int W, int H, const double** d_weights, double* total) {
+    CG_BUF(double, d_w, ctx, S_ROWW, H);
+    if (ctx->rw_w != W || ctx->rw_h != H) {
+        // shorelineForFraction (SeaLevelStage.kt:580-584): a per-grid constant table, built once.
+        std::vector<double> w(H);
+        const double PI = 3.141592653589793;
+        for (int row = 0; row < H; ++row) w[row] = std::cos(PI / 2 - (row + 0.5) / H * PI);
+        double t = 0.0;
+        for (int row = 0; row < H; ++row) t += w[row] * W;
+        CG_CUDA(ctx, cudaMemcpyAsync(d_w, w.data(), sizeof(double) * H, cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->rw_w = W;
+        ctx->rw_h = H;
+        ctx->rw_total = t;
+    }
+    *d_weights = d_w;
+    *total = ctx->rw_total;
+    return CG_OK;
+}
+
+cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float sea_level, float land_half,
+                             float sea_half, float lowstand_share, uint8_t* d_land, float* d_rel, float* h_shoreline,
+                             int* h_land_cells) {
+    size_t N = (size_t)W * H;
+    const double* d_w;
+    double total;
+    cg_status st = row_weights_dev(ctx, W, H, &d_w, &total);
+    if (st != CG_OK) return st;
+    float submerged = sea_level < 0.0f ? 0.0f : (sea_level > 1.0f ? 1.0f : sea_level);
+    double target = (double)submerged * total;
+    CG_BUF(CutState, d_s, ctx, S_SMALL, 1);
+    CG_BUF(unsigned, d_counts, ctx, S_HIST, (size_t)H * BINS);
+    CG_BUF(double, d_hist, ctx, S_SCRATCH4, BINS);
+    CG_BUF(long long, d_keys, ctx, S_BRACKET, N);
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    k_cut_init<<<1, 1, 0, sm>>>(d_s);
+    k_minmax<<<grid, 256, 0, sm>>>(d_h, N, d_s);
+    k_cut_prepare<<<1, 1, 0, sm>>>(d_s, target);
+    k_row_counts<<<H, 512, 0, sm>>>(d_h, W, d_s, d_counts);
+    k_bin_sums<<<BINS / 128, 128, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
+    k_bracket_bin<<<1, 1, 0, sm>>>(d_hist, target, d_s);
+    k_bracket_collect<<<grid, 256, 0, sm>>>(d_h, N, d_s, d_keys);
+    CG_CHECK_LAUNCH(ctx);
+    CutState hs;
+    CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    if (!hs.degenerate && hs.count > 1) {
+        if (hs.count <= SMALL_SORT) {
+            static bool configured = false;
+            if (!configured) {
+                CG_CUDA(ctx, cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)(SMALL_SORT * sizeof(long long))));
+                configured = true;
+            }
+            int P2 = 1;
+            while (P2 < hs.count) P2 <<= 1;
+            k_sort_small<<<1, 1024, P2 * sizeof(long long), sm>>>(d_keys, d_s);
+        } else {
+            int P2 = 1;
+            while (P2 < hs.count) P2 <<= 1;
+            int blocks = (P2 / 2 + 255) / 256;
+            if (blocks > grid) blocks = grid;
+            for (int k = 2; k <= P2; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) k_sort_stage<<<blocks, 256, 0, sm>>>(d_keys, hs.count, P2, k, j);
+        }
+        CG_CHECK_LAUNCH(ctx);
+    }
+    k_bracket_walk<<<1, 1, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
+    k_land_and_water<<<grid, 256, 0, sm>>>(d_h, N, d_s, lowstand_share, land_half, sea_half, d_land, d_rel);
+    CG_CHECK_LAUNCH(ctx);
+    CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    *h_shoreline = hs.todays - lowstand_share;
+    *h_land_cells = hs.land_cells;
+    return CG_OK;
+}
+
+}  // namespace cg

@@ -1,0 +1,383 @@
+// FlowRouting.fillDepressions on the device (FlowRouting.kt:52-111), reproducing the sequential
+// priority flood's result exactly.
+//
+// The reference pops cells off a heap keyed (Q, index), Q = bits(fl(f + 4)), and gives each cell
+// the level of the first neighbour popped next to it: f(n) = g(n) if g(n) > f(parent), else
+// fl(f(parent) + 1e-6). The popped Q never decreases, so a cell's parent is the neighbour of least
+// Q; when that is unique, f(n) = phi(min over neighbours of f, g(n)), a monotone fixed point. The
+// device computes that fixed point in parallel and then checks, cell by cell, whether the
+// quantised key ever left the parent open:
+//  (1) pointer jumping along strictly Q-descending neighbour chains finds every cell with such a
+//      chain to an outlet; those keep their own height (their first popped neighbour is lower);
+//  (2) the rest relax to the fixed point of f(n) = min_m phi(f(m), g(n)) from +inf, tile by tile
+//      in shared memory, each tile iterating to local convergence before its borders are
+//      republished (the monotone Bellman-Ford of a Dijkstra with non-decreasing edge functions);
+//  (3) a check pass finds cells whose least-Q neighbours share a key but would give different
+//      levels. The reference takes the one popped first: among neighbours that entered that key's
+//      level from below, the lowest index. Such a cell is repaired with that neighbour and the
+//      fixed point recomputed around it. A tie whose candidates were themselves reached inside the
+//      level (flat ground within one key quantum) is counted as unresolved and reported.
+#include <cfloat>
+#include <vector>
+
+#include "cg_common.cuh"
+#include "cg_internal.h"
+
+namespace cg {
+
+namespace {
+
+constexpr float kStep = 1e-6f;   // FlowRouting.FLAT_GRADIENT_STEP
+constexpr int T = 32;            // tile side
+constexpr int TH = 8;            // tile rows per thread pass (block is 32 x 8)
+
+// Cell classes.
+enum : uint8_t { C_WATER = 0, C_SEED = 1, C_DRAINED = 2, C_OPEN = 3, C_PINNED = 4 };
+
+__device__ __forceinline__ int qkey(float f) { return __float_as_int(__fadd_rn(f, 4.0f)); }   // FlowRouting.encode
+__device__ __forceinline__ float phi(float fp, float g) { return g > fp ? g : __fadd_rn(fp, kStep); }
+
+struct FillCounters {
+    unsigned long long ties, unresolved, repaired;
+    int active;
+    int changed;
+};
+
+// (0) classes and initial levels.
+__global__ void k_fill_init(const uint8_t* __restrict__ land, const float* __restrict__ g, int W, int H,
+                            uint8_t* __restrict__ cls, float* __restrict__ f, int* __restrict__ ptr) {
+    size_t N = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int row = (int)(i / W);
+        if (!land[i]) {
+            cls[i] = C_WATER;
+            f[i] = g[i];
+            ptr[i] = (int)i;
+            continue;
+        }
+        if (row == 0 || row == H - 1) {
+            cls[i] = C_SEED;
+            f[i] = g[i];
+            ptr[i] = (int)i;
+            continue;
+        }
+        // Steepest strictly Q-descending neighbour on the unfilled ground (water counts as is).
+        int col = (int)(i - (size_t)row * W);
+        int q = qkey(g[i]);
+        int best = (int)i, bq = q;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (rs == 0 && cs == 0) continue;
+                int n = nr * W + wrap_col(col + cs, W);
+                int qn = qkey(g[n]);
+                if (qn < bq || (qn == bq && qn < q && n < best)) {
+                    bq = qn;
+                    best = n;
+                }
+            }
+        }
+        cls[i] = C_OPEN;
+        f[i] = INFINITY;
+        ptr[i] = best;
+    }
+}
+
+// (1) pointer jumping to the chain's root.
+__global__ void k_jump(const int* __restrict__ src, int* __restrict__ dst, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[src[i]];
+}
+
+__global__ void k_mark_drained(const int* __restrict__ root, const float* __restrict__ g, size_t N,
+                               uint8_t* __restrict__ cls, float* __restrict__ f) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (cls[i] != C_OPEN) continue;
+        uint8_t rc = cls[root[i]];
+        if (rc == C_WATER || rc == C_SEED) {
+            cls[i] = C_DRAINED;
+            f[i] = g[i];
+        }
+    }
+}
+
+// (2) tile relaxation. Each CTA owns a 32x32 tile, loads f and g with a one-cell halo, relaxes its
+// OPEN cells to local convergence, writes back what fell, and activates the neighbouring tiles if
+// a border cell fell. PINNED cells take their designated parent instead of the minimum.
+__global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, const float* __restrict__ g,
+                                                     const uint8_t* __restrict__ cls,
+                                                     const int* __restrict__ pin_parent, int W, int H, int tiles_x,
+                                                     int tiles_y, const uint8_t* __restrict__ act_in,
+                                                     uint8_t* __restrict__ act_out, FillCounters* cnt,
+                                                     int max_sweeps) {
+    const int tile = blockIdx.x;
+    if (!act_in[tile]) return;
+    const int ty0 = (tile / tiles_x) * T, tx0 = (tile % tiles_x) * T;
+    __shared__ float sf[T + 2][T + 3];
+    __shared__ float sg[T][T + 1];
+    __shared__ uint8_t sc[T][T];
+    __shared__ int any_border, any_change;
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;   // 32 x 8
+    for (int i = threadIdx.x; i < (T + 2) * (T + 2); i += 256) {
+        int yy = i / (T + 2), xx = i % (T + 2);
+        int gy = ty0 + yy - 1;
+        float v = INFINITY;
+        if (gy >= 0 && gy < H) v = f[(size_t)gy * W + wrap_col(tx0 + xx - 1, W)];
+        sf[yy][xx] = v;
+    }
+    for (int i = threadIdx.x; i < T * T; i += 256) {
+        int yy = i / T, xx = i % T;
+        int gy = ty0 + yy, gx = tx0 + xx;
+        bool in = gy < H && gx < W;
+        sg[yy][xx] = in ? g[(size_t)gy * W + gx] : 0.0f;
+        sc[yy][xx] = in ? cls[(size_t)gy * W + gx] : (uint8_t)C_WATER;
+    }
+    if (threadIdx.x == 0) any_border = 0;
+    __syncthreads();
+    bool border_changed = false;
+    int unsettled = 1;
+    for (int sweep = 0; sweep < max_sweeps && unsettled; ++sweep) {
+        bool changed = false;
+        for (int yy = ly; yy < T; yy += TH) {
+            uint8_t c = sc[yy][lx];
+            if (c != C_OPEN && c != C_PINNED) continue;
+            int gy = ty0 + yy;
+            float gn = sg[yy][lx];
+            float best = sf[yy + 1][lx + 1];
+            if (c == C_OPEN) {
+                for (int rs = -1; rs <= 1; ++rs) {
+                    int ny = gy + rs;
+                    if (ny < 0 || ny >= H) continue;
+                    for (int cs = -1; cs <= 1; ++cs) {
+                        if (rs == 0 && cs == 0) continue;
+                        float fm = sf[yy + 1 + rs][lx + 1 + cs];
+                        float v = phi(fm, gn);
+                        if (v < best) best = v;
+                    }
+                }
+            } else {
+                int p = pin_parent[(size_t)gy * W + tx0 + lx];
+                int pr = p / W, pc = p % W;
+                int dy = pr - gy;
+                int dx = pc - (tx0 + lx);
+                if (dx > 1) dx -= W;
+                if (dx < -1) dx += W;
+                float v = phi(sf[yy + 1 + dy][lx + 1 + dx], gn);
+                if (v != best) best = v;   // a pinned cell follows its parent up as well as down
+            }
+            if (best != sf[yy + 1][lx + 1]) {
+                sf[yy + 1][lx + 1] = best;
+                changed = true;
+                // A border cell, or the last column when the grid is narrower than a tile (its
+                // east neighbour wraps to a column this tile only sees through its halo).
+                if (yy == 0 || yy == T - 1 || lx == 0 || lx == T - 1 || tx0 + lx == W - 1) border_changed = true;
+            }
+        }
+        unsettled = __syncthreads_or(changed);
+    }
+    // Still moving after the sweep budget: run this tile again next pass.
+    if ((__syncthreads_or(border_changed) || unsettled) && threadIdx.x == 0) any_border = 1;
+    // Write back and report.
+    bool wrote = false;
+    for (int yy = ly; yy < T; yy += TH) {
+        int gy = ty0 + yy, gx = tx0 + lx;
+        if (gy >= H || gx >= W) continue;
+        uint8_t c = sc[yy][lx];
+        if (c != C_OPEN && c != C_PINNED) continue;
+        float v = sf[yy + 1][lx + 1];
+        size_t idx = (size_t)gy * W + gx;
+        if (f[idx] != v) {
+            f[idx] = v;
+            wrote = true;
+        }
+    }
+    if (threadIdx.x == 0) any_change = 0;
+    __syncthreads();
+    if (wrote) any_change = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (any_change) atomicAdd(&cnt->changed, 1);
+        if (any_border) {
+            int tyi = tile / tiles_x, txi = tile % tiles_x;
+            for (int dy = -1; dy <= 1; ++dy) {
+                int y = tyi + dy;
+                if (y < 0 || y >= tiles_y) continue;
+                for (int dx = -1; dx <= 1; ++dx) {
+                    int x = (txi + dx + tiles_x) % tiles_x;
+                    act_out[y * tiles_x + x] = 1;
+                }
+            }
+            atomicAdd(&cnt->active, 1);
+        }
+    }
+}
+
+// A tile is active for the first pass if it holds any OPEN cell.
+__global__ void k_tiles_with_open(const uint8_t* __restrict__ cls, int W, int H, int tiles_x, int tiles_y,
+                                  uint8_t* __restrict__ act) {
+    int tile = blockIdx.x;
+    const int ty0 = (tile / tiles_x) * T, tx0 = (tile % tiles_x) * T;
+    int has = 0;
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+        int gy = ty0 + i / T, gx = tx0 + i % T;
+        if (gy < H && gx < W && cls[(size_t)gy * W + gx] >= C_OPEN) has = 1;
+    }
+    has = __syncthreads_or(has);
+    if (threadIdx.x == 0) act[tile] = has ? 1 : 0;
+}
+
+// (3) the exact parent check. For each OPEN/PINNED cell: its least-Q neighbours; if they give
+// different levels, the reference's parent is the lowest-index one among those that entered the
+// level from below. Writes the parent into pin_parent (and marks the cell PINNED) when that parent
+// disagrees with the current level.
+__global__ void k_check_ties(const float* __restrict__ f, const float* __restrict__ g, uint8_t* __restrict__ cls,
+                             int* __restrict__ pin_parent, int W, int H, FillCounters* cnt) {
+    size_t N = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        uint8_t c = cls[i];
+        if (c != C_OPEN && c != C_PINNED) continue;
+        int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+        float gn = g[i];
+        int qmin = INT_MAX;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (rs == 0 && cs == 0) continue;
+                int n = nr * W + wrap_col(col + cs, W);
+                int q = qkey(f[n]);
+                if (q < qmin) qmin = q;
+            }
+        }
+        float v0 = 0.0f;
+        bool first = true, differ = false, inside_level = false;
+        int pick = INT_MAX;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (rs == 0 && cs == 0) continue;
+                int n = nr * W + wrap_col(col + cs, W);
+                float fm = f[n];
+                if (qkey(fm) != qmin) continue;
+                float v = phi(fm, gn);
+                if (first) v0 = v, first = false;
+                else if (v != v0) differ = true;
+                if (n < pick) pick = n;
+                // Reached inside its own key level: an unraised land cell whose least-Q neighbour
+                // shares its key. Water and the polar outlets are in the heap from the start.
+                uint8_t cm = cls[n];
+                if ((cm == C_OPEN || cm == C_PINNED || cm == C_DRAINED) && fm == g[n]) {
+                    int mr = n / W, mc = n % W, mq = INT_MAX;
+                    for (int a = -1; a <= 1; ++a) {
+                        int r2 = mr + a;
+                        if (r2 < 0 || r2 >= H) continue;
+                        for (int b = -1; b <= 1; ++b) {
+                            if (a == 0 && b == 0) continue;
+                            int q2 = qkey(f[r2 * W + wrap_col(mc + b, W)]);
+                            if (q2 < mq) mq = q2;
+                        }
+                    }
+                    if (mq == qmin) inside_level = true;
+                }
+            }
+        }
+        if (!differ) continue;
+        atomicAdd(&cnt->ties, 1ull);
+        if (inside_level) {
+            atomicAdd(&cnt->unresolved, 1ull);
+            continue;
+        }
+        float want = phi(f[pick], gn);
+        if (c != C_PINNED || pin_parent[i] != pick) {
+            pin_parent[i] = pick;
+            cls[i] = C_PINNED;
+            if (want != f[i]) atomicAdd(&cnt->repaired, 1ull);
+        }
+    }
+}
+
+__global__ void k_reset_open(const uint8_t* __restrict__ cls, float* __restrict__ f, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        if (cls[i] == C_OPEN || cls[i] == C_PINNED) f[i] = INFINITY;
+}
+
+}  // namespace
+
+cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, float* d_filled,
+                               int64_t* ties, int64_t* unresolved) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    CG_BUF(uint8_t, d_cls, ctx, S_FILLFLAG, N);
+    CG_BUF(int, d_ptr, ctx, S_PTR, N);
+    CG_BUF(int, d_ptr2, ctx, S_PTR2, N);
+    CG_BUF(int, d_pin, ctx, S_FILLQ, N);
+    int tiles_x = (W + T - 1) / T, tiles_y = (H + T - 1) / T, tiles = tiles_x * tiles_y;
+    CG_BUF(uint8_t, d_act, ctx, S_TILEFLAG, 2 * (size_t)tiles);
+    CG_BUF(FillCounters, d_cnt, ctx, S_FILLF, 1);
+    int grid = ctx->num_sms * 8;
+    CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(FillCounters), sm));
+    k_fill_init<<<grid, 256, 0, sm>>>(d_land, d_rel, W, H, d_cls, d_filled, d_ptr);
+    // Chains are at most N long: ceil(log2 N) jumps reach every root.
+    int jumps = 1;
+    while (((size_t)1 << jumps) < N) ++jumps;
+    int* a = d_ptr;
+    int* b = d_ptr2;
+    for (int j = 0; j < jumps; ++j) {
+        k_jump<<<grid, 256, 0, sm>>>(a, b, N);
+        int* t = a;
+        a = b;
+        b = t;
+    }
+    k_mark_drained<<<grid, 256, 0, sm>>>(a, d_rel, N, d_cls, d_filled);
+    CG_CHECK_LAUNCH(ctx);
+
+    FillCounters hc;
+    int64_t tie_total = 0, unresolved_total = 0;
+    const int max_repairs = 8;
+    for (int repair = 0; repair <= max_repairs; ++repair) {
+        uint8_t* act = d_act;
+        uint8_t* nxt = d_act + tiles;
+        k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, W, H, tiles_x, tiles_y, act);
+        CG_CHECK_LAUNCH(ctx);
+        // Relax until no tile changes. A bounded loop: every pass lowers some level or stops, and
+        // levels only take values from a finite set; the cap is a guard, not the expected exit.
+        const int max_passes = 4 * (tiles_x + tiles_y) + 64;
+        int pass = 0;
+        for (; pass < max_passes; ++pass) {
+            CG_CUDA(ctx, cudaMemsetAsync(nxt, 0, tiles, sm));
+            CG_CUDA(ctx, cudaMemsetAsync(&d_cnt->active, 0, 2 * sizeof(int), sm));
+            k_relax_tiles<<<tiles, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, tiles_x, tiles_y, act, nxt,
+                                                 d_cnt, 4 * T);
+            CG_CHECK_LAUNCH(ctx);
+            uint8_t* t = act;
+            act = nxt;
+            nxt = t;
+            if ((pass & 3) == 3 || pass < 4) {
+                CG_CUDA(ctx, cudaMemcpyAsync(&hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, sm));
+                CG_CUDA(ctx, cudaStreamSynchronize(sm));
+                if (hc.active == 0) break;
+            }
+        }
+        if (pass >= max_passes) return fail(ctx, CG_TIMEOUT, "fill relaxation did not settle in %d passes", pass);
+        CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 3 * sizeof(unsigned long long), sm));
+        k_check_ties<<<grid, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, d_cnt);
+        CG_CHECK_LAUNCH(ctx);
+        CG_CUDA(ctx, cudaMemcpyAsync(&hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, sm));
+        CG_CUDA(ctx, cudaStreamSynchronize(sm));
+        tie_total = (int64_t)hc.ties;
+        unresolved_total = (int64_t)hc.unresolved;
+        if (hc.repaired == 0) break;
+        if (repair == max_repairs) {
+            unresolved_total += (int64_t)hc.repaired;
+            break;
+        }
+        // Recompute the fixed point with the pinned parents.
+        k_reset_open<<<grid, 256, 0, sm>>>(d_cls, d_filled, N);
+    }
+    if (ties) *ties = tie_total;
+    if (unresolved) *unresolved = unresolved_total;
+    return CG_OK;
+}
+
+}  // namespace cg

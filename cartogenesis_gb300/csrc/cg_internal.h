@@ -1,0 +1,65 @@
+// Declarations shared between the translation units of the library (not part of the C ABI).
+#pragma once
+
+#include "cg_common.cuh"
+
+namespace cg {
+
+// ---- thermal (cg_thermal.cu)
+cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, cg_thermal_limits lim, int passes,
+                             float rate, float** result);
+int thermal_launches(int passes);
+
+// ---- sea-level cut (cg_cut.cu)
+// Row weights of SeaLevelStage.shorelineForFraction and their sequential total, computed once per
+// grid shape on the host (a constant table, like a plan's twiddles) and kept on the device.
+cg_status row_weights_dev(cg_ctx* ctx, int W, int H, const double** d_weights, double* total);
+cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float sea_level, float land_half,
+                             float sea_half, float lowstand_share, uint8_t* d_land, float* d_rel, float* h_shoreline,
+                             int* h_land_cells);
+
+// ---- fill (cg_fill.cu)
+cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, float* d_filled,
+                               int64_t* ties, int64_t* unresolved);
+
+// ---- routing (cg_route.cu)
+struct FlatCounts {
+    int flats, kept, raised;
+};
+cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel,
+                              const float* d_filled, int64_t seed, double r, int lattice, bool by_facet,
+                              bool over_potential, int32_t* d_recv, double* d_surface, FlatCounts* counts);
+
+// ---- drainage tree (cg_tree.cu)
+struct TreeInfo {
+    int levels;
+};
+// Kahn drainage order of FlowRouting.drainageOrder as (level, first-source) keys, the order itself
+// (optional) and the donor counts.
+cg_status drainage_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, int land_cells,
+                            int64_t* d_key, int32_t* d_donors, int32_t* d_order, TreeInfo* info);
+cg_status accumulate_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv,
+                         const int64_t* d_key, const float* d_weights, float* d_area);
+struct InciseArgs {
+    float courant_coefficient;
+    float pond_depth;
+    float land_cells;
+    float land_range;
+    float shoreline;
+    float step_ns;
+    float step_diag;
+    int only_above_base;
+};
+cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const float* d_ground,
+                     const float* d_rel, const float* d_area, const float* d_erod, float* d_surface,
+                     const InciseArgs& a);
+struct BasinsDev {
+    int count;
+};
+cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
+                        const int32_t* d_recv, float pond_depth, int32_t* d_label, cg_basins* host_basins);
+
+// ---- small helpers (cg_api.cu)
+cg_status sync(cg_ctx* ctx);
+
+}  // namespace cg
