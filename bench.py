@@ -1,0 +1,286 @@
+"""Benchmark of the GB300 erosion stage: Mcell-rounds/s of the plain (P0, REF32) stage.
+
+A step is one whole erosion stage (ErosionStage.apply: the initial thermal sweeps, 12 hydraulic
+rounds and each round's relaxation) over one synthetic world. The workload is the plain method's
+single-GPU configuration: 8192 x 4096 cells (33.5M), fBm heights (beta 2) over [-10000, 6000] m at
+30% land by area, uplift ridges of 50-4000 m/Myr along 15 great circles, lognormal rock factor;
+383 initial sweeps and 31 per round. Inputs are larger than the 129 MB L2 (the height field alone
+is 134 MB), so no flush is needed between steps.
+
+  value: the stage on a world already resident in HBM (cg_erode_stage_dev), CUDA events on the
+         library's stream;
+  e2e:   the same stage through the host-buffer C ABI call (cg_erode_stage) from pinned memory, the
+         host->device copy of the world and the device->host copy of the result inside the timing.
+  --impl reference: the CPU restatement of the reference's stage (the Kotlin path cannot run here:
+         no JVM), all host threads for the thermal sweeps as the reference's parallelChunks does,
+         on a bounded sample of the same workload.
+Multi-GPU: replicas only (one independent world per rank, seed = rank + 1); the stage does not
+shard within a world, so there is no collective on the data path.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-rounds/s on 1 GB300: plain vs batched vs surrogate at <=5 m height RMSE"
+UNIT = "Mcell-rounds/s"
+ROUNDS = 12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=8192)
+    ap.add_argument("--height", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=1024, help="width of the CPU baseline's sample world")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def world_inputs(W, H, seed):
+    from cartogenesis_gb300 import synthetic
+    return synthetic.world(W, H, seed, uplift="ridges")
+
+
+def cpu_baseline(W_sample, steps, threads=None):
+    """The CPU restatement on a bounded sample world (same generator, smaller grid)."""
+    import oracle
+    H_sample = W_sample // 2
+    h, up, rk = world_inputs(W_sample, H_sample, 1)
+    p = oracle.default_params(W_sample, H_sample, 1, sea_level=0.70)
+    times = []
+    for _ in range(max(steps, 1)):
+        t0 = time.perf_counter()
+        oracle.erode_stage(p, h, up, rk, want=())
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    value = W_sample * H_sample * ROUNDS / t / 1e6
+    cores = threads or os.cpu_count()
+    return value, t, cores, f"full 12-round stage on the same generator's {W_sample}x{H_sample} world " \
+                            f"({oracle.thermal_limits(p)[1]} initial sweeps), median of {len(times)}"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    steps = max(args.steps, 1)
+    value, t, cores, sample = cpu_baseline(args.cpu_sample, steps, int(os.environ["OMP_NUM_THREADS"]))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": 0, "ms_per_step": round(t * 1000.0, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain P0 erosion stage, CPU restatement of the reference, sample {sample}",
+                   "grid": [args.cpu_sample, args.cpu_sample // 2], "rounds": ROUNDS},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from cartogenesis_gb300 import Context, ErosionConfig, abi
+
+    W, H = args.width, args.height
+    N = W * H
+    seed = rank + 1
+    h, up, rk = world_inputs(W, H, seed)
+    cfg = ErosionConfig(W, H, seed, sea_level=0.70)
+    ctx = Context(local)
+    lib = ctx.lib
+
+    # Device-resident world.
+    d_h = torch.from_numpy(h).cuda()
+    d_up = torch.from_numpy(up).cuda()
+    d_rk = torch.from_numpy(rk).cuda()
+    d_out = torch.empty_like(d_h)
+    dev_in = abi.Inputs(d_h.data_ptr(), d_up.data_ptr(), d_rk.data_ptr(), None, None)
+    stats = (abi.RoundStats * ROUNDS)()
+    land = C.c_int32()
+    lib_stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def step_dev(with_stats=False):
+        ctx.check(lib.cg_erode_stage_dev(ctx.handle, C.byref(cfg.params), C.byref(dev_in), d_out.data_ptr(),
+                                         C.cast(stats, C.c_void_p) if with_stats else None, C.byref(land)))
+
+    # Host path: pinned inputs and result.
+    p_h = torch.from_numpy(h).pin_memory()
+    p_up = torch.from_numpy(up).pin_memory()
+    p_rk = torch.from_numpy(rk).pin_memory()
+    p_out = torch.empty(H, W, dtype=torch.float32).pin_memory()
+    host_in = abi.Inputs(p_h.data_ptr(), p_up.data_ptr(), p_rk.data_ptr(), None, None)
+    host_out = abi.Outputs(height=p_out.data_ptr())
+
+    def step_e2e():
+        ctx.check(lib.cg_erode_stage(ctx.handle, C.byref(cfg.params), C.byref(host_in), C.byref(host_out), None))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_dev()
+    step_dev(with_stats=True)   # one untimed pass for the per-phase breakdown
+    phase = {k: sum(getattr(s, k) for s in stats) for k in
+             ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_relax", "ms_total")}
+    per_round = [{"land": s.land_cells, "flats": s.flats, "raised": s.raised_cells, "levels": s.levels,
+                  "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2)}
+                 for s in stats]
+
+    clocks = ClockSampler(local)
+    barrier()
+    launches0 = ctx.kernel_launches
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev[i][0].record(lib_stream)
+        step_dev()
+        ev[i][1].record(lib_stream)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.kernel_launches - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(step_ms) / 1000.0
+
+    # End to end through the host-buffer call.
+    for _ in range(1):
+        step_e2e()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    barrier()
+    t_e2e = time.perf_counter() - t0
+
+    times = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    t_dev, t_e2e = times.tolist()
+    cell_rounds = float(N) * ROUNDS * args.steps * world
+    value = cell_rounds / t_dev / 1e6
+    e2e = cell_rounds / t_e2e / 1e6
+
+    # Roofline of the dominant phase's kernel. The relaxation sweeps' algorithmic traffic is a read
+    # and a write of the height field per sweep (8 B per cell-sweep); with sweeps fused per launch
+    # the kernel moves less than that, so frac may exceed 1 (it is measured against the unfused bytes).
+    from cartogenesis_gb300.perf import roofline_entry
+    roof = roofline_entry(cfg, phase, ROOT)
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 * t_dev / args.steps, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain P0 erosion stage (REF32, bit-exact to the reference restatement), "
+                               f"{W}x{H} cells, {ROUNDS} rounds, fBm beta 2 + 15 uplift ridges, seed rank+1",
+                   "grid": [W, H], "rounds": ROUNDS, "sweeps": cfg.thermal_limits()[1],
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (134 MB height field)"},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * 4 * N, "d2h_bytes_per_step": 4 * N},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": roof,
+        "phases_ms_per_step": {k: round(v, 2) for k, v in phase.items()},
+        "rounds": per_round,
+    }
+    if rank == 0 and world == 1:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        v, t, cores, sample = cpu_baseline(args.cpu_sample, 1, int(os.environ["OMP_NUM_THREADS"]))
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

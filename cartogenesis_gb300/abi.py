@@ -101,7 +101,14 @@ class RoundStats(C.Structure):
         ("levels", C.c_int32),
         ("fill_ties", C.c_int64),
         ("fill_unresolved", C.c_int64),
+        ("kernel_launches", C.c_int64),
         ("ms_total", C.c_double),
+        ("ms_cut", C.c_double),
+        ("ms_fill", C.c_double),
+        ("ms_route", C.c_double),
+        ("ms_tree", C.c_double),
+        ("ms_incise", C.c_double),
+        ("ms_relax", C.c_double),
     ]
 
 

@@ -140,6 +140,10 @@ void cg_cancel(cg_ctx* ctx) {
 
 const char* cg_last_error(const cg_ctx* ctx) { return ctx ? ctx->error : "no context"; }
 
+void* cg_stream(const cg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int64_t cg_kernel_launches(const cg_ctx* ctx) { return ctx ? (int64_t)ctx->launches : 0; }
+
 cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t W, int32_t H, const float* in, float* out, cg_thermal_limits lim,
                             int32_t passes, float rate) {
     if (!ctx || !in || !out) return CG_BAD_ARG;

@@ -56,7 +56,12 @@ struct cg_ctx {
     // Row-weight table of the sea-level cut, cached for the last grid shape.
     int rw_w = 0, rw_h = 0;
     double rw_total = 0.0;
+    // Kernels launched on this context (every launch site counts itself with CG_LAUNCH).
+    long long launches = 0;
 };
+
+// Prefix of every kernel launch statement: `CG_LAUNCH(ctx) k<<<...>>>(...);` counts the launch.
+#define CG_LAUNCH(ctx) ((ctx)->launches++),
 
 namespace cg {
 

@@ -11,6 +11,7 @@
 //  - the bracket: its cells are sorted on the device and walked by one thread in the reference's
 //    order (a few thousand cells on the benchmark worlds).
 // min, max, the bin of a cell and the land/relative split are elementwise or exact reductions.
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -178,19 +179,22 @@ __global__ void __launch_bounds__(1024) k_sort_small(long long* keys, const CutS
     for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = sk[i];
 }
 
-// One compare-exchange stage of a global bitonic sort over P2 slots (slots >= n hold +inf).
-__global__ void k_sort_stage(long long* keys, int n, int P2, int k, int j) {
+// One compare-exchange stage of a global bitonic sort over P2 slots, padded with the largest key.
+__global__ void k_sort_stage(long long* keys, int P2, int k, int j) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
         int l = i ^ j;
         if (l <= i) continue;
-        long long a = i < n ? keys[i] : LLONG_MAX;
-        long long b = l < n ? keys[l] : LLONG_MAX;
+        long long a = keys[i], b = keys[l];
         bool up = (i & k) == 0;
         if ((a > b) == up) {
-            if (i < n) keys[i] = b;
-            if (l < n) keys[l] = a;
+            keys[i] = b;
+            keys[l] = a;
         }
     }
+}
+
+__global__ void k_pad(long long* keys, int n, int P2) {
+    for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) keys[i] = LLONG_MAX;
 }
 
 // SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target.
@@ -274,13 +278,13 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
     CG_BUF(long long, d_keys, ctx, S_BRACKET, N);
     cudaStream_t sm = ctx->stream;
     int grid = ctx->num_sms * 8;
-    k_cut_init<<<1, 1, 0, sm>>>(d_s);
-    k_minmax<<<grid, 256, 0, sm>>>(d_h, N, d_s);
-    k_cut_prepare<<<1, 1, 0, sm>>>(d_s, target);
-    k_row_counts<<<H, 512, 0, sm>>>(d_h, W, d_s, d_counts);
-    k_bin_sums<<<BINS / 128, 128, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
-    k_bracket_bin<<<1, 1, 0, sm>>>(d_hist, target, d_s);
-    k_bracket_collect<<<grid, 256, 0, sm>>>(d_h, N, d_s, d_keys);
+    CG_LAUNCH(ctx) k_cut_init<<<1, 1, 0, sm>>>(d_s);
+    CG_LAUNCH(ctx) k_minmax<<<grid, 256, 0, sm>>>(d_h, N, d_s);
+    CG_LAUNCH(ctx) k_cut_prepare<<<1, 1, 0, sm>>>(d_s, target);
+    CG_LAUNCH(ctx) k_row_counts<<<H, 512, 0, sm>>>(d_h, W, d_s, d_counts);
+    CG_LAUNCH(ctx) k_bin_sums<<<BINS / 128, 128, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
+    CG_LAUNCH(ctx) k_bracket_bin<<<1, 1, 0, sm>>>(d_hist, target, d_s);
+    CG_LAUNCH(ctx) k_bracket_collect<<<grid, 256, 0, sm>>>(d_h, N, d_s, d_keys);
     CG_CHECK_LAUNCH(ctx);
     CutState hs;
     CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));
@@ -295,19 +299,20 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
             }
             int P2 = 1;
             while (P2 < hs.count) P2 <<= 1;
-            k_sort_small<<<1, 1024, P2 * sizeof(long long), sm>>>(d_keys, d_s);
+            CG_LAUNCH(ctx) k_sort_small<<<1, 1024, P2 * sizeof(long long), sm>>>(d_keys, d_s);
         } else {
             int P2 = 1;
             while (P2 < hs.count) P2 <<= 1;
             int blocks = (P2 / 2 + 255) / 256;
             if (blocks > grid) blocks = grid;
+            CG_LAUNCH(ctx) k_pad<<<blocks, 256, 0, sm>>>(d_keys, hs.count, P2);
             for (int k = 2; k <= P2; k <<= 1)
-                for (int j = k >> 1; j > 0; j >>= 1) k_sort_stage<<<blocks, 256, 0, sm>>>(d_keys, hs.count, P2, k, j);
+                for (int j = k >> 1; j > 0; j >>= 1) CG_LAUNCH(ctx) k_sort_stage<<<blocks, 256, 0, sm>>>(d_keys, P2, k, j);
         }
         CG_CHECK_LAUNCH(ctx);
     }
-    k_bracket_walk<<<1, 1, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
-    k_land_and_water<<<grid, 256, 0, sm>>>(d_h, N, d_s, lowstand_share, land_half, sea_half, d_land, d_rel);
+    CG_LAUNCH(ctx) k_bracket_walk<<<1, 1, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
+    CG_LAUNCH(ctx) k_land_and_water<<<grid, 256, 0, sm>>>(d_h, N, d_s, lowstand_share, land_half, sea_half, d_land, d_rel);
     CG_CHECK_LAUNCH(ctx);
     CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));
     CG_CUDA(ctx, cudaStreamSynchronize(sm));

@@ -18,6 +18,7 @@
 //      fixed point recomputed around it. A tie whose candidates were themselves reached inside the
 //      level (flat ground within one key quantum) is counted as unresolved and reported.
 #include <cfloat>
+#include <climits>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -317,19 +318,19 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     CG_BUF(FillCounters, d_cnt, ctx, S_FILLF, 1);
     int grid = ctx->num_sms * 8;
     CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(FillCounters), sm));
-    k_fill_init<<<grid, 256, 0, sm>>>(d_land, d_rel, W, H, d_cls, d_filled, d_ptr);
+    CG_LAUNCH(ctx) k_fill_init<<<grid, 256, 0, sm>>>(d_land, d_rel, W, H, d_cls, d_filled, d_ptr);
     // Chains are at most N long: ceil(log2 N) jumps reach every root.
     int jumps = 1;
     while (((size_t)1 << jumps) < N) ++jumps;
     int* a = d_ptr;
     int* b = d_ptr2;
     for (int j = 0; j < jumps; ++j) {
-        k_jump<<<grid, 256, 0, sm>>>(a, b, N);
+        CG_LAUNCH(ctx) k_jump<<<grid, 256, 0, sm>>>(a, b, N);
         int* t = a;
         a = b;
         b = t;
     }
-    k_mark_drained<<<grid, 256, 0, sm>>>(a, d_rel, N, d_cls, d_filled);
+    CG_LAUNCH(ctx) k_mark_drained<<<grid, 256, 0, sm>>>(a, d_rel, N, d_cls, d_filled);
     CG_CHECK_LAUNCH(ctx);
 
     FillCounters hc;
@@ -338,7 +339,7 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     for (int repair = 0; repair <= max_repairs; ++repair) {
         uint8_t* act = d_act;
         uint8_t* nxt = d_act + tiles;
-        k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, W, H, tiles_x, tiles_y, act);
+        CG_LAUNCH(ctx) k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, W, H, tiles_x, tiles_y, act);
         CG_CHECK_LAUNCH(ctx);
         // Relax until no tile changes. A bounded loop: every pass lowers some level or stops, and
         // levels only take values from a finite set; the cap is a guard, not the expected exit.
@@ -347,7 +348,7 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
         for (; pass < max_passes; ++pass) {
             CG_CUDA(ctx, cudaMemsetAsync(nxt, 0, tiles, sm));
             CG_CUDA(ctx, cudaMemsetAsync(&d_cnt->active, 0, 2 * sizeof(int), sm));
-            k_relax_tiles<<<tiles, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, tiles_x, tiles_y, act, nxt,
+            CG_LAUNCH(ctx) k_relax_tiles<<<tiles, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, tiles_x, tiles_y, act, nxt,
                                                  d_cnt, 4 * T);
             CG_CHECK_LAUNCH(ctx);
             uint8_t* t = act;
@@ -361,7 +362,7 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
         }
         if (pass >= max_passes) return fail(ctx, CG_TIMEOUT, "fill relaxation did not settle in %d passes", pass);
         CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 3 * sizeof(unsigned long long), sm));
-        k_check_ties<<<grid, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, d_cnt);
+        CG_LAUNCH(ctx) k_check_ties<<<grid, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, d_cnt);
         CG_CHECK_LAUNCH(ctx);
         CG_CUDA(ctx, cudaMemcpyAsync(&hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, sm));
         CG_CUDA(ctx, cudaStreamSynchronize(sm));
@@ -373,7 +374,7 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
             break;
         }
         // Recompute the fixed point with the pinned parents.
-        k_reset_open<<<grid, 256, 0, sm>>>(d_cls, d_filled, N);
+        CG_LAUNCH(ctx) k_reset_open<<<grid, 256, 0, sm>>>(d_cls, d_filled, N);
     }
     if (ties) *ties = tie_total;
     if (unresolved) *unresolved = unresolved_total;

@@ -31,15 +31,14 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
                               bool over_potential, int32_t* d_recv, double* d_surface, FlatCounts* counts);
 
 // ---- drainage tree (cg_tree.cu)
-struct TreeInfo {
-    int levels;
-};
-// Kahn drainage order of FlowRouting.drainageOrder as (level, first-source) keys, the order itself
-// (optional) and the donor counts.
-cg_status drainage_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, int land_cells,
-                            int64_t* d_key, int32_t* d_donors, int32_t* d_order, TreeInfo* info);
-cg_status accumulate_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv,
-                         const int64_t* d_key, const float* d_weights, float* d_area);
+// Donor counts, the Kahn queue keys (level << 32 | deepest source) of FlowRouting.drainageOrder and,
+// if d_weights is given, FlowRouting.accumulate's areas, in one last-arriver walk. *h_levels
+// (optional, synchronises) receives the number of Kahn levels.
+cg_status tree_walk_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv,
+                        const float* d_weights, long long* d_key, int32_t* d_donors, float* d_area, int* h_levels);
+// The explicit drainage order (land cells sorted by key), for callers that want it.
+cg_status order_from_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const long long* d_key,
+                              int land_cells, int32_t* d_order);
 struct InciseArgs {
     float courant_coefficient;
     float pond_depth;

@@ -1,0 +1,565 @@
+// FlowRouting.flowDirections (FlowRouting.kt:179-448) with FlatRouting.surfaceOf
+// (FlatRouting.kt:58-518) on the device.
+//
+// Routing surface: the filled field (ocean cells their own ground), except across each raised flat,
+// where the potential of a Poisson problem is laid into the band between the flat's highest entry
+// and its lowest raised level. Flats are 8-connected components of raised cells and never touch one
+// another, so each is solved by its own CTA:
+//  - members are sorted by cell index (the reduction order is then fixed, so results are
+//    deterministic run to run);
+//  - each member's weighted degree and its Laplacian row are accumulated in the reference's
+//    neighbour order, and each column run's Thomas factorisation and solves are done by one thread
+//    in the reference's order, so both are bit-identical to FlatRouting's;
+//  - the conjugate-gradient dot products are block reductions, where the reference sums members in
+//    DFS order: the potential may differ from the reference's in its last bits (it is an
+//    intermediate, laid into a band whose order the receivers read).
+// The facet rule (Tarboton's D-infinity facets on ground-true legs, then the Rho8 draw from the
+// SplitMix64 cell hash) is a per-cell stencil in double, bit-exact.
+#include <cfloat>
+#include <climits>
+
+#include "cg_common.cuh"
+#include "cg_internal.h"
+#include "cg_util.h"
+
+namespace cg {
+
+namespace {
+
+// FlowRouting.seededNoise (FlowRouting.kt:426-436): SplitMix64 on wrapping 64-bit integers.
+__device__ __forceinline__ float seeded_noise(int lc, int lr, long long seed) {
+    unsigned long long m = (unsigned long long)seed ^ ((unsigned long long)(long long)lc * 0x9E3779B97F4A7C15ull) ^
+                           ((unsigned long long)(long long)lr * 0x27220A951D5A2B1Full);
+    m ^= m >> 30;
+    m *= 0xBF58476D1CE4E5B9ull;
+    m ^= m >> 27;
+    m *= 0x94D049BB133111EBull;
+    m ^= m >> 31;
+    int top = (int)(m >> 40);
+    return __fsub_rn(__fdiv_rn((float)top, 8388608.0f), 1.0f);
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return __fadd_rn(a, __fmul_rn(__fsub_rn(b, a), t)); }
+
+// FlowRouting.smoothSeededField (FlowRouting.kt:377-397).
+__device__ float smooth_seeded_field(int W, int lattice, int col, int row, long long seed) {
+    int cal = col * lattice, ral = row * lattice;
+    int ccol = cal / W, crow = ral / W;
+    float ac = __fdiv_rn((float)(cal - ccol * W), (float)W);
+    float ar = __fdiv_rn((float)(ral - crow * W), (float)W);
+    float ec = __fmul_rn(__fmul_rn(ac, ac), __fsub_rn(3.0f, __fmul_rn(2.0f, ac)));
+    float er = __fmul_rn(__fmul_rn(ar, ar), __fsub_rn(3.0f, __fmul_rn(2.0f, ar)));
+    int west = ccol % lattice, east = (ccol + 1) % lattice;
+    float north = lerpf(seeded_noise(west, crow, seed), seeded_noise(east, crow, seed), ec);
+    float south = lerpf(seeded_noise(west, crow + 1, seed), seeded_noise(east, crow + 1, seed), ec);
+    return lerpf(north, south, er);
+}
+
+constexpr long long kSubGridDrawSalt = 0x5f3a91c72b64d8e3LL;   // FlowRouting.kt:358
+constexpr long long kRainReliefSalt = 0x3c6ef372fe94f82bLL;    // FlatRouting.kt:507
+
+struct Steps {
+    float ew, ns, diag;   // GroundSteps (MA/GroundSteps.kt)
+    __device__ float of(int dc, int dr) const { return (dc != 0 && dr != 0) ? diag : (dr != 0 ? ns : ew); }
+};
+
+__device__ __forceinline__ int neighbour_at(int W, int H, int col, int row) {
+    if (row < 0 || row >= H) return -1;
+    return row * W + wrap_col(col, W);
+}
+
+// FlowRouting.facetReceiver (FlowRouting.kt:223-310).
+__device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int col, int row, Steps st, long long seed) {
+    const int ccs_t[4] = {1, 0, -1, 0};
+    const int crs_t[4] = {0, -1, 0, 1};
+    double here = rs[row * W + col];
+    double steepest = 0.0;
+    int fcard = -1, fdiag = -1;
+    double dshare = 0.0;
+    for (int side = 0; side < 4; ++side) {
+        int ccs = ccs_t[side], crs = crs_t[side];
+        int card = neighbour_at(W, H, col + ccs, row + crs);
+        if (card < 0) continue;
+        double cdrop = __dsub_rn(here, rs[card]);
+        double to_card = (double)st.of(ccs, crs);
+        double on_to_diag = (double)(ccs == 0 ? st.ew : st.ns);
+        for (int turn = -1; turn <= 1; turn += 2) {
+            int dcs = ccs == 0 ? turn : ccs;
+            int drs = crs == 0 ? turn : crs;
+            int diag = neighbour_at(W, H, col + dcs, row + drs);
+            if (diag < 0) continue;
+            double dfall = __dsub_rn(here, rs[diag]);
+            double dslope = __ddiv_rn(dfall, (double)st.diag);
+            double outward = __dsub_rn(dfall, cdrop);
+            double cslope = __ddiv_rn(cdrop, to_card);
+            double oslope = __ddiv_rn(outward, on_to_diag);
+            double share_edge = cdrop > 0.0 ? __ddiv_rn(__dmul_rn(__dmul_rn(outward, to_card), to_card),
+                                                        __dmul_rn(__dmul_rn(cdrop, on_to_diag), on_to_diag))
+                                            : 1.0;
+            bool to_cardinal = cdrop > 0.0 && outward <= 0.0;
+            bool to_diagonal = !to_cardinal && share_edge >= 1.0;
+            double fslope = to_cardinal ? cslope
+                                        : (to_diagonal ? dslope
+                                                       : __dsqrt_rn(__dadd_rn(__dmul_rn(cslope, cslope),
+                                                                              __dmul_rn(oslope, oslope))));
+            double share = to_cardinal ? 0.0 : (to_diagonal ? 1.0 : share_edge);
+            if (fslope > steepest) {
+                steepest = fslope;
+                fcard = card;
+                fdiag = diag;
+                dshare = share;
+            }
+        }
+    }
+    if (steepest <= 0.0) return -1;
+    if (dshare <= 0.0) return fcard;
+    if (dshare >= 1.0) return fdiag;
+    // FlowRouting.subGridDraw (FlowRouting.kt:355-356).
+    double draw = (double)__fmul_rn(__fadd_rn(seeded_noise(col, row, seed ^ kSubGridDrawSalt), 1.0f), 0.5f);
+    return draw < dshare ? fdiag : fcard;
+}
+
+// FlowRouting.steepestNeighbourOf (FlowRouting.kt:320-343).
+__device__ int steepest_neighbour(int W, int H, const double* __restrict__ rs, int col, int row, Steps st) {
+    int best = -1;
+    double sd = 0.0;
+    double here = rs[row * W + col];
+    for (int r = -1; r <= 1; ++r) {
+        int nr = row + r;
+        if (nr < 0 || nr >= H) continue;
+        for (int c = -1; c <= 1; ++c) {
+            if (r == 0 && c == 0) continue;
+            int n = nr * W + wrap_col(col + c, W);
+            double drop = __ddiv_rn(__dsub_rn(here, rs[n]), (double)st.of(c, r));
+            if (drop > sd) {
+                sd = drop;
+                best = n;
+            }
+        }
+    }
+    return best;
+}
+
+__global__ void k_receivers(const uint8_t* __restrict__ land, const double* __restrict__ surface, int W, int H,
+                            Steps st, long long seed, int by_facet, int32_t* __restrict__ recv) {
+    size_t N = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (!land[i]) {
+            recv[i] = -1;
+            continue;
+        }
+        int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+        recv[i] = by_facet ? facet_receiver(W, H, surface, col, row, st, seed)
+                           : steepest_neighbour(W, H, surface, col, row, st);
+    }
+}
+
+__global__ void k_surface(const uint8_t* __restrict__ land, const float* __restrict__ rel,
+                          const float* __restrict__ filled, size_t N, double* __restrict__ surface,
+                          uint8_t* __restrict__ raised, int* __restrict__ local) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        bool l = land[i] != 0;
+        surface[i] = (double)(l ? filled[i] : rel[i]);
+        if (raised) raised[i] = l && filled[i] > rel[i];
+        if (local) local[i] = -1;
+    }
+}
+
+__global__ void k_flat_count(const int* __restrict__ label, size_t N, int* __restrict__ count) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        if (label[i] >= 0) atomicAdd(&count[label[i]], 1);
+}
+
+__global__ void k_flat_scatter(const int* __restrict__ label, size_t N, const int* __restrict__ off,
+                               int* __restrict__ cursor, int* __restrict__ members) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int l = label[i];
+        if (l >= 0) members[off[l] + atomicAdd(&cursor[l], 1)] = (int)i;
+    }
+}
+
+constexpr int FT = 512;   // threads per flat CTA
+
+struct FlatArgs {
+    int W, H, lattice;
+    long long seed;
+    double ew, ns, diag;   // FlatRouting.stencil
+    const int* off;
+    const int* count;
+    int* members;
+    int* local;
+    const float* filled;
+    double* surface;
+    double* degree;
+    double* pivot;
+    double* x;
+    double* r;
+    double* z;
+    double* d;
+    double* ad;
+    int* kept;
+};
+
+template <class T, class Op>
+__device__ T block_reduce(T v, T* sh, Op op, T identity) {
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sh[lane] : identity;
+        for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    T out = sh[0];
+    __syncthreads();
+    return out;
+}
+
+struct DAdd {
+    __device__ double operator()(double a, double b) const { return __dadd_rn(a, b); }
+};
+struct DMax {
+    __device__ double operator()(double a, double b) const { return a > b ? a : b; }
+};
+struct FMin {
+    __device__ float operator()(float a, float b) const { return a < b ? a : b; }
+};
+struct IAnd {
+    __device__ int operator()(int a, int b) const { return a & b; }
+};
+
+// In-CTA sort of the flat's member list, ascending cell index, in place over exactly n entries.
+// The bitonic network in its all-ascending form: each merge of 2k-blocks first compares i with its
+// mirror i ^ (k-1), then half-cleans with i ^ j. Every comparator puts the smaller key at the lower
+// index, so a partner at or past n (an implicit +infinity) never has to move and is skipped.
+__device__ void sort_members(int* m, int n) {
+    int P2 = 1;
+    while (P2 < n) P2 <<= 1;
+    for (int k = 2; k <= P2; k <<= 1) {
+        for (int j = k - 1; j > 0; j = (j == k - 1) ? (k >> 2) : (j >> 1)) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                int l = i ^ j;
+                if (l > i && l < n) {
+                    int a = m[i], b = m[l];
+                    if (a > b) {
+                        m[i] = b;
+                        m[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+            if (k == 2) break;
+        }
+    }
+}
+
+__device__ __forceinline__ double stencil_weight(const FlatArgs& a, int cs, int rs) {
+    return (cs != 0 && rs != 0) ? a.diag : (rs != 0 ? a.ns : a.ew);
+}
+
+// Column-run preconditioner solve (FlatRouting.ColumnRuns.solve, FlatRouting.kt:399-413): one
+// thread per run, down the column then back up, in the reference's expression order.
+__device__ void runs_solve(const FlatArgs& a, int base, int n, const double* right, double* into) {
+    const int* mem = a.members + base;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int cell = mem[k];
+        int north = cell - a.W;
+        if (north >= 0 && a.local[north] >= 0) continue;   // not a run head
+        int pos = k, prev = -1;
+        int c = cell;
+        while (true) {
+            double carried = prev < 0 ? 0.0 : __dmul_rn(a.ns, into[base + prev]);
+            into[base + pos] = __ddiv_rn(__dadd_rn(right[base + pos], carried), a.pivot[base + pos]);
+            int south = c + a.W;
+            if (c / a.W + 1 >= a.H || a.local[south] < 0) break;
+            prev = pos;
+            pos = a.local[south];
+            c = south;
+        }
+        // Back up the run: pos is its last member.
+        while (true) {
+            int north2 = c - a.W;
+            if (north2 < 0 || a.local[north2] < 0) break;
+            int up = a.local[north2];
+            into[base + up] = __dadd_rn(into[base + up], __dmul_rn(__ddiv_rn(a.ns, a.pivot[base + up]),
+                                                                   into[base + pos]));
+            pos = up;
+            c = north2;
+        }
+    }
+}
+
+// Laplacian row (FlatRouting.kt:274-282): degree * x minus the member neighbours in stencil order.
+__device__ void apply_laplacian(const FlatArgs& a, int base, int n, const double* xv, double* into) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int cell = a.members[base + k];
+        int col = cell % a.W, row = cell / a.W;
+        double sum = __dmul_rn(a.degree[base + k], xv[base + k]);
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= a.H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                int nb = nr * a.W + wrap_col(col + cs, a.W);
+                int l = a.local[nb];
+                if (l >= 0) sum = __dsub_rn(sum, __dmul_rn(stencil_weight(a, cs, rs), xv[base + l]));
+            }
+        }
+        into[base + k] = sum;
+    }
+}
+
+__global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
+    __shared__ double shd[32];
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    const int f = blockIdx.x;
+    const int base = a.off[f];
+    const int n = a.count[f];
+    int* mem = a.members + base;
+    sort_members(mem, n);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a.local[mem[k]] = k;
+    __syncthreads();
+
+    // The entry level and the highest entry (FlatRouting.kt:93-115, 427-445).
+    float lo = FLT_MAX;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) lo = fminf(lo, a.filled[mem[k]]);
+    const float lowest = block_reduce(lo, shf, FMin(), FLT_MAX);
+    const double entry_level = (double)lowest;
+    double hi = -INFINITY;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int cell = mem[k];
+        int col = cell % a.W, row = cell / a.W;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= a.H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                int nb = nr * a.W + wrap_col(col + cs, a.W);
+                double there = a.surface[nb];
+                if (a.local[nb] < 0 && there < entry_level && there > hi) hi = there;
+            }
+        }
+    }
+    const double entry_height = block_reduce(hi, shd, DMax(), (double)-INFINITY);
+
+    // Degrees (FlatRouting.kt:239-271) and the rain (:289-295).
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int cell = mem[k];
+        int col = cell % a.W, row = cell / a.W;
+        double total = 0.0;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= a.H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                int nb = nr * a.W + wrap_col(col + cs, a.W);
+                double w = stencil_weight(a, cs, rs);
+                if (a.local[nb] >= 0) total = __dadd_rn(total, w);
+                else if (a.surface[nb] < entry_level) total = __dadd_rn(total, w);
+            }
+        }
+        a.degree[base + k] = total;
+        a.x[base + k] = 0.0;
+        a.r[base + k] = __dadd_rn(1.0, __dmul_rn(0.5, (double)smooth_seeded_field(a.W, a.lattice, col, row,
+                                                                                    a.seed ^ kRainReliefSalt)));
+    }
+    __syncthreads();
+    // Thomas pivots per run (FlatRouting.kt:388-395).
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int cell = mem[k];
+        int north = cell - a.W;
+        if (north >= 0 && a.local[north] >= 0) continue;
+        int pos = k, c = cell;
+        double prev = 0.0;
+        bool first = true;
+        while (true) {
+            double dg = a.degree[base + pos];
+            double p = first ? dg : __dsub_rn(dg, __ddiv_rn(__dmul_rn(a.ns, a.ns), prev));
+            a.pivot[base + pos] = p;
+            prev = p;
+            first = false;
+            int south = c + a.W;
+            if (c / a.W + 1 >= a.H || a.local[south] < 0) break;
+            pos = a.local[south];
+            c = south;
+        }
+    }
+    __syncthreads();
+
+    // Preconditioned conjugate gradients (FlatRouting.kt:296-333).
+    runs_solve(a, base, n, a.r, a.z);
+    __syncthreads();
+    double rn = 0.0, ra = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        double rv = a.r[base + k], zv = a.z[base + k];
+        a.d[base + k] = zv;
+        rn = __dadd_rn(rn, __dmul_rn(rv, rv));
+        ra = __dadd_rn(ra, __dmul_rn(rv, zv));
+    }
+    double rnorm = block_reduce(rn, shd, DAdd(), 0.0);
+    double rap = block_reduce(ra, shd, DAdd(), 0.0);
+    const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
+    const int most = 64 + (int)(8.0 * sqrt((double)n));
+    for (int it = 0; rnorm > stop_at && it < most; ++it) {
+        apply_laplacian(a, base, n, a.d, a.ad);
+        __syncthreads();
+        double e = 0.0;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) e = __dadd_rn(e, __dmul_rn(a.d[base + k], a.ad[base + k]));
+        double energy = block_reduce(e, shd, DAdd(), 0.0);
+        if (energy <= 0.0 || rap <= 0.0) break;
+        double step = __ddiv_rn(rap, energy);
+        double nn = 0.0;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            a.x[base + k] = __dadd_rn(a.x[base + k], __dmul_rn(step, a.d[base + k]));
+            double rv = __dsub_rn(a.r[base + k], __dmul_rn(step, a.ad[base + k]));
+            a.r[base + k] = rv;
+            nn = __dadd_rn(nn, __dmul_rn(rv, rv));
+        }
+        double next_norm = block_reduce(nn, shd, DAdd(), 0.0);
+        runs_solve(a, base, n, a.r, a.z);
+        __syncthreads();
+        double na = 0.0;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) na = __dadd_rn(na, __dmul_rn(a.r[base + k], a.z[base + k]));
+        double next_ap = block_reduce(na, shd, DAdd(), 0.0);
+        double improvement = __ddiv_rn(next_ap, rap);
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            a.d[base + k] = __dadd_rn(a.z[base + k], __dmul_rn(improvement, a.d[base + k]));
+        __syncthreads();
+        rnorm = next_norm;
+        rap = next_ap;
+    }
+    int positive = 1;
+    double top = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        double v = a.x[base + k];
+        if (!(v > 0.0)) positive = 0;
+        if (v > top) top = v;
+    }
+    positive = block_reduce(positive, shi, IAnd(), 1);
+    const double highest = block_reduce(top, shd, DMax(), 0.0);
+
+    // FlatRouting.layInBand (FlatRouting.kt:455-489).
+    bool laid = positive && !(highest <= 0.0 || entry_height >= entry_level);
+    if (laid) {
+        const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            a.surface[mem[k]] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(a.x[base + k], highest)));
+        __syncthreads();
+        int ok = 1;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            int cell = mem[k];
+            int col = cell % a.W, row = cell / a.W;
+            double here = a.surface[cell];
+            bool lower = false;
+            for (int rs = -1; rs <= 1 && !lower; ++rs) {
+                int nr = row + rs;
+                if (nr < 0 || nr >= a.H) continue;
+                for (int cs = -1; cs <= 1; ++cs) {
+                    if (cs == 0 && rs == 0) continue;
+                    if (a.surface[nr * a.W + wrap_col(col + cs, a.W)] < here) {
+                        lower = true;
+                        break;
+                    }
+                }
+            }
+            if (!lower) ok = 0;
+        }
+        ok = block_reduce(ok, shi, IAnd(), 1);
+        if (!ok) {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) a.surface[mem[k]] = (double)a.filled[mem[k]];
+            laid = false;
+        }
+    }
+    if (!laid && threadIdx.x == 0) atomicAdd(a.kept, 1);
+}
+
+}  // namespace
+
+cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel,
+                              const float* d_filled, int64_t seed, double r, int lattice, bool by_facet,
+                              bool over_potential, int32_t* d_recv, double* d_surface, FlatCounts* counts) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    FlatCounts fc{0, 0, 0};
+    if (!over_potential) {
+        CG_LAUNCH(ctx) k_surface<<<grid, 256, 0, sm>>>(d_land, d_rel, d_filled, N, d_surface, nullptr, nullptr);
+        CG_CHECK_LAUNCH(ctx);
+    } else {
+        CG_BUF(uint8_t, d_raised, ctx, S_FLATS, N);
+        CG_BUF(int, d_local, ctx, S_FLATIDX, N);
+        CG_BUF(int, d_root, ctx, S_LABEL, N);
+        CG_BUF(int, d_label, ctx, S_SCRATCH2, N);
+        CG_LAUNCH(ctx) k_surface<<<grid, 256, 0, sm>>>(d_land, d_rel, d_filled, N, d_surface, d_raised, d_local);
+        CG_CHECK_LAUNCH(ctx);
+        int flats = 0;
+        cg_status st = component_labels(ctx, W, H, d_raised, d_root, d_label, &flats);
+        if (st != CG_OK) return st;
+        if (flats > 0) {
+            CG_BUF(int, d_cnt, ctx, S_CG0, 3 * (size_t)flats + 1);
+            int* d_off = d_cnt + flats;
+            int* d_cur = d_off + flats;
+            int* d_kept = d_cur + flats;
+            CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(int) * (3 * (size_t)flats + 1), sm));
+            CG_LAUNCH(ctx) k_flat_count<<<grid, 256, 0, sm>>>(d_label, N, d_cnt);
+            CG_CHECK_LAUNCH(ctx);
+            int raised = 0;
+            if ((st = exclusive_scan(ctx, d_cnt, d_off, flats, &raised)) != CG_OK) return st;
+            CG_BUF(int, d_members, ctx, S_FLATMEM, raised);
+            CG_BUF(double, d_dbl, ctx, S_CG1, 7 * (size_t)raised);
+            CG_LAUNCH(ctx) k_flat_scatter<<<grid, 256, 0, sm>>>(d_label, N, d_off, d_cur, d_members);
+            CG_CHECK_LAUNCH(ctx);
+            FlatArgs a;
+            a.W = W;
+            a.H = H;
+            a.lattice = lattice;
+            a.seed = seed;
+            // FlatRouting.stencil (FlatRouting.kt:177-186).
+            if (r <= 1.0) {
+                double dg = 2.0 / (1.0 + r * r);
+                a.ew = 1.0;
+                a.ns = (1.0 + 2.0 * dg) / (r * r) - 2.0 * dg;
+                a.diag = dg;
+            } else {
+                double dg = 2.0 / (1.0 + 1.0 / (r * r));
+                a.ew = r * r * (1.0 + 2.0 * dg) - 2.0 * dg;
+                a.ns = 1.0;
+                a.diag = dg;
+            }
+            a.off = d_off;
+            a.count = d_cnt;
+            a.members = d_members;
+            a.local = d_local;
+            a.filled = d_filled;
+            a.surface = d_surface;
+            a.degree = d_dbl;
+            a.pivot = d_dbl + raised;
+            a.x = d_dbl + 2 * (size_t)raised;
+            a.r = d_dbl + 3 * (size_t)raised;
+            a.z = d_dbl + 4 * (size_t)raised;
+            a.d = d_dbl + 5 * (size_t)raised;
+            a.ad = d_dbl + 6 * (size_t)raised;
+            a.kept = d_kept;
+            CG_LAUNCH(ctx) k_flat_solve<<<flats, FT, 0, sm>>>(a);
+            CG_CHECK_LAUNCH(ctx);
+            CG_CUDA(ctx, cudaMemcpyAsync(&fc.kept, d_kept, sizeof(int), cudaMemcpyDeviceToHost, sm));
+            CG_CUDA(ctx, cudaStreamSynchronize(sm));
+            fc.flats = flats;
+            fc.raised = raised;
+        }
+    }
+    Steps steps;
+    steps.ew = 1.0f;
+    steps.ns = (float)r;
+    steps.diag = (float)std::sqrt(1.0 + r * r);
+    CG_LAUNCH(ctx) k_receivers<<<grid, 256, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed, by_facet ? 1 : 0, d_recv);
+    CG_CHECK_LAUNCH(ctx);
+    if (counts) *counts = fc;
+    return CG_OK;
+}
+
+}  // namespace cg

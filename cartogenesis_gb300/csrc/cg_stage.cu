@@ -1,0 +1,513 @@
+// ErosionStage.apply on the device (ErosionStage.kt:133-183 with HydraulicErosion.apply,
+// HydraulicErosion.kt:596-1506), profile P0, and the C entry points that run one routing function
+// on host buffers.
+//
+// The world stays resident in HBM for the whole stage: heights ping-pong between two buffers, and
+// each round's masks, fields, receivers and tree live in context buffers reused round to round. The
+// host sequences the phases and reads back one shoreline and one land count per round.
+#include <cmath>
+#include <vector>
+
+#include "cg_common.cuh"
+#include "cg_internal.h"
+#include "cg_params.h"
+#include "cg_util.h"
+
+namespace cg {
+
+namespace {
+
+// HydraulicErosion.kt:824-837: h += rate * upliftMetresPerRoundPerMm / metresPerFieldUnit where rate > 0.
+__global__ void k_uplift(float* __restrict__ h, const float* __restrict__ rate, size_t N, float per_mm,
+                         float metres_per_field) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        float r = rate[i];
+        if (r <= 0.0f) continue;
+        h[i] = __fadd_rn(h[i], __fdiv_rn(__fmul_rn(r, per_mm), metres_per_field));
+    }
+}
+
+// The weights with no weather given: rain all 1 (mean 1, weight 1) and no cover (factor 1), times
+// the rock's factor. normaliseOverLand / shieldingOverLand reduce to exactly these ones.
+__global__ void k_unit_weights(const float* __restrict__ rock, size_t N, float* __restrict__ runoff,
+                               float* __restrict__ erod) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        runoff[i] = 1.0f;
+        erod[i] = rock ? __fmul_rn(1.0f, rock[i]) : 1.0f;
+    }
+}
+
+// The reference's sequential double sum over land cells, in cell order (HydraulicErosion.kt:557,
+// 476-478): one CTA; the threads stage chunks in shared memory and one thread adds them in order.
+// mode 0: sum of x; mode 1: sum of (1 - 0.5 x).
+__global__ void __launch_bounds__(1024) k_seq_land_sum(const float* __restrict__ x, const uint8_t* __restrict__ land,
+                                                       size_t N, int mode, double* __restrict__ out) {
+    __shared__ float chunk[2][4096];
+    __shared__ uint8_t lchunk[2][4096];
+    double s = 0.0;
+    const size_t C = 4096;
+    for (size_t base = 0; base < N; base += C) {
+        int b = (int)((base / C) & 1);
+        for (size_t i = threadIdx.x; i < C && base + i < N; i += blockDim.x) {
+            chunk[b][i] = x[base + i];
+            lchunk[b][i] = land[base + i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            size_t n = N - base < C ? N - base : C;
+            for (size_t i = 0; i < n; ++i) {
+                if (!lchunk[b][i]) continue;
+                float v = chunk[b][i];
+                if (mode == 1) v = __fsub_rn(1.0f, __fmul_rn(0.5f, v));
+                s = __dadd_rn(s, (double)v);
+            }
+        }
+    }
+    if (threadIdx.x == 0) *out = s;
+}
+
+// weights[c] = rain[c] / mean, or 0 when mean <= 0 (HydraulicErosion.kt:558-567).
+__global__ void k_normalise(const float* __restrict__ rain, const double* __restrict__ sum, int land_cells, size_t N,
+                            float* __restrict__ w) {
+    float mean = (float)__ddiv_rn(*sum, (double)land_cells);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        w[i] = mean <= 0.0f ? 0.0f : __fdiv_rn(rain[i], mean);
+}
+
+// erod[c] = (1 - 0.5 d) / mean, or 1 when mean <= 0 (HydraulicErosion.kt:479-486), times the rock.
+__global__ void k_shield(const float* __restrict__ veg, const double* __restrict__ sum, int land_cells,
+                         const float* __restrict__ rock, size_t N, float* __restrict__ e) {
+    float mean = (float)__ddiv_rn(*sum, (double)land_cells);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        float v = mean <= 0.0f ? 1.0f : __fdiv_rn(__fsub_rn(1.0f, __fmul_rn(0.5f, veg[i])), mean);
+        e[i] = rock ? __fmul_rn(v, rock[i]) : v;
+    }
+}
+
+__global__ void k_fill_value(float* __restrict__ a, size_t N, float v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+__global__ void k_times_rock(float* __restrict__ e, const float* __restrict__ rock, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        e[i] = __fmul_rn(e[i], rock[i]);
+}
+
+bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+cg_status check_grid(cg_ctx* ctx, int W, int H) {
+    if (!pow2(W) || !pow2(H)) return fail(ctx, CG_BAD_ARG, "width/height must be powers of two (got %d x %d)", W, H);
+    if ((int64_t)W * H > ((int64_t)1 << 30)) return fail(ctx, CG_BAD_ARG, "grid of %d x %d cells is too large", W, H);
+    return CG_OK;
+}
+
+cg_status up(cg_ctx* ctx, void* d, const void* h, size_t bytes) {
+    CG_CUDA(ctx, cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return CG_OK;
+}
+cg_status down(cg_ctx* ctx, void* h, const void* d, size_t bytes) {
+    CG_CUDA(ctx, cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return CG_OK;
+}
+
+#define CG_TRY(x)                       \
+    do {                                \
+        cg_status s_ = (x);             \
+        if (s_ != CG_OK) return s_;     \
+    } while (0)
+
+cg_status cancelled(cg_ctx* ctx) {
+    if (ctx->cancel.exchange(0)) return fail(ctx, CG_CANCELLED, "cancelled");
+    return CG_OK;
+}
+
+}  // namespace
+
+// The round loop with the world resident on the device. `d_h` holds the input heights and
+// receives the result (through *d_result, which is d_h or the ping-pong partner).
+cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, float* d_h2, const float* d_uplift,
+                          const float* d_rock, const float* d_rain, const float* d_veg, float** d_result,
+                          cg_round_stats* stats, int* last_land_cells) {
+    const int W = p.width, H = p.height;
+    const size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    const int grid = ctx->num_sms * 8;
+    float* cur = d_h;
+    float* other = d_h2;
+    *d_result = cur;
+    *last_land_cells = -1;
+    if (!p.enabled) return CG_OK;
+    const cg_thermal_limits lim = thermal_limits(p);
+    const int sweeps = sweeps_for(p);
+    if (sweeps > 0) {
+        float* res;
+        CG_TRY(thermal_sweeps_dev(ctx, W, H, cur, other, lim, sweeps, p.rate, &res));
+        if (res != cur) std::swap(cur, other);
+    }
+    *d_result = cur;
+    int per_round = sweeps / (p.hydraulic_rounds < 1 ? 1 : p.hydraulic_rounds);
+    if (per_round < 1) per_round = 1;
+    if (p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) return CG_OK;
+
+    const ScaleF sc = scale_of(p);
+    const RatesF rates = rates_of(p);
+    const int lattice = smooth_field_lattice_columns(p.world_width_km);
+    const float land_half = std::fmax(sc.land_half(), 1e-6f);
+    const float sea_half = std::fmax(sc.sea_half(), 1e-6f);
+    const float per_mm = (float)(sc.years_per_round / 1000.0);
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_BUF(double, d_surface, ctx, S_SURFACE, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_BUF(int32_t, d_donors, ctx, S_DONORS, N);
+    CG_BUF(long long, d_key, ctx, S_KEY, N);
+    CG_BUF(float, d_area, ctx, S_AREA, N);
+    CG_BUF(float, d_runoff, ctx, S_RUNOFF, N);
+    CG_BUF(float, d_erod, ctx, S_ERODE, N);
+    CG_BUF(double, d_sum, ctx, S_CG3, 2);
+
+    // Phase boundaries of a round, for the per-phase device times of cg_round_stats.
+    cudaEvent_t ev[7] = {};
+    if (stats)
+        for (auto& e : ev) CG_CUDA(ctx, cudaEventCreate(&e));
+    struct Events {
+        cudaEvent_t* ev;
+        bool on;
+        ~Events() {
+            if (on)
+                for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+        }
+    } guard{ev, stats != nullptr};
+    auto mark = [&](int i) {
+        if (stats) cudaEventRecord(ev[i], sm);
+    };
+
+    for (int round = 0; round < p.hydraulic_rounds; ++round) {
+        CG_TRY(cancelled(ctx));
+        const long long launches0 = ctx->launches;
+        mark(0);
+        if (d_uplift) CG_LAUNCH(ctx) k_uplift<<<grid, 256, 0, sm>>>(cur, d_uplift, N, per_mm, sc.relief_span());
+        float shoreline;
+        int land_cells;
+        CG_TRY(percentile_cut_dev(ctx, W, H, cur, p.sea_level, land_half, sea_half, stand_below_today(p, round),
+                                  d_land, d_rel, &shoreline, &land_cells));
+        *last_land_cells = land_cells;
+        if (land_cells == 0) {
+            *d_result = cur;
+            return CG_OK;
+        }
+        // normaliseOverLand / shieldingOverLand (HydraulicErosion.kt:902-911).
+        if (!d_rain && (!d_veg || !p.shield_cut)) {
+            CG_LAUNCH(ctx) k_unit_weights<<<grid, 256, 0, sm>>>(d_rock, N, d_runoff, d_erod);
+        } else {
+            if (d_rain) {
+                CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_rain, d_land, N, 0, d_sum);
+                CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, sm>>>(d_rain, d_sum, land_cells, N, d_runoff);
+            } else {
+                CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_runoff, N, 1.0f);
+            }
+            if (p.shield_cut && d_veg) {
+                CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_veg, d_land, N, 1, d_sum + 1);
+                CG_LAUNCH(ctx) k_shield<<<grid, 256, 0, sm>>>(d_veg, d_sum + 1, land_cells, d_rock, N, d_erod);
+            } else {
+                CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_erod, N, 1.0f);
+                if (d_rock) CG_LAUNCH(ctx) k_times_rock<<<grid, 256, 0, sm>>>(d_erod, d_rock, N);
+            }
+        }
+        CG_CHECK_LAUNCH(ctx);
+        mark(1);
+        int64_t ties = 0, unresolved = 0;
+        CG_TRY(fill_depressions_dev(ctx, W, H, d_land, d_rel, d_filled, &ties, &unresolved));
+        mark(2);
+        FlatCounts fc{0, 0, 0};
+        CG_TRY(flow_directions_dev(ctx, W, H, d_land, d_rel, d_filled, p.seed, rates.cell_height_in_cell_widths,
+                                   lattice, p.facet_routing != 0, p.flat_potential != 0, d_recv, d_surface, &fc));
+        mark(3);
+        int levels = 0;
+        CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, stats ? &levels : nullptr));
+        mark(4);
+        InciseArgs ia;
+        ia.courant_coefficient = rates.courant_coefficient;
+        ia.pond_depth = rates.pond_depth;
+        ia.land_cells = (float)land_cells;
+        ia.land_range = land_half;
+        ia.shoreline = shoreline;
+        ia.step_ns = rates.step_ns;
+        ia.step_diag = rates.step_diag;
+        ia.only_above_base = p.receiver_clamp != 0;
+        CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_filled, d_rel, d_area, d_erod, cur, ia));
+        mark(5);
+        // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
+        float* res;
+        CG_TRY(thermal_sweeps_dev(ctx, W, H, cur, other, lim, per_round, p.rate, &res));
+        if (res != cur) std::swap(cur, other);
+        *d_result = cur;
+        mark(6);
+        if (stats) {
+            CG_CUDA(ctx, cudaEventSynchronize(ev[6]));
+            float ms[7] = {0};
+            for (int i = 1; i < 7; ++i) cudaEventElapsedTime(&ms[i], ev[i - 1], ev[i]);
+            float total = 0.0f;
+            cudaEventElapsedTime(&total, ev[0], ev[6]);
+            cg_round_stats& s = stats[round];
+            std::memset(&s, 0, sizeof(s));
+            s.round = round;
+            s.land_cells = land_cells;
+            s.shoreline = shoreline;
+            s.flats = fc.flats;
+            s.flats_kept = fc.kept;
+            s.raised_cells = fc.raised;
+            s.levels = levels;
+            s.fill_ties = ties;
+            s.fill_unresolved = unresolved;
+            s.kernel_launches = ctx->launches - launches0;
+            s.ms_total = total;
+            s.ms_cut = ms[1];
+            s.ms_fill = ms[2];
+            s.ms_route = ms[3];
+            s.ms_tree = ms[4];
+            s.ms_incise = ms[5];
+            s.ms_relax = ms[6];
+        }
+    }
+    return CG_OK;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
+                         cg_round_stats* stats) {
+    if (!ctx || !p || !in || !out || !in->height || !out->height) return CG_BAD_ARG;
+    if (p->abi_version != CG_ABI_VERSION)
+        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
+                    CG_ABI_VERSION);
+    CG_TRY(check_grid(ctx, p->width, p->height));
+    if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
+    if (p->profile != CG_PROFILE_P0) return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 only)", p->profile);
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cancel.store(0);
+    const int W = p->width, H = p->height;
+    const size_t N = (size_t)W * H;
+    CG_BUF(float, d_h, ctx, S_H0, N);
+    CG_BUF(float, d_h2, ctx, S_H1, N);
+    float* d_up = nullptr;
+    float* d_rock = nullptr;
+    float* d_rain = nullptr;
+    float* d_veg = nullptr;
+    CG_TRY(up(ctx, d_h, in->height, N * 4));
+    // Inputs, each in its own slot.
+    {
+        cg_status st = CG_OK;
+        if (in->uplift_mm_per_year) {
+            d_up = (float*)buf(ctx, S_UPLIFT, N * 4, &st);
+            if (st != CG_OK) return st;
+            CG_TRY(up(ctx, d_up, in->uplift_mm_per_year, N * 4));
+        }
+        if (in->rock_erodibility) {
+            d_rock = (float*)buf(ctx, S_ROCK, N * 4, &st);
+            if (st != CG_OK) return st;
+            CG_TRY(up(ctx, d_rock, in->rock_erodibility, N * 4));
+        }
+        if (in->rainfall_mm) {
+            d_rain = (float*)buf(ctx, S_RAIN, N * 4, &st);
+            if (st != CG_OK) return st;
+            CG_TRY(up(ctx, d_rain, in->rainfall_mm, N * 4));
+        }
+        if (in->vegetation_density) {
+            d_veg = (float*)buf(ctx, S_VEG, N * 4, &st);
+            if (st != CG_OK) return st;
+            CG_TRY(up(ctx, d_veg, in->vegetation_density, N * 4));
+        }
+    }
+    float* d_res = d_h;
+    int land_cells = -1;
+    CG_TRY(erode_stage_dev(ctx, *p, d_h, d_h2, d_up, d_rock, d_rain, d_veg, &d_res, stats, &land_cells));
+    CG_TRY(down(ctx, out->height, d_res, N * 4));
+    const bool routed = land_cells > 0 && p->enabled && p->hydraulic_rounds > 0 && p->bedrock_erodibility_per_year > 0.0f;
+    if (routed) {
+        if (out->receivers) CG_TRY(down(ctx, out->receivers, ctx->bufs[S_RECV].ptr, N * 4));
+        if (out->area) CG_TRY(down(ctx, out->area, ctx->bufs[S_AREA].ptr, N * 4));
+        if (out->filled) CG_TRY(down(ctx, out->filled, ctx->bufs[S_FILLED].ptr, N * 4));
+        if (out->relative) CG_TRY(down(ctx, out->relative, ctx->bufs[S_REL].ptr, N * 4));
+        if (out->is_land) CG_TRY(down(ctx, out->is_land, ctx->bufs[S_LAND].ptr, N));
+        if (out->donors) CG_TRY(down(ctx, out->donors, ctx->bufs[S_DONORS].ptr, N * 4));
+        if (out->order) {
+            CG_BUF(int32_t, d_order, ctx, S_ORDER, N);
+            CG_CUDA(ctx, cudaMemsetAsync(d_order, 0xFF, N * 4, ctx->stream));
+            CG_TRY(order_from_keys_dev(ctx, W, H, (const uint8_t*)ctx->bufs[S_LAND].ptr,
+                                       (const long long*)ctx->bufs[S_KEY].ptr, land_cells, d_order));
+            CG_TRY(down(ctx, out->order, d_order, N * 4));
+        }
+        if (out->basin_of_cell || out->basins) {
+            const RatesF rates = rates_of(*p);
+            CG_BUF(int32_t, d_lab, ctx, S_BASIN2, N);
+            CG_TRY(spillways_dev(ctx, W, H, (const uint8_t*)ctx->bufs[S_LAND].ptr, (const float*)ctx->bufs[S_REL].ptr,
+                                 (const float*)ctx->bufs[S_FILLED].ptr, (const int32_t*)ctx->bufs[S_RECV].ptr,
+                                 rates.pond_depth, d_lab, out->basins));
+            if (out->basin_of_cell) CG_TRY(down(ctx, out->basin_of_cell, d_lab, N * 4));
+        }
+    }
+    return sync(ctx);
+}
+
+cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, float* out_dev,
+                             cg_round_stats* stats, int32_t* land_cells_out) {
+    if (!ctx || !p || !in || !in->height || !out_dev) return CG_BAD_ARG;
+    if (p->abi_version != CG_ABI_VERSION)
+        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
+                    CG_ABI_VERSION);
+    CG_TRY(check_grid(ctx, p->width, p->height));
+    if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
+    if (p->profile != CG_PROFILE_P0) return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 only)", p->profile);
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cancel.store(0);
+    const size_t N = (size_t)p->width * p->height;
+    CG_BUF(float, d_h, ctx, S_H0, N);
+    CG_BUF(float, d_h2, ctx, S_H1, N);
+    CG_CUDA(ctx, cudaMemcpyAsync(d_h, in->height, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    float* d_res = d_h;
+    int land_cells = -1;
+    CG_TRY(erode_stage_dev(ctx, *p, d_h, d_h2, in->uplift_mm_per_year, in->rock_erodibility, in->rainfall_mm,
+                           in->vegetation_density, &d_res, stats, &land_cells));
+    CG_CUDA(ctx, cudaMemcpyAsync(out_dev, d_res, N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (land_cells_out) *land_cells_out = land_cells;
+    return sync(ctx);
+}
+
+cg_status cg_percentile_cut(cg_ctx* ctx, int32_t W, int32_t H, const float* heights, float sea_level,
+                            float highest_land, float deepest_ocean, float lowstand_share, float* shoreline,
+                            uint8_t* is_land, float* relative, int32_t* land_cells) {
+    if (!ctx || !heights || !shoreline || !is_land || !relative || !land_cells) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(float, d_h, ctx, S_H0, N);
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_TRY(up(ctx, d_h, heights, N * 4));
+    ScaleF sc{40075.0, highest_land, deepest_ocean, 0.0};
+    float s;
+    int n;
+    CG_TRY(percentile_cut_dev(ctx, W, H, d_h, sea_level, std::fmax(sc.land_half(), 1e-6f),
+                              std::fmax(sc.sea_half(), 1e-6f), lowstand_share, d_land, d_rel, &s, &n));
+    CG_TRY(down(ctx, is_land, d_land, N));
+    CG_TRY(down(ctx, relative, d_rel, N * 4));
+    CG_TRY(sync(ctx));
+    *shoreline = s;
+    *land_cells = n;
+    return CG_OK;
+}
+
+cg_status cg_fill_depressions(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const float* relative,
+                              float* filled, int64_t* ties, int64_t* unresolved) {
+    if (!ctx || !is_land || !relative || !filled) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_rel, relative, N * 4));
+    CG_TRY(fill_depressions_dev(ctx, W, H, d_land, d_rel, d_filled, ties, unresolved));
+    CG_TRY(down(ctx, filled, d_filled, N * 4));
+    return sync(ctx);
+}
+
+cg_status cg_flow_directions(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const float* relative,
+                             const float* filled, int64_t seed, double r, int32_t lattice, int32_t by_facet,
+                             int32_t over_potential, int32_t* receivers, double* surface, int32_t* flat_counts) {
+    if (!ctx || !is_land || !relative || !filled || !receivers) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    if (!(r > 0.0) || lattice < 1) return fail(ctx, CG_BAD_ARG, "bad cell aspect %g or lattice %d", r, lattice);
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_BUF(double, d_surface, ctx, S_SURFACE, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_rel, relative, N * 4));
+    CG_TRY(up(ctx, d_filled, filled, N * 4));
+    FlatCounts fc{0, 0, 0};
+    CG_TRY(flow_directions_dev(ctx, W, H, d_land, d_rel, d_filled, seed, r, lattice, by_facet != 0,
+                               over_potential != 0, d_recv, d_surface, &fc));
+    CG_TRY(down(ctx, receivers, d_recv, N * 4));
+    if (surface) CG_TRY(down(ctx, surface, d_surface, N * 8));
+    CG_TRY(sync(ctx));
+    if (flat_counts) {
+        flat_counts[0] = fc.flats;
+        flat_counts[1] = fc.kept;
+        flat_counts[2] = fc.raised;
+    }
+    return CG_OK;
+}
+
+cg_status cg_drainage_order(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const int32_t* receivers,
+                            int32_t land_cells, int32_t* order) {
+    if (!ctx || !is_land || !receivers || !order || land_cells < 0) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_BUF(int32_t, d_donors, ctx, S_DONORS, N);
+    CG_BUF(long long, d_key, ctx, S_KEY, N);
+    CG_BUF(int32_t, d_order, ctx, S_ORDER, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_recv, receivers, N * 4));
+    CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, nullptr, d_key, d_donors, nullptr, nullptr));
+    CG_TRY(order_from_keys_dev(ctx, W, H, d_land, d_key, land_cells, d_order));
+    if (land_cells > 0) CG_TRY(down(ctx, order, d_order, (size_t)land_cells * 4));
+    return sync(ctx);
+}
+
+cg_status cg_accumulate(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const int32_t* receivers,
+                        int32_t land_cells, const float* weights, float* area) {
+    if (!ctx || !is_land || !receivers || !weights || !area) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_BUF(int32_t, d_donors, ctx, S_DONORS, N);
+    CG_BUF(long long, d_key, ctx, S_KEY, N);
+    CG_BUF(float, d_w, ctx, S_RUNOFF, N);
+    CG_BUF(float, d_area, ctx, S_AREA, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_recv, receivers, N * 4));
+    CG_TRY(up(ctx, d_w, weights, N * 4));
+    CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_w, d_key, d_donors, d_area, nullptr));
+    CG_TRY(down(ctx, area, d_area, N * 4));
+    (void)land_cells;
+    return sync(ctx);
+}
+
+cg_status cg_spillways(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const float* relative,
+                       const float* filled, const int32_t* receivers, float pond_depth, int32_t* basin_of_cell,
+                       cg_basins* basins) {
+    if (!ctx || !is_land || !relative || !filled || !receivers) return CG_BAD_ARG;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t N = (size_t)W * H;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_BUF(int32_t, d_lab, ctx, S_BASIN2, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_rel, relative, N * 4));
+    CG_TRY(up(ctx, d_filled, filled, N * 4));
+    CG_TRY(up(ctx, d_recv, receivers, N * 4));
+    CG_TRY(spillways_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, pond_depth, d_lab, basins));
+    if (basin_of_cell) CG_TRY(down(ctx, basin_of_cell, d_lab, N * 4));
+    return sync(ctx);
+}
+
+}  // extern "C"

@@ -178,6 +178,7 @@ cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, 
         else if (passes >= 2) e = launch<2>(src, dst, W, H, a, ctx->stream), passes -= 2;
         else e = launch<1>(src, dst, W, H, a, ctx->stream), passes -= 1;
         if (e != cudaSuccess) return cuda_fail(ctx, e, "thermal_sweeps_kernel", __FILE__, __LINE__);
+        ctx->launches++;
         float* t = src;
         src = dst;
         dst = t;

@@ -1,0 +1,573 @@
+// The drainage tree on the device: FlowRouting.drainageOrder and accumulate
+// (FlowRouting.kt:485-511, 695-729), HydraulicErosion.incise (HydraulicErosion.kt:2298-2390) and
+// FlowRouting.spillways (FlowRouting.kt:573-677), each reproducing the reference's result exactly.
+//
+// Kahn order without a queue. The reference seeds a FIFO with the land sources in index order and
+// appends a cell when its last donor leaves the queue, so the queue is sorted by level (the longest
+// donor chain into a cell) and, within a level, by the position of the last donor to leave. By
+// induction that is the order of the chain of "deepest latest" donors back to a source, i.e. of
+// that source's index. So a cell's place is the key (level, s), s the largest source index among the
+// sources farthest upstream of it, and key(r) = max over donors of key(d) + (1, 0): a tree
+// reduction from the leaves. It runs as a last-arriver walk: one thread per source climbs down its
+// receivers; at each cell the thread that brings the donor count to zero computes the cell's key and
+// its accumulation (its weight plus its donors' areas in key order, the reference's float
+// additions in the reference's order) and carries on; the others stop. No barrier, O(N) work.
+//
+// Incision needs each receiver final before its donors: cells are bucketed by their depth below
+// the outlet (pointer jumping) and one cooperative kernel sweeps the depths in order with a grid
+// barrier between them. Every order with receivers first gives the same bits, because a cell reads
+// only its receiver's final state.
+#include <cooperative_groups.h>
+
+#include <cfloat>
+#include <climits>
+#include <vector>
+
+#include "cg_common.cuh"
+#include "cg_internal.h"
+#include "cg_util.h"
+
+namespace cg {
+
+namespace cgr = cooperative_groups;
+
+namespace {
+
+constexpr long long LEVEL_ONE = 1LL << 32;
+
+__device__ __forceinline__ bool is_land_receiver(const uint8_t* land, int r) { return r >= 0 && land[r]; }
+
+__global__ void k_donor_count(const uint8_t* __restrict__ land, const int32_t* __restrict__ recv, size_t N,
+                              int32_t* __restrict__ donors) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (!land[i]) continue;
+        int r = recv[i];
+        if (is_land_receiver(land, r)) atomicAdd(&donors[r], 1);
+    }
+}
+
+__global__ void k_pending_init(const int32_t* __restrict__ donors, size_t N, int32_t* __restrict__ pending) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        pending[i] = donors[i];
+}
+
+struct WalkArgs {
+    int W, H;
+    const uint8_t* land;
+    const int32_t* recv;
+    const int32_t* donors;
+    int32_t* pending;
+    long long* key;
+    const float* weights;   // null: keys only
+    float* area;
+    unsigned long long* max_key;
+};
+
+// The cell's donors' keys, in key order; returns how many (at most 8).
+__device__ int sorted_donors(const WalkArgs& a, int r, long long* keys, int* cells) {
+    int row = r / a.W, col = r % a.W, n = 0;
+    for (int rs = -1; rs <= 1; ++rs) {
+        int nr = row + rs;
+        if (nr < 0 || nr >= a.H) continue;
+        for (int cs = -1; cs <= 1; ++cs) {
+            if (rs == 0 && cs == 0) continue;
+            int c = nr * a.W + wrap_col(col + cs, a.W);
+            if (!a.land[c] || a.recv[c] != r) continue;
+            long long k = *((volatile long long*)&a.key[c]);
+            int j = n++;
+            while (j > 0 && keys[j - 1] > k) {
+                keys[j] = keys[j - 1];
+                cells[j] = cells[j - 1];
+                --j;
+            }
+            keys[j] = k;
+            cells[j] = c;
+        }
+    }
+    return n;
+}
+
+__global__ void k_walk(WalkArgs a) {
+    size_t N = (size_t)a.W * a.H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (!a.land[i] || a.donors[i] != 0) continue;
+        int c = (int)i;
+        long long k = (long long)c;   // a source: level 0, its own index
+        a.key[c] = k;
+        if (a.weights) a.area[c] = a.weights[c];
+        unsigned long long local_max = (unsigned long long)k;
+        while (true) {
+            int r = a.recv[c];
+            if (!is_land_receiver(a.land, r)) break;
+            __threadfence();   // this cell's key and area are visible before its arrival is counted
+            if (atomicSub(&a.pending[r], 1) != 1) break;   // not the last donor in
+            __threadfence();
+            long long keys[8];
+            int cells[8];
+            int n = sorted_donors(a, r, keys, cells);
+            long long kr = keys[n - 1] + LEVEL_ONE;
+            a.key[r] = kr;
+            if (a.weights) {
+                float s = a.weights[r];
+                for (int j = 0; j < n; ++j) s = __fadd_rn(s, *((volatile float*)&a.area[cells[j]]));
+                a.area[r] = s;
+            }
+            if ((unsigned long long)kr > local_max) local_max = (unsigned long long)kr;
+            c = r;
+        }
+        atomicMax(a.max_key, local_max);
+    }
+}
+
+// Areas of land cells are the weights where no walk reached (sea cells hold 0).
+__global__ void k_area_sea(const uint8_t* __restrict__ land, size_t N, float* __restrict__ area) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        if (!land[i]) area[i] = 0.0f;
+}
+
+// Key-value bitonic stage over P2 slots padded with the largest key. Used only to hand the
+// explicit order back to a caller that asked for it.
+__global__ void k_bitonic_kv(long long* keys, int* vals, int P2, int k, int j) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
+        int l = i ^ j;
+        if (l <= i) continue;
+        long long ka = keys[i], kb = keys[l];
+        bool up = (i & k) == 0;
+        if ((ka > kb) == up) {
+            keys[i] = kb;
+            keys[l] = ka;
+            int t = vals[i];
+            vals[i] = vals[l];
+            vals[l] = t;
+        }
+    }
+}
+
+__global__ void k_pad_kv(long long* keys, int* vals, int n, int P2) {
+    for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
+        keys[i] = LLONG_MAX;
+        vals[i] = -1;
+    }
+}
+
+__global__ void k_land_flags(const uint8_t* __restrict__ land, size_t N, int* __restrict__ flag) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        flag[i] = land[i] ? 1 : 0;
+}
+
+__global__ void k_land_compact(const uint8_t* __restrict__ land, const int* __restrict__ pos,
+                               const long long* __restrict__ key, size_t N, long long* __restrict__ okeys,
+                               int* __restrict__ ovals) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        if (land[i]) {
+            okeys[pos[i]] = key[i];
+            ovals[pos[i]] = (int)i;
+        }
+}
+
+// ---- incise
+
+// Depth below the outlet by pointer jumping: ptr = land receiver or self, dist = 1 or 0.
+__global__ void k_depth_init(const uint8_t* __restrict__ land, const int32_t* __restrict__ recv, size_t N,
+                             int* __restrict__ ptr, int* __restrict__ dist) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int r = land[i] ? recv[i] : -1;
+        bool up = r >= 0 && land[r];
+        ptr[i] = up ? r : (int)i;
+        dist[i] = up ? 1 : 0;
+    }
+}
+
+// List ranking: a root points at itself with distance 0, so adding its distance changes nothing.
+__global__ void k_depth_jump(const int* __restrict__ ptr, const int* __restrict__ dist, size_t N,
+                             int* __restrict__ ptr2, int* __restrict__ dist2) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int p = ptr[i];
+        dist2[i] = dist[i] + dist[p];
+        ptr2[i] = ptr[p];
+    }
+}
+
+__global__ void k_depth_count(const uint8_t* __restrict__ land, const int* __restrict__ dist, size_t N,
+                              int* __restrict__ count, int* __restrict__ max_depth) {
+    int local = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (!land[i]) continue;
+        int d = dist[i];
+        if (d < 0 || (size_t)d >= N) {   // only a receiver cycle could do this: flag it, write nothing
+            atomicExch(&max_depth[1], 1);
+            continue;
+        }
+        atomicAdd(&count[d], 1);
+        local = max(local, d);
+    }
+    atomicMax(max_depth, local);
+}
+
+__global__ void k_depth_scatter(const uint8_t* __restrict__ land, const int* __restrict__ dist, size_t N,
+                                int max_level, const int* __restrict__ start, int* __restrict__ cursor,
+                                int* __restrict__ bucket) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (!land[i]) continue;
+        int d = dist[i];
+        if (d < 0 || d > max_level) continue;
+        bucket[start[d] + atomicAdd(&cursor[d], 1)] = (int)i;
+    }
+}
+
+struct InciseDev {
+    InciseArgs a;
+    int W;
+    const uint8_t* land;
+    const int32_t* recv;
+    const float* ground;
+    const float* rel;
+    const float* area;
+    const float* erod;
+    float* surface;
+    float* water;
+    const int* start;   // depth buckets, [levels + 1]
+    const int* bucket;
+    int levels;
+};
+
+// HydraulicErosion.baseLevel (HydraulicErosion.kt:2380-2390).
+__device__ __forceinline__ float base_level(const InciseDev& d, int r) {
+    if (!d.land[r]) return d.a.shoreline;
+    float w = d.water[r];
+    if (!isnan(w)) return fmaxf(d.surface[r], w);
+    return d.surface[r];
+}
+
+// One cell of HydraulicErosion.incise (HydraulicErosion.kt:2322-2359).
+__device__ void incise_cell(const InciseDev& d, int cell) {
+    int r = d.recv[cell];
+    bool under = __fsub_rn(d.ground[cell], d.rel[cell]) > d.a.pond_depth;
+    if (r < 0) {
+        if (under) d.water[cell] = __fadd_rn(d.a.shoreline, __fmul_rn(d.ground[cell], d.a.land_range));
+        return;
+    }
+    float base_after = base_level(d, r);
+    if (under) {
+        float filled_level = __fadd_rn(d.a.shoreline, __fmul_rn(d.ground[cell], d.a.land_range));
+        float wr = d.land[r] ? d.water[r] : NAN;
+        float downstream = (d.land[r] && !isnan(wr)) ? wr : base_after;
+        d.water[cell] = fminf(filled_level, downstream);
+    }
+    float height = d.surface[cell];
+    // GroundSteps.between (MA/GroundSteps.kt:45-53).
+    bool same_row = cell / d.W == r / d.W, same_col = cell % d.W == r % d.W;
+    float step = (!same_row && !same_col) ? d.a.step_diag : (!same_row ? d.a.step_ns : 1.0f);
+    float courant = __fdiv_rn(__fmul_rn(__fmul_rn(d.a.courant_coefficient,
+                                                   __fsqrt_rn(__fdiv_rn(d.area[cell], d.a.land_cells))),
+                                        d.erod[cell]),
+                              step);
+    float grades_to = base_after;   // no unresolved relief in this profile
+    bool submerged = under && height <= d.water[cell];
+    float after;
+    if (submerged || (height <= grades_to && d.a.only_above_base)) {
+        after = height;
+    } else {
+        double g = (double)grades_to;
+        after = (float)__dadd_rn(g, __ddiv_rn((double)__fsub_rn(height, grades_to), __dadd_rn(1.0, (double)courant)));
+    }
+    if (after != height) d.surface[cell] = after;
+}
+
+__global__ void __launch_bounds__(256) k_incise_levels(InciseDev d) {
+    cgr::grid_group grid = cgr::this_grid();
+    const int stride = gridDim.x * blockDim.x;
+    for (int level = 0; level < d.levels; ++level) {
+        const int lo = d.start[level], hi = d.start[level + 1];
+        for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) incise_cell(d, d.bucket[i]);
+        grid.sync();
+    }
+}
+
+__global__ void k_water_init(float* __restrict__ water, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        water[i] = NAN;
+}
+
+// ---- spillways
+
+__device__ __forceinline__ unsigned ordered_key(float f) {
+    if (f == 0.0f) f = 0.0f;   // -0 and +0 compare equal in the reference
+    unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered_key(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__global__ void k_ponded(const uint8_t* __restrict__ land, const float* __restrict__ filled,
+                         const float* __restrict__ rel, float pond, size_t N, uint8_t* __restrict__ ponded) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        ponded[i] = land[i] && __fsub_rn(filled[i], rel[i]) > pond;
+}
+
+struct BasinDev {
+    int* cells;
+    unsigned* floor_key;
+    unsigned long long* spill_key;
+};
+
+__global__ void k_basin_init(BasinDev b, int count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    b.cells[i] = 0;
+    b.floor_key[i] = 0xFFFFFFFFu;
+    b.spill_key[i] = 0xFFFFFFFFFFFFFFFFull;
+}
+
+__global__ void k_basin_gather(const int* __restrict__ label, const uint8_t* __restrict__ ponded,
+                               const uint8_t* __restrict__ land, const float* __restrict__ rel,
+                               const float* __restrict__ filled, const int32_t* __restrict__ recv, size_t N,
+                               BasinDev b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int l = label[i];
+        if (l < 0) continue;
+        atomicAdd(&b.cells[l], 1);
+        atomicMin(&b.floor_key[l], ordered_key(rel[i]));
+        int r = recv[i];
+        if (r >= 0 && land[r] && !ponded[r]) {
+            unsigned long long k = ((unsigned long long)ordered_key(filled[r]) << 32) | (unsigned)r;
+            atomicMin(&b.spill_key[l], k);
+        }
+    }
+}
+
+// Per basin: the pour point down the outflow's path, the level and the fill depth
+// (FlowRouting.kt:637-671).
+__global__ void k_basin_finish(BasinDev b, int count, const uint8_t* __restrict__ land,
+                               const float* __restrict__ rel, const float* __restrict__ filled,
+                               const int32_t* __restrict__ recv, long long N, int* __restrict__ entry,
+                               int* __restrict__ spill, float* __restrict__ level, float* __restrict__ floor_out,
+                               float* __restrict__ depth) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float basin_floor = from_ordered_key(b.floor_key[i]);
+    unsigned long long sk = b.spill_key[i];
+    int sp = -1;
+    float spill_level = FLT_MAX;
+    if (sk != 0xFFFFFFFFFFFFFFFFull) {
+        sp = (int)(sk & 0xFFFFFFFFull);
+        spill_level = filled[sp];
+    }
+    int pour = sp;
+    if (sp >= 0) {
+        int cell = sp;
+        long long steps = 0;
+        while (cell >= 0 && land[cell] && filled[cell] > rel[cell] && steps < N) {
+            cell = recv[cell];
+            ++steps;
+        }
+        if (cell >= 0 && land[cell]) pour = cell;
+    }
+    float pour_level = pour >= 0 ? filled[pour] : spill_level;
+    entry[i] = sp;
+    spill[i] = pour;
+    level[i] = pour >= 0 ? pour_level : basin_floor;
+    floor_out[i] = basin_floor;
+    depth[i] = pour >= 0 ? __fsub_rn(pour_level, basin_floor) : 0.0f;
+}
+
+}  // namespace
+
+cg_status tree_walk_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv,
+                        const float* d_weights, long long* d_key, int32_t* d_donors, float* d_area, int* h_levels) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    CG_BUF(int32_t, d_pending, ctx, S_DEPTH, N);
+    CG_BUF(unsigned long long, d_max, ctx, S_STATS, 1);
+    CG_CUDA(ctx, cudaMemsetAsync(d_donors, 0, N * sizeof(int32_t), sm));
+    CG_CUDA(ctx, cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), sm));
+    CG_LAUNCH(ctx) k_donor_count<<<grid, 256, 0, sm>>>(d_land, d_recv, N, d_donors);
+    CG_LAUNCH(ctx) k_pending_init<<<grid, 256, 0, sm>>>(d_donors, N, d_pending);
+    if (d_area) CG_LAUNCH(ctx) k_area_sea<<<grid, 256, 0, sm>>>(d_land, N, d_area);
+    WalkArgs a{W, H, d_land, d_recv, d_donors, d_pending, d_key, d_weights, d_area, d_max};
+    CG_LAUNCH(ctx) k_walk<<<grid, 128, 0, sm>>>(a);
+    CG_CHECK_LAUNCH(ctx);
+    if (h_levels) {
+        unsigned long long mk;
+        CG_CUDA(ctx, cudaMemcpyAsync(&mk, d_max, sizeof(mk), cudaMemcpyDeviceToHost, sm));
+        CG_CUDA(ctx, cudaStreamSynchronize(sm));
+        *h_levels = (int)(mk >> 32) + 1;
+    }
+    return CG_OK;
+}
+
+cg_status order_from_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const long long* d_key,
+                              int land_cells, int32_t* d_order) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    if (land_cells <= 0) return CG_OK;
+    CG_BUF(int, d_flag, ctx, S_SCRATCH0, N);
+    CG_BUF(int, d_pos, ctx, S_SCRATCH1, N);
+    int P2 = 1;
+    while (P2 < land_cells) P2 <<= 1;
+    CG_BUF(long long, d_okeys, ctx, S_BRACKET2, P2);
+    CG_BUF(int, d_ovals, ctx, S_SCRATCH3, P2);
+    CG_LAUNCH(ctx) k_land_flags<<<grid, 256, 0, sm>>>(d_land, N, d_flag);
+    CG_CHECK_LAUNCH(ctx);
+    cg_status st = exclusive_scan(ctx, d_flag, d_pos, (int)N, nullptr);
+    if (st != CG_OK) return st;
+    CG_LAUNCH(ctx) k_land_compact<<<grid, 256, 0, sm>>>(d_land, d_pos, d_key, N, d_okeys, d_ovals);
+    int blocks = (P2 / 2 + 255) / 256;
+    if (blocks > grid) blocks = grid;
+    CG_LAUNCH(ctx) k_pad_kv<<<blocks, 256, 0, sm>>>(d_okeys, d_ovals, land_cells, P2);
+    for (int k = 2; k <= P2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) CG_LAUNCH(ctx) k_bitonic_kv<<<blocks, 256, 0, sm>>>(d_okeys, d_ovals, P2, k, j);
+    CG_CUDA(ctx, cudaMemcpyAsync(d_order, d_ovals, sizeof(int) * land_cells, cudaMemcpyDeviceToDevice, sm));
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const float* d_ground,
+                     const float* d_rel, const float* d_area, const float* d_erod, float* d_surface,
+                     const InciseArgs& args) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    CG_BUF(int, d_ptr, ctx, S_PTR, N);
+    CG_BUF(int, d_ptr2, ctx, S_PTR2, N);
+    CG_BUF(int, d_dist, ctx, S_SCRATCH0, N);
+    CG_BUF(int, d_dist2, ctx, S_SCRATCH1, N);
+    CG_BUF(int, d_bucket, ctx, S_SCRATCH2, N);
+    CG_BUF(float, d_water, ctx, S_WATER, N);
+    CG_BUF(int, d_small, ctx, S_LEVELCNT, 4);
+    CG_LAUNCH(ctx) k_depth_init<<<grid, 256, 0, sm>>>(d_land, d_recv, N, d_ptr, d_dist);
+    int jumps = 1;
+    while (((size_t)1 << jumps) < N) ++jumps;
+    int* p = d_ptr;
+    int* p2 = d_ptr2;
+    int* di = d_dist;
+    int* di2 = d_dist2;
+    for (int j = 0; j < jumps; ++j) {
+        CG_LAUNCH(ctx) k_depth_jump<<<grid, 256, 0, sm>>>(p, di, N, p2, di2);
+        int* t = p;
+        p = p2;
+        p2 = t;
+        t = di;
+        di = di2;
+        di2 = t;
+    }
+    CG_CUDA(ctx, cudaMemsetAsync(d_small, 0, 4 * sizeof(int), sm));
+    // Depth histogram: depths are below N; bound the count array by the maximum depth first.
+    CG_BUF(int, d_cnt, ctx, S_DEPTH, N + 2);
+    CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, (N + 2) * sizeof(int), sm));
+    CG_LAUNCH(ctx) k_depth_count<<<grid, 256, 0, sm>>>(d_land, di, N, d_cnt, d_small);
+    CG_CHECK_LAUNCH(ctx);
+    int depth_info[2] = {0, 0};
+    CG_CUDA(ctx, cudaMemcpyAsync(depth_info, d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    if (depth_info[1]) return fail(ctx, CG_BAD_ARG, "receivers do not form a forest (a cycle)");
+    int max_depth = depth_info[0];
+    int levels = max_depth + 1;
+    CG_BUF(int, d_start, ctx, S_CG2, 2 * (size_t)levels + 2);
+    int* d_cursor = d_start + levels + 1;
+    int total = 0;
+    cg_status st = exclusive_scan(ctx, d_cnt, d_start, levels, &total);
+    if (st != CG_OK) return st;
+    CG_CUDA(ctx, cudaMemcpyAsync(d_start + levels, &total, sizeof(int), cudaMemcpyHostToDevice, sm));
+    CG_CUDA(ctx, cudaMemsetAsync(d_cursor, 0, (levels + 1) * sizeof(int), sm));
+    CG_LAUNCH(ctx) k_depth_scatter<<<grid, 256, 0, sm>>>(d_land, di, N, max_depth, d_start, d_cursor, d_bucket);
+    CG_LAUNCH(ctx) k_water_init<<<grid, 256, 0, sm>>>(d_water, N);
+    CG_CHECK_LAUNCH(ctx);
+    InciseDev d;
+    d.a = args;
+    d.W = W;
+    d.land = d_land;
+    d.recv = d_recv;
+    d.ground = d_ground;
+    d.rel = d_rel;
+    d.area = d_area;
+    d.erod = d_erod;
+    d.surface = d_surface;
+    d.water = d_water;
+    d.start = d_start;
+    d.bucket = d_bucket;
+    d.levels = levels;
+    int per_sm = 0;
+    CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_incise_levels, 256, 0));
+    if (per_sm < 1) return fail(ctx, CG_CUDA, "incise kernel cannot be resident");
+    int cgrid = ctx->num_sms * (per_sm < 4 ? per_sm : 4);
+    void* kargs[] = {&d};
+    CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_incise_levels, cgrid, 256, kargs, 0, sm));
+    return CG_OK;
+}
+
+cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
+                        const int32_t* d_recv, float pond_depth, int32_t* d_label, cg_basins* hb) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    CG_BUF(uint8_t, d_ponded, ctx, S_FLATS, N);
+    CG_BUF(int, d_root, ctx, S_LABEL, N);
+    CG_LAUNCH(ctx) k_ponded<<<grid, 256, 0, sm>>>(d_land, d_filled, d_rel, pond_depth, N, d_ponded);
+    CG_CHECK_LAUNCH(ctx);
+    int count = 0;
+    cg_status st = component_labels(ctx, W, H, d_ponded, d_root, d_label, &count);
+    if (st != CG_OK) return st;
+    if (hb) {
+        hb->count = count;
+        hb->largest = -1;
+        hb->largest_cells = 0;
+        hb->largest_depth = 0.0f;
+        hb->deepest = 0.0f;
+    }
+    if (count == 0 || !hb) return sync(ctx);
+    // One block: spill keys (8 bytes each) first for alignment, then seven 4-byte arrays.
+    CG_BUF(unsigned long long, d_b, ctx, S_BASIN, (size_t)count * 5 + 8);
+    BasinDev b;
+    b.spill_key = d_b;
+    b.cells = (int*)(d_b + count);
+    b.floor_key = (unsigned*)(b.cells + count);
+    int* d_entry = (int*)(b.floor_key + count);
+    int* d_spill = d_entry + count;
+    float* d_level = (float*)(d_spill + count);
+    float* d_floor = d_level + count;
+    float* d_depth = d_floor + count;
+    CG_LAUNCH(ctx) k_basin_init<<<(count + 255) / 256, 256, 0, sm>>>(b, count);
+    CG_LAUNCH(ctx) k_basin_gather<<<grid, 256, 0, sm>>>(d_label, d_ponded, d_land, d_rel, d_filled, d_recv, N, b);
+    CG_LAUNCH(ctx) k_basin_finish<<<(count + 255) / 256, 256, 0, sm>>>(b, count, d_land, d_rel, d_filled, d_recv, (long long)N,
+                                                        d_entry, d_spill, d_level, d_floor, d_depth);
+    CG_CHECK_LAUNCH(ctx);
+    std::vector<int> cells(count), entry(count), spill(count);
+    std::vector<float> level(count), flo(count), depth(count);
+    CG_CUDA(ctx, cudaMemcpyAsync(cells.data(), b.cells, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(entry.data(), d_entry, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(spill.data(), d_spill, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(level.data(), d_level, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(flo.data(), d_floor, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(depth.data(), d_depth, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    // The running largest / deepest of FlowRouting.kt:664-670, in basin order.
+    int largest = -1, largest_cells = 0;
+    float largest_depth = 0.0f, deepest = 0.0f;
+    for (int i = 0; i < count; ++i) {
+        if (cells[i] > largest_cells) {
+            largest = i;
+            largest_cells = cells[i];
+            largest_depth = depth[i];
+        }
+        if (depth[i] > deepest) deepest = depth[i];
+    }
+    hb->largest = largest;
+    hb->largest_cells = largest_cells;
+    hb->largest_depth = largest_depth;
+    hb->deepest = deepest;
+    int n = count < hb->capacity ? count : hb->capacity;
+    for (int i = 0; i < n; ++i) {
+        if (hb->spill) hb->spill[i] = spill[i];
+        if (hb->entry) hb->entry[i] = entry[i];
+        if (hb->level) hb->level[i] = level[i];
+        if (hb->floor) hb->floor[i] = flo[i];
+        if (hb->cells) hb->cells[i] = cells[i];
+    }
+    return CG_OK;
+}
+
+}  // namespace cg

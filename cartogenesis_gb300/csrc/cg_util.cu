@@ -80,10 +80,20 @@ __global__ void k_cc_union(const uint8_t* __restrict__ mask, int* __restrict__ p
     }
 }
 
+// Point every cell straight at its root. Read-only walks: the only writes are true roots, so a
+// concurrent walk through a cell sees either its old ancestor or its root, both on the way up.
+// (Path halving here would race: a halving write could replace a root just written with an
+// intermediate ancestor.)
 __global__ void k_cc_flatten(int* __restrict__ parent, size_t N) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (parent[i] < 0) continue;
-        parent[i] = find_root(parent, (int)i);
+        int p = parent[i];
+        if (p < 0) continue;
+        int a = (int)i;
+        while (p != a) {
+            a = p;
+            p = parent[a];
+        }
+        parent[i] = a;
     }
 }
 
@@ -118,15 +128,15 @@ cg_status exclusive_scan(cg_ctx* ctx, const int* d_in, int* d_out, int n, int* h
     int* d_sums2 = d_offs1 + blocks;      // [blocks2]
     int* d_offs2 = d_sums2 + blocks2;     // [blocks2]
     int* d_total = d_offs2 + blocks2;     // [1]
-    k_scan_blocks<<<blocks, SCAN_BLOCK, 0, ctx->stream>>>(d_in, d_out, d_sums1, n);
+    CG_LAUNCH(ctx) k_scan_blocks<<<blocks, SCAN_BLOCK, 0, ctx->stream>>>(d_in, d_out, d_sums1, n);
     CG_CHECK_LAUNCH(ctx);
     if (blocks > 1) {
-        k_scan_blocks<<<blocks2, SCAN_BLOCK, 0, ctx->stream>>>(d_sums1, d_offs1, d_sums2, blocks);
+        CG_LAUNCH(ctx) k_scan_blocks<<<blocks2, SCAN_BLOCK, 0, ctx->stream>>>(d_sums1, d_offs1, d_sums2, blocks);
         if (blocks2 > 1) {
-            k_scan_blocks<<<1, SCAN_BLOCK, 0, ctx->stream>>>(d_sums2, d_offs2, d_total, blocks2);
-            k_scan_add<<<blocks2, SCAN_BLOCK, 0, ctx->stream>>>(d_offs1, d_offs2, blocks);
+            CG_LAUNCH(ctx) k_scan_blocks<<<1, SCAN_BLOCK, 0, ctx->stream>>>(d_sums2, d_offs2, d_total, blocks2);
+            CG_LAUNCH(ctx) k_scan_add<<<blocks2, SCAN_BLOCK, 0, ctx->stream>>>(d_offs1, d_offs2, blocks);
         }
-        k_scan_add<<<blocks, SCAN_BLOCK, 0, ctx->stream>>>(d_out, d_offs1, n);
+        CG_LAUNCH(ctx) k_scan_add<<<blocks, SCAN_BLOCK, 0, ctx->stream>>>(d_out, d_offs1, n);
         CG_CHECK_LAUNCH(ctx);
     }
     if (h_total) {
@@ -143,18 +153,18 @@ cg_status component_labels(cg_ctx* ctx, int W, int H, const uint8_t* d_mask, int
                            int* h_count) {
     size_t N = (size_t)W * H;
     int grid = ctx->num_sms * 8;
-    k_cc_init<<<grid, 256, 0, ctx->stream>>>(d_mask, d_root, N);
-    k_cc_union<<<grid, 256, 0, ctx->stream>>>(d_mask, d_root, W, H);
-    k_cc_flatten<<<grid, 256, 0, ctx->stream>>>(d_root, N);
+    CG_LAUNCH(ctx) k_cc_init<<<grid, 256, 0, ctx->stream>>>(d_mask, d_root, N);
+    CG_LAUNCH(ctx) k_cc_union<<<grid, 256, 0, ctx->stream>>>(d_mask, d_root, W, H);
+    CG_LAUNCH(ctx) k_cc_flatten<<<grid, 256, 0, ctx->stream>>>(d_root, N);
     CG_CHECK_LAUNCH(ctx);
     if (d_label) {
         CG_BUF(int, d_flag, ctx, S_SCRATCH0, N);
         CG_BUF(int, d_rank, ctx, S_SCRATCH1, N);
-        k_root_flags<<<grid, 256, 0, ctx->stream>>>(d_root, d_flag, N);
+        CG_LAUNCH(ctx) k_root_flags<<<grid, 256, 0, ctx->stream>>>(d_root, d_flag, N);
         CG_CHECK_LAUNCH(ctx);
         cg_status st = exclusive_scan(ctx, d_flag, d_rank, (int)N, h_count);
         if (st != CG_OK) return st;
-        k_label_from_root<<<grid, 256, 0, ctx->stream>>>(d_root, d_rank, d_label, N);
+        CG_LAUNCH(ctx) k_label_from_root<<<grid, 256, 0, ctx->stream>>>(d_root, d_rank, d_label, N);
         CG_CHECK_LAUNCH(ctx);
     }
     return CG_OK;

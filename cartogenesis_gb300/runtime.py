@@ -11,7 +11,8 @@ LIB_PATH = os.path.join(HERE, "libcg_erosion.so")
 # Every symbol include/cg_erosion.h declares; the CPU tests check the library exports them all.
 EXPORTS = [
     "cg_default_params", "cg_thermal_limits_for", "cg_create", "cg_destroy", "cg_cancel", "cg_last_error",
-    "cg_thermal_sweeps", "cg_erode_stage", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
+    "cg_stream", "cg_kernel_launches",
+    "cg_thermal_sweeps", "cg_erode_stage", "cg_erode_stage_dev", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways",
 ]
 
@@ -47,9 +48,14 @@ def load_library(path=LIB_PATH):
         L.cg_cancel.restype = None
         L.cg_last_error.argtypes = [vp]
         L.cg_last_error.restype = C.c_char_p
+        L.cg_stream.argtypes = [vp]
+        L.cg_stream.restype = vp
+        L.cg_kernel_launches.argtypes = [vp]
+        L.cg_kernel_launches.restype = i64
         L.cg_thermal_sweeps.argtypes = [vp, i32, i32, vp, vp, abi.ThermalLimits, i32, f32]
         if hasattr(L, "cg_erode_stage"):
             L.cg_erode_stage.argtypes = [vp, PP, C.POINTER(abi.Inputs), C.POINTER(abi.Outputs), vp]
+            L.cg_erode_stage_dev.argtypes = [vp, PP, C.POINTER(abi.Inputs), vp, vp, C.POINTER(i32)]
             L.cg_percentile_cut.argtypes = [vp, i32, i32, vp, f32, f32, f32, f32, C.POINTER(f32), vp, vp,
                                             C.POINTER(i32)]
             L.cg_fill_depressions.argtypes = [vp, i32, i32, vp, vp, vp, C.POINTER(i64), C.POINTER(i64)]
@@ -83,6 +89,15 @@ class Context:
 
     def cancel(self):
         self.lib.cg_cancel(self.handle)
+
+    @property
+    def stream(self):
+        """The cudaStream_t (as an int) every kernel of this context runs on."""
+        return self.lib.cg_stream(self.handle)
+
+    @property
+    def kernel_launches(self):
+        return self.lib.cg_kernel_launches(self.handle)
 
     def close(self):
         if self.handle:

@@ -145,7 +145,14 @@ typedef struct cg_round_stats {
     int32_t levels;             /* drainage levels (longest donor chain + 1) */
     int64_t fill_ties;          /* cells whose fill parent was decided on a quantised-key tie */
     int64_t fill_unresolved;    /* of those, ties the fill could not order exactly (expected 0) */
-    double  ms_total;           /* device time of the round, milliseconds */
+    int64_t kernel_launches;    /* kernels this library launched for the round */
+    double  ms_total;           /* device time of the round, milliseconds (CUDA events) */
+    double  ms_cut;             /* uplift, percentile cut and weights */
+    double  ms_fill;            /* fillDepressions */
+    double  ms_route;           /* flat potentials and receivers */
+    double  ms_tree;            /* donor counts, drainage keys and accumulation */
+    double  ms_incise;          /* the implicit incision */
+    double  ms_relax;           /* the round's thermal sweeps */
 } cg_round_stats;
 
 typedef struct cg_ctx cg_ctx;
@@ -163,6 +170,14 @@ void      cg_destroy(cg_ctx* ctx);
 void      cg_cancel(cg_ctx* ctx);
 /* The message of the last failure on this context (static storage, never NULL). */
 const char* cg_last_error(const cg_ctx* ctx);
+/*
+ * The CUDA stream every kernel of this context runs on (a cudaStream_t), for callers that time the
+ * stage with events on the launching stream or order their own work after it. No counterpart in the
+ * reference.
+ */
+void*     cg_stream(const cg_ctx* ctx);
+/* Kernels this context has launched since it was created. No counterpart in the reference. */
+int64_t   cg_kernel_launches(const cg_ctx* ctx);
 
 /*
  * ErosionAccelerator.erode (.../pipeline/ErosionAccelerator.kt:38-45; ErosionStage.kt:235-403):
@@ -179,6 +194,17 @@ cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t width, int32_t height, const fl
  */
 cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs,
                          cg_outputs* outputs, cg_round_stats* stats);
+
+/*
+ * cg_erode_stage on a world already resident on this context's device: every pointer of `inputs_dev`
+ * is device memory (read only), and `height_out_dev` (device, N floats, may alias nothing in the
+ * inputs) receives the result. No host<->device copy of the fields; the caller's stream is not
+ * used, the call returns when the stage is done. Returns the last round's land-cell count in
+ * *land_cells (may be NULL). No counterpart in the reference, which has no device-resident world;
+ * it is the same stage as cg_erode_stage for callers that keep the world in HBM.
+ */
+cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs_dev,
+                             float* height_out_dev, cg_round_stats* stats, int32_t* land_cells);
 
 /* ---- The stage's routing functions, each run alone on host buffers (FlowRouting, SeaLevelStage) ---- */
 

@@ -17,7 +17,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "cg_oracle.cpp")]
 # -ffp-contract=off: the JVM never fuses a multiply and an add, and neither may the restatement.
-CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
+CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared", "-Wall"]
 
 
 def build(force=False):

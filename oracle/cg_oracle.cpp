@@ -148,6 +148,8 @@ void thermal_sweep(int W, int H, const float* in, float* out, cg_thermal_limits 
 
     for (int s = 0; s < sweeps; ++s) {
         const float* cur = heights.data();
+        // parallelChunks over tile rows (ErosionStage.kt:292): cells are independent within a pass.
+#pragma omp parallel for schedule(dynamic)
         for (int tr = 0; tr < td; ++tr)
             for (int tc = 0; tc < ta; ++tc) {
                 int tile = tr * ta + tc;
@@ -182,6 +184,7 @@ void thermal_sweep(int W, int H, const float* in, float* out, cg_thermal_limits 
         can_change = dilate(has_excess, ta, td);
         can_hold = dilate(can_change, ta, td);
         float* wr = next.data();
+#pragma omp parallel for schedule(dynamic)
         for (int tr = 0; tr < td; ++tr)
             for (int tc = 0; tc < ta; ++tc) {
                 int tile = tr * ta + tc;

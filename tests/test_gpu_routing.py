@@ -1,0 +1,132 @@
+"""Each routing function of the round on the GPU against the oracle, on the same inputs.
+
+Integer outputs (masks, receivers, orders, donor counts, basin labels and outlets) must be
+identical; float fields must be identical bit for bit (the REF32 mode reproduces the reference's
+float arithmetic). The one documented exception is the flats' potential surface, an intermediate
+the receivers are read from: its conjugate-gradient dot products are block reductions where the
+reference sums sequentially, so it may differ in its last bits (tolerance 1e-12 relative, written
+below); the receivers read from it must still be identical.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cartogenesis_gb300 import FlowRouting, SeaLevelStage, synthetic
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(64, 32, 11), (128, 64, 3), (256, 128, 42), (512, 256, 7)]
+SURFACE_RTOL = 1e-12
+
+
+def bits(a):
+    return a.view(np.uint32) if a.dtype == np.float32 else a.view(np.uint64)
+
+
+def world_cut(W, H, seed, sea_level=0.70, lowstand=0.0):
+    h, up, rk = synthetic.world(W, H, seed)
+    return h, oracle.percentile_cut(h, sea_level, lowstand)
+
+
+@pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
+@pytest.mark.parametrize("sea_level,lowstand", [(0.70, 0.0), (0.71, 0.0075), (0.30, 0.0025)])
+def test_percentile_cut(W, H, seed, sea_level, lowstand):
+    h, _, _ = synthetic.world(W, H, seed)
+    s0, l0, r0, n0 = oracle.percentile_cut(h, sea_level, lowstand)
+    s1, l1, r1, n1 = SeaLevelStage.percentile_cut(h, sea_level, lowstand)
+    assert np.float32(s0).view(np.uint32) == np.float32(s1).view(np.uint32)
+    assert n0 == n1
+    assert np.array_equal(l0, l1)
+    assert np.array_equal(bits(r0), bits(r1))
+
+
+def test_percentile_cut_edges():
+    """A flat field (the answer is its height), a field of two levels with ties in the bracket,
+    and sea levels 0 and 1."""
+    for h in (np.full((16, 32), 0.4, np.float32),
+              np.where(np.arange(16 * 32).reshape(16, 32) % 3 == 0, 0.2, 0.7).astype(np.float32)):
+        for sl in (0.0, 0.5, 1.0):
+            s0, l0, r0, n0 = oracle.percentile_cut(h, sl)
+            s1, l1, r1, n1 = SeaLevelStage.percentile_cut(h, sl)
+            assert (s0, n0) == (s1, n1) and np.array_equal(l0, l1) and np.array_equal(bits(r0), bits(r1))
+
+
+@pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
+def test_fill_depressions(W, H, seed):
+    _, (s, land, rel, n) = world_cut(W, H, seed)
+    want = oracle.fill_depressions(land, rel)
+    got, ties, unresolved = FlowRouting.fill_depressions(land, rel, with_ties=True)
+    diff = np.flatnonzero(bits(got) != bits(want))
+    assert diff.size == 0, f"{diff.size} cells differ (ties {ties}, unresolved {unresolved}): {diff[:8]}"
+    assert unresolved == 0
+
+
+def test_fill_depression_fixture():
+    """T/DepressionFillTest.kt's 32x32 grid: the device fill equals the oracle's bit for bit."""
+    land = np.zeros((32, 32), np.uint8)
+    elev = np.full((32, 32), np.float32(-0.1), np.float32)
+    land[12:20, 12:20] = 1
+    elev[12:20, 12:20] = np.float32(-0.2)
+    land[3:8, 3:8] = 1
+    elev[3:8, 3:8] = np.float32(0.05)
+    elev[5, 5] = np.float32(0.01)
+    assert np.array_equal(bits(FlowRouting.fill_depressions(land, elev)), bits(oracle.fill_depressions(land, elev)))
+
+
+def test_fill_flat_plateaus_with_ties():
+    """Tie-heavy ground: broad exactly-flat basins and terraces whose heights share a quantised key."""
+    rng = np.random.default_rng(4)
+    W, H = 128, 64
+    g = np.round(rng.uniform(0.0, 0.02, (H, W)) * 2000) / 2000
+    g = g.astype(np.float32)
+    g[10:30, 20:60] = np.float32(0.001)
+    g[40:50, 70:120] = np.float32(0.0105)
+    land = np.ones((H, W), np.uint8)
+    land[:, :4] = 0
+    rel = np.where(land == 1, g, np.float32(-0.05)).astype(np.float32)
+    want = oracle.fill_depressions(land, rel)
+    got, ties, unresolved = FlowRouting.fill_depressions(land, rel, with_ties=True)
+    assert unresolved == 0
+    assert np.array_equal(bits(got), bits(want)), np.flatnonzero(bits(got) != bits(want))[:8]
+
+
+@pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
+@pytest.mark.parametrize("by_facet,over_potential", [(True, True), (True, False), (False, False)])
+def test_flow_directions(W, H, seed, by_facet, over_potential):
+    _, (s, land, rel, n) = world_cut(W, H, seed)
+    filled = oracle.fill_depressions(land, rel)
+    r = 0.5 if W == 2 * H else 1.0
+    want, wsurf, wc = oracle.flow_directions(land, rel, filled, seed, r, 214, by_facet, over_potential,
+                                             want_surface=True)
+    got, gsurf, gc = FlowRouting.flow_directions(land, rel, filled, seed, r, 214, by_facet, over_potential,
+                                                 want_surface=True)
+    assert list(wc) == list(gc)
+    np.testing.assert_allclose(gsurf, wsurf, rtol=SURFACE_RTOL, atol=0)
+    diff = np.flatnonzero(got != want)
+    assert diff.size == 0, f"{diff.size} receivers differ: {diff[:8]}"
+
+
+@pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
+def test_drainage_order_accumulate_spillways(W, H, seed):
+    _, (s, land, rel, n) = world_cut(W, H, seed)
+    filled = oracle.fill_depressions(land, rel)
+    rec, _ = oracle.flow_directions(land, rel, filled, seed, 0.5, 214)
+    assert np.array_equal(FlowRouting.drainage_order(land, rec, n), oracle.drainage_order(land, rec, n))
+    # Uneven weights make the float sums order-sensitive.
+    w = np.random.default_rng(seed).uniform(0.3, 3.0, (H, W)).astype(np.float32)
+    a_want = oracle.accumulate(land, rec, n, w)
+    a_got = FlowRouting.accumulate(land, rec, n, w)
+    assert np.array_equal(bits(a_got), bits(a_want))
+    pond = np.float32(24.0) / np.float32(6000.0)
+    sw_want = oracle.spillways(land, rel, filled, rec, pond)
+    sw_got = FlowRouting.spillways(land, rel, filled, rec, pond)
+    assert sw_got["count"] == sw_want["count"]
+    if W >= 512:
+        assert sw_want["count"] > 0   # the larger worlds hold basins deeper than the pond depth
+    assert np.array_equal(sw_got["labels"], sw_want["labels"])
+    for k in ("spill", "entry", "cells"):
+        assert np.array_equal(sw_got[k], sw_want[k]), k
+    for k in ("level", "floor"):
+        assert np.array_equal(bits(sw_got[k]), bits(sw_want[k])), k
+    for k in ("largest", "largest_cells", "largest_depth", "deepest"):
+        assert sw_got[k] == sw_want[k], k
