@@ -43,7 +43,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=8192)
     ap.add_argument("--height", type=int, default=4096)
-    ap.add_argument("--cpu-sample", type=int, default=1024, help="width of the CPU baseline's sample world")
+    ap.add_argument("--cpu-sample", type=int, default=2048,
+                    help="width of the CPU baseline's sample world (2048: the 2048x1024 grid of the reference's "
+                         "CPU-runnable configuration); 0 skips the CPU leg")
     return ap.parse_args()
 
 
@@ -262,7 +264,7 @@ def run_ours(args):
         "phases_ms_per_step": {k: round(v, 2) for k, v in phase.items()},
         "rounds": per_round,
     }
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_sample > 0:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
         v, t, cores, sample = cpu_baseline(args.cpu_sample, 1, int(os.environ["OMP_NUM_THREADS"]))
         line["cpu_baseline"] = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
