@@ -9,6 +9,15 @@ namespace cg {
 cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, cg_thermal_limits lim, int passes,
                              float rate, float** result);
 int thermal_launches(int passes);
+struct ThermalLaunch {
+    float limit[8];
+    float settled;
+    float rate;
+};
+ThermalLaunch thermal_launch_args(cg_thermal_limits lim, float rate);
+// One fused launch of k sweeps (k in {1, 2, 4, 8}) from src into dst.
+cudaError_t thermal_launch(const float* src, float* dst, int W, int H, const ThermalLaunch& t, int k,
+                           cudaStream_t stream);
 
 // ---- sea-level cut (cg_cut.cu)
 // Row weights of SeaLevelStage.shorelineForFraction and their sequential total, computed once per

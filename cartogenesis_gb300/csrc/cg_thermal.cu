@@ -152,6 +152,30 @@ cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs&
 
 }  // namespace
 
+ThermalLaunch thermal_launch_args(cg_thermal_limits lim, float rate) {
+    ThermalLaunch t;
+    for (int n = 0; n < 8; ++n)
+        t.limit[n] = n >= 4 ? lim.diagonal : (thermal_row_step(n) != 0 ? lim.north_south : lim.east_west);
+    t.settled = lim.east_west * 1e-3f;   // SETTLED_SHARE_OF_CRITICAL_SLOPE (ErosionStage.kt:92)
+    t.rate = rate;
+    return t;
+}
+
+// One fused launch of k sweeps (k in {1, 2, 4, 8}) from src into dst on `stream`.
+cudaError_t thermal_launch(const float* src, float* dst, int W, int H, const ThermalLaunch& t, int k,
+                           cudaStream_t stream) {
+    ThermalArgs a;
+    for (int n = 0; n < 8; ++n) a.limit[n] = t.limit[n];
+    a.settled = t.settled;
+    a.rate = t.rate;
+    switch (k) {
+        case 8: return launch<8>(src, dst, W, H, a, stream);
+        case 4: return launch<4>(src, dst, W, H, a, stream);
+        case 2: return launch<2>(src, dst, W, H, a, stream);
+        default: return launch<1>(src, dst, W, H, a, stream);
+    }
+}
+
 int thermal_launches(int passes) {
     int n = 0;
     while (passes >= 8) passes -= 8, ++n;

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libcg_erosion.so")
 EXPORTS = [
     "cg_default_params", "cg_thermal_limits_for", "cg_create", "cg_destroy", "cg_cancel", "cg_last_error",
     "cg_stream", "cg_kernel_launches",
-    "cg_thermal_sweeps", "cg_erode_stage", "cg_erode_stage_dev", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
+    "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways",
 ]
 
@@ -53,6 +53,7 @@ def load_library(path=LIB_PATH):
         L.cg_kernel_launches.argtypes = [vp]
         L.cg_kernel_launches.restype = i64
         L.cg_thermal_sweeps.argtypes = [vp, i32, i32, vp, vp, abi.ThermalLimits, i32, f32]
+        L.cg_thermal_sweeps_noalloc.argtypes = [vp, vp, i32, i32, abi.ThermalLimits, i32, f32, vp]
         if hasattr(L, "cg_erode_stage"):
             L.cg_erode_stage.argtypes = [vp, PP, C.POINTER(abi.Inputs), C.POINTER(abi.Outputs), vp]
             L.cg_erode_stage_dev.argtypes = [vp, PP, C.POINTER(abi.Inputs), vp, vp, C.POINTER(i32)]

@@ -187,6 +187,23 @@ cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t width, int32_t height, const fl
                             float* heights_out, cg_thermal_limits limits, int32_t passes, float rate);
 
 /*
+ * cg_thermal_sweeps for callers that cannot allocate device memory. No counterpart in the
+ * reference. Some callers must not call cudaMalloc: a JVM inside a memory-accounted container
+ * lending buffers it owns, a renderer that owns every allocation on its device, code replaying a
+ * graph captured elsewhere. This entry point needs no context and allocates nothing: the caller
+ * passes the input and output as device pointers (different buffers; the input is not written),
+ * and the one scratch field lives in a file-scope device array sized for grids of up to 2^20 cells
+ * (4 MiB, held by every GPU that loads the library until exit). Larger grids, a non-power-of-two
+ * side, aliased buffers or negative passes return CG_BAD_ARG. The first call on a device looks up
+ * the array's address with that device current, so make it before any stream capture. Calls share
+ * the array: calls whose work overlaps on the GPU race. `stream` is a cudaStream_t or NULL; the
+ * call returns when the work is queued.
+ */
+cg_status cg_thermal_sweeps_noalloc(const float* heights_in_dev, float* heights_out_dev, int32_t width,
+                                    int32_t height, cg_thermal_limits limits, int32_t passes, float rate,
+                                    void* stream);
+
+/*
  * ErosionStage.apply (.../pipeline/ErosionStage.kt:133-183) with HydraulicErosion.apply
  * (.../pipeline/HydraulicErosion.kt:596-1506): the initial thermal sweeps, then the hydraulic
  * rounds, each relaxed by sweepsFor/rounds sweeps. `stats`, if not NULL, receives one entry per
