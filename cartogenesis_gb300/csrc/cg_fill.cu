@@ -14,9 +14,14 @@
 //      republished (the monotone Bellman-Ford of a Dijkstra with non-decreasing edge functions);
 //  (3) a check pass finds cells whose least-Q neighbours share a key but would give different
 //      levels. The reference takes the one popped first: among neighbours that entered that key's
-//      level from below, the lowest index. Such a cell is repaired with that neighbour and the
-//      fixed point recomputed around it. A tie whose candidates were themselves reached inside the
-//      level (flat ground within one key quantum) is counted as unresolved and reported.
+//      level from below, the lowest index. Such a cell is pinned to that neighbour. A tie whose
+//      candidates were themselves reached inside the level (flat ground within one key quantum)
+//      needs the level's own pop order: the lowest such level is replayed exactly, one thread
+//      running the reference's heap over that level's cells (those that entered from below seed it;
+//      lower levels are final by then), and every cell it reaches is pinned to its exact parent.
+//      The levels from the lowest changed one upward are recomputed, and the check repeats; each
+//      replay settles its level for good, so the lowest open level only rises. A level too large
+//      to replay (over 2^18 cells) is reported as unresolved.
 #include <cfloat>
 #include <climits>
 #include <vector>
@@ -32,8 +37,11 @@ constexpr float kStep = 1e-6f;   // FlowRouting.FLAT_GRADIENT_STEP
 constexpr int T = 32;            // tile side
 constexpr int TH = 8;            // tile rows per thread pass (block is 32 x 8)
 
-// Cell classes.
-enum : uint8_t { C_WATER = 0, C_SEED = 1, C_DRAINED = 2, C_OPEN = 3, C_PINNED = 4 };
+// Cell classes. PINNED: parent fixed by the index rule on a key tie; EXACT: parent fixed by
+// replaying its key level's pops (both follow that parent instead of the minimum).
+enum : uint8_t { C_WATER = 0, C_SEED = 1, C_DRAINED = 2, C_OPEN = 3, C_PINNED = 4, C_EXACT = 5 };
+
+__device__ __forceinline__ bool follows_parent(uint8_t c) { return c == C_PINNED || c == C_EXACT; }
 
 __device__ __forceinline__ int qkey(float f) { return __float_as_int(__fadd_rn(f, 4.0f)); }   // FlowRouting.encode
 __device__ __forceinline__ float phi(float fp, float g) { return g > fp ? g : __fadd_rn(fp, kStep); }
@@ -42,6 +50,9 @@ struct FillCounters {
     unsigned long long ties, unresolved, repaired;
     int active;
     int changed;
+    int min_level;      // the lowest key level holding a tie only its own pops can order
+    int overflow;       // that level was too large to replay
+    int repair_level;   // the lowest key level at which a pin changed a cell's level
 };
 
 // (0) classes and initial levels.
@@ -141,7 +152,7 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
         bool changed = false;
         for (int yy = ly; yy < T; yy += TH) {
             uint8_t c = sc[yy][lx];
-            if (c != C_OPEN && c != C_PINNED) continue;
+            if (c != C_OPEN && !follows_parent(c)) continue;
             int gy = ty0 + yy;
             float gn = sg[yy][lx];
             float best = sf[yy + 1][lx + 1];
@@ -184,7 +195,7 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
         int gy = ty0 + yy, gx = tx0 + lx;
         if (gy >= H || gx >= W) continue;
         uint8_t c = sc[yy][lx];
-        if (c != C_OPEN && c != C_PINNED) continue;
+        if (c != C_OPEN && !follows_parent(c)) continue;
         float v = sf[yy + 1][lx + 1];
         size_t idx = (size_t)gy * W + gx;
         if (f[idx] != v) {
@@ -213,15 +224,18 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
     }
 }
 
-// A tile is active for the first pass if it holds any OPEN cell.
-__global__ void k_tiles_with_open(const uint8_t* __restrict__ cls, int W, int H, int tiles_x, int tiles_y,
-                                  uint8_t* __restrict__ act) {
+// A tile is active for the first pass if it holds a cell still to settle (a level reset to +inf).
+__global__ void k_tiles_with_open(const uint8_t* __restrict__ cls, const float* __restrict__ f, int W, int H,
+                                  int tiles_x, int tiles_y, uint8_t* __restrict__ act) {
     int tile = blockIdx.x;
     const int ty0 = (tile / tiles_x) * T, tx0 = (tile % tiles_x) * T;
     int has = 0;
     for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
         int gy = ty0 + i / T, gx = tx0 + i % T;
-        if (gy < H && gx < W && cls[(size_t)gy * W + gx] >= C_OPEN) has = 1;
+        if (gy < H && gx < W) {
+            size_t c = (size_t)gy * W + gx;
+            if (cls[c] >= C_OPEN && isinf(f[c])) has = 1;
+        }
     }
     has = __syncthreads_or(has);
     if (threadIdx.x == 0) act[tile] = has ? 1 : 0;
@@ -236,7 +250,7 @@ __global__ void k_check_ties(const float* __restrict__ f, const float* __restric
     size_t N = (size_t)W * H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         uint8_t c = cls[i];
-        if (c != C_OPEN && c != C_PINNED) continue;
+        if (c != C_OPEN && c != C_PINNED) continue;   // EXACT cells were ordered by replaying their level
         int row = (int)(i / W), col = (int)(i - (size_t)row * W);
         float gn = g[i];
         int qmin = INT_MAX;
@@ -268,7 +282,7 @@ __global__ void k_check_ties(const float* __restrict__ f, const float* __restric
                 // Reached inside its own key level: an unraised land cell whose least-Q neighbour
                 // shares its key. Water and the polar outlets are in the heap from the start.
                 uint8_t cm = cls[n];
-                if ((cm == C_OPEN || cm == C_PINNED || cm == C_DRAINED) && fm == g[n]) {
+                if ((cm == C_OPEN || follows_parent(cm) || cm == C_DRAINED) && fm == g[n]) {
                     int mr = n / W, mc = n % W, mq = INT_MAX;
                     for (int a = -1; a <= 1; ++a) {
                         int r2 = mr + a;
@@ -283,24 +297,160 @@ __global__ void k_check_ties(const float* __restrict__ f, const float* __restric
                 }
             }
         }
-        if (!differ) continue;
+        if (!differ) {
+            // No tie (any more): the least neighbour decides; release a pin from an earlier pass.
+            if (c == C_PINNED) {
+                cls[i] = C_OPEN;
+                if (f[i] != v0) {
+                    atomicAdd(&cnt->repaired, 1ull);
+                    atomicMin(&cnt->repair_level, qmin);
+                }
+            }
+            continue;
+        }
         atomicAdd(&cnt->ties, 1ull);
         if (inside_level) {
+            // Only the level's own pops can order this tie: replay the lowest such level.
             atomicAdd(&cnt->unresolved, 1ull);
+            atomicMin(&cnt->min_level, qmin);
             continue;
         }
         float want = phi(f[pick], gn);
         if (c != C_PINNED || pin_parent[i] != pick) {
             pin_parent[i] = pick;
             cls[i] = C_PINNED;
-            if (want != f[i]) atomicAdd(&cnt->repaired, 1ull);
+            if (want != f[i]) {
+                atomicAdd(&cnt->repaired, 1ull);
+                atomicMin(&cnt->repair_level, qmin);
+            }
         }
     }
 }
 
-__global__ void k_reset_open(const uint8_t* __restrict__ cls, float* __restrict__ f, size_t N) {
+// Resets every unsettled cell at or above key level Q to +inf. A cell's level depends only on its
+// parent chain, which runs through strictly lower levels, so cells below Q are already final.
+__global__ void k_reset_from(const uint8_t* __restrict__ cls, float* __restrict__ f, size_t N, int Q) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
-        if (cls[i] == C_OPEN || cls[i] == C_PINNED) f[i] = INFINITY;
+        if ((cls[i] == C_OPEN || follows_parent(cls[i])) && qkey(f[i]) >= Q) f[i] = INFINITY;
+}
+
+// The cells whose current level has key Q (the candidates for that level's heap), up to cap: land,
+// and water touching land (open water elsewhere never enters the flood).
+__global__ void k_gather_level(const float* __restrict__ f, const uint8_t* __restrict__ cls, int W, int H, int Q,
+                               int* __restrict__ list, int* __restrict__ count, int cap) {
+    size_t N = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        if (qkey(f[i]) != Q) continue;
+        if (cls[i] == C_WATER) {
+            int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+            bool touches = false;
+            for (int rs = -1; rs <= 1 && !touches; ++rs) {
+                int nr = row + rs;
+                if (nr < 0 || nr >= H) continue;
+                for (int cs = -1; cs <= 1; ++cs)
+                    if ((rs || cs) && cls[nr * W + wrap_col(col + cs, W)] != C_WATER) touches = true;
+            }
+            if (!touches) continue;
+        }
+        int s = atomicAdd(count, 1);
+        if (s < cap) list[s] = (int)i;
+    }
+}
+
+// In the heap before key level Q opens: water and the polar outlets (pushed at the start) and every
+// cell with a neighbour below Q (pushed when that neighbour was popped). Lower levels are exact here.
+__device__ bool entered_below(const float* f, const uint8_t* cls, int W, int H, int cell, int Q) {
+    uint8_t c = cls[cell];
+    if (c == C_WATER || c == C_SEED) return true;
+    int row = cell / W, col = cell % W;
+    for (int rs = -1; rs <= 1; ++rs) {
+        int nr = row + rs;
+        if (nr < 0 || nr >= H) continue;
+        for (int cs = -1; cs <= 1; ++cs) {
+            if (rs == 0 && cs == 0) continue;
+            if (qkey(f[nr * W + wrap_col(col + cs, W)]) < Q) return true;
+        }
+    }
+    return false;
+}
+
+// Replays key level Q of the priority flood (FlowRouting.kt:93-109) with one thread: a min-heap of
+// cell indices seeded with the level's cells that entered it from below; each pop visits its
+// neighbours in the reference's order, and each neighbour not yet visited takes its level from the
+// popped cell, joining this level's heap if its key is still Q. Every cell so reached gets its exact
+// parent (class EXACT). Bounded by the heap's capacity; an overflow is reported, never overrun.
+__global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ g, uint8_t* __restrict__ cls,
+                               int* __restrict__ pin, int* __restrict__ mark, int gen, const int* __restrict__ list,
+                               const int* __restrict__ list_n, int* __restrict__ heap, int cap, int W, int H, int Q,
+                               FillCounters* cnt) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int n = *list_n;
+    if (n > cap) {
+        cnt->overflow = 1;
+        return;
+    }
+    int hs = 0;
+    auto push = [&](int v) -> bool {
+        if (hs >= cap) return false;
+        int s = hs++;
+        heap[s] = v;
+        while (s > 0) {
+            int p = (s - 1) >> 1;
+            if (heap[p] <= heap[s]) break;
+            int t = heap[p];
+            heap[p] = heap[s];
+            heap[s] = t;
+            s = p;
+        }
+        return true;
+    };
+    auto pop = [&]() -> int {
+        int top = heap[0];
+        heap[0] = heap[--hs];
+        int s = 0;
+        while (true) {
+            int l = 2 * s + 1;
+            if (l >= hs) break;
+            int r = l + 1;
+            int m = (r < hs && heap[r] < heap[l]) ? r : l;
+            if (heap[s] <= heap[m]) break;
+            int t = heap[m];
+            heap[m] = heap[s];
+            heap[s] = t;
+            s = m;
+        }
+        return top;
+    };
+    for (int k = 0; k < n; ++k)
+        if (entered_below(f, cls, W, H, list[k], Q) && !push(list[k])) {
+            cnt->overflow = 1;
+            return;
+        }
+    while (hs > 0) {
+        int x = pop();
+        float fx = f[x];
+        int row = x / W, col = x % W;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (rs == 0 && cs == 0) continue;
+                int y = nr * W + wrap_col(col + cs, W);
+                if (mark[y] == gen || entered_below(f, cls, W, H, y, Q)) continue;
+                mark[y] = gen;
+                float fy = phi(fx, g[y]);
+                if (cls[y] != C_DRAINED) {
+                    pin[y] = x;
+                    cls[y] = C_EXACT;
+                }
+                f[y] = fy;
+                if (qkey(fy) == Q && !push(y)) {
+                    cnt->overflow = 1;
+                    return;
+                }
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -333,13 +483,25 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     CG_LAUNCH(ctx) k_mark_drained<<<grid, 256, 0, sm>>>(a, d_rel, N, d_cls, d_filled);
     CG_CHECK_LAUNCH(ctx);
 
+    // Scratch of the level replays: a generation mark per cell, the level's cells and the heap.
+    const int cap = 1 << 18;
+    CG_BUF(int, d_mark, ctx, S_SCRATCH3, N);
+    CG_BUF(int, d_replay, ctx, S_CG4, 2 * (size_t)cap + 4);
+    int* d_list = d_replay;
+    int* d_heap = d_replay + cap;
+    int* d_list_n = d_replay + 2 * cap;
+    CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), sm));
+    int gen = 0;
+
     FillCounters hc;
     int64_t tie_total = 0, unresolved_total = 0;
-    const int max_repairs = 8;
+    // Each pass either settles, pins tie parents by the index rule, or replays the lowest level
+    // holding a tie the index rule cannot order; the cap is a guard, not the expected exit.
+    const int max_repairs = 64;
     for (int repair = 0; repair <= max_repairs; ++repair) {
         uint8_t* act = d_act;
         uint8_t* nxt = d_act + tiles;
-        CG_LAUNCH(ctx) k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, W, H, tiles_x, tiles_y, act);
+        CG_LAUNCH(ctx) k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, d_filled, W, H, tiles_x, tiles_y, act);
         CG_CHECK_LAUNCH(ctx);
         // Relax until no tile changes. A bounded loop: every pass lowers some level or stops, and
         // levels only take values from a finite set; the cap is a guard, not the expected exit.
@@ -361,20 +523,39 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
             }
         }
         if (pass >= max_passes) return fail(ctx, CG_TIMEOUT, "fill relaxation did not settle in %d passes", pass);
-        CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 3 * sizeof(unsigned long long), sm));
+        FillCounters zero{};
+        zero.min_level = INT_MAX;
+        zero.repair_level = INT_MAX;
+        CG_CUDA(ctx, cudaMemcpyAsync(d_cnt, &zero, sizeof(zero), cudaMemcpyHostToDevice, sm));
         CG_LAUNCH(ctx) k_check_ties<<<grid, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, d_cnt);
         CG_CHECK_LAUNCH(ctx);
         CG_CUDA(ctx, cudaMemcpyAsync(&hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, sm));
         CG_CUDA(ctx, cudaStreamSynchronize(sm));
-        tie_total = (int64_t)hc.ties;
+        if (repair == 0) tie_total = (int64_t)hc.ties;
         unresolved_total = (int64_t)hc.unresolved;
-        if (hc.repaired == 0) break;
+        if (hc.repaired == 0 && hc.unresolved == 0) break;
         if (repair == max_repairs) {
             unresolved_total += (int64_t)hc.repaired;
             break;
         }
-        // Recompute the fixed point with the pinned parents.
-        CG_LAUNCH(ctx) k_reset_open<<<grid, 256, 0, sm>>>(d_cls, d_filled, N);
+        int from = hc.repaired ? hc.repair_level : INT_MAX;
+        if (hc.unresolved) {
+            // Replay the lowest key level whose ties only its own pops can order.
+            const int Q = hc.min_level;
+            ++gen;
+            CG_CUDA(ctx, cudaMemsetAsync(d_list_n, 0, sizeof(int), sm));
+            CG_LAUNCH(ctx) k_gather_level<<<grid, 256, 0, sm>>>(d_filled, d_cls, W, H, Q, d_list, d_list_n, cap);
+            CG_LAUNCH(ctx) k_replay_level<<<1, 32, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, d_mark, gen, d_list, d_list_n,
+                                                            d_heap, cap, W, H, Q, d_cnt);
+            CG_CHECK_LAUNCH(ctx);
+            int overflow = 0;
+            CG_CUDA(ctx, cudaMemcpyAsync(&overflow, &d_cnt->overflow, sizeof(int), cudaMemcpyDeviceToHost, sm));
+            CG_CUDA(ctx, cudaStreamSynchronize(sm));
+            if (overflow) break;   // reported as unresolved
+            if (Q < from) from = Q;
+        }
+        // Recompute the levels at and above the lowest one that changed.
+        CG_LAUNCH(ctx) k_reset_from<<<grid, 256, 0, sm>>>(d_cls, d_filled, N, from);
     }
     if (ties) *ties = tie_total;
     if (unresolved) *unresolved = unresolved_total;

@@ -90,6 +90,35 @@ def test_fill_flat_plateaus_with_ties():
     assert np.array_equal(bits(got), bits(want)), np.flatnonzero(bits(got) != bits(want))[:8]
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_fill_key_plateaus(seed):
+    """Ground whose neighbouring heights share a quantised heap key (steps of 1e-7, below the key's
+    2.4e-7 quantum at 4): within-level ties everywhere, which the fill resolves by replaying levels."""
+    rng = np.random.default_rng(seed)
+    W, H = 256, 128
+    g = (np.float32(0.3) + np.float32(1e-7) * rng.integers(0, 6, (H, W)).astype(np.float32)).astype(np.float32)
+    g[20:40, 30:90] -= np.float32(2e-6)       # a shallow pit in the plateau
+    land = np.ones((H, W), np.uint8)
+    land[:, 0:3] = 0
+    rel = np.where(land == 1, g, np.float32(0.29)).astype(np.float32)
+    want = oracle.fill_depressions(land, rel)
+    got, ties, unresolved = FlowRouting.fill_depressions(land, rel, with_ties=True)
+    assert unresolved == 0
+    diff = np.flatnonzero(bits(got) != bits(want))
+    assert diff.size == 0, f"{diff.size} cells differ (ties {ties}): {diff[:8]}"
+
+
+def test_fill_bench_world_8192x4096():
+    """The bench world's first cut (8192 x 4096, 33.5M cells), where the index rule alone left a few
+    within-level ties open: the device fill equals the oracle's bit for bit."""
+    h, up, rk = synthetic.world(8192, 4096, 1, uplift="ridges")
+    s, land, rel, n = oracle.percentile_cut(h, 0.70, np.float32(120.0) / np.float32(16000.0))
+    want = oracle.fill_depressions(land, rel)
+    got, ties, unresolved = FlowRouting.fill_depressions(land, rel, with_ties=True)
+    assert unresolved == 0
+    assert np.array_equal(bits(got), bits(want))
+
+
 @pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
 @pytest.mark.parametrize("by_facet,over_potential", [(True, True), (True, False), (False, False)])
 def test_flow_directions(W, H, seed, by_facet, over_potential):
