@@ -6,10 +6,12 @@
 // sequential double sums in the reference, and the answer can flip on their last bit, so both are
 // reproduced exactly:
 //  - the histogram: per (row, bin) cell counts are exact integers, and each bin's sequential sum
-//    over the rows in order is rebuilt with cg::seq_repeat_add, which replays `count` additions of
-//    the row's weight exactly (csrc/cg_fpemu.h);
-//  - the bracket: its cells are sorted on the device and walked by one thread in the reference's
-//    order (a few thousand cells on the benchmark worlds).
+//    over the rows in order is rebuilt by one warp, 32 rows at a time: inside one binade of the
+//    running sum every addition adds a whole number of ulps, so a chunk is an integer prefix sum
+//    (cg::warp_chunk_sum); a chunk that crosses a binade or meets a tie is replayed row by row with
+//    cg::seq_repeat_add, which takes `count` equal additions in closed form (csrc/cg_fpemu.h);
+//  - the bracket: its cells are sorted on the device and walked in the reference's order by one
+//    warp with the same chunking.
 // min, max, the bin of a cell and the land/relative split are elementwise or exact reductions.
 #include <climits>
 #include <cmath>
@@ -109,18 +111,33 @@ __global__ void __launch_bounds__(512) k_row_counts(const float* __restrict__ h,
     for (int b = threadIdx.x; b < BINS; b += blockDim.x) out[b] = sh[b];
 }
 
-// One thread per bin: the reference's sequential sum `histogram[bin] += rowWeights[row]`, in cell
-// order, replayed exactly row by row.
+// One warp per bin: the reference's sequential sum `histogram[bin] += rowWeights[row]`, in cell
+// order, replayed exactly, 32 rows at a time (cg::warp_chunk_sum), a chunk that leaves its binade or
+// meets a tie replayed row by row by lane 0 (cg::seq_repeat_add).
 __global__ void k_bin_sums(const unsigned* __restrict__ counts, const double* __restrict__ w, int H,
                            const CutState* s, double* __restrict__ hist) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (b >= BINS || s->degenerate) return;
     double acc = 0.0;
-    for (int r = 0; r < H; ++r) {
-        unsigned c = counts[(size_t)r * BINS + b];
-        if (c) acc = seq_repeat_add(acc, w[r], (int64_t)c);
+    for (int base = 0; base < H; base += 32) {
+        int r = base + lane;
+        unsigned c = r < H ? counts[(size_t)r * BINS + b] : 0u;
+        double wr = r < H ? w[r] : 0.0;
+        if (!__any_sync(0xFFFFFFFFu, c != 0u)) continue;
+        double before, after;
+        if (warp_chunk_sum(acc, wr, (int64_t)c, &before, &after)) {
+            acc = after;
+            continue;
+        }
+        // Exact replay of the chunk's rows in order.
+        for (int j = 0; j < 32; ++j) {
+            unsigned cj = __shfl_sync(0xFFFFFFFFu, c, j);
+            double wj = __shfl_sync(0xFFFFFFFFu, wr, j);
+            if (cj) acc = seq_repeat_add(acc, wj, (int64_t)cj);
+        }
     }
-    hist[b] = acc;
+    if (lane == 0) hist[b] = acc;
 }
 
 // SeaLevelStage.kt:614-622: the first bin that brings the weight below up to the target.
@@ -197,25 +214,49 @@ __global__ void k_pad(long long* keys, int n, int P2) {
     for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) keys[i] = LLONG_MAX;
 }
 
-// SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target.
+// SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target. One
+// warp, 32 entries at a time: each lane knows the exact sum before its entry (cg::warp_chunk_sum),
+// so the first lane at or past the target is the answer; a chunk that cannot be taken whole is
+// replayed entry by entry.
 __global__ void k_bracket_walk(const float* __restrict__ h, const long long* __restrict__ keys,
                                const double* __restrict__ w, int W, double target, CutState* s) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
     if (s->degenerate) return;
-    int n = s->count;
+    const int n = s->count;
     if (n == 0) {
-        s->todays = s->highest;
+        if (lane == 0) s->todays = s->highest;
         return;
     }
     double below = s->below_bracket;
-    for (int i = 0; i < n; ++i) {
-        int cell = (int)(keys[i] & 0xFFFFFFFFLL);
-        if (below >= target) {
-            s->todays = h[cell];
-            return;
+    for (int base = 0; base < n; base += 32) {
+        int i = base + lane;
+        int cell = i < n ? (int)(keys[i] & 0xFFFFFFFFLL) : -1;
+        double wi = i < n ? w[cell / W] : 0.0;
+        double before, after;
+        if (warp_chunk_sum(below, wi, i < n ? 1 : 0, &before, &after)) {
+            unsigned hit = __ballot_sync(FULL, i < n && before >= target);
+            if (hit) {
+                int j = __ffs(hit) - 1;
+                int c = __shfl_sync(FULL, cell, j);
+                if (lane == 0) s->todays = h[c];
+                return;
+            }
+            below = after;
+            continue;
         }
-        below += w[cell / W];
+        for (int j = 0; j < 32; ++j) {
+            int cj = __shfl_sync(FULL, cell, j);
+            double wj = __shfl_sync(FULL, wi, j);
+            if (cj < 0) break;
+            if (below >= target) {
+                if (lane == 0) s->todays = h[cj];
+                return;
+            }
+            below += wj;
+        }
     }
-    s->todays = h[(int)(keys[n - 1] & 0xFFFFFFFFLL)];
+    if (lane == 0) s->todays = h[(int)(keys[n - 1] & 0xFFFFFFFFLL)];
 }
 
 // SeaLevelStage.landAndWaterAt (SeaLevelStage.kt:175-200).
@@ -282,7 +323,7 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
     CG_LAUNCH(ctx) k_minmax<<<grid, 256, 0, sm>>>(d_h, N, d_s);
     CG_LAUNCH(ctx) k_cut_prepare<<<1, 1, 0, sm>>>(d_s, target);
     CG_LAUNCH(ctx) k_row_counts<<<H, 512, 0, sm>>>(d_h, W, d_s, d_counts);
-    CG_LAUNCH(ctx) k_bin_sums<<<BINS / 128, 128, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
+    CG_LAUNCH(ctx) k_bin_sums<<<BINS * 32 / 256, 256, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
     CG_LAUNCH(ctx) k_bracket_bin<<<1, 1, 0, sm>>>(d_hist, target, d_s);
     CG_LAUNCH(ctx) k_bracket_collect<<<grid, 256, 0, sm>>>(d_h, N, d_s, d_keys);
     CG_CHECK_LAUNCH(ctx);
@@ -311,7 +352,7 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
         }
         CG_CHECK_LAUNCH(ctx);
     }
-    CG_LAUNCH(ctx) k_bracket_walk<<<1, 1, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
+    CG_LAUNCH(ctx) k_bracket_walk<<<1, 32, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
     CG_LAUNCH(ctx) k_land_and_water<<<grid, 256, 0, sm>>>(d_h, N, d_s, lowstand_share, land_half, sea_half, d_land, d_rel);
     CG_CHECK_LAUNCH(ctx);
     CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));

@@ -74,4 +74,51 @@ CG_HD double seq_repeat_add(double s, double w, int64_t c) {
     return s;
 }
 
+#ifdef __CUDACC__
+// One warp, 32 terms: each lane adds `count` copies of its term `w` (> 0) to a running sum `s` that
+// is the same in every lane, lanes in order. When s > 0 and every addition of the chunk stays inside
+// s's binade with no tie at half an ulp, every addition adds a fixed whole number of ulps d, so the
+// chunk is an integer prefix sum. Then it returns true with, per lane, the sum before that lane's
+// first addition (*before) and the sum after the whole chunk (*after, same in all lanes); otherwise
+// it returns false and the caller replays the chunk one addition at a time.
+__device__ __forceinline__ bool warp_chunk_sum(double s, double w, int64_t count, double* before, double* after) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int64_t TOP = (int64_t)1 << 53;
+    const int lane = threadIdx.x & 31;
+    if (!(s > 0.0)) return false;
+    int e = ilogb(s);
+    double U = ldexp(1.0, e - 52);
+    int64_t m = (int64_t)(s / U);
+    bool ok = true;
+    int64_t inc = 0, q = 0, d = 0;
+    if (count > 0) {
+        double x = ldexp(w, 52 - e);   // w / U, exact
+        if (!(x < 9.0e15)) {
+            ok = false;
+        } else {
+            q = (int64_t)x;
+            double f = x - (double)q;
+            if (f == 0.5) ok = false;
+            d = q + (f > 0.5 ? 1 : 0);
+            if (d > 0 && count > TOP / d) ok = false;
+            else inc = count * d;
+        }
+    }
+    // Exclusive prefix of the increments across the warp.
+    int64_t incl = inc;
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    int64_t excl = incl - inc;
+    // Every step of this lane stays in the binade: the last one starts at m + excl + (count-1) d.
+    if (ok && count > 0 && m + excl + (count - 1) * d + q > TOP - 1) ok = false;
+    if (!__all_sync(FULL, ok)) return false;
+    int64_t total = __shfl_sync(FULL, incl, 31);
+    *before = (double)(m + excl) * U;
+    *after = (double)(m + total) * U;
+    return true;
+}
+#endif
+
 }  // namespace cg

@@ -58,9 +58,9 @@ struct InciseArgs {
     float step_diag;
     int only_above_base;
 };
-cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const float* d_ground,
-                     const float* d_rel, const float* d_area, const float* d_erod, float* d_surface,
-                     const InciseArgs& a);
+cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const long long* d_key,
+                     int levels, const float* d_ground, const float* d_rel, const float* d_area, const float* d_erod,
+                     float* d_surface, const InciseArgs& a);
 struct BasinsDev {
     int count;
 };

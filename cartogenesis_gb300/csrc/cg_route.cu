@@ -68,55 +68,96 @@ __device__ __forceinline__ int neighbour_at(int W, int H, int col, int row) {
     return row * W + wrap_col(col, W);
 }
 
-// FlowRouting.facetReceiver (FlowRouting.kt:223-310).
+// x / d, skipping the division by a leg of exactly one cell width (x / 1.0 is x in IEEE arithmetic).
+__device__ __forceinline__ double div_leg(double x, double d) { return d == 1.0 ? x : __ddiv_rn(x, d); }
+
+// FlowRouting.facetReceiver (FlowRouting.kt:223-310), with the same values in fewer FP64 operations
+// (GB300's FP64 rate is a small fraction of its FP32 rate):
+//  - a cardinal's slope is shared by its two facets and a diagonal's by its two facets, so each is
+//    computed once, and a diagonal's only if a facet is clamped to it;
+//  - the share along the far edge, a / b with a = outward tc^2 and b = cdrop od^2 (rounded products,
+//    as the reference forms them), is compared with 1 as a >= b: for positive doubles fl(a/b) >= 1
+//    exactly when a >= b, since a < b puts a/b at or below the double just under 1. The division is
+//    taken once, for the winning facet, whose share the draw is compared with.
+// Facets are visited and compared in the reference's order, so ties resolve identically.
 __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int col, int row, Steps st, long long seed) {
     const int ccs_t[4] = {1, 0, -1, 0};
     const int crs_t[4] = {0, -1, 0, 1};
-    double here = rs[row * W + col];
+    const double here = rs[row * W + col];
+    const double ew = (double)st.ew, ns = (double)st.ns, dg = (double)st.diag;
+    // Diagonal falls and slopes, indexed by (column step, row step) = (+-1, +-1).
+    double dfall[4];
+    double dslope[4];
+    bool dslope_done[4] = {false, false, false, false};
+    int dcell[4];
+    for (int k = 0; k < 4; ++k) {
+        int dcs = (k & 1) ? 1 : -1, drs = (k & 2) ? 1 : -1;
+        dcell[k] = neighbour_at(W, H, col + dcs, row + drs);
+        dfall[k] = dcell[k] >= 0 ? __dsub_rn(here, rs[dcell[k]]) : 0.0;
+    }
     double steepest = 0.0;
     int fcard = -1, fdiag = -1;
-    double dshare = 0.0;
+    int mode = 0;   // 0: cardinal, 1: diagonal, 2: inside the facet (share a / b)
+    double wa = 0.0, wb = 0.0;
     for (int side = 0; side < 4; ++side) {
-        int ccs = ccs_t[side], crs = crs_t[side];
-        int card = neighbour_at(W, H, col + ccs, row + crs);
+        const int ccs = ccs_t[side], crs = crs_t[side];
+        const int card = neighbour_at(W, H, col + ccs, row + crs);
         if (card < 0) continue;
-        double cdrop = __dsub_rn(here, rs[card]);
-        double to_card = (double)st.of(ccs, crs);
-        double on_to_diag = (double)(ccs == 0 ? st.ew : st.ns);
+        const double cdrop = __dsub_rn(here, rs[card]);
+        const double to_card = ccs != 0 ? ew : ns;     // GroundSteps.of(ccs, crs): never a diagonal here
+        const double on_to_diag = ccs == 0 ? ew : ns;
+        const double cslope = div_leg(cdrop, to_card);
         for (int turn = -1; turn <= 1; turn += 2) {
-            int dcs = ccs == 0 ? turn : ccs;
-            int drs = crs == 0 ? turn : crs;
-            int diag = neighbour_at(W, H, col + dcs, row + drs);
-            if (diag < 0) continue;
-            double dfall = __dsub_rn(here, rs[diag]);
-            double dslope = __ddiv_rn(dfall, (double)st.diag);
-            double outward = __dsub_rn(dfall, cdrop);
-            double cslope = __ddiv_rn(cdrop, to_card);
-            double oslope = __ddiv_rn(outward, on_to_diag);
-            double share_edge = cdrop > 0.0 ? __ddiv_rn(__dmul_rn(__dmul_rn(outward, to_card), to_card),
-                                                        __dmul_rn(__dmul_rn(cdrop, on_to_diag), on_to_diag))
-                                            : 1.0;
-            bool to_cardinal = cdrop > 0.0 && outward <= 0.0;
-            bool to_diagonal = !to_cardinal && share_edge >= 1.0;
-            double fslope = to_cardinal ? cslope
-                                        : (to_diagonal ? dslope
-                                                       : __dsqrt_rn(__dadd_rn(__dmul_rn(cslope, cslope),
-                                                                              __dmul_rn(oslope, oslope))));
-            double share = to_cardinal ? 0.0 : (to_diagonal ? 1.0 : share_edge);
+            const int dcs = ccs == 0 ? turn : ccs;
+            const int drs = crs == 0 ? turn : crs;
+            const int k = (dcs > 0 ? 1 : 0) | (drs > 0 ? 2 : 0);
+            if (dcell[k] < 0) continue;
+            const double df = dfall[k];
+            const double outward = __dsub_rn(df, cdrop);
+            const bool to_cardinal = cdrop > 0.0 && outward <= 0.0;
+            double a = 0.0, b = 0.0, fslope;
+            int m;
+            if (to_cardinal) {
+                fslope = cslope;
+                m = 0;
+            } else {
+                bool to_diagonal = true;   // share 1 when the cardinal is not downhill
+                if (cdrop > 0.0) {
+                    a = __dmul_rn(__dmul_rn(outward, to_card), to_card);
+                    b = __dmul_rn(__dmul_rn(cdrop, on_to_diag), on_to_diag);
+                    to_diagonal = a >= b;
+                }
+                if (to_diagonal) {
+                    if (!dslope_done[k]) {
+                        dslope[k] = __ddiv_rn(df, dg);
+                        dslope_done[k] = true;
+                    }
+                    fslope = dslope[k];
+                    m = 1;
+                } else {
+                    const double oslope = div_leg(outward, on_to_diag);
+                    fslope = __dsqrt_rn(__dadd_rn(__dmul_rn(cslope, cslope), __dmul_rn(oslope, oslope)));
+                    m = 2;
+                }
+            }
             if (fslope > steepest) {
                 steepest = fslope;
                 fcard = card;
-                fdiag = diag;
-                dshare = share;
+                fdiag = dcell[k];
+                mode = m;
+                wa = a;
+                wb = b;
             }
         }
     }
     if (steepest <= 0.0) return -1;
-    if (dshare <= 0.0) return fcard;
-    if (dshare >= 1.0) return fdiag;
+    if (mode == 0) return fcard;
+    if (mode == 1) return fdiag;
+    const double share = __ddiv_rn(wa, wb);
+    if (share <= 0.0) return fcard;
     // FlowRouting.subGridDraw (FlowRouting.kt:355-356).
-    double draw = (double)__fmul_rn(__fadd_rn(seeded_noise(col, row, seed ^ kSubGridDrawSalt), 1.0f), 0.5f);
-    return draw < dshare ? fdiag : fcard;
+    const double draw = (double)__fmul_rn(__fadd_rn(seeded_noise(col, row, seed ^ kSubGridDrawSalt), 1.0f), 0.5f);
+    return draw < share ? fdiag : fcard;
 }
 
 // FlowRouting.steepestNeighbourOf (FlowRouting.kt:320-343).
@@ -197,6 +238,7 @@ struct FlatArgs {
     double* z;
     double* d;
     double* ad;
+    double* coef;   // ns / pivot per member
     int* kept;
 };
 
@@ -260,34 +302,33 @@ __device__ __forceinline__ double stencil_weight(const FlatArgs& a, int cs, int 
     return (cs != 0 && rs != 0) ? a.diag : (rs != 0 ? a.ns : a.ew);
 }
 
-// Column-run preconditioner solve (FlatRouting.ColumnRuns.solve, FlatRouting.kt:399-413): one
-// thread per run, down the column then back up, in the reference's expression order.
+// Column-run preconditioner solve (FlatRouting.ColumnRuns.solve, FlatRouting.kt:399-413). Members
+// are ordered by (column, row), so every run is a contiguous segment, walked by one thread down the
+// column and back up with the chain carried in registers; the expressions are the reference's
+// ((right + ns * above) / pivot down, += (ns / pivot) * below up, ns / pivot kept per member).
+__device__ __forceinline__ bool run_continues(const int* mem, int n, int k, int W, int H) {
+    return k + 1 < n && mem[k + 1] == mem[k] + W && mem[k] / W + 1 < H;
+}
+__device__ __forceinline__ bool run_head(const int* mem, int k, int W) { return k == 0 || mem[k - 1] != mem[k] - W; }
+
 __device__ void runs_solve(const FlatArgs& a, int base, int n, const double* right, double* into) {
     const int* mem = a.members + base;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        int cell = mem[k];
-        int north = cell - a.W;
-        if (north >= 0 && a.local[north] >= 0) continue;   // not a run head
-        int pos = k, prev = -1;
-        int c = cell;
-        while (true) {
-            double carried = prev < 0 ? 0.0 : __dmul_rn(a.ns, into[base + prev]);
-            into[base + pos] = __ddiv_rn(__dadd_rn(right[base + pos], carried), a.pivot[base + pos]);
-            int south = c + a.W;
-            if (c / a.W + 1 >= a.H || a.local[south] < 0) break;
-            prev = pos;
-            pos = a.local[south];
-            c = south;
+        if (!run_head(mem, k, a.W)) continue;
+        int j = k;
+        double v = __ddiv_rn(__dadd_rn(right[base + j], 0.0), a.pivot[base + j]);   // carried = 0.0 at a head
+        into[base + j] = v;
+        while (run_continues(mem, n, j, a.W, a.H)) {
+            ++j;
+            v = __ddiv_rn(__dadd_rn(right[base + j], __dmul_rn(a.ns, v)), a.pivot[base + j]);
+            into[base + j] = v;
         }
-        // Back up the run: pos is its last member.
-        while (true) {
-            int north2 = c - a.W;
-            if (north2 < 0 || a.local[north2] < 0) break;
-            int up = a.local[north2];
-            into[base + up] = __dadd_rn(into[base + up], __dmul_rn(__ddiv_rn(a.ns, a.pivot[base + up]),
-                                                                   into[base + pos]));
-            pos = up;
-            c = north2;
+        // Back up the run from its last member j.
+        double below = v;
+        for (int i = j - 1; i >= k; --i) {
+            double u = __dadd_rn(into[base + i], __dmul_rn(a.coef[base + i], below));
+            into[base + i] = u;
+            below = u;
         }
     }
 }
@@ -320,7 +361,19 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     const int base = a.off[f];
     const int n = a.count[f];
     int* mem = a.members + base;
+    // Order the members by (column, row): every column run becomes a contiguous segment. The order
+    // is fixed, so the block reductions below are deterministic.
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int c = mem[k];
+        mem[k] = (c % a.W) * a.H + c / a.W;
+    }
+    __syncthreads();
     sort_members(mem, n);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int key = mem[k];
+        mem[k] = (key % a.H) * a.W + key / a.H;
+    }
+    __syncthreads();
     for (int k = threadIdx.x; k < n; k += blockDim.x) a.local[mem[k]] = k;
     __syncthreads();
 
@@ -368,24 +421,17 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
                                                                                     a.seed ^ kRainReliefSalt)));
     }
     __syncthreads();
-    // Thomas pivots per run (FlatRouting.kt:388-395).
+    // Thomas pivots per run (FlatRouting.kt:388-395), and ns / pivot for the solves' way back up.
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        int cell = mem[k];
-        int north = cell - a.W;
-        if (north >= 0 && a.local[north] >= 0) continue;
-        int pos = k, c = cell;
-        double prev = 0.0;
-        bool first = true;
+        if (!run_head(mem, k, a.W)) continue;
+        int j = k;
+        double p = a.degree[base + j];
         while (true) {
-            double dg = a.degree[base + pos];
-            double p = first ? dg : __dsub_rn(dg, __ddiv_rn(__dmul_rn(a.ns, a.ns), prev));
-            a.pivot[base + pos] = p;
-            prev = p;
-            first = false;
-            int south = c + a.W;
-            if (c / a.W + 1 >= a.H || a.local[south] < 0) break;
-            pos = a.local[south];
-            c = south;
+            a.pivot[base + j] = p;
+            a.coef[base + j] = __ddiv_rn(a.ns, p);
+            if (!run_continues(mem, n, j, a.W, a.H)) break;
+            ++j;
+            p = __dsub_rn(a.degree[base + j], __ddiv_rn(__dmul_rn(a.ns, a.ns), p));
         }
     }
     __syncthreads();
@@ -510,7 +556,7 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             int raised = 0;
             if ((st = exclusive_scan(ctx, d_cnt, d_off, flats, &raised)) != CG_OK) return st;
             CG_BUF(int, d_members, ctx, S_FLATMEM, raised);
-            CG_BUF(double, d_dbl, ctx, S_CG1, 7 * (size_t)raised);
+            CG_BUF(double, d_dbl, ctx, S_CG1, 8 * (size_t)raised);
             CG_LAUNCH(ctx) k_flat_scatter<<<grid, 256, 0, sm>>>(d_label, N, d_off, d_cur, d_members);
             CG_CHECK_LAUNCH(ctx);
             FlatArgs a;
@@ -543,6 +589,7 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             a.z = d_dbl + 4 * (size_t)raised;
             a.d = d_dbl + 5 * (size_t)raised;
             a.ad = d_dbl + 6 * (size_t)raised;
+            a.coef = d_dbl + 7 * (size_t)raised;
             a.kept = d_kept;
             CG_LAUNCH(ctx) k_flat_solve<<<flats, FT, 0, sm>>>(a);
             CG_CHECK_LAUNCH(ctx);

@@ -225,7 +225,7 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
                                    lattice, p.facet_routing != 0, p.flat_potential != 0, d_recv, d_surface, &fc));
         mark(3);
         int levels = 0;
-        CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, stats ? &levels : nullptr));
+        CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, &levels));
         mark(4);
         InciseArgs ia;
         ia.courant_coefficient = rates.courant_coefficient;
@@ -236,7 +236,7 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         ia.step_ns = rates.step_ns;
         ia.step_diag = rates.step_diag;
         ia.only_above_base = p.receiver_clamp != 0;
-        CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_filled, d_rel, d_area, d_erod, cur, ia));
+        CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia));
         mark(5);
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         float* res;

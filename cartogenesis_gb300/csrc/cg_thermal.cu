@@ -28,9 +28,20 @@ struct ThermalArgs {
     float rate;
 };
 
+// Settled-tile skip (the reference's own skip, ErosionStage.kt:269-342, restated for fused launches).
+// A launch of K sweeps carries any change at most 2K <= 16 cells, less than a tile's side, so a tile
+// can change only if a cell of it or of one of its 8 neighbouring tiles changed in the previous
+// launch. `prev` holds those per-tile "changed" bits (null: compute every tile); each launch writes
+// its own into `cur`. A skipped tile is not even copied: the launches ping-pong between two buffers,
+// and a tile that did not change in the previous launch holds the same bits in both.
+struct TileFlags {
+    const uint8_t* prev;
+    uint8_t* cur;
+};
+
 template <int K>
 __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                                 int W, int H, ThermalArgs a) {
+                                                                 int W, int H, ThermalArgs a, TileFlags fl) {
     constexpr int HALO = 2 * K;
     constexpr int RW = TX + 2 * HALO;   // region width
     constexpr int RH = TY + 2 * HALO;   // region height
@@ -38,6 +49,23 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
     float* hs = smem;                  // heights, current sweep
     float* hn = smem + RW * RH;        // heights, next sweep
     float* gv = smem + 2 * RW * RH;    // give rates
+
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    if (fl.prev) {
+        bool near_change = false;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int ty = (int)blockIdx.y + dy;
+            if (ty < 0 || ty >= (int)gridDim.y) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int tx = ((int)blockIdx.x + dx + (int)gridDim.x) % (int)gridDim.x;
+                if (fl.prev[ty * gridDim.x + tx]) near_change = true;
+            }
+        }
+        if (!near_change) {
+            if (threadIdx.x == 0) fl.cur[tile] = 0;
+            return;
+        }
+    }
 
     const int x0 = blockIdx.x * TX - HALO;
     const int y0 = blockIdx.y * TY - HALO;
@@ -122,11 +150,19 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
         hn = t;
     }
 
+    int changed = 0;
     for (int i = threadIdx.x; i < TX * TY; i += THREADS) {
         int ty = i / TX, tx = i - ty * TX;
         int gy = blockIdx.y * TY + ty, gx = blockIdx.x * TX + tx;
         if (gy >= H || gx >= W) continue;
-        out[(size_t)gy * W + gx] = hs[(ty + HALO) * RW + tx + HALO];
+        size_t idx = (size_t)gy * W + gx;
+        float v = hs[(ty + HALO) * RW + tx + HALO];
+        if (__float_as_uint(v) != __float_as_uint(in[idx])) changed = 1;
+        out[idx] = v;
+    }
+    if (fl.cur) {
+        changed = __syncthreads_or(changed);
+        if (threadIdx.x == 0) fl.cur[tile] = changed ? 1 : 0;
     }
 }
 
@@ -136,7 +172,8 @@ size_t smem_bytes() {
 }
 
 template <int K>
-cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs& a, cudaStream_t st) {
+cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs& a, cudaStream_t st,
+                   TileFlags fl = TileFlags{nullptr, nullptr}) {
     static bool configured = false;
     size_t bytes = smem_bytes<K>();
     if (!configured) {
@@ -146,7 +183,7 @@ cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs&
         configured = true;
     }
     dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
-    thermal_sweeps_kernel<K><<<grid, THREADS, bytes, st>>>(in, out, W, H, a);
+    thermal_sweeps_kernel<K><<<grid, THREADS, bytes, st>>>(in, out, W, H, a, fl);
     return cudaGetLastError();
 }
 
@@ -193,19 +230,32 @@ cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, 
         a.limit[n] = n >= 4 ? lim.diagonal : (thermal_row_step(n) != 0 ? lim.north_south : lim.east_west);
     a.settled = lim.east_west * 1e-3f;   // SETTLED_SHARE_OF_CRITICAL_SLOPE (ErosionStage.kt:92)
     a.rate = rate;
+    // Per-tile change bits of the previous and the current launch. The first launch computes every
+    // tile (the destination holds nothing yet); after it, both buffers hold a tile's bits whenever
+    // that tile did not change, so the skip needs no copy.
+    const int tiles = ((W + TX - 1) / TX) * ((H + TY - 1) / TY);
+    CG_BUF(uint8_t, d_flags, ctx, S_THERMFLAG, 2 * (size_t)tiles);
+    uint8_t* prev = d_flags;
+    uint8_t* cur = d_flags + tiles;
     float* src = d_a;
     float* dst = d_b;
+    bool first = true;
     while (passes > 0) {
         cudaError_t e;
-        if (passes >= 8) e = launch<8>(src, dst, W, H, a, ctx->stream), passes -= 8;
-        else if (passes >= 4) e = launch<4>(src, dst, W, H, a, ctx->stream), passes -= 4;
-        else if (passes >= 2) e = launch<2>(src, dst, W, H, a, ctx->stream), passes -= 2;
-        else e = launch<1>(src, dst, W, H, a, ctx->stream), passes -= 1;
+        TileFlags fl{first ? nullptr : prev, cur};
+        if (passes >= 8) e = launch<8>(src, dst, W, H, a, ctx->stream, fl), passes -= 8;
+        else if (passes >= 4) e = launch<4>(src, dst, W, H, a, ctx->stream, fl), passes -= 4;
+        else if (passes >= 2) e = launch<2>(src, dst, W, H, a, ctx->stream, fl), passes -= 2;
+        else e = launch<1>(src, dst, W, H, a, ctx->stream, fl), passes -= 1;
         if (e != cudaSuccess) return cuda_fail(ctx, e, "thermal_sweeps_kernel", __FILE__, __LINE__);
         ctx->launches++;
+        first = false;
         float* t = src;
         src = dst;
         dst = t;
+        uint8_t* tf = prev;
+        prev = cur;
+        cur = tf;
     }
     *result = src;
     return CG_OK;

@@ -13,11 +13,12 @@
 // its accumulation (its weight plus its donors' areas in key order, the reference's float
 // additions in the reference's order) and carries on; the others stop. No barrier, O(N) work.
 //
-// Incision needs each receiver final before its donors: cells are bucketed by their depth below
-// the outlet (pointer jumping) and one cooperative kernel sweeps the depths in order with a grid
-// barrier between them. Every order with receivers first gives the same bits, because a cell reads
-// only its receiver's final state.
+// Incision needs each receiver final before its donors: cells are bucketed by their Kahn level (a
+// receiver's level is always higher than its donors') and one cooperative kernel sweeps the levels
+// from the top down with a grid barrier between them. Every order with receivers first gives the
+// same bits, because a cell reads only its receiver's final state.
 #include <cooperative_groups.h>
+#include <cuda/atomic>
 
 #include <cfloat>
 #include <climits>
@@ -99,9 +100,10 @@ __global__ void k_walk(WalkArgs a) {
         while (true) {
             int r = a.recv[c];
             if (!is_land_receiver(a.land, r)) break;
-            __threadfence();   // this cell's key and area are visible before its arrival is counted
-            if (atomicSub(&a.pending[r], 1) != 1) break;   // not the last donor in
-            __threadfence();
+            // Release: this cell's key and area are visible before its arrival is counted. Acquire:
+            // the last donor in sees every other donor's.
+            cuda::atomic_ref<int, cuda::thread_scope_device> pend(a.pending[r]);
+            if (pend.fetch_sub(1, cuda::memory_order_acq_rel) != 1) break;   // not the last donor in
             long long keys[8];
             int cells[8];
             int n = sorted_donors(a, r, keys, cells);
@@ -167,51 +169,40 @@ __global__ void k_land_compact(const uint8_t* __restrict__ land, const int* __re
 
 // ---- incise
 
-// Depth below the outlet by pointer jumping: ptr = land receiver or self, dist = 1 or 0.
-__global__ void k_depth_init(const uint8_t* __restrict__ land, const int32_t* __restrict__ recv, size_t N,
-                             int* __restrict__ ptr, int* __restrict__ dist) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        int r = land[i] ? recv[i] : -1;
-        bool up = r >= 0 && land[r];
-        ptr[i] = up ? r : (int)i;
-        dist[i] = up ? 1 : 0;
+// Cells bucketed by their Kahn level (the high half of their drainage key). A cell's receiver sits
+// on a strictly higher level, so sweeping the levels from the top down reaches every receiver
+// before its donors. Warp-aggregated atomics: lanes sharing a level take one atomic between them.
+__global__ void k_level_count(const uint8_t* __restrict__ land, const long long* __restrict__ key, size_t N,
+                              int levels, int* __restrict__ count) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += stride) {
+        size_t i = base + threadIdx.x;
+        bool valid = i < N && land[i];
+        int L = valid ? (int)(key[i] >> 32) : -1;
+        if (valid && (L < 0 || L >= levels)) valid = false, L = -1;   // never for a forest's keys
+        unsigned group = __match_any_sync(FULL, L);
+        if (valid && (threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count[L], __popc(group));
     }
 }
 
-// List ranking: a root points at itself with distance 0, so adding its distance changes nothing.
-__global__ void k_depth_jump(const int* __restrict__ ptr, const int* __restrict__ dist, size_t N,
-                             int* __restrict__ ptr2, int* __restrict__ dist2) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        int p = ptr[i];
-        dist2[i] = dist[i] + dist[p];
-        ptr2[i] = ptr[p];
-    }
-}
-
-__global__ void k_depth_count(const uint8_t* __restrict__ land, const int* __restrict__ dist, size_t N,
-                              int* __restrict__ count, int* __restrict__ max_depth) {
-    int local = 0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (!land[i]) continue;
-        int d = dist[i];
-        if (d < 0 || (size_t)d >= N) {   // only a receiver cycle could do this: flag it, write nothing
-            atomicExch(&max_depth[1], 1);
-            continue;
-        }
-        atomicAdd(&count[d], 1);
-        local = max(local, d);
-    }
-    atomicMax(max_depth, local);
-}
-
-__global__ void k_depth_scatter(const uint8_t* __restrict__ land, const int* __restrict__ dist, size_t N,
-                                int max_level, const int* __restrict__ start, int* __restrict__ cursor,
+__global__ void k_level_scatter(const uint8_t* __restrict__ land, const long long* __restrict__ key, size_t N,
+                                int levels, const int* __restrict__ start, int* __restrict__ cursor,
                                 int* __restrict__ bucket) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (!land[i]) continue;
-        int d = dist[i];
-        if (d < 0 || d > max_level) continue;
-        bucket[start[d] + atomicAdd(&cursor[d], 1)] = (int)i;
+    const unsigned FULL = 0xFFFFFFFFu;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += stride) {
+        size_t i = base + threadIdx.x;
+        bool valid = i < N && land[i];
+        int L = valid ? (int)(key[i] >> 32) : -1;
+        if (valid && (L < 0 || L >= levels)) valid = false, L = -1;
+        unsigned group = __match_any_sync(FULL, L);
+        int leader = __ffs(group) - 1;
+        int slot = 0;
+        if (valid && lane == leader) slot = atomicAdd(&cursor[L], __popc(group));
+        slot = __shfl_sync(FULL, slot, leader);
+        if (valid) bucket[start[L] + slot + __popc(group & ((1u << lane) - 1u))] = (int)i;
     }
 }
 
@@ -277,7 +268,7 @@ __device__ void incise_cell(const InciseDev& d, int cell) {
 __global__ void __launch_bounds__(256) k_incise_levels(InciseDev d) {
     cgr::grid_group grid = cgr::this_grid();
     const int stride = gridDim.x * blockDim.x;
-    for (int level = 0; level < d.levels; ++level) {
+    for (int level = d.levels - 1; level >= 0; --level) {
         const int lo = d.start[level], hi = d.start[level + 1];
         for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) incise_cell(d, d.bucket[i]);
         grid.sync();
@@ -425,55 +416,26 @@ cg_status order_from_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
     return CG_OK;
 }
 
-cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const float* d_ground,
-                     const float* d_rel, const float* d_area, const float* d_erod, float* d_surface,
-                     const InciseArgs& args) {
+cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const long long* d_key,
+                     int levels, const float* d_ground, const float* d_rel, const float* d_area, const float* d_erod,
+                     float* d_surface, const InciseArgs& args) {
     size_t N = (size_t)W * H;
     cudaStream_t sm = ctx->stream;
     int grid = ctx->num_sms * 8;
-    CG_BUF(int, d_ptr, ctx, S_PTR, N);
-    CG_BUF(int, d_ptr2, ctx, S_PTR2, N);
-    CG_BUF(int, d_dist, ctx, S_SCRATCH0, N);
-    CG_BUF(int, d_dist2, ctx, S_SCRATCH1, N);
+    if (levels <= 0) return CG_OK;
     CG_BUF(int, d_bucket, ctx, S_SCRATCH2, N);
     CG_BUF(float, d_water, ctx, S_WATER, N);
-    CG_BUF(int, d_small, ctx, S_LEVELCNT, 4);
-    CG_LAUNCH(ctx) k_depth_init<<<grid, 256, 0, sm>>>(d_land, d_recv, N, d_ptr, d_dist);
-    int jumps = 1;
-    while (((size_t)1 << jumps) < N) ++jumps;
-    int* p = d_ptr;
-    int* p2 = d_ptr2;
-    int* di = d_dist;
-    int* di2 = d_dist2;
-    for (int j = 0; j < jumps; ++j) {
-        CG_LAUNCH(ctx) k_depth_jump<<<grid, 256, 0, sm>>>(p, di, N, p2, di2);
-        int* t = p;
-        p = p2;
-        p2 = t;
-        t = di;
-        di = di2;
-        di2 = t;
-    }
-    CG_CUDA(ctx, cudaMemsetAsync(d_small, 0, 4 * sizeof(int), sm));
-    // Depth histogram: depths are below N; bound the count array by the maximum depth first.
-    CG_BUF(int, d_cnt, ctx, S_DEPTH, N + 2);
-    CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, (N + 2) * sizeof(int), sm));
-    CG_LAUNCH(ctx) k_depth_count<<<grid, 256, 0, sm>>>(d_land, di, N, d_cnt, d_small);
-    CG_CHECK_LAUNCH(ctx);
-    int depth_info[2] = {0, 0};
-    CG_CUDA(ctx, cudaMemcpyAsync(depth_info, d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaStreamSynchronize(sm));
-    if (depth_info[1]) return fail(ctx, CG_BAD_ARG, "receivers do not form a forest (a cycle)");
-    int max_depth = depth_info[0];
-    int levels = max_depth + 1;
+    CG_BUF(int, d_cnt, ctx, S_DEPTH, (size_t)levels + 1);
     CG_BUF(int, d_start, ctx, S_CG2, 2 * (size_t)levels + 2);
     int* d_cursor = d_start + levels + 1;
-    int total = 0;
-    cg_status st = exclusive_scan(ctx, d_cnt, d_start, levels, &total);
+    CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, ((size_t)levels + 1) * sizeof(int), sm));
+    CG_CUDA(ctx, cudaMemsetAsync(d_cursor, 0, ((size_t)levels + 1) * sizeof(int), sm));
+    CG_LAUNCH(ctx) k_level_count<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
+    CG_CHECK_LAUNCH(ctx);
+    // The exclusive scan of levels + 1 counts (the last is zero) ends with the total at start[levels].
+    cg_status st = exclusive_scan(ctx, d_cnt, d_start, levels + 1, nullptr);
     if (st != CG_OK) return st;
-    CG_CUDA(ctx, cudaMemcpyAsync(d_start + levels, &total, sizeof(int), cudaMemcpyHostToDevice, sm));
-    CG_CUDA(ctx, cudaMemsetAsync(d_cursor, 0, (levels + 1) * sizeof(int), sm));
-    CG_LAUNCH(ctx) k_depth_scatter<<<grid, 256, 0, sm>>>(d_land, di, N, max_depth, d_start, d_cursor, d_bucket);
+    CG_LAUNCH(ctx) k_level_scatter<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
     CG_LAUNCH(ctx) k_water_init<<<grid, 256, 0, sm>>>(d_water, N);
     CG_CHECK_LAUNCH(ctx);
     InciseDev d;
@@ -495,6 +457,7 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     if (per_sm < 1) return fail(ctx, CG_CUDA, "incise kernel cannot be resident");
     int cgrid = ctx->num_sms * (per_sm < 4 ? per_sm : 4);
     void* kargs[] = {&d};
+    ctx->launches++;
     CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_incise_levels, cgrid, 256, kargs, 0, sm));
     return CG_OK;
 }
