@@ -4,9 +4,10 @@
 // Routing surface: the filled field (ocean cells their own ground), except across each raised flat,
 // where the potential of a Poisson problem is laid into the band between the flat's highest entry
 // and its lowest raised level. Flats are 8-connected components of raised cells and never touch one
-// another, so each is solved by its own CTA:
-//  - members are sorted by cell index (the reduction order is then fixed, so results are
-//    deterministic run to run);
+// another, so each is solved on its own: a warp per flat of up to 32 members (nearly all of them: the
+// fill's small depressions), a CTA per larger flat:
+//  - members are ordered by (column, row), so each column run is a contiguous segment and the
+//    reduction order is fixed (results are deterministic run to run);
 //  - each member's weighted degree and its Laplacian row are accumulated in the reference's
 //    neighbour order, and each column run's Thomas factorisation and solves are done by one thread
 //    in the reference's order, so both are bit-identical to FlatRouting's;
@@ -239,6 +240,7 @@ struct FlatArgs {
     double* d;
     double* ad;
     double* coef;   // ns / pivot per member
+    const int* large;   // flats of more than 32 members (the CTA kernel's list)
     int* kept;
 };
 
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     __shared__ int shi[32];
-    const int f = blockIdx.x;
+    const int f = a.large[blockIdx.x];
     const int base = a.off[f];
     const int n = a.count[f];
     int* mem = a.members + base;
@@ -523,6 +525,208 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     if (!laid && threadIdx.x == 0) atomicAdd(a.kept, 1);
 }
 
+// Flats of at most 32 members, one warp each (most flats are a few cells: the fill's small
+// depressions). Each lane owns one member; the per-member arithmetic (degree, Laplacian row, the
+// column runs' Thomas solves) is the reference's, done by the member's lane or the run head's lane;
+// the dot products are butterfly shuffles, which give every lane the same bits.
+constexpr int WF = 8;   // warps (flats) per block
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int flats) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    __shared__ double s_right[WF][32], s_into[WF][32], s_piv[WF][32], s_coef[WF][32], s_d[WF][32];
+    __shared__ int s_cont[WF][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f = blockIdx.x * WF + w;
+    if (f >= flats) return;
+    const int n = a.count[f];
+    if (n > 32) return;   // the CTA kernel takes it
+    const int base = a.off[f];
+    const bool act = lane < n;
+    const int W = a.W, H = a.H;
+
+    // Members by (column, row): a bitonic sort across the lanes.
+    int key = act ? (a.members[base + lane] % W) * H + a.members[base + lane] / W : INT_MAX;
+    for (int k = 2; k <= 32; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            int other = __shfl_xor_sync(FULL, key, j);
+            bool up = (lane & k) == 0;
+            bool lower = (lane & j) == 0;
+            int lo = min(key, other), hi = max(key, other);
+            key = (lower == up) ? lo : hi;
+        }
+    const int cell = act ? (key % H) * W + key / H : -1;
+    if (act) {
+        a.members[base + lane] = cell;
+        a.local[cell] = lane;
+    }
+    __syncwarp();
+    const int col = act ? cell % W : 0, row = act ? cell / W : 0;
+
+    // Entry level, highest entry, member neighbours (their lanes), degree and rain.
+    float lo = act ? a.filled[cell] : FLT_MAX;
+    for (int o = 16; o > 0; o >>= 1) lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+    const double entry_level = (double)lo;
+    double hi = -INFINITY, deg = 0.0, rv = 0.0;
+    int nb_lane[8];
+    double nb_w[8];
+    if (act) {
+        int t = 0;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                nb_lane[t] = -1;
+                nb_w[t] = 0.0;
+                if (nr >= 0 && nr < H) {
+                    int nb = nr * W + wrap_col(col + cs, W);
+                    double wgt = stencil_weight(a, cs, rs);
+                    int l = a.local[nb];
+                    double there = a.surface[nb];
+                    if (l < 0 && there < entry_level && there > hi) hi = there;
+                    if (l >= 0) {
+                        deg = __dadd_rn(deg, wgt);
+                        nb_lane[t] = l;
+                        nb_w[t] = wgt;
+                    } else if (there < entry_level) {
+                        deg = __dadd_rn(deg, wgt);
+                    }
+                }
+                ++t;
+            }
+        }
+        rv = __dadd_rn(1.0, __dmul_rn(0.5, (double)smooth_seeded_field(W, a.lattice, col, row,
+                                                                         a.seed ^ kRainReliefSalt)));
+    } else {
+        for (int t = 0; t < 8; ++t) nb_lane[t] = -1, nb_w[t] = 0.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) hi = fmax(hi, __shfl_xor_sync(FULL, hi, o));
+    const double entry_height = hi;
+
+    // Column runs: contiguous lanes. Pivots and ns / pivot down each run by its head lane.
+    const int prev_cell = __shfl_up_sync(FULL, cell, 1);
+    const int next_cell = __shfl_down_sync(FULL, cell, 1);
+    const bool head = act && (lane == 0 || prev_cell != cell - W);
+    s_cont[w][lane] = (act && lane + 1 < n && next_cell == cell + W) ? 1 : 0;
+    s_right[w][lane] = deg;
+    __syncwarp();
+    if (head) {
+        int j = lane;
+        double p = s_right[w][j];
+        while (true) {
+            s_piv[w][j] = p;
+            s_coef[w][j] = __ddiv_rn(a.ns, p);
+            if (!s_cont[w][j]) break;
+            ++j;
+            p = __dsub_rn(s_right[w][j], __ddiv_rn(__dmul_rn(a.ns, a.ns), p));
+        }
+    }
+    __syncwarp();
+
+    // z = M^-1 r through the runs (FlatRouting.ColumnRuns.solve).
+    auto precondition = [&](double right) -> double {
+        s_right[w][lane] = right;
+        __syncwarp();
+        if (head) {
+            int j = lane;
+            double v = __ddiv_rn(__dadd_rn(s_right[w][j], 0.0), s_piv[w][j]);
+            s_into[w][j] = v;
+            while (s_cont[w][j]) {
+                ++j;
+                v = __ddiv_rn(__dadd_rn(s_right[w][j], __dmul_rn(a.ns, v)), s_piv[w][j]);
+                s_into[w][j] = v;
+            }
+            double below = v;
+            for (int i = j - 1; i >= lane; --i) {
+                double u = __dadd_rn(s_into[w][i], __dmul_rn(s_coef[w][i], below));
+                s_into[w][i] = u;
+                below = u;
+            }
+        }
+        __syncwarp();
+        double z = act ? s_into[w][lane] : 0.0;
+        __syncwarp();
+        return z;
+    };
+    auto laplacian = [&](double dv) -> double {
+        s_d[w][lane] = dv;
+        __syncwarp();
+        double sum = __dmul_rn(deg, dv);
+        for (int t = 0; t < 8; ++t)
+            if (nb_lane[t] >= 0) sum = __dsub_rn(sum, __dmul_rn(nb_w[t], s_d[w][nb_lane[t]]));
+        __syncwarp();
+        return act ? sum : 0.0;
+    };
+
+    // Preconditioned conjugate gradients (FlatRouting.kt:296-333).
+    double x = 0.0, r = act ? rv : 0.0;
+    double z = precondition(r);
+    double d = z;
+    double rnorm = warp_sum(act ? __dmul_rn(r, r) : 0.0);
+    double rap = warp_sum(act ? __dmul_rn(r, z) : 0.0);
+    const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
+    const int most = 64 + (int)(8.0 * sqrt((double)n));
+    for (int it = 0; rnorm > stop_at && it < most; ++it) {
+        double ad = laplacian(d);
+        double energy = warp_sum(act ? __dmul_rn(d, ad) : 0.0);
+        if (energy <= 0.0 || rap <= 0.0) break;
+        double step = __ddiv_rn(rap, energy);
+        if (act) {
+            x = __dadd_rn(x, __dmul_rn(step, d));
+            r = __dsub_rn(r, __dmul_rn(step, ad));
+        }
+        double next_norm = warp_sum(act ? __dmul_rn(r, r) : 0.0);
+        z = precondition(r);
+        double next_ap = warp_sum(act ? __dmul_rn(r, z) : 0.0);
+        double improvement = __ddiv_rn(next_ap, rap);
+        if (act) d = __dadd_rn(z, __dmul_rn(improvement, d));
+        rnorm = next_norm;
+        rap = next_ap;
+    }
+    const bool positive = __all_sync(FULL, !act || x > 0.0);
+    double top = act ? x : 0.0;
+    for (int o = 16; o > 0; o >>= 1) top = fmax(top, __shfl_xor_sync(FULL, top, o));
+    const double highest = top > 0.0 ? top : 0.0;
+
+    // FlatRouting.layInBand (FlatRouting.kt:455-489).
+    bool laid = positive && !(highest <= 0.0 || entry_height >= entry_level);
+    if (laid) {
+        const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
+        if (act) a.surface[cell] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(x, highest)));
+        __syncwarp();
+        bool lower = !act;
+        if (act) {
+            double here = a.surface[cell];
+            for (int rs = -1; rs <= 1 && !lower; ++rs) {
+                int nr = row + rs;
+                if (nr < 0 || nr >= H) continue;
+                for (int cs = -1; cs <= 1; ++cs) {
+                    if (cs == 0 && rs == 0) continue;
+                    if (a.surface[nr * W + wrap_col(col + cs, W)] < here) {
+                        lower = true;
+                        break;
+                    }
+                }
+            }
+        }
+        if (!__all_sync(FULL, lower)) {
+            if (act) a.surface[cell] = (double)a.filled[cell];
+            laid = false;
+        }
+    }
+    if (!laid && lane == 0) atomicAdd(a.kept, 1);
+}
+
+// The flats of more than 32 members, listed for the CTA kernel.
+__global__ void k_large_flats(const int* __restrict__ count, int flats, int* __restrict__ list, int* __restrict__ n) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < flats; f += gridDim.x * blockDim.x)
+        if (count[f] > 32) list[atomicAdd(n, 1)] = f;
+}
+
 }  // namespace
 
 cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel,
@@ -591,7 +795,16 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             a.ad = d_dbl + 6 * (size_t)raised;
             a.coef = d_dbl + 7 * (size_t)raised;
             a.kept = d_kept;
-            CG_LAUNCH(ctx) k_flat_solve<<<flats, FT, 0, sm>>>(a);
+            // Small flats one warp each; the rest one CTA each, from a list.
+            CG_BUF(int, d_large, ctx, S_CG5, (size_t)flats + 1);
+            CG_CUDA(ctx, cudaMemsetAsync(d_large + flats, 0, sizeof(int), sm));
+            CG_LAUNCH(ctx) k_large_flats<<<(flats + 255) / 256, 256, 0, sm>>>(d_cnt, flats, d_large, d_large + flats);
+            a.large = d_large;
+            CG_LAUNCH(ctx) k_flat_solve_warp<<<(flats + WF - 1) / WF, 32 * WF, 0, sm>>>(a, flats);
+            int n_large = 0;
+            CG_CUDA(ctx, cudaMemcpyAsync(&n_large, d_large + flats, sizeof(int), cudaMemcpyDeviceToHost, sm));
+            CG_CUDA(ctx, cudaStreamSynchronize(sm));
+            if (n_large > 0) CG_LAUNCH(ctx) k_flat_solve<<<n_large, FT, 0, sm>>>(a);
             CG_CHECK_LAUNCH(ctx);
             CG_CUDA(ctx, cudaMemcpyAsync(&fc.kept, d_kept, sizeof(int), cudaMemcpyDeviceToHost, sm));
             CG_CUDA(ctx, cudaStreamSynchronize(sm));
