@@ -8,6 +8,9 @@ namespace cg {
 // ---- thermal (cg_thermal.cu)
 cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, cg_thermal_limits lim, int passes,
                              float rate, float** result);
+// Sweeps per fused launch when `passes_left` remain (2, or 1 for the last of an odd count), and the
+// number of launches that `passes` sweeps take.
+int thermal_step(int passes_left);
 int thermal_launches(int passes);
 struct ThermalLaunch {
     float limit[8];
@@ -15,7 +18,7 @@ struct ThermalLaunch {
     float rate;
 };
 ThermalLaunch thermal_launch_args(cg_thermal_limits lim, float rate);
-// One fused launch of k sweeps (k in {1, 2, 4, 8}) from src into dst.
+// One fused launch of k sweeps (k = thermal_step(...)) from src into dst.
 cudaError_t thermal_launch(const float* src, float* dst, int W, int H, const ThermalLaunch& t, int k,
                            cudaStream_t stream);
 

@@ -67,14 +67,14 @@ extern "C" cg_status cg_thermal_sweeps_noalloc(const float* heights_in_dev, floa
     float* scratch = nullptr;
     if (scratch_for_current_device(&scratch) != cudaSuccess) return CG_CUDA;
     const cg::ThermalLaunch t = cg::thermal_launch_args(limits, rate);
-    // The same launch sequence as cg_thermal_sweeps (8, 4, 2, 1 sweeps per launch), with the
+    // The same launch sequence as cg_thermal_sweeps (two sweeps per launch, one for an odd rest), with the
     // destinations alternating so that the last launch writes the caller's output. The input is
     // only ever read.
     const int launches = cg::thermal_launches(passes);
     const float* src = heights_in_dev;
     int left = passes;
     for (int i = 0; i < launches; ++i) {
-        int k = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        const int k = cg::thermal_step(left);
         float* dst = ((launches - 1 - i) % 2 == 0) ? heights_out_dev : scratch;
         if (cg::thermal_launch(src, dst, width, height, t, k, st) != cudaSuccess) return CG_CUDA;
         left -= k;
