@@ -114,9 +114,12 @@ cg_status cg_create(cg_ctx** out, int32_t device) {
     ctx->device = device;
     e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
-        delete ctx;
+        cg_destroy(ctx);
         return CG_CUDA;
     }
     *out = ctx;
@@ -127,9 +130,13 @@ void cg_destroy(cg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->aux) cudaStreamSynchronize(ctx->aux);
     for (auto& b : ctx->bufs)
         if (b.ptr) cudaFree(b.ptr);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

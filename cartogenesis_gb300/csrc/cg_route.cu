@@ -5,7 +5,8 @@
 // where the potential of a Poisson problem is laid into the band between the flat's highest entry
 // and its lowest raised level. Flats are 8-connected components of raised cells and never touch one
 // another, so each is solved on its own: a warp per flat of up to 32 members (nearly all of them: the
-// fill's small depressions), a CTA per larger flat:
+// fill's small depressions), a CTA per larger flat, with the solver's vectors in shared memory up to
+// 4096 members (128 threads to 512 members, 512 threads above) and in global memory beyond:
 //  - members are ordered by (column, row), so each column run is a contiguous segment and the
 //    reduction order is fixed (results are deterministic run to run);
 //  - each member's weighted degree and its Laplacian row are accumulated in the reference's
@@ -240,7 +241,8 @@ struct FlatArgs {
     double* d;
     double* ad;
     double* coef;   // ns / pivot per member
-    const int* large;   // flats of more than 32 members (the CTA kernel's list)
+    short* nbr;     // per member, the member index of its 8 neighbours in stencil order (-1: none)
+    const int* large;   // the flats that k_flat_solve takes
     int* kept;
 };
 
@@ -353,6 +355,45 @@ __device__ void apply_laplacian(const FlatArgs& a, int base, int n, const double
         }
         into[base + k] = sum;
     }
+}
+
+// FlatRouting.layInBand (FlatRouting.kt:455-489) over one flat, by the whole CTA: the potential x,
+// scaled into the band between the highest entry and the entry level, is kept only if every member
+// then has a lower neighbour; otherwise the flat keeps its filled level and counts as kept.
+__device__ void lay_in_band(const FlatArgs& a, const int* mem, int n, const double* x, bool positive, double highest,
+                            double entry_level, double entry_height, int* shi) {
+    bool laid = positive && !(highest <= 0.0 || entry_height >= entry_level);
+    if (laid) {
+        const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            a.surface[mem[k]] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(x[k], highest)));
+        __syncthreads();
+        int ok = 1;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            int cell = mem[k];
+            int col = cell % a.W, row = cell / a.W;
+            double here = a.surface[cell];
+            bool lower = false;
+            for (int rs = -1; rs <= 1 && !lower; ++rs) {
+                int nr = row + rs;
+                if (nr < 0 || nr >= a.H) continue;
+                for (int cs = -1; cs <= 1; ++cs) {
+                    if (cs == 0 && rs == 0) continue;
+                    if (a.surface[nr * a.W + wrap_col(col + cs, a.W)] < here) {
+                        lower = true;
+                        break;
+                    }
+                }
+            }
+            if (!lower) ok = 0;
+        }
+        ok = block_reduce(ok, shi, IAnd(), 1);
+        if (!ok) {
+            for (int k = threadIdx.x; k < n; k += blockDim.x) a.surface[mem[k]] = (double)a.filled[mem[k]];
+            laid = false;
+        }
+    }
+    if (!laid && threadIdx.x == 0) atomicAdd(a.kept, 1);
 }
 
 __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
@@ -490,39 +531,236 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     positive = block_reduce(positive, shi, IAnd(), 1);
     const double highest = block_reduce(top, shd, DMax(), 0.0);
 
-    // FlatRouting.layInBand (FlatRouting.kt:455-489).
-    bool laid = positive && !(highest <= 0.0 || entry_height >= entry_level);
-    if (laid) {
-        const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
-        for (int k = threadIdx.x; k < n; k += blockDim.x)
-            a.surface[mem[k]] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(a.x[base + k], highest)));
-        __syncthreads();
-        int ok = 1;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            int cell = mem[k];
-            int col = cell % a.W, row = cell / a.W;
-            double here = a.surface[cell];
-            bool lower = false;
-            for (int rs = -1; rs <= 1 && !lower; ++rs) {
-                int nr = row + rs;
-                if (nr < 0 || nr >= a.H) continue;
-                for (int cs = -1; cs <= 1; ++cs) {
-                    if (cs == 0 && rs == 0) continue;
-                    if (a.surface[nr * a.W + wrap_col(col + cs, a.W)] < here) {
-                        lower = true;
-                        break;
+    lay_in_band(a, mem, n, a.x + base, positive, highest, entry_level, entry_height, shi);
+}
+
+// Flats of 33 to 4096 members, one CTA each, with the CG's working vectors in shared memory.
+// A CG iteration is latency-bound: the column runs' Thomas solves are chains of dependent
+// divisions, one run per thread, and a valley floor can hold runs hundreds of cells long, so a
+// chain that goes through L2 at every step costs most of the iteration. Here r, z, d, A d, the
+// pivots, ns / pivot and the run table sit in shared memory; the per-member constants (degree, the
+// member neighbours) and the potential x, which a thread reads only for its own members, stay in
+// global memory. The arithmetic per member and per run is that of k_flat_solve. A dot product is
+// each thread's partial sum in member order, a warp butterfly and an ordered sum over the warps,
+// so its bits are fixed for a given CTA size.
+constexpr int MID_FLAT = 512;    // members at most for the 128-thread CTA
+constexpr int BIG_FLAT = 4096;   // members at most for the 512-thread CTA; k_flat_solve takes larger flats
+constexpr int SM_BYTES_PER_MEMBER = 6 * 8 + 4;   // six doubles and one run-table entry
+
+// Sums of u and of v over the CTA, returned to every thread. `buf` (one double2 per warp) must
+// alternate between two arrays from one call to the next: the barrier of the next call is what
+// keeps this call's readers ahead of the call after it.
+template <int NW>
+__device__ __forceinline__ double2 block_sum2(double u, double v, double2* buf) {
+    for (int o = 16; o > 0; o >>= 1) {
+        u = __dadd_rn(u, __shfl_xor_sync(0xFFFFFFFFu, u, o));
+        v = __dadd_rn(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    }
+    if ((threadIdx.x & 31) == 0) buf[threadIdx.x >> 5] = make_double2(u, v);
+    __syncthreads();
+    double2 s = buf[0];
+#pragma unroll
+    for (int w = 1; w < NW; ++w) {
+        const double2 t = buf[w];
+        s.x = __dadd_rn(s.x, t.x);
+        s.y = __dadd_rn(s.y, t.y);
+    }
+    return s;
+}
+
+__device__ __forceinline__ int nbr_lo(int v) { return (int)(short)(v & 0xFFFF); }
+__device__ __forceinline__ int nbr_hi(int v) { return v >> 16; }
+__device__ __forceinline__ int nbr_pack(int lo, int hi) { return (int)(((unsigned)lo & 0xFFFFu) | ((unsigned)hi << 16)); }
+
+template <int FT>
+__global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __restrict__ list) {
+    constexpr int NW = FT / 32;
+    extern __shared__ double dyn[];
+    __shared__ double shd[32];
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    __shared__ double2 sh2[2][NW];
+    __shared__ int s_nruns;
+    const int f = list[blockIdx.x];
+    const int base = a.off[f];
+    const int n = a.count[f];
+    const int W = a.W, H = a.H;
+    int* mem = a.members + base;
+    double* s_r = dyn;
+    double* s_z = s_r + n;
+    double* s_d = s_z + n;
+    double* s_ad = s_d + n;
+    double* s_piv = s_ad + n;
+    double* s_coef = s_piv + n;
+    unsigned* s_run = reinterpret_cast<unsigned*>(s_coef + n);   // first | last << 16
+    double* x = a.x + base;
+    double* degree = a.degree + base;
+    int4* nbr = reinterpret_cast<int4*>(a.nbr + (size_t)base * 8);
+
+    // Members by (column, row), as in k_flat_solve.
+    for (int k = threadIdx.x; k < n; k += FT) {
+        int c = mem[k];
+        mem[k] = (c % W) * H + c / W;
+    }
+    __syncthreads();
+    sort_members(mem, n);
+    for (int k = threadIdx.x; k < n; k += FT) {
+        int key = mem[k];
+        mem[k] = (key % H) * W + key / H;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += FT) a.local[mem[k]] = k;
+    if (threadIdx.x == 0) s_nruns = 0;
+    __syncthreads();
+
+    // Entry level; then per member the highest entry, the degree, the member neighbours and the rain
+    // (FlatRouting.kt:93-115, 239-295, 427-445).
+    float lo = FLT_MAX;
+    for (int k = threadIdx.x; k < n; k += FT) lo = fminf(lo, a.filled[mem[k]]);
+    const double entry_level = (double)block_reduce(lo, shf, FMin(), FLT_MAX);
+    double hi = -INFINITY;
+    for (int k = threadIdx.x; k < n; k += FT) {
+        const int cell = mem[k];
+        const int col = cell % W, row = cell / W;
+        double total = 0.0;
+        int nb8[8];
+        int t = 0;
+        for (int rs = -1; rs <= 1; ++rs) {
+            const int nr = row + rs;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                nb8[t] = -1;
+                if (nr >= 0 && nr < H) {
+                    const int nb = nr * W + wrap_col(col + cs, W);
+                    const double w = stencil_weight(a, cs, rs);
+                    const int l = a.local[nb];
+                    if (l >= 0) {
+                        total = __dadd_rn(total, w);
+                        nb8[t] = l;
+                    } else {
+                        const double there = a.surface[nb];
+                        if (there < entry_level) {
+                            total = __dadd_rn(total, w);
+                            if (there > hi) hi = there;
+                        }
                     }
                 }
+                ++t;
             }
-            if (!lower) ok = 0;
         }
-        ok = block_reduce(ok, shi, IAnd(), 1);
-        if (!ok) {
-            for (int k = threadIdx.x; k < n; k += blockDim.x) a.surface[mem[k]] = (double)a.filled[mem[k]];
-            laid = false;
+        degree[k] = total;
+        x[k] = 0.0;
+        nbr[k] = make_int4(nbr_pack(nb8[0], nb8[1]), nbr_pack(nb8[2], nb8[3]), nbr_pack(nb8[4], nb8[5]),
+                           nbr_pack(nb8[6], nb8[7]));
+        s_r[k] = __dadd_rn(1.0, __dmul_rn(0.5, (double)smooth_seeded_field(W, a.lattice, col, row,
+                                                                             a.seed ^ kRainReliefSalt)));
+        if (run_head(mem, k, W)) {
+            int j = k;
+            while (run_continues(mem, n, j, W, H)) ++j;
+            s_run[atomicAdd(&s_nruns, 1)] = (unsigned)k | ((unsigned)j << 16);
         }
     }
-    if (!laid && threadIdx.x == 0) atomicAdd(a.kept, 1);
+    const double entry_height = block_reduce(hi, shd, DMax(), (double)-INFINITY);
+    const int runs = s_nruns;
+
+    // Thomas pivots down each run (FlatRouting.kt:388-395) and ns / pivot for the way back up.
+    for (int i = threadIdx.x; i < runs; i += FT) {
+        const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
+        double p = degree[first];
+        for (int j = first;; ++j) {
+            s_piv[j] = p;
+            s_coef[j] = __ddiv_rn(a.ns, p);
+            if (j == last) break;
+            p = __dsub_rn(degree[j + 1], __ddiv_rn(__dmul_rn(a.ns, a.ns), p));
+        }
+    }
+    __syncthreads();
+
+    // z = M^-1 r through the runs (FlatRouting.ColumnRuns.solve, FlatRouting.kt:399-413).
+    auto precondition = [&]() {
+        for (int i = threadIdx.x; i < runs; i += FT) {
+            const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
+            double v = __ddiv_rn(__dadd_rn(s_r[first], 0.0), s_piv[first]);
+            s_z[first] = v;
+            for (int j = first + 1; j <= last; ++j) {
+                v = __ddiv_rn(__dadd_rn(s_r[j], __dmul_rn(a.ns, v)), s_piv[j]);
+                s_z[j] = v;
+            }
+            double below = v;
+            for (int j = last - 1; j >= first; --j) {
+                below = __dadd_rn(s_z[j], __dmul_rn(s_coef[j], below));
+                s_z[j] = below;
+            }
+        }
+    };
+    const double w8[8] = {a.diag, a.ns, a.diag, a.ew, a.ew, a.diag, a.ns, a.diag};   // stencil order
+
+    // Preconditioned conjugate gradients (FlatRouting.kt:296-333).
+    precondition();
+    __syncthreads();
+    double rn = 0.0, ra = 0.0;
+    for (int k = threadIdx.x; k < n; k += FT) {
+        const double rv = s_r[k], zv = s_z[k];
+        s_d[k] = zv;
+        rn = __dadd_rn(rn, __dmul_rn(rv, rv));
+        ra = __dadd_rn(ra, __dmul_rn(rv, zv));
+    }
+    int parity = 0;
+    double2 sums = block_sum2<NW>(rn, ra, sh2[parity]);
+    parity ^= 1;
+    double rnorm = sums.x, rap = sums.y;
+    const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
+    const int most = 64 + (int)(8.0 * sqrt((double)n));
+    for (int it = 0; rnorm > stop_at && it < most; ++it) {
+        // A d (FlatRouting.kt:274-282) and d . A d.
+        double e = 0.0;
+        for (int k = threadIdx.x; k < n; k += FT) {
+            const int4 q = nbr[k];
+            const int l8[8] = {nbr_lo(q.x), nbr_hi(q.x), nbr_lo(q.y), nbr_hi(q.y),
+                               nbr_lo(q.z), nbr_hi(q.z), nbr_lo(q.w), nbr_hi(q.w)};
+            const double dk = s_d[k];
+            double sum = __dmul_rn(degree[k], dk);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (l8[t] >= 0) sum = __dsub_rn(sum, __dmul_rn(w8[t], s_d[l8[t]]));
+            s_ad[k] = sum;
+            e = __dadd_rn(e, __dmul_rn(dk, sum));
+        }
+        const double energy = block_sum2<NW>(e, 0.0, sh2[parity]).x;
+        parity ^= 1;
+        if (energy <= 0.0 || rap <= 0.0) break;
+        const double step = __ddiv_rn(rap, energy);
+        for (int k = threadIdx.x; k < n; k += FT) {
+            x[k] = __dadd_rn(x[k], __dmul_rn(step, s_d[k]));
+            s_r[k] = __dsub_rn(s_r[k], __dmul_rn(step, s_ad[k]));
+        }
+        __syncthreads();
+        precondition();
+        __syncthreads();
+        double nn = 0.0, na = 0.0;
+        for (int k = threadIdx.x; k < n; k += FT) {
+            const double rv = s_r[k];
+            nn = __dadd_rn(nn, __dmul_rn(rv, rv));
+            na = __dadd_rn(na, __dmul_rn(rv, s_z[k]));
+        }
+        sums = block_sum2<NW>(nn, na, sh2[parity]);
+        parity ^= 1;
+        const double improvement = __ddiv_rn(sums.y, rap);
+        for (int k = threadIdx.x; k < n; k += FT) s_d[k] = __dadd_rn(s_z[k], __dmul_rn(improvement, s_d[k]));
+        __syncthreads();
+        rnorm = sums.x;
+        rap = sums.y;
+    }
+    int positive = 1;
+    double top = 0.0;
+    for (int k = threadIdx.x; k < n; k += FT) {
+        const double v = x[k];
+        if (!(v > 0.0)) positive = 0;
+        if (v > top) top = v;
+    }
+    positive = block_reduce(positive, shi, IAnd(), 1);
+    const double highest = block_reduce(top, shd, DMax(), 0.0);
+    lay_in_band(a, mem, n, x, positive, highest, entry_level, entry_height, shi);
 }
 
 // Flats of at most 32 members, one warp each (most flats are a few cells: the fill's small
@@ -721,10 +959,17 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
     if (!laid && lane == 0) atomicAdd(a.kept, 1);
 }
 
-// The flats of more than 32 members, listed for the CTA kernel.
-__global__ void k_large_flats(const int* __restrict__ count, int flats, int* __restrict__ list, int* __restrict__ n) {
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < flats; f += gridDim.x * blockDim.x)
-        if (count[f] > 32) list[atomicAdd(n, 1)] = f;
+// The flats of more than 32 members, listed by the CTA kernel that takes them: lists[0] the
+// 128-thread shared-memory kernel, lists[1] the 512-thread one, lists[2] k_flat_solve. ctr[0..2]
+// count the lists, ctr[3..4] hold the largest flat of the first two (their shared-memory size).
+__global__ void k_flat_lists(const int* __restrict__ count, int flats, int* __restrict__ lists, int* __restrict__ ctr) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < flats; f += gridDim.x * blockDim.x) {
+        const int n = count[f];
+        if (n <= 32) continue;
+        const int c = n <= MID_FLAT ? 0 : n <= BIG_FLAT ? 1 : 2;
+        lists[(size_t)c * flats + atomicAdd(&ctr[c], 1)] = f;
+        if (c < 2) atomicMax(&ctr[3 + c], n);
+    }
 }
 
 }  // namespace
@@ -760,7 +1005,7 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             int raised = 0;
             if ((st = exclusive_scan(ctx, d_cnt, d_off, flats, &raised)) != CG_OK) return st;
             CG_BUF(int, d_members, ctx, S_FLATMEM, raised);
-            CG_BUF(double, d_dbl, ctx, S_CG1, 8 * (size_t)raised);
+            CG_BUF(double, d_dbl, ctx, S_CG1, 10 * (size_t)raised);
             CG_LAUNCH(ctx) k_flat_scatter<<<grid, 256, 0, sm>>>(d_label, N, d_off, d_cur, d_members);
             CG_CHECK_LAUNCH(ctx);
             FlatArgs a;
@@ -794,18 +1039,40 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             a.d = d_dbl + 5 * (size_t)raised;
             a.ad = d_dbl + 6 * (size_t)raised;
             a.coef = d_dbl + 7 * (size_t)raised;
+            a.nbr = reinterpret_cast<short*>(d_dbl + 8 * (size_t)raised);   // 8 shorts per member
             a.kept = d_kept;
-            // Small flats one warp each; the rest one CTA each, from a list.
-            CG_BUF(int, d_large, ctx, S_CG5, (size_t)flats + 1);
-            CG_CUDA(ctx, cudaMemsetAsync(d_large + flats, 0, sizeof(int), sm));
-            CG_LAUNCH(ctx) k_large_flats<<<(flats + 255) / 256, 256, 0, sm>>>(d_cnt, flats, d_large, d_large + flats);
-            a.large = d_large;
-            CG_LAUNCH(ctx) k_flat_solve_warp<<<(flats + WF - 1) / WF, 32 * WF, 0, sm>>>(a, flats);
-            int n_large = 0;
-            CG_CUDA(ctx, cudaMemcpyAsync(&n_large, d_large + flats, sizeof(int), cudaMemcpyDeviceToHost, sm));
-            CG_CUDA(ctx, cudaStreamSynchronize(sm));
-            if (n_large > 0) CG_LAUNCH(ctx) k_flat_solve<<<n_large, FT, 0, sm>>>(a);
+            // Flats of at most 32 members one warp each; larger ones one CTA each, by size class.
+            CG_BUF(int, d_lists, ctx, S_CG5, 3 * (size_t)flats + 5);
+            int* d_ctr = d_lists + 3 * (size_t)flats;
+            CG_CUDA(ctx, cudaMemsetAsync(d_ctr, 0, 5 * sizeof(int), sm));
+            CG_LAUNCH(ctx) k_flat_lists<<<(flats + 255) / 256, 256, 0, sm>>>(d_cnt, flats, d_lists, d_ctr);
             CG_CHECK_LAUNCH(ctx);
+            int ctr[5] = {0, 0, 0, 0, 0};
+            CG_CUDA(ctx, cudaMemcpyAsync(ctr, d_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, sm));
+            CG_CUDA(ctx, cudaStreamSynchronize(sm));
+            // The small and mid-sized flats on the auxiliary stream, beside the few large ones, whose
+            // CTAs hold an SM each for the whole solve.
+            CG_CUDA(ctx, cudaEventRecord(ctx->fork, sm));
+            CG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->fork, 0));
+            CG_LAUNCH(ctx) k_flat_solve_warp<<<(flats + WF - 1) / WF, 32 * WF, 0, ctx->aux>>>(a, flats);
+            if (ctr[0] > 0)
+                CG_LAUNCH(ctx) k_flat_solve_sm<128><<<ctr[0], 128, (size_t)ctr[3] * SM_BYTES_PER_MEMBER, ctx->aux>>>(
+                    a, d_lists);
+            CG_CHECK_LAUNCH(ctx);
+            if (ctr[1] > 0) {
+                const size_t bytes = (size_t)ctr[4] * SM_BYTES_PER_MEMBER;
+                CG_CUDA(ctx, cudaFuncSetAttribute(k_flat_solve_sm<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)bytes));
+                CG_LAUNCH(ctx) k_flat_solve_sm<512><<<ctr[1], 512, bytes, sm>>>(a, d_lists + flats);
+                CG_CHECK_LAUNCH(ctx);
+            }
+            if (ctr[2] > 0) {
+                a.large = d_lists + 2 * (size_t)flats;
+                CG_LAUNCH(ctx) k_flat_solve<<<ctr[2], FT, 0, sm>>>(a);
+                CG_CHECK_LAUNCH(ctx);
+            }
+            CG_CUDA(ctx, cudaEventRecord(ctx->join, ctx->aux));
+            CG_CUDA(ctx, cudaStreamWaitEvent(sm, ctx->join, 0));
             CG_CUDA(ctx, cudaMemcpyAsync(&fc.kept, d_kept, sizeof(int), cudaMemcpyDeviceToHost, sm));
             CG_CUDA(ctx, cudaStreamSynchronize(sm));
             fc.flats = flats;
