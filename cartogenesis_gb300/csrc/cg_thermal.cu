@@ -25,6 +25,7 @@ constexpr int KMAX = 2;
 
 struct ThermalArgs {
     float limit[8];
+    float lim0[8];   // max(limit, 0)
     float settled;
     float rate;
 };
@@ -40,66 +41,127 @@ struct TileFlags {
     uint8_t* cur;
 };
 
-// The give pass over the region's rows [m, RH - m) and columns [m, RW - m).
-template <int RW, int RH, bool EDGE>
-__device__ __forceinline__ void give_pass(const float* __restrict__ hs, float* __restrict__ gv, int m, int y0, int H,
-                                          const ThermalArgs& a) {
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int ry = m + ty; ry < RH - m; ry += 8) {
-        const int gy = y0 + ry;
-        if (EDGE && (gy < 0 || gy >= H)) continue;
-        for (int rx = m + tx; rx < RW - m; rx += 32) {
-            const int c = ry * RW + rx;
-            const float here = hs[c];
-            float excess = 0.0f, steepest = 0.0f;
+// Per-cell rules, written without branches: the conditions become predicated adds in the
+// reference's neighbour order, so the sums round exactly as the reference's loop does.
+// Neighbours by name: E/W the same row, S/N the rows below/above, and the diagonals SE (+1,+1),
+// NE (+1,-1), SW (-1,+1), NW (-1,-1) as (column step, row step).
+struct Window {
+    float nw, n, ne, w, c, e, sw, s, se;   // the 3 x 3 block around a cell
+};
+
+// The give rate of a cell (ErosionStage.kt:283-311). `lim0[n]` is max(limit, 0): a drop counts
+// towards the excess when it is positive and above the limit. `has_s` / `has_n`: the rows below /
+// above exist (false only at the poles).
+__device__ __forceinline__ float give_rate(const Window& v, bool has_s, bool has_n, const ThermalArgs& a) {
+    const float nb[8] = {v.e, v.w, v.s, v.n, v.se, v.ne, v.sw, v.nw};
+    const bool ok[8] = {true, true, has_s, has_n, has_s, has_n, has_s, has_n};
+    float excess = 0.0f, steepest = 0.0f;
 #pragma unroll
-            for (int n = 0; n < 8; ++n) {
-                const int rs = thermal_row_step(n), cs = thermal_col_step(n);
-                if (EDGE && (gy + rs < 0 || gy + rs >= H)) continue;
-                const float drop = __fsub_rn(here, hs[c + rs * RW + cs]);
-                if (drop <= 0.0f) continue;
-                if (drop > steepest) steepest = drop;
-                const float limit = a.limit[n];
-                if (drop > limit) excess = __fadd_rn(excess, __fsub_rn(drop, limit));
+    for (int n = 0; n < 8; ++n) {
+        const float drop = __fsub_rn(v.c, nb[n]);
+        if (ok[n] && drop > steepest) steepest = drop;
+        const float over = __fsub_rn(drop, a.limit[n]);
+        if (ok[n] && drop > a.lim0[n]) excess = __fadd_rn(excess, over);
+    }
+    float g = 0.0f;
+    if (excess > a.settled) {
+        const float p = __fmul_rn(a.rate, excess), q = __fmul_rn(steepest, 0.5f);
+        g = __fdiv_rn(p <= q ? p : q, excess);
+    }
+    return g;
+}
+
+// The new height of a cell from its neighbours' give rates (ErosionStage.kt:313-340).
+__device__ __forceinline__ float moved(const Window& v, const Window& g, bool has_s, bool has_n,
+                                       const ThermalArgs& a) {
+    const float nb[8] = {v.e, v.w, v.s, v.n, v.se, v.ne, v.sw, v.nw};
+    const float gn[8] = {g.e, g.w, g.s, g.n, g.se, g.ne, g.sw, g.nw};
+    const bool ok[8] = {true, true, has_s, has_n, has_s, has_n, has_s, has_n};
+    float received = 0.0f, given = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float limit = a.limit[n];
+        const float incoming = __fsub_rn(nb[n], v.c);
+        const bool in = ok[n] && incoming > limit;
+        const bool out = ok[n] && !(incoming > limit) && -incoming > limit;
+        const float r = __fadd_rn(received, __fmul_rn(gn[n], __fsub_rn(incoming, limit)));
+        const float o = __fadd_rn(given, __fmul_rn(g.c, __fsub_rn(-incoming, limit)));
+        received = in ? r : received;
+        given = out ? o : given;
+    }
+    return __fadd_rn(__fsub_rn(v.c, given), received);
+}
+
+// One pass over the region's rows [M, RH - M) and columns [M, RW - M). A thread takes a column
+// segment of up to SEG rows and slides a 3 x 3 window down it, so each cell costs three
+// shared-memory loads per field instead of nine. Work items are (segment, column), columns
+// fastest, so a warp's loads are consecutive words. MOVE: the move pass (reads gv, writes dst),
+// else the give pass (writes gv).
+template <int RW, int RH, int M, bool MOVE, bool EDGE>
+__device__ __forceinline__ void pass(const float* __restrict__ hs, float* __restrict__ gv, float* __restrict__ dst,
+                                     int y0, int H, const ThermalArgs& a) {
+    constexpr int SEG = 4;
+    constexpr int COLS = RW - 2 * M, ROWS = RH - 2 * M;
+    constexpr int SEGS = (ROWS + SEG - 1) / SEG;
+    constexpr int ITEMS = COLS * SEGS;
+    for (int item = threadIdx.x; item < ITEMS; item += THREADS) {
+        const int col = M + item % COLS;
+        const int r0 = M + (item / COLS) * SEG;
+        const int r1 = r0 + SEG < RH - M ? r0 + SEG : RH - M;
+        const float* p = hs + (r0 - 1) * RW + col;
+        Window v;
+        v.nw = p[-1], v.n = p[0], v.ne = p[1];
+        v.w = p[RW - 1], v.c = p[RW], v.e = p[RW + 1];
+        Window g{};
+        if (MOVE) {
+            const float* q = gv + (r0 - 1) * RW + col;
+            g.nw = q[-1], g.n = q[0], g.ne = q[1];
+            g.w = q[RW - 1], g.c = q[RW], g.e = q[RW + 1];
+        }
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int ry = r0 + k;
+            if (ry >= r1) break;
+            const float* below = hs + (ry + 1) * RW + col;
+            v.sw = below[-1], v.s = below[0], v.se = below[1];
+            if (MOVE) {
+                const float* gb = gv + (ry + 1) * RW + col;
+                g.sw = gb[-1], g.s = gb[0], g.se = gb[1];
             }
-            float g = 0.0f;
-            if (excess > a.settled) {
-                const float p = __fmul_rn(a.rate, excess), q = __fmul_rn(steepest, 0.5f);
-                g = __fdiv_rn(p <= q ? p : q, excess);
+            const int gy = y0 + ry;
+            const bool on = !EDGE || (gy >= 0 && gy < H);
+            const bool has_s = !EDGE || gy + 1 < H;
+            const bool has_n = !EDGE || gy - 1 >= 0;
+            if (on) {
+                if (MOVE) dst[ry * RW + col] = moved(v, g, has_s, has_n, a);
+                else gv[ry * RW + col] = give_rate(v, has_s, has_n, a);
             }
-            gv[c] = g;
+            v.nw = v.w, v.n = v.c, v.ne = v.e;
+            v.w = v.sw, v.c = v.s, v.e = v.se;
+            if (MOVE) {
+                g.nw = g.w, g.n = g.c, g.ne = g.e;
+                g.w = g.sw, g.c = g.s, g.e = g.se;
+            }
         }
     }
 }
 
-// The move pass: h' = h - given + received, over rows [m, RH - m) and columns [m, RW - m).
-template <int RW, int RH, bool EDGE>
-__device__ __forceinline__ void move_pass(const float* __restrict__ hs, const float* __restrict__ gv,
-                                          float* __restrict__ hn, int m, int y0, int H, const ThermalArgs& a) {
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int ry = m + ty; ry < RH - m; ry += 8) {
-        const int gy = y0 + ry;
-        if (EDGE && (gy < 0 || gy >= H)) continue;
-        for (int rx = m + tx; rx < RW - m; rx += 32) {
-            const int c = ry * RW + rx;
-            const float here = hs[c];
-            const float gc = gv[c];
-            float received = 0.0f, given = 0.0f;
-#pragma unroll
-            for (int n = 0; n < 8; ++n) {
-                const int rs = thermal_row_step(n), cs = thermal_col_step(n);
-                if (EDGE && (gy + rs < 0 || gy + rs >= H)) continue;
-                const float limit = a.limit[n];
-                const int nc = c + rs * RW + cs;
-                const float incoming = __fsub_rn(hs[nc], here);
-                if (incoming > limit) {
-                    received = __fadd_rn(received, __fmul_rn(gv[nc], __fsub_rn(incoming, limit)));
-                } else if (-incoming > limit) {
-                    given = __fadd_rn(given, __fmul_rn(gc, __fsub_rn(-incoming, limit)));
-                }
-            }
-            hn[c] = __fadd_rn(__fsub_rn(here, given), received);
-        }
+// K sweeps on the region in shared memory: hs holds the heights and ends with the result
+// (swapping with hn each sweep); the region's valid part shrinks by two cells a side per sweep.
+template <int RW, int RH, int K, bool EDGE>
+__device__ __forceinline__ float* sweeps(float* hs, float* hn, float* gv, int y0, int H, const ThermalArgs& a) {
+    pass<RW, RH, 1, false, EDGE>(hs, gv, nullptr, y0, H, a);
+    __syncthreads();
+    pass<RW, RH, 2, true, EDGE>(hs, gv, hn, y0, H, a);
+    __syncthreads();
+    if constexpr (K == 2) {
+        pass<RW, RH, 3, false, EDGE>(hn, gv, nullptr, y0, H, a);
+        __syncthreads();
+        pass<RW, RH, 4, true, EDGE>(hn, gv, hs, y0, H, a);
+        __syncthreads();
+        return hs;
+    } else {
+        return hn;
     }
 }
 
@@ -110,8 +172,6 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
     constexpr int RW = TX + 2 * HALO;   // region width
     constexpr int RH = TY + 2 * HALO;   // region height
     __shared__ float sm_a[RW * RH], sm_b[RW * RH], sm_g[RW * RH];
-    float* hs = sm_a;   // heights, current sweep
-    float* hn = sm_b;   // heights, next sweep
 
     const int tile = blockIdx.y * gridDim.x + blockIdx.x;
     if (fl.prev) {
@@ -137,24 +197,14 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
         const int gy = y0 + ry;
         const bool valid = gy >= 0 && gy < H;
         const float* rowp = in + (size_t)(valid ? gy : 0) * W;
-        for (int rx = tx; rx < RW; rx += 32) hs[ry * RW + rx] = valid ? rowp[wrap_col(x0 + rx, W)] : 0.0f;
+        for (int rx = tx; rx < RW; rx += 32) sm_a[ry * RW + rx] = valid ? rowp[wrap_col(x0 + rx, W)] : 0.0f;
     }
     __syncthreads();
 
-    // Every row of the region on the grid: no pole checks needed.
+    // Tiles whose region lies inside the grid's rows take the path without pole checks.
     const bool edge = y0 < 0 || y0 + RH > H;
-#pragma unroll 1
-    for (int s = 0; s < K; ++s) {
-        if (edge) give_pass<RW, RH, true>(hs, sm_g, 2 * s + 1, y0, H, a);
-        else give_pass<RW, RH, false>(hs, sm_g, 2 * s + 1, y0, H, a);
-        __syncthreads();
-        if (edge) move_pass<RW, RH, true>(hs, sm_g, hn, 2 * s + 2, y0, H, a);
-        else move_pass<RW, RH, false>(hs, sm_g, hn, 2 * s + 2, y0, H, a);
-        __syncthreads();
-        float* t = hs;
-        hs = hn;
-        hn = t;
-    }
+    const float* res = edge ? sweeps<RW, RH, K, true>(sm_a, sm_b, sm_g, y0, H, a)
+                            : sweeps<RW, RH, K, false>(sm_a, sm_b, sm_g, y0, H, a);
 
     int changed = 0;
     for (int yy = ty; yy < TY; yy += 8) {
@@ -164,7 +214,7 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
             const int gx = blockIdx.x * TX + xx;
             if (gx >= W) continue;
             const size_t idx = (size_t)gy * W + gx;
-            const float v = hs[(yy + HALO) * RW + xx + HALO];
+            const float v = res[(yy + HALO) * RW + xx + HALO];
             if (__float_as_uint(v) != __float_as_uint(in[idx])) changed = 1;
             out[idx] = v;
         }
@@ -185,7 +235,7 @@ cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs&
 
 ThermalArgs args_of(const ThermalLaunch& t) {
     ThermalArgs a;
-    for (int n = 0; n < 8; ++n) a.limit[n] = t.limit[n];
+    for (int n = 0; n < 8; ++n) a.limit[n] = t.limit[n], a.lim0[n] = t.limit[n] > 0.0f ? t.limit[n] : 0.0f;
     a.settled = t.settled;
     a.rate = t.rate;
     return a;
