@@ -38,87 +38,157 @@ constexpr long long LEVEL_ONE = 1LL << 32;
 
 __device__ __forceinline__ bool is_land_receiver(const uint8_t* land, int r) { return r >= 0 && land[r]; }
 
-__global__ void k_donor_count(const uint8_t* __restrict__ land, const int32_t* __restrict__ recv, size_t N,
-                              int32_t* __restrict__ donors) {
+// Neighbour directions in stencil order (rows -1..1, then columns -1..1, the cell itself left out).
+__device__ __forceinline__ int dir_row(int t) { return t < 3 ? -1 : (t < 5 ? 0 : 1); }
+__device__ __forceinline__ int dir_col(int t) { return t < 3 ? t - 1 : (t < 5 ? (t == 3 ? -1 : 1) : t - 6); }
+__device__ __forceinline__ int dir_of(int rs, int cs) { return (rs + 1) * 3 + (cs + 1) - ((rs > 0 || (rs == 0 && cs > 0)) ? 1 : 0); }
+__device__ __forceinline__ int step_to(int W, int c, int t) {
+    const int row = c / W, col = c % W;
+    return (row + dir_row(t)) * W + wrap_col(col + dir_col(t), W);
+}
+
+// The tree's links, one byte each per cell: down[c] the direction from c to its receiver when that
+// receiver is land (0xFF otherwise), and mask[r] bit t set when the neighbour of r in direction t
+// drains into r. The mask bytes are set with a 32-bit atomicOr on the word holding them.
+__global__ void k_links(const uint8_t* __restrict__ land, const int32_t* __restrict__ recv, int W, int H,
+                        uint8_t* __restrict__ down, uint8_t* __restrict__ mask) {
+    const size_t N = (size_t)W * H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (!land[i]) continue;
-        int r = recv[i];
-        if (is_land_receiver(land, r)) atomicAdd(&donors[r], 1);
+        uint8_t d = 0xFF;
+        if (land[i]) {
+            const int r = recv[i];
+            if (is_land_receiver(land, r)) {
+                const int c = (int)i;
+                int rs = r / W - c / W;
+                int cs = r % W - c % W;
+                if (cs > 1) cs -= W;
+                if (cs < -1) cs += W;
+                d = (uint8_t)dir_of(rs, cs);
+                const int up = dir_of(-rs, -cs);   // from r back to c
+                atomicOr(reinterpret_cast<unsigned*>(mask + (r & ~3)), 1u << (up + 8 * (r & 3)));
+            }
+        }
+        down[i] = d;
     }
 }
 
-__global__ void k_pending_init(const int32_t* __restrict__ donors, size_t N, int32_t* __restrict__ pending) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
-        pending[i] = donors[i];
+// Donor counts, the pending counts of the walk, and the list of land sources (cells no land cell
+// drains into), appended per warp; their order does not matter (the walk's results do not depend on
+// which thread reaches a cell first).
+__global__ void k_sources(const uint8_t* __restrict__ land, const uint8_t* __restrict__ mask, size_t N,
+                          int32_t* __restrict__ donors, int32_t* __restrict__ pending, int* __restrict__ sources,
+                          int* __restrict__ n_sources) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = blockIdx.x * (size_t)blockDim.x; base < N; base += stride) {
+        const size_t i = base + threadIdx.x;
+        bool src = false;
+        if (i < N) {
+            const int n = __popc((unsigned)mask[i]);
+            donors[i] = n;
+            pending[i] = n;
+            src = land[i] && n == 0;
+        }
+        const unsigned group = __ballot_sync(FULL, src);
+        if (group == 0) continue;
+        const int lane = threadIdx.x & 31;
+        int slot = 0;
+        if (lane == __ffs(group) - 1) slot = atomicAdd(n_sources, __popc(group));
+        slot = __shfl_sync(FULL, slot, __ffs(group) - 1);
+        if (src) sources[slot + __popc(group & ((1u << lane) - 1u))] = (int)i;
+    }
 }
 
 struct WalkArgs {
     int W, H;
-    const uint8_t* land;
-    const int32_t* recv;
-    const int32_t* donors;
+    const uint8_t* down;
+    const uint8_t* mask;
     int32_t* pending;
     long long* key;
     const float* weights;   // null: keys only
     float* area;
+    const int* sources;
+    const int* n_sources;
     unsigned long long* max_key;
 };
 
-// The cell's donors' keys, in key order; returns how many (at most 8).
-__device__ int sorted_donors(const WalkArgs& a, int r, long long* keys, int* cells) {
-    int row = r / a.W, col = r % a.W, n = 0;
-    for (int rs = -1; rs <= 1; ++rs) {
-        int nr = row + rs;
-        if (nr < 0 || nr >= a.H) continue;
-        for (int cs = -1; cs <= 1; ++cs) {
-            if (rs == 0 && cs == 0) continue;
-            int c = nr * a.W + wrap_col(col + cs, a.W);
-            if (!a.land[c] || a.recv[c] != r) continue;
-            long long k = *((volatile long long*)&a.key[c]);
-            int j = n++;
-            while (j > 0 && keys[j - 1] > k) {
-                keys[j] = keys[j - 1];
-                cells[j] = cells[j - 1];
-                --j;
-            }
-            keys[j] = k;
-            cells[j] = c;
-        }
-    }
-    return n;
-}
-
-__global__ void k_walk(WalkArgs a) {
-    size_t N = (size_t)a.W * a.H;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (!a.land[i] || a.donors[i] != 0) continue;
-        int c = (int)i;
-        long long k = (long long)c;   // a source: level 0, its own index
-        a.key[c] = k;
-        if (a.weights) a.area[c] = a.weights[c];
-        unsigned long long local_max = (unsigned long long)k;
+// One thread per source climbs down its receivers while it is the last donor into each. At a cell
+// r it already holds the key and area of the cell it came from; r's donor mask and weight are
+// loaded beside the atomic that decides whether it goes on, so a step costs the atomic and one
+// round of loads of the other donors' keys and areas.
+__global__ void __launch_bounds__(64) k_walk(WalkArgs a) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long local_max = 0;
+    if (idx < *a.n_sources) {
+        int c = a.sources[idx];
+        long long kc = (long long)c;   // a source: level 0, its own index
+        float ac = a.weights ? a.weights[c] : 0.0f;
+        a.key[c] = kc;
+        if (a.weights) a.area[c] = ac;
+        local_max = (unsigned long long)kc;
         while (true) {
-            int r = a.recv[c];
-            if (!is_land_receiver(a.land, r)) break;
+            const int d = a.down[c];
+            if (d == 0xFF) break;
+            const int r = step_to(a.W, c, d);
+            const unsigned m = a.mask[r];
+            const float wr = a.weights ? a.weights[r] : 0.0f;
             // Release: this cell's key and area are visible before its arrival is counted. Acquire:
             // the last donor in sees every other donor's.
             cuda::atomic_ref<int, cuda::thread_scope_device> pend(a.pending[r]);
             if (pend.fetch_sub(1, cuda::memory_order_acq_rel) != 1) break;   // not the last donor in
-            long long keys[8];
-            int cells[8];
-            int n = sorted_donors(a, r, keys, cells);
-            long long kr = keys[n - 1] + LEVEL_ONE;
-            a.key[r] = kr;
-            if (a.weights) {
-                float s = a.weights[r];
-                for (int j = 0; j < n; ++j) s = __fadd_rn(s, *((volatile float*)&a.area[cells[j]]));
-                a.area[r] = s;
+            // The donors' keys and areas (the cell just left from registers). Keys are distinct, so
+            // each donor's rank is the number of smaller keys; the areas are added in rank order.
+            long long kt[8];
+            float at[8];
+            long long kmax = LLONG_MIN;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                kt[t] = LLONG_MAX;
+                at[t] = 0.0f;
+                if (!(m & (1u << t))) continue;
+                const int dn = step_to(a.W, r, t);
+                if (dn == c) {
+                    kt[t] = kc;
+                    at[t] = ac;
+                } else {
+                    kt[t] = *((volatile long long*)&a.key[dn]);
+                    if (a.weights) at[t] = *((volatile float*)&a.area[dn]);
+                }
+                kmax = kt[t] > kmax ? kt[t] : kmax;
             }
-            if ((unsigned long long)kr > local_max) local_max = (unsigned long long)kr;
+            kc = kmax + LEVEL_ONE;
+            a.key[r] = kc;
+            if (a.weights) {
+                int rank[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    rank[t] = 0;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) rank[t] += (kt[u] < kt[t]) ? 1 : 0;
+                }
+                const int n = __popc(m);
+                float sum = wr;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (j >= n) break;
+                    float pick = 0.0f;
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) pick = rank[t] == j && (m & (1u << t)) ? at[t] : pick;
+                    sum = __fadd_rn(sum, pick);
+                }
+                ac = sum;
+                a.area[r] = sum;
+            }
+            if ((unsigned long long)kc > local_max) local_max = (unsigned long long)kc;
             c = r;
         }
-        atomicMax(a.max_key, local_max);
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(FULL, local_max, o);
+        if (other > local_max) local_max = other;
+    }
+    if ((threadIdx.x & 31) == 0 && local_max) atomicMax(a.max_key, local_max);
 }
 
 // Areas of land cells are the weights where no walk reached (sea cells hold 0).
@@ -372,13 +442,23 @@ cg_status tree_walk_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const 
     int grid = ctx->num_sms * 8;
     CG_BUF(int32_t, d_pending, ctx, S_DEPTH, N);
     CG_BUF(unsigned long long, d_max, ctx, S_STATS, 1);
-    CG_CUDA(ctx, cudaMemsetAsync(d_donors, 0, N * sizeof(int32_t), sm));
+    CG_BUF(uint8_t, d_links, ctx, S_LINKS, 2 * N);
+    CG_BUF(int, d_sources, ctx, S_SOURCES, N + 1);
+    uint8_t* d_down = d_links;
+    uint8_t* d_mask = d_links + N;
+    int* d_nsrc = d_sources + N;
+    CG_CUDA(ctx, cudaMemsetAsync(d_mask, 0, N, sm));
+    CG_CUDA(ctx, cudaMemsetAsync(d_nsrc, 0, sizeof(int), sm));
     CG_CUDA(ctx, cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), sm));
-    CG_LAUNCH(ctx) k_donor_count<<<grid, 256, 0, sm>>>(d_land, d_recv, N, d_donors);
-    CG_LAUNCH(ctx) k_pending_init<<<grid, 256, 0, sm>>>(d_donors, N, d_pending);
+    CG_LAUNCH(ctx) k_links<<<grid, 256, 0, sm>>>(d_land, d_recv, W, H, d_down, d_mask);
+    CG_LAUNCH(ctx) k_sources<<<grid, 256, 0, sm>>>(d_land, d_mask, N, d_donors, d_pending, d_sources, d_nsrc);
     if (d_area) CG_LAUNCH(ctx) k_area_sea<<<grid, 256, 0, sm>>>(d_land, N, d_area);
-    WalkArgs a{W, H, d_land, d_recv, d_donors, d_pending, d_key, d_weights, d_area, d_max};
-    CG_LAUNCH(ctx) k_walk<<<grid, 128, 0, sm>>>(a);
+    CG_CHECK_LAUNCH(ctx);
+    int n_sources = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&n_sources, d_nsrc, sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    WalkArgs a{W, H, d_down, d_mask, d_pending, d_key, d_weights, d_area, d_sources, d_nsrc, d_max};
+    if (n_sources > 0) CG_LAUNCH(ctx) k_walk<<<(n_sources + 63) / 64, 64, 0, sm>>>(a);
     CG_CHECK_LAUNCH(ctx);
     if (h_levels) {
         unsigned long long mk;
