@@ -71,17 +71,48 @@ __device__ __forceinline__ int neighbour_at(int W, int H, int col, int row) {
 }
 
 // x / d, skipping the division by a leg of exactly one cell width (x / 1.0 is x in IEEE arithmetic).
-__device__ __forceinline__ double div_leg(double x, double d) { return d == 1.0 ? x : __ddiv_rn(x, d); }
+__device__ __forceinline__ double div_leg(double x, double d) {
+    return __double_as_longlong(d) == 0x3FF0000000000000LL ? x : __ddiv_rn(x, d);
+}
 
-// FlowRouting.facetReceiver (FlowRouting.kt:223-310), with the same values in fewer FP64 operations
-// (GB300's FP64 rate is a small fraction of its FP32 rate):
+// Comparisons of doubles on the integer pipes (GB300 issues FP64 instructions, compares included,
+// at a small fraction of its integer rate). For values that are not NaN, dkey maps a double to a
+// signed integer in IEEE order, with -0 and +0 equal; x > 0 is the sign-and-magnitude test.
+__device__ __forceinline__ long long dkey(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : -(b & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ bool dpos(double x) { return __double_as_longlong(x) > 0; }
+
+// Exact early outs for a facet's slope against the steepest so far (steepest >= 0). A correctly
+// rounded result can exceed steepest only if the exact one does: for fl(sqrt(s)) that needs
+// s > steepest^2, for fl(df / dg) (dg > 0) df > steepest * dg. Each exact product q lies within half
+// a unit in the last place of its rounded value t, hence above the double just below t, so a value
+// at or below that double is below q and its slope cannot win. Non-negative doubles order as their
+// bit patterns, and the double just below a positive t has the bit pattern of t minus one.
+__device__ __forceinline__ bool sqrt_cannot_win(double s, double steepest) {
+    const long long t = __double_as_longlong(__dmul_rn(steepest, steepest));
+    return t > 0 ? __double_as_longlong(s) <= t - 1 : __double_as_longlong(s) == 0;
+}
+__device__ __forceinline__ bool ratio_cannot_win(double df, double dg, double steepest) {
+    if (!dpos(df)) return true;   // df / dg <= 0 <= steepest
+    const long long t = __double_as_longlong(__dmul_rn(steepest, dg));
+    return t > 0 && __double_as_longlong(df) <= t - 1;
+}
+
+// FlowRouting.facetReceiver (FlowRouting.kt:223-310), with the same values in fewer FP64 operations:
 //  - a cardinal's slope is shared by its two facets and a diagonal's by its two facets, so each is
-//    computed once, and a diagonal's only if a facet is clamped to it;
+//    computed once, and a diagonal's only if a facet is clamped to it and could be the steepest;
+//  - an inside facet's square root is taken only if its slope could be the steepest (the early
+//    outs above), and comparisons run on the integer pipes;
 //  - the share along the far edge, a / b with a = outward tc^2 and b = cdrop od^2 (rounded products,
 //    as the reference forms them), is compared with 1 as a >= b: for positive doubles fl(a/b) >= 1
 //    exactly when a >= b, since a < b puts a/b at or below the double just under 1. The division is
-//    taken once, for the winning facet, whose share the draw is compared with.
+//    taken once, for the winning facet, whose share the draw is compared with;
+//  - UNIT: both legs are exactly one cell width (square cells), so the products and quotients by a
+//    leg are the values themselves.
 // Facets are visited and compared in the reference's order, so ties resolve identically.
+template <bool UNIT>
 __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int col, int row, Steps st, long long seed) {
     const int ccs_t[4] = {1, 0, -1, 0};
     const int crs_t[4] = {0, -1, 0, 1};
@@ -92,6 +123,7 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
     double dslope[4];
     bool dslope_done[4] = {false, false, false, false};
     int dcell[4];
+#pragma unroll
     for (int k = 0; k < 4; ++k) {
         int dcs = (k & 1) ? 1 : -1, drs = (k & 2) ? 1 : -1;
         dcell[k] = neighbour_at(W, H, col + dcs, row + drs);
@@ -101,6 +133,7 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
     int fcard = -1, fdiag = -1;
     int mode = 0;   // 0: cardinal, 1: diagonal, 2: inside the facet (share a / b)
     double wa = 0.0, wb = 0.0;
+#pragma unroll
     for (int side = 0; side < 4; ++side) {
         const int ccs = ccs_t[side], crs = crs_t[side];
         const int card = neighbour_at(W, H, col + ccs, row + crs);
@@ -108,7 +141,9 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
         const double cdrop = __dsub_rn(here, rs[card]);
         const double to_card = ccs != 0 ? ew : ns;     // GroundSteps.of(ccs, crs): never a diagonal here
         const double on_to_diag = ccs == 0 ? ew : ns;
-        const double cslope = div_leg(cdrop, to_card);
+        const double cslope = UNIT ? cdrop : div_leg(cdrop, to_card);
+        const bool cdown = dpos(cdrop);
+#pragma unroll
         for (int turn = -1; turn <= 1; turn += 2) {
             const int dcs = ccs == 0 ? turn : ccs;
             const int drs = crs == 0 ? turn : crs;
@@ -116,34 +151,44 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
             if (dcell[k] < 0) continue;
             const double df = dfall[k];
             const double outward = __dsub_rn(df, cdrop);
-            const bool to_cardinal = cdrop > 0.0 && outward <= 0.0;
-            double a = 0.0, b = 0.0, fslope;
+            double a = 0.0, b = 0.0;
+            bool wins;
             int m;
-            if (to_cardinal) {
-                fslope = cslope;
+            if (cdown && !dpos(outward)) {   // to the cardinal
+                wins = dkey(cslope) > dkey(steepest);
+                if (wins) steepest = cslope;
                 m = 0;
             } else {
                 bool to_diagonal = true;   // share 1 when the cardinal is not downhill
-                if (cdrop > 0.0) {
-                    a = __dmul_rn(__dmul_rn(outward, to_card), to_card);
-                    b = __dmul_rn(__dmul_rn(cdrop, on_to_diag), on_to_diag);
-                    to_diagonal = a >= b;
+                if (cdown) {
+                    a = UNIT ? outward : __dmul_rn(__dmul_rn(outward, to_card), to_card);
+                    b = UNIT ? cdrop : __dmul_rn(__dmul_rn(cdrop, on_to_diag), on_to_diag);
+                    to_diagonal = dkey(a) >= dkey(b);
                 }
                 if (to_diagonal) {
-                    if (!dslope_done[k]) {
-                        dslope[k] = __ddiv_rn(df, dg);
-                        dslope_done[k] = true;
+                    wins = false;
+                    if (dslope_done[k] || !ratio_cannot_win(df, dg, steepest)) {
+                        if (!dslope_done[k]) {
+                            dslope[k] = __ddiv_rn(df, dg);
+                            dslope_done[k] = true;
+                        }
+                        wins = dkey(dslope[k]) > dkey(steepest);
+                        if (wins) steepest = dslope[k];
                     }
-                    fslope = dslope[k];
                     m = 1;
                 } else {
-                    const double oslope = div_leg(outward, on_to_diag);
-                    fslope = __dsqrt_rn(__dadd_rn(__dmul_rn(cslope, cslope), __dmul_rn(oslope, oslope)));
+                    const double oslope = UNIT ? outward : div_leg(outward, on_to_diag);
+                    const double sq = __dadd_rn(__dmul_rn(cslope, cslope), __dmul_rn(oslope, oslope));
+                    wins = false;
+                    if (!sqrt_cannot_win(sq, steepest)) {
+                        const double fslope = __dsqrt_rn(sq);
+                        wins = dkey(fslope) > dkey(steepest);
+                        if (wins) steepest = fslope;
+                    }
                     m = 2;
                 }
             }
-            if (fslope > steepest) {
-                steepest = fslope;
+            if (wins) {
                 fcard = card;
                 fdiag = dcell[k];
                 mode = m;
@@ -152,14 +197,14 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
             }
         }
     }
-    if (steepest <= 0.0) return -1;
+    if (!dpos(steepest)) return -1;
     if (mode == 0) return fcard;
     if (mode == 1) return fdiag;
     const double share = __ddiv_rn(wa, wb);
-    if (share <= 0.0) return fcard;
+    if (!dpos(share)) return fcard;
     // FlowRouting.subGridDraw (FlowRouting.kt:355-356).
     const double draw = (double)__fmul_rn(__fadd_rn(seeded_noise(col, row, seed ^ kSubGridDrawSalt), 1.0f), 0.5f);
-    return draw < share ? fdiag : fcard;
+    return dkey(draw) < dkey(share) ? fdiag : fcard;
 }
 
 // FlowRouting.steepestNeighbourOf (FlowRouting.kt:320-343).
@@ -192,8 +237,10 @@ __global__ void k_receivers(const uint8_t* __restrict__ land, const double* __re
             continue;
         }
         int row = (int)(i / W), col = (int)(i - (size_t)row * W);
-        recv[i] = by_facet ? facet_receiver(W, H, surface, col, row, st, seed)
-                           : steepest_neighbour(W, H, surface, col, row, st);
+        const bool unit = st.ew == 1.0f && st.ns == 1.0f;
+        recv[i] = !by_facet ? steepest_neighbour(W, H, surface, col, row, st)
+                  : unit    ? facet_receiver<true>(W, H, surface, col, row, st, seed)
+                            : facet_receiver<false>(W, H, surface, col, row, st, seed);
     }
 }
 

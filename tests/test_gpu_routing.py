@@ -121,10 +121,11 @@ def test_fill_bench_world_8192x4096():
 
 @pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
 @pytest.mark.parametrize("by_facet,over_potential", [(True, True), (True, False), (False, False)])
-def test_flow_directions(W, H, seed, by_facet, over_potential):
+@pytest.mark.parametrize("r", [0.5, 1.0])
+def test_flow_directions(W, H, seed, by_facet, over_potential, r):
+    """r = 1.0 is the square-cell case of a 2:1 world (both legs one cell width)."""
     _, (s, land, rel, n) = world_cut(W, H, seed)
     filled = oracle.fill_depressions(land, rel)
-    r = 0.5 if W == 2 * H else 1.0
     want, wsurf, wc = oracle.flow_directions(land, rel, filled, seed, r, 214, by_facet, over_potential,
                                              want_surface=True)
     got, gsurf, gc = FlowRouting.flow_directions(land, rel, filled, seed, r, 214, by_facet, over_potential,
@@ -133,6 +134,24 @@ def test_flow_directions(W, H, seed, by_facet, over_potential):
     np.testing.assert_allclose(gsurf, wsurf, rtol=SURFACE_RTOL, atol=0)
     diff = np.flatnonzero(got != want)
     assert diff.size == 0, f"{diff.size} receivers differ: {diff[:8]}"
+
+
+@pytest.mark.parametrize("r", [1.0, 0.5, 1.75])
+@pytest.mark.parametrize("step", [1.0 / 64, 1.0 / 1024])
+def test_flow_directions_quantised_ties(r, step):
+    """Heights on a coarse lattice, so facets tie on slope, cardinals on drop and shares sit on 1:
+    the facet rule's comparisons and early outs must pick the reference's receiver at every tie."""
+    W, H, seed = 256, 128, 17
+    h, up, rk = synthetic.world(W, H, seed)
+    s, land, rel, n = oracle.percentile_cut(h, 0.55)
+    rel = (np.round(rel / step) * step).astype(np.float32)
+    filled = oracle.fill_depressions(land, rel)
+    for over_potential in (False, True):
+        want, wc = oracle.flow_directions(land, rel, filled, seed, r, 214, True, over_potential)
+        got, gc = FlowRouting.flow_directions(land, rel, filled, seed, r, 214, True, over_potential)
+        assert list(wc) == list(gc)
+        diff = np.flatnonzero(got != want)
+        assert diff.size == 0, f"{diff.size} receivers differ: {diff[:8]}"
 
 
 @pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
