@@ -5,8 +5,8 @@
 // where the potential of a Poisson problem is laid into the band between the flat's highest entry
 // and its lowest raised level. Flats are 8-connected components of raised cells and never touch one
 // another, so each is solved on its own: a warp per flat of up to 32 members (nearly all of them: the
-// fill's small depressions), a CTA per larger flat, with the solver's vectors in shared memory up to
-// 4096 members (128 threads to 512 members, 512 threads above) and in global memory beyond:
+// fill's small depressions), a CTA per flat of up to 512 members and a cluster of 8 CTAs per flat of
+// up to 16384, with the solver's vectors in shared memory, and in global memory beyond:
 //  - members are ordered by (column, row), so each column run is a contiguous segment and the
 //    reduction order is fixed (results are deterministic run to run);
 //  - each member's weighted degree and its Laplacian row are accumulated in the reference's
@@ -17,7 +17,9 @@
 //    intermediate, laid into a band whose order the receivers read).
 // The facet rule (Tarboton's D-infinity facets on ground-true legs, then the Rho8 draw from the
 // SplitMix64 cell hash) is a per-cell stencil in double, bit-exact.
+#include <algorithm>
 #include <cfloat>
+#include <cooperative_groups.h>
 #include <climits>
 
 #include "cg_common.cuh"
@@ -581,7 +583,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     lay_in_band(a, mem, n, a.x + base, positive, highest, entry_level, entry_height, shi);
 }
 
-// Flats of 33 to 4096 members, one CTA each, with the CG's working vectors in shared memory.
+// Flats of 33 to 512 members, one CTA each, with the CG's working vectors in shared memory.
 // A CG iteration is latency-bound: the column runs' Thomas solves are chains of dependent
 // divisions, one run per thread, and a valley floor can hold runs hundreds of cells long, so a
 // chain that goes through L2 at every step costs most of the iteration. Here r, z, d, A d, the
@@ -591,7 +593,6 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
 // each thread's partial sum in member order, a warp butterfly and an ordered sum over the warps,
 // so its bits are fixed for a given CTA size.
 constexpr int MID_FLAT = 512;    // members at most for the 128-thread CTA
-constexpr int BIG_FLAT = 4096;   // members at most for the 512-thread CTA; k_flat_solve takes larger flats
 constexpr int SM_BYTES_PER_MEMBER = 6 * 8 + 4;   // six doubles and one run-table entry
 
 // Sums of u and of v over the CTA, returned to every thread. `buf` (one double2 per warp) must
@@ -810,6 +811,320 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
     lay_in_band(a, mem, n, x, positive, highest, entry_level, entry_height, shi);
 }
 
+// Flats of 513 to CL_FLAT members, one thread-block cluster of CL CTAs each. On GB300 a CG
+// iteration of a large flat is bound by one SM's FP64 pipe, so the flat's members are split over
+// the cluster's SMs: CTA q owns the members [bound[q], bound[q + 1]), bounds placed at column-run
+// heads so that every Thomas chain stays in one CTA. Each CTA keeps its members' vectors in its own
+// shared memory; the Laplacian reads a neighbour owned by another CTA from that CTA's shared memory
+// (distributed shared memory), and every dot product is a CTA partial (as in k_flat_solve_sm) sent
+// to all CTAs of the cluster and summed there in rank order, so each CTA holds the same bits. A flat
+// whose ranges do not fit the shared memory this launch was given (a column run longer than the
+// slack) is handed to k_flat_solve, through its list.
+constexpr int CL = 8;                          // CTAs per cluster
+constexpr int CL_THREADS = 256;
+constexpr int CL_FLAT = 16384;                 // members at most for the cluster kernel
+constexpr int CL_RANGE_MAX = 8191;             // members per CTA: the neighbour code keeps 13 bits of offset
+
+namespace cgc = cooperative_groups;
+
+struct Sum2 {
+    __device__ double2 operator()(double2 a, double2 b) const { return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)); }
+};
+struct MinMax2 {
+    __device__ double2 operator()(double2 a, double2 b) const {
+        return make_double2(a.x < b.x ? a.x : b.x, a.y > b.y ? a.y : b.y);
+    }
+};
+
+// The CTA's combination of (u, v) (a warp butterfly, then the warps in order), sent to slot q of
+// every CTA's `slots[par]`; after the cluster barrier each CTA combines the CL slots in rank order.
+// `par` alternates between calls, as for block_sum2.
+template <class Op>
+__device__ double2 cluster_combine(double2 v, Op op, double2* warps, double2 (*slots)[CL], int& par, int q) {
+    constexpr int NW = CL_THREADS / 32;
+    for (int o = 16; o > 0; o >>= 1) {
+        double2 t;
+        t.x = __shfl_xor_sync(0xFFFFFFFFu, v.x, o);
+        t.y = __shfl_xor_sync(0xFFFFFFFFu, v.y, o);
+        v = op(v, t);
+    }
+    if ((threadIdx.x & 31) == 0) warps[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < CL) {
+        double2 s = warps[0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) s = op(s, warps[w]);
+        double2* dst = cgc::this_cluster().map_shared_rank(&slots[par][q], (int)threadIdx.x);
+        *dst = s;
+    }
+    cgc::this_cluster().sync();
+    double2 s = slots[par][0];
+#pragma unroll
+    for (int r = 1; r < CL; ++r) s = op(s, slots[par][r]);
+    par ^= 1;
+    return s;
+}
+
+// A member neighbour as owner rank (3 bits) and offset in the owner's range (13 bits); 0xFFFF is
+// none (an offset is at most CL_RANGE_MAX - 1, so rank 7 never packs to it).
+constexpr int CL_NONE = 0xFFFF;
+__device__ __forceinline__ int cl_lo(int v) { return v & 0xFFFF; }
+__device__ __forceinline__ int cl_hi(int v) { return (int)((unsigned)v >> 16); }
+__device__ __forceinline__ int cl_pack(const int* bound, int l) {
+    if (l < 0) return -1;
+    int r = 0;
+#pragma unroll
+    for (int t = 1; t < CL; ++t) r = l >= bound[t] ? t : r;
+    return (r << 13) | (l - bound[r]);
+}
+
+template <bool UNITW>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
+    k_flat_solve_cl(FlatArgs a, const int* __restrict__ list, int range_cap, int* __restrict__ spill_list,
+                    int* __restrict__ spill_count) {
+    constexpr int FT = CL_THREADS;
+    extern __shared__ double dyn[];
+    __shared__ double2 warps[FT / 32];
+    __shared__ double2 slots[2][CL];
+    __shared__ int bound[CL + 1];
+    __shared__ int s_nruns;
+    __shared__ double* s_dptr[CL];
+    cgc::cluster_group cluster = cgc::this_cluster();
+    const int q = (int)cluster.block_rank();
+    const int f = list[blockIdx.x / CL];
+    const int base = a.off[f];
+    const int n = a.count[f];
+    const int W = a.W, H = a.H;
+    int* mem = a.members + base;
+    int par = 0;
+
+    // Members by (column, row), sorted by the first CTA.
+    if (q == 0) {
+        for (int k = threadIdx.x; k < n; k += FT) {
+            int c = mem[k];
+            mem[k] = (c % W) * H + c / W;
+        }
+        __syncthreads();
+        sort_members(mem, n);
+        for (int k = threadIdx.x; k < n; k += FT) {
+            int key = mem[k];
+            mem[k] = (key % H) * W + key / H;
+        }
+    }
+    cluster.sync();
+    // Range bounds: the first run head at or after q n / CL (every CTA computes all of them).
+    if (threadIdx.x <= CL) {
+        int t = (int)((long long)n * threadIdx.x / CL);
+        while (t < n && !run_head(mem, t, W)) ++t;
+        bound[threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) s_nruns = 0;
+    __syncthreads();
+    int widest = 0;
+    for (int r = 0; r < CL; ++r) widest = max(widest, bound[r + 1] - bound[r]);
+    if (widest > range_cap) {   // the same decision in every CTA, before any shared memory is shared
+        if (q == 0 && threadIdx.x == 0) spill_list[atomicAdd(spill_count, 1)] = f;
+        return;
+    }
+    const int lo = bound[q], m = bound[q + 1] - lo;
+    // d first: the other CTAs read it at the same offset in this CTA's shared memory.
+    double* s_d = dyn;
+    double* s_r = s_d + m;
+    double* s_z = s_r + m;
+    double* s_ad = s_z + m;
+    double* s_piv = s_ad + m;
+    double* s_coef = s_piv + m;
+    unsigned* s_run = reinterpret_cast<unsigned*>(s_coef + m);   // first | last << 16, CTA-local
+    if (threadIdx.x < CL) s_dptr[threadIdx.x] = cluster.map_shared_rank(s_d, (int)threadIdx.x);
+    double* x = a.x + base + lo;
+    double* degree = a.degree + base + lo;
+    int4* nbr = reinterpret_cast<int4*>(a.nbr + (size_t)(base + lo) * 8);
+    for (int j = threadIdx.x; j < m; j += FT) a.local[mem[lo + j]] = lo + j;
+    cluster.sync();   // every member's index is in place
+
+    // Entry level and highest entry (FlatRouting.kt:93-115, 427-445), degrees, member neighbours and
+    // the rain (:239-295), as k_flat_solve_sm does for its members.
+    float lo_f = FLT_MAX;
+    for (int j = threadIdx.x; j < m; j += FT) lo_f = fminf(lo_f, a.filled[mem[lo + j]]);
+    const double entry_level =
+        cluster_combine(make_double2((double)lo_f, 0.0), MinMax2(), warps, slots, par, q).x;
+    double hi = -INFINITY;
+    for (int j = threadIdx.x; j < m; j += FT) {
+        const int k = lo + j;
+        const int cell = mem[k];
+        const int col = cell % W, row = cell / W;
+        double total = 0.0;
+        int nb8[8];
+        int t = 0;
+        for (int rs = -1; rs <= 1; ++rs) {
+            const int nr = row + rs;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                nb8[t] = -1;
+                if (nr >= 0 && nr < H) {
+                    const int nb = nr * W + wrap_col(col + cs, W);
+                    const double w = stencil_weight(a, cs, rs);
+                    const int l = a.local[nb];
+                    if (l >= 0) {
+                        total = __dadd_rn(total, w);
+                        nb8[t] = cl_pack(bound, l);
+                    } else {
+                        const double there = a.surface[nb];
+                        if (there < entry_level) {
+                            total = __dadd_rn(total, w);
+                            if (there > hi) hi = there;
+                        }
+                    }
+                }
+                ++t;
+            }
+        }
+        degree[j] = total;
+        x[j] = 0.0;
+        nbr[j] = make_int4(nbr_pack(nb8[0], nb8[1]), nbr_pack(nb8[2], nb8[3]), nbr_pack(nb8[4], nb8[5]),
+                           nbr_pack(nb8[6], nb8[7]));
+        s_r[j] = __dadd_rn(1.0, __dmul_rn(0.5, (double)smooth_seeded_field(W, a.lattice, col, row,
+                                                                             a.seed ^ kRainReliefSalt)));
+        if (run_head(mem, k, W)) {
+            int e = k;
+            while (run_continues(mem, n, e, W, H)) ++e;
+            s_run[atomicAdd(&s_nruns, 1)] = (unsigned)j | ((unsigned)(e - lo) << 16);
+        }
+    }
+    const double entry_height = cluster_combine(make_double2(0.0, hi), MinMax2(), warps, slots, par, q).y;
+    const int runs = s_nruns;
+
+    // Thomas pivots down each run (FlatRouting.kt:388-395) and ns / pivot for the way back up.
+    for (int i = threadIdx.x; i < runs; i += FT) {
+        const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
+        double p = degree[first];
+        for (int j = first;; ++j) {
+            s_piv[j] = p;
+            s_coef[j] = __ddiv_rn(a.ns, p);
+            if (j == last) break;
+            p = __dsub_rn(degree[j + 1], __ddiv_rn(UNITW ? 1.0 : __dmul_rn(a.ns, a.ns), p));
+        }
+    }
+    __syncthreads();
+
+    auto precondition = [&]() {
+        for (int i = threadIdx.x; i < runs; i += FT) {
+            const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
+            double v = __ddiv_rn(__dadd_rn(s_r[first], 0.0), s_piv[first]);
+            s_z[first] = v;
+            for (int j = first + 1; j <= last; ++j) {
+                v = __ddiv_rn(__dadd_rn(s_r[j], UNITW ? v : __dmul_rn(a.ns, v)), s_piv[j]);
+                s_z[j] = v;
+            }
+            double below = v;
+            for (int j = last - 1; j >= first; --j) {
+                below = __dadd_rn(s_z[j], __dmul_rn(s_coef[j], below));
+                s_z[j] = below;
+            }
+        }
+    };
+    const double w8[8] = {a.diag, a.ns, a.diag, a.ew, a.ew, a.diag, a.ns, a.diag};   // stencil order
+
+    // Preconditioned conjugate gradients (FlatRouting.kt:296-333).
+    precondition();
+    __syncthreads();
+    double rn = 0.0, ra = 0.0;
+    for (int j = threadIdx.x; j < m; j += FT) {
+        const double rv = s_r[j], zv = s_z[j];
+        s_d[j] = zv;
+        rn = __dadd_rn(rn, __dmul_rn(rv, rv));
+        ra = __dadd_rn(ra, __dmul_rn(rv, zv));
+    }
+    double2 sums = cluster_combine(make_double2(rn, ra), Sum2(), warps, slots, par, q);   // also publishes d
+    double rnorm = sums.x, rap = sums.y;
+    const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
+    const int most = 64 + (int)(8.0 * sqrt((double)n));
+    for (int it = 0; rnorm > stop_at && it < most; ++it) {
+        double e = 0.0;
+        for (int j = threadIdx.x; j < m; j += FT) {
+            const int4 qv = nbr[j];
+            const int l8[8] = {cl_lo(qv.x), cl_hi(qv.x), cl_lo(qv.y), cl_hi(qv.y),
+                               cl_lo(qv.z), cl_hi(qv.z), cl_lo(qv.w), cl_hi(qv.w)};
+            const double dk = s_d[j];
+            double sum = __dmul_rn(degree[j], dk);
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                if (l8[t] == CL_NONE) continue;
+                const int owner = l8[t] >> 13, off = l8[t] & 8191;
+                const double dn = owner == q ? s_d[off] : s_dptr[owner][off];
+                sum = __dsub_rn(sum, UNITW ? dn : __dmul_rn(w8[t], dn));
+            }
+            s_ad[j] = sum;
+            e = __dadd_rn(e, __dmul_rn(dk, sum));
+        }
+        const double energy = cluster_combine(make_double2(e, 0.0), Sum2(), warps, slots, par, q).x;
+        if (energy <= 0.0 || rap <= 0.0) break;
+        const double step = __ddiv_rn(rap, energy);
+        for (int j = threadIdx.x; j < m; j += FT) {
+            x[j] = __dadd_rn(x[j], __dmul_rn(step, s_d[j]));
+            s_r[j] = __dsub_rn(s_r[j], __dmul_rn(step, s_ad[j]));
+        }
+        __syncthreads();
+        precondition();
+        __syncthreads();
+        double nn = 0.0, na = 0.0;
+        for (int j = threadIdx.x; j < m; j += FT) {
+            const double rv = s_r[j];
+            nn = __dadd_rn(nn, __dmul_rn(rv, rv));
+            na = __dadd_rn(na, __dmul_rn(rv, s_z[j]));
+        }
+        sums = cluster_combine(make_double2(nn, na), Sum2(), warps, slots, par, q);
+        const double improvement = __ddiv_rn(sums.y, rap);
+        for (int j = threadIdx.x; j < m; j += FT) s_d[j] = __dadd_rn(s_z[j], __dmul_rn(improvement, s_d[j]));
+        cluster.sync();   // every CTA's new d before the next Laplacian reads it
+        rnorm = sums.x;
+        rap = sums.y;
+    }
+    int positive = 1;
+    double top = 0.0;
+    for (int j = threadIdx.x; j < m; j += FT) {
+        const double v = x[j];
+        if (!(v > 0.0)) positive = 0;
+        if (v > top) top = v;
+    }
+    const double2 pt = cluster_combine(make_double2(positive ? 1.0 : 0.0, top), MinMax2(), warps, slots, par, q);
+    const double highest = pt.y;
+
+    // FlatRouting.layInBand (FlatRouting.kt:455-489) over the cluster.
+    bool laid = pt.x > 0.0 && !(highest <= 0.0 || entry_height >= entry_level);
+    if (laid) {
+        const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
+        for (int j = threadIdx.x; j < m; j += FT)
+            a.surface[mem[lo + j]] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(x[j], highest)));
+        cluster.sync();
+        double ok = 1.0;
+        for (int j = threadIdx.x; j < m; j += FT) {
+            const int cell = mem[lo + j];
+            const int col = cell % W, row = cell / W;
+            const double here = a.surface[cell];
+            bool lower = false;
+            for (int rs = -1; rs <= 1 && !lower; ++rs) {
+                const int nr = row + rs;
+                if (nr < 0 || nr >= H) continue;
+                for (int cs = -1; cs <= 1; ++cs) {
+                    if (cs == 0 && rs == 0) continue;
+                    if (a.surface[nr * W + wrap_col(col + cs, W)] < here) {
+                        lower = true;
+                        break;
+                    }
+                }
+            }
+            if (!lower) ok = 0.0;
+        }
+        ok = cluster_combine(make_double2(ok, 0.0), MinMax2(), warps, slots, par, q).x;
+        if (ok <= 0.0) {
+            for (int j = threadIdx.x; j < m; j += FT) a.surface[mem[lo + j]] = (double)a.filled[mem[lo + j]];
+            laid = false;
+        }
+    }
+    if (!laid && q == 0 && threadIdx.x == 0) atomicAdd(a.kept, 1);
+}
+
 // Flats of at most 32 members, one warp each (most flats are a few cells: the fill's small
 // depressions). Each lane owns one member; the per-member arithmetic (degree, Laplacian row, the
 // column runs' Thomas solves) is the reference's, done by the member's lane or the run head's lane;
@@ -1006,14 +1321,14 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
     if (!laid && lane == 0) atomicAdd(a.kept, 1);
 }
 
-// The flats of more than 32 members, listed by the CTA kernel that takes them: lists[0] the
-// 128-thread shared-memory kernel, lists[1] the 512-thread one, lists[2] k_flat_solve. ctr[0..2]
-// count the lists, ctr[3..4] hold the largest flat of the first two (their shared-memory size).
+// The flats of more than 32 members, listed by the kernel that takes them: lists[0] the 128-thread
+// shared-memory kernel, lists[1] the cluster kernel, lists[2] k_flat_solve. ctr[0..2] count the
+// lists, ctr[3..4] hold the largest flat of the first two (their shared-memory size).
 __global__ void k_flat_lists(const int* __restrict__ count, int flats, int* __restrict__ lists, int* __restrict__ ctr) {
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < flats; f += gridDim.x * blockDim.x) {
         const int n = count[f];
         if (n <= 32) continue;
-        const int c = n <= MID_FLAT ? 0 : n <= BIG_FLAT ? 1 : 2;
+        const int c = n <= MID_FLAT ? 0 : n <= CL_FLAT ? 1 : 2;
         lists[(size_t)c * flats + atomicAdd(&ctr[c], 1)] = f;
         if (c < 2) atomicMax(&ctr[3 + c], n);
     }
@@ -1107,11 +1422,18 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
                     a, d_lists);
             CG_CHECK_LAUNCH(ctx);
             if (ctr[1] > 0) {
-                const size_t bytes = (size_t)ctr[4] * SM_BYTES_PER_MEMBER;
-                CG_CUDA(ctx, cudaFuncSetAttribute(k_flat_solve_sm<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)bytes));
-                CG_LAUNCH(ctx) k_flat_solve_sm<512><<<ctr[1], 512, bytes, sm>>>(a, d_lists + flats);
+                // Per CTA a share of the largest flat with room for the run-head rounding of its bounds;
+                // a flat whose ranges need more goes to k_flat_solve.
+                const int cap = std::min(CL_RANGE_MAX, std::min(ctr[4], 2 * ((ctr[4] + CL - 1) / CL) + 64));
+                const size_t bytes = (size_t)cap * SM_BYTES_PER_MEMBER;
+                const bool unit = a.ew == 1.0 && a.ns == 1.0 && a.diag == 1.0;
+                auto kernel = unit ? k_flat_solve_cl<true> : k_flat_solve_cl<false>;
+                CG_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+                CG_LAUNCH(ctx) kernel<<<ctr[1] * CL, CL_THREADS, bytes, sm>>>(a, d_lists + flats, cap,
+                                                                              d_lists + 2 * (size_t)flats, d_ctr + 2);
                 CG_CHECK_LAUNCH(ctx);
+                CG_CUDA(ctx, cudaMemcpyAsync(&ctr[2], d_ctr + 2, sizeof(int), cudaMemcpyDeviceToHost, sm));
+                CG_CUDA(ctx, cudaStreamSynchronize(sm));
             }
             if (ctr[2] > 0) {
                 a.large = d_lists + 2 * (size_t)flats;

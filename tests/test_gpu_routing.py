@@ -154,6 +154,44 @@ def test_flow_directions_quantised_ties(r, step):
         assert diff.size == 0, f"{diff.size} receivers differ: {diff[:8]}"
 
 
+def carved_pits(W, H, seed):
+    """Land everywhere but the polar rows, on the synthetic relief, with pits carved into it: round
+    pits of about 600 to 9000 cells, one across the x-wrap seam, and a two-column trench (column runs
+    several hundred cells long), so that the fill leaves flats for every flat solver (a CTA, a
+    cluster of CTAs, and the global-memory one the cluster hands long runs to)."""
+    h, _, _ = synthetic.world(W, H, seed)
+    rel = ((h - h.min()) / (h.max() - h.min()) + 0.05).astype(np.float32)
+    land = np.ones((H, W), np.uint8)
+    land[:4] = 0
+    land[-4:] = 0
+    yy, xx = np.mgrid[0:H, 0:W]
+    rng = np.random.default_rng(seed)
+    for cx, cy, rad in [(W // 5, H // 3, 14), (W // 2, H // 2, 30), (3 * W // 4, H // 3, 54),
+                        (W // 3, 2 * H // 3, 22), (0, H // 2, 18)]:
+        dx = np.minimum(np.abs(xx - cx), W - np.abs(xx - cx))
+        d2 = dx ** 2 + (yy - cy) ** 2
+        pit = d2 <= rad * rad
+        ring = (d2 <= (rad + 2) ** 2) & ~pit
+        rel[pit] = float(rel[ring].min()) - 0.01 - 0.001 * rng.random(int(pit.sum())).astype(np.float32)
+    trench = (xx >= 7 * W // 8) & (xx <= 7 * W // 8 + 1) & (yy > H // 8) & (yy < 7 * H // 8)
+    ring = (xx >= 7 * W // 8 - 1) & (xx <= 7 * W // 8 + 2) & (yy >= H // 8) & (yy <= 7 * H // 8) & ~trench
+    rel[trench] = float(rel[ring].min()) - 0.01
+    return land, rel.astype(np.float32)
+
+
+@pytest.mark.parametrize("r", [1.0, 0.5])
+def test_flow_directions_large_flats(r):
+    W, H, seed = 1024, 512, 5
+    land, rel = carved_pits(W, H, seed)
+    filled = oracle.fill_depressions(land, rel)
+    want, wsurf, wc = oracle.flow_directions(land, rel, filled, seed, r, 214, True, True, want_surface=True)
+    got, gsurf, gc = FlowRouting.flow_directions(land, rel, filled, seed, r, 214, True, True, want_surface=True)
+    assert list(wc) == list(gc)
+    np.testing.assert_allclose(gsurf, wsurf, rtol=SURFACE_RTOL, atol=0)
+    diff = np.flatnonzero(got != want)
+    assert diff.size == 0, f"{diff.size} receivers differ: {diff[:8]}"
+
+
 @pytest.mark.parametrize("W,H,seed", SIZES + [(2048, 1024, 1)])
 def test_drainage_order_accumulate_spillways(W, H, seed):
     _, (s, land, rel, n) = world_cut(W, H, seed)
