@@ -140,17 +140,22 @@ __global__ void k_bin_sums(const unsigned* __restrict__ counts, const double* __
     if (lane == 0) hist[b] = acc;
 }
 
-// SeaLevelStage.kt:614-622: the first bin that brings the weight below up to the target.
-__global__ void k_bracket_bin(const double* __restrict__ hist, double target, CutState* s) {
+// SeaLevelStage.kt:614-622: the first bin that brings the weight below up to the target. The
+// histogram is staged in shared memory by the CTA; one thread then takes the reference's sums.
+__global__ void __launch_bounds__(256) k_bracket_bin(const double* __restrict__ hist, double target, CutState* s) {
+    __shared__ double sh[BINS];
     if (s->degenerate) return;
+    for (int b = threadIdx.x; b < BINS; b += blockDim.x) sh[b] = hist[b];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     double below = 0.0;
     int bracket = BINS - 1;
     for (int b = 0; b < BINS; ++b) {
-        if (below + hist[b] >= target) {
+        if (below + sh[b] >= target) {
             bracket = b;
             break;
         }
-        below += hist[b];
+        below += sh[b];
     }
     s->bracket_bin = bracket;
     s->below_bracket = below;
@@ -214,49 +219,182 @@ __global__ void k_pad(long long* keys, int n, int P2) {
     for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) keys[i] = LLONG_MAX;
 }
 
-// SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target. One
-// warp, 32 entries at a time: each lane knows the exact sum before its entry (cg::warp_chunk_sum),
-// so the first lane at or past the target is the answer; a chunk that cannot be taken whole is
-// replayed entry by entry.
-__global__ void k_bracket_walk(const float* __restrict__ h, const long long* __restrict__ keys,
-                               const double* __restrict__ w, int W, double target, CutState* s) {
+// SeaLevelStage.kt:636-644: walk the sorted bracket until the area below reaches the target.
+//
+// The walk's sum is sequential, but it rarely leaves its binade: then every entry adds a whole
+// number of units in the last place, d_i = rne(w_i / U), and the sums before the entries are an
+// integer prefix scan. One CTA takes the bracket CHUNK entries at a time: per entry d_i and whether
+// it is clean (no tie at half a unit, the step stays in the binade); a block scan of the d_i; the
+// answer is the first entry whose sum before it reaches the target, provided every earlier entry of
+// the chunk is clean. From the first entry that is not, warp 0 replays the rest of the chunk exactly
+// (32 entries at a time with cg::warp_chunk_sum, entry by entry where that fails).
+constexpr int WALK_THREADS = 1024;
+constexpr int WALK_PER = 8;
+constexpr int WALK_CHUNK = WALK_THREADS * WALK_PER;
+
+// Warp 0's exact replay of entries [from, to) starting from `below`. Returns true with *cell the
+// answer's cell when the sum before an entry reaches the target; otherwise *below is the sum after
+// entry to - 1.
+__device__ bool walk_replay(const long long* __restrict__ keys, const double* __restrict__ w, int W, double target,
+                            int from, int to, double* below_io, int* cell_out) {
     const unsigned FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    if (s->degenerate) return;
-    const int n = s->count;
-    if (n == 0) {
-        if (lane == 0) s->todays = s->highest;
-        return;
-    }
-    double below = s->below_bracket;
-    for (int base = 0; base < n; base += 32) {
-        int i = base + lane;
-        int cell = i < n ? (int)(keys[i] & 0xFFFFFFFFLL) : -1;
-        double wi = i < n ? w[cell / W] : 0.0;
+    double below = *below_io;
+    for (int base = from; base < to; base += 32) {
+        const int i = base + lane;
+        const int cell = i < to ? (int)(keys[i] & 0xFFFFFFFFLL) : -1;
+        const double wi = i < to ? w[cell / W] : 0.0;
         double before, after;
-        if (warp_chunk_sum(below, wi, i < n ? 1 : 0, &before, &after)) {
-            unsigned hit = __ballot_sync(FULL, i < n && before >= target);
+        if (warp_chunk_sum(below, wi, i < to ? 1 : 0, &before, &after)) {
+            const unsigned hit = __ballot_sync(FULL, i < to && before >= target);
             if (hit) {
-                int j = __ffs(hit) - 1;
-                int c = __shfl_sync(FULL, cell, j);
-                if (lane == 0) s->todays = h[c];
-                return;
+                *cell_out = __shfl_sync(FULL, cell, __ffs(hit) - 1);
+                return true;
             }
             below = after;
             continue;
         }
         for (int j = 0; j < 32; ++j) {
-            int cj = __shfl_sync(FULL, cell, j);
-            double wj = __shfl_sync(FULL, wi, j);
+            const int cj = __shfl_sync(FULL, cell, j);
+            const double wj = __shfl_sync(FULL, wi, j);
             if (cj < 0) break;
             if (below >= target) {
-                if (lane == 0) s->todays = h[cj];
-                return;
+                *cell_out = cj;
+                return true;
             }
             below += wj;
         }
     }
-    if (lane == 0) s->todays = h[(int)(keys[n - 1] & 0xFFFFFFFFLL)];
+    *below_io = below;
+    return false;
+}
+
+__global__ void __launch_bounds__(WALK_THREADS) k_bracket_walk(const float* __restrict__ h,
+                                                               const long long* __restrict__ keys,
+                                                               const double* __restrict__ w, int W, double target,
+                                                               CutState* s) {
+    const int64_t TOP = (int64_t)1 << 53;
+    __shared__ long long s_warp[WALK_THREADS / 32];
+    __shared__ int s_hit, s_unclean, s_done;
+    __shared__ double s_below;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (s->degenerate) return;
+    const int n = s->count;
+    if (n == 0) {
+        if (tid == 0) s->todays = s->highest;
+        return;
+    }
+    double below = s->below_bracket;
+    for (int base = 0; base < n; base += WALK_CHUNK) {
+        const int end = min(n, base + WALK_CHUNK);
+        if (tid == 0) {
+            s_hit = INT_MAX;
+            s_unclean = below > 0.0 ? INT_MAX : base;   // a zero sum has no binade: replay from the start
+        }
+        int e = 0;
+        double U = 1.0;
+        int64_t m = 0;
+        if (below > 0.0) {
+            e = ilogb(below);
+            U = ldexp(1.0, e - 52);
+            m = (int64_t)(below / U);
+        }
+        int64_t d[WALK_PER], q[WALK_PER];
+        bool clean[WALK_PER];
+        int64_t mine = 0;
+        const int first = base + tid * WALK_PER;
+#pragma unroll
+        for (int k = 0; k < WALK_PER; ++k) {
+            const int i = first + k;
+            d[k] = 0;
+            q[k] = 0;
+            clean[k] = true;
+            if (i < end) {
+                const int cell = (int)(keys[i] & 0xFFFFFFFFLL);
+                const double x = ldexp(w[cell / W], 52 - e);   // w / U, exact
+                if (!(x < 9.0e15)) {
+                    clean[k] = false;
+                } else {
+                    q[k] = (int64_t)x;
+                    const double f = x - (double)q[k];
+                    clean[k] = f != 0.5;
+                    d[k] = q[k] + (f > 0.5 ? 1 : 0);
+                }
+            }
+            mine += d[k];
+        }
+        // Exclusive block scan of the per-thread totals.
+        int64_t incl = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int64_t v = s_warp[lane], vi = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t t = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+                if (lane >= o) vi += t;
+            }
+            s_warp[lane] = vi - v;   // exclusive over warps
+        }
+        __syncthreads();
+        int64_t run = m + s_warp[warp] + (incl - mine);   // the sum before this thread's first entry, in U
+        int hit = INT_MAX, unclean = INT_MAX;
+#pragma unroll
+        for (int k = 0; k < WALK_PER; ++k) {
+            const int i = first + k;
+            if (i >= end) break;
+            if (hit == INT_MAX && (double)run * U >= target) hit = i;
+            if (unclean == INT_MAX && (!clean[k] || run + q[k] > TOP - 1)) unclean = i;
+            run += d[k];
+        }
+        if (hit != INT_MAX) atomicMin(&s_hit, hit);
+        if (unclean != INT_MAX) atomicMin(&s_unclean, unclean);
+        __syncthreads();
+        const int h_at = s_hit, u_at = s_unclean;
+        if (h_at != INT_MAX && h_at <= u_at) {   // every entry before the answer added whole units inside the binade
+            if (tid == 0) s->todays = h[(int)(keys[h_at] & 0xFFFFFFFFLL)];
+            return;
+        }
+        // The sum before entry u_at (exact), from the thread that owns it; for a chunk that was clean
+        // throughout, the sum after its last entry.
+        if (tid == 0) s_done = 0;
+        __syncthreads();
+        {
+            int64_t r2 = m + s_warp[warp] + (incl - mine);
+#pragma unroll
+            for (int k = 0; k < WALK_PER; ++k) {
+                const int i = first + k;
+                if (i == u_at) s_below = (double)r2 * U;
+                if (i >= end) break;
+                r2 += d[k];
+                if (u_at == INT_MAX && i == end - 1) s_below = (double)r2 * U;
+            }
+        }
+        __syncthreads();
+        below = s_below;
+        if (u_at != INT_MAX) {
+            if (warp == 0) {
+                double b = below;
+                int cell;
+                if (walk_replay(keys, w, W, target, u_at, end, &b, &cell)) {
+                    if (lane == 0) {
+                        s->todays = h[cell];
+                        s_done = 1;
+                    }
+                } else if (lane == 0) {
+                    s_below = b;
+                }
+            }
+            __syncthreads();
+            if (s_done) return;
+            below = s_below;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) s->todays = h[(int)(keys[n - 1] & 0xFFFFFFFFLL)];
 }
 
 // SeaLevelStage.landAndWaterAt (SeaLevelStage.kt:175-200).
@@ -324,7 +462,7 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
     CG_LAUNCH(ctx) k_cut_prepare<<<1, 1, 0, sm>>>(d_s, target);
     CG_LAUNCH(ctx) k_row_counts<<<H, 512, 0, sm>>>(d_h, W, d_s, d_counts);
     CG_LAUNCH(ctx) k_bin_sums<<<BINS * 32 / 256, 256, 0, sm>>>(d_counts, d_w, H, d_s, d_hist);
-    CG_LAUNCH(ctx) k_bracket_bin<<<1, 1, 0, sm>>>(d_hist, target, d_s);
+    CG_LAUNCH(ctx) k_bracket_bin<<<1, 256, 0, sm>>>(d_hist, target, d_s);
     CG_LAUNCH(ctx) k_bracket_collect<<<grid, 256, 0, sm>>>(d_h, N, d_s, d_keys);
     CG_CHECK_LAUNCH(ctx);
     CutState hs;
@@ -352,7 +490,7 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
         }
         CG_CHECK_LAUNCH(ctx);
     }
-    CG_LAUNCH(ctx) k_bracket_walk<<<1, 32, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
+    CG_LAUNCH(ctx) k_bracket_walk<<<1, WALK_THREADS, 0, sm>>>(d_h, d_keys, d_w, W, target, d_s);
     CG_LAUNCH(ctx) k_land_and_water<<<grid, 256, 0, sm>>>(d_h, N, d_s, lowstand_share, land_half, sea_half, d_land, d_rel);
     CG_CHECK_LAUNCH(ctx);
     CG_CUDA(ctx, cudaMemcpyAsync(&hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, sm));
