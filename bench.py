@@ -33,6 +33,9 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-rounds/s on 1 GB300: plain vs batched vs surrogate at <=5 m height RMSE"
 UNIT = "Mcell-rounds/s"
 ROUNDS = 12
+# DRAM bytes (read + write) of one two-sweep launch of thermal_sweeps_kernel on the 8192 x 4096
+# field, from ncu (profiles/thermal_sweeps_8192x4096.md); the roofline's traffic at that size.
+SWEEP_TRAFFIC_PER_LAUNCH = None
 
 
 def parse():
@@ -202,13 +205,12 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         step_dev()
-    step_dev(with_stats=True)   # one untimed pass for the per-phase breakdown
-    phase = {k: sum(getattr(s, k) for s in stats) for k in
-             ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_relax", "ms_total")}
-    per_round = [{"land": s.land_cells, "flats": s.flats, "raised": s.raised_cells, "levels": s.levels,
-                  "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2)}
-                 for s in stats]
 
+    # The timed steps also fill cg_round_stats: the library records CUDA events on its stream around
+    # each phase of each round, which gives the per-phase device times (and the sweep kernel's
+    # launch durations for the roofline) over the timed region itself.
+    PHASES = ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_relax", "ms_total")
+    phase = {k: 0.0 for k in PHASES}
     clocks = ClockSampler(local)
     barrier()
     launches0 = ctx.kernel_launches
@@ -216,9 +218,14 @@ def run_ours(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         ev[i][0].record(lib_stream)
-        step_dev()
+        step_dev(with_stats=True)
         ev[i][1].record(lib_stream)
+        for k in PHASES:
+            phase[k] += sum(getattr(s, k) for s in stats) / args.steps
     barrier()
+    per_round = [{"land": s.land_cells, "flats": s.flats, "raised": s.raised_cells, "levels": s.levels,
+                  "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2)}
+                 for s in stats]
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -243,11 +250,11 @@ def run_ours(args):
     value = cell_rounds / t_dev / 1e6
     e2e = cell_rounds / t_e2e / 1e6
 
-    # Roofline of the dominant phase's kernel. The relaxation sweeps' algorithmic traffic is a read
-    # and a write of the height field per sweep (8 B per cell-sweep); with sweeps fused per launch
-    # the kernel moves less than that, so frac may exceed 1 (it is measured against the unfused bytes).
+    # Roofline of the dominant kernel, the fused thermal sweeps. Their algorithmic traffic is a read
+    # and a write of the height field per sweep (8 B per cell-sweep); with two sweeps fused per
+    # launch the kernel moves less than that (the traffic key, from ncu).
     from cartogenesis_gb300.perf import roofline_entry
-    roof = roofline_entry(cfg, phase, ROOT)
+    roof = roofline_entry(cfg, phase, ROOT, traffic=SWEEP_TRAFFIC_PER_LAUNCH if (W, H) == (8192, 4096) else None)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -262,6 +269,7 @@ def run_ours(args):
         "clocks": clk,
         "roofline": roof,
         "phases_ms_per_step": {k: round(v, 2) for k, v in phase.items()},
+        "ms_outside_rounds": round(1000.0 * t_dev / args.steps - phase["ms_total"], 2),
         "rounds": per_round,
     }
     if rank == 0 and world == 1 and args.cpu_sample > 0:

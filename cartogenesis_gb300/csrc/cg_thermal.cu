@@ -82,12 +82,13 @@ __device__ __forceinline__ float moved(const Window& v, const Window& g, bool ha
     for (int n = 0; n < 8; ++n) {
         const float limit = a.limit[n];
         const float incoming = __fsub_rn(nb[n], v.c);
-        const bool in = ok[n] && incoming > limit;
-        const bool out = ok[n] && !(incoming > limit) && -incoming > limit;
-        const float r = __fadd_rn(received, __fmul_rn(gn[n], __fsub_rn(incoming, limit)));
-        const float o = __fadd_rn(given, __fmul_rn(g.c, __fsub_rn(-incoming, limit)));
-        received = in ? r : received;
-        given = out ? o : given;
+        const bool in = incoming > limit;
+        const bool out = !in && -incoming > limit;
+        // One product serves both branches: (incoming - limit) * g_n coming in, (-incoming - limit) * g_c
+        // going out; the sums take it only under their own condition, in the reference's order.
+        const float p = __fmul_rn(in ? gn[n] : g.c, __fsub_rn(in ? incoming : -incoming, limit));
+        if (ok[n] && in) received = __fadd_rn(received, p);
+        if (ok[n] && out) given = __fadd_rn(given, p);
     }
     return __fadd_rn(__fsub_rn(v.c, given), received);
 }
@@ -113,10 +114,13 @@ __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __rest
         v.nw = p[-1], v.n = p[0], v.ne = p[1];
         v.w = p[RW - 1], v.c = p[RW], v.e = p[RW + 1];
         Window g{};
+        unsigned or_top = 0, or_mid = 0;   // bitwise OR of the give rates' bits, per window row
         if (MOVE) {
             const float* q = gv + (r0 - 1) * RW + col;
             g.nw = q[-1], g.n = q[0], g.ne = q[1];
             g.w = q[RW - 1], g.c = q[RW], g.e = q[RW + 1];
+            or_top = __float_as_uint(g.nw) | __float_as_uint(g.n) | __float_as_uint(g.ne);
+            or_mid = __float_as_uint(g.w) | __float_as_uint(g.c) | __float_as_uint(g.e);
         }
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
@@ -124,23 +128,34 @@ __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __rest
             if (ry >= r1) break;
             const float* below = hs + (ry + 1) * RW + col;
             v.sw = below[-1], v.s = below[0], v.se = below[1];
+            unsigned or_bot = 0;
             if (MOVE) {
                 const float* gb = gv + (ry + 1) * RW + col;
                 g.sw = gb[-1], g.s = gb[0], g.se = gb[1];
+                or_bot = __float_as_uint(g.sw) | __float_as_uint(g.s) | __float_as_uint(g.se);
             }
             const int gy = y0 + ry;
             const bool on = !EDGE || (gy >= 0 && gy < H);
             const bool has_s = !EDGE || gy + 1 < H;
             const bool has_n = !EDGE || gy - 1 >= 0;
             if (on) {
-                if (MOVE) dst[ry * RW + col] = moved(v, g, has_s, has_n, a);
-                else gv[ry * RW + col] = give_rate(v, has_s, has_n, a);
+                if (MOVE) {
+                    // Every give rate around the cell +0: each product the rule could add is +0, so the
+                    // sums stay +0 and the cell moves to (h - 0) + 0. Rows off the grid (EDGE) are
+                    // left to the full rule.
+                    const bool still = !EDGE && (or_top | or_mid | or_bot) == 0u;
+                    dst[ry * RW + col] = still ? __fadd_rn(__fsub_rn(v.c, 0.0f), 0.0f) : moved(v, g, has_s, has_n, a);
+                } else {
+                    gv[ry * RW + col] = give_rate(v, has_s, has_n, a);
+                }
             }
             v.nw = v.w, v.n = v.c, v.ne = v.e;
             v.w = v.sw, v.c = v.s, v.e = v.se;
             if (MOVE) {
                 g.nw = g.w, g.n = g.c, g.ne = g.e;
                 g.w = g.sw, g.c = g.s, g.e = g.se;
+                or_top = or_mid;
+                or_mid = or_bot;
             }
         }
     }

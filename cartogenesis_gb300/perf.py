@@ -18,8 +18,8 @@ BYTES_PER_CELL = {"ms_cut": 41.0, "ms_fill": 9.0, "ms_route": 28.0, "ms_tree": 2
 PHASE_KERNELS = {
     "ms_cut": "k_minmax, k_row_counts, k_bin_sums, k_bracket_*, k_land_and_water, k_uplift, k_unit_weights",
     "ms_fill": "k_fill_init, k_jump, k_mark_drained, k_relax_tiles, k_check_ties",
-    "ms_route": "k_surface, k_cc_*, k_flat_solve, k_receivers",
-    "ms_tree": "k_donor_count, k_walk",
+    "ms_route": "k_surface, k_cc_*, k_flat_solve_warp/_sm/_cl, k_flat_solve, k_receivers",
+    "ms_tree": "k_links, k_sources, k_walk",
     "ms_incise": "k_depth_*, k_incise_levels",
     "ms_relax": "thermal_sweeps_kernel",
 }
@@ -41,24 +41,40 @@ def phase_bytes_per_cell(phase, sweeps_per_round):
     return BYTES_PER_CELL[phase]
 
 
-def roofline_entry(cfg, phase_ms_per_stage, root, traffic=None):
-    """The roofline object for the phase that takes the most device time over a stage's rounds.
+def sweep_launches(sweeps):
+    """Fused thermal launches for `sweeps` sweeps: two sweeps per launch, one for an odd rest."""
+    return (sweeps + 1) // 2
 
-    phase_ms_per_stage maps ms_* to that phase's device milliseconds summed over the stage's
-    rounds (CUDA events on the library's stream).
+
+def roofline_entry(cfg, phase_ms_per_stage, root, traffic=None):
+    """The roofline object for the dominant kernel, the thermal sweeps of the relax phase.
+
+    phase_ms_per_stage maps ms_* to that phase's device milliseconds summed over a stage's rounds
+    (CUDA events the library records on its stream around each phase, over the timed steps). The
+    relax phase is nothing but the fused sweep launches, so their average launch duration is the
+    phase's time over its launches, and a launch's algorithmic bytes are a read and a write of the
+    height field per sweep it fuses (8 B per cell-sweep). `traffic` is the DRAM bytes of one launch
+    from an ncu capture, or None. The other phases follow under "phases", each against its own
+    compulsory bytes per cell and round (the module docstring).
     """
     p = cfg.params
     N = p.width * p.height
     rounds = max(p.hydraulic_rounds, 1)
     _, sweeps = cfg.thermal_limits()
     per_round = max(sweeps // rounds, 1)
-    phases = [k for k in phase_ms_per_stage if k != "ms_total"]
-    dom = max(phases, key=lambda k: phase_ms_per_stage[k])
-    ms_per_round = phase_ms_per_stage[dom] / rounds
-    algo = phase_bytes_per_cell(dom, per_round) * N   # bytes per round of that phase
-    achieved = algo / (ms_per_round / 1000.0) / 1e9 if ms_per_round > 0 else 0.0
+    launches = sweep_launches(per_round)
     peak, kind = peak_hbm(root)
+    ms_launch = phase_ms_per_stage["ms_relax"] / rounds / launches
+    algo = 8.0 * N * per_round / launches   # bytes per launch (average over the round's launches)
+    achieved = algo / (ms_launch / 1000.0) / 1e9 if ms_launch > 0 else 0.0
+    phases = {}
+    for k, v in phase_ms_per_stage.items():
+        if k == "ms_total" or v <= 0:
+            continue
+        gbs = phase_bytes_per_cell(k, per_round) * N / (v / rounds / 1000.0) / 1e9
+        phases[k[3:]] = {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4),
+                         "ms_per_round": round(v / rounds, 3), "kernels": PHASE_KERNELS[k]}
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": kind,
-            "kernel": f"{dom[3:]} phase ({PHASE_KERNELS[dom]})",
-            "algorithmic_bytes_per_launch_group": algo, "ms_per_round": round(ms_per_round, 3)}
+            "kernel": "thermal_sweeps_kernel (relax phase)", "launches_per_round": launches,
+            "algorithmic_bytes_per_launch": algo, "ms_per_launch": round(ms_launch, 4), "phases": phases}
