@@ -23,10 +23,12 @@ constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
 __host__ __device__ constexpr int thermal_col_step(int n) { return n == 0 ? 1 : n == 1 ? -1 : n < 4 ? 0 : (n < 6 ? 1 : -1); }
 __host__ __device__ constexpr int thermal_row_step(int n) { return n == 0 || n == 1 ? 0 : n == 2 ? 1 : n == 3 ? -1 : ((n & 1) == 0 ? 1 : -1); }
 
-__device__ __forceinline__ int wrap_col(int c, int W) {
-    int r = c % W;
-    return r < 0 ? r + W : r;
-}
+// Grid sides are powers of two (every entry point checks, the noalloc sweeps included), so a
+// division or remainder of a non-negative index by a side is a shift or a mask, and a column wraps
+// by masking (for any int column, negative ones included).
+__device__ __forceinline__ int pdiv(int x, int n) { return x >> (31 - __clz(n)); }
+__device__ __forceinline__ int pmod(int x, int n) { return x & (n - 1); }
+__device__ __forceinline__ int wrap_col(int c, int W) { return c & (W - 1); }
 
 // Float <-> raw bits, as Float.toRawBits.
 __device__ __forceinline__ int32_t float_bits(float f) { return __float_as_int(f); }

@@ -243,7 +243,7 @@ __device__ bool walk_replay(const long long* __restrict__ keys, const double* __
     for (int base = from; base < to; base += 32) {
         const int i = base + lane;
         const int cell = i < to ? (int)(keys[i] & 0xFFFFFFFFLL) : -1;
-        const double wi = i < to ? w[cell / W] : 0.0;
+        const double wi = i < to ? w[pdiv(cell, W)] : 0.0;
         double before, after;
         if (warp_chunk_sum(below, wi, i < to ? 1 : 0, &before, &after)) {
             const unsigned hit = __ballot_sync(FULL, i < to && before >= target);
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(WALK_THREADS) k_bracket_walk(const float* __re
             clean[k] = true;
             if (i < end) {
                 const int cell = (int)(keys[i] & 0xFFFFFFFFLL);
-                const double x = ldexp(w[cell / W], 52 - e);   // w / U, exact
+                const double x = ldexp(w[pdiv(cell, W)], 52 - e);   // w / U, exact
                 if (!(x < 9.0e15)) {
                     clean[k] = false;
                 } else {

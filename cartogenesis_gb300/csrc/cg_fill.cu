@@ -60,7 +60,7 @@ __global__ void k_fill_init(const uint8_t* __restrict__ land, const float* __res
                             uint8_t* __restrict__ cls, float* __restrict__ f, int* __restrict__ ptr) {
     size_t N = (size_t)W * H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        int row = (int)(i / W);
+        const int row = pdiv((int)i, W);
         if (!land[i]) {
             cls[i] = C_WATER;
             f[i] = g[i];
@@ -74,7 +74,7 @@ __global__ void k_fill_init(const uint8_t* __restrict__ land, const float* __res
             continue;
         }
         // Steepest strictly Q-descending neighbour on the unfilled ground (water counts as is).
-        int col = (int)(i - (size_t)row * W);
+        const int col = pmod((int)i, W);
         int q = qkey(g[i]);
         int best = (int)i, bq = q;
         for (int rs = -1; rs <= 1; ++rs) {
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
                 }
             } else {
                 int p = pin_parent[(size_t)gy * W + tx0 + lx];
-                int pr = p / W, pc = p % W;
+                int pr = pdiv(p, W), pc = pmod(p, W);
                 int dy = pr - gy;
                 int dx = pc - (tx0 + lx);
                 if (dx > 1) dx -= W;
@@ -251,7 +251,7 @@ __global__ void k_check_ties(const float* __restrict__ f, const float* __restric
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         uint8_t c = cls[i];
         if (c != C_OPEN && c != C_PINNED) continue;   // EXACT cells were ordered by replaying their level
-        int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+        const int row = pdiv((int)i, W), col = pmod((int)i, W);
         float gn = g[i];
         int qmin = INT_MAX;
         for (int rs = -1; rs <= 1; ++rs) {
@@ -283,7 +283,7 @@ __global__ void k_check_ties(const float* __restrict__ f, const float* __restric
                 // shares its key. Water and the polar outlets are in the heap from the start.
                 uint8_t cm = cls[n];
                 if ((cm == C_OPEN || follows_parent(cm) || cm == C_DRAINED) && fm == g[n]) {
-                    int mr = n / W, mc = n % W, mq = INT_MAX;
+                    int mr = pdiv(n, W), mc = pmod(n, W), mq = INT_MAX;
                     for (int a = -1; a <= 1; ++a) {
                         int r2 = mr + a;
                         if (r2 < 0 || r2 >= H) continue;
@@ -342,7 +342,7 @@ __global__ void k_gather_level(const float* __restrict__ f, const uint8_t* __res
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         if (qkey(f[i]) != Q) continue;
         if (cls[i] == C_WATER) {
-            int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+            const int row = pdiv((int)i, W), col = pmod((int)i, W);
             bool touches = false;
             for (int rs = -1; rs <= 1 && !touches; ++rs) {
                 int nr = row + rs;
@@ -362,7 +362,7 @@ __global__ void k_gather_level(const float* __restrict__ f, const uint8_t* __res
 __device__ bool entered_below(const float* f, const uint8_t* cls, int W, int H, int cell, int Q) {
     uint8_t c = cls[cell];
     if (c == C_WATER || c == C_SEED) return true;
-    int row = cell / W, col = cell % W;
+    int row = pdiv(cell, W), col = pmod(cell, W);
     for (int rs = -1; rs <= 1; ++rs) {
         int nr = row + rs;
         if (nr < 0 || nr >= H) continue;
@@ -429,7 +429,7 @@ __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ 
     while (hs > 0) {
         int x = pop();
         float fx = f[x];
-        int row = x / W, col = x % W;
+        int row = pdiv(x, W), col = pmod(x, W);
         for (int rs = -1; rs <= 1; ++rs) {
             int nr = row + rs;
             if (nr < 0 || nr >= H) continue;

@@ -48,7 +48,7 @@ __device__ __forceinline__ float lerpf(float a, float b, float t) { return __fad
 // FlowRouting.smoothSeededField (FlowRouting.kt:377-397).
 __device__ float smooth_seeded_field(int W, int lattice, int col, int row, long long seed) {
     int cal = col * lattice, ral = row * lattice;
-    int ccol = cal / W, crow = ral / W;
+    int ccol = pdiv(cal, W), crow = pdiv(ral, W);
     float ac = __fdiv_rn((float)(cal - ccol * W), (float)W);
     float ar = __fdiv_rn((float)(ral - crow * W), (float)W);
     float ec = __fmul_rn(__fmul_rn(ac, ac), __fsub_rn(3.0f, __fmul_rn(2.0f, ac)));
@@ -238,7 +238,7 @@ __global__ void k_receivers(const uint8_t* __restrict__ land, const double* __re
             recv[i] = -1;
             continue;
         }
-        int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+        const int row = pdiv((int)i, W), col = pmod((int)i, W);
         const bool unit = st.ew == 1.0f && st.ns == 1.0f;
         recv[i] = !by_facet ? steepest_neighbour(W, H, surface, col, row, st)
                   : unit    ? facet_receiver<true>(W, H, surface, col, row, st, seed)
@@ -360,7 +360,7 @@ __device__ __forceinline__ double stencil_weight(const FlatArgs& a, int cs, int 
 // column and back up with the chain carried in registers; the expressions are the reference's
 // ((right + ns * above) / pivot down, += (ns / pivot) * below up, ns / pivot kept per member).
 __device__ __forceinline__ bool run_continues(const int* mem, int n, int k, int W, int H) {
-    return k + 1 < n && mem[k + 1] == mem[k] + W && mem[k] / W + 1 < H;
+    return k + 1 < n && mem[k + 1] == mem[k] + W && pdiv(mem[k], W) + 1 < H;
 }
 __device__ __forceinline__ bool run_head(const int* mem, int k, int W) { return k == 0 || mem[k - 1] != mem[k] - W; }
 
@@ -390,7 +390,7 @@ __device__ void runs_solve(const FlatArgs& a, int base, int n, const double* rig
 __device__ void apply_laplacian(const FlatArgs& a, int base, int n, const double* xv, double* into) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         int cell = a.members[base + k];
-        int col = cell % a.W, row = cell / a.W;
+        int col = pmod(cell, a.W), row = pdiv(cell, a.W);
         double sum = __dmul_rn(a.degree[base + k], xv[base + k]);
         for (int rs = -1; rs <= 1; ++rs) {
             int nr = row + rs;
@@ -420,7 +420,7 @@ __device__ void lay_in_band(const FlatArgs& a, const int* mem, int n, const doub
         int ok = 1;
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
             int cell = mem[k];
-            int col = cell % a.W, row = cell / a.W;
+            int col = pmod(cell, a.W), row = pdiv(cell, a.W);
             double here = a.surface[cell];
             bool lower = false;
             for (int rs = -1; rs <= 1 && !lower; ++rs) {
@@ -457,13 +457,13 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     // is fixed, so the block reductions below are deterministic.
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         int c = mem[k];
-        mem[k] = (c % a.W) * a.H + c / a.W;
+        mem[k] = pmod(c, a.W) * a.H + pdiv(c, a.W);
     }
     __syncthreads();
     sort_members(mem, n);
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         int key = mem[k];
-        mem[k] = (key % a.H) * a.W + key / a.H;
+        mem[k] = pmod(key, a.H) * a.W + pdiv(key, a.H);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < n; k += blockDim.x) a.local[mem[k]] = k;
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     double hi = -INFINITY;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         int cell = mem[k];
-        int col = cell % a.W, row = cell / a.W;
+        int col = pmod(cell, a.W), row = pdiv(cell, a.W);
         for (int rs = -1; rs <= 1; ++rs) {
             int nr = row + rs;
             if (nr < 0 || nr >= a.H) continue;
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
     // Degrees (FlatRouting.kt:239-271) and the rain (:289-295).
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         int cell = mem[k];
-        int col = cell % a.W, row = cell / a.W;
+        int col = pmod(cell, a.W), row = pdiv(cell, a.W);
         double total = 0.0;
         for (int rs = -1; rs <= 1; ++rs) {
             int nr = row + rs;
@@ -648,13 +648,13 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
     // Members by (column, row), as in k_flat_solve.
     for (int k = threadIdx.x; k < n; k += FT) {
         int c = mem[k];
-        mem[k] = (c % W) * H + c / W;
+        mem[k] = pmod(c, W) * H + pdiv(c, W);
     }
     __syncthreads();
     sort_members(mem, n);
     for (int k = threadIdx.x; k < n; k += FT) {
         int key = mem[k];
-        mem[k] = (key % H) * W + key / H;
+        mem[k] = pmod(key, H) * W + pdiv(key, H);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < n; k += FT) a.local[mem[k]] = k;
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
     double hi = -INFINITY;
     for (int k = threadIdx.x; k < n; k += FT) {
         const int cell = mem[k];
-        const int col = cell % W, row = cell / W;
+        const int col = pmod(cell, W), row = pdiv(cell, W);
         double total = 0.0;
         int nb8[8];
         int t = 0;
@@ -902,13 +902,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     if (q == 0) {
         for (int k = threadIdx.x; k < n; k += FT) {
             int c = mem[k];
-            mem[k] = (c % W) * H + c / W;
+            mem[k] = pmod(c, W) * H + pdiv(c, W);
         }
         __syncthreads();
         sort_members(mem, n);
         for (int k = threadIdx.x; k < n; k += FT) {
             int key = mem[k];
-            mem[k] = (key % H) * W + key / H;
+            mem[k] = pmod(key, H) * W + pdiv(key, H);
         }
     }
     cluster.sync();
@@ -952,7 +952,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     for (int j = threadIdx.x; j < m; j += FT) {
         const int k = lo + j;
         const int cell = mem[k];
-        const int col = cell % W, row = cell / W;
+        const int col = pmod(cell, W), row = pdiv(cell, W);
         double total = 0.0;
         int nb8[8];
         int t = 0;
@@ -1100,7 +1100,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
         double ok = 1.0;
         for (int j = threadIdx.x; j < m; j += FT) {
             const int cell = mem[lo + j];
-            const int col = cell % W, row = cell / W;
+            const int col = pmod(cell, W), row = pdiv(cell, W);
             const double here = a.surface[cell];
             bool lower = false;
             for (int rs = -1; rs <= 1 && !lower; ++rs) {
@@ -1150,7 +1150,7 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
     const int W = a.W, H = a.H;
 
     // Members by (column, row): a bitonic sort across the lanes.
-    int key = act ? (a.members[base + lane] % W) * H + a.members[base + lane] / W : INT_MAX;
+    int key = act ? pmod(a.members[base + lane], W) * H + pdiv(a.members[base + lane], W) : INT_MAX;
     for (int k = 2; k <= 32; k <<= 1)
         for (int j = k >> 1; j > 0; j >>= 1) {
             int other = __shfl_xor_sync(FULL, key, j);
@@ -1159,13 +1159,13 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
             int lo = min(key, other), hi = max(key, other);
             key = (lower == up) ? lo : hi;
         }
-    const int cell = act ? (key % H) * W + key / H : -1;
+    const int cell = act ? pmod(key, H) * W + pdiv(key, H) : -1;
     if (act) {
         a.members[base + lane] = cell;
         a.local[cell] = lane;
     }
     __syncwarp();
-    const int col = act ? cell % W : 0, row = act ? cell / W : 0;
+    const int col = act ? pmod(cell, W) : 0, row = act ? pdiv(cell, W) : 0;
 
     // Entry level, highest entry, member neighbours (their lanes), degree and rain.
     float lo = act ? a.filled[cell] : FLT_MAX;

@@ -43,7 +43,7 @@ __device__ __forceinline__ int dir_row(int t) { return t < 3 ? -1 : (t < 5 ? 0 :
 __device__ __forceinline__ int dir_col(int t) { return t < 3 ? t - 1 : (t < 5 ? (t == 3 ? -1 : 1) : t - 6); }
 __device__ __forceinline__ int dir_of(int rs, int cs) { return (rs + 1) * 3 + (cs + 1) - ((rs > 0 || (rs == 0 && cs > 0)) ? 1 : 0); }
 __device__ __forceinline__ int step_to(int W, int c, int t) {
-    const int row = c / W, col = c % W;
+    const int row = pdiv(c, W), col = pmod(c, W);
     return (row + dir_row(t)) * W + wrap_col(col + dir_col(t), W);
 }
 
@@ -59,8 +59,8 @@ __global__ void k_links(const uint8_t* __restrict__ land, const int32_t* __restr
             const int r = recv[i];
             if (is_land_receiver(land, r)) {
                 const int c = (int)i;
-                int rs = r / W - c / W;
-                int cs = r % W - c % W;
+                int rs = pdiv(r, W) - pdiv(c, W);
+                int cs = pmod(r, W) - pmod(c, W);
                 if (cs > 1) cs -= W;
                 if (cs < -1) cs += W;
                 d = (uint8_t)dir_of(rs, cs);

@@ -68,7 +68,7 @@ __global__ void k_cc_union(const uint8_t* __restrict__ mask, int* __restrict__ p
     size_t N = (size_t)W * H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         if (!mask[i]) continue;
-        int row = (int)(i / W), col = (int)(i - (size_t)row * W);
+        const int row = pdiv((int)i, W), col = pmod((int)i, W);
         int e = row * W + wrap_col(col + 1, W);
         if (mask[e]) unite(parent, (int)i, e);
         if (row + 1 < H) {
