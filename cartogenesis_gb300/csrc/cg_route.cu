@@ -351,6 +351,16 @@ __device__ void sort_members(int* m, int n) {
     }
 }
 
+// x / p for a pivot p > 0 whose reciprocal r = 1 / p (correctly rounded) is kept: q0 = x r and one
+// correction with fused multiply-adds, q = q0 + (x - q0 p) r. With a correctly rounded reciprocal
+// this is the correctly rounded quotient (Markstein's theorem, barring overflow and underflow), so
+// the bits of x / p, in three dependent operations instead of a division's sequence; the column
+// runs' solves are chains of such divisions, so their latency is the CG iteration's.
+__device__ __forceinline__ double div_by(double x, double p, double r) {
+    const double q0 = __dmul_rn(x, r);
+    return __fma_rn(__fma_rn(-q0, p, x), r, q0);
+}
+
 __device__ __forceinline__ double stencil_weight(const FlatArgs& a, int cs, int rs) {
     return (cs != 0 && rs != 0) ? a.diag : (rs != 0 ? a.ns : a.ew);
 }
@@ -593,7 +603,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
 // each thread's partial sum in member order, a warp butterfly and an ordered sum over the warps,
 // so its bits are fixed for a given CTA size.
 constexpr int MID_FLAT = 512;    // members at most for the 128-thread CTA
-constexpr int SM_BYTES_PER_MEMBER = 6 * 8 + 4;   // six doubles and one run-table entry
+constexpr int SM_BYTES_PER_MEMBER = 7 * 8 + 4;   // seven doubles and one run-table entry
 
 // Sums of u and of v over the CTA, returned to every thread. `buf` (one double2 per warp) must
 // alternate between two arrays from one call to the next: the barrier of the next call is what
@@ -640,7 +650,8 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
     double* s_ad = s_d + n;
     double* s_piv = s_ad + n;
     double* s_coef = s_piv + n;
-    unsigned* s_run = reinterpret_cast<unsigned*>(s_coef + n);   // first | last << 16
+    double* s_rcp = s_coef + n;   // 1 / pivot
+    unsigned* s_run = reinterpret_cast<unsigned*>(s_rcp + n);   // first | last << 16
     double* x = a.x + base;
     double* degree = a.degree + base;
     int4* nbr = reinterpret_cast<int4*>(a.nbr + (size_t)base * 8);
@@ -718,6 +729,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
         for (int j = first;; ++j) {
             s_piv[j] = p;
             s_coef[j] = __ddiv_rn(a.ns, p);
+            s_rcp[j] = __ddiv_rn(1.0, p);
             if (j == last) break;
             p = __dsub_rn(degree[j + 1], __ddiv_rn(__dmul_rn(a.ns, a.ns), p));
         }
@@ -728,10 +740,10 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
     auto precondition = [&]() {
         for (int i = threadIdx.x; i < runs; i += FT) {
             const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
-            double v = __ddiv_rn(__dadd_rn(s_r[first], 0.0), s_piv[first]);
+            double v = div_by(__dadd_rn(s_r[first], 0.0), s_piv[first], s_rcp[first]);
             s_z[first] = v;
             for (int j = first + 1; j <= last; ++j) {
-                v = __ddiv_rn(__dadd_rn(s_r[j], __dmul_rn(a.ns, v)), s_piv[j]);
+                v = div_by(__dadd_rn(s_r[j], __dmul_rn(a.ns, v)), s_piv[j], s_rcp[j]);
                 s_z[j] = v;
             }
             double below = v;
@@ -824,6 +836,7 @@ constexpr int CL = 8;                          // CTAs per cluster
 constexpr int CL_THREADS = 256;
 constexpr int CL_FLAT = 16384;                 // members at most for the cluster kernel
 constexpr int CL_RANGE_MAX = 8191;             // members per CTA: the neighbour code keeps 13 bits of offset
+constexpr int CL_SMEM_MEMBERS = (227 * 1024 - 2048) / SM_BYTES_PER_MEMBER;   // members per CTA that fit
 
 namespace cgc = cooperative_groups;
 
@@ -837,10 +850,12 @@ struct MinMax2 {
 };
 
 // The CTA's combination of (u, v) (a warp butterfly, then the warps in order), sent to slot q of
-// every CTA's `slots[par]`; after the cluster barrier each CTA combines the CL slots in rank order.
-// `par` alternates between calls, as for block_sum2.
+// every CTA's `slots[par]`; after the cluster barrier each CTA's first warp combines the CL slots in
+// rank order and hands the result to the CTA through shared memory (the FP64 pipe is the scarce
+// resource: the other warps need not repeat it). `par` alternates between calls, as for block_sum2.
 template <class Op>
-__device__ double2 cluster_combine(double2 v, Op op, double2* warps, double2 (*slots)[CL], int& par, int q) {
+__device__ double2 cluster_combine(double2 v, Op op, double2* warps, double2 (*slots)[CL], double2* result, int& par,
+                                   int q) {
     constexpr int NW = CL_THREADS / 32;
     for (int o = 16; o > 0; o >>= 1) {
         double2 t;
@@ -858,9 +873,14 @@ __device__ double2 cluster_combine(double2 v, Op op, double2* warps, double2 (*s
         *dst = s;
     }
     cgc::this_cluster().sync();
-    double2 s = slots[par][0];
+    if (threadIdx.x < 32) {
+        double2 s = slots[par][0];
 #pragma unroll
-    for (int r = 1; r < CL; ++r) s = op(s, slots[par][r]);
+        for (int r = 1; r < CL; ++r) s = op(s, slots[par][r]);
+        if (threadIdx.x == 0) result[par] = s;
+    }
+    __syncthreads();
+    const double2 s = result[par];
     par ^= 1;
     return s;
 }
@@ -886,6 +906,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     extern __shared__ double dyn[];
     __shared__ double2 warps[FT / 32];
     __shared__ double2 slots[2][CL];
+    __shared__ double2 result[2];
     __shared__ int bound[CL + 1];
     __shared__ int s_nruns;
     __shared__ double* s_dptr[CL];
@@ -934,7 +955,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     double* s_ad = s_z + m;
     double* s_piv = s_ad + m;
     double* s_coef = s_piv + m;
-    unsigned* s_run = reinterpret_cast<unsigned*>(s_coef + m);   // first | last << 16, CTA-local
+    double* s_rcp = s_coef + m;   // 1 / pivot
+    unsigned* s_run = reinterpret_cast<unsigned*>(s_rcp + m);   // first | last << 16, CTA-local
     if (threadIdx.x < CL) s_dptr[threadIdx.x] = cluster.map_shared_rank(s_d, (int)threadIdx.x);
     double* x = a.x + base + lo;
     double* degree = a.degree + base + lo;
@@ -947,7 +969,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     float lo_f = FLT_MAX;
     for (int j = threadIdx.x; j < m; j += FT) lo_f = fminf(lo_f, a.filled[mem[lo + j]]);
     const double entry_level =
-        cluster_combine(make_double2((double)lo_f, 0.0), MinMax2(), warps, slots, par, q).x;
+        cluster_combine(make_double2((double)lo_f, 0.0), MinMax2(), warps, slots, result, par, q).x;
     double hi = -INFINITY;
     for (int j = threadIdx.x; j < m; j += FT) {
         const int k = lo + j;
@@ -991,7 +1013,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
             s_run[atomicAdd(&s_nruns, 1)] = (unsigned)j | ((unsigned)(e - lo) << 16);
         }
     }
-    const double entry_height = cluster_combine(make_double2(0.0, hi), MinMax2(), warps, slots, par, q).y;
+    const double entry_height = cluster_combine(make_double2(0.0, hi), MinMax2(), warps, slots, result, par, q).y;
     const int runs = s_nruns;
 
     // Thomas pivots down each run (FlatRouting.kt:388-395) and ns / pivot for the way back up.
@@ -1001,6 +1023,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
         for (int j = first;; ++j) {
             s_piv[j] = p;
             s_coef[j] = __ddiv_rn(a.ns, p);
+            s_rcp[j] = __ddiv_rn(1.0, p);
             if (j == last) break;
             p = __dsub_rn(degree[j + 1], __ddiv_rn(UNITW ? 1.0 : __dmul_rn(a.ns, a.ns), p));
         }
@@ -1010,10 +1033,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     auto precondition = [&]() {
         for (int i = threadIdx.x; i < runs; i += FT) {
             const int first = (int)(s_run[i] & 0xFFFFu), last = (int)(s_run[i] >> 16);
-            double v = __ddiv_rn(__dadd_rn(s_r[first], 0.0), s_piv[first]);
+            double v = div_by(__dadd_rn(s_r[first], 0.0), s_piv[first], s_rcp[first]);
             s_z[first] = v;
             for (int j = first + 1; j <= last; ++j) {
-                v = __ddiv_rn(__dadd_rn(s_r[j], UNITW ? v : __dmul_rn(a.ns, v)), s_piv[j]);
+                v = div_by(__dadd_rn(s_r[j], UNITW ? v : __dmul_rn(a.ns, v)), s_piv[j], s_rcp[j]);
                 s_z[j] = v;
             }
             double below = v;
@@ -1035,7 +1058,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
         rn = __dadd_rn(rn, __dmul_rn(rv, rv));
         ra = __dadd_rn(ra, __dmul_rn(rv, zv));
     }
-    double2 sums = cluster_combine(make_double2(rn, ra), Sum2(), warps, slots, par, q);   // also publishes d
+    double2 sums = cluster_combine(make_double2(rn, ra), Sum2(), warps, slots, result, par, q);   // also publishes d
     double rnorm = sums.x, rap = sums.y;
     const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
     const int most = 64 + (int)(8.0 * sqrt((double)n));
@@ -1057,7 +1080,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
             s_ad[j] = sum;
             e = __dadd_rn(e, __dmul_rn(dk, sum));
         }
-        const double energy = cluster_combine(make_double2(e, 0.0), Sum2(), warps, slots, par, q).x;
+        const double energy = cluster_combine(make_double2(e, 0.0), Sum2(), warps, slots, result, par, q).x;
         if (energy <= 0.0 || rap <= 0.0) break;
         const double step = __ddiv_rn(rap, energy);
         for (int j = threadIdx.x; j < m; j += FT) {
@@ -1073,7 +1096,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
             nn = __dadd_rn(nn, __dmul_rn(rv, rv));
             na = __dadd_rn(na, __dmul_rn(rv, s_z[j]));
         }
-        sums = cluster_combine(make_double2(nn, na), Sum2(), warps, slots, par, q);
+        sums = cluster_combine(make_double2(nn, na), Sum2(), warps, slots, result, par, q);
         const double improvement = __ddiv_rn(sums.y, rap);
         for (int j = threadIdx.x; j < m; j += FT) s_d[j] = __dadd_rn(s_z[j], __dmul_rn(improvement, s_d[j]));
         cluster.sync();   // every CTA's new d before the next Laplacian reads it
@@ -1087,7 +1110,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
         if (!(v > 0.0)) positive = 0;
         if (v > top) top = v;
     }
-    const double2 pt = cluster_combine(make_double2(positive ? 1.0 : 0.0, top), MinMax2(), warps, slots, par, q);
+    const double2 pt = cluster_combine(make_double2(positive ? 1.0 : 0.0, top), MinMax2(), warps, slots, result, par, q);
     const double highest = pt.y;
 
     // FlatRouting.layInBand (FlatRouting.kt:455-489) over the cluster.
@@ -1116,7 +1139,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
             }
             if (!lower) ok = 0.0;
         }
-        ok = cluster_combine(make_double2(ok, 0.0), MinMax2(), warps, slots, par, q).x;
+        ok = cluster_combine(make_double2(ok, 0.0), MinMax2(), warps, slots, result, par, q).x;
         if (ok <= 0.0) {
             for (int j = threadIdx.x; j < m; j += FT) a.surface[mem[lo + j]] = (double)a.filled[mem[lo + j]];
             laid = false;
@@ -1138,7 +1161,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int flats) {
     const unsigned FULL = 0xFFFFFFFFu;
-    __shared__ double s_right[WF][32], s_into[WF][32], s_piv[WF][32], s_coef[WF][32], s_d[WF][32];
+    __shared__ double s_right[WF][32], s_into[WF][32], s_piv[WF][32], s_coef[WF][32], s_rcp[WF][32], s_d[WF][32];
     __shared__ int s_cont[WF][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int f = blockIdx.x * WF + w;
@@ -1220,6 +1243,7 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
         while (true) {
             s_piv[w][j] = p;
             s_coef[w][j] = __ddiv_rn(a.ns, p);
+            s_rcp[w][j] = __ddiv_rn(1.0, p);
             if (!s_cont[w][j]) break;
             ++j;
             p = __dsub_rn(s_right[w][j], __ddiv_rn(__dmul_rn(a.ns, a.ns), p));
@@ -1233,11 +1257,11 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
         __syncwarp();
         if (head) {
             int j = lane;
-            double v = __ddiv_rn(__dadd_rn(s_right[w][j], 0.0), s_piv[w][j]);
+            double v = div_by(__dadd_rn(s_right[w][j], 0.0), s_piv[w][j], s_rcp[w][j]);
             s_into[w][j] = v;
             while (s_cont[w][j]) {
                 ++j;
-                v = __ddiv_rn(__dadd_rn(s_right[w][j], __dmul_rn(a.ns, v)), s_piv[w][j]);
+                v = div_by(__dadd_rn(s_right[w][j], __dmul_rn(a.ns, v)), s_piv[w][j], s_rcp[w][j]);
                 s_into[w][j] = v;
             }
             double below = v;
@@ -1424,8 +1448,11 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             if (ctr[1] > 0) {
                 // Per CTA a share of the largest flat with room for the run-head rounding of its bounds;
                 // a flat whose ranges need more goes to k_flat_solve.
-                const int cap = std::min(CL_RANGE_MAX, std::min(ctr[4], 2 * ((ctr[4] + CL - 1) / CL) + 64));
-                const size_t bytes = (size_t)cap * SM_BYTES_PER_MEMBER;
+                const int cap = std::min(std::min(CL_RANGE_MAX, CL_SMEM_MEMBERS),
+                                         std::min(ctr[4], 2 * ((ctr[4] + CL - 1) / CL) + 64));
+                // More than half an SM's shared memory, so that no two CTAs of a cluster share an SM (and
+                // its FP64 pipe, which bounds the solve).
+                const size_t bytes = std::max((size_t)cap * SM_BYTES_PER_MEMBER, (size_t)116 * 1024);
                 const bool unit = a.ew == 1.0 && a.ns == 1.0 && a.diag == 1.0;
                 auto kernel = unit ? k_flat_solve_cl<true> : k_flat_solve_cl<false>;
                 CG_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
