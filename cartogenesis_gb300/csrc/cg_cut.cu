@@ -8,8 +8,9 @@
 //  - the histogram: per (row, bin) cell counts are exact integers, and each bin's sequential sum
 //    over the rows in order is rebuilt by one warp, 32 rows at a time: inside one binade of the
 //    running sum every addition adds a whole number of ulps, so a chunk is an integer prefix sum
-//    (cg::warp_chunk_sum); a chunk that crosses a binade or meets a tie is replayed row by row with
-//    cg::seq_repeat_add, which takes `count` equal additions in closed form (csrc/cg_fpemu.h);
+//    (cg::warp_seq_sum, on the integer pipes); a row whose additions cross a binade or meet a tie is
+//    taken alone by cg::seq_repeat_add, which takes `count` equal additions in closed form
+//    (csrc/cg_fpemu.h);
 //  - the bracket: its cells are sorted on the device and walked in the reference's order by one
 //    warp with the same chunking.
 // min, max, the bin of a cell and the land/relative split are elementwise or exact reductions.
@@ -112,8 +113,7 @@ __global__ void __launch_bounds__(512) k_row_counts(const float* __restrict__ h,
 }
 
 // One warp per bin: the reference's sequential sum `histogram[bin] += rowWeights[row]`, in cell
-// order, replayed exactly, 32 rows at a time (cg::warp_chunk_sum), a chunk that leaves its binade or
-// meets a tie replayed row by row by lane 0 (cg::seq_repeat_add).
+// order, replayed exactly, 32 rows at a time (cg::warp_seq_sum).
 __global__ void k_bin_sums(const unsigned* __restrict__ counts, const double* __restrict__ w, int H,
                            const CutState* s, double* __restrict__ hist) {
     const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -125,17 +125,8 @@ __global__ void k_bin_sums(const unsigned* __restrict__ counts, const double* __
         unsigned c = r < H ? counts[(size_t)r * BINS + b] : 0u;
         double wr = r < H ? w[r] : 0.0;
         if (!__any_sync(0xFFFFFFFFu, c != 0u)) continue;
-        double before, after;
-        if (warp_chunk_sum(acc, wr, (int64_t)c, &before, &after)) {
-            acc = after;
-            continue;
-        }
-        // Exact replay of the chunk's rows in order.
-        for (int j = 0; j < 32; ++j) {
-            unsigned cj = __shfl_sync(0xFFFFFFFFu, c, j);
-            double wj = __shfl_sync(0xFFFFFFFFu, wr, j);
-            if (cj) acc = seq_repeat_add(acc, wj, (int64_t)cj);
-        }
+        double before;
+        acc = warp_seq_sum(acc, wr, (int64_t)c, &before);
     }
     if (lane == 0) hist[b] = acc;
 }
@@ -227,7 +218,7 @@ __global__ void k_pad(long long* keys, int n, int P2) {
 // it is clean (no tie at half a unit, the step stays in the binade); a block scan of the d_i; the
 // answer is the first entry whose sum before it reaches the target, provided every earlier entry of
 // the chunk is clean. From the first entry that is not, warp 0 replays the rest of the chunk exactly
-// (32 entries at a time with cg::warp_chunk_sum, entry by entry where that fails).
+// (32 entries at a time with cg::warp_seq_sum).
 constexpr int WALK_THREADS = 1024;
 constexpr int WALK_PER = 8;
 constexpr int WALK_CHUNK = WALK_THREADS * WALK_PER;
@@ -244,26 +235,14 @@ __device__ bool walk_replay(const long long* __restrict__ keys, const double* __
         const int i = base + lane;
         const int cell = i < to ? (int)(keys[i] & 0xFFFFFFFFLL) : -1;
         const double wi = i < to ? w[pdiv(cell, W)] : 0.0;
-        double before, after;
-        if (warp_chunk_sum(below, wi, i < to ? 1 : 0, &before, &after)) {
-            const unsigned hit = __ballot_sync(FULL, i < to && before >= target);
-            if (hit) {
-                *cell_out = __shfl_sync(FULL, cell, __ffs(hit) - 1);
-                return true;
-            }
-            below = after;
-            continue;
+        double before;
+        const double after = warp_seq_sum(below, wi, i < to ? 1 : 0, &before);
+        const unsigned hit = __ballot_sync(FULL, i < to && before >= target);
+        if (hit) {
+            *cell_out = __shfl_sync(FULL, cell, __ffs(hit) - 1);
+            return true;
         }
-        for (int j = 0; j < 32; ++j) {
-            const int cj = __shfl_sync(FULL, cell, j);
-            const double wj = __shfl_sync(FULL, wi, j);
-            if (cj < 0) break;
-            if (below >= target) {
-                *cell_out = cj;
-                return true;
-            }
-            below += wj;
-        }
+        below = after;
     }
     *below_io = below;
     return false;

@@ -75,49 +75,80 @@ CG_HD double seq_repeat_add(double s, double w, int64_t c) {
 }
 
 #ifdef __CUDACC__
-// One warp, 32 terms: each lane adds `count` copies of its term `w` (> 0) to a running sum `s` that
-// is the same in every lane, lanes in order. When s > 0 and every addition of the chunk stays inside
-// s's binade with no tie at half an ulp, every addition adds a fixed whole number of ulps d, so the
-// chunk is an integer prefix sum. Then it returns true with, per lane, the sum before that lane's
-// first addition (*before) and the sum after the whole chunk (*after, same in all lanes); otherwise
-// it returns false and the caller replays the chunk one addition at a time.
-__device__ __forceinline__ bool warp_chunk_sum(double s, double w, int64_t count, double* before, double* after) {
+// The double m * 2^(e-52) for 2^52 <= m <= 2^53 (the top of the binade [2^e, 2^(e+1)) included).
+__device__ __forceinline__ double from_binade(int64_t m, int e) {
+    if (m == ((int64_t)1 << 53)) return __longlong_as_double((long long)(e + 1 + 1023) << 52);
+    return __longlong_as_double(((long long)(e + 1023) << 52) | (long long)(m - ((int64_t)1 << 52)));
+}
+
+// One warp's share of a sequential double sum: lane j adds `count` copies of its term w > 0 (count
+// may be 0), lanes in order, to a running sum s >= 0 that is the same in every lane. Returns the
+// sum after the whole warp (the same in every lane) and sets *before, per lane, to the sum before
+// the lane's first addition. Exact, and on the integer pipes: while the sum stays in one binade
+// [2^e, 2^(e+1)) and no addition falls on a tie, every addition adds a whole number d of units
+// U = 2^(e-52) (d = w / U rounded to nearest, read off the bits of w), so a run of lanes is an
+// integer prefix sum of count * d. The first lane whose additions would leave the binade or meet a
+// tie is taken alone by seq_repeat_add, and the scan resumes after it.
+__device__ double warp_seq_sum(double s, double w, int64_t count, double* before) {
     const unsigned FULL = 0xFFFFFFFFu;
     const int64_t TOP = (int64_t)1 << 53;
     const int lane = threadIdx.x & 31;
-    if (!(s > 0.0)) return false;
-    int e = ilogb(s);
-    double U = ldexp(1.0, e - 52);
-    int64_t m = (int64_t)(s / U);
-    bool ok = true;
-    int64_t inc = 0, q = 0, d = 0;
-    if (count > 0) {
-        double x = ldexp(w, 52 - e);   // w / U, exact
-        if (!(x < 9.0e15)) {
-            ok = false;
+    const long long wb = __double_as_longlong(w);
+    const int ew = (int)((wb >> 52) & 0x7FF) - 1023;
+    const int64_t mw = (int64_t)((wb & ((1LL << 52) - 1)) | (1LL << 52));
+    const bool w_normal = ((wb >> 52) & 0x7FF) != 0 && wb > 0;
+    int start = 0;
+    while (start < 32) {
+        const long long sb = __double_as_longlong(s);
+        const int es = (int)((sb >> 52) & 0x7FF);
+        int first_bad;
+        int64_t m = 0, excl = 0, total = 0;
+        int e = 0;
+        if (sb > 0 && es != 0 && es != 0x7FF) {   // s positive and normal: it has a binade
+            e = es - 1023;
+            m = (int64_t)((sb & ((1LL << 52) - 1)) | (1LL << 52));
+            int64_t q = 0, d = 0, inc = 0;
+            bool ok = true;
+            if (lane >= start && count > 0) {
+                const int shift = e - ew;
+                if (!w_normal || shift < 0) {
+                    ok = false;   // the term alone reaches the next binade
+                } else if (shift == 0) {
+                    q = d = mw;
+                } else if (shift < 63) {
+                    q = mw >> shift;
+                    const int64_t rem = mw & (((int64_t)1 << shift) - 1), half = (int64_t)1 << (shift - 1);
+                    if (rem == half) ok = false;   // a tie: the parity of the sum decides
+                    d = q + (rem > half ? 1 : 0);
+                }   // shift >= 63: w is below half a unit, every addition rounds back (d = 0)
+                if (ok && d > 0 && count > TOP / d) ok = false;
+                if (ok) inc = count * d;
+            }
+            int64_t incl = inc;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            excl = incl - inc;
+            total = __shfl_sync(FULL, incl, 31);
+            // Every addition of this lane stays in the binade: the last one starts at m + excl + (count-1) d.
+            if (ok && lane >= start && count > 0 && m + excl + (count - 1) * d + q > TOP - 1) ok = false;
+            const unsigned bad = __ballot_sync(FULL, !ok);
+            first_bad = bad ? __ffs(bad) - 1 : 32;
+            if (lane >= start && lane < first_bad) *before = from_binade(m + excl, e);
+            if (first_bad == 32) return from_binade(m + total, e);
+            s = from_binade(m + __shfl_sync(FULL, excl, first_bad), e);
         } else {
-            q = (int64_t)x;
-            double f = x - (double)q;
-            if (f == 0.5) ok = false;
-            d = q + (f > 0.5 ? 1 : 0);
-            if (d > 0 && count > TOP / d) ok = false;
-            else inc = count * d;
+            first_bad = start;   // no binade (zero or subnormal sum): one lane at a time
         }
+        // Lane first_bad alone, in closed form.
+        const double wj = __shfl_sync(FULL, w, first_bad);
+        const int64_t cj = __shfl_sync(FULL, count, first_bad);
+        if (lane == first_bad) *before = s;
+        if (cj > 0) s = seq_repeat_add(s, wj, cj);
+        start = first_bad + 1;
     }
-    // Exclusive prefix of the increments across the warp.
-    int64_t incl = inc;
-    for (int o = 1; o < 32; o <<= 1) {
-        int64_t t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-    }
-    int64_t excl = incl - inc;
-    // Every step of this lane stays in the binade: the last one starts at m + excl + (count-1) d.
-    if (ok && count > 0 && m + excl + (count - 1) * d + q > TOP - 1) ok = false;
-    if (!__all_sync(FULL, ok)) return false;
-    int64_t total = __shfl_sync(FULL, incl, 31);
-    *before = (double)(m + excl) * U;
-    *after = (double)(m + total) * U;
-    return true;
+    return s;
 }
 #endif
 
