@@ -22,7 +22,9 @@
 //      The levels from the lowest changed one upward are recomputed, and the check repeats; each
 //      replay settles its level for good, so the lowest open level only rises. A level too large
 //      to replay (over 2^18 cells) is reported as unresolved.
+#include <algorithm>
 #include <cfloat>
+#include <cooperative_groups.h>
 #include <climits>
 #include <vector>
 
@@ -30,6 +32,8 @@
 #include "cg_internal.h"
 
 namespace cg {
+
+namespace cgr = cooperative_groups;
 
 namespace {
 
@@ -95,10 +99,20 @@ __global__ void k_fill_init(const uint8_t* __restrict__ land, const float* __res
     }
 }
 
-// (1) pointer jumping to the chain's root.
-__global__ void k_jump(const int* __restrict__ src, int* __restrict__ dst, size_t N) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = src[src[i]];
+// (1) pointer jumping to the chain's root, in place: p[i] <- p[p[i]]. Whatever a concurrent update
+// lets a thread read is an ancestor of i on its chain, so the pass only jumps further, and a pass
+// that changes no pointer leaves every cell on its root. `changed` is set when some pointer moved.
+__global__ void k_jump(int* __restrict__ p, size_t N, int* __restrict__ changed) {
+    bool moved = false;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        const int o = p[i];
+        const int n = p[o];
+        if (n != o) {
+            p[i] = n;
+            moved = true;
+        }
+    }
+    if (__any_sync(0xFFFFFFFFu, moved) && (threadIdx.x & 31) == 0) atomicOr(changed, 1);
 }
 
 __global__ void k_mark_drained(const int* __restrict__ root, const float* __restrict__ g, size_t N,
@@ -113,28 +127,32 @@ __global__ void k_mark_drained(const int* __restrict__ root, const float* __rest
     }
 }
 
-// (2) tile relaxation. Each CTA owns a 32x32 tile, loads f and g with a one-cell halo, relaxes its
-// OPEN cells to local convergence, writes back what fell, and activates the neighbouring tiles if
-// a border cell fell. PINNED cells take their designated parent instead of the minimum.
-__global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, const float* __restrict__ g,
-                                                     const uint8_t* __restrict__ cls,
-                                                     const int* __restrict__ pin_parent, int W, int H, int tiles_x,
-                                                     int tiles_y, const uint8_t* __restrict__ act_in,
-                                                     uint8_t* __restrict__ act_out, FillCounters* cnt,
-                                                     int max_sweeps) {
-    const int tile = blockIdx.x;
-    if (!act_in[tile]) return;
+// (2) tile relaxation. A CTA takes a 32x32 tile, loads f and g with a one-cell halo, relaxes its
+// OPEN cells to local convergence, and writes back what fell. PINNED cells take their designated
+// parent instead of the minimum. Returns (in every thread) whether a border cell fell or the tile
+// is still moving: then it and its neighbours go on the next pass's list.
+struct TileSmem {
+    float sf[T + 2][T + 3];
+    float sg[T][T + 1];
+    uint8_t sc[T][T];
+    int any_border;
+};
+
+__device__ __forceinline__ bool relax_tile(TileSmem& sm, int tile, float* __restrict__ f, const float* __restrict__ g,
+                           const uint8_t* __restrict__ cls, const int* __restrict__ pin_parent, int W, int H,
+                           int tiles_x, int max_sweeps) {
     const int ty0 = (tile / tiles_x) * T, tx0 = (tile % tiles_x) * T;
-    __shared__ float sf[T + 2][T + 3];
-    __shared__ float sg[T][T + 1];
-    __shared__ uint8_t sc[T][T];
-    __shared__ int any_border, any_change;
+    auto& sf = sm.sf;
+    auto& sg = sm.sg;
+    auto& sc = sm.sc;
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;   // 32 x 8
     for (int i = threadIdx.x; i < (T + 2) * (T + 2); i += 256) {
         int yy = i / (T + 2), xx = i % (T + 2);
         int gy = ty0 + yy - 1;
         float v = INFINITY;
-        if (gy >= 0 && gy < H) v = f[(size_t)gy * W + wrap_col(tx0 + xx - 1, W)];
+        // L1-bypassing loads: neighbouring tiles on other SMs wrote these in earlier passes of the
+        // same launch, and a stale L1 line could make the tile look settled.
+        if (gy >= 0 && gy < H) v = __ldcg(f + (size_t)gy * W + wrap_col(tx0 + xx - 1, W));
         sf[yy][xx] = v;
     }
     for (int i = threadIdx.x; i < T * T; i += 256) {
@@ -144,7 +162,6 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
         sg[yy][xx] = in ? g[(size_t)gy * W + gx] : 0.0f;
         sc[yy][xx] = in ? cls[(size_t)gy * W + gx] : (uint8_t)C_WATER;
     }
-    if (threadIdx.x == 0) any_border = 0;
     __syncthreads();
     bool border_changed = false;
     int unsettled = 1;
@@ -188,9 +205,7 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
         unsettled = __syncthreads_or(changed);
     }
     // Still moving after the sweep budget: run this tile again next pass.
-    if ((__syncthreads_or(border_changed) || unsettled) && threadIdx.x == 0) any_border = 1;
-    // Write back and report.
-    bool wrote = false;
+    const bool again = __syncthreads_or(border_changed) || unsettled;
     for (int yy = ly; yy < T; yy += TH) {
         int gy = ty0 + yy, gx = tx0 + lx;
         if (gy >= H || gx >= W) continue;
@@ -198,35 +213,61 @@ __global__ void __launch_bounds__(256) k_relax_tiles(float* __restrict__ f, cons
         if (c != C_OPEN && !follows_parent(c)) continue;
         float v = sf[yy + 1][lx + 1];
         size_t idx = (size_t)gy * W + gx;
-        if (f[idx] != v) {
-            f[idx] = v;
-            wrote = true;
-        }
+        if (__ldcg(f + idx) != v) f[idx] = v;
     }
-    if (threadIdx.x == 0) any_change = 0;
-    __syncthreads();
-    if (wrote) any_change = 1;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (any_change) atomicAdd(&cnt->changed, 1);
-        if (any_border) {
-            int tyi = tile / tiles_x, txi = tile % tiles_x;
-            for (int dy = -1; dy <= 1; ++dy) {
-                int y = tyi + dy;
-                if (y < 0 || y >= tiles_y) continue;
-                for (int dx = -1; dx <= 1; ++dx) {
-                    int x = (txi + dx + tiles_x) % tiles_x;
-                    act_out[y * tiles_x + x] = 1;
-                }
-            }
-            atomicAdd(&cnt->active, 1);
-        }
-    }
+    __syncthreads();   // the shared tile is free for the next one
+    return again;
 }
 
-// A tile is active for the first pass if it holds a cell still to settle (a level reset to +inf).
+// The relaxation passes in one cooperative launch. Pass p takes the tiles of list[p & 1] (each marked
+// in mark[p & 1]); a tile that must run again puts itself and its 8 neighbours on the other list,
+// once each (the mark), and clears its own mark for the list after next. A grid barrier separates
+// the passes; the loop ends when a pass leaves the next list empty, or at max_passes (timed_out).
+struct RelaxArgs {
+    float* f;
+    const float* g;
+    const uint8_t* cls;
+    const int* pin;
+    int W, H, tiles_x, tiles_y;
+    int* list[2];
+    int* mark[2];
+    int* count;   // [2]
+    int* timed_out;
+    int max_passes;
+};
+
+__global__ void __launch_bounds__(256) k_relax_passes(RelaxArgs a) {
+    cgr::grid_group grid = cgr::this_grid();
+    __shared__ TileSmem sm;
+    int pass = 0;
+    for (; pass < a.max_passes; ++pass) {
+        const int cur = pass & 1, nxt = cur ^ 1;
+        const int n = *(volatile int*)&a.count[cur];
+        if (n == 0) break;
+        for (int t = blockIdx.x; t < n; t += gridDim.x) {
+            const int tile = __ldcg(a.list[cur] + t);
+            if (threadIdx.x == 0) a.mark[cur][tile] = 0;
+            if (relax_tile(sm, tile, a.f, a.g, a.cls, a.pin, a.W, a.H, a.tiles_x, 4 * T) && threadIdx.x < 9) {
+                const int dy = (int)threadIdx.x / 3 - 1, dx = (int)threadIdx.x % 3 - 1;
+                const int y = tile / a.tiles_x + dy;
+                if (y >= 0 && y < a.tiles_y) {
+                    const int nb = y * a.tiles_x + (tile % a.tiles_x + dx + a.tiles_x) % a.tiles_x;
+                    if (atomicExch(&a.mark[nxt][nb], 1) == 0) a.list[nxt][atomicAdd(&a.count[nxt], 1)] = nb;
+                }
+            }
+        }
+        grid.sync();
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.count[cur] = 0;
+        grid.sync();
+    }
+    if (pass == a.max_passes && blockIdx.x == 0 && threadIdx.x == 0 && *(volatile int*)&a.count[pass & 1] != 0)
+        *a.timed_out = 1;
+}
+
+// A tile is on the first pass's list if it holds a cell still to settle (a level reset to +inf).
 __global__ void k_tiles_with_open(const uint8_t* __restrict__ cls, const float* __restrict__ f, int W, int H,
-                                  int tiles_x, int tiles_y, uint8_t* __restrict__ act) {
+                                  int tiles_x, int* __restrict__ mark, int* __restrict__ list,
+                                  int* __restrict__ count) {
     int tile = blockIdx.x;
     const int ty0 = (tile / tiles_x) * T, tx0 = (tile % tiles_x) * T;
     int has = 0;
@@ -238,7 +279,10 @@ __global__ void k_tiles_with_open(const uint8_t* __restrict__ cls, const float* 
         }
     }
     has = __syncthreads_or(has);
-    if (threadIdx.x == 0) act[tile] = has ? 1 : 0;
+    if (threadIdx.x == 0) {
+        mark[tile] = has ? 1 : 0;
+        if (has) list[atomicAdd(count, 1)] = tile;
+    }
 }
 
 // (3) the exact parent check. For each OPEN/PINNED cell: its least-Q neighbours; if they give
@@ -461,26 +505,50 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     cudaStream_t sm = ctx->stream;
     CG_BUF(uint8_t, d_cls, ctx, S_FILLFLAG, N);
     CG_BUF(int, d_ptr, ctx, S_PTR, N);
-    CG_BUF(int, d_ptr2, ctx, S_PTR2, N);
+    CG_BUF(int, d_moved, ctx, S_PTR2, 2);   // the jumping passes' change flags
     CG_BUF(int, d_pin, ctx, S_FILLQ, N);
     int tiles_x = (W + T - 1) / T, tiles_y = (H + T - 1) / T, tiles = tiles_x * tiles_y;
-    CG_BUF(uint8_t, d_act, ctx, S_TILEFLAG, 2 * (size_t)tiles);
+    // Two tile lists and their marks, two list counts, the timeout flag (zeroed before each relaxation).
+    CG_BUF(int, d_marks, ctx, S_TILEFLAG, 2 * (size_t)tiles);
+    CG_BUF(int, d_lists, ctx, S_FILLLIST, 2 * (size_t)tiles + 4);
+    RelaxArgs ra;
+    ra.f = d_filled;
+    ra.g = d_rel;
+    ra.cls = d_cls;
+    ra.pin = d_pin;
+    ra.W = W;
+    ra.H = H;
+    ra.tiles_x = tiles_x;
+    ra.tiles_y = tiles_y;
+    ra.list[0] = d_lists;
+    ra.list[1] = d_lists + tiles;
+    ra.count = d_lists + 2 * (size_t)tiles;
+    ra.timed_out = ra.count + 2;
+    ra.mark[0] = d_marks;
+    ra.mark[1] = d_marks + tiles;
+    ra.max_passes = 4 * (tiles_x + tiles_y) + 64;
+    int per_sm = 0;
+    CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax_passes, 256, 0));
+    if (per_sm < 1) return fail(ctx, CG_CUDA, "k_relax_passes cannot be resident");
+    const int relax_grid = ctx->num_sms * std::min(per_sm, 8);
     CG_BUF(FillCounters, d_cnt, ctx, S_FILLF, 1);
     int grid = ctx->num_sms * 8;
     CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(FillCounters), sm));
     CG_LAUNCH(ctx) k_fill_init<<<grid, 256, 0, sm>>>(d_land, d_rel, W, H, d_cls, d_filled, d_ptr);
-    // Chains are at most N long: ceil(log2 N) jumps reach every root.
+    // Chains are at most N long: ceil(log2 N) jumps reach every root; most worlds need far fewer, so
+    // the passes stop at the first that moves no pointer (checked every second pass).
     int jumps = 1;
     while (((size_t)1 << jumps) < N) ++jumps;
-    int* a = d_ptr;
-    int* b = d_ptr2;
-    for (int j = 0; j < jumps; ++j) {
-        CG_LAUNCH(ctx) k_jump<<<grid, 256, 0, sm>>>(a, b, N);
-        int* t = a;
-        a = b;
-        b = t;
+    for (int j = 0; j < jumps + 2; j += 2) {
+        CG_CUDA(ctx, cudaMemsetAsync(d_moved, 0, 2 * sizeof(int), sm));
+        CG_LAUNCH(ctx) k_jump<<<grid, 256, 0, sm>>>(d_ptr, N, d_moved);
+        CG_LAUNCH(ctx) k_jump<<<grid, 256, 0, sm>>>(d_ptr, N, d_moved + 1);
+        int moved[2] = {0, 0};
+        CG_CUDA(ctx, cudaMemcpyAsync(moved, d_moved, sizeof(moved), cudaMemcpyDeviceToHost, sm));
+        CG_CUDA(ctx, cudaStreamSynchronize(sm));
+        if (!moved[1]) break;
     }
-    CG_LAUNCH(ctx) k_mark_drained<<<grid, 256, 0, sm>>>(a, d_rel, N, d_cls, d_filled);
+    CG_LAUNCH(ctx) k_mark_drained<<<grid, 256, 0, sm>>>(d_ptr, d_rel, N, d_cls, d_filled);
     CG_CHECK_LAUNCH(ctx);
 
     // Scratch of the level replays: a generation mark per cell, the level's cells and the heap.
@@ -499,30 +567,22 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     // holding a tie the index rule cannot order; the cap is a guard, not the expected exit.
     const int max_repairs = 64;
     for (int repair = 0; repair <= max_repairs; ++repair) {
-        uint8_t* act = d_act;
-        uint8_t* nxt = d_act + tiles;
-        CG_LAUNCH(ctx) k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, d_filled, W, H, tiles_x, tiles_y, act);
+        CG_CUDA(ctx, cudaMemsetAsync(d_lists, 0, (2 * (size_t)tiles + 4) * sizeof(int), sm));
+        CG_CUDA(ctx, cudaMemsetAsync(d_marks, 0, 2 * (size_t)tiles * sizeof(int), sm));
+        CG_LAUNCH(ctx) k_tiles_with_open<<<tiles, 256, 0, sm>>>(d_cls, d_filled, W, H, tiles_x, ra.mark[0], ra.list[0],
+                                                                ra.count);
         CG_CHECK_LAUNCH(ctx);
-        // Relax until no tile changes. A bounded loop: every pass lowers some level or stops, and
-        // levels only take values from a finite set; the cap is a guard, not the expected exit.
-        const int max_passes = 4 * (tiles_x + tiles_y) + 64;
-        int pass = 0;
-        for (; pass < max_passes; ++pass) {
-            CG_CUDA(ctx, cudaMemsetAsync(nxt, 0, tiles, sm));
-            CG_CUDA(ctx, cudaMemsetAsync(&d_cnt->active, 0, 2 * sizeof(int), sm));
-            CG_LAUNCH(ctx) k_relax_tiles<<<tiles, 256, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, W, H, tiles_x, tiles_y, act, nxt,
-                                                 d_cnt, 4 * T);
-            CG_CHECK_LAUNCH(ctx);
-            uint8_t* t = act;
-            act = nxt;
-            nxt = t;
-            if ((pass & 3) == 3 || pass < 4) {
-                CG_CUDA(ctx, cudaMemcpyAsync(&hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, sm));
-                CG_CUDA(ctx, cudaStreamSynchronize(sm));
-                if (hc.active == 0) break;
-            }
+        // Relax until no tile changes, in one cooperative launch. Bounded: every pass lowers some level
+        // or stops, and levels only take values from a finite set; the cap is a guard, not the exit.
+        {
+            void* kargs[] = {&ra};
+            ctx->launches++;
+            CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_relax_passes, relax_grid, 256, kargs, 0, sm));
         }
-        if (pass >= max_passes) return fail(ctx, CG_TIMEOUT, "fill relaxation did not settle in %d passes", pass);
+        int timed_out = 0;
+        CG_CUDA(ctx, cudaMemcpyAsync(&timed_out, ra.timed_out, sizeof(int), cudaMemcpyDeviceToHost, sm));
+        CG_CUDA(ctx, cudaStreamSynchronize(sm));
+        if (timed_out) return fail(ctx, CG_TIMEOUT, "fill relaxation did not settle in %d passes", ra.max_passes);
         FillCounters zero{};
         zero.min_level = INT_MAX;
         zero.repair_level = INT_MAX;
