@@ -230,19 +230,52 @@ __device__ int steepest_neighbour(int W, int H, const double* __restrict__ rs, i
     return best;
 }
 
-__global__ void k_receivers(const uint8_t* __restrict__ land, const double* __restrict__ surface, int W, int H,
-                            Steps st, long long seed, int by_facet, int32_t* __restrict__ recv) {
-    size_t N = (size_t)W * H;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (!land[i]) {
-            recv[i] = -1;
-            continue;
+// Receivers of every land cell (sea cells get -1). The facet rule is FP64 work, and an FP64 warp
+// instruction costs the same with one lane active as with 32, so each warp compacts the land cells
+// of the chunks it scans into a small queue in shared memory and runs the rule 32 land cells at a
+// time.
+constexpr int RECV_THREADS = 256;
+
+__device__ __forceinline__ int receiver_of(int cell, const double* __restrict__ surface, int W, int H, Steps st,
+                                           long long seed, int by_facet, bool unit) {
+    const int row = pdiv(cell, W), col = pmod(cell, W);
+    return !by_facet ? steepest_neighbour(W, H, surface, col, row, st)
+           : unit    ? facet_receiver<true>(W, H, surface, col, row, st, seed)
+                     : facet_receiver<false>(W, H, surface, col, row, st, seed);
+}
+
+__global__ void __launch_bounds__(RECV_THREADS) k_receivers(const uint8_t* __restrict__ land,
+                                                            const double* __restrict__ surface, int W, int H,
+                                                            Steps st, long long seed, int by_facet,
+                                                            int32_t* __restrict__ recv) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    __shared__ int queue[RECV_THREADS / 32][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int* q = queue[warp];
+    const bool unit = st.ew == 1.0f && st.ns == 1.0f;
+    const size_t N = (size_t)W * H;
+    const size_t warps = (size_t)gridDim.x * (RECV_THREADS / 32);
+    int n = 0;   // queued land cells (the same in every lane)
+    for (size_t base = ((size_t)blockIdx.x * (RECV_THREADS / 32) + warp) * 32; base < N; base += warps * 32) {
+        const size_t i = base + lane;
+        const bool l = i < N && land[i];
+        if (i < N && !l) recv[i] = -1;
+        const unsigned m = __ballot_sync(FULL, l);
+        if (l) q[n + __popc(m & ((1u << lane) - 1u))] = (int)i;
+        n += __popc(m);
+        __syncwarp();
+        if (n >= 32) {
+            const int cell = q[lane];
+            recv[cell] = receiver_of(cell, surface, W, H, st, seed, by_facet, unit);
+            __syncwarp();
+            if (lane < n - 32) q[lane] = q[32 + lane];
+            n -= 32;
+            __syncwarp();
         }
-        const int row = pdiv((int)i, W), col = pmod((int)i, W);
-        const bool unit = st.ew == 1.0f && st.ns == 1.0f;
-        recv[i] = !by_facet ? steepest_neighbour(W, H, surface, col, row, st)
-                  : unit    ? facet_receiver<true>(W, H, surface, col, row, st, seed)
-                            : facet_receiver<false>(W, H, surface, col, row, st, seed);
+    }
+    if (lane < n) {
+        const int cell = q[lane];
+        recv[cell] = receiver_of(cell, surface, W, H, st, seed, by_facet, unit);
     }
 }
 
@@ -600,30 +633,44 @@ __global__ void __launch_bounds__(FT) k_flat_solve(FlatArgs a) {
 // pivots, ns / pivot and the run table sit in shared memory; the per-member constants (degree, the
 // member neighbours) and the potential x, which a thread reads only for its own members, stay in
 // global memory. The arithmetic per member and per run is that of k_flat_solve. A dot product is
-// each thread's partial sum in member order, a warp butterfly and an ordered sum over the warps,
-// so its bits are fixed for a given CTA size.
+// each thread's partial sum in member order, then block_reduce2's fixed order, so its bits are fixed
+// for a given CTA size.
 constexpr int MID_FLAT = 512;    // members at most for the 128-thread CTA
 constexpr int SM_BYTES_PER_MEMBER = 7 * 8 + 4;   // seven doubles and one run-table entry
 
-// Sums of u and of v over the CTA, returned to every thread. `buf` (one double2 per warp) must
-// alternate between two arrays from one call to the next: the barrier of the next call is what
-// keeps this call's readers ahead of the call after it.
-template <int NW>
-__device__ __forceinline__ double2 block_sum2(double u, double v, double2* buf) {
-    for (int o = 16; o > 0; o >>= 1) {
-        u = __dadd_rn(u, __shfl_xor_sync(0xFFFFFFFFu, u, o));
-        v = __dadd_rn(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+struct Sum2 {
+    __device__ double2 operator()(double2 a, double2 b) const { return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)); }
+};
+struct MinMax2 {
+    __device__ double2 operator()(double2 a, double2 b) const {
+        return make_double2(a.x < b.x ? a.x : b.x, a.y > b.y ? a.y : b.y);
     }
-    if ((threadIdx.x & 31) == 0) buf[threadIdx.x >> 5] = make_double2(u, v);
+};
+
+// The CTA's combination of v (two values), returned to every thread. Every thread's partial goes to
+// shared memory; the first warp folds the FT / 32 partials of each lane in thread order, then a
+// butterfly over its lanes, and hands the result out. The FP64 pipe is the scarce resource: this
+// takes FT / 32 - 1 + 5 FP64 operations of one warp per value, where a butterfly in every warp
+// takes 5 in each. `buf` holds FT double2 and `out` one; the two barriers keep consecutive calls
+// apart.
+template <int FT, class Op>
+__device__ __forceinline__ double2 block_reduce2(double2 v, Op op, double2* buf, double2* out) {
+    buf[threadIdx.x] = v;
     __syncthreads();
-    double2 s = buf[0];
+    if (threadIdx.x < 32) {
+        double2 s = buf[threadIdx.x];
 #pragma unroll
-    for (int w = 1; w < NW; ++w) {
-        const double2 t = buf[w];
-        s.x = __dadd_rn(s.x, t.x);
-        s.y = __dadd_rn(s.y, t.y);
+        for (int k = 1; k < FT / 32; ++k) s = op(s, buf[threadIdx.x + 32 * k]);
+        for (int o = 16; o > 0; o >>= 1) {
+            double2 t;
+            t.x = __shfl_xor_sync(0xFFFFFFFFu, s.x, o);
+            t.y = __shfl_xor_sync(0xFFFFFFFFu, s.y, o);
+            s = op(s, t);
+        }
+        if (threadIdx.x == 0) *out = s;
     }
-    return s;
+    __syncthreads();
+    return *out;
 }
 
 __device__ __forceinline__ int nbr_lo(int v) { return (int)(short)(v & 0xFFFF); }
@@ -632,12 +679,12 @@ __device__ __forceinline__ int nbr_pack(int lo, int hi) { return (int)(((unsigne
 
 template <int FT>
 __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __restrict__ list) {
-    constexpr int NW = FT / 32;
     extern __shared__ double dyn[];
     __shared__ double shd[32];
     __shared__ float shf[32];
     __shared__ int shi[32];
-    __shared__ double2 sh2[2][NW];
+    __shared__ double2 red[FT];
+    __shared__ double2 red_out;
     __shared__ int s_nruns;
     const int f = list[blockIdx.x];
     const int base = a.off[f];
@@ -765,9 +812,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
         rn = __dadd_rn(rn, __dmul_rn(rv, rv));
         ra = __dadd_rn(ra, __dmul_rn(rv, zv));
     }
-    int parity = 0;
-    double2 sums = block_sum2<NW>(rn, ra, sh2[parity]);
-    parity ^= 1;
+    double2 sums = block_reduce2<FT>(make_double2(rn, ra), Sum2(), red, &red_out);
     double rnorm = sums.x, rap = sums.y;
     const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
     const int most = 64 + (int)(8.0 * sqrt((double)n));
@@ -786,8 +831,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
             s_ad[k] = sum;
             e = __dadd_rn(e, __dmul_rn(dk, sum));
         }
-        const double energy = block_sum2<NW>(e, 0.0, sh2[parity]).x;
-        parity ^= 1;
+        const double energy = block_reduce2<FT>(make_double2(e, 0.0), Sum2(), red, &red_out).x;
         if (energy <= 0.0 || rap <= 0.0) break;
         const double step = __ddiv_rn(rap, energy);
         for (int k = threadIdx.x; k < n; k += FT) {
@@ -803,8 +847,7 @@ __global__ void __launch_bounds__(FT) k_flat_solve_sm(FlatArgs a, const int* __r
             nn = __dadd_rn(nn, __dmul_rn(rv, rv));
             na = __dadd_rn(na, __dmul_rn(rv, s_z[k]));
         }
-        sums = block_sum2<NW>(nn, na, sh2[parity]);
-        parity ^= 1;
+        sums = block_reduce2<FT>(make_double2(nn, na), Sum2(), red, &red_out);
         const double improvement = __ddiv_rn(sums.y, rap);
         for (int k = threadIdx.x; k < n; k += FT) s_d[k] = __dadd_rn(s_z[k], __dmul_rn(improvement, s_d[k]));
         __syncthreads();
@@ -836,41 +879,23 @@ constexpr int CL = 8;                          // CTAs per cluster
 constexpr int CL_THREADS = 256;
 constexpr int CL_FLAT = 16384;                 // members at most for the cluster kernel
 constexpr int CL_RANGE_MAX = 8191;             // members per CTA: the neighbour code keeps 13 bits of offset
-constexpr int CL_SMEM_MEMBERS = (227 * 1024 - 2048) / SM_BYTES_PER_MEMBER;   // members per CTA that fit
+constexpr int CL_SMEM_MEMBERS = (227 * 1024 - 8192) / SM_BYTES_PER_MEMBER;   // members per CTA that fit beside the static arrays
 
 namespace cgc = cooperative_groups;
 
-struct Sum2 {
-    __device__ double2 operator()(double2 a, double2 b) const { return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)); }
-};
-struct MinMax2 {
-    __device__ double2 operator()(double2 a, double2 b) const {
-        return make_double2(a.x < b.x ? a.x : b.x, a.y > b.y ? a.y : b.y);
-    }
-};
 
-// The CTA's combination of (u, v) (a warp butterfly, then the warps in order), sent to slot q of
-// every CTA's `slots[par]`; after the cluster barrier each CTA's first warp combines the CL slots in
-// rank order and hands the result to the CTA through shared memory (the FP64 pipe is the scarce
-// resource: the other warps need not repeat it). `par` alternates between calls, as for block_sum2.
+// The CTA's combination of (u, v) (block_reduce2), sent to slot q of every CTA's `slots[par]`; after
+// the cluster barrier each CTA's first warp combines the CL slots in rank order and hands the result
+// to the CTA through shared memory (the FP64 pipe is the scarce resource: the other warps need not
+// repeat it). `par` alternates between calls: the next call's barrier keeps this call's readers
+// ahead of the call after it.
 template <class Op>
 __device__ double2 cluster_combine(double2 v, Op op, double2* warps, double2 (*slots)[CL], double2* result, int& par,
                                    int q) {
-    constexpr int NW = CL_THREADS / 32;
-    for (int o = 16; o > 0; o >>= 1) {
-        double2 t;
-        t.x = __shfl_xor_sync(0xFFFFFFFFu, v.x, o);
-        t.y = __shfl_xor_sync(0xFFFFFFFFu, v.y, o);
-        v = op(v, t);
-    }
-    if ((threadIdx.x & 31) == 0) warps[threadIdx.x >> 5] = v;
-    __syncthreads();
+    const double2 cta = block_reduce2<CL_THREADS>(v, op, warps, result + 2);
     if (threadIdx.x < CL) {
-        double2 s = warps[0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w) s = op(s, warps[w]);
         double2* dst = cgc::this_cluster().map_shared_rank(&slots[par][q], (int)threadIdx.x);
-        *dst = s;
+        *dst = cta;
     }
     cgc::this_cluster().sync();
     if (threadIdx.x < 32) {
@@ -904,9 +929,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
                     int* __restrict__ spill_count) {
     constexpr int FT = CL_THREADS;
     extern __shared__ double dyn[];
-    __shared__ double2 warps[FT / 32];
+    __shared__ double2 warps[FT];   // block_reduce2's partials
     __shared__ double2 slots[2][CL];
-    __shared__ double2 result[2];
+    __shared__ double2 result[3];   // two for the cluster's results, one for the CTA's
     __shared__ int bound[CL + 1];
     __shared__ int s_nruns;
     __shared__ double* s_dptr[CL];
@@ -1479,7 +1504,8 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
     steps.ew = 1.0f;
     steps.ns = (float)r;
     steps.diag = (float)std::sqrt(1.0 + r * r);
-    CG_LAUNCH(ctx) k_receivers<<<grid, 256, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed, by_facet ? 1 : 0, d_recv);
+    CG_LAUNCH(ctx) k_receivers<<<grid, RECV_THREADS, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed,
+                                                              by_facet ? 1 : 0, d_recv);
     CG_CHECK_LAUNCH(ctx);
     if (counts) *counts = fc;
     return CG_OK;
