@@ -290,6 +290,7 @@ struct InciseDev {
     const int* start;   // depth buckets, [levels + 1]
     const int* bucket;
     int levels;
+    int* split;         // the highest level left to the whole grid
 };
 
 // HydraulicErosion.baseLevel (HydraulicErosion.kt:2380-2390).
@@ -335,10 +336,25 @@ __device__ void incise_cell(const InciseDev& d, int cell) {
     if (after != height) d.surface[cell] = after;
 }
 
+// Levels from the top down. The highest levels are the main stems of the largest rivers, a few
+// cells each: while a level fits one pass of a CTA, the first CTA takes it alone, with a CTA barrier
+// between levels (its own writes are visible to it); the rest of the grid waits at one grid barrier
+// and then sweeps the lower, larger levels with a grid barrier per level.
 __global__ void __launch_bounds__(256) k_incise_levels(InciseDev d) {
     cgr::grid_group grid = cgr::this_grid();
+    if (blockIdx.x == 0) {
+        int level = d.levels - 1;
+        for (; level >= 0; --level) {
+            const int lo = d.start[level], hi = d.start[level + 1];
+            if (hi - lo > (int)blockDim.x) break;
+            if (lo + (int)threadIdx.x < hi) incise_cell(d, d.bucket[lo + threadIdx.x]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) *d.split = level;
+    }
+    grid.sync();
     const int stride = gridDim.x * blockDim.x;
-    for (int level = d.levels - 1; level >= 0; --level) {
+    for (int level = *(volatile int*)d.split; level >= 0; --level) {
         const int lo = d.start[level], hi = d.start[level + 1];
         for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) incise_cell(d, d.bucket[i]);
         grid.sync();
@@ -532,6 +548,7 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     d.start = d_start;
     d.bucket = d_bucket;
     d.levels = levels;
+    d.split = d_cursor;   // the scatter's cursors are free by now
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_incise_levels, 256, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "incise kernel cannot be resident");
