@@ -115,8 +115,10 @@ cg_status cg_create(cg_ctx** out, int32_t device) {
     e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
         cg_destroy(ctx);
@@ -131,12 +133,15 @@ void cg_destroy(cg_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->aux) cudaStreamSynchronize(ctx->aux);
+    if (ctx->aux2) cudaStreamSynchronize(ctx->aux2);
     for (auto& b : ctx->bufs)
         if (b.ptr) cudaFree(b.ptr);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->join2) cudaEventDestroy(ctx->join2);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->aux2) cudaStreamDestroy(ctx->aux2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

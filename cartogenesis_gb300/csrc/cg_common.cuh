@@ -47,10 +47,10 @@ struct Timer;
 struct cg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    // A second stream for work that overlaps the main one inside a call (forked from and joined
-    // back into `stream` with the two events), so callers only ever see `stream`.
-    cudaStream_t aux = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    // Two more streams for work that overlaps the main one inside a call (forked from and joined
+    // back into `stream` with the events), so callers only ever see `stream`.
+    cudaStream_t aux = nullptr, aux2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, join2 = nullptr;
     std::atomic<int> cancel{0};
     char error[512] = {0};
     // Named scratch buffers, grown on demand and reused across calls.

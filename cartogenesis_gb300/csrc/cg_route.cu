@@ -230,10 +230,13 @@ __device__ int steepest_neighbour(int W, int H, const double* __restrict__ rs, i
     return best;
 }
 
-// Receivers of every land cell (sea cells get -1). The facet rule is FP64 work, and an FP64 warp
+// Receivers of land cells (sea cells get -1). The facet rule is FP64 work, and an FP64 warp
 // instruction costs the same with one lane active as with 32, so each warp compacts the land cells
 // of the chunks it scans into a small queue in shared memory and runs the rule 32 land cells at a
-// time.
+// time. `near` splits the work around the flats: 0 every land cell; 1 the cells with no raised cell
+// in their 3x3 block (their surface and their neighbours' are final before the flats are solved,
+// so this pass runs beside the flat solvers) and the sea; 2 the cells with a raised cell in their
+// 3x3 block, after the flats.
 constexpr int RECV_THREADS = 256;
 
 __device__ __forceinline__ int receiver_of(int cell, const double* __restrict__ surface, int W, int H, Steps st,
@@ -244,9 +247,23 @@ __device__ __forceinline__ int receiver_of(int cell, const double* __restrict__ 
                      : facet_receiver<false>(W, H, surface, col, row, st, seed);
 }
 
+__device__ __forceinline__ bool near_raised(const uint8_t* __restrict__ raised, int cell, int W, int H) {
+    const int row = pdiv(cell, W), col = pmod(cell, W);
+    unsigned any = 0;
+#pragma unroll
+    for (int rs = -1; rs <= 1; ++rs) {
+        const int nr = row + rs;
+        if (nr < 0 || nr >= H) continue;
+#pragma unroll
+        for (int cs = -1; cs <= 1; ++cs) any |= raised[nr * W + wrap_col(col + cs, W)];
+    }
+    return any != 0;
+}
+
 __global__ void __launch_bounds__(RECV_THREADS) k_receivers(const uint8_t* __restrict__ land,
                                                             const double* __restrict__ surface, int W, int H,
                                                             Steps st, long long seed, int by_facet,
+                                                            const uint8_t* __restrict__ raised, int near,
                                                             int32_t* __restrict__ recv) {
     const unsigned FULL = 0xFFFFFFFFu;
     __shared__ int queue[RECV_THREADS / 32][64];
@@ -258,8 +275,9 @@ __global__ void __launch_bounds__(RECV_THREADS) k_receivers(const uint8_t* __res
     int n = 0;   // queued land cells (the same in every lane)
     for (size_t base = ((size_t)blockIdx.x * (RECV_THREADS / 32) + warp) * 32; base < N; base += warps * 32) {
         const size_t i = base + lane;
-        const bool l = i < N && land[i];
-        if (i < N && !l) recv[i] = -1;
+        const bool is_land = i < N && land[i];
+        if (i < N && !is_land && near != 2) recv[i] = -1;
+        const bool l = is_land && (near == 0 || near_raised(raised, (int)i, W, H) == (near == 2));
         const unsigned m = __ballot_sync(FULL, l);
         if (l) q[n + __popc(m & ((1u << lane) - 1u))] = (int)i;
         n += __popc(m);
@@ -1392,6 +1410,12 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
     cudaStream_t sm = ctx->stream;
     int grid = ctx->num_sms * 8;
     FlatCounts fc{0, 0, 0};
+    Steps steps;
+    steps.ew = 1.0f;
+    steps.ns = (float)r;
+    steps.diag = (float)std::sqrt(1.0 + r * r);
+    const int by = by_facet ? 1 : 0;
+    bool routed = false;   // receivers already written (in two passes around the flats)
     if (!over_potential) {
         CG_LAUNCH(ctx) k_surface<<<grid, 256, 0, sm>>>(d_land, d_rel, d_filled, N, d_surface, nullptr, nullptr);
         CG_CHECK_LAUNCH(ctx);
@@ -1465,6 +1489,12 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             // CTAs hold an SM each for the whole solve.
             CG_CUDA(ctx, cudaEventRecord(ctx->fork, sm));
             CG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->fork, 0));
+            CG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux2, ctx->fork, 0));
+            // The receivers away from the flats on the third stream, beside the flat solvers.
+            CG_LAUNCH(ctx) k_receivers<<<grid, RECV_THREADS, 0, ctx->aux2>>>(d_land, d_surface, W, H, steps,
+                                                                            (long long)seed, by, d_raised, 1, d_recv);
+            CG_CHECK_LAUNCH(ctx);
+            CG_CUDA(ctx, cudaEventRecord(ctx->join2, ctx->aux2));
             CG_LAUNCH(ctx) k_flat_solve_warp<<<(flats + WF - 1) / WF, 32 * WF, 0, ctx->aux>>>(a, flats);
             if (ctr[0] > 0)
                 CG_LAUNCH(ctx) k_flat_solve_sm<128><<<ctr[0], 128, (size_t)ctr[3] * SM_BYTES_PER_MEMBER, ctx->aux>>>(
@@ -1494,19 +1524,23 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             }
             CG_CUDA(ctx, cudaEventRecord(ctx->join, ctx->aux));
             CG_CUDA(ctx, cudaStreamWaitEvent(sm, ctx->join, 0));
+            CG_CUDA(ctx, cudaStreamWaitEvent(sm, ctx->join2, 0));
+            // The receivers next to raised cells, now that the flats' surfaces are laid.
+            CG_LAUNCH(ctx) k_receivers<<<grid, RECV_THREADS, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed,
+                                                                     by, d_raised, 2, d_recv);
+            CG_CHECK_LAUNCH(ctx);
+            routed = true;
             CG_CUDA(ctx, cudaMemcpyAsync(&fc.kept, d_kept, sizeof(int), cudaMemcpyDeviceToHost, sm));
             CG_CUDA(ctx, cudaStreamSynchronize(sm));
             fc.flats = flats;
             fc.raised = raised;
         }
     }
-    Steps steps;
-    steps.ew = 1.0f;
-    steps.ns = (float)r;
-    steps.diag = (float)std::sqrt(1.0 + r * r);
-    CG_LAUNCH(ctx) k_receivers<<<grid, RECV_THREADS, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed,
-                                                              by_facet ? 1 : 0, d_recv);
-    CG_CHECK_LAUNCH(ctx);
+    if (!routed) {
+        CG_LAUNCH(ctx) k_receivers<<<grid, RECV_THREADS, 0, sm>>>(d_land, d_surface, W, H, steps, (long long)seed, by,
+                                                                  nullptr, 0, d_recv);
+        CG_CHECK_LAUNCH(ctx);
+    }
     if (counts) *counts = fc;
     return CG_OK;
 }
