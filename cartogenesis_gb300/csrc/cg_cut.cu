@@ -206,6 +206,42 @@ __global__ void k_sort_stage(long long* keys, int P2, int k, int j) {
     }
 }
 
+// The bitonic network over P2 keys with its short strides in shared memory: a CTA holds a chunk of
+// SORT_CH keys and takes every compare-exchange whose stride is below SORT_CH (directions from the
+// keys' global positions, as in k_sort_stage); only the longer strides go through global memory,
+// one launch each.
+constexpr int SORT_CH = 4096;
+
+__device__ __forceinline__ void chunk_steps(long long* sk, int base, int k, int jmax) {
+    for (int j = jmax; j > 0; j >>= 1) {
+        for (int p = threadIdx.x; p < SORT_CH / 2; p += blockDim.x) {
+            const int i = (p & (j - 1)) | ((p & ~(j - 1)) << 1);
+            const int l = i | j;
+            const bool up = ((base + i) & k) == 0;
+            const long long a = sk[i], b = sk[l];
+            if ((a > b) == up) {
+                sk[i] = b;
+                sk[l] = a;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Every stage k <= SORT_CH, whole, per chunk (merge = 0); or the strides below SORT_CH of stage k.
+__global__ void __launch_bounds__(1024) k_sort_chunk(long long* keys, int merge) {
+    __shared__ long long sk[SORT_CH];
+    const int base = blockIdx.x * SORT_CH;
+    for (int i = threadIdx.x; i < SORT_CH; i += blockDim.x) sk[i] = keys[base + i];
+    __syncthreads();
+    if (merge == 0) {
+        for (int k = 2; k <= SORT_CH; k <<= 1) chunk_steps(sk, base, k, k >> 1);
+    } else {
+        chunk_steps(sk, base, merge, SORT_CH / 2);
+    }
+    for (int i = threadIdx.x; i < SORT_CH; i += blockDim.x) keys[base + i] = sk[i];
+}
+
 __global__ void k_pad(long long* keys, int n, int P2) {
     for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) keys[i] = LLONG_MAX;
 }
@@ -464,8 +500,13 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
             int blocks = (P2 / 2 + 255) / 256;
             if (blocks > grid) blocks = grid;
             CG_LAUNCH(ctx) k_pad<<<blocks, 256, 0, sm>>>(d_keys, hs.count, P2);
-            for (int k = 2; k <= P2; k <<= 1)
-                for (int j = k >> 1; j > 0; j >>= 1) CG_LAUNCH(ctx) k_sort_stage<<<blocks, 256, 0, sm>>>(d_keys, P2, k, j);
+            // P2 > SMALL_SORT >= SORT_CH: whole chunks of SORT_CH keys.
+            CG_LAUNCH(ctx) k_sort_chunk<<<P2 / SORT_CH, 1024, 0, sm>>>(d_keys, 0);
+            for (int k = 2 * SORT_CH; k <= P2; k <<= 1) {
+                for (int j = k >> 1; j >= SORT_CH; j >>= 1)
+                    CG_LAUNCH(ctx) k_sort_stage<<<blocks, 256, 0, sm>>>(d_keys, P2, k, j);
+                CG_LAUNCH(ctx) k_sort_chunk<<<P2 / SORT_CH, 1024, 0, sm>>>(d_keys, k);
+            }
         }
         CG_CHECK_LAUNCH(ctx);
     }
