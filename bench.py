@@ -13,7 +13,8 @@ is 134 MB), so no flush is needed between steps.
          host->device copy of the world and the device->host copy of the result inside the timing.
   --impl reference: the CPU restatement of the reference's stage (the Kotlin path cannot run here:
          no JVM), all host threads for the thermal sweeps as the reference's parallelChunks does,
-         on a bounded sample of the same workload.
+         on a bounded sample of the same workload: per step one round of the 12-round stage on the
+         same world after its initial sweeps, plus a twelfth of those sweeps.
 Multi-GPU: replicas only (one independent world per rank, seed = rank + 1); the stage does not
 shard within a world, so there is no collective on the data path.
 """
@@ -46,9 +47,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=8192)
     ap.add_argument("--height", type=int, default=4096)
-    ap.add_argument("--cpu-sample", type=int, default=2048,
-                    help="width of the CPU baseline's sample world (2048: the 2048x1024 grid of the reference's "
-                         "CPU-runnable configuration); 0 skips the CPU leg")
+    ap.add_argument("--cpu-sample", type=int, default=1,
+                    help="samples of the CPU baseline (one round of the stage on the bench world plus a twelfth "
+                         "of its initial sweeps, on the CPU restatement); 0 skips the CPU leg")
     return ap.parse_args()
 
 
@@ -115,22 +116,38 @@ def world_inputs(W, H, seed):
     return synthetic.world(W, H, seed, uplift="ridges")
 
 
-def cpu_baseline(W_sample, steps, threads=None):
-    """The CPU restatement on a bounded sample world (same generator, smaller grid)."""
-    import oracle
-    H_sample = W_sample // 2
-    h, up, rk = world_inputs(W_sample, H_sample, 1)
-    p = oracle.default_params(W_sample, H_sample, 1, sea_level=0.70)
-    times = []
-    for _ in range(max(steps, 1)):
+class CpuSample:
+    """The CPU restatement (oracle) on a bounded sample of the bench workload itself: one of the
+    12 rounds of the stage on the 8192 x 4096 world, taken from the world after its initial sweeps
+    (computed once, untimed), plus a twelfth of those initial sweeps, timed together. Cell-rounds
+    per sample: the grid's cells times one round."""
+
+    def __init__(self, W, H, threads):
+        import oracle
+        self.oracle = oracle
+        self.W, self.H, self.cores = W, H, threads
+        h, self.up, self.rk = world_inputs(W, H, 1)
+        self.p = oracle.default_params(W, H, 1, sea_level=0.70)
+        self.lim, self.sweeps = oracle.thermal_limits(self.p)
+        self.share = (self.sweeps + ROUNDS - 1) // ROUNDS
+        self.swept = oracle.thermal_sweep(h, self.lim, self.sweeps, self.p.rate)
+
+    def step(self):
         t0 = time.perf_counter()
-        oracle.erode_stage(p, h, up, rk, want=())
-        times.append(time.perf_counter() - t0)
+        self.oracle.thermal_sweep(self.swept, self.lim, self.share, self.p.rate)
+        self.oracle.stage_rounds(self.p, self.swept, self.up, self.rk, rounds=1)
+        return time.perf_counter() - t0
+
+    def describe(self, n):
+        return (f"round 1 of the 12-round stage on the {self.W}x{self.H} world after its {self.sweeps} initial "
+                f"sweeps, plus {self.share} sweeps (a twelfth of them); median of {n}")
+
+
+def cpu_baseline(W, H, steps, threads):
+    s = CpuSample(W, H, threads)
+    times = [s.step() for _ in range(max(steps, 1))]
     t = statistics.median(times)
-    value = W_sample * H_sample * ROUNDS / t / 1e6
-    cores = threads or os.cpu_count()
-    return value, t, cores, f"full 12-round stage on the same generator's {W_sample}x{H_sample} world " \
-                            f"({oracle.thermal_limits(p)[1]} initial sweeps), median of {len(times)}"
+    return W * H / t / 1e6, t, threads, s.describe(len(times))
 
 
 def run_reference(args):
@@ -138,15 +155,21 @@ def run_reference(args):
     if rank != 0:
         return 0
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-    steps = max(args.steps, 1)
-    value, t, cores, sample = cpu_baseline(args.cpu_sample, steps, int(os.environ["OMP_NUM_THREADS"]))
+    threads = int(os.environ["OMP_NUM_THREADS"])
+    s = CpuSample(args.width, args.height, threads)
+    for _ in range(args.warmup):
+        s.step()
+    times = [s.step() for _ in range(max(args.steps, 1))]
+    t = sum(times) / len(times)
+    value = args.width * args.height / t / 1e6
+    sample = s.describe(len(times)).replace("median", "mean")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
-        "steps": steps, "warmup": 0, "ms_per_step": round(t * 1000.0, 1), "higher_is_better": True,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": round(t * 1000.0, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"plain P0 erosion stage, CPU restatement of the reference, sample {sample}",
-                   "grid": [args.cpu_sample, args.cpu_sample // 2], "rounds": ROUNDS},
-        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "config": {"workload": f"plain P0 erosion stage (REF32), CPU restatement of the reference: {sample}",
+                   "grid": [args.width, args.height], "rounds": ROUNDS, "sample_rounds_per_step": 1},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -274,7 +297,7 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-        v, t, cores, sample = cpu_baseline(args.cpu_sample, 1, int(os.environ["OMP_NUM_THREADS"]))
+        v, t, cores, sample = cpu_baseline(W, H, args.cpu_sample, int(os.environ["OMP_NUM_THREADS"]))
         line["cpu_baseline"] = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -64,6 +64,9 @@ def lib():
         L.or_erode_stage.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), C.POINTER(abi.Outputs),
                                      vp]
         L.or_erode_stage.restype = i32
+        L.or_stage_rounds.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), C.POINTER(abi.Outputs),
+                                      i32]
+        L.or_stage_rounds.restype = i32
         L.or_hydraulic_apply.argtypes = L.or_erode_stage.argtypes
         L.or_hydraulic_apply.restype = i32
         _lib = L
@@ -196,6 +199,19 @@ def stand_below_today(params, round_):
 
 def seeded_noise(c, r, seed):
     return lib().or_seeded_noise(c, r, seed)
+
+
+def stage_rounds(params, height, uplift=None, rock=None, rounds=1):
+    """The first `rounds` rounds of the stage from already swept heights (no initial sweeps)."""
+    H, W = params.height, params.width
+    keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+            for a in (height, uplift, rock)]
+    inputs = abi.Inputs(*[P(a) if a is not None else None for a in keep], None, None)
+    out = np.empty((H, W), np.float32)
+    o = abi.Outputs(height=P(out))
+    st = lib().or_stage_rounds(C.byref(params), C.byref(inputs), C.byref(o), rounds)
+    assert st == 0, st
+    return out
 
 
 def erode_stage(params, height, uplift=None, rock=None, rain=None, veg=None, thermal=True, want=("receivers", "area", "filled",

@@ -1000,8 +1000,10 @@ struct StageOut {
 // ErosionStage.apply (ErosionStage.kt:133-183) with HydraulicErosion.apply (HydraulicErosion.kt:596-1506)
 // for profile P0: no provisional climate (the given weather is held), no belt replay, no flexure, no
 // deposition, no outlet notch.
+// run_rounds >= 0 stops after that many rounds (the relaxation keeps the whole stage's share per
+// round) and initial = false leaves out the initial sweeps: a bounded sample of a stage.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
-                bool with_thermal = true) {
+                bool with_thermal = true, bool initial = true, int run_rounds = -1) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -1013,7 +1015,8 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     cg_thermal_limits lim = thermal_limits(p);
     int sweeps = sweeps_for(p);
     // thermalErosion -> thermalSweep(skipSettled = true) (ErosionStage.kt:189-222).
-    if (with_thermal && sweeps > 0) thermal_sweep(W, H, working.data(), working.data(), lim, sweeps, p.rate, true);
+    if (with_thermal && initial && sweeps > 0)
+        thermal_sweep(W, H, working.data(), working.data(), lim, sweeps, p.rate, true);
     int rounds_for_relax = p.hydraulic_rounds < 1 ? 1 : p.hydraulic_rounds;
     int per_round = sweeps / rounds_for_relax;
     if (per_round < 1) per_round = 1;
@@ -1036,7 +1039,8 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     std::vector<float> filled(N), area(N);
     std::vector<int32_t> dirs(N), order;
     FlatCounts flats;
-    for (int round = 0; round < p.hydraulic_rounds; ++round) {
+    const int last = run_rounds >= 0 && run_rounds < p.hydraulic_rounds ? run_rounds : p.hydraulic_rounds;
+    for (int round = 0; round < last; ++round) {
         if (in.uplift_mm_per_year) {
             const float* rate = in.uplift_mm_per_year;
             for (size_t c = 0; c < N; ++c) {
@@ -1262,6 +1266,12 @@ int32_t or_erode_stage(const cg_erosion_params* p, const cg_inputs* in, cg_outpu
 int32_t or_hydraulic_apply(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
                            cg_round_stats* stats) {
     return erode_stage(*p, *in, out, stats, false);
+}
+
+// The first `rounds` rounds of ErosionStage.apply from heights already swept (no initial sweeps),
+// each with its relaxation: a bounded sample of the stage for timing.
+int32_t or_stage_rounds(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, int32_t rounds) {
+    return erode_stage(*p, *in, out, nullptr, true, false, rounds);
 }
 
 }  // extern "C"
