@@ -73,29 +73,57 @@ __global__ void k_links(const uint8_t* __restrict__ land, const int32_t* __restr
 }
 
 // Donor counts, the pending counts of the walk, and the list of land sources (cells no land cell
-// drains into), appended per warp; their order does not matter (the walk's results do not depend on
-// which thread reaches a cell first).
-__global__ void k_sources(const uint8_t* __restrict__ land, const uint8_t* __restrict__ mask, size_t N,
-                          int32_t* __restrict__ donors, int32_t* __restrict__ pending, int* __restrict__ sources,
-                          int* __restrict__ n_sources) {
+// drains into). A CTA takes SRC_PER cells per thread at a time and reserves its sources' slots with
+// one atomic (a per-warp atomic on the one counter was the kernel's cost); the list's order does not
+// matter, since the walk's results do not depend on which thread reaches a cell first.
+constexpr int SRC_PER = 8;
+
+__global__ void __launch_bounds__(256) k_sources(const uint8_t* __restrict__ land, const uint8_t* __restrict__ mask,
+                                                 size_t N, int32_t* __restrict__ donors,
+                                                 int32_t* __restrict__ pending, int* __restrict__ sources,
+                                                 int* __restrict__ n_sources) {
     const unsigned FULL = 0xFFFFFFFFu;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t base = blockIdx.x * (size_t)blockDim.x; base < N; base += stride) {
-        const size_t i = base + threadIdx.x;
-        bool src = false;
-        if (i < N) {
+    __shared__ int warp_tot[8];
+    __shared__ int s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t chunk = (size_t)blockDim.x * SRC_PER;
+    for (size_t cb = (size_t)blockIdx.x * chunk; cb < N; cb += (size_t)gridDim.x * chunk) {
+        unsigned bits = 0;
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < SRC_PER; ++k) {
+            const size_t i = cb + (size_t)k * blockDim.x + threadIdx.x;
+            if (i >= N) continue;
             const int n = __popc((unsigned)mask[i]);
             donors[i] = n;
             pending[i] = n;
-            src = land[i] && n == 0;
+            if (land[i] && n == 0) {
+                bits |= 1u << k;
+                ++cnt;
+            }
         }
-        const unsigned group = __ballot_sync(FULL, src);
-        if (group == 0) continue;
-        const int lane = threadIdx.x & 31;
-        int slot = 0;
-        if (lane == __ffs(group) - 1) slot = atomicAdd(n_sources, __popc(group));
-        slot = __shfl_sync(FULL, slot, __ffs(group) - 1);
-        if (src) sources[slot + __popc(group & ((1u << lane) - 1u))] = (int)i;
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const int t = warp_tot[w];
+                warp_tot[w] = run;
+                run += t;
+            }
+            s_base = run ? atomicAdd(n_sources, run) : 0;
+        }
+        __syncthreads();
+        int slot = s_base + warp_tot[warp] + incl - cnt;
+#pragma unroll
+        for (int k = 0; k < SRC_PER; ++k)
+            if (bits & (1u << k)) sources[slot++] = (int)(cb + (size_t)k * blockDim.x + threadIdx.x);
+        __syncthreads();
     }
 }
 
@@ -242,20 +270,72 @@ __global__ void k_land_compact(const uint8_t* __restrict__ land, const int* __re
 // Cells bucketed by their Kahn level (the high half of their drainage key). A cell's receiver sits
 // on a strictly higher level, so sweeping the levels from the top down reaches every receiver
 // before its donors. Warp-aggregated atomics: lanes sharing a level take one atomic between them.
+// Cells per Kahn level, and the cells bucketed by level. A CTA counts its cells per level in shared
+// memory and adds each nonzero count to the global one with a single atomic; the scatter does the
+// same per chunk of LVL_PER cells per thread, a cell's slot being its rank within the chunk's level
+// (a shared-memory atomic) after the chunk's base for that level. Level 0 holds millions of cells,
+// so atomics per warp on its cursor were the kernels' cost. Worlds with more than LVL_SMEM levels
+// take the per-warp kernels.
+constexpr int LVL_SMEM = 4096;
+constexpr int LVL_PER = 8;
+
+__device__ __forceinline__ int level_of(const uint8_t* land, const long long* key, size_t i, size_t N, int levels) {
+    if (i >= N || !land[i]) return -1;
+    const int L = (int)(key[i] >> 32);
+    return (L < 0 || L >= levels) ? -1 : L;   // never out of range for a forest's keys
+}
+
+__global__ void __launch_bounds__(256) k_level_count_cta(const uint8_t* __restrict__ land,
+                                                         const long long* __restrict__ key, size_t N, int levels,
+                                                         int* __restrict__ count) {
+    __shared__ int hist[LVL_SMEM];
+    for (int l = threadIdx.x; l < levels; l += blockDim.x) hist[l] = 0;
+    __syncthreads();
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        const int L = level_of(land, key, i, N, levels);
+        if (L >= 0) atomicAdd(&hist[L], 1);
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < levels; l += blockDim.x)
+        if (hist[l]) atomicAdd(&count[l], hist[l]);
+}
+
+__global__ void __launch_bounds__(256) k_level_scatter_cta(const uint8_t* __restrict__ land,
+                                                           const long long* __restrict__ key, size_t N, int levels,
+                                                           const int* __restrict__ start, int* __restrict__ cursor,
+                                                           int* __restrict__ bucket) {
+    __shared__ int hist[LVL_SMEM];
+    const size_t chunk = (size_t)blockDim.x * LVL_PER;
+    for (size_t cb = (size_t)blockIdx.x * chunk; cb < N; cb += (size_t)gridDim.x * chunk) {
+        for (int l = threadIdx.x; l < levels; l += blockDim.x) hist[l] = 0;
+        __syncthreads();
+        int lv[LVL_PER], rank[LVL_PER];
+#pragma unroll
+        for (int k = 0; k < LVL_PER; ++k) {
+            lv[k] = level_of(land, key, cb + (size_t)k * blockDim.x + threadIdx.x, N, levels);
+            rank[k] = lv[k] >= 0 ? atomicAdd(&hist[lv[k]], 1) : 0;
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < levels; l += blockDim.x)
+            if (hist[l]) hist[l] = start[l] + atomicAdd(&cursor[l], hist[l]);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < LVL_PER; ++k)
+            if (lv[k] >= 0) bucket[hist[lv[k]] + rank[k]] = (int)(cb + (size_t)k * blockDim.x + threadIdx.x);
+        __syncthreads();
+    }
+}
+
 __global__ void k_level_count(const uint8_t* __restrict__ land, const long long* __restrict__ key, size_t N,
                               int levels, int* __restrict__ count) {
     const unsigned FULL = 0xFFFFFFFFu;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += stride) {
-        size_t i = base + threadIdx.x;
-        bool valid = i < N && land[i];
-        int L = valid ? (int)(key[i] >> 32) : -1;
-        if (valid && (L < 0 || L >= levels)) valid = false, L = -1;   // never for a forest's keys
+        const int L = level_of(land, key, base + threadIdx.x, N, levels);
         unsigned group = __match_any_sync(FULL, L);
-        if (valid && (threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count[L], __popc(group));
+        if (L >= 0 && (threadIdx.x & 31) == __ffs(group) - 1) atomicAdd(&count[L], __popc(group));
     }
 }
-
 __global__ void k_level_scatter(const uint8_t* __restrict__ land, const long long* __restrict__ key, size_t N,
                                 int levels, const int* __restrict__ start, int* __restrict__ cursor,
                                 int* __restrict__ bucket) {
@@ -263,16 +343,14 @@ __global__ void k_level_scatter(const uint8_t* __restrict__ land, const long lon
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += stride) {
-        size_t i = base + threadIdx.x;
-        bool valid = i < N && land[i];
-        int L = valid ? (int)(key[i] >> 32) : -1;
-        if (valid && (L < 0 || L >= levels)) valid = false, L = -1;
+        const size_t i = base + threadIdx.x;
+        const int L = level_of(land, key, i, N, levels);
         unsigned group = __match_any_sync(FULL, L);
         int leader = __ffs(group) - 1;
         int slot = 0;
-        if (valid && lane == leader) slot = atomicAdd(&cursor[L], __popc(group));
+        if (L >= 0 && lane == leader) slot = atomicAdd(&cursor[L], __popc(group));
         slot = __shfl_sync(FULL, slot, leader);
-        if (valid) bucket[start[L] + slot + __popc(group & ((1u << lane) - 1u))] = (int)i;
+        if (L >= 0) bucket[start[L] + slot + __popc(group & ((1u << lane) - 1u))] = (int)i;
     }
 }
 
@@ -526,12 +604,15 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     int* d_cursor = d_start + levels + 1;
     CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, ((size_t)levels + 1) * sizeof(int), sm));
     CG_CUDA(ctx, cudaMemsetAsync(d_cursor, 0, ((size_t)levels + 1) * sizeof(int), sm));
-    CG_LAUNCH(ctx) k_level_count<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
+    const bool cta_hist = levels <= LVL_SMEM;
+    if (cta_hist) CG_LAUNCH(ctx) k_level_count_cta<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
+    else CG_LAUNCH(ctx) k_level_count<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
     CG_CHECK_LAUNCH(ctx);
     // The exclusive scan of levels + 1 counts (the last is zero) ends with the total at start[levels].
     cg_status st = exclusive_scan(ctx, d_cnt, d_start, levels + 1, nullptr);
     if (st != CG_OK) return st;
-    CG_LAUNCH(ctx) k_level_scatter<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
+    if (cta_hist) CG_LAUNCH(ctx) k_level_scatter_cta<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
+    else CG_LAUNCH(ctx) k_level_scatter<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
     CG_LAUNCH(ctx) k_water_init<<<grid, 256, 0, sm>>>(d_water, N);
     CG_CHECK_LAUNCH(ctx);
     InciseDev d;
@@ -552,7 +633,8 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_incise_levels, 256, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "incise kernel cannot be resident");
-    int cgrid = ctx->num_sms * (per_sm < 4 ? per_sm : 4);
+    // Two CTAs per SM: the lower levels still fill the GPU, and a grid barrier over fewer CTAs is shorter.
+    int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
     void* kargs[] = {&d};
     ctx->launches++;
     CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_incise_levels, cgrid, 256, kargs, 0, sm));
