@@ -154,13 +154,23 @@ __global__ void __launch_bounds__(256) k_bracket_bin(const double* __restrict__ 
 
 __global__ void k_bracket_collect(const float* __restrict__ h, size_t N, CutState* s, long long* __restrict__ keys) {
     if (s->degenerate) return;
+    const unsigned FULL = 0xFFFFFFFFu;
     const float lo = s->lowest, per = s->per;
     const int bracket = s->bracket_bin;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        float v = h[i];
-        if (bin_of(v, lo, per) != bracket) continue;
-        int slot = atomicAdd(&s->count, 1);
-        keys[slot] = (long long)(((unsigned long long)(long long)sortable_bits(v) << 32) | (unsigned long long)i);
+    const int lane = threadIdx.x & 31;
+    // Whole warps step together, so the bracket's cells of a warp take one atomic (the list's order
+    // does not matter: it is sorted next).
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += stride) {
+        const size_t i = base + threadIdx.x;
+        const float v = i < N ? h[i] : 0.0f;
+        const bool in = i < N && bin_of(v, lo, per) == bracket;
+        const unsigned m = __ballot_sync(FULL, in);
+        if (!m) continue;
+        int slot = 0;
+        if (lane == __ffs(m) - 1) slot = atomicAdd(&s->count, __popc(m));
+        slot = __shfl_sync(FULL, slot, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1u));
+        if (in) keys[slot] = (long long)(((unsigned long long)(long long)sortable_bits(v) << 32) | (unsigned long long)i);
     }
 }
 
