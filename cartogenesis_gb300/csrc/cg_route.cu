@@ -1191,72 +1191,85 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_THREADS)
     if (!laid && q == 0 && threadIdx.x == 0) atomicAdd(a.kept, 1);
 }
 
-// Flats of at most 32 members, one warp each (most flats are a few cells: the fill's small
-// depressions). Each lane owns one member; the per-member arithmetic (degree, Laplacian row, the
-// column runs' Thomas solves) is the reference's, done by the member's lane or the run head's lane;
-// the dot products are butterfly shuffles, which give every lane the same bits.
-constexpr int WF = 8;   // warps (flats) per block
+// Flats of at most 32 members (nearly all flats: the fill's small depressions), packed 32 / S to a
+// warp by size class, S in {4, 8, 16, 32}: a flat takes a segment of S lanes, one member per lane.
+// An FP64 warp instruction costs the same however few lanes are busy, so packing the small flats
+// divides their cost. The per-member arithmetic (degree, Laplacian row, the column runs' Thomas
+// solves) is the reference's, done by the member's lane or the run head's lane; the dot products
+// are butterflies within the segment, which give every lane of the segment the same bits; each
+// segment runs its own CG iterations and stops on its own test (the warp loops while any segment
+// is still going, a stopped segment's state no longer changes).
+constexpr int WF = 8;   // warps per block
 
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+template <int S>
+__device__ __forceinline__ double seg_sum(double v) {
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
     return v;
 }
 
-__global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int flats) {
+template <int S>
+__global__ void __launch_bounds__(32 * WF) k_flat_solve_seg(FlatArgs a, const int* __restrict__ list, int count) {
+    constexpr int G = 32 / S;   // flats per warp
     const unsigned FULL = 0xFFFFFFFFu;
     __shared__ double s_right[WF][32], s_into[WF][32], s_piv[WF][32], s_coef[WF][32], s_rcp[WF][32], s_d[WF][32];
     __shared__ int s_cont[WF][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f = blockIdx.x * WF + w;
-    if (f >= flats) return;
-    const int n = a.count[f];
-    if (n > 32) return;   // the CTA kernel takes it
-    const int base = a.off[f];
-    const bool act = lane < n;
+    const int seg = lane / S, sl = lane % S;
+    const unsigned seg_mask = (S == 32 ? FULL : ((1u << S) - 1u)) << (seg * S);
+    const int slot = (blockIdx.x * WF + w) * G + seg;
+    if ((blockIdx.x * WF + w) * G >= count) return;   // the whole warp is past the list
+    const int f = slot < count ? list[slot] : -1;
+    const int n = f >= 0 ? a.count[f] : 0;
+    const int base = f >= 0 ? a.off[f] : 0;
+    const bool act = sl < n;
     const int W = a.W, H = a.H;
 
-    // Members by (column, row): a bitonic sort across the lanes.
-    int key = act ? pmod(a.members[base + lane], W) * H + pdiv(a.members[base + lane], W) : INT_MAX;
-    for (int k = 2; k <= 32; k <<= 1)
+    // Members by (column, row): a bitonic sort across the segment's lanes.
+    int key = act ? pmod(a.members[base + sl], W) * H + pdiv(a.members[base + sl], W) : INT_MAX;
+#pragma unroll
+    for (int k = 2; k <= S; k <<= 1)
+#pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
-            int other = __shfl_xor_sync(FULL, key, j);
-            bool up = (lane & k) == 0;
-            bool lower = (lane & j) == 0;
-            int lo = min(key, other), hi = max(key, other);
+            const int other = __shfl_xor_sync(FULL, key, j);
+            const bool up = (sl & k) == 0;
+            const bool lower = (sl & j) == 0;
+            const int lo = min(key, other), hi = max(key, other);
             key = (lower == up) ? lo : hi;
         }
     const int cell = act ? pmod(key, H) * W + pdiv(key, H) : -1;
     if (act) {
-        a.members[base + lane] = cell;
-        a.local[cell] = lane;
+        a.members[base + sl] = cell;
+        a.local[cell] = sl;
     }
     __syncwarp();
     const int col = act ? pmod(cell, W) : 0, row = act ? pdiv(cell, W) : 0;
 
     // Entry level, highest entry, member neighbours (their lanes), degree and rain.
     float lo = act ? a.filled[cell] : FLT_MAX;
-    for (int o = 16; o > 0; o >>= 1) lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
     const double entry_level = (double)lo;
     double hi = -INFINITY, deg = 0.0, rv = 0.0;
     int nb_lane[8];
     double nb_w[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) nb_lane[t] = -1, nb_w[t] = 0.0;
     if (act) {
         int t = 0;
         for (int rs = -1; rs <= 1; ++rs) {
-            int nr = row + rs;
+            const int nr = row + rs;
             for (int cs = -1; cs <= 1; ++cs) {
                 if (cs == 0 && rs == 0) continue;
-                nb_lane[t] = -1;
-                nb_w[t] = 0.0;
                 if (nr >= 0 && nr < H) {
-                    int nb = nr * W + wrap_col(col + cs, W);
-                    double wgt = stencil_weight(a, cs, rs);
-                    int l = a.local[nb];
-                    double there = a.surface[nb];
+                    const int nb = nr * W + wrap_col(col + cs, W);
+                    const double wgt = stencil_weight(a, cs, rs);
+                    const int l = a.local[nb];
+                    const double there = a.surface[nb];
                     if (l < 0 && there < entry_level && there > hi) hi = there;
                     if (l >= 0) {
                         deg = __dadd_rn(deg, wgt);
-                        nb_lane[t] = l;
+                        nb_lane[t] = seg * S + l;
                         nb_w[t] = wgt;
                     } else if (there < entry_level) {
                         deg = __dadd_rn(deg, wgt);
@@ -1267,17 +1280,16 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
         }
         rv = __dadd_rn(1.0, __dmul_rn(0.5, (double)smooth_seeded_field(W, a.lattice, col, row,
                                                                          a.seed ^ kRainReliefSalt)));
-    } else {
-        for (int t = 0; t < 8; ++t) nb_lane[t] = -1, nb_w[t] = 0.0;
     }
-    for (int o = 16; o > 0; o >>= 1) hi = fmax(hi, __shfl_xor_sync(FULL, hi, o));
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) hi = fmax(hi, __shfl_xor_sync(FULL, hi, o));
     const double entry_height = hi;
 
-    // Column runs: contiguous lanes. Pivots and ns / pivot down each run by its head lane.
+    // Column runs: contiguous lanes of the segment. Pivots and ns / pivot down each run by its head.
     const int prev_cell = __shfl_up_sync(FULL, cell, 1);
     const int next_cell = __shfl_down_sync(FULL, cell, 1);
-    const bool head = act && (lane == 0 || prev_cell != cell - W);
-    s_cont[w][lane] = (act && lane + 1 < n && next_cell == cell + W) ? 1 : 0;
+    const bool head = act && (sl == 0 || prev_cell != cell - W);
+    s_cont[w][lane] = (act && sl + 1 < n && next_cell == cell + W) ? 1 : 0;
     s_right[w][lane] = deg;
     __syncwarp();
     if (head) {
@@ -1309,13 +1321,13 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
             }
             double below = v;
             for (int i = j - 1; i >= lane; --i) {
-                double u = __dadd_rn(s_into[w][i], __dmul_rn(s_coef[w][i], below));
+                const double u = __dadd_rn(s_into[w][i], __dmul_rn(s_coef[w][i], below));
                 s_into[w][i] = u;
                 below = u;
             }
         }
         __syncwarp();
-        double z = act ? s_into[w][lane] : 0.0;
+        const double z = act ? s_into[w][lane] : 0.0;
         __syncwarp();
         return z;
     };
@@ -1323,81 +1335,110 @@ __global__ void __launch_bounds__(32 * WF) k_flat_solve_warp(FlatArgs a, int fla
         s_d[w][lane] = dv;
         __syncwarp();
         double sum = __dmul_rn(deg, dv);
+#pragma unroll
         for (int t = 0; t < 8; ++t)
             if (nb_lane[t] >= 0) sum = __dsub_rn(sum, __dmul_rn(nb_w[t], s_d[w][nb_lane[t]]));
         __syncwarp();
         return act ? sum : 0.0;
     };
 
-    // Preconditioned conjugate gradients (FlatRouting.kt:296-333).
+    // Preconditioned conjugate gradients (FlatRouting.kt:296-333), per segment.
     double x = 0.0, r = act ? rv : 0.0;
     double z = precondition(r);
     double d = z;
-    double rnorm = warp_sum(act ? __dmul_rn(r, r) : 0.0);
-    double rap = warp_sum(act ? __dmul_rn(r, z) : 0.0);
+    double rnorm = seg_sum<S>(act ? __dmul_rn(r, r) : 0.0);
+    double rap = seg_sum<S>(act ? __dmul_rn(r, z) : 0.0);
     const double stop_at = __dmul_rn(__dmul_rn(rnorm, 1e-7), 1e-7);
-    const int most = 64 + (int)(8.0 * sqrt((double)n));
-    for (int it = 0; rnorm > stop_at && it < most; ++it) {
-        double ad = laplacian(d);
-        double energy = warp_sum(act ? __dmul_rn(d, ad) : 0.0);
-        if (energy <= 0.0 || rap <= 0.0) break;
-        double step = __ddiv_rn(rap, energy);
-        if (act) {
+    const int most = 64 + (int)(8.0 * sqrt((double)(n > 0 ? n : 1)));
+    bool stopped = f < 0;
+    for (int it = 0;; ++it) {
+        if (!stopped && !(rnorm > stop_at && it < most)) stopped = true;
+        if (!__any_sync(FULL, !stopped)) break;
+        const double ad = laplacian(d);
+        const double energy = seg_sum<S>(act ? __dmul_rn(d, ad) : 0.0);
+        if (!stopped && (energy <= 0.0 || rap <= 0.0)) stopped = true;
+        const bool go = !stopped;
+        const double step = __ddiv_rn(rap, energy);
+        if (go && act) {
             x = __dadd_rn(x, __dmul_rn(step, d));
             r = __dsub_rn(r, __dmul_rn(step, ad));
         }
-        double next_norm = warp_sum(act ? __dmul_rn(r, r) : 0.0);
-        z = precondition(r);
-        double next_ap = warp_sum(act ? __dmul_rn(r, z) : 0.0);
-        double improvement = __ddiv_rn(next_ap, rap);
-        if (act) d = __dadd_rn(z, __dmul_rn(improvement, d));
-        rnorm = next_norm;
-        rap = next_ap;
+        const double next_norm = seg_sum<S>(act ? __dmul_rn(r, r) : 0.0);
+        const double zn = precondition(r);
+        const double next_ap = seg_sum<S>(act ? __dmul_rn(r, zn) : 0.0);
+        if (go) {
+            const double improvement = __ddiv_rn(next_ap, rap);
+            if (act) d = __dadd_rn(zn, __dmul_rn(improvement, d));
+            rnorm = next_norm;
+            rap = next_ap;
+        }
     }
-    const bool positive = __all_sync(FULL, !act || x > 0.0);
+    // Every collective below runs with the whole warp; a segment's decisions are read from its bits.
+    const bool positive = (__ballot_sync(FULL, act && !(x > 0.0)) & seg_mask) == 0;
     double top = act ? x : 0.0;
-    for (int o = 16; o > 0; o >>= 1) top = fmax(top, __shfl_xor_sync(FULL, top, o));
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) top = fmax(top, __shfl_xor_sync(FULL, top, o));
     const double highest = top > 0.0 ? top : 0.0;
 
     // FlatRouting.layInBand (FlatRouting.kt:455-489).
-    bool laid = positive && !(highest <= 0.0 || entry_height >= entry_level);
-    if (laid) {
+    bool laid = f >= 0 && positive && !(highest <= 0.0 || entry_height >= entry_level);
+    if (laid && act) {
         const double band = __dmul_rn(__dsub_rn(entry_level, entry_height), 0.9);
-        if (act) a.surface[cell] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(x, highest)));
-        __syncwarp();
-        bool lower = !act;
-        if (act) {
-            double here = a.surface[cell];
-            for (int rs = -1; rs <= 1 && !lower; ++rs) {
-                int nr = row + rs;
-                if (nr < 0 || nr >= H) continue;
-                for (int cs = -1; cs <= 1; ++cs) {
-                    if (cs == 0 && rs == 0) continue;
-                    if (a.surface[nr * W + wrap_col(col + cs, W)] < here) {
-                        lower = true;
-                        break;
-                    }
+        a.surface[cell] = __dadd_rn(entry_height, __dmul_rn(band, __ddiv_rn(x, highest)));
+    }
+    __syncwarp();
+    bool lower = !act;
+    if (laid && act) {
+        const double here = a.surface[cell];
+        for (int rs = -1; rs <= 1 && !lower; ++rs) {
+            const int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                if (a.surface[nr * W + wrap_col(col + cs, W)] < here) {
+                    lower = true;
+                    break;
                 }
             }
         }
-        if (!__all_sync(FULL, lower)) {
-            if (act) a.surface[cell] = (double)a.filled[cell];
-            laid = false;
-        }
     }
-    if (!laid && lane == 0) atomicAdd(a.kept, 1);
+    const bool all_lower = (__ballot_sync(FULL, lower) & seg_mask) == seg_mask;
+    if (laid && !all_lower) {
+        if (act) a.surface[cell] = (double)a.filled[cell];
+        laid = false;
+    }
+    if (f >= 0 && !laid && sl == 0) atomicAdd(a.kept, 1);
 }
 
-// The flats of more than 32 members, listed by the kernel that takes them: lists[0] the 128-thread
-// shared-memory kernel, lists[1] the cluster kernel, lists[2] k_flat_solve. ctr[0..2] count the
-// lists, ctr[3..4] hold the largest flat of the first two (their shared-memory size).
+// Every flat, listed by the kernel that takes it: lists[0] the 128-thread shared-memory kernel
+// (33-512 members), lists[1] the cluster kernel (513-CL_FLAT), lists[2] k_flat_solve (larger),
+// lists[3..6] k_flat_solve_seg with segments of 4, 8, 16 and 32 lanes. ctr[0..2] count the first
+// three, ctr[3..4] hold the largest flat of the first two (their shared-memory size), ctr[5..8]
+// count lists 3-6. A warp's flats of one class take one atomic.
+constexpr int FLAT_CLASSES = 7;
+
+__device__ __forceinline__ int flat_class(int n) {
+    return n <= 4 ? 3 : n <= 8 ? 4 : n <= 16 ? 5 : n <= 32 ? 6 : n <= MID_FLAT ? 0 : n <= CL_FLAT ? 1 : 2;
+}
+
 __global__ void k_flat_lists(const int* __restrict__ count, int flats, int* __restrict__ lists, int* __restrict__ ctr) {
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < flats; f += gridDim.x * blockDim.x) {
-        const int n = count[f];
-        if (n <= 32) continue;
-        const int c = n <= MID_FLAT ? 0 : n <= CL_FLAT ? 1 : 2;
-        lists[(size_t)c * flats + atomicAdd(&ctr[c], 1)] = f;
-        if (c < 2) atomicMax(&ctr[3 + c], n);
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < flats; base += stride) {
+        const int f = base + threadIdx.x;
+        const int n = f < flats ? count[f] : 0;
+        const int c = f < flats ? flat_class(n) : -1;
+        const unsigned group = __match_any_sync(FULL, c);
+        const int leader = __ffs(group) - 1;
+        int* counter = c >= 3 ? &ctr[2 + c] : &ctr[c < 0 ? 0 : c];
+        int slot = 0;
+        if (c >= 0 && lane == leader) slot = atomicAdd(counter, __popc(group));
+        slot = __shfl_sync(FULL, slot, leader) + __popc(group & ((1u << lane) - 1u));
+        if (c >= 0) {
+            lists[(size_t)c * flats + slot] = f;
+            if (c < 2) atomicMax(&ctr[3 + c], n);
+        }
     }
 }
 
@@ -1477,12 +1518,12 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
             a.nbr = reinterpret_cast<short*>(d_dbl + 8 * (size_t)raised);   // 8 shorts per member
             a.kept = d_kept;
             // Flats of at most 32 members one warp each; larger ones one CTA each, by size class.
-            CG_BUF(int, d_lists, ctx, S_CG5, 3 * (size_t)flats + 5);
-            int* d_ctr = d_lists + 3 * (size_t)flats;
-            CG_CUDA(ctx, cudaMemsetAsync(d_ctr, 0, 5 * sizeof(int), sm));
+            CG_BUF(int, d_lists, ctx, S_CG5, FLAT_CLASSES * (size_t)flats + 9);
+            int* d_ctr = d_lists + FLAT_CLASSES * (size_t)flats;
+            CG_CUDA(ctx, cudaMemsetAsync(d_ctr, 0, 9 * sizeof(int), sm));
             CG_LAUNCH(ctx) k_flat_lists<<<(flats + 255) / 256, 256, 0, sm>>>(d_cnt, flats, d_lists, d_ctr);
             CG_CHECK_LAUNCH(ctx);
-            int ctr[5] = {0, 0, 0, 0, 0};
+            int ctr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             CG_CUDA(ctx, cudaMemcpyAsync(ctr, d_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, sm));
             CG_CUDA(ctx, cudaStreamSynchronize(sm));
             // The small and mid-sized flats on the auxiliary stream, beside the few large ones, whose
@@ -1495,7 +1536,20 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
                                                                             (long long)seed, by, d_raised, 1, d_recv);
             CG_CHECK_LAUNCH(ctx);
             CG_CUDA(ctx, cudaEventRecord(ctx->join2, ctx->aux2));
-            CG_LAUNCH(ctx) k_flat_solve_warp<<<(flats + WF - 1) / WF, 32 * WF, 0, ctx->aux>>>(a, flats);
+            {
+                const int* small = d_lists + 3 * (size_t)flats;
+                if (ctr[5] > 0)
+                    CG_LAUNCH(ctx) k_flat_solve_seg<4><<<(ctr[5] + 8 * WF - 1) / (8 * WF), 32 * WF, 0, ctx->aux>>>(a, small, ctr[5]);
+                if (ctr[6] > 0)
+                    CG_LAUNCH(ctx) k_flat_solve_seg<8><<<(ctr[6] + 4 * WF - 1) / (4 * WF), 32 * WF, 0, ctx->aux>>>(
+                        a, small + flats, ctr[6]);
+                if (ctr[7] > 0)
+                    CG_LAUNCH(ctx) k_flat_solve_seg<16><<<(ctr[7] + 2 * WF - 1) / (2 * WF), 32 * WF, 0, ctx->aux>>>(
+                        a, small + 2 * (size_t)flats, ctr[7]);
+                if (ctr[8] > 0)
+                    CG_LAUNCH(ctx) k_flat_solve_seg<32><<<(ctr[8] + WF - 1) / WF, 32 * WF, 0, ctx->aux>>>(
+                        a, small + 3 * (size_t)flats, ctr[8]);
+            }
             if (ctr[0] > 0)
                 CG_LAUNCH(ctx) k_flat_solve_sm<128><<<ctr[0], 128, (size_t)ctr[3] * SM_BYTES_PER_MEMBER, ctx->aux>>>(
                     a, d_lists);
