@@ -100,7 +100,7 @@ __device__ __forceinline__ float moved(const Window& v, const Window& g, bool ha
 // else the give pass (writes gv).
 template <int RW, int RH, int M, bool MOVE, bool EDGE>
 __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __restrict__ gv, float* __restrict__ dst,
-                                     int y0, int H, const ThermalArgs& a) {
+                                     int y0, int H, const ThermalArgs& a, int halo, bool& changed) {
     constexpr int SEG = 4;
     constexpr int COLS = RW - 2 * M, ROWS = RH - 2 * M;
     constexpr int SEGS = (ROWS + SEG - 1) / SEG;
@@ -144,7 +144,12 @@ __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __rest
                     // sums stay +0 and the cell moves to (h - 0) + 0. Rows off the grid (EDGE) are
                     // left to the full rule.
                     const bool still = !EDGE && (or_top | or_mid | or_bot) == 0u;
-                    dst[ry * RW + col] = still ? __fadd_rn(__fsub_rn(v.c, 0.0f), 0.0f) : moved(v, g, has_s, has_n, a);
+                    const float nv = still ? __fadd_rn(__fsub_rn(v.c, 0.0f), 0.0f) : moved(v, g, has_s, has_n, a);
+                    dst[ry * RW + col] = nv;
+                    // A cell of the tile itself that moved (in any sweep) marks the tile as changed.
+                    if (__float_as_uint(nv) != __float_as_uint(v.c) && ry >= halo && ry < RH - halo &&
+                        col >= halo && col < RW - halo)
+                        changed = true;
                 } else {
                     gv[ry * RW + col] = give_rate(v, has_s, has_n, a);
                 }
@@ -164,15 +169,17 @@ __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __rest
 // K sweeps on the region in shared memory: hs holds the heights and ends with the result
 // (swapping with hn each sweep); the region's valid part shrinks by two cells a side per sweep.
 template <int RW, int RH, int K, bool EDGE>
-__device__ __forceinline__ float* sweeps(float* hs, float* hn, float* gv, int y0, int H, const ThermalArgs& a) {
-    pass<RW, RH, 1, false, EDGE>(hs, gv, nullptr, y0, H, a);
+__device__ __forceinline__ float* sweeps(float* hs, float* hn, float* gv, int y0, int H, const ThermalArgs& a,
+                                         bool& changed) {
+    constexpr int HALO = 2 * K;
+    pass<RW, RH, 1, false, EDGE>(hs, gv, nullptr, y0, H, a, HALO, changed);
     __syncthreads();
-    pass<RW, RH, 2, true, EDGE>(hs, gv, hn, y0, H, a);
+    pass<RW, RH, 2, true, EDGE>(hs, gv, hn, y0, H, a, HALO, changed);
     __syncthreads();
     if constexpr (K == 2) {
-        pass<RW, RH, 3, false, EDGE>(hn, gv, nullptr, y0, H, a);
+        pass<RW, RH, 3, false, EDGE>(hn, gv, nullptr, y0, H, a, HALO, changed);
         __syncthreads();
-        pass<RW, RH, 4, true, EDGE>(hn, gv, hs, y0, H, a);
+        pass<RW, RH, 4, true, EDGE>(hn, gv, hs, y0, H, a, HALO, changed);
         __syncthreads();
         return hs;
     } else {
@@ -181,7 +188,7 @@ __device__ __forceinline__ float* sweeps(float* hs, float* hn, float* gv, int y0
 }
 
 template <int K>
-__global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __restrict__ in, float* __restrict__ out,
+__global__ void __launch_bounds__(THREADS, 6) thermal_sweeps_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                                  int W, int H, ThermalArgs a, TileFlags fl) {
     constexpr int HALO = 2 * K;
     constexpr int RW = TX + 2 * HALO;   // region width
@@ -218,24 +225,21 @@ __global__ void __launch_bounds__(THREADS) thermal_sweeps_kernel(const float* __
 
     // Tiles whose region lies inside the grid's rows take the path without pole checks.
     const bool edge = y0 < 0 || y0 + RH > H;
-    const float* res = edge ? sweeps<RW, RH, K, true>(sm_a, sm_b, sm_g, y0, H, a)
-                            : sweeps<RW, RH, K, false>(sm_a, sm_b, sm_g, y0, H, a);
+    bool moved_any = false;
+    const float* res = edge ? sweeps<RW, RH, K, true>(sm_a, sm_b, sm_g, y0, H, a, moved_any)
+                            : sweeps<RW, RH, K, false>(sm_a, sm_b, sm_g, y0, H, a, moved_any);
 
-    int changed = 0;
     for (int yy = ty; yy < TY; yy += 8) {
         const int gy = blockIdx.y * TY + yy;
         if (gy >= H) continue;
         for (int xx = tx; xx < TX; xx += 32) {
             const int gx = blockIdx.x * TX + xx;
             if (gx >= W) continue;
-            const size_t idx = (size_t)gy * W + gx;
-            const float v = res[(yy + HALO) * RW + xx + HALO];
-            if (__float_as_uint(v) != __float_as_uint(in[idx])) changed = 1;
-            out[idx] = v;
+            out[(size_t)gy * W + gx] = res[(yy + HALO) * RW + xx + HALO];
         }
     }
     if (fl.cur) {
-        changed = __syncthreads_or(changed);
+        const int changed = __syncthreads_or(moved_any);
         if (threadIdx.x == 0) fl.cur[tile] = changed ? 1 : 0;
     }
 }
