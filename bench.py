@@ -36,7 +36,7 @@ UNIT = "Mcell-rounds/s"
 ROUNDS = 12
 # DRAM bytes (read + write) of one two-sweep launch of thermal_sweeps_kernel on the 8192 x 4096
 # field, from ncu (profiles/thermal_sweeps_8192x4096.md); the roofline's traffic at that size.
-SWEEP_TRAFFIC_PER_LAUNCH = 229.8e6
+SWEEP_TRAFFIC_PER_LAUNCH = 228.1e6
 
 
 def parse():
