@@ -7,6 +7,7 @@ cartogenesis/worldgen/pipeline):
   SeaLevelStage.percentile_cut -> SeaLevelStage.percentileCut (P/SeaLevelStage.kt:146-200)
   FlowRouting.*                -> FlowRouting.fillDepressions, flowDirections, drainageOrder,
                                   accumulate, spillways (P/FlowRouting.kt)
+  HydraulicErosion.breach      -> HydraulicErosion.breach    (P/HydraulicErosion.kt:1931-2171)
 Arrays are numpy, row-major [height, width]. Every call runs on the GPU; none falls back to a CPU.
 """
 import ctypes as C
@@ -237,3 +238,24 @@ class FlowRouting:
         out.update(count=b.count, largest=b.largest, largest_cells=b.largest_cells, largest_depth=b.largest_depth,
                    deepest=b.deepest, labels=labels)
         return out
+
+
+class HydraulicErosion:
+    @staticmethod
+    def breach(config, is_land, relative, ground, directions, area, land_cells, land_range, surface, ctx=None):
+        """HydraulicErosion.breach (belowSea false, nothing carried) over the basins of this routing.
+        `relative`, `ground` and `surface` (float32, C-contiguous) are cut in place, as the reference
+        cuts its arrays; returns the number of cells the notch lowered."""
+        ctx = ctx or default_context()
+        H, W = config.params.height, config.params.width
+        for a in (relative, ground, surface):
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != W * H:
+                raise ValueError("relative, ground and surface must be C-contiguous float32 grids")
+        il = np.ascontiguousarray(is_land, dtype=np.uint8)
+        rec = np.ascontiguousarray(directions, dtype=np.int32)
+        ar = np.ascontiguousarray(area, dtype=np.float32)
+        cells = C.c_int32()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_breach(ctx.handle, C.byref(config.params), P(il), P(relative), P(ground), P(rec),
+                                        P(ar), land_cells, land_range, P(surface), C.byref(cells)))
+        return cells.value

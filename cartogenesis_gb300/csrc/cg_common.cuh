@@ -78,7 +78,7 @@ enum Slot {
     S_SCRATCH1, S_SCRATCH2, S_SCRATCH3, S_ROWW, S_HIST, S_BRACKET, S_BRACKET2, S_SMALL, S_FLATS,
     S_FLATIDX, S_FLATMEM, S_CG0, S_CG1, S_CG2, S_CG3, S_CG4, S_CG5, S_LEVELCNT, S_DEPTH, S_STATS,
     S_BASIN, S_BASIN2, S_FILLQ, S_FILLF, S_FILLFLAG, S_TILEFLAG, S_SCRATCH4, S_SCRATCH5, S_THERMFLAG,
-    S_LINKS, S_SOURCES, S_FILLLIST,
+    S_LINKS, S_SOURCES, S_FILLLIST, S_CLAIM, S_FOOT, S_BREACH,
     S_COUNT
 };
 

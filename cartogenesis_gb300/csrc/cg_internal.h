@@ -64,11 +64,37 @@ struct InciseArgs {
 cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const long long* d_key,
                      int levels, const float* d_ground, const float* d_rel, const float* d_area, const float* d_erod,
                      float* d_surface, const InciseArgs& a);
-struct BasinsDev {
-    int count;
+// FlowRouting.spillways on the device: per basin (in the order the reference finds them) its entry,
+// pour point, level, floor, fill depth and cell count, in the context's basin block; d_label
+// receives each ponded cell's basin. *h_count (synchronises) receives the number of basins.
+struct BasinArrays {
+    int* entry = nullptr;
+    int* spill = nullptr;
+    float* level = nullptr;
+    float* floor_ = nullptr;
+    float* depth = nullptr;
+    int* cells = nullptr;
 };
+cg_status basins_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
+                     const int32_t* d_recv, float pond_depth, int32_t* d_label, BasinArrays* out, int* h_count);
+// The same, with the basins copied into host_basins (largest and deepest as the reference keeps them).
 cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
                         const int32_t* d_recv, float pond_depth, int32_t* d_label, cg_basins* host_basins);
+
+// ---- outlet notch (cg_breach.cu)
+struct BreachRates {
+    float relative_incision_coefficient;   // HydraulicErosion.Rates.relativeIncisionCoefficient
+    float notch_fall_per_cell;             // HydraulicErosion.Rates.notchFallPerCell
+    int outlet_reach_cells;                // HydraulicErosion.Rates.outletReachCells
+    float pond_depth;
+    float step_ns;
+    float step_diag;
+};
+// HydraulicErosion.breach over the basins of this routing: d_rel, d_ground and d_surface are cut in
+// place. *h_cells (optional) receives the cells cut.
+cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_rel, float* d_ground,
+                     const int32_t* d_recv, const float* d_area, float land_cells, float land_range,
+                     const BreachRates& rates, float* d_surface, int* h_cells);
 
 // ---- small helpers (cg_api.cu)
 cg_status sync(cg_ctx* ctx);

@@ -89,6 +89,10 @@ struct RatesF {
     float step_ns;
     float step_diag;
     double cell_height_in_cell_widths;
+    // The outlet notch's constants (profile P1).
+    float relative_incision_coefficient;   // HydraulicErosion.kt:246-247
+    float notch_fall_per_cell;             // HydraulicErosion.kt:281-282, NOTCH_FALL_METRES_PER_KM 0.0025
+    int outlet_reach_cells;                // HydraulicErosion.kt:303, ErosionConfig.outletReachKm 1500
 };
 
 inline RatesF rates_of(const cg_erosion_params& p) {
@@ -107,6 +111,9 @@ inline RatesF rates_of(const cg_erosion_params& p) {
     double cr = r.cell_height_in_cell_widths;
     r.step_ns = (float)cr;                          // GroundSteps.northSouth
     r.step_diag = (float)std::sqrt(1.0 + cr * cr);  // GroundSteps.diagonal
+    r.relative_incision_coefficient = r.incision_coefficient * s.relief_span() / s.highest_land;
+    r.notch_fall_per_cell = s.relief_share_of_metres(0.0025f * (float)s.cell_width_km(p.width));
+    r.outlet_reach_cells = whole_cells_for(p, 1500.0, 1);
     return r;
 }
 

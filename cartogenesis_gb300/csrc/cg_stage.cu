@@ -155,6 +155,13 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
     const float land_half = std::fmax(sc.land_half(), 1e-6f);
     const float sea_half = std::fmax(sc.sea_half(), 1e-6f);
     const float per_mm = (float)(sc.years_per_round / 1000.0);
+    BreachRates brates;
+    brates.relative_incision_coefficient = rates.relative_incision_coefficient;
+    brates.notch_fall_per_cell = rates.notch_fall_per_cell;
+    brates.outlet_reach_cells = rates.outlet_reach_cells;
+    brates.pond_depth = rates.pond_depth;
+    brates.step_ns = rates.step_ns;
+    brates.step_diag = rates.step_diag;
     CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
     CG_BUF(float, d_rel, ctx, S_REL, N);
     CG_BUF(float, d_filled, ctx, S_FILLED, N);
@@ -227,6 +234,9 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         int levels = 0;
         CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, &levels));
         mark(4);
+        if (p.profile == CG_PROFILE_P1)
+            CG_TRY(breach_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, d_area, (float)land_cells, land_half, brates,
+                              cur, nullptr));
         InciseArgs ia;
         ia.courant_coefficient = rates.courant_coefficient;
         ia.pond_depth = rates.pond_depth;
@@ -237,6 +247,33 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         ia.step_diag = rates.step_diag;
         ia.only_above_base = p.receiver_clamp != 0;
         CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia));
+        if (p.profile == CG_PROFILE_P1 && round == p.hydraulic_rounds - 1) {
+            // The closing breach (HydraulicErosion.kt:1404-1442): a fresh cut at today's shoreline over
+            // the finished surface, its own fill, routing and discharge, then one more notch. Its
+            // routing is what the stage reports.
+            float closing_shoreline;
+            int closing_land;
+            CG_TRY(percentile_cut_dev(ctx, W, H, cur, p.sea_level, land_half, sea_half, 0.0f, d_land, d_rel,
+                                      &closing_shoreline, &closing_land));
+            *last_land_cells = closing_land;
+            if (closing_land > 0) {
+                if (d_rain) {
+                    CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_rain, d_land, N, 0, d_sum);
+                    CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, sm>>>(d_rain, d_sum, closing_land, N, d_runoff);
+                } else {
+                    CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_runoff, N, 1.0f);
+                }
+                CG_CHECK_LAUNCH(ctx);
+                CG_TRY(fill_depressions_dev(ctx, W, H, d_land, d_rel, d_filled, nullptr, nullptr));
+                FlatCounts closing_flats{0, 0, 0};
+                CG_TRY(flow_directions_dev(ctx, W, H, d_land, d_rel, d_filled, p.seed, rates.cell_height_in_cell_widths,
+                                           lattice, p.facet_routing != 0, p.flat_potential != 0, d_recv, d_surface,
+                                           &closing_flats));
+                CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, nullptr));
+                CG_TRY(breach_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, d_area, (float)closing_land, land_half,
+                                  brates, cur, nullptr));
+            }
+        }
         mark(5);
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         float* res;
@@ -288,7 +325,8 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_input
                     CG_ABI_VERSION);
     CG_TRY(check_grid(ctx, p->width, p->height));
     if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
-    if (p->profile != CG_PROFILE_P0) return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 only)", p->profile);
+    if (p->profile != CG_PROFILE_P0 && p->profile != CG_PROFILE_P1)
+        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 and P1 only)", p->profile);
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->cancel.store(0);
     const int W = p->width, H = p->height;
@@ -363,7 +401,8 @@ cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* p, const cg_i
                     CG_ABI_VERSION);
     CG_TRY(check_grid(ctx, p->width, p->height));
     if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
-    if (p->profile != CG_PROFILE_P0) return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 only)", p->profile);
+    if (p->profile != CG_PROFILE_P0 && p->profile != CG_PROFILE_P1)
+        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 and P1 only)", p->profile);
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->cancel.store(0);
     const size_t N = (size_t)p->width * p->height;
@@ -487,6 +526,47 @@ cg_status cg_accumulate(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_lan
     CG_TRY(down(ctx, area, d_area, N * 4));
     (void)land_cells;
     return sync(ctx);
+}
+
+cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* p, const uint8_t* is_land, float* relative, float* ground,
+                    const int32_t* receivers, const float* area, float land_cells, float land_range, float* surface,
+                    int32_t* cells_cut) {
+    if (!ctx || !p || !is_land || !relative || !ground || !receivers || !area || !surface) return CG_BAD_ARG;
+    if (p->abi_version != CG_ABI_VERSION)
+        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
+                    CG_ABI_VERSION);
+    CG_TRY(check_grid(ctx, p->width, p->height));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int W = p->width, H = p->height;
+    const size_t N = (size_t)W * H;
+    const RatesF rates = rates_of(*p);
+    BreachRates br;
+    br.relative_incision_coefficient = rates.relative_incision_coefficient;
+    br.notch_fall_per_cell = rates.notch_fall_per_cell;
+    br.outlet_reach_cells = rates.outlet_reach_cells;
+    br.pond_depth = rates.pond_depth;
+    br.step_ns = rates.step_ns;
+    br.step_diag = rates.step_diag;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_BUF(float, d_area, ctx, S_AREA, N);
+    CG_BUF(float, d_h, ctx, S_H0, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_rel, relative, N * 4));
+    CG_TRY(up(ctx, d_filled, ground, N * 4));
+    CG_TRY(up(ctx, d_recv, receivers, N * 4));
+    CG_TRY(up(ctx, d_area, area, N * 4));
+    CG_TRY(up(ctx, d_h, surface, N * 4));
+    int cells = 0;
+    CG_TRY(breach_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, d_area, land_cells, land_range, br, d_h, &cells));
+    CG_TRY(down(ctx, relative, d_rel, N * 4));
+    CG_TRY(down(ctx, ground, d_filled, N * 4));
+    CG_TRY(down(ctx, surface, d_h, N * 4));
+    CG_TRY(sync(ctx));
+    if (cells_cut) *cells_cut = cells;
+    return CG_OK;
 }
 
 cg_status cg_spillways(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const float* relative,

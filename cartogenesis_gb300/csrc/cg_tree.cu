@@ -641,8 +641,8 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     return CG_OK;
 }
 
-cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
-                        const int32_t* d_recv, float pond_depth, int32_t* d_label, cg_basins* hb) {
+cg_status basins_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
+                     const int32_t* d_recv, float pond_depth, int32_t* d_label, BasinArrays* out, int* h_count) {
     size_t N = (size_t)W * H;
     cudaStream_t sm = ctx->stream;
     int grid = ctx->num_sms * 8;
@@ -653,6 +653,36 @@ cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const 
     int count = 0;
     cg_status st = component_labels(ctx, W, H, d_ponded, d_root, d_label, &count);
     if (st != CG_OK) return st;
+    *h_count = count;
+    *out = BasinArrays{};
+    if (count == 0) return CG_OK;
+    // One block: spill keys (8 bytes each) first for alignment, then seven 4-byte arrays.
+    CG_BUF(unsigned long long, d_b, ctx, S_BASIN, (size_t)count * 5 + 8);
+    BasinDev b;
+    b.spill_key = d_b;
+    b.cells = (int*)(d_b + count);
+    b.floor_key = (unsigned*)(b.cells + count);
+    out->cells = b.cells;
+    out->entry = (int*)(b.floor_key + count);
+    out->spill = out->entry + count;
+    out->level = (float*)(out->spill + count);
+    out->floor_ = out->level + count;
+    out->depth = out->floor_ + count;
+    CG_LAUNCH(ctx) k_basin_init<<<(count + 255) / 256, 256, 0, sm>>>(b, count);
+    CG_LAUNCH(ctx) k_basin_gather<<<grid, 256, 0, sm>>>(d_label, d_ponded, d_land, d_rel, d_filled, d_recv, N, b);
+    CG_LAUNCH(ctx) k_basin_finish<<<(count + 255) / 256, 256, 0, sm>>>(b, count, d_land, d_rel, d_filled, d_recv, (long long)N,
+                                                        out->entry, out->spill, out->level, out->floor_, out->depth);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel, const float* d_filled,
+                        const int32_t* d_recv, float pond_depth, int32_t* d_label, cg_basins* hb) {
+    cudaStream_t sm = ctx->stream;
+    int count = 0;
+    BasinArrays d;
+    cg_status st = basins_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, pond_depth, d_label, &d, &count);
+    if (st != CG_OK) return st;
     if (hb) {
         hb->count = count;
         hb->largest = -1;
@@ -661,30 +691,14 @@ cg_status spillways_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const 
         hb->deepest = 0.0f;
     }
     if (count == 0 || !hb) return sync(ctx);
-    // One block: spill keys (8 bytes each) first for alignment, then seven 4-byte arrays.
-    CG_BUF(unsigned long long, d_b, ctx, S_BASIN, (size_t)count * 5 + 8);
-    BasinDev b;
-    b.spill_key = d_b;
-    b.cells = (int*)(d_b + count);
-    b.floor_key = (unsigned*)(b.cells + count);
-    int* d_entry = (int*)(b.floor_key + count);
-    int* d_spill = d_entry + count;
-    float* d_level = (float*)(d_spill + count);
-    float* d_floor = d_level + count;
-    float* d_depth = d_floor + count;
-    CG_LAUNCH(ctx) k_basin_init<<<(count + 255) / 256, 256, 0, sm>>>(b, count);
-    CG_LAUNCH(ctx) k_basin_gather<<<grid, 256, 0, sm>>>(d_label, d_ponded, d_land, d_rel, d_filled, d_recv, N, b);
-    CG_LAUNCH(ctx) k_basin_finish<<<(count + 255) / 256, 256, 0, sm>>>(b, count, d_land, d_rel, d_filled, d_recv, (long long)N,
-                                                        d_entry, d_spill, d_level, d_floor, d_depth);
-    CG_CHECK_LAUNCH(ctx);
     std::vector<int> cells(count), entry(count), spill(count);
     std::vector<float> level(count), flo(count), depth(count);
-    CG_CUDA(ctx, cudaMemcpyAsync(cells.data(), b.cells, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaMemcpyAsync(entry.data(), d_entry, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaMemcpyAsync(spill.data(), d_spill, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaMemcpyAsync(level.data(), d_level, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaMemcpyAsync(flo.data(), d_floor, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
-    CG_CUDA(ctx, cudaMemcpyAsync(depth.data(), d_depth, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(cells.data(), d.cells, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(entry.data(), d.entry, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(spill.data(), d.spill, count * sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(level.data(), d.level, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(flo.data(), d.floor_, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(depth.data(), d.depth, count * sizeof(float), cudaMemcpyDeviceToHost, sm));
     CG_CUDA(ctx, cudaStreamSynchronize(sm));
     // The running largest / deepest of FlowRouting.kt:664-670, in basin order.
     int largest = -1, largest_cells = 0;

@@ -49,6 +49,9 @@ typedef enum cg_mode { CG_MODE_REF32 = 0 } cg_mode;
 /*
  * Round-tail profile. P0: uplift, percentile cut, weights, fill, routing, accumulation, incision
  * and relaxation (climateFeed, deposition, outletIncision, flexure and the belt replay off).
+ * P1: P0 with ErosionConfig.outletIncision: each round's notch before the incision and the closing
+ * breach before the last relaxation (HydraulicErosion.kt:1002-1028, 1404-1442); the routing outputs
+ * are then the closing pass's, as its notch left them. P2 (deposition) is not built.
  */
 typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2 } cg_profile;
 
@@ -91,7 +94,7 @@ typedef struct cg_erosion_params {
     /* Test switches, never set by a production caller */
     int32_t  receiver_clamp;              /* 1: HydraulicErosion.incise onlyAboveBase */
     int32_t  shield_cut;                  /* 1: incision takes the cover's factor */
-    int32_t  profile;                     /* cg_profile; only P0 is implemented */
+    int32_t  profile;                     /* cg_profile; P0 and P1 are implemented */
     int32_t  reserved;
 } cg_erosion_params;
 
@@ -261,6 +264,16 @@ cg_status cg_accumulate(cg_ctx* ctx, int32_t width, int32_t height, const uint8_
 cg_status cg_spillways(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
                        const float* relative, const float* filled, const int32_t* receivers,
                        float pond_depth, int32_t* basin_of_cell, cg_basins* basins);
+
+/*
+ * HydraulicErosion.breach (.../pipeline/HydraulicErosion.kt:1931-2171), the outlet notch of profile
+ * P1, over the basins FlowRouting.spillways finds on this routing (`ground` is the filled surface):
+ * belowSea false, nothing carried. `relative`, `ground` and `surface` (the height field) are cut in
+ * place; `cells_cut` (may be NULL) receives the cells the notch lowered. Rates come from `params`.
+ */
+cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* params, const uint8_t* is_land,
+                    float* relative, float* ground, const int32_t* receivers, const float* area,
+                    float land_cells, float land_range, float* surface, int32_t* cells_cut);
 
 #ifdef __cplusplus
 }

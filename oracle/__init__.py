@@ -54,6 +54,9 @@ def lib():
         L.or_spillways.restype = i32
         L.or_incise.argtypes = [C.POINTER(abi.ErosionParams), vp, i32, vp, vp, vp, vp, vp, f32, f32, f32, vp, vp,
                                 i32, vp]
+        L.or_breach.argtypes = [C.POINTER(abi.ErosionParams), vp, vp, vp, vp, vp, f32, f32, vp, C.POINTER(f64)]
+        L.or_breach.restype = i32
+        L.or_outlet_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(i32)]
         L.or_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)]
         L.or_stand_below_today.argtypes = [C.POINTER(abi.ErosionParams), i32]
         L.or_stand_below_today.restype = f32
@@ -191,6 +194,27 @@ def incise(params, order, directions, is_land, ground, relative, discharge, land
     lib().or_incise(C.byref(params), P(order), len(order), P(directions), P(is_land), P(ground), P(relative),
                     P(discharge), land_cells, land_range, shoreline, P(erodibility), P(surface),
                     int(only_above_base), P(unresolved))
+
+
+def outlet_rates(params):
+    """(relativeIncisionCoefficient, notchFallPerCell, outletReachCells) of HydraulicErosion.Rates."""
+    a, b, c = C.c_float(), C.c_float(), C.c_int32()
+    lib().or_outlet_rates(C.byref(params), C.byref(a), C.byref(b), C.byref(c))
+    return a.value, b.value, c.value
+
+
+def breach(params, is_land, relative, ground, directions, area, land_cells, land_range, surface):
+    """HydraulicErosion.breach over the basins of this routing. `relative`, `ground` and `surface`
+    (float32, contiguous) are cut in place; returns (cells cut, amount moved)."""
+    for a in (relative, ground, surface):
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+    il = np.ascontiguousarray(is_land, dtype=np.uint8)
+    rec = np.ascontiguousarray(directions, dtype=np.int32)
+    ar = np.ascontiguousarray(area, dtype=np.float32)
+    moved = C.c_double()
+    cells = lib().or_breach(C.byref(params), P(il), P(relative), P(ground), P(rec), P(ar), land_cells, land_range,
+                            P(surface), C.byref(moved))
+    return cells, moved.value
 
 
 def stand_below_today(params, round_):

@@ -888,10 +888,13 @@ void spillways(int W, int H, const u8* is_land, const float* elev, const float* 
 const float kPondDepthMetres = 24.0f;    // HydraulicErosion.kt:192
 const float kVegetationShielding = 0.5f; // HydraulicErosion.kt:1716
 
-struct Rates {   // HydraulicErosion.Rates (HydraulicErosion.kt:203-312), the P0 members
+struct Rates {   // HydraulicErosion.Rates (HydraulicErosion.kt:203-312), the P0 and P1 members
     float incision_coefficient;
     float courant_coefficient;
     float pond_depth;
+    float relative_incision_coefficient;   // HydraulicErosion.kt:246-247
+    float notch_fall_per_cell;             // HydraulicErosion.kt:281-282, NOTCH_FALL_METRES_PER_KM 0.0025
+    int outlet_reach_cells;                // HydraulicErosion.kt:303, ErosionConfig.outletReachKm 1500
     GroundSteps steps;
     explicit Rates(const cg_erosion_params& p) : steps(0.0) {
         Scale s = scale_of(p);
@@ -904,6 +907,9 @@ struct Rates {   // HydraulicErosion.Rates (HydraulicErosion.kt:203-312), the P0
         incision_coefficient = (float)(per_year * geometry * ratio);
         courant_coefficient = incision_coefficient / s.land_half() * (float)p.width;
         pond_depth = s.relief_share_of_metres(kPondDepthMetres);
+        relative_incision_coefficient = incision_coefficient * s.relief_span() / s.highest_land;
+        notch_fall_per_cell = s.relief_share_of_metres(0.0025f * (float)s.cell_width_km(p.width));
+        outlet_reach_cells = whole_cells_for(p, 1500.0, 1);
         steps = GroundSteps(s.cell_height_km(p.height) / s.cell_width_km(p.width));
     }
 };
@@ -989,6 +995,126 @@ void incise(const Rates& rates, int W, size_t N, const int32_t* order, int order
     }
 }
 
+// Math.min(float, float) on the JVM: NaN if either is, and -0 below +0.
+inline float jvm_min(float a, float b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    if (a == 0.0f && b == 0.0f) return std::signbit(a) ? a : b;
+    return a < b ? a : b;
+}
+
+// HydraulicErosion.raise (HydraulicErosion.kt:2535-2539): the change actually made, in double.
+inline double raise(float* field, int cell, double amount) {
+    float prior = field[cell];
+    field[cell] = (float)((double)prior + amount);
+    return (double)field[cell] - (double)prior;
+}
+
+struct Breached {
+    double moved = 0.0;
+    int cells = 0;
+};
+
+// HydraulicErosion.breach (HydraulicErosion.kt:1931-2171) as the rounds and the closing pass run it:
+// belowSea false, no settled field and no load (nothing is carried in profile P1), and
+// ErosionConfig's outletIncisionRatio 1.125 and outletFallToTheWater on. Basins are taken in the
+// order spillways found them; `relative`, `ground` and `surface` are cut in place.
+Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_land, float* relative, float* ground,
+                const int32_t* dirs, const float* area, float land_cells, float land_range, float* surface) {
+    Breached out;
+    const GroundSteps& steps = rates.steps;
+    const float reach = (float)rates.outlet_reach_cells;   // Float < Int compares as floats
+    const float gradient = rates.notch_fall_per_cell;
+    auto take_down_to = [&](int cell, float cut_level) {
+        double take = (double)(relative[cell] - cut_level) * (double)land_range;
+        bool ponded = ground[cell] - relative[cell] > rates.pond_depth;
+        double removed = -raise(surface, cell, -take);
+        if (removed > 0.0) {
+            float as_relative = (float)(removed / (double)land_range);
+            relative[cell] -= as_relative;
+            if (!ponded) ground[cell] -= as_relative;
+            out.moved += removed;
+            out.cells++;
+        }
+    };
+    for (int b = 0; b < notch.count; ++b) {
+        int spill = notch.spill[b];
+        if (spill < 0) continue;
+        float level = notch.level[b];
+        float floor_ = notch.floor_[b];
+        if (level - floor_ <= 0.0f) continue;
+        // The channel's fall and length below the lip.
+        float fall = 0.0f, length = 0.0f, last_step = steps.east_west;
+        int walked = 0;
+        int cell = spill;
+        while (cell >= 0 && is_land[cell] && length < reach) {
+            fall = level - relative[cell];
+            if (fall > level - floor_) break;
+            int next = dirs[cell];
+            last_step = next >= 0 ? steps.between(cell, next, W) : steps.east_west;
+            length += last_step;
+            walked++;
+            cell = next;
+        }
+        // A sill level to the water measures the step into it (FlowRouting.FLAT_GRADIENT_STEP 1e-6).
+        if (fall <= 1e-6f * (float)walked && cell >= 0 && !is_land[cell]) {
+            fall = level - relative[cell];
+            length += last_step;
+        }
+        if (walked == 0) continue;
+        float slope = fall / length * (float)W;
+        if (slope < 0.0f) slope = 0.0f;
+        float power = rates.relative_incision_coefficient * 1.125f * std::sqrt(area[spill] / land_cells) * slope;
+        float drop = jvm_min(power, jvm_min(level - floor_, level));
+        if (drop <= 0.0f) continue;
+        float new_level = level - drop;
+        // Down the channel from the lip, falling `gradient` a cell width, never below the shoreline.
+        float from_lip = 0.0f;
+        cell = spill;
+        while (cell >= 0 && is_land[cell] && from_lip < reach) {
+            float falling = new_level - from_lip * gradient;
+            float cut_level = falling < 0.0f ? 0.0f : falling;
+            if (relative[cell] <= cut_level) break;
+            take_down_to(cell, cut_level);
+            int next = dirs[cell];
+            from_lip += next >= 0 ? steps.between(cell, next, W) : steps.east_west;
+            cell = next;
+        }
+        // Back across the shallow margin, from the lip towards the entry, rising by the same gradient.
+        int entry = notch.entry[b];
+        if (entry >= 0 && entry != spill) {
+            int margin_cells = 0;
+            int walker = entry;
+            float widths = 0.0f;
+            while (walker >= 0 && walker != spill && is_land[walker] && widths <= reach) {
+                int next = dirs[walker];
+                widths += next >= 0 ? steps.between(walker, next, W) : steps.east_west;
+                margin_cells++;
+                walker = next;
+            }
+            if (walker == spill) {
+                std::vector<int> margin(margin_cells);
+                walker = entry;
+                for (int i = 0; i < margin_cells; ++i) {
+                    margin[i] = walker;
+                    walker = dirs[walker];
+                }
+                float back = 0.0f;
+                int downstream = spill;
+                for (int i = margin_cells - 1; i >= 0; --i) {
+                    int m = margin[i];
+                    back += steps.between(m, downstream, W);
+                    float cut_level = new_level + back * gradient;
+                    if (relative[m] <= cut_level) break;
+                    take_down_to(m, cut_level);
+                    downstream = m;
+                }
+            }
+        }
+    }
+    return out;
+}
+
 struct StageOut {
     std::vector<float> height;
     Cut cut;
@@ -998,8 +1124,11 @@ struct StageOut {
 };
 
 // ErosionStage.apply (ErosionStage.kt:133-183) with HydraulicErosion.apply (HydraulicErosion.kt:596-1506)
-// for profile P0: no provisional climate (the given weather is held), no belt replay, no flexure, no
-// deposition, no outlet notch.
+// for profiles P0 and P1: no provisional climate (the given weather is held), no belt replay, no
+// flexure, no deposition; P1 adds the outlet notch (ErosionConfig.outletIncision): each round's breach
+// before the incision (HydraulicErosion.kt:1002-1028) and the closing breach before the last
+// relaxation (HydraulicErosion.kt:1404-1442). P1's routing outputs are the closing pass's, as its
+// breach left them.
 // run_rounds >= 0 stops after that many rounds (the relaxation keeps the whole stage's share per
 // round) and initial = false leaves out the initial sweeps: a bounded sample of a stage.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
@@ -1039,6 +1168,7 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     std::vector<float> filled(N), area(N);
     std::vector<int32_t> dirs(N), order;
     FlatCounts flats;
+    bool routed = true;
     const int last = run_rounds >= 0 && run_rounds < p.hydraulic_rounds ? run_rounds : p.hydraulic_rounds;
     for (int round = 0; round < last; ++round) {
         if (in.uplift_mm_per_year) {
@@ -1067,6 +1197,13 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
         drainage_order(W, H, cut.is_land.data(), dirs.data(), cut.land_cells, order.data());
         float land_cells = (float)cut.land_cells;
         float land_range = std::max(sc.land_half(), 1e-6f);
+        if (p.profile == CG_PROFILE_P1) {
+            Spillways notch;
+            spillways(W, H, cut.is_land.data(), cut.relative.data(), filled.data(), dirs.data(), rates.pond_depth,
+                      notch, nullptr);
+            breach(rates, W, notch, cut.is_land.data(), cut.relative.data(), filled.data(), dirs.data(), area.data(),
+                   land_cells, land_range, working.data());
+        }
         incise(rates, W, N, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(), filled.data(),
                cut.relative.data(), area.data(), land_cells, land_range, cut.shoreline, erod.data(), working.data(),
                p.receiver_clamp != 0, nullptr);
@@ -1080,10 +1217,35 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
             s.flats_kept = flats.kept;
             s.raised_cells = flats.raised;
         }
+        if (p.profile == CG_PROFILE_P1 && round == p.hydraulic_rounds - 1) {
+            // The closing breach over the finished surface: a fresh cut at today's shoreline, its own
+            // fill, routing and discharge, then one more notch.
+            Cut after;
+            percentile_cut(W, H, working.data(), p.sea_level, sc, 0.0f, after);
+            if (after.land_cells == 0) {
+                routed = false;
+            } else {
+                fill_depressions(W, H, after.is_land.data(), after.relative.data(), filled.data());
+                FlatCounts closing_flats;
+                flow_directions(W, H, after.is_land.data(), after.relative.data(), filled.data(), p.seed, r, lattice,
+                                p.facet_routing != 0, p.flat_potential != 0, dirs.data(), nullptr, &closing_flats);
+                normalise_over_land(rain, after.is_land.data(), after.land_cells, N, runoff.data());
+                accumulate(W, H, after.is_land.data(), dirs.data(), after.land_cells, runoff.data(), area.data());
+                Spillways notch;
+                spillways(W, H, after.is_land.data(), after.relative.data(), filled.data(), dirs.data(),
+                          rates.pond_depth, notch, nullptr);
+                breach(rates, W, notch, after.is_land.data(), after.relative.data(), filled.data(), dirs.data(),
+                       area.data(), (float)after.land_cells, land_range, working.data());
+                order.assign(after.land_cells, 0);
+                drainage_order(W, H, after.is_land.data(), dirs.data(), after.land_cells, order.data());
+                cut = std::move(after);
+            }
+        }
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         if (with_thermal) thermal_sweep(W, H, working.data(), working.data(), lim, per_round, p.rate, true);
     }
     std::memcpy(out->height, working.data(), N * sizeof(float));
+    if (!routed) return CG_OK;
     if (out->receivers) std::memcpy(out->receivers, dirs.data(), N * sizeof(int32_t));
     if (out->area) std::memcpy(out->area, area.data(), N * sizeof(float));
     if (out->filled) std::memcpy(out->filled, filled.data(), N * sizeof(float));
@@ -1239,6 +1401,28 @@ void or_incise(const cg_erosion_params* p, const int32_t* order, int32_t order_l
     Rates rates(*p);
     incise(rates, p->width, (size_t)p->width * p->height, order, order_len, directions, is_land, ground, relative,
            discharge, land_cells, land_range, shoreline, erodibility, surface, only_above_base != 0, unresolved);
+}
+
+// HydraulicErosion.breach over the basins FlowRouting.spillways finds on the given routing; relative,
+// ground and surface are cut in place. Returns the cells cut; *moved receives the amount taken.
+int32_t or_breach(const cg_erosion_params* p, const uint8_t* is_land, float* relative, float* ground,
+                  const int32_t* directions, const float* area, float land_cells, float land_range, float* surface,
+                  double* moved) {
+    Rates rates(*p);
+    Spillways notch;
+    spillways(p->width, p->height, is_land, relative, ground, directions, rates.pond_depth, notch, nullptr);
+    Breached b = breach(rates, p->width, notch, is_land, relative, ground, directions, area, land_cells, land_range,
+                        surface);
+    if (moved) *moved = b.moved;
+    return b.cells;
+}
+
+void or_outlet_rates(const cg_erosion_params* p, float* relative_incision_coefficient, float* notch_fall_per_cell,
+                     int32_t* outlet_reach_cells) {
+    Rates rates(*p);
+    *relative_incision_coefficient = rates.relative_incision_coefficient;
+    *notch_fall_per_cell = rates.notch_fall_per_cell;
+    *outlet_reach_cells = rates.outlet_reach_cells;
 }
 
 void or_rates(const cg_erosion_params* p, float* incision_coefficient, float* courant_coefficient,
