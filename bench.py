@@ -15,6 +15,8 @@ is 134 MB), so no flush is needed between steps.
          no JVM), all host threads for the thermal sweeps as the reference's parallelChunks does,
          on a bounded sample of the same workload: per step one round of the 12-round stage on the
          same world after its initial sweeps, plus a twelfth of those sweeps.
+  --profile 1: the same measurement of profile P1 (P0 with the outlet notch in every round and the
+         closing breach); the default is P0, the plain stage the metric names.
 Multi-GPU: replicas only (one independent world per rank, seed = rank + 1); the stage does not
 shard within a world, so there is no collective on the data path.
 """
@@ -47,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=8192)
     ap.add_argument("--height", type=int, default=4096)
+    ap.add_argument("--profile", type=int, default=0, choices=[0, 1],
+                    help="round-tail profile: 0 = P0 (the plain stage), 1 = P1 (P0 with the outlet notch and the "
+                         "closing breach)")
     ap.add_argument("--cpu-sample", type=int, default=1,
                     help="samples of the CPU baseline (one round of the stage on the bench world plus a twelfth "
                          "of its initial sweeps, on the CPU restatement); 0 skips the CPU leg")
@@ -122,12 +127,12 @@ class CpuSample:
     (computed once, untimed), plus a twelfth of those initial sweeps, timed together. Cell-rounds
     per sample: the grid's cells times one round."""
 
-    def __init__(self, W, H, threads):
+    def __init__(self, W, H, threads, profile=0):
         import oracle
         self.oracle = oracle
-        self.W, self.H, self.cores = W, H, threads
+        self.W, self.H, self.cores, self.profile = W, H, threads, profile
         h, self.up, self.rk = world_inputs(W, H, 1)
-        self.p = oracle.default_params(W, H, 1, sea_level=0.70)
+        self.p = oracle.default_params(W, H, 1, sea_level=0.70, profile=profile)
         self.lim, self.sweeps = oracle.thermal_limits(self.p)
         self.share = (self.sweeps + ROUNDS - 1) // ROUNDS
         self.swept = oracle.thermal_sweep(h, self.lim, self.sweeps, self.p.rate)
@@ -139,12 +144,14 @@ class CpuSample:
         return time.perf_counter() - t0
 
     def describe(self, n):
+        notch = (" (P1: the round's notch included, the stage's one closing breach not)" if self.profile == 1
+                 else "")
         return (f"round 1 of the 12-round stage on the {self.W}x{self.H} world after its {self.sweeps} initial "
-                f"sweeps, plus {self.share} sweeps (a twelfth of them); median of {n}")
+                f"sweeps, plus {self.share} sweeps (a twelfth of them){notch}; median of {n}")
 
 
-def cpu_baseline(W, H, steps, threads):
-    s = CpuSample(W, H, threads)
+def cpu_baseline(W, H, steps, threads, profile=0):
+    s = CpuSample(W, H, threads, profile)
     times = [s.step() for _ in range(max(steps, 1))]
     t = statistics.median(times)
     return W * H / t / 1e6, t, threads, s.describe(len(times))
@@ -156,7 +163,7 @@ def run_reference(args):
         return 0
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     threads = int(os.environ["OMP_NUM_THREADS"])
-    s = CpuSample(args.width, args.height, threads)
+    s = CpuSample(args.width, args.height, threads, args.profile)
     for _ in range(args.warmup):
         s.step()
     times = [s.step() for _ in range(max(args.steps, 1))]
@@ -167,8 +174,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": len(times), "warmup": args.warmup, "ms_per_step": round(t * 1000.0, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"plain P0 erosion stage (REF32), CPU restatement of the reference: {sample}",
-                   "grid": [args.width, args.height], "rounds": ROUNDS, "sample_rounds_per_step": 1},
+        "config": {"workload": f"plain P{args.profile} erosion stage (REF32), CPU restatement of the reference: "
+                               f"{sample}",
+                   "grid": [args.width, args.height], "rounds": ROUNDS, "profile": f"P{args.profile}",
+                   "sample_rounds_per_step": 1},
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -191,7 +200,7 @@ def run_ours(args):
     N = W * H
     seed = rank + 1
     h, up, rk = world_inputs(W, H, seed)
-    cfg = ErosionConfig(W, H, seed, sea_level=0.70)
+    cfg = ErosionConfig(W, H, seed, sea_level=0.70, profile=args.profile)
     ctx = Context(local)
     lib = ctx.lib
 
@@ -283,9 +292,9 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1000.0 * t_dev / args.steps, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"plain P0 erosion stage (REF32, bit-exact to the reference restatement), "
+        "config": {"workload": f"plain P{args.profile} erosion stage (REF32, bit-exact to the reference restatement), "
                                f"{W}x{H} cells, {ROUNDS} rounds, fBm beta 2 + 15 uplift ridges, seed rank+1",
-                   "grid": [W, H], "rounds": ROUNDS, "sweeps": cfg.thermal_limits()[1],
+                   "grid": [W, H], "rounds": ROUNDS, "profile": f"P{args.profile}", "sweeps": cfg.thermal_limits()[1],
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (134 MB height field)"},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * 4 * N, "d2h_bytes_per_step": 4 * N},
         "gpu_launches": int(launches),
@@ -297,7 +306,7 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-        v, t, cores, sample = cpu_baseline(W, H, args.cpu_sample, int(os.environ["OMP_NUM_THREADS"]))
+        v, t, cores, sample = cpu_baseline(W, H, args.cpu_sample, int(os.environ["OMP_NUM_THREADS"]), args.profile)
         line["cpu_baseline"] = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)

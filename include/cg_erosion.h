@@ -154,7 +154,8 @@ typedef struct cg_round_stats {
     double  ms_fill;            /* fillDepressions */
     double  ms_route;           /* flat potentials and receivers */
     double  ms_tree;            /* donor counts, drainage keys and accumulation */
-    double  ms_incise;          /* the implicit incision */
+    double  ms_incise;          /* the implicit incision (P1: with the round's notch and, in the last
+                                   round, the closing breach's cut, fill, routing and notch) */
     double  ms_relax;           /* the round's thermal sweeps */
 } cg_round_stats;
 
