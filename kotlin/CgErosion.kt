@@ -27,6 +27,9 @@ import kotlinx.coroutines.CancellationException
 interface HydraulicAccelerator {
     val name: String
 
+    /** Whether this accelerator runs the stage `config` asks for; the engine keeps its own rounds if not. */
+    fun supports(config: WorldGenConfig): Boolean
+
     /** The stage's result heights, or throws; there is no CPU fallback once this is selected. */
     fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
                    rockErodibility: FloatField?, rainfallMm: FloatArray?, vegetation: FloatArray?): FloatField
@@ -81,6 +84,16 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
         output.toArray(JAVA_FLOAT)
     }
 
+    // cg_profile: P0 without the outlet notch, P1 with it (HydraulicErosion.breach and the closing
+    // breach); deposition is P2, which this build refuses.
+    private fun profileOf(config: WorldGenConfig): Int = when {
+        config.erosion.deposition -> 2
+        config.erosion.outletIncision -> 1
+        else -> 0
+    }
+
+    override fun supports(config: WorldGenConfig): Boolean = profileOf(config) <= 1
+
     override fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
                             rockErodibility: FloatField?, rainfallMm: FloatArray?, vegetation: FloatArray?): FloatField =
         Arena.ofConfined().use { a ->
@@ -101,6 +114,7 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
             p.set(JAVA_INT, 80, if (config.flatPotential) 1 else 0)
             p.set(JAVA_FLOAT, 84, config.seaLevel)
             p.set(JAVA_FLOAT, 88, config.sea.lowstandMetres)
+            p.set(JAVA_INT, 100, profileOf(config))
             fun field(f: FloatArray?) = if (f == null) MemorySegment.NULL else a.allocateFrom(JAVA_FLOAT, *f)
             val inputs = a.allocate(40, 8)
             inputs.set(ADDRESS, 0, field(height.data))
