@@ -13,9 +13,14 @@
 // earlier basin they overlap has already been cut, so cutting them all at once gives the sequential
 // result. The lowest waiting basin always holds its claims, so the waves end.
 //
-// One cooperative kernel runs the waves with two grid barriers each. A warp takes a basin: its lanes
-// place and check the claims; lane 0 replays the reference's walks over the footprint list. Heights
-// that an earlier wave may have cut on another SM are read through L2 (ld.cg) and written through it.
+// One cooperative kernel runs the waves with two grid barriers each. Most footprints are a few cells
+// (3.5 on average at 8192 x 4096): a thread takes such a basin, loads its cells and their heights
+// up front (all loads in flight at once), places and checks its claims and replays the reference's
+// walks in registers. A footprint longer than SHORT goes to a warp: the lanes load 32
+// cells at a time, find where each walk stops with a ballot, carry the walks' float sums of steps
+// lane by lane in the reference's order through shuffles, and cut the cells before the stop in
+// parallel (each cut reads and writes only its own cell). Heights that an earlier wave may have cut
+// on another SM are read through L2 (ld.cg) and written through it.
 #include <cooperative_groups.h>
 
 #include <climits>
@@ -31,9 +36,11 @@ namespace cgr = cooperative_groups;
 namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
+// Footprints of up to this many cells are cut by a thread, longer ones by a warp.
+constexpr int SHORT = 8;
 
 // Per-call control words at the end of the breach block.
-enum { Q_PENDING0 = 0, Q_PENDING1 = 1, Q_ERROR = 2, Q_CELLS = 3, Q_WAVES = 4, Q_WORDS = 8 };
+enum { Q_SHORT0 = 0, Q_SHORT1 = 1, Q_LONG0 = 2, Q_LONG1 = 3, Q_ERROR = 4, Q_CELLS = 5, Q_WAVES = 6, Q_WORDS = 8 };
 
 struct BreachDev {
     int W;
@@ -62,7 +69,7 @@ struct BreachDev {
     int* n1;             // of those, the channel's
     int* foot;           // the channel from the lip, then the margin from the entry
     unsigned long long* claim;
-    int* queue;          // two lists of `count` waiting basins
+    int* queue;          // four lists of `count` waiting basins: short (two waves), then long
     int* q;              // Q_* words
 };
 
@@ -147,20 +154,22 @@ __global__ void k_footprint_fill(BreachDev a) {
     if (a.n[b] > n1) margin(a, a.spill[b], a.entry[b], dst + n1);
 }
 
+// Basins with a footprint of at most SHORT cells go to the short queue (a thread each), the rest
+// to the long one (a warp each).
 __global__ void k_queue_init(BreachDev a) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= a.count || a.n[b] == 0) return;
-    a.queue[atomicAdd(&a.q[Q_PENDING0], 1)] = b;
+    if (a.n[b] <= SHORT) a.queue[atomicAdd(&a.q[Q_SHORT0], 1)] = b;
+    else a.queue[2 * (size_t)a.count + atomicAdd(&a.q[Q_LONG0], 1)] = b;
 }
 
 // HydraulicErosion.raise with the amount `-take`, and the cut it makes in the shoreline-relative
-// fields (HydraulicErosion.kt:2035-2050, 2084-2097). r is relative[cell] as read.
-__device__ __forceinline__ int take_down_to(const BreachDev& a, int cell, float r, float cut_level) {
-    const double take = __dmul_rn((double)__fsub_rn(r, cut_level), (double)a.land_range);
-    const float g = __ldcg(a.ground + cell);
+// fields (HydraulicErosion.kt:2035-2050, 2084-2097). r, g and prior are relative[cell], ground[cell]
+// and surface[cell] as read before this basin's cut (each cell is cut at most once per basin).
+__device__ __forceinline__ int take(const BreachDev& a, int cell, float r, float g, float prior, float cut_level) {
+    const double amount = __dmul_rn((double)__fsub_rn(r, cut_level), (double)a.land_range);
     const bool ponded = __fsub_rn(g, r) > a.pond_depth;
-    const float prior = __ldcg(a.surface + cell);
-    const float now = (float)__dadd_rn((double)prior, -take);
+    const float now = (float)__dadd_rn((double)prior, -amount);
     __stcg(a.surface + cell, now);
     const double removed = -__dsub_rn((double)now, (double)prior);
     if (removed > 0.0) {
@@ -172,66 +181,203 @@ __device__ __forceinline__ int take_down_to(const BreachDev& a, int cell, float 
     return 0;
 }
 
-// One basin's notch (HydraulicErosion.kt:1958-2100) over its footprint list. Returns the cells cut.
-__device__ int cut_basin(const BreachDev& a, int b) {
+__device__ __forceinline__ int take_down_to(const BreachDev& a, int cell, float r, float cut_level) {
+    return take(a, cell, r, __ldcg(a.ground + cell), __ldcg(a.surface + cell), cut_level);
+}
+
+// walk 1's outcome, shared by both cutters: the new level of the lip, or false where the basin cuts
+// nothing (HydraulicErosion.kt:2001-2027).
+__device__ __forceinline__ bool new_level_of(const BreachDev& a, int spill, float level, float depth, float fall,
+                                             float length, float last_step, int walked, int cell, float* out) {
+    if (fall <= __fmul_rn(1e-6f, (float)walked) && cell >= 0 && !a.land[cell]) {
+        fall = __fsub_rn(level, __ldcg(a.rel + cell));   // water: no basin cuts it
+        length = __fadd_rn(length, last_step);
+    }
+    if (walked == 0) return false;
+    float slope = __fmul_rn(__fdiv_rn(fall, length), (float)a.W);
+    if (slope < 0.0f) slope = 0.0f;
+    const float power = __fmul_rn(__fmul_rn(a.coefficient, __fsqrt_rn(__fdiv_rn(a.area[spill], a.land_cells))), slope);
+    const float drop = jvm_min(power, jvm_min(depth, level));
+    if (drop <= 0.0f) return false;
+    *out = __fsub_rn(level, drop);
+    return true;
+}
+
+__device__ __forceinline__ unsigned long long claim_key(int wave, int b) {
+    return ((unsigned long long)wave << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)b);
+}
+
+// A short basin's footprint cells, all loads in flight at once.
+__device__ __forceinline__ int short_cells(const BreachDev& a, int b, int (&c)[SHORT]) {
+    const int s0 = a.start[b];
+    const int n = a.start[b + 1] - s0;
+#pragma unroll
+    for (int k = 0; k < SHORT; ++k) c[k] = k < n ? a.foot[s0 + k] : 0;
+    return n;
+}
+
+// One short basin's notch by one thread (HydraulicErosion.kt:1958-2100): the footprint's heights
+// are read up front, then the walks run in registers. Returns the cells cut.
+__device__ int cut_short(const BreachDev& a, int b, const int (&c)[SHORT], int n) {
+    const int n1 = a.n1[b];
+    int nx[SHORT];
+    float r[SHORT], g[SHORT], su[SHORT];
+#pragma unroll
+    for (int k = 0; k < SHORT; ++k) {
+        if (k < n) {
+            r[k] = __ldcg(a.rel + c[k]);
+            g[k] = __ldcg(a.ground + c[k]);
+            su[k] = __ldcg(a.surface + c[k]);
+            nx[k] = a.recv[c[k]];
+        } else {
+            r[k] = g[k] = su[k] = 0.0f;
+            nx[k] = -1;
+        }
+    }
+    const float level = a.level[b];
+    const float depth = __fsub_rn(level, a.floor_[b]);
+    // Walk 1: the channel's fall and length.
+    float fall = 0.0f, length = 0.0f, last_step = 1.0f;
+    int walked = 0, cell = -1;
+    bool going = true;
+#pragma unroll
+    for (int k = 0; k < SHORT; ++k) {
+        if (going && k < n1) {
+            fall = __fsub_rn(level, r[k]);
+            if (fall > depth) {
+                going = false;
+                cell = c[k];
+            } else {
+                last_step = walk_step(a, c[k], nx[k]);
+                length = __fadd_rn(length, last_step);
+                ++walked;
+                cell = nx[k];   // where the walk goes next, or left the land, or ran out of reach
+            }
+        }
+    }
+    float new_level;
+    if (!new_level_of(a, c[0], level, depth, fall, length, last_step, walked, cell, &new_level)) return 0;
+    int cut = 0;
+    // Walk 2: down the channel, falling `gradient` a cell width, never below the shoreline.
+    float from_lip = 0.0f;
+    going = true;
+#pragma unroll
+    for (int k = 0; k < SHORT; ++k) {
+        if (going && k < n1) {
+            const float falling = __fsub_rn(new_level, __fmul_rn(from_lip, a.gradient));
+            const float cut_level = falling < 0.0f ? 0.0f : falling;
+            if (r[k] <= cut_level) {
+                going = false;
+            } else {
+                cut += take(a, c[k], r[k], g[k], su[k], cut_level);
+                from_lip = __fadd_rn(from_lip, walk_step(a, c[k], nx[k]));
+            }
+        }
+    }
+    // Back across the margin from the lip (margin cell k drains into k + 1, the last into the lip).
+    float back = 0.0f;
+    going = true;
+#pragma unroll
+    for (int k = SHORT - 1; k >= 0; --k) {
+        if (going && k < n && k >= n1) {
+            back = __fadd_rn(back, ground_step(a, c[k], nx[k]));
+            const float cut_level = __fadd_rn(new_level, __fmul_rn(back, a.gradient));
+            if (r[k] <= cut_level) going = false;
+            else cut += take(a, c[k], r[k], g[k], su[k], cut_level);
+        }
+    }
+    return cut;
+}
+
+// One long basin's notch by a whole warp (every lane calls it; all control flow is warp-uniform). The
+// same walks as cut_short: walk 1 stops at the first cell whose fall exceeds the basin's depth, so a
+// ballot finds it in each chunk of 32, and its length is the steps before it summed in order; walk 2
+// and the margin stop at the first cell already at or below its cut level, which needs each lane's
+// own running sum of steps (the reference's float additions, in its order) before the ballot. Returns
+// this lane's count of cut cells.
+__device__ int cut_long(const BreachDev& a, int b, int lane) {
     const int* list = a.foot + a.start[b];
     const int n1 = a.n1[b];
     const int n = a.n[b];
     const int spill = list[0];
     const float level = a.level[b];
     const float depth = __fsub_rn(level, a.floor_[b]);
-    // Walk 1: the channel's fall and length.
     float fall = 0.0f, length = 0.0f, last_step = 1.0f;
     int walked = 0;
-    int cell = spill;
-    bool stopped = false;
-    for (int i = 0; i < n1; ++i) {
-        cell = list[i];
-        fall = __fsub_rn(level, __ldcg(a.rel + cell));
-        if (fall > depth) {
-            stopped = true;
+    int cell = -1;
+    for (int k0 = 0; k0 < n1; k0 += 32) {
+        const int j = k0 + lane;
+        const bool valid = j < n1;
+        int c = 0, next = -1;
+        float f = 0.0f, step = 0.0f;
+        if (valid) {
+            c = list[j];
+            f = __fsub_rn(level, __ldcg(a.rel + c));
+            next = a.recv[c];
+            step = walk_step(a, c, next);
+        }
+        const unsigned stop = __ballot_sync(FULL, valid && f > depth);
+        const int m = stop ? __ffs(stop) - 1 : min(32, n1 - k0);   // cells walked in this chunk
+        for (int t = 0; t < m; ++t) length = __fadd_rn(length, __shfl_sync(FULL, step, t));
+        if (m > 0) last_step = __shfl_sync(FULL, step, m - 1);
+        walked += m;
+        if (stop) {
+            fall = __shfl_sync(FULL, f, m);
+            cell = __shfl_sync(FULL, c, m);
             break;
         }
-        last_step = walk_step(a, cell, a.recv[cell]);
-        length = __fadd_rn(length, last_step);
-        ++walked;
+        fall = __shfl_sync(FULL, f, m - 1);
+        cell = __shfl_sync(FULL, next, m - 1);   // where the walk left the land or ran out of reach
     }
-    if (!stopped) cell = a.recv[list[n1 - 1]];   // where the walk left the land or ran out of reach
-    // A sill level to the water measures the step into it (FlowRouting.FLAT_GRADIENT_STEP, 1e-6).
-    if (fall <= __fmul_rn(1e-6f, (float)walked) && cell >= 0 && !a.land[cell]) {
-        fall = __fsub_rn(level, __ldcg(a.rel + cell));   // water: no basin cuts it
-        length = __fadd_rn(length, last_step);
-    }
-    if (walked == 0) return 0;
-    float slope = __fmul_rn(__fdiv_rn(fall, length), (float)a.W);
-    if (slope < 0.0f) slope = 0.0f;
-    const float power = __fmul_rn(__fmul_rn(a.coefficient, __fsqrt_rn(__fdiv_rn(a.area[spill], a.land_cells))), slope);
-    const float drop = jvm_min(power, jvm_min(depth, level));
-    if (drop <= 0.0f) return 0;
-    const float new_level = __fsub_rn(level, drop);
+    float new_level;
+    if (!new_level_of(a, spill, level, depth, fall, length, last_step, walked, cell, &new_level)) return 0;
     int cut = 0;
-    // Walk 2: down the channel, falling `gradient` a cell width, never below the shoreline.
-    float from_lip = 0.0f;
-    for (int i = 0; i < n1; ++i) {
-        cell = list[i];
+    float base = 0.0f;
+    for (int k0 = 0; k0 < n1; k0 += 32) {
+        const int j = k0 + lane;
+        const bool valid = j < n1;
+        int c = 0;
+        float r = 0.0f, step = 0.0f;
+        if (valid) {
+            c = list[j];
+            r = __ldcg(a.rel + c);
+            step = walk_step(a, c, a.recv[c]);
+        }
+        float from_lip = base;
+        for (int t = 0; t < 31; ++t) {
+            const float v = __shfl_sync(FULL, step, t);
+            if (t < lane) from_lip = __fadd_rn(from_lip, v);
+        }
         const float falling = __fsub_rn(new_level, __fmul_rn(from_lip, a.gradient));
         const float cut_level = falling < 0.0f ? 0.0f : falling;
-        const float r = __ldcg(a.rel + cell);
-        if (r <= cut_level) break;
-        cut += take_down_to(a, cell, r, cut_level);
-        from_lip = __fadd_rn(from_lip, walk_step(a, cell, a.recv[cell]));
+        const unsigned stop = __ballot_sync(FULL, valid && r <= cut_level);
+        const int m = stop ? __ffs(stop) - 1 : 32;
+        if (valid && lane < m) cut += take_down_to(a, c, r, cut_level);
+        if (stop) break;
+        base = __shfl_sync(FULL, __fadd_rn(from_lip, step), 31);
     }
-    // Back across the margin from the lip, rising by the same gradient.
     float back = 0.0f;
-    int downstream = spill;
-    for (int i = n - 1; i >= n1; --i) {
-        const int m = list[i];
-        back = __fadd_rn(back, ground_step(a, m, downstream));
-        const float cut_level = __fadd_rn(new_level, __fmul_rn(back, a.gradient));
-        const float r = __ldcg(a.rel + m);
-        if (r <= cut_level) break;
-        cut += take_down_to(a, m, r, cut_level);
-        downstream = m;
+    for (int top = n - 1; top >= n1; top -= 32) {
+        const int i = top - lane;
+        const bool valid = i >= n1;
+        int c = 0;
+        float r = 0.0f, step = 0.0f;
+        if (valid) {
+            c = list[i];
+            r = __ldcg(a.rel + c);
+            step = ground_step(a, c, a.recv[c]);
+        }
+        float acc = back;
+        for (int t = 0; t < 32; ++t) {
+            const float v = __shfl_sync(FULL, step, t);
+            if (t <= lane) acc = __fadd_rn(acc, v);
+        }
+        const float cut_level = __fadd_rn(new_level, __fmul_rn(acc, a.gradient));
+        const unsigned stop = __ballot_sync(FULL, valid && r <= cut_level);
+        const int m = stop ? __ffs(stop) - 1 : 32;
+        if (valid && lane < m) cut += take_down_to(a, c, r, cut_level);
+        if (stop) break;
+        back = __shfl_sync(FULL, acc, 31);
     }
     return cut;
 }
@@ -239,44 +385,73 @@ __device__ int cut_basin(const BreachDev& a, int b) {
 __global__ void __launch_bounds__(256) k_breach_waves(BreachDev a) {
     cgr::grid_group grid = cgr::this_grid();
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    const bool first = blockIdx.x == 0 && threadIdx.x == 0;
+    const int thread = blockIdx.x * blockDim.x + threadIdx.x;
+    const int threads = gridDim.x * blockDim.x;
+    const int warp = thread >> 5;
+    const int warps = threads >> 5;
+    const bool first = thread == 0;
     int cells = 0;
     int cur = 0;
     int wave = 1;
     for (;; ++wave) {
-        const int pending = __ldcg(a.q + Q_PENDING0 + cur);
-        if (pending == 0) break;
+        const int shorts = __ldcg(a.q + Q_SHORT0 + cur);
+        const int longs = __ldcg(a.q + Q_LONG0 + cur);
+        if (shorts + longs == 0) break;
         if (wave > a.count + 1) {   // the lowest waiting basin cuts in every wave: cannot happen
             if (first) a.q[Q_ERROR] = 1;
             break;
         }
-        const int* list = a.queue + (size_t)cur * a.count;
-        int* next_list = a.queue + (size_t)(cur ^ 1) * a.count;
-        const unsigned long long hi = (unsigned long long)wave << 32;
-        for (int i = warp; i < pending; i += warps) {
-            const int b = __ldcg(list + i);
-            const unsigned long long key = hi | (unsigned long long)(0xFFFFFFFFu - (unsigned)b);
+        const int* short_list = a.queue + (size_t)cur * a.count;
+        const int* long_list = a.queue + (size_t)(2 + cur) * a.count;
+        int* next_short = a.queue + (size_t)(cur ^ 1) * a.count;
+        int* next_long = a.queue + (size_t)(2 + (cur ^ 1)) * a.count;
+        int* next_shorts = a.q + Q_SHORT0 + (cur ^ 1);
+        int* next_longs = a.q + Q_LONG0 + (cur ^ 1);
+        // Claims. The atomics need no answer, so they do not wait.
+        for (int i = warp; i < longs; i += warps) {
+            const int b = __ldcg(long_list + i);
+            const unsigned long long key = claim_key(wave, b);
             for (int j = a.start[b] + lane; j < a.start[b + 1]; j += 32) atomicMax(a.claim + a.foot[j], key);
         }
-        if (first) a.q[Q_PENDING0 + (cur ^ 1)] = 0;
+        for (int i = thread; i < shorts; i += threads) {
+            const int b = __ldcg(short_list + i);
+            const unsigned long long key = claim_key(wave, b);
+            int c[SHORT];
+            const int n = short_cells(a, b, c);
+#pragma unroll
+            for (int k = 0; k < SHORT; ++k)
+                if (k < n) atomicMax(a.claim + c[k], key);
+        }
+        if (first) {
+            *next_shorts = 0;
+            *next_longs = 0;
+        }
         grid.sync();
-        for (int i = warp; i < pending; i += warps) {
-            const int b = __ldcg(list + i);
-            const unsigned long long key = hi | (unsigned long long)(0xFFFFFFFFu - (unsigned)b);
+        // A basin holding every claim it placed cuts; the others wait for the next wave.
+        for (int i = warp; i < longs; i += warps) {
+            const int b = __ldcg(long_list + i);
+            const unsigned long long key = claim_key(wave, b);
             bool held = true;
             for (int j = a.start[b] + lane; j < a.start[b + 1]; j += 32) held &= __ldcg(a.claim + a.foot[j]) == key;
-            held = __all_sync(FULL, held);
-            if (lane == 0) {
-                if (held) cells += cut_basin(a, b);
-                else __stcg(next_list + atomicAdd(a.q + Q_PENDING0 + (cur ^ 1), 1), b);
-            }
+            if (__all_sync(FULL, held)) cells += cut_long(a, b, lane);
+            else if (lane == 0) __stcg(next_long + atomicAdd(next_longs, 1), b);
+        }
+        for (int i = thread; i < shorts; i += threads) {
+            const int b = __ldcg(short_list + i);
+            const unsigned long long key = claim_key(wave, b);
+            int c[SHORT];
+            const int n = short_cells(a, b, c);
+            bool held = true;
+#pragma unroll
+            for (int k = 0; k < SHORT; ++k)
+                if (k < n) held &= __ldcg(a.claim + c[k]) == key;
+            if (held) cells += cut_short(a, b, c, n);
+            else __stcg(next_short + atomicAdd(next_shorts, 1), b);
         }
         grid.sync();
         cur ^= 1;
     }
-    if (lane == 0 && cells) atomicAdd(a.q + Q_CELLS, cells);
+    if (cells) atomicAdd(a.q + Q_CELLS, cells);
     if (first) a.q[Q_WAVES] = wave - 1;
 }
 
@@ -294,8 +469,8 @@ cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_
     cg_status st = basins_dev(ctx, W, H, d_land, d_rel, d_ground, d_recv, rates.pond_depth, d_label, &bas, &count);
     if (st != CG_OK) return st;
     if (count == 0) return CG_OK;
-    // n (count + 1) | start (count + 1) | n1 (count) | two queues (2 count) | control words.
-    CG_BUF(int, d_block, ctx, S_BREACH, 5 * (size_t)count + 2 + Q_WORDS);
+    // n (count + 1) | start (count + 1) | n1 (count) | four queues (4 count) | control words.
+    CG_BUF(int, d_block, ctx, S_BREACH, 7 * (size_t)count + 2 + Q_WORDS);
     BreachDev a;
     a.W = W;
     a.count = count;
@@ -322,7 +497,7 @@ cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_
     a.start = a.n + count + 1;
     a.n1 = a.start + count + 1;
     a.queue = a.n1 + count;
-    a.q = a.queue + 2 * (size_t)count;
+    a.q = a.queue + 4 * (size_t)count;
     a.foot = nullptr;
     a.claim = nullptr;
     const int blocks = (count + 1 + 255) / 256;
@@ -344,6 +519,7 @@ cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_breach_waves, 256, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "breach kernel cannot be resident");
+    // Up to two CTAs per SM: the first waves hold most of the basins, a thread each.
     const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
     void* kargs[] = {&a};
     ctx->launches++;

@@ -186,6 +186,50 @@ def test_breach_cuts_only_down_from_its_lips():
     assert set(changed.tolist()) <= allowed
 
 
+def long_margin_case(W=2048, H=1024, seed=7):
+    """The shelved basin again, stretched so that one notch cuts a long channel margin: a 30 m deep
+    core behind a margin shelving gently from 1 m to 1.5 m below the lip over 46 columns, drained
+    through a lip at column 24 and a channel falling 2 m a cell to the sea. Its margin walk from the
+    entry to the lip is longer than a warp's 32 cells."""
+    row = np.arange(H)[:, None].repeat(W, 1)
+    col = np.arange(W)[None, :].repeat(H, 0)
+    land = (col >= 4).astype(np.uint8)
+    lip_r, lip_c, margin_last, core_last = H // 2, 24, 70, 120
+    m = (f32(900) + col.astype(f32)).astype(f32)
+    basin = np.abs(row - lip_r) <= 14
+    m = np.where(basin & (col >= 25) & (col <= margin_last),
+                 f32(599) - f32(0.5) * (col - 25).astype(f32) / f32(margin_last - 25), m)
+    m = np.where(basin & (col > margin_last) & (col <= core_last), f32(570), m)
+    m = np.where((row == lip_r) & (col < lip_c), f32(600) - f32(2) * (lip_c - col).astype(f32), m)
+    m = np.where((row == lip_r) & (col == lip_c), f32(600), m)
+    rel = (np.where(land == 0, f32(-600), m).astype(f32) / f32(6000)).astype(f32)
+    filled = oracle.fill_depressions(land, rel)
+    flow, _ = oracle.flow_directions(land, rel, filled, seed, 0.5 * W / H, LATTICE)
+    area = oracle.accumulate(land, flow, int(land.sum()), np.ones((H, W), np.float32))
+    land_half = f32(f32(6000) / f32(16000))
+    surface = (f32(f32(10000) / f32(16000)) + rel * land_half).astype(np.float32)
+    return dict(params=oracle.default_params(W, H, seed), land=land, relative=rel, filled=filled, flow=flow,
+                area=area, land_cells=float(land.sum()), land_half=float(land_half), surface=surface)
+
+
+def test_long_margin_case_poses_the_question():
+    """One basin, its entry far up the margin (more than 32 cells of margin walk to the lip, within the
+    reach), and a notch that cuts more cells than one warp's chunk."""
+    c = long_margin_case()
+    pond = oracle.rates(c["params"])[2]
+    sw = oracle.spillways(c["land"], c["relative"], c["filled"], c["flow"], pond)
+    assert sw["count"] == 1
+    flow = c["flow"].ravel()
+    cell, steps = sw["entry"][0], 0
+    while cell >= 0 and cell != sw["spill"][0]:
+        cell, steps = flow[cell], steps + 1
+    assert cell == sw["spill"][0] and 32 < steps <= oracle.outlet_rates(c["params"])[2]
+    rel, fil, sur = c["relative"].copy(), c["filled"].copy(), c["surface"].copy()
+    cells, _ = oracle.breach(c["params"], c["land"], rel, fil, c["flow"], c["area"], c["land_cells"],
+                             c["land_half"], sur)
+    assert cells > 64
+
+
 def test_p1_stage_adds_the_notch():
     """Profile P1 runs the notch in every round and the closing breach: it differs from P0, and its
     routing outputs are the closing pass's, a valid drainage of the final field's own cut."""
@@ -214,6 +258,22 @@ def test_gpu_breach_shelf_matches_oracle():
     got = [c["relative"].copy(), c["filled"].copy(), c["surface"].copy()]
     cells = HydraulicErosion.breach(ErosionConfig(SHELF_GRID, SHELF_GRID, 7), c["land"], got[0], got[1], c["flow"],
                                     c["area"], c["land_cells"], c["land_half"], got[2])
+    assert cells == cells_want
+    for g, w in zip(got, want):
+        assert np.array_equal(bits(g), bits(w))
+
+
+@pytest.mark.gpu
+def test_gpu_breach_long_margin_matches_oracle():
+    """A notch whose margin spans several warp chunks (the warp-parallel cut)."""
+    from cartogenesis_gb300 import ErosionConfig, HydraulicErosion
+    c = long_margin_case()
+    want = [c["relative"].copy(), c["filled"].copy(), c["surface"].copy()]
+    cells_want, _ = oracle.breach(c["params"], c["land"], *want[:2], c["flow"], c["area"], c["land_cells"],
+                                  c["land_half"], want[2])
+    got = [c["relative"].copy(), c["filled"].copy(), c["surface"].copy()]
+    cells = HydraulicErosion.breach(ErosionConfig(2048, 1024, 7), c["land"], got[0], got[1], c["flow"], c["area"],
+                                    c["land_cells"], c["land_half"], got[2])
     assert cells == cells_want
     for g, w in zip(got, want):
         assert np.array_equal(bits(g), bits(w))
