@@ -323,3 +323,18 @@ def test_gpu_stage_p1_2048x1024_with_weather():
     assert np.array_equal(got.receivers, want["receivers"])
     for k in ("area", "filled", "relative"):
         assert np.array_equal(bits(getattr(got, k)), bits(want[k])), k
+
+
+@pytest.mark.gpu
+def test_gpu_stage_p1_bench_world_8192x4096():
+    """The benchmark workload with the outlet notch: 8192 x 4096 cells, 12 rounds and the closing
+    breach, every routing output of the closing pass bit for bit (the oracle takes a few minutes)."""
+    from cartogenesis_gb300 import ErosionConfig, ErosionStage
+    from test_gpu_stage import compare
+    W, H, seed = 8192, 4096, 1
+    h, up, rk = synthetic.world(W, H, seed, uplift="ridges")
+    keys = ("receivers", "area", "filled", "relative", "is_land", "basin_of_cell", "donors")
+    got = ErosionStage.apply(ErosionConfig(W, H, seed, sea_level=0.70, profile=1), h, up, rk, want=keys)
+    want = oracle.erode_stage(oracle.default_params(W, H, seed, sea_level=0.70, profile=1), h, up, rk, want=keys)
+    compare(got, want, order=False)
+
