@@ -116,6 +116,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, world):
+    """Each timing's maximum over the ranks (the slowest replica decides the whole job's time)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(cells, steps, world, seconds):
+    """Mcell-rounds/s of the whole job: every rank's world, every round of every step."""
+    return float(cells) * ROUNDS * steps * world / seconds / 1e6
+
+
 def world_inputs(W, H, seed):
     from cartogenesis_gb300 import synthetic
     return synthetic.world(W, H, seed, uplift="ridges")
@@ -273,14 +288,9 @@ def run_ours(args):
     barrier()
     t_e2e = time.perf_counter() - t0
 
-    times = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    t_dev, t_e2e = times.tolist()
-    cell_rounds = float(N) * ROUNDS * args.steps * world
-    value = cell_rounds / t_dev / 1e6
-    e2e = cell_rounds / t_e2e / 1e6
+    t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], world)
+    value = whole_job_rate(N, args.steps, world, t_dev)
+    e2e = whole_job_rate(N, args.steps, world, t_e2e)
 
     # Roofline of the dominant kernel, the fused thermal sweeps. Their algorithmic traffic is a read
     # and a write of the height field per sweep (8 B per cell-sweep); with two sweeps fused per
