@@ -112,6 +112,15 @@ class RoundStats(C.Structure):
     ]
 
 
+class World(C.Structure):
+    """cg_world: one world of a batch."""
+    _fields_ = [
+        ("params", ErosionParams),
+        ("inputs", Inputs),
+        ("outputs", Outputs),
+    ]
+
+
 def ptr(a):
     """Address of a numpy array's data, or None."""
     return None if a is None else a.ctypes.data

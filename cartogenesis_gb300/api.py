@@ -144,6 +144,31 @@ class ErosionStage:
         return ErosionResult(**outs)
 
 
+    @staticmethod
+    def apply_batch(worlds, ctx=None):
+        """Many worlds in one call (cg_erode_batch): `worlds` is a list of (config, height, uplift, rock)
+        tuples (uplift and rock may be None), grids of any shapes. Returns one height array per world,
+        each exactly what ErosionStage.apply gives for that world alone."""
+        ctx = ctx or default_context()
+        keep, descs, outs = [], (abi.World * len(worlds))(), []
+        for i, (config, height, uplift, rock) in enumerate(worlds):
+            H, W = config.params.height, config.params.width
+            arrays = [_f32(a, (H, W)) for a in (height, uplift, rock)]
+            out = np.empty((H, W), np.float32)
+            keep.append(arrays)
+            outs.append(out)
+            descs[i].params = config.params
+            descs[i].inputs = abi.Inputs(*[P(a) for a in arrays], None, None)
+            descs[i].outputs = abi.Outputs(height=P(out))
+        status = (C.c_int32 * max(len(worlds), 1))()
+        with ctx.lock:
+            st = ctx.lib.cg_erode_batch(ctx.handle, len(worlds), descs, C.cast(status, C.c_void_p))
+            if st != abi.CG_OK:
+                bad = [i for i in range(len(worlds)) if status[i] != abi.CG_OK]
+                raise CgError(st, f"worlds {bad} failed: " + ctx.lib.cg_last_error(ctx.handle).decode(errors="replace"))
+        return outs
+
+
 class SeaLevelStage:
     @staticmethod
     def percentile_cut(height, sea_level_fraction, lowstand_share_of_field=0.0, highest_land_metres=6000.0,

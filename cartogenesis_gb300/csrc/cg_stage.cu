@@ -315,10 +315,11 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
 
 using namespace cg;
 
-extern "C" {
+namespace {
 
-cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
-                         cg_round_stats* stats) {
+// cg_erode_stage without clearing the cancel flag (a batch clears it once for all its worlds).
+cg_status erode_stage_host(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
+                           cg_round_stats* stats) {
     if (!ctx || !p || !in || !out || !in->height || !out->height) return CG_BAD_ARG;
     if (p->abi_version != CG_ABI_VERSION)
         return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
@@ -328,7 +329,6 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_input
     if (p->profile != CG_PROFILE_P0 && p->profile != CG_PROFILE_P1)
         return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 and P1 only)", p->profile);
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
-    ctx->cancel.store(0);
     const int W = p->width, H = p->height;
     const size_t N = (size_t)W * H;
     CG_BUF(float, d_h, ctx, S_H0, N);
@@ -391,6 +391,38 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_input
         }
     }
     return sync(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
+                         cg_round_stats* stats) {
+    if (!ctx) return CG_BAD_ARG;
+    ctx->cancel.store(0);
+    return erode_stage_host(ctx, p, in, out, stats);
+}
+
+cg_status cg_erode_batch(cg_ctx* ctx, int32_t n_worlds, const cg_world* worlds, cg_status* status) {
+    if (!ctx || n_worlds < 0 || (n_worlds > 0 && !worlds)) return CG_BAD_ARG;
+    ctx->cancel.store(0);
+    cg_status first = CG_OK;
+    for (int32_t i = 0; i < n_worlds; ++i) {
+        cg_status st = cancelled(ctx);
+        if (st == CG_OK) {
+            cg_outputs out = worlds[i].outputs;
+            st = erode_stage_host(ctx, &worlds[i].params, &worlds[i].inputs, &out, nullptr);
+        }
+        if (status) status[i] = st;
+        if (st != CG_OK && first == CG_OK) first = st;
+        if (st == CG_CANCELLED) {
+            for (int32_t j = i + 1; j < n_worlds; ++j)
+                if (status) status[j] = CG_CANCELLED;
+            break;
+        }
+    }
+    return first;
 }
 
 cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, float* out_dev,

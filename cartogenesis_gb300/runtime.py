@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libcg_erosion.so")
 EXPORTS = [
     "cg_default_params", "cg_thermal_limits_for", "cg_create", "cg_destroy", "cg_cancel", "cg_last_error",
     "cg_stream", "cg_kernel_launches",
-    "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
+    "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_erode_batch", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
 ]
 
@@ -64,6 +64,7 @@ def load_library(path=LIB_PATH):
             L.cg_drainage_order.argtypes = [vp, i32, i32, vp, vp, i32, vp]
             L.cg_accumulate.argtypes = [vp, i32, i32, vp, vp, i32, vp, vp]
             L.cg_spillways.argtypes = [vp, i32, i32, vp, vp, vp, vp, f32, vp, C.POINTER(abi.Basins)]
+            L.cg_erode_batch.argtypes = [vp, i32, C.POINTER(abi.World), vp]
             L.cg_breach.argtypes = [vp, PP, vp, vp, vp, vp, vp, f32, f32, vp, C.POINTER(i32)]
         _lib = L
         return _lib

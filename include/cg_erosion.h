@@ -227,6 +227,23 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* params, const cg_
 cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs_dev,
                              float* height_out_dev, cg_round_stats* stats, int32_t* land_cells);
 
+/* One world of a batch: its own grid, seed and scale, host inputs and host outputs. */
+typedef struct cg_world {
+    cg_erosion_params params;
+    cg_inputs inputs;
+    cg_outputs outputs;     /* outputs.height required */
+} cg_world;
+
+/*
+ * Many worlds in one call (seeds and planet sizes of different grid shapes): each world's result is
+ * exactly cg_erode_stage's on that world. The worlds run one after another on this context's device,
+ * reusing its buffers (grown to the largest world). `status` (may be NULL, n_worlds entries) receives each
+ * world's cg_status. Returns CG_OK if every world succeeded, else the first failure's status; a
+ * failed world does not stop the others, except CG_CANCELLED, which stops the batch (the worlds not
+ * run get CG_CANCELLED). No counterpart in the reference, which generates one world at a time.
+ */
+cg_status cg_erode_batch(cg_ctx* ctx, int32_t n_worlds, const cg_world* worlds, cg_status* status);
+
 /* ---- The stage's routing functions, each run alone on host buffers (FlowRouting, SeaLevelStage) ---- */
 
 /* SeaLevelStage.percentileCut (.../pipeline/SeaLevelStage.kt:146-200, 579-651). */

@@ -42,7 +42,8 @@ def test_ctypes_structs_match_the_header():
 #define S(T) printf(#T " %zu\n", sizeof(T));
 #define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
 int main(void) {
-  S(cg_erosion_params) S(cg_inputs) S(cg_outputs) S(cg_basins) S(cg_round_stats) S(cg_thermal_limits)
+  S(cg_erosion_params) S(cg_inputs) S(cg_outputs) S(cg_basins) S(cg_round_stats) S(cg_thermal_limits) S(cg_world)
+  O(cg_world, inputs) O(cg_world, outputs)
   O(cg_erosion_params, seed) O(cg_erosion_params, world_width_km) O(cg_erosion_params, years_per_hydraulic_round)
   O(cg_erosion_params, debris_travel_km) O(cg_erosion_params, sea_level) O(cg_erosion_params, profile)
   O(cg_outputs, basins) O(cg_basins, largest) O(cg_round_stats, fill_ties) O(cg_round_stats, ms_total) O(cg_round_stats, ms_relax)
@@ -56,7 +57,8 @@ int main(void) {
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
     got = dict(line.rsplit(" ", 1) for line in out if line)
     types = {"cg_erosion_params": abi.ErosionParams, "cg_inputs": abi.Inputs, "cg_outputs": abi.Outputs,
-             "cg_basins": abi.Basins, "cg_round_stats": abi.RoundStats, "cg_thermal_limits": abi.ThermalLimits}
+             "cg_basins": abi.Basins, "cg_round_stats": abi.RoundStats, "cg_thermal_limits": abi.ThermalLimits,
+             "cg_world": abi.World}
     for k, v in got.items():
         if "." in k:
             t, f = k.split(".")
