@@ -495,12 +495,10 @@ cg_status percentile_cut_dev(cg_ctx* ctx, int W, int H, const float* d_h, float 
     CG_CUDA(ctx, cudaStreamSynchronize(sm));
     if (!hs.degenerate && hs.count > 1) {
         if (hs.count <= SMALL_SORT) {
-            static bool configured = false;
-            if (!configured) {
-                CG_CUDA(ctx, cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)(SMALL_SORT * sizeof(long long))));
-                configured = true;
-            }
+            // Set on every call (it is cheap): a flag kept across calls would be shared by every
+            // context and device of the process.
+            CG_CUDA(ctx, cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)(SMALL_SORT * sizeof(long long))));
             int P2 = 1;
             while (P2 < hs.count) P2 <<= 1;
             CG_LAUNCH(ctx) k_sort_small<<<1, 1024, P2 * sizeof(long long), sm>>>(d_keys, d_s);

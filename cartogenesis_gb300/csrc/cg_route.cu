@@ -1564,7 +1564,12 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
                 const size_t bytes = std::max((size_t)cap * SM_BYTES_PER_MEMBER, (size_t)116 * 1024);
                 const bool unit = a.ew == 1.0 && a.ns == 1.0 && a.diag == 1.0;
                 auto kernel = unit ? k_flat_solve_cl<true> : k_flat_solve_cl<false>;
-                CG_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+                // The attribute is the kernel's, shared by every context of the process: set it to the
+                // most any launch asks for, so that a context on another thread lowering it between this
+                // call and the launch below cannot make the launch fail.
+                const size_t most = std::max((size_t)std::min(CL_RANGE_MAX, CL_SMEM_MEMBERS) * SM_BYTES_PER_MEMBER,
+                                             (size_t)116 * 1024);
+                CG_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
                 CG_LAUNCH(ctx) kernel<<<ctr[1] * CL, CL_THREADS, bytes, sm>>>(a, d_lists + flats, cap,
                                                                               d_lists + 2 * (size_t)flats, d_ctr + 2);
                 CG_CHECK_LAUNCH(ctx);
