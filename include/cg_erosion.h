@@ -51,7 +51,8 @@ typedef enum cg_mode { CG_MODE_REF32 = 0 } cg_mode;
  * and relaxation (climateFeed, deposition, outletIncision, flexure and the belt replay off).
  * P1: P0 with ErosionConfig.outletIncision: each round's notch before the incision and the closing
  * breach before the last relaxation (HydraulicErosion.kt:1002-1028, 1404-1442); the routing outputs
- * are then the closing pass's, as its notch left them. P2 (deposition) is not built.
+ * are then the closing pass's, as its notch left them. P0 and P1 have ErosionConfig.deltaLobe off
+ * (the closing mouths pass belongs to P2). P2 (deposition) is not built on the device.
  */
 typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2 } cg_profile;
 

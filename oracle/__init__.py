@@ -57,6 +57,9 @@ def lib():
         L.or_breach.argtypes = [C.POINTER(abi.ErosionParams), vp, vp, vp, vp, vp, f32, f32, vp, C.POINTER(f64)]
         L.or_breach.restype = i32
         L.or_outlet_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(i32)]
+        L.or_erode_stage_switched.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
+                                              C.POINTER(abi.Outputs), vp, vp, i32]
+        L.or_erode_stage_switched.restype = i32
         L.or_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)]
         L.or_stand_below_today.argtypes = [C.POINTER(abi.ErosionParams), i32]
         L.or_stand_below_today.restype = f32
@@ -215,6 +218,39 @@ def breach(params, is_land, relative, ground, directions, area, land_cells, land
     cells = lib().or_breach(C.byref(params), P(il), P(relative), P(ground), P(rec), P(ar), land_cells, land_range,
                             P(surface), C.byref(moved))
     return cells, moved.value
+
+
+class Switches(C.Structure):
+    """or_switches: the round tail's switches and the deposition's knobs, reference defaults."""
+    _fields_ = [("outlet_incision", C.c_int32), ("deposition", C.c_int32), ("delta_lobe", C.c_int32),
+                ("graded_aggradation", C.c_int32), ("transport_capacity", C.c_float),
+                ("deposition_rate", C.c_float), ("delta_share", C.c_float), ("lake_share", C.c_float),
+                ("delta_min_catchment_km2", C.c_double), ("delta_reach_km", C.c_double),
+                ("delta_freeboard_metres", C.c_float)]
+
+    def __init__(self, profile=2, **knobs):
+        on = profile >= 2
+        super().__init__(int(profile >= 1), int(on), int(on), int(on), 20.0, 0.06, 0.15, 0.1, 70000.0, 140.625,
+                         48.0)
+        for k, v in knobs.items():
+            setattr(self, k, v)
+
+
+def erode_stage_switched(params, height, uplift=None, rock=None, switches=None, thermal=True):
+    """The stage with explicit switches; returns (heights, tallies[rounds, 4]) where a tally is
+    (incised, deposited, lost, field drop) of one round."""
+    H, W = params.height, params.width
+    keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+            for a in (height, uplift, rock)]
+    inputs = abi.Inputs(*[P(a) if a is not None else None for a in keep], None, None)
+    out = np.empty((H, W), np.float32)
+    o = abi.Outputs(height=P(out))
+    tallies = np.zeros((max(params.hydraulic_rounds, 1), 4), np.float64)
+    sw = switches if switches is not None else Switches(params.profile)
+    st = lib().or_erode_stage_switched(C.byref(params), C.byref(inputs), C.byref(o), C.byref(sw), P(tallies),
+                                       int(thermal))
+    assert st == 0, st
+    return out, tallies
 
 
 def stand_below_today(params, round_):

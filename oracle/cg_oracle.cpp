@@ -22,6 +22,7 @@
 #include <cstring>
 #include <functional>
 #include <queue>
+#include <memory>
 #include <vector>
 
 #include "../include/cg_erosion.h"
@@ -964,7 +965,7 @@ inline float base_level(int r, const float* surface, const u8* is_land, const fl
 void incise(const Rates& rates, int W, size_t N, const int32_t* order, int order_len, const int32_t* directions,
             const u8* is_land, const float* ground, const float* relative, const float* discharge, float land_cells,
             float land_range, float shoreline, const float* erodibility, float* surface, bool only_above_base,
-            const float* unresolved) {
+            const float* unresolved, double* incised_at = nullptr) {
     std::vector<float> water(N, NAN);
     for (int rank = order_len - 1; rank >= 0; --rank) {
         int cell = order[rank];
@@ -991,7 +992,10 @@ void incise(const Rates& rates, int W, size_t N, const int32_t* order, int order
         float after;
         if (submerged || (height <= grades_to && only_above_base)) after = height;
         else after = (float)((double)grades_to + (double)(height - grades_to) / (1.0 + (double)courant));
-        if (after != height) surface[cell] = after;
+        if (after != height) {
+            surface[cell] = after;
+            if (incised_at && after < height) incised_at[cell] = (double)height - (double)after;
+        }
     }
 }
 
@@ -1016,11 +1020,12 @@ struct Breached {
 };
 
 // HydraulicErosion.breach (HydraulicErosion.kt:1931-2171) as the rounds and the closing pass run it:
-// belowSea false, no settled field and no load (nothing is carried in profile P1), and
+// belowSea false; `settled` and `load` given where sediment is carried (profile P2's rounds), and
 // ErosionConfig's outletIncisionRatio 1.125 and outletFallToTheWater on. Basins are taken in the
 // order spillways found them; `relative`, `ground` and `surface` are cut in place.
 Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_land, float* relative, float* ground,
-                const int32_t* dirs, const float* area, float land_cells, float land_range, float* surface) {
+                const int32_t* dirs, const float* area, float land_cells, float land_range, float* surface,
+                float* settled = nullptr, double* load = nullptr) {
     Breached out;
     const GroundSteps& steps = rates.steps;
     const float reach = (float)rates.outlet_reach_cells;   // Float < Int compares as floats
@@ -1033,6 +1038,8 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
             float as_relative = (float)(removed / (double)land_range);
             relative[cell] -= as_relative;
             if (!ponded) ground[cell] -= as_relative;
+            if (settled) settled[cell] -= as_relative;
+            if (load) load[cell] += removed;
             out.moved += removed;
             out.cells++;
         }
@@ -1115,6 +1122,548 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
     return out;
 }
 
+// ---------------------------------------------------------------- deposition (profile P2)
+
+// The switches the round tail reads (ErosionConfig, M:WorldGenConfig.kt:2068-2496) and the knobs of
+// the deposition beside them. A profile sets the switches; tests may change the knobs.
+struct Switches {
+    bool outlet_incision = false;     // ErosionConfig.outletIncision
+    bool deposition = false;          // ErosionConfig.deposition
+    bool delta_lobe = false;          // ErosionConfig.deltaLobe (the closing mouths pass runs on it)
+    bool graded_aggradation = false;  // ErosionConfig.gradedAggradation
+    float transport_capacity = 20.0f;        // ErosionConfig.transportCapacity
+    float deposition_rate = 0.06f;           // ErosionConfig.depositionRate
+    float delta_share = 0.15f;               // ErosionConfig.deltaShare
+    float lake_share = 0.1f;                 // ErosionConfig.lakeShare
+    double delta_min_catchment_km2 = 70000.0;   // ErosionConfig.deltaMinCatchmentKm2
+    double delta_reach_km = 140.625;         // ErosionConfig.deltaReachKm
+    float delta_freeboard_metres = 48.0f;    // ErosionConfig.deltaFreeboardMetres
+};
+
+// P0: the plain core; P1 adds the outlet notch; P2 adds deposition with the lobed, outlined and
+// graded deltas (deltaOutline is on in P2 and is the only outline restated here).
+Switches switches_of(const cg_erosion_params& p) {
+    Switches s;
+    s.outlet_incision = p.profile >= CG_PROFILE_P1;
+    s.deposition = s.delta_lobe = s.graded_aggradation = p.profile >= CG_PROFILE_P2;
+    return s;
+}
+
+const float kLobeRim = 0.15f;                       // HydraulicErosion.LOBE_RIM
+const float kDepthCost = 1.0f;                      // HydraulicErosion.DEPTH_COST
+const float kGrooveKeep = 0.45f;                    // HydraulicErosion.GROOVE_KEEP
+const float kLakeFanSlope = 1.5f;                   // HydraulicErosion.LAKE_FAN_SLOPE
+const float kDistributaryFallPerKm = 0.15f / 23.4375f;   // HydraulicErosion.DISTRIBUTARY_FALL_PER_KM
+const float kMinDistributaryFall = 1e-7f;           // HydraulicErosion.MIN_DISTRIBUTARY_FALL
+const int kMouthKeyRowStride = 0x2000;              // HydraulicErosion.MOUTH_KEY_ROW_STRIDE
+const double kDrawnRiverCatchmentKm2 = 70000.0 / 5; // HydraulicErosion.DRAWN_RIVER_CATCHMENT_KM2
+const float kShelfBreakMetres = 130.0f;             // HydraulicErosion.SHELF_BREAK_METRES
+
+// The deposition members of HydraulicErosion.Rates (HydraulicErosion.kt:285-300) and the stage's own
+// cell counts (HydraulicErosion.kt:639-640, 1673-1674).
+struct DepositionRates {
+    float delta_freeboard;
+    int delta_reach_cells;
+    float shelf_break;
+    float delta_min_cells;
+    float drawn_river_cells;
+    DepositionRates(const cg_erosion_params& p, const Switches& sw) {
+        Scale s = scale_of(p);
+        delta_freeboard = s.relief_share_of_metres(sw.delta_freeboard_metres);
+        delta_reach_cells = whole_cells_for(p, sw.delta_reach_km, 1);
+        shelf_break = s.field_share_of_metres(kShelfBreakMetres);
+        double km2 = s.cell_width_km(p.width) * s.cell_height_km(p.height);   // squareKilometresPerCell
+        delta_min_cells = (float)(sw.delta_min_catchment_km2 / km2);
+        drawn_river_cells = (float)(kDrawnRiverCatchmentKm2 / km2);
+    }
+};
+
+// Math.min(double, double) on the JVM.
+inline double jvm_min(double a, double b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    if (a == 0.0 && b == 0.0) return std::signbit(a) ? a : b;
+    return a < b ? a : b;
+}
+
+// HydraulicErosion.shortestX / DeltaFan.wrapDx: a column difference taken the short way round.
+inline int shortest_x(int dx, int W) {
+    if (dx > W / 2) return dx - W;
+    if (dx < -W / 2) return dx + W;
+    return dx;
+}
+
+// HydraulicErosion.wobble (HydraulicErosion.kt:1574-1581): Int arithmetic, wrapping.
+inline float cell_wobble(int cell) {
+    uint32_t bits = (uint32_t)cell * 0x9E3779B9u;
+    bits ^= bits >> 15;
+    bits *= 0x2c1b3c6du;
+    bits ^= bits >> 12;
+    return (float)((bits >> 8) & 0xFFFFu) / 65535.0f;
+}
+
+// HydraulicErosion.mouthKey (HydraulicErosion.kt:1567-1571).
+inline int mouth_key(int apex, int reach_cells, int W) {
+    int block = reach_cells < 1 ? 1 : reach_cells;
+    return (apex / W / block) * kMouthKeyRowStride + (apex % W / block);
+}
+
+// HydraulicErosion.fallToReceiver (HydraulicErosion.kt:2229-2230).
+inline float fall_to_receiver(const float* ground, const u8* is_land, int cell, int receiver) {
+    return ground[cell] - (is_land[receiver] ? ground[receiver] : 0.0f);
+}
+
+// HydraulicErosion.headroom (HydraulicErosion.kt:2400-2424).
+float headroom(int W, int H, int cell, float drop, const int32_t* dirs, const float* settled, float grade,
+               const GroundSteps& steps) {
+    float room = 3.402823466e+38f;
+    bool fed = false;
+    for_each_neighbour(W, H, cell % W, cell / W, [&](int n, int, int) {
+        if (dirs[n] != cell) return;
+        fed = true;
+        float step = steps.between(n, cell, W);
+        float margin = settled[n] - settled[cell] - grade * step;
+        if (margin < room) room = margin;
+    });
+    return fed ? room : drop - grade;
+}
+
+// DeltaFan.hash (DeltaFan.kt): SplitMix64-style mixing of the seed and a mouth's key, Long wrapping.
+int32_t fan_hash(int64_t seed, int32_t index) {
+    uint64_t mixed = (uint64_t)seed * (uint64_t)(-0x61c8864680b583ebLL) +
+                     (uint64_t)(int64_t)index * (uint64_t)(-0x7ee3623a03d3c83fLL) + (uint64_t)0x5DE17A11;
+    mixed = (mixed ^ (mixed >> 30)) * (uint64_t)(-0x40a7b892e31b1a47LL);
+    mixed = (mixed ^ (mixed >> 27)) * (uint64_t)(-0x6b2fb644ecceee15LL);
+    mixed = mixed ^ (mixed >> 31);
+    return (int32_t)(uint32_t)(mixed >> 17);
+}
+
+// DeltaFan.draw: a number in 0..1 for (hash, slot), Int wrapping.
+float fan_draw(int32_t hash, int slot) {
+    uint32_t mixed = (uint32_t)hash + (uint32_t)slot * 0x9E3779B9u;
+    mixed ^= mixed >> 15;
+    mixed *= 0x2c1b3c6du;
+    mixed ^= mixed >> 12;
+    mixed *= 0x297a2d39u;
+    mixed ^= mixed >> 15;
+    return (float)((mixed >> 8) & 0xFFFFu) / 65535.0f;
+}
+
+const float kSideReachShare = 0.38f;   // DeltaFan.SIDE_REACH_SHARE
+const float kFanWobble = 0.30f;        // DeltaFan.WOBBLE
+const float kWobbleW2 = 1.0f, kWobbleW3 = 0.7f, kWobbleW5 = 0.5f, kWobbleW7 = 0.45f;
+const float kWobbleTotalInverse = 1.0f / (kWobbleW2 + kWobbleW3 + kWobbleW5 + kWobbleW7);
+const float kDistributarySpread = 1.1f;
+const float kGrooveHalfWidthShare = 0.05f;
+const int kGrooveMinReachCells = 4;
+const float kMinGrooveHalfWidthCells = 0.55f;
+const int kGrooveDrawSlot = 10;
+const float kGrooveJitterShare = 0.8f;
+
+// DeltaFan.Rim: a lobe's outline around its apex, its bearing, its wobble and its grooves.
+struct Rim {
+    int apex, width;
+    float reach_cells;
+    int apex_column, apex_row;
+    float ahead_x = 0.0f, ahead_y = 0.0f;
+    float ph2x, ph2y, ph3x, ph3y, ph5x, ph5y, ph7x, ph7y;
+    int distributaries = 0, live = 0;
+    float groove_x[5] = {0}, groove_y[5] = {0};
+    float groove_half_width;
+    GroundSteps steps;
+    float row_scale;
+
+    static void phase(int32_t hash, int slot, float& x, float& y) {
+        float hx = fan_draw(hash, slot * 2) * 2.0f - 1.0f;
+        float hy = fan_draw(hash, slot * 2 + 1) * 2.0f - 1.0f;
+        float len = std::sqrt(hx * hx + hy * hy);
+        if (len < 1e-4f) {
+            x = 1.0f;
+            y = 0.0f;
+        } else {
+            x = hx / len;
+            y = hy / len;
+        }
+    }
+
+    Rim(int apex_, int width_, double r, float reach, float out_x, float out_y, int32_t hash, bool grooved)
+        : apex(apex_), width(width_), reach_cells(reach), apex_column(apex_ % width_), apex_row(apex_ / width_),
+          steps(r), row_scale((float)r) {
+        groove_half_width = reach * kGrooveHalfWidthShare > kMinGrooveHalfWidthCells ? reach * kGrooveHalfWidthShare
+                                                                                    : kMinGrooveHalfWidthCells;
+        float out_down = out_y * row_scale;
+        float out_length = std::sqrt(out_x * out_x + out_down * out_down);
+        if (out_length > 0.0f) {
+            ahead_x = out_x / out_length;
+            ahead_y = out_down / out_length;
+        }
+        phase(hash, 1, ph2x, ph2y);
+        phase(hash, 2, ph3x, ph3y);
+        phase(hash, 3, ph5x, ph5y);
+        phase(hash, 4, ph7x, ph7y);
+        distributaries = (!grooved || reach < (float)kGrooveMinReachCells || out_length <= 0.0f)
+                             ? 0
+                             : 2 + (int)(((uint32_t)hash >> 3) & 3u);
+        if (distributaries > 0) {
+            int n = distributaries;
+            float left_x = -ahead_y, left_y = ahead_x;
+            float span = n > 1 ? 2.0f * kDistributarySpread / (float)(n - 1) : 0.0f;
+            for (int g = 0; g < n; ++g) {
+                float jitter = (fan_draw(hash, kGrooveDrawSlot + g) - 0.5f) * kGrooveJitterShare * span;
+                float off_axis = n > 1 ? -kDistributarySpread + span * (float)g + jitter : jitter;
+                float ray_x = ahead_x + left_x * off_axis;
+                float ray_y = ahead_y + left_y * off_axis;
+                float ray_length = std::sqrt(ray_x * ray_x + ray_y * ray_y);
+                if (ray_length < 1e-6f) ray_length = 1e-6f;
+                groove_x[g] = ray_x / ray_length;
+                groove_y[g] = ray_y / ray_length;
+            }
+        }
+        live = distributaries;
+    }
+
+    float radius(float column_offset, float row_offset, float distance) const {
+        if (distance <= 0.0f) return reach_cells;
+        float c1 = column_offset / distance, s1 = row_offset / distance;
+        float ahead = c1 * ahead_x + s1 * ahead_y;
+        float nose = kSideReachShare + (1.0f - kSideReachShare) * (ahead > 0.0f ? ahead : 0.0f);
+        float c2 = c1 * c1 - s1 * s1, s2 = 2.0f * c1 * s1;
+        float c3 = c2 * c1 - s2 * s1, s3 = s2 * c1 + c2 * s1;
+        float c5 = c3 * c2 - s3 * s2, s5 = s3 * c2 + c3 * s2;
+        float c7 = c5 * c2 - s5 * s2, s7 = s5 * c2 + c5 * s2;
+        float term = (kWobbleW2 * (c2 * ph2x - s2 * ph2y) + kWobbleW3 * (c3 * ph3x - s3 * ph3y) +
+                      kWobbleW5 * (c5 * ph5x - s5 * ph5y) + kWobbleW7 * (c7 * ph7x - s7 * ph7y)) *
+                     kWobbleTotalInverse;
+        return reach_cells * nose * (1.0f + kFanWobble * term);
+    }
+
+    bool grooved(float column_offset, float row_offset) const {
+        for (int g = 0; g < live; ++g) {
+            if (column_offset * groove_x[g] + row_offset * groove_y[g] < 0.0f) continue;
+            float across = column_offset * groove_y[g] - row_offset * groove_x[g];
+            if (across > -groove_half_width && across < groove_half_width) return true;
+        }
+        return false;
+    }
+
+    template <class Open>
+    void prune_grooves(int height, Open&& open) {
+        int kept = 0;
+        for (int g = 0; g < distributaries; ++g) {
+            float rx = groove_x[g], ry = groove_y[g];
+            float ray_reach = radius(rx, ry, 1.0f);
+            bool blocked = false;
+            float stride = std::min(1.0f, row_scale);
+            float along = stride;
+            while (along <= (float)(int)ray_reach) {
+                int row = apex_row + (int)(ry * along / row_scale);
+                if (row < 0 || row >= height) {
+                    blocked = true;
+                    break;
+                }
+                int column = (apex_column + (int)(rx * along)) % width;
+                if (column < 0) column += width;
+                if (!open(row * width + column)) {
+                    blocked = true;
+                    break;
+                }
+                along += stride;
+            }
+            if (blocked) continue;
+            if (kept != g) {
+                groove_x[kept] = groove_x[g];
+                groove_y[kept] = groove_y[g];
+            }
+            kept++;
+        }
+        live = kept;
+    }
+
+    float column_offset(int cell) const { return (float)shortest_x(cell % width - apex_column, width); }
+    float row_offset(int cell) const { return (float)(cell / width - apex_row) * row_scale; }
+};
+
+// DeltaFan.Scratch: the stamps, a binary min-heap on (key, cell) and the admitted list.
+struct FanScratch {
+    std::vector<int> stamp;
+    int capacity;
+    std::vector<int> cells;
+    std::vector<float> keys, penalties;
+    int size = 0;
+    std::vector<int> admitted;
+    int admitted_count = 0;
+    int out_cell = -1;
+    float out_penalty = 0.0f;
+
+    FanScratch(size_t n, int reach_cells, double r) : stamp(n, 0) {
+        int reach_rows = (int)std::ceil(reach_cells / r);
+        capacity = std::max((2 * reach_cells + 1) * (2 * reach_rows + 1), 9);
+        cells.assign(capacity, 0);
+        keys.assign(capacity, 0.0f);
+        penalties.assign(capacity, 0.0f);
+        admitted.assign(capacity, 0);
+    }
+    bool less(int a, int b) const { return keys[a] < keys[b] || (keys[a] == keys[b] && cells[a] < cells[b]); }
+    void swap_slots(int a, int b) {
+        std::swap(cells[a], cells[b]);
+        std::swap(keys[a], keys[b]);
+        std::swap(penalties[a], penalties[b]);
+    }
+    void admit(int cell) {
+        if (admitted_count < capacity) admitted[admitted_count++] = cell;
+    }
+    void push(int cell, float key, float penalty) {
+        if (size >= capacity) return;
+        int slot = size++;
+        cells[slot] = cell;
+        keys[slot] = key;
+        penalties[slot] = penalty;
+        while (slot > 0) {
+            int parent = (slot - 1) / 2;
+            if (!less(slot, parent)) break;
+            swap_slots(slot, parent);
+            slot = parent;
+        }
+    }
+    bool pop() {
+        if (size == 0) return false;
+        out_cell = cells[0];
+        out_penalty = penalties[0];
+        size--;
+        if (size > 0) {
+            cells[0] = cells[size];
+            keys[0] = keys[size];
+            penalties[0] = penalties[size];
+            int slot = 0;
+            while (true) {
+                int left = 2 * slot + 1;
+                if (left >= size) break;
+                int right = left + 1;
+                int smaller = left;
+                if (right < size && less(right, left)) smaller = right;
+                if (!less(smaller, slot)) break;
+                swap_slots(slot, smaller);
+                slot = smaller;
+            }
+        }
+        return true;
+    }
+};
+
+// growFan (DeltaFan.kt): best-first admission of cells inside the rim, distance bent by `advance`,
+// then laying `budget` into the admitted cells nearest first, each up to `level_of` and no higher.
+template <class Accepts, class Advance, class LevelOf>
+double grow_fan(int W, int H, double budget, const Rim& rim, FanScratch& scratch, int id, const float* surface,
+                float* sediment, float* settled, float to_relative, bool whole_cells, Accepts&& accepts,
+                Advance&& advance, LevelOf&& level_of) {
+    int apex = rim.apex;
+    if (budget <= 0.0 || !accepts(apex)) return 0.0;
+    scratch.size = 0;
+    scratch.admitted_count = 0;
+    scratch.stamp[apex] = id;
+    scratch.push(apex, 0.0f, 0.0f);
+    while (scratch.pop()) {
+        int cell = scratch.out_cell;
+        float penalty = scratch.out_penalty;
+        scratch.admit(cell);
+        int column = cell % W, row = cell / W;
+        for (int sy = -1; sy <= 1; ++sy) {
+            int nr = row + sy;
+            if (nr < 0 || nr >= H) continue;
+            for (int sx = -1; sx <= 1; ++sx) {
+                if (sx == 0 && sy == 0) continue;
+                int nc = (column + sx) % W;
+                if (nc < 0) nc += W;
+                int n = nr * W + nc;
+                if (scratch.stamp[n] == id || !accepts(n)) continue;
+                float co = rim.column_offset(n), ro = rim.row_offset(n);
+                float distance = std::sqrt(co * co + ro * ro);
+                float step = rim.steps.of(sx, sy);
+                float np = penalty + step * (advance(n) - 1.0f);
+                float rim_here = rim.radius(co, ro, distance);
+                if (distance + np > rim_here) continue;
+                scratch.stamp[n] = id;
+                scratch.push(n, distance + np, np);
+            }
+        }
+    }
+    int count = scratch.admitted_count;
+    scratch.size = 0;
+    for (int k = 0; k < count; ++k) {
+        int cell = scratch.admitted[k];
+        float co = rim.column_offset(cell), ro = rim.row_offset(cell);
+        scratch.push(cell, std::sqrt(co * co + ro * ro), 0.0f);
+    }
+    double remaining = budget, laid = 0.0;
+    while (remaining > 0.0 && scratch.pop()) {
+        int cell = scratch.out_cell;
+        float co = rim.column_offset(cell), ro = rim.row_offset(cell);
+        float distance = std::sqrt(co * co + ro * ro);
+        float fraction = distance / rim.reach_cells;
+        if (fraction > 1.0f) fraction = 1.0f;
+        double need = (double)level_of(cell, fraction) - (double)surface[cell] - (double)sediment[cell];
+        if (need <= 0.0) continue;
+        if (whole_cells && need > remaining) break;
+        double moved = raise(sediment, cell, need < remaining ? need : remaining);
+        settled[cell] += (float)(moved * (double)to_relative);
+        remaining -= moved;
+        laid += moved;
+    }
+    return laid;
+}
+
+struct Tally {   // one round's mass budget (RoundMass, HydraulicErosion.kt:1477-1484)
+    double incised = 0.0, deposited = 0.0, lost = 0.0, field_drop = 0.0;
+};
+
+// The deposition walk (HydraulicErosion.kt:1068-1349) over one round's drainage order, sources first:
+// each cell picks up what the incision took off it, settles any surplus over the flow's capacity on a
+// floodplain (never above the ground that feeds it), and hands the rest on; at the sea a river's
+// share builds a lobe, at a lake a share builds a fan. P2's lobes and fans are the outlined ones
+// (growFan).
+void deposition_walk(const cg_erosion_params& p, const Switches& sw, const DepositionRates& dr, const Rates& rates,
+                     const int32_t* order, int order_len, const int32_t* dirs, const u8* is_land,
+                     const float* ground, const float* relative, const float* area, float land_cells,
+                     float land_range, float to_relative, float shoreline, float* surface, float* sediment,
+                     float* settled, double* load, const double* incised_at, FanScratch& scratch, int& mouth_id,
+                     Tally& t) {
+    const int W = p.width, H = p.height;
+    const double r = scale_of(p).cell_height_km(H) / scale_of(p).cell_width_km(W);
+    const int reach_cells = dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells;
+    const float delta_top = shoreline + dr.delta_freeboard * land_range;
+    const float rim_top = shoreline + (delta_top - shoreline) * kLobeRim;
+    const float shelf_depth = dr.shelf_break < 1e-9f ? 1e-9f : dr.shelf_break;
+    for (int rank = 0; rank < order_len; ++rank) {
+        int cell = order[rank];
+        int receiver = dirs[cell];
+        double carried = load[cell];
+        if (receiver < 0) {
+            t.lost += carried;
+            continue;
+        }
+        bool to_sea = !is_land[receiver];
+        float drop = fall_to_receiver(ground, is_land, cell, receiver);
+        bool ponded = ground[cell] - relative[cell] > rates.pond_depth;
+        {
+            float distance = rates.steps.between(cell, receiver, W);
+            float slope = drop > 0.0f ? drop / distance * (float)W : 0.0f;
+            double capacity = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells) * slope);
+            double moved = incised_at[cell];
+            if (moved > 0.0) {
+                settled[cell] -= (float)(moved * (double)to_relative);
+                carried += moved;
+                t.incised += moved;
+            }
+            if (!ponded && carried > capacity) {
+                float grade = 0.0f;
+                if (sw.graded_aggradation) {
+                    double conveyance = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells));
+                    grade = conveyance > 1e-12 ? (float)(carried / conveyance / (double)W) : 0.0f;
+                }
+                float room = headroom(W, H, cell, drop, dirs, settled, grade, rates.steps) * land_range;
+                double give = jvm_min(carried - capacity, (double)room) * (double)sw.deposition_rate;
+                if (give > 0.0) {
+                    double laid = raise(sediment, cell, give);
+                    settled[cell] += (float)(laid * (double)to_relative);
+                    carried -= laid;
+                    t.deposited += laid;
+                }
+            }
+        }
+        if (to_sea) {
+            bool river = area[cell] >= dr.delta_min_cells;
+            float out_x = (float)shortest_x(receiver % W - cell % W, W);
+            float out_y = (float)(receiver / W - cell / W);
+            double budget = river ? carried * (double)sw.delta_share : 0.0;
+            Rim rim(receiver, W, r, (float)reach_cells, out_x, out_y,
+                    fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), true);
+            rim.prune_grooves(H, [&](int c) { return !is_land[c]; });
+            double laid = grow_fan(
+                W, H, budget, rim, scratch, ++mouth_id, surface, sediment, settled, to_relative, true,
+                [&](int c) { return !is_land[c]; },
+                [&](int c) {
+                    float depth = shoreline - (surface[c] + sediment[c]);
+                    return 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / shelf_depth;
+                },
+                [&](int c, float fraction) {
+                    float level = delta_top + (rim_top - delta_top) * fraction;
+                    if (rim.grooved(rim.column_offset(c), rim.row_offset(c)))
+                        return shoreline + (level - shoreline) * kGrooveKeep;
+                    return level;
+                });
+            t.deposited += laid;
+            t.lost += carried - laid;
+        } else if (!ponded && ground[receiver] - relative[receiver] > rates.pond_depth) {
+            float in_x = (float)shortest_x(receiver % W - cell % W, W);
+            float in_y = (float)(receiver / W - cell / W);
+            Rim rim(receiver, W, r, (float)reach_cells, in_x, in_y,
+                    fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), false);
+            double laid = grow_fan(
+                W, H, carried * (double)sw.lake_share, rim, scratch, ++mouth_id, surface, sediment, settled,
+                to_relative, false,
+                [&](int c) { return is_land[c] && ground[c] - relative[c] > rates.pond_depth; },
+                [&](int c) {
+                    float depth = (ground[c] - relative[c]) * land_range;
+                    return 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / shelf_depth;
+                },
+                [&](int c, float fraction) {
+                    float depth = 2.0f * rates.pond_depth * (1.0f + kLakeFanSlope * fraction) *
+                                  (0.9f + 0.35f * cell_wobble(c));
+                    return shoreline + (ground[c] - depth) * land_range;
+                });
+            t.deposited += laid;
+            load[receiver] += carried - laid;
+        } else {
+            load[receiver] += carried;
+        }
+    }
+}
+
+// HydraulicErosion.openMouths (HydraulicErosion.kt:1804-1892): a fresh cut, fill, routing and
+// discharge over the finished surface, then each drawn river's path across raised ground (or its own
+// fresh spoil) cut to a surface falling a fixed step a cell, receivers before their donors.
+double open_mouths(const cg_erosion_params& p, float* working, const float* spoil, float pond_depth,
+                   const float* rain, double r, int lattice, const DepositionRates& dr) {
+    const int W = p.width, H = p.height;
+    const size_t N = (size_t)W * H;
+    Scale sc = scale_of(p);
+    Cut sea;
+    percentile_cut(W, H, working, p.sea_level, sc, 0.0f, sea);
+    if (sea.land_cells == 0) return 0.0;
+    const float land_range = std::max(sc.land_half(), 1e-6f);
+    const float step = pond_depth * land_range;
+    const float fall_per_cell_width = step * kDistributaryFallPerKm * (float)sc.cell_width_km(W);
+    GroundSteps steps(r);
+    const float floor_ = sea.shoreline + step * kLobeRim;
+    std::vector<float> filled(N), runoff(N), area(N);
+    std::vector<int32_t> flow(N);
+    fill_depressions(W, H, sea.is_land.data(), sea.relative.data(), filled.data());
+    FlatCounts fc;
+    flow_directions(W, H, sea.is_land.data(), sea.relative.data(), filled.data(), p.seed, r, lattice,
+                    p.facet_routing != 0, p.flat_potential != 0, flow.data(), nullptr, &fc);
+    normalise_over_land(rain, sea.is_land.data(), sea.land_cells, N, runoff.data());
+    accumulate(W, H, sea.is_land.data(), flow.data(), sea.land_cells, runoff.data(), area.data());
+    std::vector<int32_t> order(sea.land_cells);
+    drainage_order(W, H, sea.is_land.data(), flow.data(), sea.land_cells, order.data());
+    double removed = 0.0;
+    for (int rank = sea.land_cells - 1; rank >= 0; --rank) {
+        int cell = order[rank];
+        if (area[cell] < dr.drawn_river_cells) continue;
+        float standing = filled[cell] - sea.relative[cell];
+        bool on_flat = standing > 0.0f && (standing <= pond_depth || spoil[cell] > 0.0f);
+        if (!on_flat) continue;
+        int receiver = flow[cell];
+        if (receiver < 0) continue;
+        float below = sea.is_land[receiver] ? working[receiver] : sea.shoreline;
+        float fall = fall_per_cell_width * steps.between(cell, receiver, W);
+        if (fall < kMinDistributaryFall) fall = kMinDistributaryFall;
+        float want = jvm_min(working[cell], below + fall);
+        if (want < floor_) want = floor_;
+        if (working[cell] > want) removed += -raise(working, cell, (double)(want - working[cell]));
+    }
+    return removed;
+}
+
 struct StageOut {
     std::vector<float> height;
     Cut cut;
@@ -1132,7 +1681,8 @@ struct StageOut {
 // run_rounds >= 0 stops after that many rounds (the relaxation keeps the whole stage's share per
 // round) and initial = false leaves out the initial sweeps: a bounded sample of a stage.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
-                bool with_thermal = true, bool initial = true, int run_rounds = -1) {
+                bool with_thermal = true, bool initial = true, int run_rounds = -1,
+                const Switches* switches = nullptr, Tally* tallies = nullptr) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -1155,8 +1705,29 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
         return CG_OK;
     }
     Rates rates(p);
+    const Switches sw = switches ? *switches : switches_of(p);
     double r = sc.cell_height_km(H) / sc.cell_width_km(W);   // cellHeightInCellWidths
     int lattice = smooth_field_lattice_columns(p.world_width_km);
+    // What deposition carries (HydraulicErosion.kt:729-789): the load in transit (double), the spoil at
+    // rest (laid on the terrain once, at the end), the incision's take per cell, and one set of fan
+    // stamps for the whole stage, the mouth ids only ever increasing.
+    const DepositionRates dr(p, sw);
+    std::vector<float> sediment, settled;
+    std::vector<double> load, incised_at;
+    std::unique_ptr<FanScratch> scratch;
+    int mouth_id = 0;
+    if (sw.deposition) {
+        sediment.assign(N, 0.0f);
+        settled.assign(N, 0.0f);
+        load.assign(N, 0.0);
+        incised_at.assign(N, 0.0);
+        scratch.reset(new FanScratch(N, dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells, r));
+    }
+    auto total_mass = [&](const std::vector<float>& f) {
+        double sum = 0.0;
+        for (float v : f) sum += (double)v;
+        return sum;
+    };
     std::vector<float> ones(N, 1.0f), zeros(N, 0.0f);
     const float* rain = in.rainfall_mm ? in.rainfall_mm : ones.data();
     const float* veg = in.vegetation_density ? in.vegetation_density : zeros.data();
@@ -1197,16 +1768,31 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
         drainage_order(W, H, cut.is_land.data(), dirs.data(), cut.land_cells, order.data());
         float land_cells = (float)cut.land_cells;
         float land_range = std::max(sc.land_half(), 1e-6f);
-        if (p.profile == CG_PROFILE_P1) {
+        float to_relative = 1.0f / land_range;
+        Tally t;
+        if (sw.deposition) {   // HydraulicErosion.kt:940-945
+            std::fill(load.begin(), load.end(), 0.0);
+            std::fill(incised_at.begin(), incised_at.end(), 0.0);
+            for (size_t c = 0; c < N; ++c) settled[c] = cut.relative[c] + sediment[c] * to_relative;
+        }
+        const double starting_mass = tallies ? total_mass(working) + (sw.deposition ? total_mass(sediment) : 0.0) : 0.0;
+        if (sw.outlet_incision) {
             Spillways notch;
             spillways(W, H, cut.is_land.data(), cut.relative.data(), filled.data(), dirs.data(), rates.pond_depth,
                       notch, nullptr);
-            breach(rates, W, notch, cut.is_land.data(), cut.relative.data(), filled.data(), dirs.data(), area.data(),
-                   land_cells, land_range, working.data());
+            Breached b = breach(rates, W, notch, cut.is_land.data(), cut.relative.data(), filled.data(), dirs.data(),
+                                area.data(), land_cells, land_range, working.data(),
+                                sw.deposition ? settled.data() : nullptr, sw.deposition ? load.data() : nullptr);
+            t.incised += b.moved;
         }
         incise(rates, W, N, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(), filled.data(),
                cut.relative.data(), area.data(), land_cells, land_range, cut.shoreline, erod.data(), working.data(),
-               p.receiver_clamp != 0, nullptr);
+               p.receiver_clamp != 0, nullptr, sw.deposition ? incised_at.data() : nullptr);
+        if (sw.deposition)
+            deposition_walk(p, sw, dr, rates, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(),
+                            filled.data(), cut.relative.data(), area.data(), land_cells, land_range, to_relative,
+                            cut.shoreline, working.data(), sediment.data(), settled.data(), load.data(),
+                            incised_at.data(), *scratch, mouth_id, t);
         if (stats) {
             cg_round_stats& s = stats[round];
             std::memset(&s, 0, sizeof(s));
@@ -1217,7 +1803,16 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
             s.flats_kept = flats.kept;
             s.raised_cells = flats.raised;
         }
-        if (p.profile == CG_PROFILE_P1 && round == p.hydraulic_rounds - 1) {
+        const bool closing = round == p.hydraulic_rounds - 1;
+        // The spoil, kept before it becomes terrain (the mouths pass tells fresh ground by it), and
+        // settle(): the whole stage's deposition laid on the rock at once (HydraulicErosion.kt:1351-1364).
+        std::vector<float> spoil;
+        if (closing && sw.delta_lobe) spoil = sw.deposition ? sediment : std::vector<float>(N, 0.0f);
+        if (closing && sw.deposition) {
+            for (size_t c = 0; c < N; ++c) working[c] += sediment[c];
+            std::fill(sediment.begin(), sediment.end(), 0.0f);
+        }
+        if (closing && sw.outlet_incision) {
             // The closing breach over the finished surface: a fresh cut at today's shoreline, its own
             // fill, routing and discharge, then one more notch.
             Cut after;
@@ -1234,15 +1829,26 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
                 Spillways notch;
                 spillways(W, H, after.is_land.data(), after.relative.data(), filled.data(), dirs.data(),
                           rates.pond_depth, notch, nullptr);
-                breach(rates, W, notch, after.is_land.data(), after.relative.data(), filled.data(), dirs.data(),
-                       area.data(), (float)after.land_cells, land_range, working.data());
+                Breached b = breach(rates, W, notch, after.is_land.data(), after.relative.data(), filled.data(),
+                                    dirs.data(), area.data(), (float)after.land_cells, land_range, working.data());
+                t.incised += b.moved;
+                t.lost += b.moved;
                 order.assign(after.land_cells, 0);
                 drainage_order(W, H, after.is_land.data(), dirs.data(), after.land_cells, order.data());
                 cut = std::move(after);
             }
         }
+        if (closing && sw.delta_lobe) {   // HydraulicErosion.kt:1451-1462
+            double removed = open_mouths(p, working.data(), spoil.data(), rates.pond_depth, rain, r, lattice, dr);
+            t.incised += removed;
+            t.lost += removed;
+        }
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         if (with_thermal) thermal_sweep(W, H, working.data(), working.data(), lim, per_round, p.rate, true);
+        if (tallies) {
+            t.field_drop = starting_mass - total_mass(working) - (sw.deposition ? total_mass(sediment) : 0.0);
+            tallies[round] = t;
+        }
     }
     std::memcpy(out->height, working.data(), N * sizeof(float));
     if (!routed) return CG_OK;
@@ -1454,6 +2060,44 @@ int32_t or_hydraulic_apply(const cg_erosion_params* p, const cg_inputs* in, cg_o
 
 // The first `rounds` rounds of ErosionStage.apply from heights already swept (no initial sweeps),
 // each with its relaxation: a bounded sample of the stage for timing.
+// The round tail's switches and the deposition's knobs, for tests that set them one by one
+// (ErosionConfig.outletIncision, deposition, deltaLobe, gradedAggradation, transportCapacity,
+// depositionRate, deltaShare, lakeShare, deltaMinCatchmentKm2, deltaReachKm, deltaFreeboardMetres).
+struct or_switches {
+    int32_t outlet_incision, deposition, delta_lobe, graded_aggradation;
+    float transport_capacity, deposition_rate, delta_share, lake_share;
+    double delta_min_catchment_km2, delta_reach_km;
+    float delta_freeboard_metres;
+};
+
+// ErosionStage.apply with explicit switches; tallies (may be NULL) receives per round the incised,
+// deposited and lost amounts and the field's drop (RoundMass), 4 doubles a round.
+int32_t or_erode_stage_switched(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
+                                const or_switches* s, double* tallies, int32_t with_thermal) {
+    Switches sw;
+    sw.outlet_incision = s->outlet_incision != 0;
+    sw.deposition = s->deposition != 0;
+    sw.delta_lobe = s->delta_lobe != 0;
+    sw.graded_aggradation = s->graded_aggradation != 0;
+    sw.transport_capacity = s->transport_capacity;
+    sw.deposition_rate = s->deposition_rate;
+    sw.delta_share = s->delta_share;
+    sw.lake_share = s->lake_share;
+    sw.delta_min_catchment_km2 = s->delta_min_catchment_km2;
+    sw.delta_reach_km = s->delta_reach_km;
+    sw.delta_freeboard_metres = s->delta_freeboard_metres;
+    std::vector<Tally> t(p->hydraulic_rounds > 0 ? p->hydraulic_rounds : 1);
+    int st = erode_stage(*p, *in, out, nullptr, with_thermal != 0, true, -1, &sw, tallies ? t.data() : nullptr);
+    if (tallies)
+        for (int i = 0; i < p->hydraulic_rounds; ++i) {
+            tallies[4 * i + 0] = t[i].incised;
+            tallies[4 * i + 1] = t[i].deposited;
+            tallies[4 * i + 2] = t[i].lost;
+            tallies[4 * i + 3] = t[i].field_drop;
+        }
+    return st;
+}
+
 int32_t or_stage_rounds(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, int32_t rounds) {
     return erode_stage(*p, *in, out, nullptr, true, false, rounds);
 }

@@ -1,0 +1,67 @@
+"""The oracle's restatement of profile P2's deposition (the walk, the outlined sea lobes and lake fans,
+settle, the closing mouths pass), pinned to the reference's DepositionTest
+(T/DepositionTest.kt, T = worldgen/src/jvmTest/kotlin/com/cartogenesis/worldgen): every round's mass
+budget closes, and deposition switched off is deposition absent, whatever its knobs say, while
+deposition running with every rate at zero leaves the rock bit-identical. The GPU does not run P2 yet
+(cg_erode_stage answers CG_UNSUPPORTED); these tests hold the restatement it will be checked against.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cartogenesis_gb300 import synthetic
+
+
+def bits(a):
+    return a.view(np.uint32)
+
+
+@pytest.mark.parametrize("W,H,seed", [(256, 128, 42), (512, 256, 7)])
+def test_every_round_conserves_mass(W, H, seed):
+    """T/DepositionTest.kt:44-94: incised = deposited + lost, and the field fell by what was lost,
+    each within 1% in every round, and every round deposited something."""
+    h, up, rk = synthetic.world(W, H, seed)
+    p = oracle.default_params(W, H, seed, sea_level=0.70, profile=2)
+    _, tallies = oracle.erode_stage_switched(p, h, up, rk)
+    assert tallies.shape == (12, 4)
+    for incised, deposited, lost, drop in tallies:
+        assert abs(incised - (deposited + lost)) / max(incised, 1e-12) < 0.01
+        assert abs(drop - lost) / max(lost, 1e-12) < 0.01
+        assert deposited > 0.0
+
+
+def test_deposition_off_is_deposition_absent():
+    """T/DepositionTest.kt:165-214: with deposition off no knob beside it leaks into the world, and with
+    deposition running but every rate that lays spoil at zero the rock is bit-identical to the rock
+    with the machinery off."""
+    W, H, seed = 256, 128, 42
+    h, up, rk = synthetic.world(W, H, seed)
+    p = oracle.default_params(W, H, seed, sea_level=0.70)
+    off, _ = oracle.erode_stage_switched(p, h, up, rk, oracle.Switches(2, deposition=0))
+    fiddled, _ = oracle.erode_stage_switched(
+        p, h, up, rk, oracle.Switches(2, deposition=0, transport_capacity=0.1, deposition_rate=1.0, delta_share=1.0,
+                                      delta_min_catchment_km2=0.0, lake_share=1.0, delta_reach_km=469.0,
+                                      delta_freeboard_metres=3000.0))
+    silent, _ = oracle.erode_stage_switched(
+        p, h, up, rk, oracle.Switches(2, delta_share=0.0, deposition_rate=0.0, lake_share=0.0))
+    on, tallies = oracle.erode_stage_switched(p, h, up, rk, oracle.Switches(2))
+    assert np.array_equal(bits(fiddled), bits(off))
+    assert np.array_equal(bits(silent), bits(off))
+    assert not np.array_equal(bits(on), bits(off))
+    assert tallies[:, 1].sum() > 0.0
+
+
+def test_profiles_nest():
+    """The profile switches: P2 through the ABI's profile field is the switched stage with the reference
+    defaults, and the mouths pass (deltaLobe) is the only difference between P1 and P2 with deposition
+    off."""
+    W, H, seed = 128, 64, 3
+    h, up, rk = synthetic.world(W, H, seed)
+    p2 = oracle.default_params(W, H, seed, sea_level=0.70, profile=2)
+    via_profile = oracle.erode_stage(p2, h, up, rk, want=())["height"]
+    switched, _ = oracle.erode_stage_switched(p2, h, up, rk, oracle.Switches(2))
+    assert np.array_equal(bits(via_profile), bits(switched))
+    p1 = oracle.default_params(W, H, seed, sea_level=0.70, profile=1)
+    plain_p1 = oracle.erode_stage(p1, h, up, rk, want=())["height"]
+    switched_p1, _ = oracle.erode_stage_switched(p1, h, up, rk, oracle.Switches(1))
+    assert np.array_equal(bits(plain_p1), bits(switched_p1))
