@@ -338,3 +338,23 @@ def test_gpu_stage_p1_bench_world_8192x4096():
     want = oracle.erode_stage(oracle.default_params(W, H, seed, sea_level=0.70, profile=1), h, up, rk, want=keys)
     compare(got, want, order=False)
 
+
+
+@pytest.mark.gpu
+def test_gpu_breach_without_basins_changes_nothing():
+    """A plane falling to the sea has no basin: the notch's early return leaves every array as it was."""
+    from cartogenesis_gb300 import ErosionConfig, HydraulicErosion
+    W, H = 64, 32
+    col = np.arange(W)[None, :].repeat(H, 0)
+    land = (col >= 8).astype(np.uint8)
+    rel = np.where(land == 1, (col - 7).astype(np.float32) * f32(0.01), f32(-0.5)).astype(np.float32)
+    filled = oracle.fill_depressions(land, rel)
+    flow, _ = oracle.flow_directions(land, rel, filled, 1, 0.5 * W / H, LATTICE)
+    area = oracle.accumulate(land, flow, int(land.sum()), np.ones((H, W), np.float32))
+    surface = (f32(0.625) + rel * f32(0.375)).astype(np.float32)
+    got = [rel.copy(), filled.copy(), surface.copy()]
+    cells = HydraulicErosion.breach(ErosionConfig(W, H, 1), land, got[0], got[1], flow, area, float(land.sum()),
+                                    0.375, got[2])
+    assert cells == 0
+    for g, w in zip(got, (rel, filled, surface)):
+        assert np.array_equal(bits(g), bits(w))
