@@ -223,15 +223,15 @@ def breach(params, is_land, relative, ground, directions, area, land_cells, land
 class Switches(C.Structure):
     """or_switches: the round tail's switches and the deposition's knobs, reference defaults."""
     _fields_ = [("outlet_incision", C.c_int32), ("deposition", C.c_int32), ("delta_lobe", C.c_int32),
-                ("graded_aggradation", C.c_int32), ("transport_capacity", C.c_float),
+                ("graded_aggradation", C.c_int32), ("delta_outline", C.c_int32), ("transport_capacity", C.c_float),
                 ("deposition_rate", C.c_float), ("delta_share", C.c_float), ("lake_share", C.c_float),
                 ("delta_min_catchment_km2", C.c_double), ("delta_reach_km", C.c_double),
                 ("delta_freeboard_metres", C.c_float)]
 
     def __init__(self, profile=2, **knobs):
         on = profile >= 2
-        super().__init__(int(profile >= 1), int(on), int(on), int(on), 20.0, 0.06, 0.15, 0.1, 70000.0, 140.625,
-                         48.0)
+        super().__init__(int(profile >= 1), int(on), int(on), int(on), int(on), 20.0, 0.06, 0.15, 0.1, 70000.0,
+                         140.625, 48.0)
         for k, v in knobs.items():
             setattr(self, k, v)
 

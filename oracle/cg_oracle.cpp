@@ -1130,6 +1130,7 @@ struct Switches {
     bool outlet_incision = false;     // ErosionConfig.outletIncision
     bool deposition = false;          // ErosionConfig.deposition
     bool delta_lobe = false;          // ErosionConfig.deltaLobe (the closing mouths pass runs on it)
+    bool delta_outline = false;       // ErosionConfig.deltaOutline: best-first outlined fans, else square ones
     bool graded_aggradation = false;  // ErosionConfig.gradedAggradation
     float transport_capacity = 20.0f;        // ErosionConfig.transportCapacity
     float deposition_rate = 0.06f;           // ErosionConfig.depositionRate
@@ -1141,15 +1142,17 @@ struct Switches {
 };
 
 // P0: the plain core; P1 adds the outlet notch; P2 adds deposition with the lobed, outlined and
-// graded deltas (deltaOutline is on in P2 and is the only outline restated here).
+// graded deltas.
 Switches switches_of(const cg_erosion_params& p) {
     Switches s;
     s.outlet_incision = p.profile >= CG_PROFILE_P1;
-    s.deposition = s.delta_lobe = s.graded_aggradation = p.profile >= CG_PROFILE_P2;
+    s.deposition = s.delta_lobe = s.delta_outline = s.graded_aggradation = p.profile >= CG_PROFILE_P2;
     return s;
 }
 
 const float kLobeRim = 0.15f;                       // HydraulicErosion.LOBE_RIM
+const float kLobeSides = 0.38f;                     // HydraulicErosion.LOBE_SIDES
+const float kLobeWobble = 0.18f;                    // HydraulicErosion.LOBE_WOBBLE
 const float kDepthCost = 1.0f;                      // HydraulicErosion.DEPTH_COST
 const float kGrooveKeep = 0.45f;                    // HydraulicErosion.GROOVE_KEEP
 const float kLakeFanSlope = 1.5f;                   // HydraulicErosion.LAKE_FAN_SLOPE
@@ -1206,6 +1209,23 @@ inline float cell_wobble(int cell) {
 inline int mouth_key(int apex, int reach_cells, int W) {
     int block = reach_cells < 1 ? 1 : reach_cells;
     return (apex / W / block) * kMouthKeyRowStride + (apex % W / block);
+}
+
+// HydraulicErosion.lobeLevel (HydraulicErosion.kt:1519-1527): a square lobe's surface `d` cells out.
+inline float lobe_level(float apex_level, float shoreline, int reach_cells, int distance_cells) {
+    float rim = shoreline + (apex_level - shoreline) * kLobeRim;
+    return apex_level + (rim - apex_level) * (float)distance_cells / (float)(reach_cells + 1);
+}
+
+// HydraulicErosion.lobeReach (HydraulicErosion.kt:1539-1556): how far a square lobe may grow towards a cell.
+int lobe_reach(int reach_cells, int apex, int cell, float out_x, float out_y, int W) {
+    float co = (float)shortest_x(cell % W - apex % W, W);
+    float ro = (float)(cell / W - apex / W);
+    float distance = std::sqrt(co * co + ro * ro);
+    float out_length = std::sqrt(out_x * out_x + out_y * out_y);
+    float ahead = (distance <= 0.0f || out_length <= 0.0f) ? 1.0f : (co * out_x + ro * out_y) / (distance * out_length);
+    float shape = kLobeSides + (1.0f - kLobeSides) * (ahead < 0.0f ? 0.0f : ahead);
+    return (int)((float)reach_cells * (shape + kLobeWobble * cell_wobble(cell)));
 }
 
 // HydraulicErosion.fallToReceiver (HydraulicErosion.kt:2229-2230).
@@ -1512,6 +1532,63 @@ double grow_fan(int W, int H, double budget, const Rim& rim, FanScratch& scratch
     return laid;
 }
 
+// HydraulicErosion.fan (HydraulicErosion.kt:2446-2525): the square fan, breadth-first from the mouth
+// out to the reach, each cell built up to `level_of` and no higher, nearest first. The stamps are
+// the stage's own array (ids only ever increase); the queue holds (2 reach + 1)^2 cells.
+template <class Accepts, class LevelOf>
+double square_fan(int W, int H, int start, double budget, int reach_cells, std::vector<int>& stamp, int id,
+                  std::vector<int>& queue, std::vector<int>& distance_at, const float* surface, float* sediment,
+                  float* settled, float to_relative, bool whole_cells, Accepts&& accepts, LevelOf&& level_of) {
+    if (budget <= 0.0 || !accepts(start, 0)) return 0.0;
+    double remaining = budget, laid = 0.0;
+    int head = 0, tail = 0;
+    queue[tail] = start;
+    distance_at[tail] = 0;
+    tail++;
+    stamp[start] = id;
+    while (head < tail && remaining > 0.0) {
+        int cell = queue[head];
+        int steps = distance_at[head];
+        head++;
+        double need = (double)level_of(cell, steps) - (double)surface[cell] - (double)sediment[cell];
+        if (need > 0.0) {
+            if (whole_cells && need > remaining) break;
+            double moved = raise(sediment, cell, need < remaining ? need : remaining);
+            settled[cell] += (float)(moved * (double)to_relative);
+            remaining -= moved;
+            laid += moved;
+        }
+        if (steps >= reach_cells) continue;
+        int column = cell % W, row = cell / W;
+        for (int rs = -1; rs <= 1; ++rs) {
+            int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (cs == 0 && rs == 0) continue;
+                int nc = (column + cs) % W;
+                if (nc < 0) nc += W;
+                int n = nr * W + nc;
+                if (stamp[n] == id || !accepts(n, steps + 1)) continue;
+                stamp[n] = id;
+                if (tail < (int)queue.size()) {
+                    queue[tail] = n;
+                    distance_at[tail] = steps + 1;
+                    tail++;
+                }
+            }
+        }
+    }
+    return laid;
+}
+
+// Scratch of the square fans (HydraulicErosion.kt:773-776): present where some fan is square.
+struct SquareScratch {
+    std::vector<int> stamp, queue, distance_at;
+    SquareScratch(size_t n, int reach_cells)
+        : stamp(n, 0), queue((size_t)(2 * reach_cells + 1) * (2 * reach_cells + 1)),
+          distance_at((size_t)(2 * reach_cells + 1) * (2 * reach_cells + 1)) {}
+};
+
 struct Tally {   // one round's mass budget (RoundMass, HydraulicErosion.kt:1477-1484)
     double incised = 0.0, deposited = 0.0, lost = 0.0, field_drop = 0.0;
 };
@@ -1525,8 +1602,8 @@ void deposition_walk(const cg_erosion_params& p, const Switches& sw, const Depos
                      const int32_t* order, int order_len, const int32_t* dirs, const u8* is_land,
                      const float* ground, const float* relative, const float* area, float land_cells,
                      float land_range, float to_relative, float shoreline, float* surface, float* sediment,
-                     float* settled, double* load, const double* incised_at, FanScratch& scratch, int& mouth_id,
-                     Tally& t) {
+                     float* settled, double* load, const double* incised_at, FanScratch* scratch,
+                     SquareScratch* square, int& mouth_id, Tally& t) {
     const int W = p.width, H = p.height;
     const double r = scale_of(p).cell_height_km(H) / scale_of(p).cell_width_km(W);
     const int reach_cells = dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells;
@@ -1575,11 +1652,28 @@ void deposition_walk(const cg_erosion_params& p, const Switches& sw, const Depos
             float out_x = (float)shortest_x(receiver % W - cell % W, W);
             float out_y = (float)(receiver / W - cell / W);
             double budget = river ? carried * (double)sw.delta_share : 0.0;
+            double laid;
+            if (!(sw.delta_lobe && sw.delta_outline)) {
+                // The square lobe, or with the lobe off the flat slab (HydraulicErosion.kt:1230-1253).
+                laid = square_fan(
+                    W, H, receiver, budget, reach_cells, square->stamp, ++mouth_id, square->queue, square->distance_at,
+                    surface, sediment, settled, to_relative, sw.delta_lobe,
+                    [&](int c, int steps) {
+                        return !is_land[c] &&
+                               (!sw.delta_lobe || steps <= lobe_reach(reach_cells, receiver, c, out_x, out_y, W));
+                    },
+                    [&](int, int steps) {
+                        return sw.delta_lobe ? lobe_level(delta_top, shoreline, reach_cells, steps) : delta_top;
+                    });
+                t.deposited += laid;
+                t.lost += carried - laid;
+                continue;
+            }
             Rim rim(receiver, W, r, (float)reach_cells, out_x, out_y,
                     fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), true);
             rim.prune_grooves(H, [&](int c) { return !is_land[c]; });
-            double laid = grow_fan(
-                W, H, budget, rim, scratch, ++mouth_id, surface, sediment, settled, to_relative, true,
+            laid = grow_fan(
+                W, H, budget, rim, *scratch, ++mouth_id, surface, sediment, settled, to_relative, true,
                 [&](int c) { return !is_land[c]; },
                 [&](int c) {
                     float depth = shoreline - (surface[c] + sediment[c]);
@@ -1596,10 +1690,25 @@ void deposition_walk(const cg_erosion_params& p, const Switches& sw, const Depos
         } else if (!ponded && ground[receiver] - relative[receiver] > rates.pond_depth) {
             float in_x = (float)shortest_x(receiver % W - cell % W, W);
             float in_y = (float)(receiver / W - cell / W);
+            if (!sw.delta_outline) {   // the square lake fan (HydraulicErosion.kt:1321-1344)
+                double laid = square_fan(
+                    W, H, receiver, carried * (double)sw.lake_share, reach_cells, square->stamp, ++mouth_id,
+                    square->queue, square->distance_at, surface, sediment, settled, to_relative, false,
+                    [&](int c, int) { return is_land[c] && ground[c] - relative[c] > rates.pond_depth; },
+                    [&](int c, int steps) {
+                        float depth = 2.0f * rates.pond_depth *
+                                      (1.0f + kLakeFanSlope * (float)steps / (float)(reach_cells < 1 ? 1 : reach_cells)) *
+                                      (0.9f + 0.35f * cell_wobble(c));
+                        return shoreline + (ground[c] - depth) * land_range;
+                    });
+                t.deposited += laid;
+                load[receiver] += carried - laid;
+                continue;
+            }
             Rim rim(receiver, W, r, (float)reach_cells, in_x, in_y,
                     fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), false);
             double laid = grow_fan(
-                W, H, carried * (double)sw.lake_share, rim, scratch, ++mouth_id, surface, sediment, settled,
+                W, H, carried * (double)sw.lake_share, rim, *scratch, ++mouth_id, surface, sediment, settled,
                 to_relative, false,
                 [&](int c) { return is_land[c] && ground[c] - relative[c] > rates.pond_depth; },
                 [&](int c) {
@@ -1715,13 +1824,16 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     std::vector<float> sediment, settled;
     std::vector<double> load, incised_at;
     std::unique_ptr<FanScratch> scratch;
+    std::unique_ptr<SquareScratch> square;
     int mouth_id = 0;
     if (sw.deposition) {
+        const int reach = dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells;
         sediment.assign(N, 0.0f);
         settled.assign(N, 0.0f);
         load.assign(N, 0.0);
         incised_at.assign(N, 0.0);
-        scratch.reset(new FanScratch(N, dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells, r));
+        if (sw.delta_outline) scratch.reset(new FanScratch(N, reach, r));
+        if (!sw.delta_outline || !sw.delta_lobe) square.reset(new SquareScratch(N, reach));
     }
     auto total_mass = [&](const std::vector<float>& f) {
         double sum = 0.0;
@@ -1792,7 +1904,7 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
             deposition_walk(p, sw, dr, rates, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(),
                             filled.data(), cut.relative.data(), area.data(), land_cells, land_range, to_relative,
                             cut.shoreline, working.data(), sediment.data(), settled.data(), load.data(),
-                            incised_at.data(), *scratch, mouth_id, t);
+                            incised_at.data(), scratch.get(), square.get(), mouth_id, t);
         if (stats) {
             cg_round_stats& s = stats[round];
             std::memset(&s, 0, sizeof(s));
@@ -2061,10 +2173,10 @@ int32_t or_hydraulic_apply(const cg_erosion_params* p, const cg_inputs* in, cg_o
 // The first `rounds` rounds of ErosionStage.apply from heights already swept (no initial sweeps),
 // each with its relaxation: a bounded sample of the stage for timing.
 // The round tail's switches and the deposition's knobs, for tests that set them one by one
-// (ErosionConfig.outletIncision, deposition, deltaLobe, gradedAggradation, transportCapacity,
+// (ErosionConfig.outletIncision, deposition, deltaLobe, gradedAggradation, deltaOutline, transportCapacity,
 // depositionRate, deltaShare, lakeShare, deltaMinCatchmentKm2, deltaReachKm, deltaFreeboardMetres).
 struct or_switches {
-    int32_t outlet_incision, deposition, delta_lobe, graded_aggradation;
+    int32_t outlet_incision, deposition, delta_lobe, graded_aggradation, delta_outline;
     float transport_capacity, deposition_rate, delta_share, lake_share;
     double delta_min_catchment_km2, delta_reach_km;
     float delta_freeboard_metres;
@@ -2079,6 +2191,7 @@ int32_t or_erode_stage_switched(const cg_erosion_params* p, const cg_inputs* in,
     sw.deposition = s->deposition != 0;
     sw.delta_lobe = s->delta_lobe != 0;
     sw.graded_aggradation = s->graded_aggradation != 0;
+    sw.delta_outline = s->delta_outline != 0;
     sw.transport_capacity = s->transport_capacity;
     sw.deposition_rate = s->deposition_rate;
     sw.delta_share = s->delta_share;

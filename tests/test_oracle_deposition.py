@@ -16,13 +16,17 @@ def bits(a):
     return a.view(np.uint32)
 
 
-@pytest.mark.parametrize("W,H,seed", [(256, 128, 42), (512, 256, 7)])
-def test_every_round_conserves_mass(W, H, seed):
+@pytest.mark.parametrize("W,H,seed,knobs", [
+    (256, 128, 42, {}), (512, 256, 7, {}),
+    (256, 128, 42, {"delta_outline": 0}),                    # square lobes and lake fans
+    (256, 128, 42, {"delta_outline": 0, "delta_lobe": 0}),   # the flat slab, no mouths pass
+])
+def test_every_round_conserves_mass(W, H, seed, knobs):
     """T/DepositionTest.kt:44-94: incised = deposited + lost, and the field fell by what was lost,
     each within 1% in every round, and every round deposited something."""
     h, up, rk = synthetic.world(W, H, seed)
     p = oracle.default_params(W, H, seed, sea_level=0.70, profile=2)
-    _, tallies = oracle.erode_stage_switched(p, h, up, rk)
+    _, tallies = oracle.erode_stage_switched(p, h, up, rk, oracle.Switches(2, **knobs))
     assert tallies.shape == (12, 4)
     for incised, deposited, lost, drop in tallies:
         assert abs(incised - (deposited + lost)) / max(incised, 1e-12) < 0.01
@@ -65,3 +69,17 @@ def test_profiles_nest():
     plain_p1 = oracle.erode_stage(p1, h, up, rk, want=())["height"]
     switched_p1, _ = oracle.erode_stage_switched(p1, h, up, rk, oracle.Switches(1))
     assert np.array_equal(bits(plain_p1), bits(switched_p1))
+
+
+def test_fan_shapes_differ():
+    """The outlined fans, the square lobes and the flat slab lay different spoil: each shape reaches
+    the terrain."""
+    W, H, seed = 256, 128, 42
+    h, up, rk = synthetic.world(W, H, seed)
+    p = oracle.default_params(W, H, seed, sea_level=0.70)
+    outs = [oracle.erode_stage_switched(p, h, up, rk, oracle.Switches(2, **k))[0]
+            for k in ({}, {"delta_outline": 0}, {"delta_outline": 0, "delta_lobe": 0})]
+    for i in range(3):
+        for j in range(i + 1, 3):
+            assert not np.array_equal(bits(outs[i]), bits(outs[j]))
+
