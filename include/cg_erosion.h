@@ -40,7 +40,7 @@ typedef enum cg_status {
     CG_BAD_ARG = 3,     /* a size, pointer or parameter failed validation */
     CG_OOM = 4,         /* device or pinned-host allocation failed */
     CG_CUDA = 5,        /* a CUDA call failed; cg_last_error says which */
-    CG_UNSUPPORTED = 6  /* a switch this build does not implement (e.g. profile P2) */
+    CG_UNSUPPORTED = 6  /* a switch the library does not implement (e.g. profile P2) */
 } cg_status;
 
 /* Parity mode. REF32 is the reference's own arithmetic (FP32 field, FP64 where Kotlin promotes). */

@@ -85,7 +85,7 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     }
 
     // cg_profile: P0 without the outlet notch, P1 with it (HydraulicErosion.breach and the closing
-    // breach); deposition is P2, which this build refuses.
+    // breach); deposition is P2, which the library does not run yet.
     private fun profileOf(config: WorldGenConfig): Int = when {
         config.erosion.deposition -> 2
         config.erosion.outletIncision -> 1
