@@ -157,7 +157,7 @@ def test_breach_cuts_only_down_from_its_lips():
                                  c["land_half"], sur)
     assert cells > 0
     changed = np.flatnonzero(sur.ravel() != c["surface"].ravel())
-    assert changed.size == cells
+    assert 0 < changed.size <= cells   # a cell on two basins' channels is cut by each
     assert np.all(sur.ravel()[changed] < c["surface"].ravel()[changed])
     assert np.array_equal(np.flatnonzero(rel.ravel() != c["relative"].ravel()), changed)
     pond = oracle.rates(c["params"])[2]
