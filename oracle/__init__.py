@@ -60,6 +60,9 @@ def lib():
         L.or_erode_stage_switched.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
                                               C.POINTER(abi.Outputs), vp, vp, i32]
         L.or_erode_stage_switched.restype = i32
+        L.or_erode_stage_levels.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
+                                            C.POINTER(abi.Outputs), vp]
+        L.or_erode_stage_levels.restype = i32
         L.or_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)]
         L.or_stand_below_today.argtypes = [C.POINTER(abi.ErosionParams), i32]
         L.or_stand_below_today.restype = f32
@@ -251,6 +254,21 @@ def erode_stage_switched(params, height, uplift=None, rock=None, switches=None, 
                                        int(thermal))
     assert st == 0, st
     return out, tallies
+
+
+def erode_stage_levels(params, height, uplift=None, rock=None):
+    """The stage with the deposition walk in the device's level order; returns (heights, (ponded cells
+    replayed, levels redone))."""
+    H, W = params.height, params.width
+    keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+            for a in (height, uplift, rock)]
+    inputs = abi.Inputs(*[P(a) if a is not None else None for a in keep], None, None)
+    out = np.empty((H, W), np.float32)
+    o = abi.Outputs(height=P(out))
+    repairs = np.zeros(2, np.int64)
+    st = lib().or_erode_stage_levels(C.byref(params), C.byref(inputs), C.byref(o), P(repairs))
+    assert st == 0, st
+    return out, tuple(int(v) for v in repairs)
 
 
 def stand_below_today(params, round_):

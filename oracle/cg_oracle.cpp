@@ -1470,12 +1470,29 @@ struct FanScratch {
     }
 };
 
+// A cell a fan laid into: its settled height and sediment before, and what its settled height gained.
+struct FanTouch {
+    int cell;
+    float settled_before, sediment_before, increment;
+};
+
+// raise() of a fan's deposit into one cell, its settled height following; recorded if asked.
+inline double lay(float* sediment, float* settled, int cell, double amount, float to_relative,
+                  std::vector<FanTouch>* touched) {
+    if (touched) touched->push_back({cell, settled[cell], sediment[cell], 0.0f});
+    double moved = raise(sediment, cell, amount);
+    float increment = (float)(moved * (double)to_relative);
+    settled[cell] += increment;
+    if (touched) touched->back().increment = increment;
+    return moved;
+}
+
 // growFan (DeltaFan.kt): best-first admission of cells inside the rim, distance bent by `advance`,
 // then laying `budget` into the admitted cells nearest first, each up to `level_of` and no higher.
 template <class Accepts, class Advance, class LevelOf>
 double grow_fan(int W, int H, double budget, const Rim& rim, FanScratch& scratch, int id, const float* surface,
-                float* sediment, float* settled, float to_relative, bool whole_cells, Accepts&& accepts,
-                Advance&& advance, LevelOf&& level_of) {
+                float* sediment, float* settled, float to_relative, bool whole_cells,
+                std::vector<FanTouch>* touched, Accepts&& accepts, Advance&& advance, LevelOf&& level_of) {
     int apex = rim.apex;
     if (budget <= 0.0 || !accepts(apex)) return 0.0;
     scratch.size = 0;
@@ -1524,8 +1541,7 @@ double grow_fan(int W, int H, double budget, const Rim& rim, FanScratch& scratch
         double need = (double)level_of(cell, fraction) - (double)surface[cell] - (double)sediment[cell];
         if (need <= 0.0) continue;
         if (whole_cells && need > remaining) break;
-        double moved = raise(sediment, cell, need < remaining ? need : remaining);
-        settled[cell] += (float)(moved * (double)to_relative);
+        double moved = lay(sediment, settled, cell, need < remaining ? need : remaining, to_relative, touched);
         remaining -= moved;
         laid += moved;
     }
@@ -1538,7 +1554,8 @@ double grow_fan(int W, int H, double budget, const Rim& rim, FanScratch& scratch
 template <class Accepts, class LevelOf>
 double square_fan(int W, int H, int start, double budget, int reach_cells, std::vector<int>& stamp, int id,
                   std::vector<int>& queue, std::vector<int>& distance_at, const float* surface, float* sediment,
-                  float* settled, float to_relative, bool whole_cells, Accepts&& accepts, LevelOf&& level_of) {
+                  float* settled, float to_relative, bool whole_cells, std::vector<FanTouch>* touched,
+                  Accepts&& accepts, LevelOf&& level_of) {
     if (budget <= 0.0 || !accepts(start, 0)) return 0.0;
     double remaining = budget, laid = 0.0;
     int head = 0, tail = 0;
@@ -1553,8 +1570,7 @@ double square_fan(int W, int H, int start, double budget, int reach_cells, std::
         double need = (double)level_of(cell, steps) - (double)surface[cell] - (double)sediment[cell];
         if (need > 0.0) {
             if (whole_cells && need > remaining) break;
-            double moved = raise(sediment, cell, need < remaining ? need : remaining);
-            settled[cell] += (float)(moved * (double)to_relative);
+            double moved = lay(sediment, settled, cell, need < remaining ? need : remaining, to_relative, touched);
             remaining -= moved;
             laid += moved;
         }
@@ -1596,68 +1612,104 @@ struct Tally {   // one round's mass budget (RoundMass, HydraulicErosion.kt:1477
 // The deposition walk (HydraulicErosion.kt:1068-1349) over one round's drainage order, sources first:
 // each cell picks up what the incision took off it, settles any surplus over the flow's capacity on a
 // floodplain (never above the ground that feeds it), and hands the rest on; at the sea a river's
-// share builds a lobe, at a lake a share builds a fan. P2's lobes and fans are the outlined ones
-// (growFan).
-void deposition_walk(const cg_erosion_params& p, const Switches& sw, const DepositionRates& dr, const Rates& rates,
-                     const int32_t* order, int order_len, const int32_t* dirs, const u8* is_land,
-                     const float* ground, const float* relative, const float* area, float land_cells,
-                     float land_range, float to_relative, float shoreline, float* surface, float* sediment,
-                     float* settled, double* load, const double* incised_at, FanScratch* scratch,
-                     SquareScratch* square, int& mouth_id, Tally& t) {
-    const int W = p.width, H = p.height;
-    const double r = scale_of(p).cell_height_km(H) / scale_of(p).cell_width_km(W);
-    const int reach_cells = dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells;
-    const float delta_top = shoreline + dr.delta_freeboard * land_range;
-    const float rim_top = shoreline + (delta_top - shoreline) * kLobeRim;
-    const float shelf_depth = dr.shelf_break < 1e-9f ? 1e-9f : dr.shelf_break;
-    for (int rank = 0; rank < order_len; ++rank) {
-        int cell = order[rank];
+// share builds a lobe, at a lake a share builds a fan. The walk's two halves are kept apart (a cell's
+// own walk, then its mouth) so that the level schedule below can reorder them.
+struct DepositionWalk {
+    enum { OFF_MAP = -1, ON = 0, SEA = 1, LAKE = 2 };
+    const cg_erosion_params& p;
+    const Switches& sw;
+    const Rates& rates;
+    const int32_t* dirs;
+    const u8* is_land;
+    const float *ground, *relative, *area;
+    float land_cells, land_range, to_relative, shoreline;
+    float *surface, *sediment, *settled;
+    const double* incised_at;
+    FanScratch* scratch;
+    SquareScratch* square;
+    int& mouth_id;
+    Tally& t;
+    int W, H, reach_cells;
+    double r;
+    float delta_top, rim_top, shelf_depth, delta_min_cells;
+    // Fan deposits of the current mouth as (cell, settled increment), when a caller wants them.
+    std::vector<FanTouch>* touched = nullptr;
+
+    DepositionWalk(const cg_erosion_params& p_, const Switches& sw_, const DepositionRates& dr, const Rates& rates_,
+                   const int32_t* dirs_, const u8* is_land_, const float* ground_, const float* relative_,
+                   const float* area_, float land_cells_, float land_range_, float to_relative_, float shoreline_,
+                   float* surface_, float* sediment_, float* settled_, const double* incised_at_, FanScratch* scratch_,
+                   SquareScratch* square_, int& mouth_id_, Tally& t_)
+        : p(p_), sw(sw_), rates(rates_), dirs(dirs_), is_land(is_land_), ground(ground_), relative(relative_),
+          area(area_), land_cells(land_cells_), land_range(land_range_), to_relative(to_relative_),
+          shoreline(shoreline_), surface(surface_), sediment(sediment_), settled(settled_), incised_at(incised_at_),
+          scratch(scratch_), square(square_), mouth_id(mouth_id_), t(t_) {
+        W = p.width;
+        H = p.height;
+        r = scale_of(p).cell_height_km(H) / scale_of(p).cell_width_km(W);
+        reach_cells = dr.delta_reach_cells < 0 ? 0 : dr.delta_reach_cells;
+        delta_top = shoreline + dr.delta_freeboard * land_range;
+        rim_top = shoreline + (delta_top - shoreline) * kLobeRim;
+        shelf_depth = dr.shelf_break < 1e-9f ? 1e-9f : dr.shelf_break;
+        delta_min_cells = dr.delta_min_cells;
+    }
+
+    bool ponded(int c) const { return ground[c] - relative[c] > rates.pond_depth; }
+
+    // A cell's own walk (HydraulicErosion.kt:1068-1186), `carried` arriving: returns what it carries on
+    // and where it goes. *used_headroom (if given) says whether it read its donors' settled heights.
+    int own(int cell, double& carried, bool* used_headroom = nullptr) {
         int receiver = dirs[cell];
-        double carried = load[cell];
-        if (receiver < 0) {
-            t.lost += carried;
-            continue;
-        }
+        if (used_headroom) *used_headroom = false;
+        if (receiver < 0) return OFF_MAP;
         bool to_sea = !is_land[receiver];
         float drop = fall_to_receiver(ground, is_land, cell, receiver);
-        bool ponded = ground[cell] - relative[cell] > rates.pond_depth;
-        {
-            float distance = rates.steps.between(cell, receiver, W);
-            float slope = drop > 0.0f ? drop / distance * (float)W : 0.0f;
-            double capacity = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells) * slope);
-            double moved = incised_at[cell];
-            if (moved > 0.0) {
-                settled[cell] -= (float)(moved * (double)to_relative);
-                carried += moved;
-                t.incised += moved;
+        bool wet = ponded(cell);
+        float distance = rates.steps.between(cell, receiver, W);
+        float slope = drop > 0.0f ? drop / distance * (float)W : 0.0f;
+        double capacity = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells) * slope);
+        double moved = incised_at[cell];
+        if (moved > 0.0) {
+            settled[cell] -= (float)(moved * (double)to_relative);
+            carried += moved;
+            t.incised += moved;
+        }
+        if (!wet && carried > capacity) {
+            float grade = 0.0f;
+            if (sw.graded_aggradation) {
+                double conveyance = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells));
+                grade = conveyance > 1e-12 ? (float)(carried / conveyance / (double)W) : 0.0f;
             }
-            if (!ponded && carried > capacity) {
-                float grade = 0.0f;
-                if (sw.graded_aggradation) {
-                    double conveyance = (double)(sw.transport_capacity * std::sqrt(area[cell] / land_cells));
-                    grade = conveyance > 1e-12 ? (float)(carried / conveyance / (double)W) : 0.0f;
-                }
-                float room = headroom(W, H, cell, drop, dirs, settled, grade, rates.steps) * land_range;
-                double give = jvm_min(carried - capacity, (double)room) * (double)sw.deposition_rate;
-                if (give > 0.0) {
-                    double laid = raise(sediment, cell, give);
-                    settled[cell] += (float)(laid * (double)to_relative);
-                    carried -= laid;
-                    t.deposited += laid;
-                }
+            if (used_headroom) *used_headroom = true;
+            float room = headroom(W, H, cell, drop, dirs, settled, grade, rates.steps) * land_range;
+            double give = jvm_min(carried - capacity, (double)room) * (double)sw.deposition_rate;
+            if (give > 0.0) {
+                double laid = raise(sediment, cell, give);
+                settled[cell] += (float)(laid * (double)to_relative);
+                carried -= laid;
+                t.deposited += laid;
             }
         }
-        if (to_sea) {
-            bool river = area[cell] >= dr.delta_min_cells;
-            float out_x = (float)shortest_x(receiver % W - cell % W, W);
-            float out_y = (float)(receiver / W - cell / W);
+        if (to_sea) return SEA;
+        if (!wet && ponded(receiver)) return LAKE;
+        return ON;
+    }
+
+    // A cell's mouth (HydraulicErosion.kt:1187-1349): the lobe at the sea or the fan in a lake. Returns
+    // what it laid; the caller hands the rest on (lake) or counts it lost (sea).
+    double mouth(int cell, double carried, int kind) {
+        int receiver = dirs[cell];
+        float out_x = (float)shortest_x(receiver % W - cell % W, W);
+        float out_y = (float)(receiver / W - cell / W);
+        double laid;
+        if (kind == SEA) {
+            bool river = area[cell] >= delta_min_cells;
             double budget = river ? carried * (double)sw.delta_share : 0.0;
-            double laid;
             if (!(sw.delta_lobe && sw.delta_outline)) {
                 // The square lobe, or with the lobe off the flat slab (HydraulicErosion.kt:1230-1253).
                 laid = square_fan(
                     W, H, receiver, budget, reach_cells, square->stamp, ++mouth_id, square->queue, square->distance_at,
-                    surface, sediment, settled, to_relative, sw.delta_lobe,
+                    surface, sediment, settled, to_relative, sw.delta_lobe, touched,
                     [&](int c, int steps) {
                         return !is_land[c] &&
                                (!sw.delta_lobe || steps <= lobe_reach(reach_cells, receiver, c, out_x, out_y, W));
@@ -1665,52 +1717,46 @@ void deposition_walk(const cg_erosion_params& p, const Switches& sw, const Depos
                     [&](int, int steps) {
                         return sw.delta_lobe ? lobe_level(delta_top, shoreline, reach_cells, steps) : delta_top;
                     });
-                t.deposited += laid;
-                t.lost += carried - laid;
-                continue;
+            } else {
+                Rim rim(receiver, W, r, (float)reach_cells, out_x, out_y,
+                        fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), true);
+                rim.prune_grooves(H, [&](int c) { return !is_land[c]; });
+                laid = grow_fan(
+                    W, H, budget, rim, *scratch, ++mouth_id, surface, sediment, settled, to_relative, true, touched,
+                    [&](int c) { return !is_land[c]; },
+                    [&](int c) {
+                        float depth = shoreline - (surface[c] + sediment[c]);
+                        return 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / shelf_depth;
+                    },
+                    [&](int c, float fraction) {
+                        float level = delta_top + (rim_top - delta_top) * fraction;
+                        if (rim.grooved(rim.column_offset(c), rim.row_offset(c)))
+                            return shoreline + (level - shoreline) * kGrooveKeep;
+                        return level;
+                    });
             }
-            Rim rim(receiver, W, r, (float)reach_cells, out_x, out_y,
-                    fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), true);
-            rim.prune_grooves(H, [&](int c) { return !is_land[c]; });
-            laid = grow_fan(
-                W, H, budget, rim, *scratch, ++mouth_id, surface, sediment, settled, to_relative, true,
-                [&](int c) { return !is_land[c]; },
-                [&](int c) {
-                    float depth = shoreline - (surface[c] + sediment[c]);
-                    return 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / shelf_depth;
-                },
-                [&](int c, float fraction) {
-                    float level = delta_top + (rim_top - delta_top) * fraction;
-                    if (rim.grooved(rim.column_offset(c), rim.row_offset(c)))
-                        return shoreline + (level - shoreline) * kGrooveKeep;
-                    return level;
-                });
             t.deposited += laid;
             t.lost += carried - laid;
-        } else if (!ponded && ground[receiver] - relative[receiver] > rates.pond_depth) {
-            float in_x = (float)shortest_x(receiver % W - cell % W, W);
-            float in_y = (float)(receiver / W - cell / W);
-            if (!sw.delta_outline) {   // the square lake fan (HydraulicErosion.kt:1321-1344)
-                double laid = square_fan(
-                    W, H, receiver, carried * (double)sw.lake_share, reach_cells, square->stamp, ++mouth_id,
-                    square->queue, square->distance_at, surface, sediment, settled, to_relative, false,
-                    [&](int c, int) { return is_land[c] && ground[c] - relative[c] > rates.pond_depth; },
-                    [&](int c, int steps) {
-                        float depth = 2.0f * rates.pond_depth *
-                                      (1.0f + kLakeFanSlope * (float)steps / (float)(reach_cells < 1 ? 1 : reach_cells)) *
-                                      (0.9f + 0.35f * cell_wobble(c));
-                        return shoreline + (ground[c] - depth) * land_range;
-                    });
-                t.deposited += laid;
-                load[receiver] += carried - laid;
-                continue;
-            }
-            Rim rim(receiver, W, r, (float)reach_cells, in_x, in_y,
+            return laid;
+        }
+        if (!sw.delta_outline) {   // the square lake fan (HydraulicErosion.kt:1321-1344)
+            laid = square_fan(
+                W, H, receiver, carried * (double)sw.lake_share, reach_cells, square->stamp, ++mouth_id,
+                square->queue, square->distance_at, surface, sediment, settled, to_relative, false, touched,
+                [&](int c, int) { return is_land[c] && ponded(c); },
+                [&](int c, int steps) {
+                    float depth = 2.0f * rates.pond_depth *
+                                  (1.0f + kLakeFanSlope * (float)steps / (float)(reach_cells < 1 ? 1 : reach_cells)) *
+                                  (0.9f + 0.35f * cell_wobble(c));
+                    return shoreline + (ground[c] - depth) * land_range;
+                });
+        } else {
+            Rim rim(receiver, W, r, (float)reach_cells, out_x, out_y,
                     fan_hash(p.seed, mouth_key(receiver, reach_cells, W)), false);
-            double laid = grow_fan(
+            laid = grow_fan(
                 W, H, carried * (double)sw.lake_share, rim, *scratch, ++mouth_id, surface, sediment, settled,
-                to_relative, false,
-                [&](int c) { return is_land[c] && ground[c] - relative[c] > rates.pond_depth; },
+                to_relative, false, touched,
+                [&](int c) { return is_land[c] && ponded(c); },
                 [&](int c) {
                     float depth = (ground[c] - relative[c]) * land_range;
                     return 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / shelf_depth;
@@ -1720,11 +1766,164 @@ void deposition_walk(const cg_erosion_params& p, const Switches& sw, const Depos
                                   (0.9f + 0.35f * cell_wobble(c));
                     return shoreline + (ground[c] - depth) * land_range;
                 });
-            t.deposited += laid;
-            load[receiver] += carried - laid;
-        } else {
-            load[receiver] += carried;
         }
+        t.deposited += laid;
+        return laid;
+    }
+
+    // The reference's order: one cell after another, load[] gathering each hand-off as it is made.
+    void run(const int32_t* order, int order_len, double* load) {
+        for (int rank = 0; rank < order_len; ++rank) {
+            int cell = order[rank];
+            double carried = load[cell];
+            int kind = own(cell, carried);
+            if (kind == OFF_MAP) t.lost += carried;   // off the polar edge, with whatever it carries
+            else if (kind == SEA) mouth(cell, carried, kind);
+            else if (kind == LAKE) load[dirs[cell]] += carried - mouth(cell, carried, kind);
+            else load[dirs[cell]] += carried;
+        }
+    }
+};
+
+// How often the level schedule had to repair a level (see run_levels).
+struct LevelRepairs {
+    long replayed = 0;   // ponded cells of a fan's own level, ranked after it, whose settled height was replayed
+    long redone = 0;     // levels restored and walked again one cell after another
+};
+
+// The same walk in the order a device runs it, to show that this order gives the reference's bits.
+// The Kahn order is level-major, so the walk goes level by level from the sources. In a level every
+// cell first does its own walk (cells of one level never read one another: a cell reads its own state
+// and its donors', which are lower), its load being its notch hand-off plus its donors' hand-offs in
+// rank order, the reference's additions in the reference's order. Then the level's mouths run in rank
+// order. A fan changes only sea cells and ponded land cells, which no own walk reads, except (a) a
+// ponded cell of the fan's level ranked after it, whose settled height took its own subtraction before
+// the fan's addition instead of after: replayed in rank order; and (b) a donor whose settled height a
+// later cell of the level read in its headroom: the level is restored and walked one cell after another.
+void run_levels(DepositionWalk& w, const int32_t* order, int order_len, const double* notch_load, size_t N,
+                LevelRepairs& repairs) {
+    const int32_t* dirs = w.dirs;
+    const u8* land = w.is_land;
+    std::vector<int> level(N, -1), rank_of(N, -1);
+    for (int k = 0; k < order_len; ++k) {
+        level[order[k]] = 0;
+        rank_of[order[k]] = k;
+    }
+    for (int k = 0; k < order_len; ++k) {
+        int c = order[k], rr = dirs[c];
+        if (rr >= 0 && land[rr]) level[rr] = std::max(level[rr], level[c] + 1);
+    }
+    std::vector<int> dstart(N + 1, 0), donors;   // donors in rank order
+    for (int k = 0; k < order_len; ++k) {
+        int rr = dirs[order[k]];
+        if (rr >= 0 && land[rr]) dstart[rr + 1]++;
+    }
+    for (size_t c = 0; c < N; ++c) dstart[c + 1] += dstart[c];
+    donors.resize(dstart[N]);
+    {
+        std::vector<int> next(dstart.begin(), dstart.end() - 1);
+        for (int k = 0; k < order_len; ++k) {
+            int c = order[k], rr = dirs[c];
+            if (rr >= 0 && land[rr]) donors[next[rr]++] = c;
+        }
+    }
+    std::vector<double> handoff(N, 0.0);
+    std::vector<char> used(N, 0);
+    auto arriving = [&](int c) {
+        double carried = notch_load[c];
+        for (int k = dstart[c]; k < dstart[c + 1]; ++k) carried += handoff[donors[k]];
+        return carried;
+    };
+    auto walk_one = [&](int c) {   // a cell's whole step, the reference's way
+        double carried = arriving(c);
+        int kind = w.own(c, carried);
+        if (kind == DepositionWalk::OFF_MAP) w.t.lost += carried;
+        else if (kind == DepositionWalk::SEA) w.mouth(c, carried, kind);
+        else if (kind == DepositionWalk::LAKE) handoff[c] = carried - w.mouth(c, carried, kind);
+        else handoff[c] = carried;
+    };
+    struct Event {
+        int rank, cell, kind;
+        double carried;
+        std::vector<FanTouch> touched;
+    };
+    int lo = 0;
+    while (lo < order_len) {
+        const int L = level[order[lo]];
+        int hi = lo;
+        while (hi < order_len && level[order[hi]] == L) ++hi;
+        const Tally t0 = w.t;
+        std::vector<float> settled0(hi - lo), sediment0(hi - lo);
+        for (int k = lo; k < hi; ++k) {
+            settled0[k - lo] = w.settled[order[k]];
+            sediment0[k - lo] = w.sediment[order[k]];
+        }
+        std::vector<Event> events;
+        for (int k = lo; k < hi; ++k) {   // every own walk of the level, as if at once
+            int c = order[k];
+            double carried = arriving(c);
+            bool used_headroom = false;
+            int kind = w.own(c, carried, &used_headroom);
+            used[c] = used_headroom;
+            if (kind == DepositionWalk::OFF_MAP) w.t.lost += carried;
+            else if (kind == DepositionWalk::ON) handoff[c] = carried;
+            else events.push_back({k, c, kind, carried, {}});
+        }
+        for (Event& e : events) {   // the mouths, in rank order
+            w.touched = &e.touched;
+            double laid = w.mouth(e.cell, e.carried, e.kind);
+            w.touched = nullptr;
+            if (e.kind == DepositionWalk::LAKE) handoff[e.cell] = e.carried - laid;
+        }
+        bool redo = false;
+        std::vector<int> replay;
+        for (const Event& e : events)
+            for (const FanTouch& f : e.touched) {
+                int x = f.cell;
+                if (!land[x]) continue;
+                if (level[x] == L && rank_of[x] > e.rank) replay.push_back(x);
+                int rr = dirs[x];
+                if (rr >= 0 && land[rr] && level[rr] == L && rank_of[rr] > e.rank && used[rr]) redo = true;
+            }
+        if (redo) {
+            repairs.redone++;
+            for (auto e = events.rbegin(); e != events.rend(); ++e)
+                for (auto f = e->touched.rbegin(); f != e->touched.rend(); ++f) {
+                    w.settled[f->cell] = f->settled_before;
+                    w.sediment[f->cell] = f->sediment_before;
+                }
+            for (int k = lo; k < hi; ++k) {
+                w.settled[order[k]] = settled0[k - lo];
+                w.sediment[order[k]] = sediment0[k - lo];
+            }
+            w.t = t0;
+            for (int k = lo; k < hi; ++k) walk_one(order[k]);
+        } else if (!replay.empty()) {
+            std::sort(replay.begin(), replay.end());
+            replay.erase(std::unique(replay.begin(), replay.end()), replay.end());
+            for (int x : replay) {
+                repairs.replayed++;
+                // The cell's own subtraction and the fans' increments, in rank order.
+                std::vector<std::pair<int, float>> ops;   // (rank, increment); the own op marked by rank_of[x]
+                for (const Event& e : events)
+                    for (const FanTouch& f : e.touched)
+                        if (f.cell == x) ops.push_back({e.rank, f.increment});
+                float v = settled0[rank_of[x] - lo];
+                bool own_done = false;
+                auto own_op = [&]() {
+                    double moved = w.incised_at[x];
+                    if (moved > 0.0) v -= (float)(moved * (double)w.to_relative);
+                    own_done = true;
+                };
+                for (const auto& op : ops) {
+                    if (!own_done && op.first > rank_of[x]) own_op();
+                    v += op.second;
+                }
+                if (!own_done) own_op();
+                w.settled[x] = v;
+            }
+        }
+        lo = hi;
     }
 }
 
@@ -1791,7 +1990,8 @@ struct StageOut {
 // round) and initial = false leaves out the initial sweeps: a bounded sample of a stage.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
                 bool with_thermal = true, bool initial = true, int run_rounds = -1,
-                const Switches* switches = nullptr, Tally* tallies = nullptr) {
+                const Switches* switches = nullptr, Tally* tallies = nullptr,
+                LevelRepairs* level_repairs = nullptr) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -1900,11 +2100,14 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
         incise(rates, W, N, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(), filled.data(),
                cut.relative.data(), area.data(), land_cells, land_range, cut.shoreline, erod.data(), working.data(),
                p.receiver_clamp != 0, nullptr, sw.deposition ? incised_at.data() : nullptr);
-        if (sw.deposition)
-            deposition_walk(p, sw, dr, rates, order.data(), cut.land_cells, dirs.data(), cut.is_land.data(),
-                            filled.data(), cut.relative.data(), area.data(), land_cells, land_range, to_relative,
-                            cut.shoreline, working.data(), sediment.data(), settled.data(), load.data(),
-                            incised_at.data(), scratch.get(), square.get(), mouth_id, t);
+        if (sw.deposition) {
+            DepositionWalk walk(p, sw, dr, rates, dirs.data(), cut.is_land.data(), filled.data(), cut.relative.data(),
+                                area.data(), land_cells, land_range, to_relative, cut.shoreline, working.data(),
+                                sediment.data(), settled.data(), incised_at.data(), scratch.get(), square.get(),
+                                mouth_id, t);
+            if (level_repairs) run_levels(walk, order.data(), cut.land_cells, load.data(), N, *level_repairs);
+            else walk.run(order.data(), cut.land_cells, load.data());
+        }
         if (stats) {
             cg_round_stats& s = stats[round];
             std::memset(&s, 0, sizeof(s));
@@ -2208,6 +2411,18 @@ int32_t or_erode_stage_switched(const cg_erosion_params* p, const cg_inputs* in,
             tallies[4 * i + 2] = t[i].lost;
             tallies[4 * i + 3] = t[i].field_drop;
         }
+    return st;
+}
+
+// The stage with the deposition walk run in the device's level order (run_levels); repairs (may be
+// NULL) receives the ponded cells replayed and the levels redone over the whole stage.
+int32_t or_erode_stage_levels(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, int64_t* repairs) {
+    LevelRepairs r;
+    int st = erode_stage(*p, *in, out, nullptr, true, true, -1, nullptr, nullptr, &r);
+    if (repairs) {
+        repairs[0] = r.replayed;
+        repairs[1] = r.redone;
+    }
     return st;
 }
 

@@ -83,3 +83,20 @@ def test_fan_shapes_differ():
         for j in range(i + 1, 3):
             assert not np.array_equal(bits(outs[i]), bits(outs[j]))
 
+
+
+@pytest.mark.parametrize("W,H,seed,uplift,replays,redos", [
+    (512, 256, 7, "bands", 1, 0),
+    (2048, 1024, 1, "ridges", 1, 1),
+])
+def test_level_schedule_reproduces_the_walk(W, H, seed, uplift, replays, redos):
+    """The deposition walk in the order a device runs it (level by level, each level's own walks at
+    once, then its mouths in rank order, with the two repairs for fans that reach into their own level)
+    gives the reference order's bits over the whole P2 stage; the worlds are chosen so that the repairs
+    happen (at least the given counts)."""
+    h, up, rk = synthetic.world(W, H, seed, uplift=uplift)
+    p = oracle.default_params(W, H, seed, sea_level=0.70, profile=2)
+    walk = oracle.erode_stage(p, h, up, rk, want=())["height"]
+    levels, (replayed, redone) = oracle.erode_stage_levels(p, h, up, rk)
+    assert np.array_equal(bits(levels), bits(walk))
+    assert replayed >= replays and redone >= redos
