@@ -23,8 +23,6 @@
 // on another SM are read through L2 (ld.cg) and written through it.
 #include <cooperative_groups.h>
 
-#include <climits>
-
 #include "cg_common.cuh"
 #include "cg_internal.h"
 #include "cg_util.h"
