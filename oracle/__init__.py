@@ -63,6 +63,8 @@ def lib():
         L.or_erode_stage_levels.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
                                             C.POINTER(abi.Outputs), vp]
         L.or_erode_stage_levels.restype = i32
+        L.or_capture_walk.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), i32] + [vp] * 16
+        L.or_capture_walk.restype = i32
         L.or_rates.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)]
         L.or_stand_below_today.argtypes = [C.POINTER(abi.ErosionParams), i32]
         L.or_stand_below_today.restype = f32
@@ -269,6 +271,32 @@ def erode_stage_levels(params, height, uplift=None, rock=None):
     st = lib().or_erode_stage_levels(C.byref(params), C.byref(inputs), C.byref(o), P(repairs))
     assert st == 0, st
     return out, tuple(int(v) for v in repairs)
+
+
+def capture_walk(params, height, uplift=None, rock=None, round_=0):
+    """The P2 stage's deposition walk of one round: its inputs and, after the reference's order, the
+    sediment, settled heights and loads. Returns a dict of arrays and scalars."""
+    H, W = params.height, params.width
+    N = W * H
+    keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+            for a in (height, uplift, rock)]
+    inputs = abi.Inputs(*[P(a) if a is not None else None for a in keep], None, None)
+    spec = [("order", np.int32), ("dirs", np.int32), ("land", np.uint8), ("ground", np.float32),
+            ("relative", np.float32), ("area", np.float32), ("surface", np.float32), ("sediment", np.float32),
+            ("settled", np.float32), ("load", np.float64), ("incised_at", np.float64)]
+    a = {k: np.zeros(N, dt) for k, dt in spec}
+    scalars = np.zeros(4, np.float32)
+    ints = np.zeros(2, np.int32)
+    after = {k: np.zeros(N, dt) for k, dt in [("sediment_after", np.float32), ("settled_after", np.float32),
+                                               ("load_after", np.float64)]}
+    st = lib().or_capture_walk(C.byref(params), C.byref(inputs), round_, *[P(a[k]) for k, _ in spec], P(scalars),
+                               P(ints), *[P(v) for v in after.values()])
+    assert st == 0, st
+    a.update(after)
+    a["order"] = a["order"][:ints[0]]
+    a.update(land_cells=float(scalars[0]), land_range=float(scalars[1]), to_relative=float(scalars[2]),
+             shoreline=float(scalars[3]), mouth_id=int(ints[1]))
+    return a
 
 
 def stand_below_today(params, round_):

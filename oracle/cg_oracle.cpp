@@ -1605,6 +1605,21 @@ struct SquareScratch {
           distance_at((size_t)(2 * reach_cells + 1) * (2 * reach_cells + 1)) {}
 };
 
+// One round's deposition walk captured for tests of the device's walk: its inputs just before the
+// walk and the fields it changed just after (the reference's order).
+struct WalkCapture {
+    int round = -1;
+    bool taken = false;
+    std::vector<int32_t> order, dirs;
+    std::vector<u8> land;
+    std::vector<float> ground, relative, area, surface, sediment, settled;
+    std::vector<double> load, incised_at;
+    float land_cells = 0, land_range = 0, to_relative = 0, shoreline = 0;
+    int mouth_id = 0;
+    std::vector<float> sediment_after, settled_after;
+    std::vector<double> load_after;
+};
+
 struct Tally {   // one round's mass budget (RoundMass, HydraulicErosion.kt:1477-1484)
     double incised = 0.0, deposited = 0.0, lost = 0.0, field_drop = 0.0;
 };
@@ -1991,7 +2006,7 @@ struct StageOut {
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
                 bool with_thermal = true, bool initial = true, int run_rounds = -1,
                 const Switches* switches = nullptr, Tally* tallies = nullptr,
-                LevelRepairs* level_repairs = nullptr) {
+                LevelRepairs* level_repairs = nullptr, WalkCapture* capture = nullptr) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -2105,8 +2120,34 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
                                 area.data(), land_cells, land_range, to_relative, cut.shoreline, working.data(),
                                 sediment.data(), settled.data(), incised_at.data(), scratch.get(), square.get(),
                                 mouth_id, t);
+            const bool capturing = capture && round == capture->round;
+            if (capturing) {
+                WalkCapture& c = *capture;
+                c.taken = true;
+                c.order = order;
+                c.dirs = dirs;
+                c.land = cut.is_land;
+                c.ground = filled;
+                c.relative = cut.relative;
+                c.area = area;
+                c.surface = working;
+                c.sediment = sediment;
+                c.settled = settled;
+                c.load = load;
+                c.incised_at = incised_at;
+                c.land_cells = land_cells;
+                c.land_range = land_range;
+                c.to_relative = to_relative;
+                c.shoreline = cut.shoreline;
+                c.mouth_id = mouth_id;
+            }
             if (level_repairs) run_levels(walk, order.data(), cut.land_cells, load.data(), N, *level_repairs);
             else walk.run(order.data(), cut.land_cells, load.data());
+            if (capturing) {
+                capture->sediment_after = sediment;
+                capture->settled_after = settled;
+                capture->load_after = load;
+            }
         }
         if (stats) {
             cg_round_stats& s = stats[round];
@@ -2424,6 +2465,45 @@ int32_t or_erode_stage_levels(const cg_erosion_params* p, const cg_inputs* in, c
         repairs[1] = r.redone;
     }
     return st;
+}
+
+// The P2 stage's deposition walk of round `round`, captured: the walk's inputs (N-cell arrays, the
+// order holding order_len cells) and, after it, the sediment, settled heights and loads (the load a
+// cell passes on is its arriving load). scalars: land_cells, land_range, to_relative, shoreline;
+// ints: order_len, the mouth id before the walk. Returns 0 if the round was reached.
+int32_t or_capture_walk(const cg_erosion_params* p, const cg_inputs* in, int32_t round, int32_t* order,
+                        int32_t* dirs, uint8_t* land, float* ground, float* relative, float* area, float* surface,
+                        float* sediment, float* settled, double* load, double* incised_at, float* scalars,
+                        int32_t* ints, float* sediment_after, float* settled_after, double* load_after) {
+    size_t N = (size_t)p->width * p->height;
+    std::vector<float> height(N);
+    cg_outputs out{};
+    out.height = height.data();
+    WalkCapture c;
+    c.round = round;
+    int st = erode_stage(*p, *in, &out, nullptr, true, true, -1, nullptr, nullptr, nullptr, &c);
+    if (st != CG_OK || !c.taken) return 1;
+    std::memcpy(order, c.order.data(), c.order.size() * 4);
+    std::memcpy(dirs, c.dirs.data(), N * 4);
+    std::memcpy(land, c.land.data(), N);
+    std::memcpy(ground, c.ground.data(), N * 4);
+    std::memcpy(relative, c.relative.data(), N * 4);
+    std::memcpy(area, c.area.data(), N * 4);
+    std::memcpy(surface, c.surface.data(), N * 4);
+    std::memcpy(sediment, c.sediment.data(), N * 4);
+    std::memcpy(settled, c.settled.data(), N * 4);
+    std::memcpy(load, c.load.data(), N * 8);
+    std::memcpy(incised_at, c.incised_at.data(), N * 8);
+    scalars[0] = c.land_cells;
+    scalars[1] = c.land_range;
+    scalars[2] = c.to_relative;
+    scalars[3] = c.shoreline;
+    ints[0] = (int32_t)c.order.size();
+    ints[1] = c.mouth_id;
+    std::memcpy(sediment_after, c.sediment_after.data(), N * 4);
+    std::memcpy(settled_after, c.settled_after.data(), N * 4);
+    std::memcpy(load_after, c.load_after.data(), N * 8);
+    return 0;
 }
 
 int32_t or_stage_rounds(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, int32_t rounds) {

@@ -1,0 +1,157 @@
+// The device's deposition logic (cartogenesis_gb300/csrc/cg_deposit.cuh) built for the host, run on a
+// round captured from the oracle in the reference's order and in the device's level order, so that
+// tests can hold both against the oracle's own walk.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../cartogenesis_gb300/csrc/cg_deposit.cuh"
+
+using namespace cg::dep;
+
+extern "C" {
+
+// mode 0: the reference's order; mode 1: level by level (own walks, then the level's mouths in rank
+// order, with the two repairs). arriving[] receives each cell's arriving load (the notch's hand-off
+// plus its donors'). repairs[0..1]: ponded cells replayed, levels redone.
+int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land_range, float to_relative,
+             float shoreline, const int32_t* order, int order_len, const int32_t* dirs, const uint8_t* land,
+             const float* ground, const float* relative, const float* area, const float* surface, float* sediment,
+             float* settled, const double* load0, const double* incised_at, int first_id, double* arriving,
+             long* repairs) {
+    const Params p = make_params(*cp, land_cells, land_range, to_relative, shoreline);
+    const size_t N = (size_t)p.W * p.H;
+    const Fields f{dirs, land, ground, relative, area, surface, sediment, settled, incised_at};
+    std::vector<int> stamp(N, 0);
+    const int cap = heap_capacity(p);
+    std::vector<int> hc(cap), ha(cap);
+    std::vector<float> hk(cap), hp(cap);
+    Heap heap{hc.data(), hk.data(), hp.data(), ha.data(), cap, 0, 0};
+    int id = first_id;
+    double incised = 0, deposited = 0;
+    repairs[0] = repairs[1] = 0;
+    if (mode == 0) {
+        std::vector<double> load(load0, load0 + N);
+        for (int k = 0; k < order_len; ++k) {
+            int c = order[k];
+            double carried = load[c];
+            bool used;
+            int kind = own_walk(p, f, c, carried, &used, &incised, &deposited);
+            if (kind == SEA) mouth(p, f, c, carried, kind, stamp.data(), ++id, heap, nullptr);
+            else if (kind == LAKE) load[dirs[c]] += carried - mouth(p, f, c, carried, kind, stamp.data(), ++id, heap, nullptr);
+            else if (kind == ON) load[dirs[c]] += carried;
+        }
+        std::memcpy(arriving, load.data(), N * 8);
+        return 0;
+    }
+    // Levels.
+    std::vector<int> level(N, -1), rank_of(N, -1);
+    for (int k = 0; k < order_len; ++k) level[order[k]] = 0, rank_of[order[k]] = k;
+    for (int k = 0; k < order_len; ++k) {
+        int c = order[k], r = dirs[c];
+        if (r >= 0 && land[r]) level[r] = std::max(level[r], level[c] + 1);
+    }
+    std::vector<int> dstart(N + 1, 0), donors;
+    for (int k = 0; k < order_len; ++k) {
+        int r = dirs[order[k]];
+        if (r >= 0 && land[r]) dstart[r + 1]++;
+    }
+    for (size_t c = 0; c < N; ++c) dstart[c + 1] += dstart[c];
+    donors.resize(dstart[N]);
+    {
+        std::vector<int> next(dstart.begin(), dstart.end() - 1);
+        for (int k = 0; k < order_len; ++k) {
+            int c = order[k], r = dirs[c];
+            if (r >= 0 && land[r]) donors[next[r]++] = c;
+        }
+    }
+    std::vector<double> handoff(N, 0.0);
+    std::vector<char> used(N, 0);
+    auto arrive = [&](int c) {
+        double v = load0[c];
+        for (int k = dstart[c]; k < dstart[c + 1]; ++k) v += handoff[donors[k]];
+        return v;
+    };
+    struct Event {
+        int rank, cell, kind;
+        double carried;
+        std::vector<Touch> touches;
+    };
+    std::vector<Touch> buffer(cap);
+    int lo = 0;
+    while (lo < order_len) {
+        const int L = level[order[lo]];
+        int hi = lo;
+        while (hi < order_len && level[order[hi]] == L) ++hi;
+        std::vector<float> settled0(hi - lo), sediment0(hi - lo);
+        for (int k = lo; k < hi; ++k) settled0[k - lo] = settled[order[k]], sediment0[k - lo] = sediment[order[k]];
+        std::vector<Event> events;
+        for (int k = lo; k < hi; ++k) {
+            int c = order[k];
+            double carried = arrive(c);
+            bool u;
+            int kind = own_walk(p, f, c, carried, &u, &incised, &deposited);
+            used[c] = u;
+            if (kind == ON) handoff[c] = carried;
+            else if (kind == SEA || kind == LAKE) events.push_back({k, c, kind, carried, {}});
+        }
+        for (Event& e : events) {
+            TouchLog log{buffer.data(), cap, 0, 0};
+            double laid = mouth(p, f, e.cell, e.carried, e.kind, stamp.data(), ++id, heap, &log);
+            if (log.overflow) return 2;
+            e.touches.assign(buffer.begin(), buffer.begin() + log.count);
+            if (e.kind == LAKE) handoff[e.cell] = e.carried - laid;
+        }
+        bool redo = false;
+        std::vector<int> replay;
+        for (const Event& e : events)
+            for (const Touch& t : e.touches) {
+                int x = t.cell;
+                if (!land[x]) continue;
+                if (level[x] == L && rank_of[x] > e.rank) replay.push_back(x);
+                int r = dirs[x];
+                if (r >= 0 && land[r] && level[r] == L && rank_of[r] > e.rank && used[r]) redo = true;
+            }
+        if (redo) {
+            repairs[1]++;
+            for (auto e = events.rbegin(); e != events.rend(); ++e)
+                for (auto t = e->touches.rbegin(); t != e->touches.rend(); ++t)
+                    settled[t->cell] = t->settled_before, sediment[t->cell] = t->sediment_before;
+            for (int k = lo; k < hi; ++k) settled[order[k]] = settled0[k - lo], sediment[order[k]] = sediment0[k - lo];
+            for (int k = lo; k < hi; ++k) {
+                int c = order[k];
+                double carried = arrive(c);
+                bool u;
+                int kind = own_walk(p, f, c, carried, &u, &incised, &deposited);
+                if (kind == ON) handoff[c] = carried;
+                else if (kind == SEA) mouth(p, f, c, carried, kind, stamp.data(), ++id, heap, nullptr);
+                else if (kind == LAKE) handoff[c] = carried - mouth(p, f, c, carried, kind, stamp.data(), ++id, heap, nullptr);
+            }
+        } else if (!replay.empty()) {
+            std::sort(replay.begin(), replay.end());
+            replay.erase(std::unique(replay.begin(), replay.end()), replay.end());
+            for (int x : replay) {
+                repairs[0]++;
+                float v = settled0[rank_of[x] - lo];
+                bool own_done = false;
+                auto own_op = [&]() {
+                    if (incised_at[x] > 0.0) v -= (float)(incised_at[x] * (double)p.to_relative);
+                    own_done = true;
+                };
+                for (const Event& e : events)
+                    for (const Touch& t : e.touches)
+                        if (t.cell == x) {
+                            if (!own_done && e.rank > rank_of[x]) own_op();
+                            v += t.increment;
+                        }
+                if (!own_done) own_op();
+                settled[x] = v;
+            }
+        }
+        lo = hi;
+    }
+    for (size_t c = 0; c < N; ++c) arriving[c] = land[c] ? arrive((int)c) : load0[c];
+    return 0;
+}
+
+}  // extern "C"
