@@ -1,5 +1,5 @@
-// Profile P2's deposition, the per-cell logic shared by the device kernels (cg_deposit.cu) and a host
-// build of the same code that tests run against the oracle: a cell's own walk and its mouth
+// Profile P2's deposition, the per-cell logic for the device kernels of the deposition walk, built
+// for the host too so that tests can run it against the oracle: a cell's own walk and its mouth
 // (HydraulicErosion.kt:1068-1349), the floodplain's headroom (HydraulicErosion.kt:2400-2424), the
 // outlined lobes and lake fans (DeltaFan.kt: Rim, Scratch, growFan) and the helpers they hash with.
 //
