@@ -2,6 +2,8 @@
 // round captured from the oracle in the reference's order and in the device's level order, so that
 // tests can hold both against the oracle's own walk.
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -12,8 +14,9 @@ using namespace cg::dep;
 extern "C" {
 
 // mode 0: the reference's order; mode 1: level by level (own walks, then the level's mouths in rank
-// order, with the two repairs). arriving[] receives each cell's arriving load (the notch's hand-off
-// plus its donors'). repairs[0..1]: ponded cells replayed, levels redone.
+// order, with the two repairs); mode 2: mode 1 with each level's mouths in waves of fans whose reaches
+// do not overlap. arriving[] receives each cell's arriving load (the notch's hand-off plus its
+// donors'). repairs[0..2]: ponded cells replayed, levels redone, fan waves.
 int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land_range, float to_relative,
              float shoreline, const int32_t* order, int order_len, const int32_t* dirs, const uint8_t* land,
              const float* ground, const float* relative, const float* area, const float* surface, float* sediment,
@@ -29,7 +32,7 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
     Heap heap{hc.data(), hk.data(), hp.data(), ha.data(), cap, 0, 0};
     int id = first_id;
     double incised = 0, deposited = 0;
-    repairs[0] = repairs[1] = 0;
+    repairs[0] = repairs[1] = repairs[2] = 0;
     if (mode == 0) {
         std::vector<double> load(load0, load0 + N);
         for (int k = 0; k < order_len; ++k) {
@@ -95,12 +98,61 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
             if (kind == ON) handoff[c] = carried;
             else if (kind == SEA || kind == LAKE) events.push_back({k, c, kind, carried, {}});
         }
-        for (Event& e : events) {
+        auto run_fan = [&](Event& e) {
             TouchLog log{buffer.data(), cap, 0, 0};
             double laid = mouth(p, f, e.cell, e.carried, e.kind, stamp.data(), ++id, heap, &log);
-            if (log.overflow) return 2;
+            if (log.overflow) return false;
             e.touches.assign(buffer.begin(), buffer.begin() + log.count);
             if (e.kind == LAKE) handoff[e.cell] = e.carried - laid;
+            return true;
+        };
+        if (mode == 1) {
+            for (Event& e : events)
+                if (!run_fan(e)) return 2;
+        } else {
+            // Waves: a fan runs once no earlier waiting fan's reach overlaps its own (the rim's widest
+            // reach, 1.3 reach cells, plus the neighbours its admission reads); a wave's fans run in
+            // reverse rank order, which only disjoint fans can afford.
+            const int bx = (int)std::ceil(1.3 * p.reach_cells) + 1;
+            const int by = (int)std::ceil(1.3 * p.reach_cells / p.r) + 1;
+            auto overlap = [&](int a, int b) {
+                int dx = std::abs(a % p.W - b % p.W);
+                dx = std::min(dx, p.W - dx);
+                int dy = std::abs(a / p.W - b / p.W);
+                return dx <= 2 * bx && dy <= 2 * by;
+            };
+            // Earlier waiting fans are looked up in coarse blocks of the map, one block a reach wide.
+            const int sx = 2 * bx + 1, sy = 2 * by + 1;
+            const int nbx = (p.W + sx - 1) / sx, nby = (p.H + sy - 1) / sy;
+            std::vector<int> waiting(events.size());
+            for (size_t i = 0; i < events.size(); ++i) waiting[i] = (int)i;
+            while (!waiting.empty()) {
+                std::vector<std::vector<int>> block(nbx * nby);
+                std::vector<int> wave, rest;
+                for (int i : waiting) {
+                    const int apex = dirs[events[i].cell];
+                    const int ax = (apex % p.W) / sx, ay = (apex / p.W) / sy;
+                    bool blocked = false;
+                    for (int oy = -1; oy <= 1 && !blocked; ++oy) {
+                        const int yy = ay + oy;
+                        if (yy < 0 || yy >= nby) continue;
+                        for (int ox = -1; ox <= 1 && !blocked; ++ox) {
+                            const int xx = ((ax + ox) % nbx + nbx) % nbx;
+                            for (int j : block[yy * nbx + xx])
+                                if (overlap(apex, dirs[events[j].cell])) {
+                                    blocked = true;
+                                    break;
+                                }
+                        }
+                    }
+                    (blocked ? rest : wave).push_back(i);
+                    block[ay * nbx + ax].push_back(i);   // every waiting fan blocks the later ones
+                }
+                for (auto it = wave.rbegin(); it != wave.rend(); ++it)
+                    if (!run_fan(events[*it])) return 2;
+                repairs[2]++;
+                waiting.swap(rest);
+            }
         }
         bool redo = false;
         std::vector<int> replay;
