@@ -464,28 +464,37 @@ struct TouchLog {
 };
 
 // The mouth of `cell` (HydraulicErosion.kt:1187-1349) with the outlined fans of profile P2: a sea lobe
-// or a lake fan grown from the receiver by growFan (DeltaFan.kt). Returns what it laid.
-CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, int kind, int* stamp, int id,
-                   Heap& heap, TouchLog* log) {
+// or a lake fan grown from the receiver by growFan (DeltaFan.kt), in two halves. The admission grows
+// the admitted set best-first over distance bent by depth inside the rim; a lake fan's admission reads
+// only fixed fields (land, the lake's depth), a sea lobe's reads the sediment earlier lobes laid. The
+// laying then builds the admitted cells nearest first, each up to its level.
+CG_HD bool mouth_accepts(const Params& p, const Fields& f, bool sea, int c) {
+    return sea ? !f.land[c] : (f.land[c] && ponded(p, f, c));
+}
+
+CG_HD double mouth_budget(const Params& p, const Fields& f, int cell, double carried, int kind) {
+    if (kind == SEA) return f.area[cell] >= p.delta_min_cells ? carried * (double)p.delta_share : 0.0;
+    return carried * (double)p.lake_share;
+}
+
+CG_HD void mouth_rim(const Params& p, const Fields& f, int cell, int kind, Rim& m) {
     const int receiver = f.dirs[cell];
     const int W = p.W;
     const float out_x = (float)shortest_x(receiver % W - cell % W, W);
     const float out_y = (float)(receiver / W - cell / W);
-    const bool sea = kind == SEA;
-    double budget;
-    if (sea) budget = f.area[cell] >= p.delta_min_cells ? carried * (double)p.delta_share : 0.0;
-    else budget = carried * (double)p.lake_share;
-    Rim m;
     rim_init(m, receiver, W, p.r, p.step_ns, p.step_diag, (float)p.reach_cells, out_x, out_y,
-             fan_hash(p.seed, mouth_key(receiver, p.reach_cells, W)), sea);
-    if (sea) rim_prune(m, p.H, f.land);
-    auto accepts = [&](int c) { return sea ? !f.land[c] : (f.land[c] && ponded(p, f, c)); };
-    if (budget <= 0.0 || !accepts(receiver)) return 0.0;
-    // Admission: best-first over distance bent by depth, inside the rim.
+             fan_hash(p.seed, mouth_key(receiver, p.reach_cells, W)), kind == SEA);
+    if (kind == SEA) rim_prune(m, p.H, f.land);
+}
+
+// The admission; heap.admitted[0..returned) holds the admitted cells in admission order. `stamp`
+// marks the cells this fan has pushed (cells equal to `id`); ids only increase.
+CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, int* stamp, int id, Heap& heap) {
+    const int W = p.W;
     heap.size = 0;
     heap.admitted_count = 0;
-    stamp[receiver] = id;
-    heap_push(heap, receiver, 0.0f, 0.0f);
+    stamp[m.apex] = id;
+    heap_push(heap, m.apex, 0.0f, 0.0f);
     int cur;
     float penalty;
     while (heap_pop(heap, cur, penalty)) {
@@ -499,7 +508,7 @@ CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, i
                 int nc = (column + sx) % W;
                 if (nc < 0) nc += W;
                 int n = nr * W + nc;
-                if (stamp[n] == id || !accepts(n)) continue;
+                if (stamp[n] == id || !mouth_accepts(p, f, sea, n)) continue;
                 float co = rim_column_offset(m, n), ro = rim_row_offset(m, n);
                 float distance = sqrt_rn(co * co + ro * ro);
                 float depth = sea ? p.shoreline - (f.surface[n] + f.sediment[n])
@@ -512,15 +521,22 @@ CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, i
             }
         }
     }
-    // Laying: the admitted cells nearest first, each up to its level.
-    const int count = heap.admitted_count;
+    return heap.admitted_count;
+}
+
+// The laying over `count` admitted cells (the heap's own arrays order them; `admitted` must not be
+// the heap's cells array). Returns what it laid.
+CG_HD double lay_admitted(const Params& p, const Fields& f, const Rim& m, bool sea, const int* admitted, int count,
+                          double budget, Heap& heap, TouchLog* log) {
     heap.size = 0;
     for (int k = 0; k < count; ++k) {
-        int c = heap.admitted[k];
+        int c = admitted[k];
         float co = rim_column_offset(m, c), ro = rim_row_offset(m, c);
         heap_push(heap, c, sqrt_rn(co * co + ro * ro), 0.0f);
     }
     double remaining = budget, laid = 0.0;
+    int cur;
+    float penalty;
     while (remaining > 0.0 && heap_pop(heap, cur, penalty)) {
         float co = rim_column_offset(m, cur), ro = rim_row_offset(m, cur);
         float distance = sqrt_rn(co * co + ro * ro);
@@ -549,6 +565,18 @@ CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, i
         laid += moved;
     }
     return laid;
+}
+
+// The whole mouth. Returns what it laid.
+CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, int kind, int* stamp, int id,
+                   Heap& heap, TouchLog* log) {
+    const bool sea = kind == SEA;
+    const double budget = mouth_budget(p, f, cell, carried, kind);
+    Rim m;
+    mouth_rim(p, f, cell, kind, m);
+    if (budget <= 0.0 || !mouth_accepts(p, f, sea, m.apex)) return 0.0;
+    const int count = admit(p, f, m, sea, stamp, id, heap);
+    return lay_admitted(p, f, m, sea, heap.admitted, count, budget, heap, log);
 }
 
 }  // namespace dep

@@ -15,7 +15,7 @@ extern "C" {
 
 // mode 0: the reference's order; mode 1: level by level (own walks, then the level's mouths in rank
 // order, with the two repairs); mode 2: mode 1 with each level's mouths in waves of fans whose reaches
-// do not overlap. arriving[] receives each cell's arriving load (the notch's hand-off plus its
+// do not overlap; mode 3: mode 1 with every lake fan's admission done first, out of order. arriving[] receives each cell's arriving load (the notch's hand-off plus its
 // donors'). repairs[0..2]: ponded cells replayed, levels redone, fan waves.
 int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land_range, float to_relative,
              float shoreline, const int32_t* order, int order_len, const int32_t* dirs, const uint8_t* land,
@@ -109,6 +109,40 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
         if (mode == 1) {
             for (Event& e : events)
                 if (!run_fan(e)) return 2;
+        } else if (mode == 3) {
+            // Every lake fan's admission first, in reverse rank order (they read only fixed fields),
+            // then the mouths in rank order, the lake fans laying over their admitted cells.
+            std::vector<std::vector<int>> admitted(events.size());
+            std::vector<char> admitted_ok(events.size(), 0);
+            for (size_t i = events.size(); i-- > 0;) {
+                Event& e = events[i];
+                if (e.kind != LAKE) continue;
+                const double budget = mouth_budget(p, f, e.cell, e.carried, e.kind);
+                Rim m;
+                mouth_rim(p, f, e.cell, e.kind, m);
+                if (budget <= 0.0 || !mouth_accepts(p, f, false, m.apex)) continue;
+                const int n = admit(p, f, m, false, stamp.data(), ++id, heap);
+                admitted[i].assign(heap.admitted, heap.admitted + n);
+                admitted_ok[i] = 1;
+            }
+            for (size_t i = 0; i < events.size(); ++i) {
+                Event& e = events[i];
+                if (e.kind == SEA) {
+                    if (!run_fan(e)) return 2;
+                    continue;
+                }
+                double laid = 0.0;
+                if (admitted_ok[i]) {
+                    Rim m;
+                    mouth_rim(p, f, e.cell, e.kind, m);
+                    TouchLog log{buffer.data(), cap, 0, 0};
+                    laid = lay_admitted(p, f, m, false, admitted[i].data(), (int)admitted[i].size(),
+                                        mouth_budget(p, f, e.cell, e.carried, e.kind), heap, &log);
+                    if (log.overflow) return 2;
+                    e.touches.assign(buffer.begin(), buffer.begin() + log.count);
+                }
+                handoff[e.cell] = e.carried - laid;
+            }
         } else {
             // Waves: a fan runs once no earlier waiting fan's reach overlaps its own (the rim's widest
             // reach, 1.3 reach cells, plus the neighbours its admission reads); a wave's fans run in

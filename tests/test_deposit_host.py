@@ -1,7 +1,8 @@
 """The device's deposition logic (cartogenesis_gb300/csrc/cg_deposit.cuh: a cell's own walk, the
 outlined lobes and lake fans) built for the host and run on rounds captured from the oracle, in the
-reference's order and in the device's level order: the sediment, settled heights and loads it leaves
-must be the oracle walk's, bit for bit."""
+reference's order, in the device's level order, with a level's fans in waves, and with every lake
+fan's admission done first and out of order: the sediment, settled heights and loads it leaves must
+be the oracle walk's, bit for bit."""
 import ctypes as C
 import os
 import subprocess
@@ -57,7 +58,7 @@ def test_device_walk_matches_the_oracle(host, W, H, seed, uplift, rounds):
         c = oracle.capture_walk(p, h, up, rk, r)
         land = c["land"].astype(bool)
         # The wave mode's host emulation is quadratic in the fans of a crowded level: small worlds only.
-        for mode in ((0, 1, 2) if W * H <= 512 * 256 else (0, 1)):
+        for mode in ((0, 1, 2, 3) if W * H <= 512 * 256 else (0, 1, 3)):
             sediment, settled, arriving, repairs = run(host, mode, p, c)
             assert np.array_equal(sediment.view(np.uint32), c["sediment_after"].view(np.uint32)), (r, mode)
             assert np.array_equal(settled.view(np.uint32), c["settled_after"].view(np.uint32)), (r, mode)
