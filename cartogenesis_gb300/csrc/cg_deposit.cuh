@@ -487,13 +487,53 @@ CG_HD void mouth_rim(const Params& p, const Fields& f, int cell, int kind, Rim& 
     if (kind == SEA) rim_prune(m, p.H, f.land);
 }
 
-// The admission; heap.admitted[0..returned) holds the admitted cells in admission order. `stamp`
-// marks the cells this fan has pushed (cells equal to `id`); ids only increase.
-CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, int* stamp, int id, Heap& heap) {
+// The cells a fan has pushed: the stage's stamps (a cell is this fan's when it holds the fan's id;
+// ids only increase), for fans that run one at a time.
+struct StampVisited {
+    int* stamp;
+    int id;
+    CG_HD bool seen(int n) const { return stamp[n] == id; }
+    CG_HD void mark(int n) { stamp[n] = id; }
+};
+
+// The same for a fan that runs beside others: its own bits over the box its admission can reach
+// (the rim's widest reach, 1.3 reach cells, and the neighbours it reads). A cell outside the box,
+// which the rim's bound excludes, sets `outside` and reads as seen.
+struct BoxVisited {
+    uint32_t* bits;
+    int W, apex_col, apex_row, bx, by;
+    int* outside;
+    CG_HD int index(int n) const {
+        int dx = shortest_x(n % W - apex_col, W), dy = n / W - apex_row;
+        if (dx < -bx || dx > bx || dy < -by || dy > by) return -1;
+        return (dy + by) * (2 * bx + 1) + (dx + bx);
+    }
+    CG_HD bool seen(int n) const {
+        int i = index(n);
+        if (i < 0) {
+            *outside = 1;
+            return true;
+        }
+        return (bits[i >> 5] >> (i & 31)) & 1u;
+    }
+    CG_HD void mark(int n) {
+        int i = index(n);
+        if (i >= 0) bits[i >> 5] |= 1u << (i & 31);
+    }
+};
+
+// The half sizes of a BoxVisited box, and its words.
+CG_HD int box_bx(const Params& p) { return (int)ceilf(1.3f * (float)p.reach_cells) + 2; }
+CG_HD int box_by(const Params& p) { return (int)ceil(1.3 * (double)p.reach_cells / p.r) + 2; }
+CG_HD int box_words(const Params& p) { return ((2 * box_bx(p) + 1) * (2 * box_by(p) + 1) + 31) / 32; }
+
+// The admission; heap.admitted[0..returned) holds the admitted cells in admission order.
+template <class Visited>
+CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, Visited& visited, Heap& heap) {
     const int W = p.W;
     heap.size = 0;
     heap.admitted_count = 0;
-    stamp[m.apex] = id;
+    visited.mark(m.apex);
     heap_push(heap, m.apex, 0.0f, 0.0f);
     int cur;
     float penalty;
@@ -508,7 +548,7 @@ CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, int* s
                 int nc = (column + sx) % W;
                 if (nc < 0) nc += W;
                 int n = nr * W + nc;
-                if (stamp[n] == id || !mouth_accepts(p, f, sea, n)) continue;
+                if (visited.seen(n) || !mouth_accepts(p, f, sea, n)) continue;
                 float co = rim_column_offset(m, n), ro = rim_row_offset(m, n);
                 float distance = sqrt_rn(co * co + ro * ro);
                 float depth = sea ? p.shoreline - (f.surface[n] + f.sediment[n])
@@ -516,7 +556,7 @@ CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, int* s
                 float advance = 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / p.shelf_depth;
                 float np = penalty + step_of(p, sx, sy) * (advance - 1.0f);
                 if (distance + np > rim_radius(m, co, ro, distance)) continue;
-                stamp[n] = id;
+                visited.mark(n);
                 heap_push(heap, n, distance + np, np);
             }
         }
@@ -575,7 +615,8 @@ CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, i
     Rim m;
     mouth_rim(p, f, cell, kind, m);
     if (budget <= 0.0 || !mouth_accepts(p, f, sea, m.apex)) return 0.0;
-    const int count = admit(p, f, m, sea, stamp, id, heap);
+    StampVisited visited{stamp, id};
+    const int count = admit(p, f, m, sea, visited, heap);
     return lay_admitted(p, f, m, sea, heap.admitted, count, budget, heap, log);
 }
 

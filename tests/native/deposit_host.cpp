@@ -15,7 +15,8 @@ extern "C" {
 
 // mode 0: the reference's order; mode 1: level by level (own walks, then the level's mouths in rank
 // order, with the two repairs); mode 2: mode 1 with each level's mouths in waves of fans whose reaches
-// do not overlap; mode 3: mode 1 with every lake fan's admission done first, out of order. arriving[] receives each cell's arriving load (the notch's hand-off plus its
+// do not overlap; mode 3: mode 1 with every lake fan's admission done first, out of order; mode 4:
+// mode 3 with each admission's own visited bits over its box, as fans running side by side keep them. arriving[] receives each cell's arriving load (the notch's hand-off plus its
 // donors'). repairs[0..2]: ponded cells replayed, levels redone, fan waves.
 int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land_range, float to_relative,
              float shoreline, const int32_t* order, int order_len, const int32_t* dirs, const uint8_t* land,
@@ -109,7 +110,7 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
         if (mode == 1) {
             for (Event& e : events)
                 if (!run_fan(e)) return 2;
-        } else if (mode == 3) {
+        } else if (mode == 3 || mode == 4) {
             // Every lake fan's admission first, in reverse rank order (they read only fixed fields),
             // then the mouths in rank order, the lake fans laying over their admitted cells.
             std::vector<std::vector<int>> admitted(events.size());
@@ -121,7 +122,17 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
                 Rim m;
                 mouth_rim(p, f, e.cell, e.kind, m);
                 if (budget <= 0.0 || !mouth_accepts(p, f, false, m.apex)) continue;
-                const int n = admit(p, f, m, false, stamp.data(), ++id, heap);
+                int n;
+                if (mode == 3) {
+                    StampVisited v{stamp.data(), ++id};
+                    n = admit(p, f, m, false, v, heap);
+                } else {
+                    std::vector<uint32_t> bits(box_words(p), 0u);
+                    int outside = 0;
+                    BoxVisited v{bits.data(), p.W, m.apex_column, m.apex_row, box_bx(p), box_by(p), &outside};
+                    n = admit(p, f, m, false, v, heap);
+                    if (outside) return 3;
+                }
                 admitted[i].assign(heap.admitted, heap.admitted + n);
                 admitted_ok[i] = 1;
             }

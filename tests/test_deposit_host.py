@@ -58,7 +58,7 @@ def test_device_walk_matches_the_oracle(host, W, H, seed, uplift, rounds):
         c = oracle.capture_walk(p, h, up, rk, r)
         land = c["land"].astype(bool)
         # The wave mode's host emulation is quadratic in the fans of a crowded level: small worlds only.
-        for mode in ((0, 1, 2, 3) if W * H <= 512 * 256 else (0, 1, 3)):
+        for mode in ((0, 1, 2, 3, 4) if W * H <= 512 * 256 else (0, 1, 3, 4)):
             sediment, settled, arriving, repairs = run(host, mode, p, c)
             assert np.array_equal(sediment.view(np.uint32), c["sediment_after"].view(np.uint32)), (r, mode)
             assert np.array_equal(settled.view(np.uint32), c["settled_after"].view(np.uint32)), (r, mode)
