@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "../../cartogenesis_gb300/csrc/cg_deposit.cuh"
@@ -16,7 +17,9 @@ extern "C" {
 // mode 0: the reference's order; mode 1: level by level (own walks, then the level's mouths in rank
 // order, with the two repairs); mode 2: mode 1 with each level's mouths in waves of fans whose reaches
 // do not overlap; mode 3: mode 1 with every lake fan's admission done first, out of order; mode 4:
-// mode 3 with each admission's own visited bits over its box, as fans running side by side keep them. arriving[] receives each cell's arriving load (the notch's hand-off plus its
+// mode 3 with each admission's own visited bits over its box, as fans running side by side keep them;
+// mode 5: mode 3 with the lake fans laying in waves of fans whose admitted cells do not meet.
+// repairs[3] counts mode 5's laying waves. arriving[] receives each cell's arriving load (the notch's hand-off plus its
 // donors'). repairs[0..2]: ponded cells replayed, levels redone, fan waves.
 int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land_range, float to_relative,
              float shoreline, const int32_t* order, int order_len, const int32_t* dirs, const uint8_t* land,
@@ -33,7 +36,7 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
     Heap heap{hc.data(), hk.data(), hp.data(), ha.data(), cap, 0, 0};
     int id = first_id;
     double incised = 0, deposited = 0;
-    repairs[0] = repairs[1] = repairs[2] = 0;
+    repairs[0] = repairs[1] = repairs[2] = repairs[3] = 0;
     if (mode == 0) {
         std::vector<double> load(load0, load0 + N);
         for (int k = 0; k < order_len; ++k) {
@@ -110,7 +113,7 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
         if (mode == 1) {
             for (Event& e : events)
                 if (!run_fan(e)) return 2;
-        } else if (mode == 3 || mode == 4) {
+        } else if (mode == 3 || mode == 4 || mode == 5) {
             // Every lake fan's admission first, in reverse rank order (they read only fixed fields),
             // then the mouths in rank order, the lake fans laying over their admitted cells.
             std::vector<std::vector<int>> admitted(events.size());
@@ -123,7 +126,7 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
                 mouth_rim(p, f, e.cell, e.kind, m);
                 if (budget <= 0.0 || !mouth_accepts(p, f, false, m.apex)) continue;
                 int n;
-                if (mode == 3) {
+                if (mode == 3 || mode == 5) {
                     StampVisited v{stamp.data(), ++id};
                     n = admit(p, f, m, false, v, heap);
                 } else {
@@ -136,12 +139,8 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
                 admitted[i].assign(heap.admitted, heap.admitted + n);
                 admitted_ok[i] = 1;
             }
-            for (size_t i = 0; i < events.size(); ++i) {
+            auto lay_lake = [&](size_t i) {
                 Event& e = events[i];
-                if (e.kind == SEA) {
-                    if (!run_fan(e)) return 2;
-                    continue;
-                }
                 double laid = 0.0;
                 if (admitted_ok[i]) {
                     Rim m;
@@ -149,10 +148,45 @@ int dep_walk(int mode, const cg_erosion_params* cp, float land_cells, float land
                     TouchLog log{buffer.data(), cap, 0, 0};
                     laid = lay_admitted(p, f, m, false, admitted[i].data(), (int)admitted[i].size(),
                                         mouth_budget(p, f, e.cell, e.carried, e.kind), heap, &log);
-                    if (log.overflow) return 2;
+                    if (log.overflow) return false;
                     e.touches.assign(buffer.begin(), buffer.begin() + log.count);
                 }
                 handoff[e.cell] = e.carried - laid;
+                return true;
+            };
+            if (mode == 3 || mode == 4) {
+                for (size_t i = 0; i < events.size(); ++i) {
+                    if (events[i].kind == SEA) {
+                        if (!run_fan(events[i])) return 2;
+                    } else if (!lay_lake(i)) {
+                        return 2;
+                    }
+                }
+            } else {
+                // Mode 5: the sea lobes in rank order (they touch only sea cells), and the lake fans'
+                // laying in waves: a fan lays once no earlier waiting fan admitted any of its cells; a
+                // wave lays in reverse rank order.
+                for (size_t i = 0; i < events.size(); ++i)
+                    if (events[i].kind == SEA && !run_fan(events[i])) return 2;
+                std::vector<int> waiting;
+                for (size_t i = 0; i < events.size(); ++i)
+                    if (events[i].kind == LAKE) waiting.push_back((int)i);
+                std::unordered_map<int, int> claim;
+                while (!waiting.empty()) {
+                    claim.clear();
+                    for (int i : waiting)
+                        for (int c : admitted[i]) claim.emplace(c, i);   // the earliest waiting fan keeps a cell
+                    std::vector<int> wave, rest;
+                    for (int i : waiting) {
+                        bool held = true;
+                        for (int c : admitted[i]) held = held && claim[c] == i;
+                        (held ? wave : rest).push_back(i);
+                    }
+                    for (auto it = wave.rbegin(); it != wave.rend(); ++it)
+                        if (!lay_lake(*it)) return 2;
+                    repairs[3]++;
+                    waiting.swap(rest);
+                }
             }
         } else {
             // Waves: a fan runs once no earlier waiting fan's reach overlaps its own (the rim's widest

@@ -36,7 +36,7 @@ def host():
 def run(host, mode, params, c):
     sediment, settled = c["sediment"].copy(), c["settled"].copy()
     arriving = np.zeros_like(c["load"])
-    repairs = np.zeros(3, np.int64)
+    repairs = np.zeros(4, np.int64)
     P = abi.ptr
     st = host.dep_walk(mode, C.byref(params), c["land_cells"], c["land_range"], c["to_relative"], c["shoreline"],
                        P(c["order"]), len(c["order"]), P(c["dirs"]), P(c["land"]), P(c["ground"]), P(c["relative"]),
@@ -58,7 +58,7 @@ def test_device_walk_matches_the_oracle(host, W, H, seed, uplift, rounds):
         c = oracle.capture_walk(p, h, up, rk, r)
         land = c["land"].astype(bool)
         # The wave mode's host emulation is quadratic in the fans of a crowded level: small worlds only.
-        for mode in ((0, 1, 2, 3, 4) if W * H <= 512 * 256 else (0, 1, 3, 4)):
+        for mode in ((0, 1, 2, 3, 4, 5) if W * H <= 512 * 256 else (0, 1, 3, 4, 5)):
             sediment, settled, arriving, repairs = run(host, mode, p, c)
             assert np.array_equal(sediment.view(np.uint32), c["sediment_after"].view(np.uint32)), (r, mode)
             assert np.array_equal(settled.view(np.uint32), c["settled_after"].view(np.uint32)), (r, mode)
