@@ -37,7 +37,8 @@ METRIC = "Mcell-rounds/s on 1 GB300: plain vs batched vs surrogate at <=5 m heig
 UNIT = "Mcell-rounds/s"
 ROUNDS = 12
 # DRAM bytes (read + write) of one two-sweep launch of thermal_sweeps_kernel on the 8192 x 4096
-# field, from ncu (profiles/thermal_sweeps_8192x4096.md); the roofline's traffic at that size.
+# field, read from an ncu capture of that launch (ncu cannot run inside the timed bench); the
+# roofline's traffic at that size, null at other sizes.
 SWEEP_TRAFFIC_PER_LAUNCH = 228.1e6
 
 

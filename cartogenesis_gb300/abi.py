@@ -7,10 +7,10 @@ import ctypes as C
 
 CG_ABI_VERSION = 1
 
-CG_OK, CG_CANCELLED, CG_TIMEOUT, CG_BAD_ARG, CG_OOM, CG_CUDA, CG_UNSUPPORTED = range(7)
+CG_OK, CG_CANCELLED, CG_TIMEOUT, CG_BAD_ARG, CG_OOM, CG_CUDA, CG_UNSUPPORTED, CG_INEXACT = range(8)
 STATUS_NAMES = {
     CG_OK: "OK", CG_CANCELLED: "CANCELLED", CG_TIMEOUT: "TIMEOUT", CG_BAD_ARG: "BAD_ARG",
-    CG_OOM: "OOM", CG_CUDA: "CUDA", CG_UNSUPPORTED: "UNSUPPORTED",
+    CG_OOM: "OOM", CG_CUDA: "CUDA", CG_UNSUPPORTED: "UNSUPPORTED", CG_INEXACT: "INEXACT",
 }
 CG_MODE_REF32 = 0
 CG_PROFILE_P0, CG_PROFILE_P1, CG_PROFILE_P2 = 0, 1, 2

@@ -20,8 +20,10 @@
 //      running the reference's heap over that level's cells (those that entered from below seed it;
 //      lower levels are final by then), and every cell it reaches is pinned to its exact parent.
 //      The levels from the lowest changed one upward are recomputed, and the check repeats; each
-//      replay settles its level for good, so the lowest open level only rises. A level too large
-//      to replay (over 2^18 cells) is reported as unresolved.
+//      replay settles its level for good, so the lowest open level only rises. The replay's list
+//      and heap are sized for the whole grid, so a level of any size is replayed. If the repairs'
+//      guard (64 passes) is ever reached with ties still open, the fill returns CG_INEXACT: its
+//      result is then not the reference's, and the stage does not carry on with it.
 #include <algorithm>
 #include <cfloat>
 #include <cooperative_groups.h>
@@ -551,8 +553,9 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     CG_LAUNCH(ctx) k_mark_drained<<<grid, 256, 0, sm>>>(d_ptr, d_rel, N, d_cls, d_filled);
     CG_CHECK_LAUNCH(ctx);
 
-    // Scratch of the level replays: a generation mark per cell, the level's cells and the heap.
-    const int cap = 1 << 18;
+    // Scratch of the level replays: a generation mark per cell, the level's cells and the heap, each
+    // sized for every cell of the grid (a key level can hold any share of the grid).
+    const int cap = (int)N;
     CG_BUF(int, d_mark, ctx, S_SCRATCH3, N);
     CG_BUF(int, d_replay, ctx, S_CG4, 2 * (size_t)cap + 4);
     int* d_list = d_replay;
@@ -611,7 +614,10 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
             int overflow = 0;
             CG_CUDA(ctx, cudaMemcpyAsync(&overflow, &d_cnt->overflow, sizeof(int), cudaMemcpyDeviceToHost, sm));
             CG_CUDA(ctx, cudaStreamSynchronize(sm));
-            if (overflow) break;   // reported as unresolved
+            if (overflow) {   // cannot happen with cap = N; kept as a guard
+                unresolved_total += 1;
+                break;
+            }
             if (Q < from) from = Q;
         }
         // Recompute the levels at and above the lowest one that changed.
@@ -619,6 +625,8 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     }
     if (ties) *ties = tie_total;
     if (unresolved) *unresolved = unresolved_total;
+    if (unresolved_total > 0)
+        return fail(ctx, CG_INEXACT, "fillDepressions left %lld quantised-key ties unordered", (long long)unresolved_total);
     return CG_OK;
 }
 

@@ -110,3 +110,17 @@ def world(width, height, seed=1, uplift="bands"):
     up = uplift_bands(width, height, seed) if uplift == "bands" else uplift_ridges(width, height, seed)
     rk = rock_erodibility(width, height, seed)
     return h, up, rk
+
+
+def batch_shapes(n, seed=1, max_rows=2048):
+    """The batched workload's world shapes: n planets of radius r ~ U(0.25, 2.0) Earth radii, each
+    grid 2R x R cells with R the power of two nearest 1024 r (WorldGenConfig wants powers of two),
+    in {256, ..., max_rows}. Returns [(width, height, seed_i, radius)]; seed_i = seed * 1000 + i."""
+    rng = _rng(seed, 4000)
+    out = []
+    for i in range(n):
+        r = float(rng.uniform(0.25, 2.0))
+        rows = int(2 ** np.round(np.log2(1024.0 * r)))
+        rows = int(min(max(rows, 256), max_rows))
+        out.append((2 * rows, rows, seed * 1000 + i, r))
+    return out

@@ -40,7 +40,9 @@ typedef enum cg_status {
     CG_BAD_ARG = 3,     /* a size, pointer or parameter failed validation */
     CG_OOM = 4,         /* device or pinned-host allocation failed */
     CG_CUDA = 5,        /* a CUDA call failed; cg_last_error says which */
-    CG_UNSUPPORTED = 6  /* a switch the library does not implement (e.g. profile P2) */
+    CG_UNSUPPORTED = 6, /* a switch the library does not implement */
+    CG_INEXACT = 7      /* a result could not be made the reference's exactly (a fill tie left
+                           unordered by the repairs' guard); outputs are not written */
 } cg_status;
 
 /* Parity mode. REF32 is the reference's own arithmetic (FP32 field, FP64 where Kotlin promotes). */
@@ -199,10 +201,11 @@ cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t width, int32_t height, const fl
  * passes the input and output as device pointers (different buffers; the input is not written),
  * and the one scratch field lives in a file-scope device array sized for grids of up to 2^20 cells
  * (4 MiB, held by every GPU that loads the library until exit). Larger grids, a non-power-of-two
- * side, aliased buffers or negative passes return CG_BAD_ARG. The first call on a device looks up
- * the array's address with that device current, so make it before any stream capture. Calls share
- * the array: calls whose work overlaps on the GPU race. `stream` is a cudaStream_t or NULL; the
- * call returns when the work is queued.
+ * side, input and output byte ranges that overlap at all, or negative passes return CG_BAD_ARG.
+ * Every CUDA context holds its own copy of the array: the first call in a context (the primary one
+ * or a driver-API context the caller made current) looks up the array's address with that context
+ * current, so make it before any stream capture. Calls share the array: calls whose work overlaps
+ * on the GPU race. `stream` is a cudaStream_t or NULL; the call returns when the work is queued.
  */
 cg_status cg_thermal_sweeps_noalloc(const float* heights_in_dev, float* heights_out_dev, int32_t width,
                                     int32_t height, cg_thermal_limits limits, int32_t passes, float rate,

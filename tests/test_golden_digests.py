@@ -1,4 +1,4 @@
-"""The oracle's whole-stage outputs on small seeded worlds, for every profile, against the committed
+"""A regression lock: the oracle's whole-stage outputs on small seeded worlds, for every profile, against the committed
 digests (tests/golden/stage_digests.json, written by tests/golden/make_stage_digests.py): any change
 to the restatement that moves an output bit shows here. The GPU is held to the oracle itself by the
 parity tests."""

@@ -120,6 +120,26 @@ def test_fill_key_plateaus(seed):
     assert diff.size == 0, f"{diff.size} cells differ (ties {ties}): {diff[:8]}"
 
 
+def test_fill_key_level_larger_than_any_fixed_cap():
+    """A coastal plain of 512K cells whose heights all lie within about one quantum of the heap key
+    (steps of 1e-7 around 0.3): each key level holds far more than 2^18 cells, so its ties can only be
+    ordered by replaying the whole level. The fill must give the oracle's bits (and so report no
+    unresolved tie), whatever the level's size."""
+    rng = np.random.default_rng(9)
+    W, H = 2048, 256
+    g = (np.float32(0.3) + np.float32(1e-7) * rng.integers(0, 4, (H, W)).astype(np.float32)).astype(np.float32)
+    land = np.ones((H, W), np.uint8)
+    land[:, 0:2] = 0
+    rel = np.where(land == 1, g, np.float32(0.29)).astype(np.float32)
+    q = (rel[land == 1] + np.float32(4.0)).astype(np.float32).view(np.int32)
+    assert np.bincount(q - q.min()).max() > (1 << 18)   # one key level alone is over 2^18 cells
+    want = oracle.fill_depressions(land, rel)
+    got, ties, unresolved = FlowRouting.fill_depressions(land, rel, with_ties=True)
+    assert unresolved == 0
+    diff = np.flatnonzero(bits(got) != bits(want))
+    assert diff.size == 0, f"{diff.size} cells differ (ties {ties}): {diff[:8]}"
+
+
 def test_fill_bench_world_8192x4096():
     """The bench world's first cut (8192 x 4096, 33.5M cells), where the index rule alone left a few
     within-level ties open: the device fill equals the oracle's bit for bit."""
