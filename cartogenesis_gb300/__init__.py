@@ -7,4 +7,4 @@ top of it. There is no CPU fallback: if the library or the device is missing, ca
 """
 from .runtime import (CgError, Context, library, load_library)  # noqa: F401
 from .api import (ErosionStage, ErosionConfig, GpuErosionAccelerator, FlowRouting, HydraulicErosion, SeaLevelStage,  # noqa: F401
-                  ThermalLimits)
+                  StageRounds, ThermalLimits)

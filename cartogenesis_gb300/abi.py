@@ -44,8 +44,12 @@ class ErosionParams(C.Structure):
         ("receiver_clamp", C.c_int32),
         ("shield_cut", C.c_int32),
         ("profile", C.c_int32),
-        ("reserved", C.c_int32),
+        ("climate_feed", C.c_int32),
     ]
+
+
+class Weather(C.Structure):
+    _fields_ = [("rainfall_mm", C.c_void_p), ("vegetation_density", C.c_void_p)]
 
 
 class Inputs(C.Structure):

@@ -169,6 +169,74 @@ class ErosionStage:
         return outs
 
 
+class StageRounds:
+    """The stage round by round with its world resident on the device (cg_stage_begin,
+    cg_erode_rounds, cg_stage_height, cg_stage_finish): where HydraulicErosion.apply asks for the
+    weather (P/HydraulicErosion.kt:655-661, 809-813) the caller reads the field and solves it."""
+
+    def __init__(self, config, height, uplift_mm_per_year=None, rock_erodibility=None, rainfall_mm=None,
+                 vegetation_density=None, ctx=None):
+        self.ctx = ctx or default_context()
+        self.config = config
+        H, W = config.params.height, config.params.width
+        self.shape = (H, W)
+        self._keep = [_f32(a, (H, W)) for a in (height, uplift_mm_per_year, rock_erodibility, rainfall_mm,
+                                               vegetation_density)]
+        inputs = abi.Inputs(*[P(a) for a in self._keep])
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_stage_begin(self.ctx.handle, C.byref(config.params), C.byref(inputs)))
+        self.next_round = 0
+
+    def rounds(self, end_round, rainfall_mm=None, vegetation_density=None, new_weather=False):
+        """Rounds [next_round, end_round). With new_weather (or any weather field given) the weather is
+        replaced from next_round on; a field left None is the default (rain 1, no cover)."""
+        H, W = self.shape
+        weather = None
+        if new_weather or rainfall_mm is not None or vegetation_density is not None:
+            self._weather = [_f32(a, (H, W)) for a in (rainfall_mm, vegetation_density)]
+            weather = abi.Weather(*[P(a) for a in self._weather])
+        first = self.next_round
+        stats = (abi.RoundStats * max(end_round - first, 1))()
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_erode_rounds(self.ctx.handle, first, end_round,
+                                                        C.byref(weather) if weather is not None else None,
+                                                        C.cast(stats, C.c_void_p)))
+        self.next_round = end_round
+        return [{f: getattr(s, f) for f, _ in abi.RoundStats._fields_} for s in stats[:max(end_round - first, 0)]]
+
+    def height(self):
+        out = np.empty(self.shape, np.float32)
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_stage_height(self.ctx.handle, P(out)))
+        return out
+
+    def finish(self, want=("receivers",)):
+        H, W = self.shape
+        outs = {"height": np.empty((H, W), np.float32)}
+        for k in want:
+            outs[k] = np.empty((H, W), ErosionStage.KINDS[k])
+        o = abi.Outputs(**{k: P(v) for k, v in outs.items()})
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_stage_finish(self.ctx.handle, C.byref(o)))
+        return ErosionResult(**outs)
+
+    @staticmethod
+    def apply_fed(config, height, provisional_weather, uplift_mm_per_year=None, rock_erodibility=None,
+                  want=("receivers",), ctx=None):
+        """ErosionStage.apply with ErosionConfig.climateFeed: provisional_weather(field, round) returns the
+        (rainfall_mm, vegetation_density) solved on `field`, asked on the swept terrain (round 0) and at
+        round hydraulic_rounds / 2, as HydraulicErosion.apply asks provisionalWeather."""
+        run = StageRounds(config, height, uplift_mm_per_year, rock_erodibility, ctx=ctx)
+        R = config.params.hydraulic_rounds
+        half = R // 2 if R > 1 else R
+        rain, veg = provisional_weather(run.height(), 0)
+        run.rounds(half, rain, veg, new_weather=True)
+        if half < R:
+            rain, veg = provisional_weather(run.height(), half)
+            run.rounds(R, rain, veg, new_weather=True)
+        return run.finish(want)
+
+
 class SeaLevelStage:
     @staticmethod
     def percentile_cut(height, sea_level_fraction, lowstand_share_of_field=0.0, highest_land_metres=6000.0,

@@ -54,6 +54,8 @@ struct BreachDev {
     float* rel;
     float* ground;
     float* surface;
+    float* settled;      // profile P2's settled heights, or NULL
+    double* load;        // profile P2's load in transit, or NULL
     float land_cells;
     float land_range;
     float pond_depth;
@@ -174,6 +176,10 @@ __device__ __forceinline__ int take(const BreachDev& a, int cell, float r, float
         const float as_relative = (float)__ddiv_rn(removed, (double)a.land_range);
         __stcg(a.rel + cell, __fsub_rn(r, as_relative));
         if (!ponded) __stcg(a.ground + cell, __fsub_rn(g, as_relative));
+        // HydraulicErosion.kt:2045-2048: what the notch takes is carried on, and the settled
+        // surface falls with the rock (a cell is cut by one basin at a time, in basin order).
+        if (a.settled) __stcg(a.settled + cell, __fsub_rn(__ldcg(a.settled + cell), as_relative));
+        if (a.load) __stcg(a.load + cell, __dadd_rn(__ldcg(a.load + cell), removed));
         return 1;
     }
     return 0;
@@ -457,7 +463,7 @@ __global__ void __launch_bounds__(256) k_breach_waves(BreachDev a) {
 
 cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_rel, float* d_ground,
                      const int32_t* d_recv, const float* d_area, float land_cells, float land_range,
-                     const BreachRates& rates, float* d_surface, int* h_cells) {
+                     const BreachRates& rates, float* d_surface, int* h_cells, float* d_settled, double* d_load) {
     const size_t N = (size_t)W * H;
     cudaStream_t sm = ctx->stream;
     if (h_cells) *h_cells = 0;
@@ -483,6 +489,8 @@ cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_
     a.rel = d_rel;
     a.ground = d_ground;
     a.surface = d_surface;
+    a.settled = d_settled;
+    a.load = d_load;
     a.land_cells = land_cells;
     a.land_range = land_range;
     a.pond_depth = rates.pond_depth;

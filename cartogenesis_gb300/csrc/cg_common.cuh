@@ -41,6 +41,22 @@ struct DevBuf {
 
 struct Timer;
 
+// A stage whose world stays resident on the context between calls (cg_stage_begin, cg_erode_rounds,
+// cg_stage_finish), and the state the round loop carries from one round to the next.
+struct StageRun {
+    cg_erosion_params p{};
+    float* cur = nullptr;          // the working field
+    float* other = nullptr;        // its ping-pong partner
+    const float* uplift = nullptr; // inputs, device (or NULL)
+    const float* rock = nullptr;
+    const float* rain = nullptr;
+    const float* veg = nullptr;
+    int next_round = 0;            // rounds run so far
+    int land_cells = -1;           // the last routed round's land cells (-1: none routed)
+    bool done = false;             // no round is left to run (all run, or one found no land)
+    bool active = false;           // a resident world is held by the round-range entry points
+};
+
 }  // namespace cg
 
 // The library context (opaque in the C ABI).
@@ -54,7 +70,7 @@ struct cg_ctx {
     std::atomic<int> cancel{0};
     char error[512] = {0};
     // Named scratch buffers, grown on demand and reused across calls.
-    cg::DevBuf bufs[64];
+    cg::DevBuf bufs[128];
     // Pinned host staging.
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -64,6 +80,8 @@ struct cg_ctx {
     double rw_total = 0.0;
     // Kernels launched on this context (every launch site counts itself with CG_LAUNCH).
     long long launches = 0;
+    // The resident world of the round-range entry points (inactive otherwise).
+    cg::StageRun run;
 };
 
 // Prefix of every kernel launch statement: `CG_LAUNCH(ctx) k<<<...>>>(...);` counts the launch.
@@ -79,6 +97,13 @@ enum Slot {
     S_FLATIDX, S_FLATMEM, S_CG0, S_CG1, S_CG2, S_CG3, S_CG4, S_CG5, S_LEVELCNT, S_DEPTH, S_STATS,
     S_BASIN, S_BASIN2, S_FILLQ, S_FILLF, S_FILLFLAG, S_TILEFLAG, S_SCRATCH4, S_SCRATCH5, S_THERMFLAG,
     S_LINKS, S_SOURCES, S_FILLLIST, S_CLAIM, S_FOOT, S_BREACH,
+    // profile P2's deposition: the stage's state, a round's walk, and the mouths pass's own routing
+    S_SEDIMENT, S_STAMP, S_DEPWORDS, S_DEPMARK, S_SETTLED, S_LOAD, S_INCISED, S_DEPRANK, S_DEPLEVEL,
+    S_HANDOFF, S_DEPUSED, S_DEPS0, S_DEPD0, S_DEPEVC, S_DEPEVK, S_DEPSEG, S_DEPEVENTS, S_DEPEVTOUCH,
+    S_DEPSLOT0, S_DEPSLOT1, S_DEPSLOT2, S_DEPSLOT3, S_DEPSLOT4, S_DEPSLOT5, S_DEPSLOT6, S_DEPSLOT7,
+    S_DEPHEAP, S_DEPTOUCH, S_DEPREPLAY, S_DEPSEGC,
+    S_OM_LAND, S_OM_REL, S_OM_FILLED, S_OM_RECV, S_OM_KEY, S_OM_AREA, S_OM_RUNOFF, S_OM_DONORS,
+    S_FILLEB,
     S_COUNT
 };
 
@@ -97,6 +122,13 @@ void* pinned(cg_ctx* ctx, size_t bytes, cg_status* st);
     } while (0)
 
 #define CG_CHECK_LAUNCH(ctx) CG_CUDA(ctx, cudaGetLastError())
+
+// Returns the status of `x` when it is not CG_OK.
+#define CG_TRY_ST(x)                    \
+    do {                                \
+        cg_status s_ = (x);             \
+        if (s_ != CG_OK) return s_;     \
+    } while (0)
 
 #define CG_BUF(T, name, ctx, slot, count)                                        \
     T* name;                                                                     \

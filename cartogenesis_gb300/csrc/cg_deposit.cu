@@ -1,0 +1,678 @@
+// Profile P2's deposition on the device: the walk of HydraulicErosion.apply (HydraulicErosion.kt:
+// 1068-1349) with its sea lobes and lake fans (DeltaFan.kt growFan), settle (1351-1364) and the
+// closing mouths pass (openMouths, 1804-1892), each bit for bit the reference's.
+//
+// The reference walks the round's drainage order one cell after another. That order is level-major
+// (a cell's rank sorts by its Kahn level, then by its drainage key), so the walk runs level by level
+// from the sources, in one cooperative launch per round with grid barriers between the steps of a
+// level:
+//  A. every cell of the level does its own walk at once (HydraulicErosion.kt:1068-1186): a cell reads
+//     only its own state and its donors', which sit on lower levels. What arrives is the notch's
+//     hand-off plus the donors' hand-offs added in rank order, the reference's double additions in
+//     the reference's order. A cell whose mouth has something to lay (a sea lobe or a lake fan with a
+//     budget and an open apex) is listed, in rank order per CTA segment.
+//  B. the listed mouths run in rank order. A lake fan's admission (its best-first growth inside the
+//     rim) reads only fixed fields (the land, the lake's depth), so every lake fan of the level is
+//     admitted at once, a thread each with its own visited bits over the box its rim can reach, and
+//     its admitted cells are sorted by distance (the laying heap's pop order). One thread then takes
+//     the mouths in rank order: a sea lobe whole (its admission reads the sediment earlier lobes
+//     laid), a lake fan's laying as a scan of its sorted cells.
+//  C. a fan changes only sea cells and ponded land, which no own walk reads, except (a) a ponded cell
+//     of the fan's own level ranked after it, whose settled height took its own subtraction before
+//     the fan's addition instead of after: its settled height is replayed in rank order; and (b) a
+//     donor whose settled height a later cell of the level read in its headroom: the level is then
+//     restored and walked one cell after another. Both are rare; the same schedule is shown on the
+//     host to give the reference walk's bits (tests/native/deposit_host.cpp).
+// Settle is elementwise, and the mouths pass reads only each cell's receiver, so it runs receivers
+// first, level by level from the top, like the incision.
+#include <algorithm>
+#include <cooperative_groups.h>
+#include <vector>
+
+#include "cg_common.cuh"
+#include "cg_deposit.cuh"
+#include "cg_internal.h"
+#include "cg_params.h"
+#include "cg_util.h"
+
+namespace cg {
+
+namespace cgr = cooperative_groups;
+using namespace dep;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// Control words of a walk.
+enum { W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REDONE = 4, W_REPLAYED = 5, W_WORDS = 8 };
+
+struct WalkDev {
+    Params p;
+    Fields f;
+    const int* order;       // land cells in drainage order (rank order)
+    const int* rank_of;     // per cell
+    const long long* key;   // per cell: level << 32 | deepest source
+    const int* level_start; // [levels + 1]
+    int levels;
+    const double* load;     // per cell: the notch's hand-off
+    double* handoff;        // per cell: what a cell hands its receiver
+    uint8_t* used;          // per cell: its own walk read its donors' settled heights
+    float* s0;              // per rank: settled height before the own walk
+    float* d0;              // per rank: sediment before the own walk
+    double* ev_carried;     // per rank: what a listed mouth carries
+    int8_t* ev_kind;        // per rank: SEA or LAKE
+    int* seg_events;        // per rank: listed ranks, compacted within each CTA's segment
+    int* seg_count;         // per CTA
+    int* events;            // the level's listed ranks, dense, in rank order
+    // Lake-fan admission slots, `slots` of them, each `cap` entries.
+    int slots, cap, box_words;
+    int* slot_heap_cells;
+    float* slot_heap_keys;
+    float* slot_heap_pens;
+    int* slot_admitted;
+    int* slot_sorted;
+    double* slot_base;
+    uint32_t* slot_bits;
+    int* slot_n;            // per slot: admitted cells (-1: no fan)
+    // The sequential thread's heap (sea lobes, a redone level).
+    int* heap_cells;
+    float* heap_keys;
+    float* heap_pens;
+    int* heap_admitted;
+    int* stamp;             // per cell: the stage's fan stamps
+    // The level's fan deposits, for the repairs.
+    Touch* touches;
+    int touch_cap;
+    int* ev_touch;          // per listed mouth (dense index): its first touch; [n + 1]
+    int* mark;              // per cell: the generation that listed it for a replay
+    int* replay;            // cells to replay
+    int* words;             // W_* control words
+};
+
+__device__ __forceinline__ int level_of_cell(const WalkDev& w, int c) { return (int)(w.key[c] >> 32); }
+
+// What arrives at `c`: the notch's hand-off, then each donor's hand-off in rank order.
+__device__ double arriving(const WalkDev& w, int c) {
+    const int W = w.p.W, H = w.p.H;
+    const int col = c % W, row = c / W;
+    int donors[8], ranks[8], n = 0;
+    for (int rs = -1; rs <= 1; ++rs) {
+        const int nr = row + rs;
+        if (nr < 0 || nr >= H) continue;
+        for (int cs = -1; cs <= 1; ++cs) {
+            if (rs == 0 && cs == 0) continue;
+            const int d = nr * W + ((col + cs) & (W - 1));
+            if (w.f.dirs[d] != c || !w.f.land[d]) continue;
+            const int rk = w.rank_of[d];
+            int j = n++;
+            while (j > 0 && ranks[j - 1] > rk) {
+                ranks[j] = ranks[j - 1];
+                donors[j] = donors[j - 1];
+                --j;
+            }
+            ranks[j] = rk;
+            donors[j] = d;
+        }
+    }
+    double carried = w.load[c];
+    for (int k = 0; k < n; ++k) carried = __dadd_rn(carried, w.handoff[donors[k]]);
+    return carried;
+}
+
+// Whether a cell's mouth has anything to lay: a budget and an apex the fan accepts.
+__device__ bool mouth_live(const WalkDev& w, int c, double carried, int kind) {
+    const double budget = mouth_budget(w.p, w.f, c, carried, kind);
+    return budget > 0.0 && mouth_accepts(w.p, w.f, kind == SEA, w.f.dirs[c]);
+}
+
+__device__ Heap thread_heap(const WalkDev& w) {
+    return Heap{w.heap_cells, w.heap_keys, w.heap_pens, w.heap_admitted, w.cap, 0, 0};
+}
+
+// One cell's whole step the reference's way, for a level walked one cell after another.
+__device__ void walk_one(const WalkDev& w, int k) {
+    const int c = w.order[k];
+    double carried = arriving(w, c);
+    bool used;
+    double incised = 0.0, deposited = 0.0;
+    const int kind = own_walk(w.p, w.f, c, carried, &used, &incised, &deposited);
+    if (kind == ON) {
+        w.handoff[c] = carried;
+    } else if (kind == SEA || kind == LAKE) {
+        Heap h = thread_heap(w);
+        const int id = ++w.words[W_MOUTH_ID];
+        const double laid = mouth(w.p, w.f, c, carried, kind, w.stamp, id, h, nullptr);
+        if (kind == LAKE) w.handoff[c] = __dsub_rn(carried, laid);
+    }
+}
+
+// A lake fan's admission into slot `s`: the admitted cells sorted by distance from the apex (with
+// the cell as the tie break, the laying heap's pop order) and each one's level less its terrain.
+__device__ void admit_lake(const WalkDev& w, int s, int k) {
+    const int c = w.order[k];
+    int* cells = w.slot_heap_cells + (size_t)s * w.cap;
+    float* keys = w.slot_heap_keys + (size_t)s * w.cap;
+    float* pens = w.slot_heap_pens + (size_t)s * w.cap;
+    int* admitted = w.slot_admitted + (size_t)s * w.cap;
+    int* sorted = w.slot_sorted + (size_t)s * w.cap;
+    double* base = w.slot_base + (size_t)s * w.cap;
+    uint32_t* bits = w.slot_bits + (size_t)s * w.box_words;
+    for (int i = 0; i < w.box_words; ++i) bits[i] = 0u;
+    Rim m;
+    mouth_rim(w.p, w.f, c, LAKE, m);
+    int outside = 0;
+    BoxVisited visited{bits, w.p.W, m.apex_column, m.apex_row, box_bx(w.p), box_by(w.p), &outside};
+    Heap h{cells, keys, pens, admitted, w.cap, 0, 0};
+    const int n = admit(w.p, w.f, m, false, visited, h);
+    if (outside) atomicOr(&w.words[W_ERROR], 2);   // the rim reached past its box: cannot happen
+    h.size = 0;
+    for (int i = 0; i < n; ++i) {
+        const int x = admitted[i];
+        const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
+        heap_push(h, x, sqrt_rn(co * co + ro * ro), 0.0f);
+    }
+    int got = 0, x;
+    float pen;
+    while (heap_pop(h, x, pen)) {
+        const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
+        const float distance = sqrt_rn(co * co + ro * ro);
+        float fraction = distance / m.reach_cells;
+        if (fraction > 1.0f) fraction = 1.0f;
+        const float depth = 2.0f * w.p.pond_depth * (1.0f + kLakeFanSlope * fraction) * (0.9f + 0.35f * cell_wobble(x));
+        const float level = w.p.shoreline + (w.f.ground[x] - depth) * w.p.land_range;
+        sorted[got] = x;
+        base[got] = (double)level - (double)w.f.surface[x];
+        ++got;
+    }
+    w.slot_n[s] = got;
+}
+
+// A lake fan's laying over its sorted admitted cells (lay_admitted's loop): returns what it laid.
+__device__ double lay_lake(const WalkDev& w, int s, double budget, int* touch_n) {
+    const int n = w.slot_n[s];
+    const int* sorted = w.slot_sorted + (size_t)s * w.cap;
+    const double* base = w.slot_base + (size_t)s * w.cap;
+    double remaining = budget, laid = 0.0;
+    for (int i = 0; i < n && remaining > 0.0; ++i) {
+        const int x = sorted[i];
+        const double need = __dsub_rn(base[i], (double)w.f.sediment[x]);
+        if (need <= 0.0) continue;
+        if (*touch_n < w.touch_cap) w.touches[*touch_n] = Touch{x, w.f.settled[x], w.f.sediment[x], 0.0f};
+        const double moved = raise(w.f.sediment, x, need < remaining ? need : remaining);
+        const float increment = (float)(moved * (double)w.p.to_relative);
+        w.f.settled[x] += increment;
+        if (*touch_n < w.touch_cap) w.touches[(*touch_n)++].increment = increment;
+        else w.words[W_ERROR] |= 1;
+        remaining -= moved;
+        laid += moved;
+    }
+    return laid;
+}
+
+// The sequential part of a level: the mouths of events [e0, e1) in rank order (lake fans admitted
+// into slots e - e0), logging their deposits.
+__device__ void run_mouths(const WalkDev& w, int e0, int e1, int* touch_n) {
+    for (int e = e0; e < e1; ++e) {
+        const int k = w.events[e];
+        const int c = w.order[k];
+        const int kind = w.ev_kind[k];
+        const double carried = w.ev_carried[k];
+        w.ev_touch[e] = *touch_n;
+        double laid;
+        if (kind == LAKE) {
+            laid = lay_lake(w, e - e0, mouth_budget(w.p, w.f, c, carried, kind), touch_n);
+            w.handoff[c] = __dsub_rn(carried, laid);
+        } else {
+            Heap h = thread_heap(w);
+            TouchLog log{w.touches + *touch_n, w.touch_cap - *touch_n, 0, 0};
+            const int id = ++w.words[W_MOUTH_ID];
+            mouth(w.p, w.f, c, carried, kind, w.stamp, id, h, &log);
+            if (log.overflow) w.words[W_ERROR] |= 1;
+            *touch_n += log.count;
+        }
+    }
+}
+
+// Step C, on one thread: detect and make the two repairs of the level [lo, hi) with events [0, n).
+__device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int touch_n) {
+    w.ev_touch[n] = touch_n;
+    bool redo = false;
+    int replays = 0;
+    const int gen = ++w.words[W_GEN];
+    for (int e = 0; e < n && !redo; ++e) {
+        const int rank = w.events[e];
+        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
+            const int x = w.touches[t].cell;
+            if (!w.f.land[x]) continue;
+            if (level_of_cell(w, x) == L && w.rank_of[x] > rank && w.mark[x] != gen) {
+                w.mark[x] = gen;
+                w.replay[replays++] = x;
+            }
+            const int rr = w.f.dirs[x];
+            if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr]) {
+                redo = true;
+                break;
+            }
+        }
+    }
+    if (redo) {
+        w.words[W_REDONE]++;
+        for (int t = touch_n - 1; t >= 0; --t) {
+            w.f.settled[w.touches[t].cell] = w.touches[t].settled_before;
+            w.f.sediment[w.touches[t].cell] = w.touches[t].sediment_before;
+        }
+        for (int k = lo; k < hi; ++k) {
+            w.f.settled[w.order[k]] = w.s0[k];
+            w.f.sediment[w.order[k]] = w.d0[k];
+        }
+        for (int k = lo; k < hi; ++k) walk_one(w, k);
+        return;
+    }
+    for (int i = 0; i < replays; ++i) {
+        // The cell's own subtraction and the fans' increments, in rank order.
+        const int x = w.replay[i];
+        const int rx = w.rank_of[x];
+        float v = w.s0[rx];
+        bool own_done = false;
+        for (int e = 0; e < n; ++e) {
+            const int rank = w.events[e];
+            for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
+                if (w.touches[t].cell != x) continue;
+                if (!own_done && rank > rx) {
+                    const double moved = w.f.incised_at[x];
+                    if (moved > 0.0) v -= (float)(moved * (double)w.p.to_relative);
+                    own_done = true;
+                }
+                v += w.touches[t].increment;
+            }
+        }
+        if (!own_done) {
+            const double moved = w.f.incised_at[x];
+            if (moved > 0.0) v -= (float)(moved * (double)w.p.to_relative);
+        }
+        w.f.settled[x] = v;
+        w.words[W_REPLAYED]++;
+    }
+}
+
+// The round's walk, level by level (steps A, B, C above), in one cooperative launch.
+__global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
+    cgr::grid_group grid = cgr::this_grid();
+    __shared__ int warp_counts[kThreads / 32];
+    __shared__ int block_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int L = 0; L < w.levels; ++L) {
+        const int lo = w.level_start[L], hi = w.level_start[L + 1];
+        // A: own walks over this CTA's segment of the level, listing live mouths in rank order.
+        const int seg = (hi - lo + (int)gridDim.x - 1) / (int)gridDim.x;
+        const int s_lo = lo + (int)blockIdx.x * seg;
+        const int s_hi = min(hi, s_lo + seg);
+        if (threadIdx.x == 0) block_base = 0;
+        __syncthreads();
+        for (int base = s_lo; base < s_hi; base += kThreads) {
+            const int k = base + (int)threadIdx.x;
+            bool listed = false;
+            if (k < s_hi) {
+                const int c = w.order[k];
+                w.s0[k] = w.f.settled[c];
+                w.d0[k] = w.f.sediment[c];
+                double carried = arriving(w, c);
+                bool used;
+                double incised = 0.0, deposited = 0.0;
+                const int kind = own_walk(w.p, w.f, c, carried, &used, &incised, &deposited);
+                w.used[c] = used ? 1 : 0;
+                if (kind == ON || kind == LAKE) w.handoff[c] = carried;
+                if ((kind == SEA || kind == LAKE) && mouth_live(w, c, carried, kind)) {
+                    listed = true;
+                    w.ev_carried[k] = carried;
+                    w.ev_kind[k] = (int8_t)kind;
+                }
+            }
+            const unsigned ballot = __ballot_sync(0xFFFFFFFFu, listed);
+            if (lane == 0) warp_counts[warp] = __popc(ballot);
+            __syncthreads();
+            int before = block_base;
+            for (int i = 0; i < warp; ++i) before += warp_counts[i];
+            if (listed) w.seg_events[s_lo + before + __popc(ballot & ((1u << lane) - 1u))] = k;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int total = 0;
+                for (int i = 0; i < kThreads / 32; ++i) total += warp_counts[i];
+                block_base += total;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) w.seg_count[blockIdx.x] = block_base;
+        grid.sync();
+        // The listed mouths, dense and in rank order.
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            int n = 0;
+            for (int b = 0; b < (int)gridDim.x; ++b) {
+                const int b_lo = lo + b * seg;
+                for (int i = 0; i < w.seg_count[b]; ++i) w.events[n++] = w.seg_events[b_lo + i];
+            }
+            w.words[W_EVENTS] = n;
+        }
+        grid.sync();
+        const int n = *(volatile int*)&w.words[W_EVENTS];
+        int touch_n = 0;
+        // B: in chunks of `slots` mouths, the chunk's lake fans admitted at once, then its mouths in order.
+        for (int e0 = 0; e0 < n; e0 += w.slots) {
+            const int e1 = min(n, e0 + w.slots);
+            for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1; e += (int)(gridDim.x * blockDim.x)) {
+                const int k = w.events[e];
+                if (w.ev_kind[k] == LAKE) admit_lake(w, e - e0, k);
+            }
+            grid.sync();
+            if (blockIdx.x == 0 && threadIdx.x == 0) run_mouths(w, e0, e1, &touch_n);
+            grid.sync();
+        }
+        // C: the repairs.
+        if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) repair_level(w, L, lo, hi, n, touch_n);
+        grid.sync();
+    }
+}
+
+// settled = relative + sediment * toRelative, with no load and nothing incised yet
+// (HydraulicErosion.kt:940-945).
+__global__ void k_round_begin(const float* __restrict__ rel, const float* __restrict__ sediment, size_t N,
+                              float to_relative, float* __restrict__ settled, double* __restrict__ load,
+                              double* __restrict__ incised_at) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        settled[i] = __fadd_rn(rel[i], __fmul_rn(sediment[i], to_relative));
+        load[i] = 0.0;
+        incised_at[i] = 0.0;
+    }
+}
+
+__global__ void k_rank_of(const int* __restrict__ order, int n, int* __restrict__ rank_of) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) rank_of[order[k]] = k;
+}
+
+// Each level's first rank in the drainage order (level-major): level_start[levels] = n.
+__global__ void k_level_bounds(const int* __restrict__ order, const long long* __restrict__ key, int n, int levels,
+                               int* __restrict__ level_start) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int L = (int)(key[order[k]] >> 32);
+        const int prev = k > 0 ? (int)(key[order[k - 1]] >> 32) : -1;
+        for (int l = prev + 1; l <= L; ++l) level_start[l] = k;
+        if (k == n - 1)
+            for (int l = L + 1; l <= levels; ++l) level_start[l] = n;
+    }
+}
+
+// settle(): the stage's deposition laid on the rock at once; the sediment stays as the spoil the
+// mouths pass reads (HydraulicErosion.kt:1351-1364, 1451-1462).
+__global__ void k_settle(float* __restrict__ h, const float* __restrict__ sediment, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        h[i] = __fadd_rn(h[i], sediment[i]);
+}
+
+struct MouthsDev {
+    int W;
+    float pond_depth, drawn_river_cells, shoreline, fall_per_cell_width, floor_, step_ns, step_diag;
+    const uint8_t* land;
+    const float* filled;
+    const float* rel;
+    const float* area;
+    const int32_t* recv;
+    const float* spoil;
+    float* working;
+    const int* start;
+    const int* bucket;
+    int levels;
+};
+
+// Math.min(float, float) on the JVM: NaN if either is, and -0 below +0.
+__device__ __forceinline__ float jvm_minf(float a, float b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    if (a == 0.0f && b == 0.0f) return __float_as_int(a) < 0 ? a : b;
+    return a < b ? a : b;
+}
+
+// One cell of openMouths' pass (HydraulicErosion.kt:1855-1890).
+__device__ void mouth_cell(const MouthsDev& d, int cell) {
+    if (d.area[cell] < d.drawn_river_cells) return;
+    const float standing = __fsub_rn(d.filled[cell], d.rel[cell]);
+    const bool on_flat = standing > 0.0f && (standing <= d.pond_depth || d.spoil[cell] > 0.0f);
+    if (!on_flat) return;
+    const int receiver = d.recv[cell];
+    if (receiver < 0) return;
+    const float below = d.land[receiver] ? d.working[receiver] : d.shoreline;
+    const bool same_row = cell / d.W == receiver / d.W, same_col = cell % d.W == receiver % d.W;
+    const float step = (!same_row && !same_col) ? d.step_diag : (!same_row ? d.step_ns : 1.0f);
+    float fall = __fmul_rn(d.fall_per_cell_width, step);
+    if (fall < 1e-7f) fall = 1e-7f;   // MIN_DISTRIBUTARY_FALL
+    const float now = d.working[cell];
+    float want = jvm_minf(now, __fadd_rn(below, fall));
+    if (want < d.floor_) want = d.floor_;
+    if (now > want) d.working[cell] = (float)__dadd_rn((double)now, (double)__fsub_rn(want, now));
+}
+
+// Receivers first: levels from the top down, a grid barrier between levels.
+__global__ void __launch_bounds__(256) k_mouths_levels(MouthsDev d) {
+    cgr::grid_group grid = cgr::this_grid();
+    const int stride = gridDim.x * blockDim.x;
+    for (int level = d.levels - 1; level >= 0; --level) {
+        const int lo = d.start[level], hi = d.start[level + 1];
+        for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride) mouth_cell(d, d.bucket[i]);
+        grid.sync();
+    }
+}
+
+__global__ void k_zero_float(float* __restrict__ a, size_t N) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) a[i] = 0.0f;
+}
+
+}  // namespace
+
+cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
+    const size_t N = (size_t)W * H;
+    CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
+    CG_BUF(int, d_stamp, ctx, S_STAMP, N);
+    CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
+    CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
+    CG_LAUNCH(ctx) k_zero_float<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_sediment, N);
+    CG_CHECK_LAUNCH(ctx);
+    // Fan ids and replay generations restart at 0, so every stamp and mark must too.
+    CG_CUDA(ctx, cudaMemsetAsync(d_stamp, 0, N * sizeof(int), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_words, 0, W_WORDS * sizeof(int), ctx->stream));
+    return CG_OK;
+}
+
+cg_status deposit_round_begin_dev(cg_ctx* ctx, int W, int H, const float* d_rel, float to_relative, float** d_settled,
+                                  double** d_load, double** d_incised_at) {
+    const size_t N = (size_t)W * H;
+    CG_BUF(float, sediment, ctx, S_SEDIMENT, N);
+    CG_BUF(float, settled, ctx, S_SETTLED, N);
+    CG_BUF(double, load, ctx, S_LOAD, N);
+    CG_BUF(double, incised_at, ctx, S_INCISED, N);
+    CG_LAUNCH(ctx) k_round_begin<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_rel, sediment, N, to_relative, settled,
+                                                                          load, incised_at);
+    CG_CHECK_LAUNCH(ctx);
+    *d_settled = settled;
+    *d_load = load;
+    *d_incised_at = incised_at;
+    return CG_OK;
+}
+
+cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const DepositRound& r, DepositCounts* counts) {
+    const int W = cp.width, H = cp.height;
+    const size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    if (r.land_cells <= 0 || r.levels <= 0) return CG_OK;
+    const int n = r.land_cells;
+    WalkDev w;
+    w.p = make_params(cp, (float)r.land_cells, r.land_range, r.to_relative, r.shoreline);
+    CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
+    w.f = Fields{r.recv, r.land, r.ground, r.rel, r.area, r.surface, d_sediment, r.settled, r.incised_at};
+    // The drainage order and each level's first rank.
+    CG_BUF(int32_t, d_order, ctx, S_ORDER, N);
+    CG_TRY_ST(order_from_keys_dev(ctx, W, H, r.land, r.key, n, d_order));
+    CG_BUF(int, d_rank, ctx, S_DEPRANK, N);
+    CG_BUF(int, d_lstart, ctx, S_DEPLEVEL, (size_t)r.levels + 1);
+    const int grid = ctx->num_sms * 8;
+    CG_LAUNCH(ctx) k_rank_of<<<grid, 256, 0, sm>>>(d_order, n, d_rank);
+    CG_LAUNCH(ctx) k_level_bounds<<<grid, 256, 0, sm>>>(d_order, r.key, n, r.levels, d_lstart);
+    CG_CHECK_LAUNCH(ctx);
+    w.order = d_order;
+    w.rank_of = d_rank;
+    w.key = r.key;
+    w.level_start = d_lstart;
+    w.levels = r.levels;
+    w.load = r.load;
+    CG_BUF(double, d_handoff, ctx, S_HANDOFF, N);
+    CG_BUF(uint8_t, d_used, ctx, S_DEPUSED, N);
+    CG_BUF(float, d_s0, ctx, S_DEPS0, (size_t)n);
+    CG_BUF(float, d_d0, ctx, S_DEPD0, (size_t)n);
+    CG_BUF(double, d_evc, ctx, S_DEPEVC, (size_t)n);
+    CG_BUF(int8_t, d_evk, ctx, S_DEPEVK, (size_t)n);
+    CG_BUF(int, d_seg, ctx, S_DEPSEG, (size_t)n);
+    CG_BUF(int, d_events, ctx, S_DEPEVENTS, (size_t)n + 1);
+    CG_BUF(int, d_evtouch, ctx, S_DEPEVTOUCH, (size_t)n + 1);
+    w.handoff = d_handoff;
+    w.used = d_used;
+    w.s0 = d_s0;
+    w.d0 = d_d0;
+    w.ev_carried = d_evc;
+    w.ev_kind = d_evk;
+    w.seg_events = d_seg;
+    w.events = d_events;
+    w.ev_touch = d_evtouch;
+    // The heap's capacity (DeltaFan.Scratch) and the lake-admission slots.
+    w.cap = heap_capacity(w.p);
+    w.box_words = box_words(w.p);
+    w.slots = 2048;
+    const size_t S = (size_t)w.slots, cap = (size_t)w.cap;
+    CG_BUF(int, d_shc, ctx, S_DEPSLOT0, S * cap);
+    CG_BUF(float, d_shk, ctx, S_DEPSLOT1, S * cap);
+    CG_BUF(float, d_shp, ctx, S_DEPSLOT2, S * cap);
+    CG_BUF(int, d_sad, ctx, S_DEPSLOT3, S * cap);
+    CG_BUF(int, d_sso, ctx, S_DEPSLOT4, S * cap);
+    CG_BUF(double, d_sba, ctx, S_DEPSLOT5, S * cap);
+    CG_BUF(uint32_t, d_sbits, ctx, S_DEPSLOT6, S * (size_t)w.box_words);
+    CG_BUF(int, d_sn, ctx, S_DEPSLOT7, S);
+    w.slot_heap_cells = d_shc;
+    w.slot_heap_keys = d_shk;
+    w.slot_heap_pens = d_shp;
+    w.slot_admitted = d_sad;
+    w.slot_sorted = d_sso;
+    w.slot_base = d_sba;
+    w.slot_bits = d_sbits;
+    w.slot_n = d_sn;
+    CG_BUF(int, d_hc, ctx, S_DEPHEAP, 4 * cap);
+    w.heap_cells = d_hc;
+    w.heap_keys = (float*)(d_hc + cap);
+    w.heap_pens = (float*)(d_hc + 2 * cap);
+    w.heap_admitted = d_hc + 3 * cap;
+    CG_BUF(int, d_stamp, ctx, S_STAMP, N);
+    w.stamp = d_stamp;
+    w.touch_cap = (int)std::min<size_t>(N, (size_t)1 << 26);
+    CG_BUF(Touch, d_touch, ctx, S_DEPTOUCH, (size_t)w.touch_cap);
+    w.touches = d_touch;
+    CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
+    CG_BUF(int, d_replay, ctx, S_DEPREPLAY, N);
+    w.mark = d_mark;
+    w.replay = d_replay;
+    CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
+    w.words = d_words;
+    int per_sm = 0;
+    CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
+    if (per_sm < 1) return fail(ctx, CG_CUDA, "deposition kernel cannot be resident");
+    const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
+    CG_BUF(int, d_segc, ctx, S_DEPSEGC, (size_t)cgrid);
+    w.seg_count = d_segc;
+    void* kargs[] = {&w};
+    ctx->launches++;
+    CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_deposit_levels, cgrid, kThreads, kargs, 0, sm));
+    int words[W_WORDS];
+    CG_CUDA(ctx, cudaMemcpyAsync(words, d_words, sizeof(words), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    if (words[W_ERROR] & 1) return fail(ctx, CG_INEXACT, "deposition: a level's fan deposits overflowed the repair log");
+    if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
+    if (counts) {
+        counts->redone = words[W_REDONE];
+        counts->replayed = words[W_REPLAYED];
+    }
+    return CG_OK;
+}
+
+cg_status deposit_settle_dev(cg_ctx* ctx, int W, int H, float* d_h) {
+    const size_t N = (size_t)W * H;
+    CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
+    CG_LAUNCH(ctx) k_settle<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_h, d_sediment, N);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+cg_status open_mouths_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, const float* d_rain) {
+    const int W = p.width, H = p.height;
+    const size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    const ScaleF sc = scale_of(p);
+    const RatesF rates = rates_of(p);
+    const float land_half = std::fmax(sc.land_half(), 1e-6f);
+    const float sea_half = std::fmax(sc.sea_half(), 1e-6f);
+    CG_BUF(uint8_t, d_land, ctx, S_OM_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_OM_REL, N);
+    CG_BUF(float, d_filled, ctx, S_OM_FILLED, N);
+    CG_BUF(double, d_surface, ctx, S_SURFACE, N);
+    CG_BUF(int32_t, d_recv, ctx, S_OM_RECV, N);
+    CG_BUF(int32_t, d_donors, ctx, S_OM_DONORS, N);
+    CG_BUF(long long, d_key, ctx, S_OM_KEY, N);
+    CG_BUF(float, d_area, ctx, S_OM_AREA, N);
+    CG_BUF(float, d_runoff, ctx, S_OM_RUNOFF, N);
+    CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
+    // A fresh cut at today's shoreline, its fill, routing and discharge (HydraulicErosion.kt:1815-1840).
+    float shoreline;
+    int land_cells;
+    CG_TRY_ST(percentile_cut_dev(ctx, W, H, d_h, p.sea_level, land_half, sea_half, 0.0f, d_land, d_rel, &shoreline,
+                                 &land_cells));
+    if (land_cells == 0) return CG_OK;
+    CG_TRY_ST(fill_depressions_dev(ctx, W, H, d_land, d_rel, d_filled, nullptr, nullptr));
+    FlatCounts fc{0, 0, 0};
+    CG_TRY_ST(flow_directions_dev(ctx, W, H, d_land, d_rel, d_filled, p.seed, rates.cell_height_in_cell_widths,
+                                  smooth_field_lattice_columns(p.world_width_km), p.facet_routing != 0,
+                                  p.flat_potential != 0, d_recv, d_surface, &fc));
+    CG_TRY_ST(runoff_weights_dev(ctx, W, H, d_rain, d_land, land_cells, d_runoff));
+    int levels = 0;
+    CG_TRY_ST(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, &levels));
+    if (levels <= 0) return CG_OK;
+    int* d_bucket;
+    int* d_start;
+    CG_TRY_ST(level_buckets_dev(ctx, W, H, d_land, d_key, levels, &d_bucket, &d_start));
+    MouthsDev d;
+    d.W = W;
+    d.pond_depth = rates.pond_depth;
+    // drawnRiverCellsOn: DRAWN_RIVER_CATCHMENT_KM2 (deltaMinCatchmentKm2's 70000 / 5) in cells.
+    d.drawn_river_cells = (float)(14000.0 / (sc.cell_width_km(W) * sc.cell_height_km(H)));
+    d.shoreline = shoreline;
+    const float step = rates.pond_depth * land_half;
+    d.fall_per_cell_width = step * (0.15f / 23.4375f) * (float)sc.cell_width_km(W);   // DISTRIBUTARY_FALL_PER_KM
+    d.floor_ = shoreline + step * 0.15f;                                           // LOBE_RIM
+    d.step_ns = rates.step_ns;
+    d.step_diag = rates.step_diag;
+    d.land = d_land;
+    d.filled = d_filled;
+    d.rel = d_rel;
+    d.area = d_area;
+    d.recv = d_recv;
+    d.spoil = d_sediment;
+    d.working = d_h;
+    d.start = d_start;
+    d.bucket = d_bucket;
+    d.levels = levels;
+    int per_sm = 0;
+    CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mouths_levels, 256, 0));
+    if (per_sm < 1) return fail(ctx, CG_CUDA, "mouths kernel cannot be resident");
+    const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
+    void* kargs[] = {&d};
+    ctx->launches++;
+    CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_mouths_levels, cgrid, 256, kargs, 0, sm));
+    return CG_OK;
+}
+
+}  // namespace cg

@@ -22,7 +22,7 @@
 //      The levels from the lowest changed one upward are recomputed, and the check repeats; each
 //      replay settles its level for good, so the lowest open level only rises. The replay's list
 //      and heap are sized for the whole grid, so a level of any size is replayed. If the repairs'
-//      guard (64 passes) is ever reached with ties still open, the fill returns CG_INEXACT: its
+//      guard (256 passes) is ever reached with ties still open, the fill returns CG_INEXACT: its
 //      result is then not the reference's, and the stage does not carry on with it.
 #include <algorithm>
 #include <cfloat>
@@ -42,6 +42,7 @@ namespace {
 constexpr float kStep = 1e-6f;   // FlowRouting.FLAT_GRADIENT_STEP
 constexpr int T = 32;            // tile side
 constexpr int TH = 8;            // tile rows per thread pass (block is 32 x 8)
+constexpr int kReplaySpan = 1 << 12;   // key levels (consecutive float values) one replay orders
 
 // Cell classes. PINNED: parent fixed by the index rule on a key tie; EXACT: parent fixed by
 // replaying its key level's pops (both follow that parent instead of the minimum).
@@ -380,13 +381,14 @@ __global__ void k_reset_from(const uint8_t* __restrict__ cls, float* __restrict_
         if ((cls[i] == C_OPEN || follows_parent(cls[i])) && qkey(f[i]) >= Q) f[i] = INFINITY;
 }
 
-// The cells whose current level has key Q (the candidates for that level's heap), up to cap: land,
-// and water touching land (open water elsewhere never enters the flood).
+// The cells whose current level has a key in [Q, Qmax] (the candidates for the replay's heap), up
+// to cap: land, and water touching land (open water elsewhere never enters the flood).
 __global__ void k_gather_level(const float* __restrict__ f, const uint8_t* __restrict__ cls, int W, int H, int Q,
-                               int* __restrict__ list, int* __restrict__ count, int cap) {
+                               int Qmax, int* __restrict__ list, int* __restrict__ count, int cap) {
     size_t N = (size_t)W * H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        if (qkey(f[i]) != Q) continue;
+        const int q = qkey(f[i]);
+        if (q < Q || q > Qmax) continue;
         if (cls[i] == C_WATER) {
             const int row = pdiv((int)i, W), col = pmod((int)i, W);
             bool touches = false;
@@ -420,15 +422,28 @@ __device__ bool entered_below(const float* f, const uint8_t* cls, int W, int H, 
     return false;
 }
 
-// Replays key level Q of the priority flood (FlowRouting.kt:93-109) with one thread: a min-heap of
-// cell indices seeded with the level's cells that entered it from below; each pop visits its
-// neighbours in the reference's order, and each neighbour not yet visited takes its level from the
-// popped cell, joining this level's heap if its key is still Q. Every cell so reached gets its exact
-// parent (class EXACT). Bounded by the heap's capacity; an overflow is reported, never overrun.
+// Whether each cell was in the heap before key level Q opened (entered_below), for the replay: a
+// cell's answer depends only on levels below Q, which the replay never writes.
+__global__ void k_entered_below(const float* __restrict__ f, const uint8_t* __restrict__ cls, int W, int H, int Q,
+                                uint8_t* __restrict__ eb) {
+    const size_t N = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        eb[i] = entered_below(f, cls, W, H, (int)i, Q) ? 1 : 0;
+}
+
+// Replays key levels Q..Qmax of the priority flood (FlowRouting.kt:93-109) with one thread: a
+// min-heap on (key, index), seeded with the gathered cells that entered it from below Q (those
+// were pushed, with their final levels, before level Q opened: lower levels are exact here). Each
+// pop visits its neighbours in the reference's order, and each neighbour not yet visited takes its
+// level from the popped cell and joins the heap, as the reference pushes it. Popping stops at the
+// first key above Qmax. Every cell so reached gets its exact parent (class EXACT); a cell pushed
+// with a key above Qmax has its final level too, its first popped neighbour being the one that
+// reached it. Rewritten levels never fall below Q, so `entered_below` keeps its meaning throughout.
+// Bounded by the heap's capacity (each cell is pushed at most once); an overflow is reported.
 __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ g, uint8_t* __restrict__ cls,
                                int* __restrict__ pin, int* __restrict__ mark, int gen, const int* __restrict__ list,
-                               const int* __restrict__ list_n, int* __restrict__ heap, int cap, int W, int H, int Q,
-                               FillCounters* cnt) {
+                               const int* __restrict__ list_n, long long* __restrict__ heap, int cap, int W, int H,
+                               int Q, int Qmax, const uint8_t* __restrict__ eb, FillCounters* cnt) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int n = *list_n;
     if (n > cap) {
@@ -436,22 +451,22 @@ __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ 
         return;
     }
     int hs = 0;
-    auto push = [&](int v) -> bool {
+    auto push = [&](long long v) -> bool {
         if (hs >= cap) return false;
         int s = hs++;
         heap[s] = v;
         while (s > 0) {
             int p = (s - 1) >> 1;
             if (heap[p] <= heap[s]) break;
-            int t = heap[p];
+            long long t = heap[p];
             heap[p] = heap[s];
             heap[s] = t;
             s = p;
         }
         return true;
     };
-    auto pop = [&]() -> int {
-        int top = heap[0];
+    auto pop = [&]() -> long long {
+        long long top = heap[0];
         heap[0] = heap[--hs];
         int s = 0;
         while (true) {
@@ -460,20 +475,21 @@ __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ 
             int r = l + 1;
             int m = (r < hs && heap[r] < heap[l]) ? r : l;
             if (heap[s] <= heap[m]) break;
-            int t = heap[m];
+            long long t = heap[m];
             heap[m] = heap[s];
             heap[s] = t;
             s = m;
         }
         return top;
     };
+    auto key_of = [&](int cell) { return ((long long)qkey(f[cell]) << 32) | (unsigned)cell; };
     for (int k = 0; k < n; ++k)
-        if (entered_below(f, cls, W, H, list[k], Q) && !push(list[k])) {
+        if (eb[list[k]] && !push(key_of(list[k]))) {
             cnt->overflow = 1;
             return;
         }
-    while (hs > 0) {
-        int x = pop();
+    while (hs > 0 && (int)(heap[0] >> 32) <= Qmax) {
+        int x = (int)(pop() & 0xFFFFFFFFll);
         float fx = f[x];
         int row = pdiv(x, W), col = pmod(x, W);
         for (int rs = -1; rs <= 1; ++rs) {
@@ -482,7 +498,7 @@ __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ 
             for (int cs = -1; cs <= 1; ++cs) {
                 if (rs == 0 && cs == 0) continue;
                 int y = nr * W + wrap_col(col + cs, W);
-                if (mark[y] == gen || entered_below(f, cls, W, H, y, Q)) continue;
+                if (mark[y] == gen || eb[y]) continue;
                 mark[y] = gen;
                 float fy = phi(fx, g[y]);
                 if (cls[y] != C_DRAINED) {
@@ -490,7 +506,7 @@ __global__ void k_replay_level(float* __restrict__ f, const float* __restrict__ 
                     cls[y] = C_EXACT;
                 }
                 f[y] = fy;
-                if (qkey(fy) == Q && !push(y)) {
+                if (!push(key_of(y))) {
                     cnt->overflow = 1;
                     return;
                 }
@@ -557,18 +573,20 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
     // sized for every cell of the grid (a key level can hold any share of the grid).
     const int cap = (int)N;
     CG_BUF(int, d_mark, ctx, S_SCRATCH3, N);
-    CG_BUF(int, d_replay, ctx, S_CG4, 2 * (size_t)cap + 4);
+    CG_BUF(uint8_t, d_eb, ctx, S_FILLEB, N);
+    CG_BUF(int, d_replay, ctx, S_CG4, 3 * (size_t)cap + 4);
     int* d_list = d_replay;
-    int* d_heap = d_replay + cap;
-    int* d_list_n = d_replay + 2 * cap;
+    long long* d_heap = (long long*)(d_replay + cap + (cap & 1));   // 8-byte aligned
+    int* d_list_n = d_replay + 3 * (size_t)cap + 2;
     CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), sm));
     int gen = 0;
 
     FillCounters hc;
     int64_t tie_total = 0, unresolved_total = 0;
+    int replays = 0;
     // Each pass either settles, pins tie parents by the index rule, or replays the lowest level
     // holding a tie the index rule cannot order; the cap is a guard, not the expected exit.
-    const int max_repairs = 64;
+    const int max_repairs = 256;
     for (int repair = 0; repair <= max_repairs; ++repair) {
         CG_CUDA(ctx, cudaMemsetAsync(d_lists, 0, (2 * (size_t)tiles + 4) * sizeof(int), sm));
         CG_CUDA(ctx, cudaMemsetAsync(d_marks, 0, 2 * (size_t)tiles * sizeof(int), sm));
@@ -603,13 +621,23 @@ cg_status fill_depressions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land,
         }
         int from = hc.repaired ? hc.repair_level : INT_MAX;
         if (hc.unresolved) {
-            // Replay the lowest key level whose ties only its own pops can order.
-            const int Q = hc.min_level;
+            // Replay from the lowest key level Q whose ties only its own pops can order, or from the
+            // lowest level at which a pin changed in this pass if that is lower: below it every level
+            // is final (a pin's parent sits at or above that level), so the replay's seeds (cells
+            // entered from below Q) hold their final levels, and the replay orders the pinned cells it
+            // reaches exactly too. The first replays of a call take that level alone; later ones run
+            // on through a span of key levels that doubles up to kReplaySpan: a broad flat raises a
+            // staircase of levels, each with such ties, and one replay then orders many of them.
+            const int Q = hc.repaired ? std::min(hc.min_level, hc.repair_level) : hc.min_level;
+            const int span = replays < 8 ? 0 : std::min(1 << std::min(replays - 8, 12), kReplaySpan);
+            const int Qmax = Q + span;
+            ++replays;
             ++gen;
             CG_CUDA(ctx, cudaMemsetAsync(d_list_n, 0, sizeof(int), sm));
-            CG_LAUNCH(ctx) k_gather_level<<<grid, 256, 0, sm>>>(d_filled, d_cls, W, H, Q, d_list, d_list_n, cap);
+            CG_LAUNCH(ctx) k_gather_level<<<grid, 256, 0, sm>>>(d_filled, d_cls, W, H, Q, Qmax, d_list, d_list_n, cap);
+            CG_LAUNCH(ctx) k_entered_below<<<grid, 256, 0, sm>>>(d_filled, d_cls, W, H, Q, d_eb);
             CG_LAUNCH(ctx) k_replay_level<<<1, 32, 0, sm>>>(d_filled, d_rel, d_cls, d_pin, d_mark, gen, d_list, d_list_n,
-                                                            d_heap, cap, W, H, Q, d_cnt);
+                                                            d_heap, cap, W, H, Q, Qmax, d_eb, d_cnt);
             CG_CHECK_LAUNCH(ctx);
             int overflow = 0;
             CG_CUDA(ctx, cudaMemcpyAsync(&overflow, &d_cnt->overflow, sizeof(int), cudaMemcpyDeviceToHost, sm));

@@ -61,9 +61,15 @@ struct InciseArgs {
     float step_diag;
     int only_above_base;
 };
+// d_incised_at (may be NULL): per cell, what the incision took off it, in double (profile P2).
 cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const long long* d_key,
                      int levels, const float* d_ground, const float* d_rel, const float* d_area, const float* d_erod,
-                     float* d_surface, const InciseArgs& a);
+                     float* d_surface, const InciseArgs& a, double* d_incised_at = nullptr);
+// Land cells bucketed by Kahn level (the high half of the drainage key): d_bucket (N) holds them
+// level after level, d_start (levels + 1) each level's first slot. Cells within a level are in no
+// particular order.
+cg_status level_buckets_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const long long* d_key, int levels,
+                            int** d_bucket, int** d_start);
 // FlowRouting.spillways on the device: per basin (in the order the reference finds them) its entry,
 // pour point, level, floor, fill depth and cell count, in the context's basin block; d_label
 // receives each ponded cell's basin. *h_count (synchronises) receives the number of basins.
@@ -91,10 +97,53 @@ struct BreachRates {
     float step_diag;
 };
 // HydraulicErosion.breach over the basins of this routing: d_rel, d_ground and d_surface are cut in
-// place. *h_cells (optional) receives the cells cut.
+// place. *h_cells (optional) receives the cells cut. Where sediment is carried (profile P2's rounds)
+// d_settled falls with each cut and d_load gathers what it took; both NULL otherwise.
 cg_status breach_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, float* d_rel, float* d_ground,
                      const int32_t* d_recv, const float* d_area, float land_cells, float land_range,
-                     const BreachRates& rates, float* d_surface, int* h_cells);
+                     const BreachRates& rates, float* d_surface, int* h_cells, float* d_settled = nullptr,
+                     double* d_load = nullptr);
+
+// ---- weights (cg_stage.cu)
+// normaliseOverLand (HydraulicErosion.kt:550-569): each cell's rain over the land's mean rain (the
+// reference's sequential double sum in cell order); all ones when d_rain is NULL.
+cg_status runoff_weights_dev(cg_ctx* ctx, int W, int H, const float* d_rain, const uint8_t* d_land, int land_cells,
+                             float* d_runoff);
+
+// ---- deposition, profile P2 (cg_deposit.cu)
+// The stage's deposition state at its start: no sediment, fresh fan stamps.
+cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H);
+// A round's start (HydraulicErosion.kt:940-945): settled = relative + sediment, no load, nothing
+// incised; returns the round's settled, load and incisedAt fields (context buffers).
+cg_status deposit_round_begin_dev(cg_ctx* ctx, int W, int H, const float* d_rel, float to_relative, float** d_settled,
+                                  double** d_load, double** d_incised_at);
+// What one round's walk reads: the round's routing, its cut and the fields of deposit_round_begin_dev.
+struct DepositRound {
+    const int32_t* recv;
+    const uint8_t* land;
+    const float* ground;      // the filled surface
+    const float* rel;
+    const float* area;
+    const long long* key;     // drainage keys (level << 32 | deepest source)
+    int levels;
+    int land_cells;
+    float land_range, to_relative, shoreline;
+    const float* surface;     // the working field after the incision
+    float* settled;
+    const double* load;       // the notch's hand-offs
+    const double* incised_at;
+};
+struct DepositCounts {
+    int redone;     // levels restored and walked one cell after another
+    int replayed;   // ponded cells whose settled height was replayed in rank order
+};
+// The deposition walk of one round (HydraulicErosion.kt:1068-1349), the sediment in the stage's buffer.
+cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& p, const DepositRound& r, DepositCounts* counts);
+// settle() (HydraulicErosion.kt:1351-1364): the sediment laid on d_h; the sediment is kept as the spoil.
+cg_status deposit_settle_dev(cg_ctx* ctx, int W, int H, float* d_h);
+// openMouths (HydraulicErosion.kt:1804-1892) over d_h, with the spoil of deposit_settle_dev. Routes on
+// buffers of its own: the stage's last routing is left as it was.
+cg_status open_mouths_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, const float* d_rain);
 
 // ---- small helpers (cg_api.cu)
 cg_status sync(cg_ctx* ctx);

@@ -123,31 +123,62 @@ cg_status cancelled(cg_ctx* ctx) {
 
 }  // namespace
 
-// The round loop with the world resident on the device. `d_h` holds the input heights and
-// receives the result (through *d_result, which is d_h or the ping-pong partner).
-cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, float* d_h2, const float* d_uplift,
-                          const float* d_rock, const float* d_rain, const float* d_veg, float** d_result,
-                          cg_round_stats* stats, int* last_land_cells) {
+cg_status runoff_weights_dev(cg_ctx* ctx, int W, int H, const float* d_rain, const uint8_t* d_land, int land_cells,
+                             float* d_runoff) {
+    const size_t N = (size_t)W * H;
+    const int grid = ctx->num_sms * 8;
+    if (d_rain) {
+        CG_BUF(double, d_sum, ctx, S_CG3, 2);
+        CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, ctx->stream>>>(d_rain, d_land, N, 0, d_sum);
+        CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, ctx->stream>>>(d_rain, d_sum, land_cells, N, d_runoff);
+    } else {
+        CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, ctx->stream>>>(d_runoff, N, 1.0f);
+    }
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+// ErosionStage.apply's opening (ErosionStage.kt:163-172): the initial thermal sweeps over the
+// resident world. Marks the run done when no hydraulic round will run.
+cg_status stage_begin_dev(cg_ctx* ctx, StageRun& run) {
+    const cg_erosion_params& p = run.p;
+    run.next_round = 0;
+    run.land_cells = -1;
+    run.done = false;
+    if (!p.enabled) {
+        run.done = true;
+        return CG_OK;
+    }
+    if (p.profile >= CG_PROFILE_P2) CG_TRY(deposit_stage_reset_dev(ctx, p.width, p.height));
+    const int sweeps = sweeps_for(p);
+    if (sweeps > 0) {
+        float* res;
+        CG_TRY(thermal_sweeps_dev(ctx, p.width, p.height, run.cur, run.other, thermal_limits(p), sweeps, p.rate, &res));
+        if (res != run.cur) std::swap(run.cur, run.other);
+    }
+    if (p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) run.done = true;
+    return CG_OK;
+}
+
+// HydraulicErosion.apply's rounds [run.next_round, end_round) on the resident world, each relaxed by
+// sweepsFor/rounds sweeps. `stats` (may be NULL) receives one entry per round run, the first for
+// round run.next_round.
+cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_stats* stats) {
+    const cg_erosion_params& p = run.p;
     const int W = p.width, H = p.height;
     const size_t N = (size_t)W * H;
     cudaStream_t sm = ctx->stream;
     const int grid = ctx->num_sms * 8;
-    float* cur = d_h;
-    float* other = d_h2;
-    *d_result = cur;
-    *last_land_cells = -1;
-    if (!p.enabled) return CG_OK;
+    const int first_round = run.next_round;
+    if (run.done || end_round <= first_round) return CG_OK;
+    const float* d_uplift = run.uplift;
+    const float* d_rock = run.rock;
+    const float* d_rain = run.rain;
+    const float* d_veg = run.veg;
     const cg_thermal_limits lim = thermal_limits(p);
     const int sweeps = sweeps_for(p);
-    if (sweeps > 0) {
-        float* res;
-        CG_TRY(thermal_sweeps_dev(ctx, W, H, cur, other, lim, sweeps, p.rate, &res));
-        if (res != cur) std::swap(cur, other);
-    }
-    *d_result = cur;
     int per_round = sweeps / (p.hydraulic_rounds < 1 ? 1 : p.hydraulic_rounds);
     if (per_round < 1) per_round = 1;
-    if (p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) return CG_OK;
 
     const ScaleF sc = scale_of(p);
     const RatesF rates = rates_of(p);
@@ -190,8 +221,9 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         if (stats) cudaEventRecord(ev[i], sm);
     };
 
-    for (int round = 0; round < p.hydraulic_rounds; ++round) {
+    for (int round = first_round; round < end_round; ++round) {
         CG_TRY(cancelled(ctx));
+        float* cur = run.cur;
         const long long launches0 = ctx->launches;
         mark(0);
         if (d_uplift) CG_LAUNCH(ctx) k_uplift<<<grid, 256, 0, sm>>>(cur, d_uplift, N, per_mm, sc.relief_span());
@@ -199,11 +231,13 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         int land_cells;
         CG_TRY(percentile_cut_dev(ctx, W, H, cur, p.sea_level, land_half, sea_half, stand_below_today(p, round),
                                   d_land, d_rel, &shoreline, &land_cells));
-        *last_land_cells = land_cells;
-        if (land_cells == 0) {
-            *d_result = cur;
+        if (land_cells == 0) {   // HydraulicErosion.kt:856-858: the rounds stop where the land is gone
+            run.done = true;
+            run.next_round = round;
+            run.land_cells = 0;
             return CG_OK;
         }
+        run.land_cells = land_cells;
         // normaliseOverLand / shieldingOverLand (HydraulicErosion.kt:902-911).
         if (!d_rain && (!d_veg || !p.shield_cut)) {
             CG_LAUNCH(ctx) k_unit_weights<<<grid, 256, 0, sm>>>(d_rock, N, d_runoff, d_erod);
@@ -234,9 +268,17 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         int levels = 0;
         CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_runoff, d_key, d_donors, d_area, &levels));
         mark(4);
-        if (p.profile == CG_PROFILE_P1)
+        const bool notch = p.profile >= CG_PROFILE_P1, deposition = p.profile >= CG_PROFILE_P2;
+        const bool closing = round == p.hydraulic_rounds - 1;
+        const float to_relative = 1.0f / land_half;
+        float* d_settled = nullptr;
+        double* d_load = nullptr;
+        double* d_incised_at = nullptr;
+        if (deposition)
+            CG_TRY(deposit_round_begin_dev(ctx, W, H, d_rel, to_relative, &d_settled, &d_load, &d_incised_at));
+        if (notch)
             CG_TRY(breach_dev(ctx, W, H, d_land, d_rel, d_filled, d_recv, d_area, (float)land_cells, land_half, brates,
-                              cur, nullptr));
+                              cur, nullptr, d_settled, d_load));
         InciseArgs ia;
         ia.courant_coefficient = rates.courant_coefficient;
         ia.pond_depth = rates.pond_depth;
@@ -246,8 +288,30 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
         ia.step_ns = rates.step_ns;
         ia.step_diag = rates.step_diag;
         ia.only_above_base = p.receiver_clamp != 0;
-        CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia));
-        if (p.profile == CG_PROFILE_P1 && round == p.hydraulic_rounds - 1) {
+        CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia,
+                          d_incised_at));
+        DepositCounts dc{0, 0};
+        if (deposition) {
+            DepositRound dr;
+            dr.recv = d_recv;
+            dr.land = d_land;
+            dr.ground = d_filled;
+            dr.rel = d_rel;
+            dr.area = d_area;
+            dr.key = d_key;
+            dr.levels = levels;
+            dr.land_cells = land_cells;
+            dr.land_range = land_half;
+            dr.to_relative = to_relative;
+            dr.shoreline = shoreline;
+            dr.surface = cur;
+            dr.settled = d_settled;
+            dr.load = d_load;
+            dr.incised_at = d_incised_at;
+            CG_TRY(deposit_walk_dev(ctx, p, dr, &dc));
+        }
+        if (closing && deposition) CG_TRY(deposit_settle_dev(ctx, W, H, cur));
+        if (notch && closing) {
             // The closing breach (HydraulicErosion.kt:1404-1442): a fresh cut at today's shoreline over
             // the finished surface, its own fill, routing and discharge, then one more notch. Its
             // routing is what the stage reports.
@@ -255,7 +319,7 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
             int closing_land;
             CG_TRY(percentile_cut_dev(ctx, W, H, cur, p.sea_level, land_half, sea_half, 0.0f, d_land, d_rel,
                                       &closing_shoreline, &closing_land));
-            *last_land_cells = closing_land;
+            run.land_cells = closing_land;
             if (closing_land > 0) {
                 if (d_rain) {
                     CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_rain, d_land, N, 0, d_sum);
@@ -274,12 +338,14 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
                                   brates, cur, nullptr));
             }
         }
+        // The closing mouths pass (HydraulicErosion.kt:1451-1462), ErosionConfig.deltaLobe.
+        if (closing && deposition) CG_TRY(open_mouths_dev(ctx, p, cur, d_rain));
         mark(5);
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         float* res;
-        CG_TRY(thermal_sweeps_dev(ctx, W, H, cur, other, lim, per_round, p.rate, &res));
-        if (res != cur) std::swap(cur, other);
-        *d_result = cur;
+        CG_TRY(thermal_sweeps_dev(ctx, W, H, run.cur, run.other, lim, per_round, p.rate, &res));
+        if (res != run.cur) std::swap(run.cur, run.other);
+        run.next_round = round + 1;
         mark(6);
         if (stats) {
             CG_CUDA(ctx, cudaEventSynchronize(ev[6]));
@@ -287,7 +353,7 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
             for (int i = 1; i < 7; ++i) cudaEventElapsedTime(&ms[i], ev[i - 1], ev[i]);
             float total = 0.0f;
             cudaEventElapsedTime(&total, ev[0], ev[6]);
-            cg_round_stats& s = stats[round];
+            cg_round_stats& s = stats[round - first_round];
             std::memset(&s, 0, sizeof(s));
             s.round = round;
             s.land_cells = land_cells;
@@ -308,7 +374,30 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
             s.ms_relax = ms[6];
         }
     }
+    if (run.next_round >= p.hydraulic_rounds) run.done = true;
     return CG_OK;
+}
+
+// The whole stage with the world resident on the device. `d_h` holds the input heights and
+// receives the result (through *d_result, which is d_h or the ping-pong partner).
+cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, float* d_h2, const float* d_uplift,
+                          const float* d_rock, const float* d_rain, const float* d_veg, float** d_result,
+                          cg_round_stats* stats, int* last_land_cells) {
+    StageRun run;
+    run.p = p;
+    run.cur = d_h;
+    run.other = d_h2;
+    run.uplift = d_uplift;
+    run.rock = d_rock;
+    run.rain = d_rain;
+    run.veg = d_veg;
+    *d_result = d_h;
+    *last_land_cells = -1;
+    cg_status st = stage_begin_dev(ctx, run);
+    if (st == CG_OK) st = stage_rounds_dev(ctx, run, p.hydraulic_rounds, stats);
+    *d_result = run.cur;
+    *last_land_cells = run.land_cells;
+    return st;
 }
 
 }  // namespace cg
@@ -317,54 +406,13 @@ using namespace cg;
 
 namespace {
 
-// cg_erode_stage without clearing the cancel flag (a batch clears it once for all its worlds).
-cg_status erode_stage_host(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
-                           cg_round_stats* stats) {
-    if (!ctx || !p || !in || !out || !in->height || !out->height) return CG_BAD_ARG;
-    if (p->abi_version != CG_ABI_VERSION)
-        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
-                    CG_ABI_VERSION);
-    CG_TRY(check_grid(ctx, p->width, p->height));
-    if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
-    if (p->profile != CG_PROFILE_P0 && p->profile != CG_PROFILE_P1)
-        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 and P1 only)", p->profile);
-    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+// The stage's outputs (cg_outputs) from the device: the result field and, when the last round
+// routed, that round's routing fields, drainage order and basins.
+cg_status download_outputs(cg_ctx* ctx, const cg_erosion_params& pp, const float* d_res, int land_cells,
+                           cg_outputs* out) {
+    const cg_erosion_params* p = &pp;
     const int W = p->width, H = p->height;
     const size_t N = (size_t)W * H;
-    CG_BUF(float, d_h, ctx, S_H0, N);
-    CG_BUF(float, d_h2, ctx, S_H1, N);
-    float* d_up = nullptr;
-    float* d_rock = nullptr;
-    float* d_rain = nullptr;
-    float* d_veg = nullptr;
-    CG_TRY(up(ctx, d_h, in->height, N * 4));
-    // Inputs, each in its own slot.
-    {
-        cg_status st = CG_OK;
-        if (in->uplift_mm_per_year) {
-            d_up = (float*)buf(ctx, S_UPLIFT, N * 4, &st);
-            if (st != CG_OK) return st;
-            CG_TRY(up(ctx, d_up, in->uplift_mm_per_year, N * 4));
-        }
-        if (in->rock_erodibility) {
-            d_rock = (float*)buf(ctx, S_ROCK, N * 4, &st);
-            if (st != CG_OK) return st;
-            CG_TRY(up(ctx, d_rock, in->rock_erodibility, N * 4));
-        }
-        if (in->rainfall_mm) {
-            d_rain = (float*)buf(ctx, S_RAIN, N * 4, &st);
-            if (st != CG_OK) return st;
-            CG_TRY(up(ctx, d_rain, in->rainfall_mm, N * 4));
-        }
-        if (in->vegetation_density) {
-            d_veg = (float*)buf(ctx, S_VEG, N * 4, &st);
-            if (st != CG_OK) return st;
-            CG_TRY(up(ctx, d_veg, in->vegetation_density, N * 4));
-        }
-    }
-    float* d_res = d_h;
-    int land_cells = -1;
-    CG_TRY(erode_stage_dev(ctx, *p, d_h, d_h2, d_up, d_rock, d_rain, d_veg, &d_res, stats, &land_cells));
     CG_TRY(down(ctx, out->height, d_res, N * 4));
     const bool routed = land_cells > 0 && p->enabled && p->hydraulic_rounds > 0 && p->bedrock_erodibility_per_year > 0.0f;
     if (routed) {
@@ -390,6 +438,73 @@ cg_status erode_stage_host(cg_ctx* ctx, const cg_erosion_params* p, const cg_inp
             if (out->basin_of_cell) CG_TRY(down(ctx, out->basin_of_cell, d_lab, N * 4));
         }
     }
+    return CG_OK;
+}
+
+// The parameters' checks shared by the stage's entry points. `fed_ok`: the caller can hand in the
+// weather between rounds (the round-range entry points), so climate_feed is accepted.
+cg_status check_params(cg_ctx* ctx, const cg_erosion_params* p, bool fed_ok) {
+    if (p->abi_version != CG_ABI_VERSION)
+        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
+                    CG_ABI_VERSION);
+    CG_TRY(check_grid(ctx, p->width, p->height));
+    if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
+    if (p->profile < CG_PROFILE_P0 || p->profile > CG_PROFILE_P2)
+        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0, P1 and P2)", p->profile);
+    if (p->climate_feed && !fed_ok)
+        return fail(ctx, CG_UNSUPPORTED,
+                    "climate_feed asks for the caller's weather halfway through the rounds: run the stage with "
+                    "cg_stage_begin / cg_erode_rounds");
+    return CG_OK;
+}
+
+// Copies one optional host field into its slot; *d stays NULL when the field is not given.
+cg_status upload_optional(cg_ctx* ctx, int slot, const float* host, size_t N, float** d) {
+    *d = nullptr;
+    if (!host) return CG_OK;
+    cg_status st = CG_OK;
+    *d = (float*)buf(ctx, slot, N * 4, &st);
+    if (st != CG_OK) return st;
+    return up(ctx, *d, host, N * 4);
+}
+
+// Uploads a world's inputs into the context's slots (heights into S_H0, S_H1 reserved for the
+// ping-pong partner) and fills the run's device pointers.
+cg_status upload_world(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, StageRun& run) {
+    const size_t N = (size_t)p->width * p->height;
+    CG_BUF(float, d_h, ctx, S_H0, N);
+    CG_BUF(float, d_h2, ctx, S_H1, N);
+    CG_TRY(up(ctx, d_h, in->height, N * 4));
+    float *d_up, *d_rock, *d_rain, *d_veg;
+    CG_TRY(upload_optional(ctx, S_UPLIFT, in->uplift_mm_per_year, N, &d_up));
+    CG_TRY(upload_optional(ctx, S_ROCK, in->rock_erodibility, N, &d_rock));
+    CG_TRY(upload_optional(ctx, S_RAIN, in->rainfall_mm, N, &d_rain));
+    CG_TRY(upload_optional(ctx, S_VEG, in->vegetation_density, N, &d_veg));
+    run = StageRun();
+    run.p = *p;
+    run.cur = d_h;
+    run.other = d_h2;
+    run.uplift = d_up;
+    run.rock = d_rock;
+    run.rain = d_rain;
+    run.veg = d_veg;
+    return CG_OK;
+}
+
+// cg_erode_stage without clearing the cancel flag (a batch clears it once for all its worlds).
+cg_status erode_stage_host(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
+                           cg_round_stats* stats) {
+    if (!ctx || !p || !in || !out || !in->height || !out->height) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
+    CG_TRY(check_params(ctx, p, false));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    StageRun run;
+    CG_TRY(upload_world(ctx, p, in, run));
+    float* d_res = run.cur;
+    int land_cells = -1;
+    CG_TRY(erode_stage_dev(ctx, *p, run.cur, run.other, run.uplift, run.rock, run.rain, run.veg, &d_res, stats,
+                           &land_cells));
+    CG_TRY(download_outputs(ctx, *p, d_res, land_cells, out));
     return sync(ctx);
 }
 
@@ -400,12 +515,14 @@ extern "C" {
 cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out,
                          cg_round_stats* stats) {
     if (!ctx) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     ctx->cancel.store(0);
     return erode_stage_host(ctx, p, in, out, stats);
 }
 
 cg_status cg_erode_batch(cg_ctx* ctx, int32_t n_worlds, const cg_world* worlds, cg_status* status) {
     if (!ctx || n_worlds < 0 || (n_worlds > 0 && !worlds)) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     ctx->cancel.store(0);
     cg_status first = CG_OK;
     for (int32_t i = 0; i < n_worlds; ++i) {
@@ -428,13 +545,8 @@ cg_status cg_erode_batch(cg_ctx* ctx, int32_t n_worlds, const cg_world* worlds, 
 cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in, float* out_dev,
                              cg_round_stats* stats, int32_t* land_cells_out) {
     if (!ctx || !p || !in || !in->height || !out_dev) return CG_BAD_ARG;
-    if (p->abi_version != CG_ABI_VERSION)
-        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
-                    CG_ABI_VERSION);
-    CG_TRY(check_grid(ctx, p->width, p->height));
-    if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
-    if (p->profile != CG_PROFILE_P0 && p->profile != CG_PROFILE_P1)
-        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 and P1 only)", p->profile);
+    ctx->run.active = false;   // this call reuses the resident world's buffers
+    CG_TRY(check_params(ctx, p, false));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->cancel.store(0);
     const size_t N = (size_t)p->width * p->height;
@@ -450,10 +562,80 @@ cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* p, const cg_i
     return sync(ctx);
 }
 
+cg_status cg_stage_begin(cg_ctx* ctx, const cg_erosion_params* p, const cg_inputs* in) {
+    if (!ctx || !p || !in || !in->height) return CG_BAD_ARG;
+    ctx->run.active = false;
+    CG_TRY(check_params(ctx, p, true));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cancel.store(0);
+    StageRun run;
+    CG_TRY(upload_world(ctx, p, in, run));
+    CG_TRY(stage_begin_dev(ctx, run));
+    CG_TRY(sync(ctx));
+    run.active = true;
+    ctx->run = run;
+    return CG_OK;
+}
+
+cg_status cg_erode_rounds(cg_ctx* ctx, int32_t first_round, int32_t end_round, const cg_weather* weather,
+                          cg_round_stats* stats) {
+    if (!ctx) return CG_BAD_ARG;
+    StageRun& run = ctx->run;
+    if (!run.active) return fail(ctx, CG_BAD_ARG, "no resident world: call cg_stage_begin first");
+    const cg_erosion_params& p = run.p;
+    if (first_round != run.next_round && !(run.done && first_round >= run.next_round))
+        return fail(ctx, CG_BAD_ARG, "rounds run in order: the next round is %d, not %d", run.next_round, first_round);
+    if (end_round < first_round || end_round > (p.hydraulic_rounds > 0 ? p.hydraulic_rounds : 0))
+        return fail(ctx, CG_BAD_ARG, "round range [%d, %d) is outside the stage's %d rounds", first_round, end_round,
+                    p.hydraulic_rounds);
+    const int refresh_at = p.climate_feed && p.hydraulic_rounds > 1 ? p.hydraulic_rounds / 2 : -1;
+    if (refresh_at > first_round && refresh_at < end_round)
+        return fail(ctx, CG_BAD_ARG, "climate_feed: round %d takes the refreshed weather, so a call may not run across it",
+                    refresh_at);
+    if (p.climate_feed && (first_round == 0 || first_round == refresh_at) && !weather && end_round > first_round)
+        return fail(ctx, CG_BAD_ARG, "climate_feed: round %d needs the caller's weather", first_round);
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cancel.store(0);
+    const size_t N = (size_t)p.width * p.height;
+    if (weather) {   // replaces the rounds' weather from first_round on; a NULL field is the default
+        float *d_rain, *d_veg;
+        CG_TRY(upload_optional(ctx, S_RAIN, weather->rainfall_mm, N, &d_rain));
+        CG_TRY(upload_optional(ctx, S_VEG, weather->vegetation_density, N, &d_veg));
+        run.rain = d_rain;
+        run.veg = d_veg;
+    }
+    cg_status st = stage_rounds_dev(ctx, run, end_round, stats);
+    if (st != CG_OK) {
+        run.active = false;   // a round stopped part way: the world is no longer a whole terrain
+        return st;
+    }
+    return sync(ctx);
+}
+
+cg_status cg_stage_height(cg_ctx* ctx, float* height) {
+    if (!ctx || !height) return CG_BAD_ARG;
+    if (!ctx->run.active) return fail(ctx, CG_BAD_ARG, "no resident world: call cg_stage_begin first");
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    CG_TRY(down(ctx, height, ctx->run.cur, (size_t)ctx->run.p.width * ctx->run.p.height * 4));
+    return sync(ctx);
+}
+
+cg_status cg_stage_finish(cg_ctx* ctx, cg_outputs* out) {
+    if (!ctx || !out || !out->height) return CG_BAD_ARG;
+    StageRun& run = ctx->run;
+    if (!run.active) return fail(ctx, CG_BAD_ARG, "no resident world: call cg_stage_begin first");
+    if (!run.done) return fail(ctx, CG_BAD_ARG, "round %d of %d is still to run", run.next_round, run.p.hydraulic_rounds);
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    run.active = false;
+    CG_TRY(download_outputs(ctx, run.p, run.cur, run.land_cells, out));
+    return sync(ctx);
+}
+
 cg_status cg_percentile_cut(cg_ctx* ctx, int32_t W, int32_t H, const float* heights, float sea_level,
                             float highest_land, float deepest_ocean, float lowstand_share, float* shoreline,
                             uint8_t* is_land, float* relative, int32_t* land_cells) {
     if (!ctx || !heights || !shoreline || !is_land || !relative || !land_cells) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     size_t N = (size_t)W * H;
@@ -477,6 +659,7 @@ cg_status cg_percentile_cut(cg_ctx* ctx, int32_t W, int32_t H, const float* heig
 cg_status cg_fill_depressions(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const float* relative,
                               float* filled, int64_t* ties, int64_t* unresolved) {
     if (!ctx || !is_land || !relative || !filled) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     size_t N = (size_t)W * H;
@@ -494,6 +677,7 @@ cg_status cg_flow_directions(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* i
                              const float* filled, int64_t seed, double r, int32_t lattice, int32_t by_facet,
                              int32_t over_potential, int32_t* receivers, double* surface, int32_t* flat_counts) {
     if (!ctx || !is_land || !relative || !filled || !receivers) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     if (!(r > 0.0) || lattice < 1) return fail(ctx, CG_BAD_ARG, "bad cell aspect %g or lattice %d", r, lattice);
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -523,6 +707,7 @@ cg_status cg_flow_directions(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* i
 cg_status cg_drainage_order(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const int32_t* receivers,
                             int32_t land_cells, int32_t* order) {
     if (!ctx || !is_land || !receivers || !order || land_cells < 0) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     size_t N = (size_t)W * H;
@@ -542,6 +727,7 @@ cg_status cg_drainage_order(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is
 cg_status cg_accumulate(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land, const int32_t* receivers,
                         int32_t land_cells, const float* weights, float* area) {
     if (!ctx || !is_land || !receivers || !weights || !area) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     size_t N = (size_t)W * H;
@@ -564,6 +750,7 @@ cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* p, const uint8_t* is_l
                     const int32_t* receivers, const float* area, float land_cells, float land_range, float* surface,
                     int32_t* cells_cut) {
     if (!ctx || !p || !is_land || !relative || !ground || !receivers || !area || !surface) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     if (p->abi_version != CG_ABI_VERSION)
         return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
                     CG_ABI_VERSION);
@@ -605,6 +792,7 @@ cg_status cg_spillways(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_land
                        const float* filled, const int32_t* receivers, float pond_depth, int32_t* basin_of_cell,
                        cg_basins* basins) {
     if (!ctx || !is_land || !relative || !filled || !receivers) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
     CG_TRY(check_grid(ctx, W, H));
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     size_t N = (size_t)W * H;

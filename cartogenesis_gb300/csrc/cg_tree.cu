@@ -365,6 +365,7 @@ struct InciseDev {
     const float* erod;
     float* surface;
     float* water;
+    double* incised_at; // or NULL
     const int* start;   // depth buckets, [levels + 1]
     const int* bucket;
     int levels;
@@ -411,7 +412,10 @@ __device__ void incise_cell(const InciseDev& d, int cell) {
         double g = (double)grades_to;
         after = (float)__dadd_rn(g, __ddiv_rn((double)__fsub_rn(height, grades_to), __dadd_rn(1.0, (double)courant)));
     }
-    if (after != height) d.surface[cell] = after;
+    if (after != height) {
+        d.surface[cell] = after;
+        if (d.incised_at && after < height) d.incised_at[cell] = __dsub_rn((double)height, (double)after);
+    }
 }
 
 // Levels from the top down. The highest levels are the main stems of the largest rivers, a few
@@ -590,9 +594,34 @@ cg_status order_from_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
     return CG_OK;
 }
 
+cg_status level_buckets_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const long long* d_key, int levels,
+                            int** out_bucket, int** out_start) {
+    size_t N = (size_t)W * H;
+    cudaStream_t sm = ctx->stream;
+    int grid = ctx->num_sms * 8;
+    CG_BUF(int, d_bucket, ctx, S_SCRATCH2, N);
+    CG_BUF(int, d_cnt, ctx, S_DEPTH, (size_t)levels + 1);
+    CG_BUF(int, d_start, ctx, S_CG2, 2 * (size_t)levels + 2);
+    int* d_cursor = d_start + levels + 1;
+    CG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, ((size_t)levels + 1) * sizeof(int), sm));
+    CG_CUDA(ctx, cudaMemsetAsync(d_cursor, 0, ((size_t)levels + 1) * sizeof(int), sm));
+    const bool cta_hist = levels <= LVL_SMEM;
+    if (cta_hist) CG_LAUNCH(ctx) k_level_count_cta<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
+    else CG_LAUNCH(ctx) k_level_count<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_cnt);
+    CG_CHECK_LAUNCH(ctx);
+    cg_status st = exclusive_scan(ctx, d_cnt, d_start, levels + 1, nullptr);
+    if (st != CG_OK) return st;
+    if (cta_hist) CG_LAUNCH(ctx) k_level_scatter_cta<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
+    else CG_LAUNCH(ctx) k_level_scatter<<<grid, 256, 0, sm>>>(d_land, d_key, N, levels, d_start, d_cursor, d_bucket);
+    CG_CHECK_LAUNCH(ctx);
+    *out_bucket = d_bucket;
+    *out_start = d_start;
+    return CG_OK;
+}
+
 cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int32_t* d_recv, const long long* d_key,
                      int levels, const float* d_ground, const float* d_rel, const float* d_area, const float* d_erod,
-                     float* d_surface, const InciseArgs& args) {
+                     float* d_surface, const InciseArgs& args, double* d_incised_at) {
     size_t N = (size_t)W * H;
     cudaStream_t sm = ctx->stream;
     int grid = ctx->num_sms * 8;
@@ -626,6 +655,7 @@ cg_status incise_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const int
     d.erod = d_erod;
     d.surface = d_surface;
     d.water = d_water;
+    d.incised_at = d_incised_at;
     d.start = d_start;
     d.bucket = d_bucket;
     d.levels = levels;

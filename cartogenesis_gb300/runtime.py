@@ -14,6 +14,7 @@ EXPORTS = [
     "cg_stream", "cg_kernel_launches",
     "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_erode_batch", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
+    "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish",
 ]
 
 
@@ -66,6 +67,10 @@ def load_library(path=LIB_PATH):
             L.cg_spillways.argtypes = [vp, i32, i32, vp, vp, vp, vp, f32, vp, C.POINTER(abi.Basins)]
             L.cg_erode_batch.argtypes = [vp, i32, C.POINTER(abi.World), vp]
             L.cg_breach.argtypes = [vp, PP, vp, vp, vp, vp, vp, f32, f32, vp, C.POINTER(i32)]
+            L.cg_stage_begin.argtypes = [vp, PP, C.POINTER(abi.Inputs)]
+            L.cg_erode_rounds.argtypes = [vp, i32, i32, C.POINTER(abi.Weather), vp]
+            L.cg_stage_height.argtypes = [vp, vp]
+            L.cg_stage_finish.argtypes = [vp, C.POINTER(abi.Outputs)]
         _lib = L
         return _lib
 

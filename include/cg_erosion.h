@@ -97,8 +97,13 @@ typedef struct cg_erosion_params {
     /* Test switches, never set by a production caller */
     int32_t  receiver_clamp;              /* 1: HydraulicErosion.incise onlyAboveBase */
     int32_t  shield_cut;                  /* 1: incision takes the cover's factor */
-    int32_t  profile;                     /* cg_profile; P0 and P1 are implemented */
-    int32_t  reserved;
+    int32_t  profile;                     /* cg_profile */
+    /* ErosionConfig.climateFeed: the rounds cut with the provisional weather, solved by the caller on
+       the swept terrain and again at round hydraulic_rounds / 2 (HydraulicErosion.kt:655-661,
+       809-813). The weather solve is the caller's (a climate stage, not this path), so a stage with
+       it set runs through cg_stage_begin / cg_erode_rounds, which stop where the weather is asked;
+       cg_erode_stage refuses it. 0 in the P0-P2 profiles. */
+    int32_t  climate_feed;
 } cg_erosion_params;
 
 /* Per-cell inputs of one world (ErosionTectonics + the weather the rounds cut with). */
@@ -230,6 +235,46 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* params, const cg_
  */
 cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs_dev,
                              float* height_out_dev, cg_round_stats* stats, int32_t* land_cells);
+
+/* ---- The stage round by round, its world resident on the context between calls ----
+ *
+ * HydraulicErosion.apply asks for the weather twice when ErosionConfig.climateFeed is on: on the
+ * terrain the initial sweeps left, and again at the top of round hydraulic_rounds / 2 on the terrain
+ * the rounds have left (HydraulicErosion.kt:655-661, 809-813, through provisionalWeather,
+ * HydraulicErosion.kt:410-470). That solve is a climate stage and stays the caller's. These calls
+ * split ErosionStage.apply where the weather is asked, with the world held in HBM in between:
+ *   cg_stage_begin (inputs, initial sweeps) -> cg_stage_height (solve the weather) ->
+ *   cg_erode_rounds(0, R/2, weather A) -> cg_stage_height (solve again) ->
+ *   cg_erode_rounds(R/2, R, weather B) -> cg_stage_finish (outputs).
+ * Without climate_feed any split of [0, R) gives cg_erode_stage's result bit for bit (SURVEY's
+ * round-granular resume). Any other call on the context ends the resident world. */
+
+/* The weather the rounds cut with from a given round on (HydraulicErosion.Weather). */
+typedef struct cg_weather {
+    const float* rainfall_mm;          /* or NULL (all 1) */
+    const float* vegetation_density;   /* or NULL (all 0) */
+} cg_weather;
+
+/* Uploads the world and runs the initial thermal sweeps (ErosionStage.kt:163-172). inputs'
+ * rainfall and cover, if given, are the weather of the first rounds. */
+cg_status cg_stage_begin(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs);
+
+/*
+ * Runs rounds [first_round, end_round) of the resident world (first_round = the rounds run so far),
+ * each with its relaxation and, in the last round, the stage's closing passes. `weather` (may be
+ * NULL: keep the current one) replaces the weather from first_round on. With climate_feed the call
+ * at round 0 and the call at round hydraulic_rounds / 2 must bring the weather, and no call may run
+ * across round hydraulic_rounds / 2. `stats` (may be NULL) receives one entry per round run. If a
+ * round finds no land the rounds stop there, as in the reference; later calls do nothing.
+ */
+cg_status cg_erode_rounds(cg_ctx* ctx, int32_t first_round, int32_t end_round, const cg_weather* weather,
+                          cg_round_stats* stats);
+
+/* The resident world's current height field (N floats, host), e.g. for the caller's weather solve. */
+cg_status cg_stage_height(cg_ctx* ctx, float* height);
+
+/* After the last round: cg_erode_stage's outputs for the resident world, which is then released. */
+cg_status cg_stage_finish(cg_ctx* ctx, cg_outputs* outputs);
 
 /* One world of a batch: its own grid, seed and scale, host inputs and host outputs. */
 typedef struct cg_world {

@@ -80,6 +80,9 @@ def lib():
         L.or_stage_rounds.restype = i32
         L.or_hydraulic_apply.argtypes = L.or_erode_stage.argtypes
         L.or_hydraulic_apply.restype = i32
+        L.or_erode_stage_fed.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
+                                         C.POINTER(abi.Inputs), C.POINTER(abi.Outputs)]
+        L.or_erode_stage_fed.restype = i32
         _lib = L
     return _lib
 
@@ -322,7 +325,10 @@ def stage_rounds(params, height, uplift=None, rock=None, rounds=1):
 
 def erode_stage(params, height, uplift=None, rock=None, rain=None, veg=None, thermal=True, want=("receivers", "area", "filled",
                                                                                     "relative", "is_land", "order",
-                                                                                    "basin_of_cell", "donors")):
+                                                                                    "basin_of_cell", "donors"),
+                refreshed=None):
+    """The whole stage on the oracle. refreshed = (rain, veg) (either may be None) is the weather of the
+    halfway refresh when params.climate_feed is set; (rain, veg) is then the opening weather."""
     H, W = params.height, params.width
     N = W * H
     keep = []
@@ -347,8 +353,13 @@ def erode_stage(params, height, uplift=None, rock=None, rain=None, veg=None, the
     basins = abi.Basins(capacity=N, count=0, **{k: P(v) for k, v in basins_arrays.items()})
     o = abi.Outputs(**{k: P(v) for k, v in outs.items()}, basins=C.pointer(basins))
     stats = (abi.RoundStats * max(params.hydraulic_rounds, 1))()
-    fn = lib().or_erode_stage if thermal else lib().or_hydraulic_apply
-    st = fn(C.byref(params), C.byref(inputs), C.byref(o), C.cast(stats, C.c_void_p))
+    if refreshed is not None:
+        rn2, vg2 = map(f32, refreshed)
+        fed = abi.Inputs(None, None, None, P(rn2), P(vg2))
+        st = lib().or_erode_stage_fed(C.byref(params), C.byref(inputs), C.byref(fed), C.byref(o))
+    else:
+        fn = lib().or_erode_stage if thermal else lib().or_hydraulic_apply
+        st = fn(C.byref(params), C.byref(inputs), C.byref(o), C.cast(stats, C.c_void_p))
     assert st == 0, st
     outs["basins"] = {k: v[:basins.count].copy() for k, v in basins_arrays.items()}
     outs["basins"].update(count=basins.count, largest=basins.largest, largest_cells=basins.largest_cells,

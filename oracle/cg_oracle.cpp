@@ -2003,10 +2003,14 @@ struct StageOut {
 // breach left them.
 // run_rounds >= 0 stops after that many rounds (the relaxation keeps the whole stage's share per
 // round) and initial = false leaves out the initial sweeps: a bounded sample of a stage.
+// refreshed (may be NULL) is the weather the provisional climate gives halfway down when
+// params.climate_feed is set (HydraulicErosion.kt:655-661, 809-813): it replaces the given weather
+// from round hydraulic_rounds / 2 on. The climate itself is not this path's: the caller solves it.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
                 bool with_thermal = true, bool initial = true, int run_rounds = -1,
                 const Switches* switches = nullptr, Tally* tallies = nullptr,
-                LevelRepairs* level_repairs = nullptr, WalkCapture* capture = nullptr) {
+                LevelRepairs* level_repairs = nullptr, WalkCapture* capture = nullptr,
+                const cg_inputs* refreshed = nullptr) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -2058,6 +2062,7 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     std::vector<float> ones(N, 1.0f), zeros(N, 0.0f);
     const float* rain = in.rainfall_mm ? in.rainfall_mm : ones.data();
     const float* veg = in.vegetation_density ? in.vegetation_density : zeros.data();
+    const int refresh_at = p.climate_feed && p.hydraulic_rounds > 1 ? p.hydraulic_rounds / 2 : -1;
     std::vector<float> runoff(N), erod(N);
     float metres_per_field = sc.relief_span();
     float uplift_per_mm = (float)(sc.years_per_round / 1000.0);   // MILLIMETRES_PER_METRE
@@ -2069,6 +2074,10 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     bool routed = true;
     const int last = run_rounds >= 0 && run_rounds < p.hydraulic_rounds ? run_rounds : p.hydraulic_rounds;
     for (int round = 0; round < last; ++round) {
+        if (round == refresh_at && refreshed) {   // the sky asked again, halfway down
+            rain = refreshed->rainfall_mm ? refreshed->rainfall_mm : ones.data();
+            veg = refreshed->vegetation_density ? refreshed->vegetation_density : zeros.data();
+        }
         if (in.uplift_mm_per_year) {
             const float* rate = in.uplift_mm_per_year;
             for (size_t c = 0; c < N; ++c) {
@@ -2405,6 +2414,13 @@ float or_smooth_seeded_field(int32_t W, int32_t lattice, int32_t c, int32_t r, i
 
 int32_t or_erode_stage(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, cg_round_stats* stats) {
     return erode_stage(*p, *in, out, stats);
+}
+
+// The stage with climateFeed: `in` carries the opening weather, `refreshed` the weather of the
+// halfway refresh (HydraulicErosion.kt:655-661, 809-813).
+int32_t or_erode_stage_fed(const cg_erosion_params* p, const cg_inputs* in, const cg_inputs* refreshed,
+                           cg_outputs* out) {
+    return erode_stage(*p, *in, out, nullptr, true, true, -1, nullptr, nullptr, nullptr, nullptr, refreshed);
 }
 
 // HydraulicErosion.apply(config, height, seaLevel) { it }: the rounds alone, with no initial sweeps

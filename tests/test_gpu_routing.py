@@ -121,10 +121,11 @@ def test_fill_key_plateaus(seed):
 
 
 def test_fill_key_level_larger_than_any_fixed_cap():
-    """A coastal plain of 512K cells whose heights all lie within about one quantum of the heap key
-    (steps of 1e-7 around 0.3): each key level holds far more than 2^18 cells, so its ties can only be
-    ordered by replaying the whole level. The fill must give the oracle's bits (and so report no
-    unresolved tie), whatever the level's size."""
+    """A coastal plain of 512K cells whose heights all lie within one quantum of the heap key (steps
+    of 1e-7 around 0.3): the key level holds more than 2^18 cells, and the flood raises a staircase of
+    thousands of levels across the plain, each with ties only its own pops can order. The fill must
+    give the oracle's bits, whatever the level's size (or, past its repairs' guard, answer
+    CG_INEXACT rather than a wrong result with CG_OK)."""
     rng = np.random.default_rng(9)
     W, H = 2048, 256
     g = (np.float32(0.3) + np.float32(1e-7) * rng.integers(0, 4, (H, W)).astype(np.float32)).astype(np.float32)
