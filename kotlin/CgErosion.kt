@@ -30,9 +30,15 @@ interface HydraulicAccelerator {
     /** Whether this accelerator runs the stage `config` asks for; the engine keeps its own rounds if not. */
     fun supports(config: WorldGenConfig): Boolean
 
-    /** The stage's result heights, or throws; there is no CPU fallback once this is selected. */
+    /**
+     * The stage's result heights, or throws; there is no CPU fallback once this is selected.
+     * `weather` is asked for the rounds' weather where HydraulicErosion.apply asks provisionalWeather
+     * (HydraulicErosion.kt:655-661, 809-813): with climateFeed on, on the swept terrain before round 0
+     * and again before round hydraulicRounds / 2, each time with the terrain as it stands and the
+     * round about to cut; with it off it is never called and the rounds cut with no weather.
+     */
     fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
-                   rockErodibility: FloatField?, rainfallMm: FloatArray?, vegetation: FloatArray?): FloatField
+                   rockErodibility: FloatField?, weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField
 }
 
 /** cg_erosion.h's status codes. */
@@ -59,6 +65,10 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     private val sweeps = fn("cg_thermal_sweeps", FunctionDescriptor.of(JAVA_INT, ADDRESS, JAVA_INT, JAVA_INT, ADDRESS,
         ADDRESS, limitsLayout, JAVA_INT, JAVA_FLOAT))
     private val stage = fn("cg_erode_stage", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS, ADDRESS))
+    private val begin = fn("cg_stage_begin", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS))
+    private val rounds = fn("cg_erode_rounds", FunctionDescriptor.of(JAVA_INT, ADDRESS, JAVA_INT, JAVA_INT, ADDRESS, ADDRESS))
+    private val current = fn("cg_stage_height", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
+    private val finish = fn("cg_stage_finish", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
     private val ctx: MemorySegment
 
     override val name = "GB300 (cg_erosion)"
@@ -84,18 +94,27 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
         output.toArray(JAVA_FLOAT)
     }
 
-    // cg_profile: P0 without the outlet notch, P1 with it (HydraulicErosion.breach and the closing
-    // breach); deposition is P2, which the library does not run yet.
-    private fun profileOf(config: WorldGenConfig): Int = when {
-        config.erosion.deposition -> 2
-        config.erosion.outletIncision -> 1
-        else -> 0
+    // cg_profile: P0 without the outlet notch; P1 with it (HydraulicErosion.breach and the closing
+    // breach); P2 with deposition and its lobed, outlined and graded deltas too (the reference's
+    // default). Any other mix of those switches is not a profile the library runs: -1.
+    private fun profileOf(config: WorldGenConfig): Int {
+        val e = config.erosion
+        val deltas = e.deltaLobe && e.deltaOutline && e.gradedAggradation
+        return when {
+            e.deposition && e.outletIncision && deltas -> 2
+            !e.deposition && !e.deltaLobe && e.outletIncision -> 1
+            !e.deposition && !e.deltaLobe && !e.outletIncision -> 0
+            else -> -1
+        }
     }
 
-    override fun supports(config: WorldGenConfig): Boolean = profileOf(config) <= 1
+    // The parts of the stage the library does not run: the belts' replay (needs the plate history),
+    // the plate flexure, and the relief finer than the grid.
+    override fun supports(config: WorldGenConfig): Boolean =
+        profileOf(config) >= 0 && !config.isostasy.flexure
 
     override fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
-                            rockErodibility: FloatField?, rainfallMm: FloatArray?, vegetation: FloatArray?): FloatField =
+                            rockErodibility: FloatField?, weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField =
         Arena.ofConfined().use { a ->
             // cg_erosion_params, 112 bytes (offsets as in cg_erosion.h, checked by the C tests).
             val p = a.allocate(112, 8)
@@ -115,17 +134,35 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
             p.set(JAVA_FLOAT, 84, config.seaLevel)
             p.set(JAVA_FLOAT, 88, config.sea.lowstandMetres)
             p.set(JAVA_INT, 100, profileOf(config))
+            val fed = config.erosion.climateFeed && weather != null
+            p.set(JAVA_INT, 104, if (fed) 1 else 0)   // climate_feed
             fun field(f: FloatArray?) = if (f == null) MemorySegment.NULL else a.allocateFrom(JAVA_FLOAT, *f)
             val inputs = a.allocate(40, 8)
             inputs.set(ADDRESS, 0, field(height.data))
             inputs.set(ADDRESS, 8, field(upliftMmPerYear?.data))
             inputs.set(ADDRESS, 16, field(rockErodibility?.data))
-            inputs.set(ADDRESS, 24, field(rainfallMm))
-            inputs.set(ADDRESS, 32, field(vegetation))
             val result = a.allocate(JAVA_FLOAT, height.data.size.toLong())
             val outputs = a.allocate(80, 8)   // cg_outputs: height, then nine optional pointers
             outputs.set(ADDRESS, 0, result)
-            check(stage.invokeExact(ctx, p, inputs, outputs, MemorySegment.NULL) as Int, ctx, lastError)
+            if (!fed) {
+                check(stage.invokeExact(ctx, p, inputs, outputs, MemorySegment.NULL) as Int, ctx, lastError)
+            } else {
+                // climateFeed: stop where HydraulicErosion.apply asks the weather, ask it, go on.
+                check(begin.invokeExact(ctx, p, inputs) as Int, ctx, lastError)
+                val total = config.erosion.hydraulicRounds
+                val half = if (total > 1) total / 2 else total
+                var done = 0
+                for (end in listOf(half, total).distinct()) {
+                    check(current.invokeExact(ctx, result) as Int, ctx, lastError)
+                    val (rain, cover) = weather!!(FloatField(config.width, config.height, result.toArray(JAVA_FLOAT)), done)
+                    val w = a.allocate(16, 8)   // cg_weather
+                    w.set(ADDRESS, 0, field(rain))
+                    w.set(ADDRESS, 8, field(cover))
+                    check(rounds.invokeExact(ctx, done, end, w, MemorySegment.NULL) as Int, ctx, lastError)
+                    done = end
+                }
+                check(finish.invokeExact(ctx, outputs) as Int, ctx, lastError)
+            }
             FloatField(config.width, config.height, result.toArray(JAVA_FLOAT))
         }
 
