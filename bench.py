@@ -50,9 +50,15 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=8192)
     ap.add_argument("--height", type=int, default=4096)
-    ap.add_argument("--profile", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--profile", type=int, default=0, choices=[0, 1, 2],
                     help="round-tail profile: 0 = P0 (the plain stage), 1 = P1 (P0 with the outlet notch and the "
-                         "closing breach)")
+                         "closing breach), 2 = P2 (P1 with deposition, its lobed and outlined deltas and the "
+                         "closing mouths pass: the reference's default)")
+    ap.add_argument("--case", default=None, choices=["thermal", "stage"],
+                    help="one public call on the bench world for a profiler, then exit: `thermal` runs the sweeps "
+                         "(--passes of them), `stage` the stage with --rounds rounds; prints nothing to parse")
+    ap.add_argument("--passes", type=int, default=4, help="--case thermal: sweeps")
+    ap.add_argument("--rounds", type=int, default=2, help="--case stage: hydraulic rounds")
     ap.add_argument("--cpu-sample", type=int, default=1,
                     help="samples of the CPU baseline (one round of the stage on the bench world plus a twelfth "
                          "of its initial sweeps, on the CPU restatement); 0 skips the CPU leg")
@@ -257,7 +263,7 @@ def run_ours(args):
     # The timed steps also fill cg_round_stats: the library records CUDA events on its stream around
     # each phase of each round, which gives the per-phase device times (and the sweep kernel's
     # launch durations for the roofline) over the timed region itself.
-    PHASES = ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_relax", "ms_total")
+    PHASES = ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_deposit", "ms_relax", "ms_total")
     phase = {k: 0.0 for k in PHASES}
     clocks = ClockSampler(local)
     barrier()
@@ -272,7 +278,8 @@ def run_ours(args):
             phase[k] += sum(getattr(s, k) for s in stats) / args.steps
     barrier()
     per_round = [{"land": s.land_cells, "flats": s.flats, "raised": s.raised_cells, "levels": s.levels,
-                  "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2)}
+                  "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2),
+                  **({"replayed": s.deposit_replayed, "redone": s.deposit_redone} if args.profile == 2 else {})}
                  for s in stats]
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
@@ -328,8 +335,29 @@ def run_ours(args):
     return 0
 
 
+def run_case(args):
+    """One public call on the bench world, for a profiler: the thermal sweeps alone
+    (GpuErosionAccelerator.erode) or the stage with a few rounds (ErosionStage.apply). Each holds only
+    what its call needs on the device, so a profiler that saves and restores device memory around a
+    replayed kernel has little to save."""
+    from cartogenesis_gb300 import ErosionConfig, ErosionStage, GpuErosionAccelerator
+    W, H = args.width, args.height
+    h, up, rk = world_inputs(W, H, 1)
+    cfg = ErosionConfig(W, H, 1, sea_level=0.70, hydraulic_rounds=args.rounds, profile=args.profile)
+    t = time.perf_counter()
+    if args.case == "thermal":
+        limits, _ = cfg.thermal_limits()
+        GpuErosionAccelerator().erode(W, H, h, limits, args.passes, cfg.params.rate)
+    else:
+        ErosionStage.apply(cfg, h, up, rk, want=("receivers",))
+    print(f"case {args.case} {W}x{H}: {time.perf_counter() - t:.3f} s", file=sys.stderr)
+    return 0
+
+
 def main():
     args = parse()
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -5,7 +5,7 @@ alignment rules, so a change to one side must be made to the other.
 """
 import ctypes as C
 
-CG_ABI_VERSION = 1
+CG_ABI_VERSION = 2
 
 CG_OK, CG_CANCELLED, CG_TIMEOUT, CG_BAD_ARG, CG_OOM, CG_CUDA, CG_UNSUPPORTED, CG_INEXACT = range(8)
 STATUS_NAMES = {
@@ -113,6 +113,9 @@ class RoundStats(C.Structure):
         ("ms_tree", C.c_double),
         ("ms_incise", C.c_double),
         ("ms_relax", C.c_double),
+        ("ms_deposit", C.c_double),
+        ("deposit_replayed", C.c_int32),
+        ("deposit_redone", C.c_int32),
     ]
 
 

@@ -206,7 +206,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
     CG_BUF(double, d_sum, ctx, S_CG3, 2);
 
     // Phase boundaries of a round, for the per-phase device times of cg_round_stats.
-    cudaEvent_t ev[7] = {};
+    cudaEvent_t ev[8] = {};
     if (stats)
         for (auto& e : ev) CG_CUDA(ctx, cudaEventCreate(&e));
     struct Events {
@@ -214,7 +214,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         bool on;
         ~Events() {
             if (on)
-                for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+                for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
         }
     } guard{ev, stats != nullptr};
     auto mark = [&](int i) {
@@ -290,6 +290,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         ia.only_above_base = p.receiver_clamp != 0;
         CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia,
                           d_incised_at));
+        mark(5);
         DepositCounts dc{0, 0};
         if (deposition) {
             DepositRound dr;
@@ -340,19 +341,19 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         }
         // The closing mouths pass (HydraulicErosion.kt:1451-1462), ErosionConfig.deltaLobe.
         if (closing && deposition) CG_TRY(open_mouths_dev(ctx, p, cur, d_rain));
-        mark(5);
+        mark(6);
         // relax = thermalErosion(config, field, accelerator, sweepsPerRound) (ErosionStage.kt:178-180).
         float* res;
         CG_TRY(thermal_sweeps_dev(ctx, W, H, run.cur, run.other, lim, per_round, p.rate, &res));
         if (res != run.cur) std::swap(run.cur, run.other);
         run.next_round = round + 1;
-        mark(6);
+        mark(7);
         if (stats) {
-            CG_CUDA(ctx, cudaEventSynchronize(ev[6]));
-            float ms[7] = {0};
-            for (int i = 1; i < 7; ++i) cudaEventElapsedTime(&ms[i], ev[i - 1], ev[i]);
+            CG_CUDA(ctx, cudaEventSynchronize(ev[7]));
+            float ms[8] = {0};
+            for (int i = 1; i < 8; ++i) cudaEventElapsedTime(&ms[i], ev[i - 1], ev[i]);
             float total = 0.0f;
-            cudaEventElapsedTime(&total, ev[0], ev[6]);
+            cudaEventElapsedTime(&total, ev[0], ev[7]);
             cg_round_stats& s = stats[round - first_round];
             std::memset(&s, 0, sizeof(s));
             s.round = round;
@@ -371,7 +372,10 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             s.ms_route = ms[3];
             s.ms_tree = ms[4];
             s.ms_incise = ms[5];
-            s.ms_relax = ms[6];
+            s.ms_deposit = ms[6];
+            s.ms_relax = ms[7];
+            s.deposit_replayed = dc.replayed;
+            s.deposit_redone = dc.redone;
         }
     }
     if (run.next_round >= p.hydraulic_rounds) run.done = true;

@@ -7,6 +7,8 @@ B = 4 bytes per height (the REF32 field):
   route (routing surface 2B + 8, receivers 8 + 4)               28
   tree (donor counts, keys, accumulation: 4+4+4+4+B)            20
   incise (5B + 8 + B)                                           32
+  deposit (P2's walk: routing, cut and load inputs 33, incisedAt 8, load 8, settled and sediment
+           read and written 16, hand-off 8, order and rank 8)     81
   relax (s sweeps, a read and a write of the field each: 2B s)   8 s
 The peak is the measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json, written by
 the pool's driver), else the recipe's fallback of 6.8 TB/s.
@@ -14,13 +16,16 @@ the pool's driver), else the recipe's fallback of 6.8 TB/s.
 import json
 import os
 
-BYTES_PER_CELL = {"ms_cut": 41.0, "ms_fill": 9.0, "ms_route": 28.0, "ms_tree": 20.0, "ms_incise": 32.0}
+BYTES_PER_CELL = {"ms_cut": 41.0, "ms_fill": 9.0, "ms_route": 28.0, "ms_tree": 20.0, "ms_incise": 32.0,
+                  "ms_deposit": 81.0}
 PHASE_KERNELS = {
     "ms_cut": "k_minmax, k_row_counts, k_bin_sums, k_bracket_*, k_land_and_water, k_uplift, k_unit_weights",
     "ms_fill": "k_fill_init, k_jump, k_mark_drained, k_relax_tiles, k_check_ties",
     "ms_route": "k_surface, k_cc_*, k_flat_solve_warp/_sm/_cl, k_flat_solve, k_receivers",
     "ms_tree": "k_links, k_sources, k_walk",
-    "ms_incise": "k_depth_*, k_incise_levels",
+    "ms_incise": "k_depth_*, k_incise_levels (P1, P2: the notch's k_footprint_*, k_breach_waves)",
+    "ms_deposit": "k_round_begin, k_rank_of, k_level_bounds, k_deposit_levels, k_settle, k_mouths_levels "
+                  "(last round: the closing breach's cut, fill, routing and notch)",
     "ms_relax": "thermal_sweeps_kernel",
 }
 FALLBACK_HBM_GBS = 6800.0

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define CG_ABI_VERSION 1u
+#define CG_ABI_VERSION 2u
 
 typedef enum cg_status {
     CG_OK = 0,
@@ -54,7 +54,10 @@ typedef enum cg_mode { CG_MODE_REF32 = 0 } cg_mode;
  * P1: P0 with ErosionConfig.outletIncision: each round's notch before the incision and the closing
  * breach before the last relaxation (HydraulicErosion.kt:1002-1028, 1404-1442); the routing outputs
  * are then the closing pass's, as its notch left them. P0 and P1 have ErosionConfig.deltaLobe off
- * (the closing mouths pass belongs to P2). P2 (deposition) is not built on the device.
+ * (the closing mouths pass belongs to P2). P2: P1 with ErosionConfig.deposition, deltaLobe,
+ * deltaOutline and gradedAggradation (the reference's default round tail): each round's deposition
+ * walk with its sea lobes and lake fans, settle and the closing mouths pass (HydraulicErosion.kt:
+ * 1068-1349, 1351-1364, 1451-1462, 1804-1892; DeltaFan.kt).
  */
 typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2 } cg_profile;
 
@@ -162,9 +165,12 @@ typedef struct cg_round_stats {
     double  ms_fill;            /* fillDepressions */
     double  ms_route;           /* flat potentials and receivers */
     double  ms_tree;            /* donor counts, drainage keys and accumulation */
-    double  ms_incise;          /* the implicit incision (P1: with the round's notch and, in the last
-                                   round, the closing breach's cut, fill, routing and notch) */
+    double  ms_incise;          /* the implicit incision (P1, P2: with the round's notch) */
     double  ms_relax;           /* the round's thermal sweeps */
+    double  ms_deposit;         /* P2's deposition walk and, in the last round, settle, the closing
+                                   breach (P1, P2: its cut, fill, routing and notch) and the mouths pass */
+    int32_t deposit_replayed;   /* P2: ponded cells whose settled height the level schedule replayed */
+    int32_t deposit_redone;     /* P2: levels the schedule restored and walked one cell after another */
 } cg_round_stats;
 
 typedef struct cg_ctx cg_ctx;
