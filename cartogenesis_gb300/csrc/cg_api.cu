@@ -168,9 +168,10 @@ cg_status cg_thermal_sweeps(cg_ctx* ctx, int32_t W, int32_t H, const float* in, 
     CG_BUF(float, d_b, ctx, S_H1, N);
     if ((st = upload(ctx, d_a, in, N * sizeof(float))) != CG_OK) return st;
     float* res = d_a;
+    if ((st = thermal_error_reset_dev(ctx)) != CG_OK) return st;
     if (passes > 0 && (st = thermal_sweeps_dev(ctx, W, H, d_a, d_b, lim, passes, rate, &res)) != CG_OK) return st;
     if ((st = download(ctx, out, res, N * sizeof(float))) != CG_OK) return st;
-    return sync(ctx);
+    return thermal_error_check(ctx);
 }
 
 }  // extern "C"

@@ -103,7 +103,7 @@ enum Slot {
     S_DEPSLOT0, S_DEPSLOT1, S_DEPSLOT2, S_DEPSLOT3, S_DEPSLOT4, S_DEPSLOT5, S_DEPSLOT6, S_DEPSLOT7,
     S_DEPHEAP, S_DEPTOUCH, S_DEPREPLAY, S_DEPSEGC,
     S_OM_LAND, S_OM_REL, S_OM_FILLED, S_OM_RECV, S_OM_KEY, S_OM_AREA, S_OM_RUNOFF, S_OM_DONORS,
-    S_FILLEB,
+    S_FILLEB, S_THERMERR,
     S_COUNT
 };
 

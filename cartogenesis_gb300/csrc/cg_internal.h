@@ -8,6 +8,10 @@ namespace cg {
 // ---- thermal (cg_thermal.cu)
 cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, cg_thermal_limits lim, int passes,
                              float rate, float** result);
+// The sweeps' error word: a region copy whose bounded wait ran out sets it. Reset clears it (async);
+// check reads it (synchronises) and answers CG_TIMEOUT when it is set.
+cg_status thermal_error_reset_dev(cg_ctx* ctx);
+cg_status thermal_error_check(cg_ctx* ctx);
 // Sweeps per fused launch when `passes_left` remain (2, or 1 for the last of an odd count), and the
 // number of launches that `passes` sweeps take.
 int thermal_step(int passes_left);

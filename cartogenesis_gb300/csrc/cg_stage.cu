@@ -1,10 +1,11 @@
 // ErosionStage.apply on the device (ErosionStage.kt:133-183 with HydraulicErosion.apply,
-// HydraulicErosion.kt:596-1506), profile P0, and the C entry points that run one routing function
-// on host buffers.
+// HydraulicErosion.kt:596-1506) in profiles P0, P1 and P2, whole or a range of rounds at a time, and
+// the C entry points that run one routing function on host buffers.
 //
 // The world stays resident in HBM for the whole stage: heights ping-pong between two buffers, and
-// each round's masks, fields, receivers and tree live in context buffers reused round to round. The
-// host sequences the phases and reads back one shoreline and one land count per round.
+// each round's masks, fields, receivers and tree live in context buffers reused round to round (P2's
+// sediment too, carried from round to round). The host sequences the phases and reads back one
+// shoreline and one land count per round.
 #include <cmath>
 #include <vector>
 
@@ -149,6 +150,7 @@ cg_status stage_begin_dev(cg_ctx* ctx, StageRun& run) {
         run.done = true;
         return CG_OK;
     }
+    CG_TRY(thermal_error_reset_dev(ctx));
     if (p.profile >= CG_PROFILE_P2) CG_TRY(deposit_stage_reset_dev(ctx, p.width, p.height));
     const int sweeps = sweeps_for(p);
     if (sweeps > 0) {
@@ -399,6 +401,7 @@ cg_status erode_stage_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, f
     *last_land_cells = -1;
     cg_status st = stage_begin_dev(ctx, run);
     if (st == CG_OK) st = stage_rounds_dev(ctx, run, p.hydraulic_rounds, stats);
+    if (st == CG_OK) st = thermal_error_check(ctx);
     *d_result = run.cur;
     *last_land_cells = run.land_cells;
     return st;
@@ -575,7 +578,7 @@ cg_status cg_stage_begin(cg_ctx* ctx, const cg_erosion_params* p, const cg_input
     StageRun run;
     CG_TRY(upload_world(ctx, p, in, run));
     CG_TRY(stage_begin_dev(ctx, run));
-    CG_TRY(sync(ctx));
+    CG_TRY(thermal_error_check(ctx));
     run.active = true;
     ctx->run = run;
     return CG_OK;
@@ -609,6 +612,7 @@ cg_status cg_erode_rounds(cg_ctx* ctx, int32_t first_round, int32_t end_round, c
         run.veg = d_veg;
     }
     cg_status st = stage_rounds_dev(ctx, run, end_round, stats);
+    if (st == CG_OK) st = thermal_error_check(ctx);
     if (st != CG_OK) {
         run.active = false;   // a round stopped part way: the world is no longer a whole terrain
         return st;

@@ -11,6 +11,10 @@
 // The arithmetic per cell is the reference's, in the same neighbour order, in float, with no
 // fused multiply-add, so the result is bit-identical to ErosionStage.thermalSweep. Tiles away from
 // the poles take a path without the per-neighbour row checks; both paths compute the same values.
+#include <cuda.h>
+
+#include <cmath>
+
 #include "cg_common.cuh"
 #include "cg_internal.h"
 
@@ -28,6 +32,8 @@ struct ThermalArgs {
     float lim0[8];   // max(limit, 0)
     float settled;
     float rate;
+    float min_lim0;  // the least of lim0
+    int plain;       // every limit >= 0 and settled >= 0: the shortcuts below are exact
 };
 
 // Settled-tile skip (the reference's own skip, ErosionStage.kt:269-342, restated for fused launches).
@@ -41,6 +47,36 @@ struct TileFlags {
     uint8_t* cur;
 };
 
+// The region load by the tensor memory accelerator: one cp.async.bulk.tensor.2d per CTA of the
+// whole (TX + 2 HALO) x (TY + 2 HALO) region, rows off the grid filled with zeros by the copy
+// itself. Used for K = 2 (the region's first column, x0 = 64 bx - 4, is 16-byte aligned as TMA
+// requires) on tiles whose region does not wrap east-west; the two wrapping tile columns and the
+// odd single-sweep launch load by threads. `err` (device) is set when a copy's wait runs out, after
+// which the CTA waits once more for its copy and leaves without computing; the host reports it.
+struct RegionLoad {
+    CUtensorMap map;   // the source field, box = the region
+    int on;            // a map was made for this launch
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Waits on the mbarrier's phase 0 for at most `tries` polls; true when the phase completed.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, int tries) {
+    for (int i = 0; i < tries; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(0)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // Per-cell rules, written without branches: the conditions become predicated adds in the
 // reference's neighbour order, so the sums round exactly as the reference's loop does.
 // Neighbours by name: E/W the same row, S/N the rows below/above, and the diagonals SE (+1,+1),
@@ -48,6 +84,55 @@ struct TileFlags {
 struct Window {
     float nw, n, ne, w, c, e, sw, s, se;   // the 3 x 3 block around a cell
 };
+
+// The give rate of a cell away from the poles with plain limits (every limit and the settled share
+// >= 0), the same bits as give_rate with fewer instructions:
+//  - a cell no drop of which exceeds the least max(limit, 0) gives nothing. Float subtraction is
+//    monotone, so c - min(neighbours) bounds every drop from above, and then the excess stays +0,
+//    which is not above the settled share (>= 0): the rate is +0, as the full rule returns;
+//  - the steepest drop as a running max: the reference keeps the larger of the two, and the heights
+//    are finite; the max may return -0 where the rule keeps +0, which changes neither the rate's
+//    products nor any sum (every sum starts at +0 and adds terms >= 0).
+__device__ __forceinline__ float give_rate_plain(const Window& v, const ThermalArgs& a) {
+    const float lowest = fminf(fminf(fminf(v.e, v.w), fminf(v.s, v.n)), fminf(fminf(v.se, v.ne), fminf(v.sw, v.nw)));
+    if (__fsub_rn(v.c, lowest) <= a.min_lim0) return 0.0f;
+    const float nb[8] = {v.e, v.w, v.s, v.n, v.se, v.ne, v.sw, v.nw};
+    float excess = 0.0f, steepest = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float drop = __fsub_rn(v.c, nb[n]);
+        steepest = fmaxf(steepest, drop);
+        const float over = __fsub_rn(drop, a.limit[n]);
+        if (drop > a.lim0[n]) excess = __fadd_rn(excess, over);
+    }
+    float g = 0.0f;
+    if (excess > a.settled) {
+        const float p = __fmul_rn(a.rate, excess), q = __fmul_rn(steepest, 0.5f);
+        g = __fdiv_rn(p <= q ? p : q, excess);
+    }
+    return g;
+}
+
+// The new height of a cell away from the poles with plain limits, the same bits as `moved`: with a
+// limit >= 0 a drop that moves material either way has magnitude |incoming|, so one absolute value
+// replaces the select of the sign; a term is added as +0 where the rule skips it (sums start at +0
+// and gain only terms >= 0, so adding +0 changes no bit).
+__device__ __forceinline__ float moved_plain(const Window& v, const Window& g, const ThermalArgs& a) {
+    const float nb[8] = {v.e, v.w, v.s, v.n, v.se, v.ne, v.sw, v.nw};
+    const float gn[8] = {g.e, g.w, g.s, g.n, g.se, g.ne, g.sw, g.nw};
+    float received = 0.0f, given = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float limit = a.limit[n];
+        const float incoming = __fsub_rn(nb[n], v.c);
+        const bool in = incoming > limit;
+        const bool out = incoming < -limit;
+        const float p = __fmul_rn(in ? gn[n] : g.c, __fsub_rn(fabsf(incoming), limit));
+        received = __fadd_rn(received, in ? p : 0.0f);
+        given = __fadd_rn(given, out ? p : 0.0f);
+    }
+    return __fadd_rn(__fsub_rn(v.c, given), received);
+}
 
 // The give rate of a cell (ErosionStage.kt:283-311). `lim0[n]` is max(limit, 0): a drop counts
 // towards the excess when it is positive and above the limit. `has_s` / `has_n`: the rows below /
@@ -144,14 +229,15 @@ __device__ __forceinline__ void pass(const float* __restrict__ hs, float* __rest
                     // sums stay +0 and the cell moves to (h - 0) + 0. Rows off the grid (EDGE) are
                     // left to the full rule.
                     const bool still = !EDGE && (or_top | or_mid | or_bot) == 0u;
-                    const float nv = still ? __fadd_rn(__fsub_rn(v.c, 0.0f), 0.0f) : moved(v, g, has_s, has_n, a);
+                    const float nv = still ? __fadd_rn(__fsub_rn(v.c, 0.0f), 0.0f)
+                                           : (!EDGE && a.plain) ? moved_plain(v, g, a) : moved(v, g, has_s, has_n, a);
                     dst[ry * RW + col] = nv;
                     // A cell of the tile itself that moved (in any sweep) marks the tile as changed.
                     if (__float_as_uint(nv) != __float_as_uint(v.c) && ry >= halo && ry < RH - halo &&
                         col >= halo && col < RW - halo)
                         changed = true;
                 } else {
-                    gv[ry * RW + col] = give_rate(v, has_s, has_n, a);
+                    gv[ry * RW + col] = (!EDGE && a.plain) ? give_rate_plain(v, a) : give_rate(v, has_s, has_n, a);
                 }
             }
             v.nw = v.w, v.n = v.c, v.ne = v.e;
@@ -189,11 +275,14 @@ __device__ __forceinline__ float* sweeps(float* hs, float* hn, float* gv, int y0
 
 template <int K>
 __global__ void __launch_bounds__(THREADS, 6) thermal_sweeps_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                                 int W, int H, ThermalArgs a, TileFlags fl) {
+                                                                 int W, int H, ThermalArgs a, TileFlags fl,
+                                                                 const __grid_constant__ RegionLoad rl) {
     constexpr int HALO = 2 * K;
     constexpr int RW = TX + 2 * HALO;   // region width
     constexpr int RH = TY + 2 * HALO;   // region height
-    __shared__ float sm_a[RW * RH], sm_b[RW * RH], sm_g[RW * RH];
+    __shared__ __align__(128) float sm_a[RW * RH];
+    __shared__ __align__(16) float sm_b[RW * RH], sm_g[RW * RH];
+    __shared__ __align__(8) unsigned long long bar;
 
     const int tile = blockIdx.y * gridDim.x + blockIdx.x;
     if (fl.prev) {
@@ -215,11 +304,34 @@ __global__ void __launch_bounds__(THREADS, 6) thermal_sweeps_kernel(const float*
     const int x0 = blockIdx.x * TX - HALO;
     const int y0 = blockIdx.y * TY - HALO;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int ry = ty; ry < RH; ry += 8) {
-        const int gy = y0 + ry;
-        const bool valid = gy >= 0 && gy < H;
-        const float* rowp = in + (size_t)(valid ? gy : 0) * W;
-        for (int rx = tx; rx < RW; rx += 32) sm_a[ry * RW + rx] = valid ? rowp[wrap_col(x0 + rx, W)] : 0.0f;
+    if (K == 2 && rl.on && x0 >= 0 && x0 + RW <= W) {
+        const uint32_t b = smem_addr(&bar);
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(RW * RH * 4) : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                ::"r"(smem_addr(sm_a)), "l"(&rl.map), "r"(x0), "r"(y0), "r"(b)
+                : "memory");
+        }
+        __syncthreads();
+        if (!mbar_wait(b, 1 << 22)) {
+            // The copy did not land: record it, give it one more bounded wait, and leave.
+            if (threadIdx.x == 0) {
+                atomicOr(rl.err, 1);
+                mbar_wait(b, 1 << 22);
+            }
+            __syncthreads();
+            return;
+        }
+    } else {
+        for (int ry = ty; ry < RH; ry += 8) {
+            const int gy = y0 + ry;
+            const bool valid = gy >= 0 && gy < H;
+            const float* rowp = in + (size_t)(valid ? gy : 0) * W;
+            for (int rx = tx; rx < RW; rx += 32) sm_a[ry * RW + rx] = valid ? rowp[wrap_col(x0 + rx, W)] : 0.0f;
+        }
     }
     __syncthreads();
 
@@ -246,15 +358,61 @@ __global__ void __launch_bounds__(THREADS, 6) thermal_sweeps_kernel(const float*
 
 template <int K>
 cudaError_t launch(const float* in, float* out, int W, int H, const ThermalArgs& a, cudaStream_t st,
-                   TileFlags fl = TileFlags{nullptr, nullptr}) {
+                   TileFlags fl = TileFlags{nullptr, nullptr}, const RegionLoad* rl = nullptr) {
     dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
-    thermal_sweeps_kernel<K><<<grid, THREADS, 0, st>>>(in, out, W, H, a, fl);
+    static const RegionLoad none{};
+    thermal_sweeps_kernel<K><<<grid, THREADS, 0, st>>>(in, out, W, H, a, fl, rl ? *rl : none);
     return cudaGetLastError();
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// The driver's cuTensorMapEncodeTiled, fetched through the runtime (the library links no libcuda).
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// The region-load map of a field for K = 2 launches: the whole W x H field, a box of the region.
+// Off (threads load every tile) where the driver has no encoder or the grid is too narrow.
+RegionLoad region_load_of(const float* field, int W, int H, int* err) {
+    RegionLoad rl{};
+    rl.err = err;
+    constexpr int RW = TX + 8, RH = TY + 8;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || !err || W < 2 * RW || (((uintptr_t)field) & 15) != 0) return rl;
+    const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+    const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
+    const cuuint32_t box[2] = {RW, RH};
+    const cuuint32_t estride[2] = {1, 1};
+    if (enc(&rl.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)field, dims, strides, box, estride,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+        rl.on = 1;
+    return rl;
 }
 
 ThermalArgs args_of(const ThermalLaunch& t) {
     ThermalArgs a;
-    for (int n = 0; n < 8; ++n) a.limit[n] = t.limit[n], a.lim0[n] = t.limit[n] > 0.0f ? t.limit[n] : 0.0f;
+    a.plain = t.settled >= 0.0f;
+    a.min_lim0 = 3.402823466e+38f;
+    for (int n = 0; n < 8; ++n) {
+        a.limit[n] = t.limit[n];
+        a.lim0[n] = t.limit[n] > 0.0f ? t.limit[n] : 0.0f;
+        a.min_lim0 = std::fmin(a.min_lim0, a.lim0[n]);
+        if (!(t.limit[n] >= 0.0f)) a.plain = 0;
+    }
     a.settled = t.settled;
     a.rate = t.rate;
     return a;
@@ -295,15 +453,19 @@ cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, 
     // that tile did not change, so the skip needs no copy.
     const int tiles = ((W + TX - 1) / TX) * ((H + TY - 1) / TY);
     CG_BUF(uint8_t, d_flags, ctx, S_THERMFLAG, 2 * (size_t)tiles);
+    CG_BUF(int, d_err, ctx, S_THERMERR, 1);
     uint8_t* prev = d_flags;
     uint8_t* cur = d_flags + tiles;
     float* src = d_a;
     float* dst = d_b;
+    const RegionLoad maps[2] = {region_load_of(d_a, W, H, d_err), region_load_of(d_b, W, H, d_err)};
     bool first = true;
     while (passes > 0) {
         const int k = thermal_step(passes);
         TileFlags fl{first ? nullptr : prev, cur};
-        cudaError_t e = k == 2 ? launch<2>(src, dst, W, H, a, ctx->stream, fl) : launch<1>(src, dst, W, H, a, ctx->stream, fl);
+        const RegionLoad* rl = &maps[src == d_a ? 0 : 1];
+        cudaError_t e = k == 2 ? launch<2>(src, dst, W, H, a, ctx->stream, fl, rl)
+                               : launch<1>(src, dst, W, H, a, ctx->stream, fl);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "thermal_sweeps_kernel", __FILE__, __LINE__);
         passes -= k;
         ctx->launches++;
@@ -316,6 +478,21 @@ cg_status thermal_sweeps_dev(cg_ctx* ctx, int W, int H, float* d_a, float* d_b, 
         cur = tf;
     }
     *result = src;
+    return CG_OK;
+}
+
+cg_status thermal_error_reset_dev(cg_ctx* ctx) {
+    CG_BUF(int, d_err, ctx, S_THERMERR, 1);
+    CG_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+    return CG_OK;
+}
+
+cg_status thermal_error_check(cg_ctx* ctx) {
+    CG_BUF(int, d_err, ctx, S_THERMERR, 1);
+    int err = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (err) return fail(ctx, CG_TIMEOUT, "thermal sweeps: a region copy did not arrive in its bounded wait");
     return CG_OK;
 }
 

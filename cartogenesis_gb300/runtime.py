@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libcg_erosion.so")
 # Every symbol include/cg_erosion.h declares; the CPU tests check the library exports them all.
 EXPORTS = [
     "cg_default_params", "cg_thermal_limits_for", "cg_create", "cg_destroy", "cg_cancel", "cg_last_error",
-    "cg_stream", "cg_kernel_launches",
+    "cg_stream", "cg_kernel_launches", "cg_probe_fp64_rate",
     "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_erode_batch", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
     "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish",
@@ -53,6 +53,7 @@ def load_library(path=LIB_PATH):
         L.cg_stream.restype = vp
         L.cg_kernel_launches.argtypes = [vp]
         L.cg_kernel_launches.restype = i64
+        L.cg_probe_fp64_rate.argtypes = [vp, C.POINTER(f64)]
         L.cg_thermal_sweeps.argtypes = [vp, i32, i32, vp, vp, abi.ThermalLimits, i32, f32]
         L.cg_thermal_sweeps_noalloc.argtypes = [vp, vp, i32, i32, abi.ThermalLimits, i32, f32, vp]
         if hasattr(L, "cg_erode_stage"):

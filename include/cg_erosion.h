@@ -196,6 +196,12 @@ const char* cg_last_error(const cg_ctx* ctx);
 void*     cg_stream(const cg_ctx* ctx);
 /* Kernels this context has launched since it was created. No counterpart in the reference. */
 int64_t   cg_kernel_launches(const cg_ctx* ctx);
+/*
+ * This GPU's measured FP64 fused multiply-add rate in GFLOP/s (a chain of independent FMAs on every
+ * SM, best of four timed launches): the ceiling of the phases the reference computes in double, for
+ * their roofline. No counterpart in the reference.
+ */
+cg_status cg_probe_fp64_rate(cg_ctx* ctx, double* gflops);
 
 /*
  * ErosionAccelerator.erode (.../pipeline/ErosionAccelerator.kt:38-45; ErosionStage.kt:235-403):

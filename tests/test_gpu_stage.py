@@ -91,7 +91,9 @@ def test_stage_rejects_bad_arguments():
     with pytest.raises(CgError):
         ErosionStage.apply(ErosionConfig(48, 32, 1), h)
     with pytest.raises(CgError):
-        ErosionStage.apply(ErosionConfig(64, 32, 1, profile=2), np.zeros((32, 64), np.float32))
+        ErosionStage.apply(ErosionConfig(64, 32, 1, profile=3), np.zeros((32, 64), np.float32))
+    with pytest.raises(CgError):
+        ErosionStage.apply(ErosionConfig(64, 32, 1, mode=1), np.zeros((32, 64), np.float32))
 
 
 def test_stage_disabled_and_no_rounds_are_copies_or_sweeps():

@@ -2,8 +2,8 @@
 settle, the closing mouths pass), pinned to the reference's DepositionTest
 (T/DepositionTest.kt, T = worldgen/src/jvmTest/kotlin/com/cartogenesis/worldgen): every round's mass
 budget closes, and deposition switched off is deposition absent, whatever its knobs say, while
-deposition running with every rate at zero leaves the rock bit-identical. The GPU does not run P2 yet
-(cg_erode_stage answers CG_UNSUPPORTED); these tests hold the restatement it will be checked against.
+deposition running with every rate at zero leaves the rock bit-identical. The GPU's P2 stage is held
+to this restatement bit for bit by tests/test_gpu_deposition.py.
 """
 import numpy as np
 import pytest
