@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--case", default=None, choices=["thermal", "stage"],
                     help="one public call on the bench world for a profiler, then exit: `thermal` runs the sweeps "
                          "(--passes of them), `stage` the stage with --rounds rounds; prints nothing to parse")
+    ap.add_argument("--batched", type=int, default=0, metavar="WORLDS",
+                    help="the batched workload instead: WORLDS planets of radius U(0.25, 2.0) Earth radii (grids "
+                         "512 x 256 to 4096 x 2048, each its own seed) through cg_erode_batch, one batch per step")
     ap.add_argument("--passes", type=int, default=4, help="--case thermal: sweeps")
     ap.add_argument("--rounds", type=int, default=2, help="--case stage: hydraulic rounds")
     ap.add_argument("--cpu-sample", type=int, default=1,
@@ -354,10 +357,62 @@ def run_case(args):
     return 0
 
 
+def run_batched(args):
+    """The batched workload: `args.batched` worlds of uneven size through the public batch call
+    (ErosionStage.apply_batch -> cg_erode_batch), host inputs and outputs, one batch per step. The
+    worlds run one after another inside the call; the line reports the batch's whole throughput."""
+    import torch
+    from cartogenesis_gb300 import ErosionConfig, ErosionStage, synthetic
+    from cartogenesis_gb300.api import default_context
+    shapes = synthetic.batch_shapes(args.batched, seed=1)
+    worlds = []
+    for i, (W, H, seed, radius) in enumerate(shapes):
+        h, up, rk = synthetic.world(W, H, seed, uplift="ridges")
+        cfg = ErosionConfig(W, H, seed, sea_level=0.70, world_width_km=synthetic.EARTH_KM * radius,
+                            profile=args.profile)
+        worlds.append((cfg, h, up, rk))
+    cells = sum(c.params.width * c.params.height for c, _, _, _ in worlds)
+    ctx = default_context()
+    for _ in range(args.warmup):
+        ErosionStage.apply_batch(worlds, ctx=ctx)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = ctx.kernel_launches
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ErosionStage.apply_batch(worlds, ctx=ctx)
+    t = time.perf_counter() - t0
+    clk = clocks.stop()
+    value = cells * ROUNDS * args.steps / t / 1e6
+    sizes = {}
+    for c, _, _, _ in worlds:
+        key = f"{c.params.width}x{c.params.height}"
+        sizes[key] = sizes.get(key, 0) + 1
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 * t / args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched plain P{args.profile} stage: {len(worlds)} worlds of radius U(0.25, 2.0) "
+                               f"Earth radii, 12 rounds each, host inputs and outputs through cg_erode_batch "
+                               f"(worlds one after another in the call)",
+                   "worlds": sizes, "cells": cells, "rounds": ROUNDS, "profile": f"P{args.profile}",
+                   "l2": "most worlds larger than L2"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 12 * cells,
+                "d2h_bytes_per_step": 4 * cells},
+        "gpu_launches": int(ctx.kernel_launches - launches0),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.case:
         return run_case(args)
+    if args.batched:
+        return run_batched(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

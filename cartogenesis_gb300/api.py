@@ -239,6 +239,22 @@ class StageRounds:
 
 class SeaLevelStage:
     @staticmethod
+    def drained_cut(config, height, enclosed_sea_max_share=0.00073, post_cut_outlet=True, ctx=None):
+        """SeaLevelStage.apply's cut with its enclosure rule and the drowned basins' outlets
+        (P/SeaLevelStage.kt:243-270, 371-437, 478-560): (shoreline, is_land, relative, land_cells, passes)."""
+        ctx = ctx or default_context()
+        H, W = config.params.height, config.params.width
+        h = _f32(height, (H, W))
+        land = np.empty((H, W), np.uint8)
+        rel = np.empty((H, W), np.float32)
+        s, n, passes = C.c_float(), C.c_int32(), C.c_int32()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_sea_level_cut(ctx.handle, C.byref(config.params), P(h), enclosed_sea_max_share,
+                                               int(post_cut_outlet), C.byref(s), P(land), P(rel), C.byref(n),
+                                               C.byref(passes)))
+        return s.value, land, rel, n.value, passes.value
+
+    @staticmethod
     def percentile_cut(height, sea_level_fraction, lowstand_share_of_field=0.0, highest_land_metres=6000.0,
                        deepest_ocean_metres=10000.0, ctx=None):
         """SeaLevelStage.percentileCut: (shoreline, is_land, relative, land_cells)."""

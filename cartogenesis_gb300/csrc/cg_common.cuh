@@ -103,9 +103,11 @@ enum Slot {
     S_DEPSLOT0, S_DEPSLOT1, S_DEPSLOT2, S_DEPSLOT3, S_DEPSLOT4, S_DEPSLOT5, S_DEPSLOT6, S_DEPSLOT7,
     S_DEPHEAP, S_DEPTOUCH, S_DEPREPLAY, S_DEPSEGC,
     S_OM_LAND, S_OM_REL, S_OM_FILLED, S_OM_RECV, S_OM_KEY, S_OM_AREA, S_OM_RUNOFF, S_OM_DONORS,
-    S_FILLEB, S_THERMERR,
+    S_FILLEB, S_THERMERR, S_SL_MASK, S_SL_LABEL, S_SL_SIZE, S_SL_WORDS, S_DEPSLOT8, S_DEPSLOT9, S_DEPSLOT10,
+    S_DEPCLAIM,
     S_COUNT
 };
+static_assert(S_COUNT <= (int)(sizeof(((cg_ctx*)nullptr)->bufs) / sizeof(DevBuf)), "a slot past the context's buffers");
 
 cg_status fail(cg_ctx* ctx, cg_status st, const char* fmt, ...);
 cg_status cuda_fail(cg_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);

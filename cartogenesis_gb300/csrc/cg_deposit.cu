@@ -45,7 +45,10 @@ namespace {
 constexpr int kThreads = 256;
 
 // Control words of a walk.
-enum { W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REDONE = 4, W_REPLAYED = 5, W_WORDS = 8 };
+enum {
+    W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REDONE = 4, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
+    W_WAIT0 = 8, W_WAIT1 = 9, W_WORDS = 16
+};
 
 struct WalkDev {
     Params p;
@@ -74,7 +77,12 @@ struct WalkDev {
     int* slot_sorted;
     double* slot_base;
     uint32_t* slot_bits;
-    int* slot_n;            // per slot: admitted cells (-1: no fan)
+    int* slot_n;            // per slot: admitted cells
+    int* slot_state;        // per slot: 1 while a lake fan waits to lay, else 0
+    double* slot_laid;      // per slot: what its fan laid
+    Touch* slot_touch;      // per slot: its fan's deposits, `cap` entries
+    int* slot_touch_n;
+    unsigned long long* claim;   // per cell: the (wave, rank) of the fan holding it
     // The sequential thread's heap (sea lobes, a redone level).
     int* heap_cells;
     float* heap_keys;
@@ -188,53 +196,84 @@ __device__ void admit_lake(const WalkDev& w, int s, int k) {
     w.slot_n[s] = got;
 }
 
-// A lake fan's laying over its sorted admitted cells (lay_admitted's loop): returns what it laid.
-__device__ double lay_lake(const WalkDev& w, int s, double budget, int* touch_n) {
+// A claim on a cell for a fan of rank `rank` in wave `wave`: later waves outrank earlier ones, and in
+// a wave the lowest rank holds the cell.
+__device__ __forceinline__ unsigned long long claim_key(unsigned wave, int rank) {
+    return ((unsigned long long)wave << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)rank);
+}
+
+// A lake fan's laying by one warp (lay_admitted's loop over the distance-sorted admitted cells). A
+// fan's cells are distinct, so laying into one changes no other's need: the warp reads 32 needs at
+// once and lays into the ones above zero one after another, in order, while the budget lasts. The
+// deposits go to the slot's own log.
+__device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) {
+    const unsigned FULL = 0xFFFFFFFFu;
     const int n = w.slot_n[s];
     const int* sorted = w.slot_sorted + (size_t)s * w.cap;
     const double* base = w.slot_base + (size_t)s * w.cap;
+    Touch* log = w.slot_touch + (size_t)s * w.cap;
     double remaining = budget, laid = 0.0;
-    for (int i = 0; i < n && remaining > 0.0; ++i) {
-        const int x = sorted[i];
-        const double need = __dsub_rn(base[i], (double)w.f.sediment[x]);
-        if (need <= 0.0) continue;
-        if (*touch_n < w.touch_cap) w.touches[*touch_n] = Touch{x, w.f.settled[x], w.f.sediment[x], 0.0f};
-        const double moved = raise(w.f.sediment, x, need < remaining ? need : remaining);
-        const float increment = (float)(moved * (double)w.p.to_relative);
-        w.f.settled[x] += increment;
-        if (*touch_n < w.touch_cap) w.touches[(*touch_n)++].increment = increment;
-        else w.words[W_ERROR] |= 1;
-        remaining -= moved;
-        laid += moved;
+    int logged = 0;
+    for (int i0 = 0; i0 < n && remaining > 0.0; i0 += 32) {
+        const int i = i0 + lane;
+        int x = -1;
+        double need = 0.0;
+        if (i < n) {
+            x = sorted[i];
+            need = __dsub_rn(base[i], (double)w.f.sediment[x]);
+        }
+        unsigned live = __ballot_sync(FULL, i < n && need > 0.0);
+        while (live && remaining > 0.0) {
+            const int j = __ffs(live) - 1;
+            live &= live - 1;
+            double moved = 0.0;
+            if (lane == j) {
+                log[logged] = Touch{x, w.f.settled[x], w.f.sediment[x], 0.0f};
+                moved = raise(w.f.sediment, x, need < remaining ? need : remaining);
+                const float increment = (float)(moved * (double)w.p.to_relative);
+                w.f.settled[x] += increment;
+                log[logged].increment = increment;
+            }
+            moved = __shfl_sync(FULL, moved, j);
+            ++logged;
+            remaining -= moved;
+            laid += moved;
+        }
     }
-    return laid;
+    if (lane == 0) {
+        w.slot_laid[s] = laid;
+        w.slot_touch_n[s] = logged;
+    }
 }
 
-// The sequential part of a level: the mouths of events [e0, e1) in rank order (lake fans admitted
-// into slots e - e0), logging their deposits.
-__device__ void run_mouths(const WalkDev& w, int e0, int e1, int* touch_n) {
+// The mouths of events [e0, e1) in rank order on one thread, into the level's log: a lake fan's
+// deposits (already laid in the waves) copied from its slot, a sea lobe run whole (its admission
+// reads what earlier lobes laid). ev_touch[e] receives each event's first entry.
+__device__ void log_and_run_seas(const WalkDev& w, int e0, int e1, int* touch_n) {
     for (int e = e0; e < e1; ++e) {
         const int k = w.events[e];
-        const int c = w.order[k];
-        const int kind = w.ev_kind[k];
-        const double carried = w.ev_carried[k];
         w.ev_touch[e] = *touch_n;
-        double laid;
-        if (kind == LAKE) {
-            laid = lay_lake(w, e - e0, mouth_budget(w.p, w.f, c, carried, kind), touch_n);
-            w.handoff[c] = __dsub_rn(carried, laid);
+        if (w.ev_kind[k] == LAKE) {
+            const Touch* t = w.slot_touch + (size_t)(e - e0) * w.cap;
+            const int nt = w.slot_touch_n[e - e0];
+            for (int i = 0; i < nt; ++i) {
+                if (*touch_n < w.touch_cap) w.touches[(*touch_n)++] = t[i];
+                else w.words[W_ERROR] |= 1;
+            }
         } else {
+            const int c = w.order[k];
             Heap h = thread_heap(w);
             TouchLog log{w.touches + *touch_n, w.touch_cap - *touch_n, 0, 0};
             const int id = ++w.words[W_MOUTH_ID];
-            mouth(w.p, w.f, c, carried, kind, w.stamp, id, h, &log);
+            mouth(w.p, w.f, c, w.ev_carried[k], SEA, w.stamp, id, h, &log);
             if (log.overflow) w.words[W_ERROR] |= 1;
             *touch_n += log.count;
         }
     }
 }
 
-// Step C, on one thread: detect and make the two repairs of the level [lo, hi) with events [0, n).
+// Step C, on one thread: detect and make the two repairs of the level [lo, hi) with events [0, n),
+// whose deposits are in the level's log in rank order.
 __device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int touch_n) {
     w.ev_touch[n] = touch_n;
     bool redo = false;
@@ -356,19 +395,71 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         }
         grid.sync();
         const int n = *(volatile int*)&w.words[W_EVENTS];
+        const int lane = threadIdx.x & 31;
+        const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+        const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
         int touch_n = 0;
-        // B: in chunks of `slots` mouths, the chunk's lake fans admitted at once, then its mouths in order.
+        // B in chunks of `slots` mouths, in rank order.
         for (int e0 = 0; e0 < n; e0 += w.slots) {
             const int e1 = min(n, e0 + w.slots);
+            // The chunk's lake fans admitted at once, a thread each.
             for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1; e += (int)(gridDim.x * blockDim.x)) {
                 const int k = w.events[e];
-                if (w.ev_kind[k] == LAKE) admit_lake(w, e - e0, k);
+                const bool lake = w.ev_kind[k] == LAKE;
+                if (lake) admit_lake(w, e - e0, k);
+                w.slot_state[e - e0] = lake ? 1 : 0;
+                w.slot_touch_n[e - e0] = 0;
             }
             grid.sync();
-            if (blockIdx.x == 0 && threadIdx.x == 0) run_mouths(w, e0, e1, &touch_n);
+            // The lake fans lay in waves, a warp each: a fan lays once no earlier waiting fan admitted
+            // any of its cells (its claims all hold), so overlapping fans lay in rank order and
+            // disjoint ones at once (their layings touch different cells). Bounded: the lowest waiting
+            // rank always holds its claims, so every wave lays at least one fan.
+            const unsigned wave0 = (unsigned)*(volatile int*)&w.words[W_WAVEBASE];
+            unsigned wave = wave0;
+            for (int guard = 0; guard <= e1 - e0; ++guard) {
+                const int par = (int)(wave & 1u);
+                for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
+                    if (!w.slot_state[sl]) continue;
+                    const unsigned long long key = claim_key(wave, w.events[e0 + sl]);
+                    const int* cells = w.slot_sorted + (size_t)sl * w.cap;
+                    for (int i = lane; i < w.slot_n[sl]; i += 32) atomicMax(&w.claim[cells[i]], key);
+                }
+                if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
+                grid.sync();
+                for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
+                    if (!w.slot_state[sl]) continue;
+                    const int rank = w.events[e0 + sl];
+                    const unsigned long long key = claim_key(wave, rank);
+                    const int* cells = w.slot_sorted + (size_t)sl * w.cap;
+                    bool held = true;
+                    for (int i = lane; i < w.slot_n[sl]; i += 32) held &= __ldcg(&w.claim[cells[i]]) == key;
+                    if (__all_sync(0xFFFFFFFFu, held)) {
+                        const int c = w.order[rank];
+                        const double carried = w.ev_carried[rank];
+                        lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
+                        if (lane == 0) {
+                            w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
+                            w.slot_state[sl] = 0;
+                        }
+                    } else if (lane == 0) {
+                        atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
+                    }
+                }
+                grid.sync();
+                ++wave;
+                if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
+                if (guard == e1 - e0 && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
+            }
+            // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                w.words[W_WAVEBASE] = (int)wave;
+                w.words[W_WAVES] += (int)(wave - wave0);
+                log_and_run_seas(w, e0, e1, &touch_n);
+            }
             grid.sync();
         }
-        // C: the repairs.
+        // C: the repairs, with every deposit of the level in its log.
         if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) repair_level(w, L, lo, hi, n, touch_n);
         grid.sync();
     }
@@ -473,12 +564,14 @@ cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
     CG_BUF(int, d_stamp, ctx, S_STAMP, N);
     CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
+    CG_BUF(unsigned long long, d_claim, ctx, S_DEPCLAIM, N);
     CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
     CG_LAUNCH(ctx) k_zero_float<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_sediment, N);
     CG_CHECK_LAUNCH(ctx);
-    // Fan ids and replay generations restart at 0, so every stamp and mark must too.
+    // Fan ids, replay generations and laying waves restart at 0, so every stamp, mark and claim must too.
     CG_CUDA(ctx, cudaMemsetAsync(d_stamp, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_claim, 0, N * sizeof(unsigned long long), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_words, 0, W_WORDS * sizeof(int), ctx->stream));
     return CG_OK;
 }
@@ -554,7 +647,11 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_BUF(int, d_sso, ctx, S_DEPSLOT4, S * cap);
     CG_BUF(double, d_sba, ctx, S_DEPSLOT5, S * cap);
     CG_BUF(uint32_t, d_sbits, ctx, S_DEPSLOT6, S * (size_t)w.box_words);
-    CG_BUF(int, d_sn, ctx, S_DEPSLOT7, S);
+    CG_BUF(int, d_sn, ctx, S_DEPSLOT7, 2 * S);
+    CG_BUF(double, d_slaid, ctx, S_DEPSLOT8, S);
+    CG_BUF(Touch, d_stouch, ctx, S_DEPSLOT9, S * cap);
+    CG_BUF(int, d_stn, ctx, S_DEPSLOT10, S);
+    CG_BUF(unsigned long long, d_claim, ctx, S_DEPCLAIM, N);
     w.slot_heap_cells = d_shc;
     w.slot_heap_keys = d_shk;
     w.slot_heap_pens = d_shp;
@@ -563,6 +660,11 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.slot_base = d_sba;
     w.slot_bits = d_sbits;
     w.slot_n = d_sn;
+    w.slot_state = d_sn + S;
+    w.slot_laid = d_slaid;
+    w.slot_touch = d_stouch;
+    w.slot_touch_n = d_stn;
+    w.claim = d_claim;
     CG_BUF(int, d_hc, ctx, S_DEPHEAP, 4 * cap);
     w.heap_cells = d_hc;
     w.heap_keys = (float*)(d_hc + cap);
@@ -593,9 +695,11 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_CUDA(ctx, cudaStreamSynchronize(sm));
     if (words[W_ERROR] & 1) return fail(ctx, CG_INEXACT, "deposition: a level's fan deposits overflowed the repair log");
     if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
+    if (words[W_ERROR] & 4) return fail(ctx, CG_INEXACT, "deposition: the lake fans' laying waves did not converge");
     if (counts) {
         counts->redone = words[W_REDONE];
         counts->replayed = words[W_REPLAYED];
+        counts->waves = words[W_WAVES];
     }
     return CG_OK;
 }

@@ -14,7 +14,7 @@ EXPORTS = [
     "cg_stream", "cg_kernel_launches", "cg_probe_fp64_rate",
     "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_erode_batch", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
-    "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish",
+    "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish", "cg_sea_level_cut",
 ]
 
 
@@ -72,6 +72,8 @@ def load_library(path=LIB_PATH):
             L.cg_erode_rounds.argtypes = [vp, i32, i32, C.POINTER(abi.Weather), vp]
             L.cg_stage_height.argtypes = [vp, vp]
             L.cg_stage_finish.argtypes = [vp, C.POINTER(abi.Outputs)]
+            L.cg_sea_level_cut.argtypes = [vp, PP, vp, f64, i32, C.POINTER(f32), vp, vp, C.POINTER(i32),
+                                           C.POINTER(i32)]
         _lib = L
         return _lib
 

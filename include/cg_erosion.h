@@ -314,6 +314,22 @@ cg_status cg_percentile_cut(cg_ctx* ctx, int32_t width, int32_t height, const fl
                             float* shoreline, uint8_t* is_land, float* relative,
                             int32_t* land_cells);
 
+/*
+ * SeaLevelStage.apply's cut up to the drowned basins' outlets (.../pipeline/SeaLevelStage.kt:243-270):
+ * the percentile cut at today's stand, the enclosure rule (markUnreachableWaterAsLand, :371-437: every
+ * water body but the ocean no larger than enclosed_sea_max_share of the planet's map area becomes land)
+ * and, with post_cut_outlet, up to 16 outlet passes over the basins whose floor lies below the
+ * shoreline (drainDrownedBasins, :478-560: fill, routing, accumulation and spillways over the whole
+ * grid, the notch with belowSea, then the re-cut at the same shoreline). The reference runs the
+ * erosion stage's routing here, outside the stage. The drowned valleys, littoral grading and shelf
+ * that follow in SeaLevelStage.apply are not this library's. `height` is host memory and is not
+ * written (the passes cut a copy); `passes` (may be NULL) receives the outlet passes that cut.
+ * Defaults: SeaConfig.enclosedSeaMaxShareOfSurface 0.00073, postCutOutlet 1.
+ */
+cg_status cg_sea_level_cut(cg_ctx* ctx, const cg_erosion_params* params, const float* height,
+                           double enclosed_sea_max_share, int32_t post_cut_outlet, float* shoreline,
+                           uint8_t* is_land, float* relative, int32_t* land_cells, int32_t* passes);
+
 /* FlowRouting.fillDepressions (.../pipeline/FlowRouting.kt:52-111). */
 cg_status cg_fill_depressions(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
                               const float* relative, float* filled, int64_t* ties,

@@ -7,6 +7,7 @@ package com.cartogenesis.desktop
 import com.cartogenesis.worldgen.model.FloatField
 import com.cartogenesis.worldgen.model.WorldGenConfig
 import com.cartogenesis.worldgen.pipeline.ErosionAccelerator
+import com.cartogenesis.worldgen.pipeline.SeaLevelResult
 import com.cartogenesis.worldgen.pipeline.ThermalLimits
 import java.lang.foreign.Arena
 import java.lang.foreign.FunctionDescriptor
@@ -69,6 +70,8 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     private val rounds = fn("cg_erode_rounds", FunctionDescriptor.of(JAVA_INT, ADDRESS, JAVA_INT, JAVA_INT, ADDRESS, ADDRESS))
     private val current = fn("cg_stage_height", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
     private val finish = fn("cg_stage_finish", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
+    private val seaCut = fn("cg_sea_level_cut", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS, JAVA_DOUBLE,
+        JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS, ADDRESS))
     private val ctx: MemorySegment
 
     override val name = "GB300 (cg_erosion)"
@@ -165,6 +168,34 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
             }
             FloatField(config.width, config.height, result.toArray(JAVA_FLOAT))
         }
+
+    /**
+     * SeaLevelStage.applyWithValleyBar's first three steps (SeaLevelStage.kt:243-270): the percentile cut,
+     * the enclosure rule and the drowned basins' outlet passes, on the device. Returns the
+     * SeaLevelResult the rest of the stage (DrownedValleys, LittoralGrading, the shelf) continues from.
+     */
+    fun drainedCut(config: WorldGenConfig, height: FloatField, enclosedSeaMaxShare: Double,
+                   postCutOutlet: Boolean): SeaLevelResult = Arena.ofConfined().use { a ->
+        val p = a.allocate(112, 8)
+        defaults.invokeExact(p, config.width, config.height, config.seed)
+        p.set(JAVA_DOUBLE, 24, config.scale.worldWidthKm)
+        p.set(JAVA_FLOAT, 32, config.scale.highestLandMetres)
+        p.set(JAVA_FLOAT, 36, config.scale.deepestOceanMetres)
+        p.set(JAVA_INT, 76, if (config.facetRouting) 1 else 0)
+        p.set(JAVA_INT, 80, if (config.flatPotential) 1 else 0)
+        p.set(JAVA_FLOAT, 84, config.seaLevel)
+        val cells = height.data.size.toLong()
+        val h = a.allocateFrom(JAVA_FLOAT, *height.data)
+        val shoreline = a.allocate(JAVA_FLOAT)
+        val land = a.allocate(cells)
+        val relative = a.allocate(JAVA_FLOAT, cells)
+        val count = a.allocate(JAVA_INT)
+        check(seaCut.invokeExact(ctx, p, h, enclosedSeaMaxShare, if (postCutOutlet) 1 else 0, shoreline, land,
+                                 relative, count, MemorySegment.NULL) as Int, ctx, lastError)
+        val isLand = BooleanArray(cells.toInt()) { land.get(java.lang.foreign.ValueLayout.JAVA_BYTE, it.toLong()) != 0.toByte() }
+        SeaLevelResult(shoreline.get(JAVA_FLOAT, 0), isLand,
+                       FloatField(config.width, config.height, relative.toArray(JAVA_FLOAT)), count.get(JAVA_INT, 0))
+    }
 
     override fun close() {
         destroy.invokeExact(ctx)

@@ -83,6 +83,9 @@ def lib():
         L.or_erode_stage_fed.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs),
                                          C.POINTER(abi.Inputs), C.POINTER(abi.Outputs)]
         L.or_erode_stage_fed.restype = i32
+        L.or_sea_level_drained_cut.argtypes = [C.POINTER(abi.ErosionParams), vp, f64, i32, C.POINTER(f32), vp, vp,
+                                               C.POINTER(i32), C.POINTER(i32)]
+        L.or_sea_level_drained_cut.restype = i32
         _lib = L
     return _lib
 
@@ -366,3 +369,17 @@ def erode_stage(params, height, uplift=None, rock=None, rain=None, veg=None, the
                           largest_depth=basins.largest_depth, deepest=basins.deepest)
     outs["stats"] = [{f: getattr(s, f) for f, _ in abi.RoundStats._fields_} for s in stats]
     return outs
+
+
+def sea_level_drained_cut(params, height, enclosed_max_share=0.00073, post_cut_outlet=True):
+    """SeaLevelStage.apply's cut with the enclosure rule and the drowned basins' outlets:
+    (shoreline, is_land, relative, land_cells, passes)."""
+    H, W = params.height, params.width
+    h = np.ascontiguousarray(height, dtype=np.float32).reshape(H, W)
+    land = np.empty((H, W), np.uint8)
+    rel = np.empty((H, W), np.float32)
+    s, n, passes = C.c_float(), C.c_int32(), C.c_int32()
+    st = lib().or_sea_level_drained_cut(C.byref(params), P(h), enclosed_max_share, int(post_cut_outlet), C.byref(s),
+                                        P(land), P(rel), C.byref(n), C.byref(passes))
+    assert st == 0, st
+    return s.value, land, rel, n.value, passes.value

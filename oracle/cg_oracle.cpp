@@ -1025,7 +1025,7 @@ struct Breached {
 // order spillways found them; `relative`, `ground` and `surface` are cut in place.
 Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_land, float* relative, float* ground,
                 const int32_t* dirs, const float* area, float land_cells, float land_range, float* surface,
-                float* settled = nullptr, double* load = nullptr) {
+                float* settled = nullptr, double* load = nullptr, bool below_sea = false, int rows = 0) {
     Breached out;
     const GroundSteps& steps = rates.steps;
     const float reach = (float)rates.outlet_reach_cells;   // Float < Int compares as floats
@@ -1072,15 +1072,17 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
         float slope = fall / length * (float)W;
         if (slope < 0.0f) slope = 0.0f;
         float power = rates.relative_incision_coefficient * 1.125f * std::sqrt(area[spill] / land_cells) * slope;
-        float drop = jvm_min(power, jvm_min(level - floor_, level));
+        // Never below the basin's floor; inside the rounds never below the sea either (belowSea off).
+        float drop = below_sea ? jvm_min(power, level - floor_) : jvm_min(power, jvm_min(level - floor_, level));
         if (drop <= 0.0f) continue;
         float new_level = level - drop;
-        // Down the channel from the lip, falling `gradient` a cell width, never below the shoreline.
+        // Down the channel from the lip, falling `gradient` a cell width, never below the shoreline
+        // (belowSea: down to wherever the falling surface goes).
         float from_lip = 0.0f;
         cell = spill;
         while (cell >= 0 && is_land[cell] && from_lip < reach) {
             float falling = new_level - from_lip * gradient;
-            float cut_level = falling < 0.0f ? 0.0f : falling;
+            float cut_level = below_sea ? falling : (falling < 0.0f ? 0.0f : falling);
             if (relative[cell] <= cut_level) break;
             take_down_to(cell, cut_level);
             int next = dirs[cell];
@@ -1089,6 +1091,7 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
         }
         // Back across the shallow margin, from the lip towards the entry, rising by the same gradient.
         int entry = notch.entry[b];
+        float back = 0.0f;
         if (entry >= 0 && entry != spill) {
             int margin_cells = 0;
             int walker = entry;
@@ -1106,7 +1109,6 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
                     margin[i] = walker;
                     walker = dirs[walker];
                 }
-                float back = 0.0f;
                 int downstream = spill;
                 for (int i = margin_cells - 1; i >= 0; --i) {
                     int m = margin[i];
@@ -1118,8 +1120,158 @@ Breached breach(const Rates& rates, int W, const Spillways& notch, const u8* is_
                 }
             }
         }
+        // belowSea: the sill on the basin's own side too (HydraulicErosion.kt:2099-2168), the same
+        // surface continued back across the lake bed up the inflow of the largest catchment (ties to
+        // the lower index), rising by the gradient, never leaving the water, within the reach.
+        if (below_sea) {
+            const int H = rows;
+            int from = entry >= 0 ? entry : spill;
+            while (back <= reach) {
+                int best = -1;
+                float best_area = -1.0f;
+                for_each_neighbour(W, H, from % W, from / W, [&](int n, int, int) {
+                    if (is_land[n] && dirs[n] == from && ground[n] - relative[n] > rates.pond_depth) {
+                        float a = area[n];
+                        bool ties = a == best_area && (best < 0 || n < best);
+                        if (a > best_area || ties) {
+                            best_area = a;
+                            best = n;
+                        }
+                    }
+                });
+                if (best < 0) break;
+                back += steps.between(best, from, W);
+                if (back > reach) break;
+                float cut_level = new_level + back * gradient;
+                if (relative[best] <= cut_level) break;
+                double take = (double)(relative[best] - cut_level) * (double)land_range;
+                double taken = -raise(surface, best, -take);
+                if (taken > 0.0) {
+                    float as_relative = (float)(taken / (double)land_range);
+                    relative[best] -= as_relative;
+                    if (settled) settled[best] -= as_relative;
+                    if (load) load[best] += taken;
+                    out.moved += taken;
+                    out.cells++;
+                }
+                from = best;
+            }
+        }
     }
     return out;
+}
+
+// ---------------------------------------------------------------- SeaLevelStage's drowned basins
+
+// SeaLevelStage.landAndWaterAt (SeaLevelStage.kt:175-200): the cut at a given shoreline.
+void land_and_water_at(int W, int H, const float* h, float shoreline, const Scale& sc, Cut& out) {
+    const size_t N = (size_t)W * H;
+    const float land_half = std::max(sc.land_half(), 1e-6f), sea_half = std::max(sc.sea_half(), 1e-6f);
+    out.shoreline = shoreline;
+    out.is_land.assign(N, 0);
+    out.relative.assign(N, 0.0f);
+    out.land_cells = 0;
+    for (size_t c = 0; c < N; ++c) {
+        if (h[c] >= shoreline) {
+            out.is_land[c] = 1;
+            out.land_cells++;
+            out.relative[c] = (h[c] - shoreline) / land_half;
+        } else {
+            out.relative[c] = (h[c] - shoreline) / sea_half;
+        }
+    }
+}
+
+// SeaLevelStage.markUnreachableWaterAsLand (SeaLevelStage.kt:371-437): the water bodies (8-connected,
+// found from ascending start cells by a stack), the largest the ocean (the first found of that size);
+// every other body no larger than the largest lake Earth has becomes land at its own height.
+void mark_unreachable_water_as_land(int W, int H, Cut& cut, const float* h, const Scale& sc, double km2_per_cell,
+                                    double enclosed_max_share) {
+    const size_t N = (size_t)W * H;
+    const int water = (int)N - cut.land_cells;
+    if (water == 0) return;
+    std::vector<int> body_of(N, -1), frontier(water);
+    std::vector<int> cells_in;
+    int bodies = 0, ocean = -1, ocean_cells = 0;
+    for (size_t start = 0; start < N; ++start) {
+        if (cut.is_land[start] || body_of[start] >= 0) continue;
+        const int body = bodies++;
+        int fs = 0;
+        body_of[start] = body;
+        frontier[fs++] = (int)start;
+        int found = 0;
+        while (fs > 0) {
+            const int c = frontier[--fs];
+            found++;
+            for_each_neighbour(W, H, c % W, c / W, [&](int n, int, int) {
+                if (!cut.is_land[n] && body_of[n] < 0) {
+                    body_of[n] = body;
+                    frontier[fs++] = n;
+                }
+            });
+        }
+        cells_in.push_back(found);
+        if (found > ocean_cells) {
+            ocean_cells = found;
+            ocean = body;
+        }
+    }
+    if (bodies <= 1) return;
+    const int largest_lake = (int)(enclosed_max_share * sc.world_area_km2() / km2_per_cell);
+    const float land_half = std::max(sc.land_half(), 1e-6f);
+    for (size_t c = 0; c < N; ++c) {
+        const int body = body_of[c];
+        if (body < 0 || body == ocean || cells_in[body] > largest_lake) continue;
+        cut.is_land[c] = 1;
+        cut.land_cells++;
+        cut.relative[c] = (h[c] - cut.shoreline) / land_half;
+    }
+}
+
+// SeaLevelStage.drainDrownedBasins (SeaLevelStage.kt:478-560): the outlet notch once more, belowSea,
+// over only the basins whose floor lies below the shoreline, up to MAX_POST_CUT_OUTLET_PASSES times,
+// each pass re-cut at the same shoreline with the enclosure rule. The terrain it cuts is a copy.
+void drain_drowned_basins(const cg_erosion_params& p, Cut& current, const float* height, double enclosed_max_share,
+                          int* passes_run) {
+    const int W = p.width, H = p.height;
+    const size_t N = (size_t)W * H;
+    const Scale sc = scale_of(p);
+    const float land_half = std::max(sc.land_half(), 1e-6f);
+    const Rates rates(p);
+    const double r = sc.cell_height_km(H) / sc.cell_width_km(W);
+    const int lattice = smooth_field_lattice_columns(p.world_width_km);
+    const double km2_per_cell = sc.cell_width_km(W) * sc.cell_height_km(H);
+    std::vector<float> terrain;
+    std::vector<float> ones(N, 1.0f), filled(N), area(N);
+    std::vector<int32_t> dirs(N);
+    *passes_run = 0;
+    for (int pass = 0; pass < 16; ++pass) {   // SeaLevelStage.MAX_POST_CUT_OUTLET_PASSES
+        if (current.land_cells == 0) return;
+        std::vector<float> relative = current.relative;
+        fill_depressions(W, H, current.is_land.data(), relative.data(), filled.data());
+        FlatCounts fc;
+        flow_directions(W, H, current.is_land.data(), relative.data(), filled.data(), p.seed, r, lattice,
+                        p.facet_routing != 0, p.flat_potential != 0, dirs.data(), nullptr, &fc);
+        accumulate(W, H, current.is_land.data(), dirs.data(), current.land_cells, ones.data(), area.data());
+        Spillways sw;
+        spillways(W, H, current.is_land.data(), relative.data(), filled.data(), dirs.data(), rates.pond_depth, sw,
+                  nullptr);
+        int drowned = 0;
+        for (int b = 0; b < sw.count; ++b) {
+            if (sw.floor_[b] >= 0.0f) sw.spill[b] = -1;
+            else if (sw.spill[b] >= 0) drowned++;
+        }
+        if (drowned == 0) return;
+        if (terrain.empty()) terrain.assign(height, height + N);
+        *passes_run = pass + 1;
+        Breached b = breach(rates, W, sw, current.is_land.data(), relative.data(), filled.data(), dirs.data(),
+                            area.data(), (float)current.land_cells, land_half, terrain.data(), nullptr, nullptr, true, H);
+        if (b.cells == 0) return;
+        Cut next;
+        land_and_water_at(W, H, terrain.data(), current.shoreline, sc, next);
+        mark_unreachable_water_as_land(W, H, next, terrain.data(), sc, km2_per_cell, enclosed_max_share);
+        current = std::move(next);
+    }
 }
 
 // ---------------------------------------------------------------- deposition (profile P2)
@@ -2519,6 +2671,29 @@ int32_t or_capture_walk(const cg_erosion_params* p, const cg_inputs* in, int32_t
     std::memcpy(sediment_after, c.sediment_after.data(), N * 4);
     std::memcpy(settled_after, c.settled_after.data(), N * 4);
     std::memcpy(load_after, c.load_after.data(), N * 8);
+    return 0;
+}
+
+// SeaLevelStage.apply's cut with its enclosure rule and the drowned basins' outlets
+// (SeaLevelStage.kt:243-270, enclosedSeaIsLand and postCutOutlet on; the drowned valleys, littoral
+// grading and shelf after them are not this path's): is_land, relative, land_cells and the passes run.
+int32_t or_sea_level_drained_cut(const cg_erosion_params* p, const float* height, double enclosed_max_share,
+                                 int32_t post_cut_outlet, float* shoreline, uint8_t* is_land, float* relative,
+                                 int32_t* land_cells, int32_t* passes) {
+    const int W = p->width, H = p->height;
+    const size_t N = (size_t)W * H;
+    const Scale sc = scale_of(*p);
+    Cut cut;
+    percentile_cut(W, H, height, p->sea_level, sc, 0.0f, cut);
+    mark_unreachable_water_as_land(W, H, cut, height, sc, sc.cell_width_km(W) * sc.cell_height_km(H),
+                                   enclosed_max_share);
+    int run = 0;
+    if (post_cut_outlet) drain_drowned_basins(*p, cut, height, enclosed_max_share, &run);
+    *shoreline = cut.shoreline;
+    std::memcpy(is_land, cut.is_land.data(), N);
+    std::memcpy(relative, cut.relative.data(), N * 4);
+    *land_cells = cut.land_cells;
+    *passes = run;
     return 0;
 }
 
