@@ -116,6 +116,8 @@ class RoundStats(C.Structure):
         ("ms_deposit", C.c_double),
         ("deposit_replayed", C.c_int32),
         ("deposit_redone", C.c_int32),
+        ("deposit_refitted", C.c_int32),
+        ("deposit_waves", C.c_int32),
     ]
 
 

@@ -47,7 +47,7 @@ constexpr int kThreads = 256;
 // Control words of a walk.
 enum {
     W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REDONE = 4, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
-    W_WAIT0 = 8, W_WAIT1 = 9, W_WORDS = 16
+    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_WORDS = 16
 };
 
 struct WalkDev {
@@ -68,15 +68,16 @@ struct WalkDev {
     int* seg_events;        // per rank: listed ranks, compacted within each CTA's segment
     int* seg_count;         // per CTA
     int* events;            // the level's listed ranks, dense, in rank order
-    // Lake-fan admission slots, `slots` of them, each `cap` entries.
+    // The round's lake fans, admitted before the walk (k_admit_lakes): per candidate mouth cell its
+    // admitted cells sorted by distance and each one's level less its terrain, in a pool.
+    const int* cand_of;     // per cell: its candidate index, -1 if it is no lake mouth
+    const int* cand_n;      // per candidate: admitted cells
+    const long long* cand_off;   // per candidate: first pool entry
+    const int* pool_cells;
+    const double* pool_base;
+    // The mouths of a chunk, `slots` of them at a time.
     int slots, cap, box_words;
-    int* slot_heap_cells;
-    float* slot_heap_keys;
-    float* slot_heap_pens;
-    int* slot_admitted;
-    int* slot_sorted;
-    double* slot_base;
-    uint32_t* slot_bits;
+    long long* slot_off;    // per slot: its fan's first pool entry
     int* slot_n;            // per slot: admitted cells
     int* slot_state;        // per slot: 1 while a lake fan waits to lay, else 0
     double* slot_laid;      // per slot: what its fan laid
@@ -95,6 +96,7 @@ struct WalkDev {
     int* ev_touch;          // per listed mouth (dense index): its first touch; [n + 1]
     int* mark;              // per cell: the generation that listed it for a replay
     int* replay;            // cells to replay
+    int* refit;             // cells to refit
     int* words;             // W_* control words
 };
 
@@ -155,45 +157,119 @@ __device__ void walk_one(const WalkDev& w, int k) {
     }
 }
 
-// A lake fan's admission into slot `s`: the admitted cells sorted by distance from the apex (with
-// the cell as the tie break, the laying heap's pop order) and each one's level less its terrain.
-__device__ void admit_lake(const WalkDev& w, int s, int k) {
-    const int c = w.order[k];
-    int* cells = w.slot_heap_cells + (size_t)s * w.cap;
-    float* keys = w.slot_heap_keys + (size_t)s * w.cap;
-    float* pens = w.slot_heap_pens + (size_t)s * w.cap;
-    int* admitted = w.slot_admitted + (size_t)s * w.cap;
-    int* sorted = w.slot_sorted + (size_t)s * w.cap;
-    double* base = w.slot_base + (size_t)s * w.cap;
-    uint32_t* bits = w.slot_bits + (size_t)s * w.box_words;
-    for (int i = 0; i < w.box_words; ++i) bits[i] = 0u;
-    Rim m;
-    mouth_rim(w.p, w.f, c, LAKE, m);
-    int outside = 0;
-    BoxVisited visited{bits, w.p.W, m.apex_column, m.apex_row, box_bx(w.p), box_by(w.p), &outside};
-    Heap h{cells, keys, pens, admitted, w.cap, 0, 0};
-    const int n = admit(w.p, w.f, m, false, visited, h);
-    if (outside) atomicOr(&w.words[W_ERROR], 2);   // the rim reached past its box: cannot happen
-    h.size = 0;
-    for (int i = 0; i < n; ++i) {
-        const int x = admitted[i];
-        const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
-        heap_push(h, x, sqrt_rn(co * co + ro * ro), 0.0f);
+// The round's lake mouths and their fans' admissions, ahead of the walk. A lake fan's admission (its
+// best-first growth inside the rim, DeltaFan.growFan) reads only fixed fields: the land, the lake's
+// depth (ground less relative height) and the rim, which depends on the mouth and its receiver. So
+// every cell whose step ends in a lake (kind LAKE: dry, its land receiver ponded) has its fan admitted
+// once per round, all at once, whether or not the walk later gives it anything to lay.
+struct AdmitDev {
+    Params p;
+    Fields f;
+    int cap, box_words;
+    const int* cand;        // candidate mouth cells
+    int ncand;
+    int* cand_n;            // pass 1 writes the admitted counts
+    const long long* cand_off;   // pass 2 reads the pool offsets
+    int* pool_cells;
+    double* pool_base;
+    int* h_cells;           // per thread: a heap of `cap` entries and the visited bits of a box
+    float* h_keys;
+    float* h_pens;
+    int* h_admitted;
+    uint32_t* h_bits;
+    int fill;               // 0: count, 1: fill the pool
+    int* err;
+};
+
+__global__ void k_lake_candidates(Params p, Fields f, int N, int* __restrict__ cand, int* __restrict__ ncand,
+                                  int* __restrict__ cand_of) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+        int idx = -1;
+        const int r = f.dirs[c];
+        if (f.land[c] && r >= 0 && f.land[r] && !ponded(p, f, c) && ponded(p, f, r)) {
+            idx = atomicAdd(ncand, 1);
+            cand[idx] = c;
+        }
+        cand_of[c] = idx;
     }
-    int got = 0, x;
-    float pen;
-    while (heap_pop(h, x, pen)) {
-        const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
-        const float distance = sqrt_rn(co * co + ro * ro);
-        float fraction = distance / m.reach_cells;
-        if (fraction > 1.0f) fraction = 1.0f;
-        const float depth = 2.0f * w.p.pond_depth * (1.0f + kLakeFanSlope * fraction) * (0.9f + 0.35f * cell_wobble(x));
-        const float level = w.p.shoreline + (w.f.ground[x] - depth) * w.p.land_range;
-        sorted[got] = x;
-        base[got] = (double)level - (double)w.f.surface[x];
-        ++got;
+}
+
+// A candidate's admission; pass 1 counts its admitted cells, pass 2 writes them to the pool sorted by
+// distance from the apex with the cell as the tie break (the laying heap's pop order), each with its
+// level less its terrain (lay_admitted's need before the sediment).
+__global__ void __launch_bounds__(128) k_admit_lakes(AdmitDev a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int threads = gridDim.x * blockDim.x;
+    int* cells = a.h_cells + (size_t)t * a.cap;
+    float* keys = a.h_keys + (size_t)t * a.cap;
+    float* pens = a.h_pens + (size_t)t * a.cap;
+    int* admitted = a.h_admitted + (size_t)t * a.cap;
+    uint32_t* bits = a.h_bits + (size_t)t * a.box_words;
+    for (int i = t; i < a.ncand; i += threads) {
+        const int c = a.cand[i];
+        for (int j = 0; j < a.box_words; ++j) bits[j] = 0u;
+        Rim m;
+        mouth_rim(a.p, a.f, c, LAKE, m);
+        int outside = 0;
+        BoxVisited visited{bits, a.p.W, m.apex_column, m.apex_row, box_bx(a.p), box_by(a.p), &outside};
+        Heap h{cells, keys, pens, admitted, a.cap, 0, 0};
+        const int n = admit(a.p, a.f, m, false, visited, h);
+        if (outside) atomicOr(a.err, 2);   // the rim reached past its box: cannot happen
+        if (!a.fill) {
+            a.cand_n[i] = n;
+            continue;
+        }
+        h.size = 0;
+        for (int k = 0; k < n; ++k) {
+            const int x = admitted[k];
+            const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
+            heap_push(h, x, sqrt_rn(co * co + ro * ro), 0.0f);
+        }
+        int* sorted = a.pool_cells + a.cand_off[i];
+        double* base = a.pool_base + a.cand_off[i];
+        int got = 0, x;
+        float pen;
+        while (heap_pop(h, x, pen)) {
+            const float co = rim_column_offset(m, x), ro = rim_row_offset(m, x);
+            const float distance = sqrt_rn(co * co + ro * ro);
+            float fraction = distance / m.reach_cells;
+            if (fraction > 1.0f) fraction = 1.0f;
+            const float depth =
+                2.0f * a.p.pond_depth * (1.0f + kLakeFanSlope * fraction) * (0.9f + 0.35f * cell_wobble(x));
+            const float level = a.p.shoreline + (a.f.ground[x] - depth) * a.p.land_range;
+            sorted[got] = x;
+            base[got] = (double)level - (double)a.f.surface[x];
+            ++got;
+        }
     }
-    w.slot_n[s] = got;
+}
+
+// Exclusive prefix sum of n 64-bit counts by one CTA, chunk after chunk; out[n] receives the total.
+__global__ void __launch_bounds__(1024) k_scan64_one_block(const long long* __restrict__ in, long long* __restrict__ out,
+                                                          int n) {
+    __shared__ long long sh[1024];
+    long long carry = 0;
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + (int)threadIdx.x;
+        const long long v = i < n ? in[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const long long t = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n) out[i] = carry + sh[threadIdx.x] - v;
+        const long long chunk = sh[1023];
+        __syncthreads();
+        carry += chunk;
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_widen_counts(const int* __restrict__ n, int count, long long* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) out[i] = n[i];
 }
 
 // A claim on a cell for a fan of rank `rank` in wave `wave`: later waves outrank earlier ones, and in
@@ -209,8 +285,8 @@ __device__ __forceinline__ unsigned long long claim_key(unsigned wave, int rank)
 __device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) {
     const unsigned FULL = 0xFFFFFFFFu;
     const int n = w.slot_n[s];
-    const int* sorted = w.slot_sorted + (size_t)s * w.cap;
-    const double* base = w.slot_base + (size_t)s * w.cap;
+    const int* sorted = w.pool_cells + w.slot_off[s];
+    const double* base = w.pool_base + w.slot_off[s];
     Touch* log = w.slot_touch + (size_t)s * w.cap;
     double remaining = budget, laid = 0.0;
     int logged = 0;
@@ -272,14 +348,86 @@ __device__ void log_and_run_seas(const WalkDev& w, int e0, int e1, int* touch_n)
     }
 }
 
-// Step C, on one thread: detect and make the two repairs of the level [lo, hi) with events [0, n),
-// whose deposits are in the level's log in rank order.
+// The kind of a cell's step (own_walk's answer), read from the fixed fields alone.
+__device__ __forceinline__ int kind_of(const WalkDev& w, int c) {
+    const int r = w.f.dirs[c];
+    if (r < 0) return OFF_MAP;
+    if (!w.f.land[r]) return SEA;
+    if (!ponded(w.p, w.f, c) && ponded(w.p, w.f, r)) return LAKE;
+    return ON;
+}
+
+// Cell d's settled height as the reference's walk shows it to the cell of rank `rc` of this level:
+// its value before the level's fans, plus the increments of the level's fans ranked before rc, in
+// order. False when no fan of the level touched d (its current value is then the answer).
+__device__ bool settled_as_of(const WalkDev& w, int d, int rc, int n, float* out) {
+    bool seen = false;
+    float v = 0.0f;
+    for (int e = 0; e < n; ++e) {
+        const int rank = w.events[e];
+        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
+            if (w.touches[t].cell != d) continue;
+            if (!seen) {
+                seen = true;
+                v = w.touches[t].settled_before;
+            }
+            if (rank < rc) v += w.touches[t].increment;
+        }
+    }
+    *out = v;
+    return seen;
+}
+
+// A dry cell of the level whose headroom read a donor that an earlier fan of the level raised, when
+// its step hands everything on to a land receiver (kind ON): its own walk is taken again from its
+// state before it, with each donor's settled height as the reference's walk shows it at the cell's
+// rank. Nothing else of the level reads such a cell (fans touch only ponded land and sea, and cells of
+// one level never read one another), so the fix is local. Returns false (a whole redo is needed)
+// where the cell has a mouth, whose fan would change with it.
+__device__ bool refit_cell(const WalkDev& w, int c, int n) {
+    if (kind_of(w, c) != ON) return false;
+    const int rc = w.rank_of[c];
+    w.f.settled[c] = w.s0[rc];
+    w.f.sediment[c] = w.d0[rc];
+    const int W = w.p.W, H = w.p.H, col = c % W, row = c / W;
+    int patched[8];
+    float kept[8];
+    int np = 0;
+    for (int rs = -1; rs <= 1; ++rs) {
+        const int nr = row + rs;
+        if (nr < 0 || nr >= H) continue;
+        for (int cs = -1; cs <= 1; ++cs) {
+            if (rs == 0 && cs == 0) continue;
+            const int d = nr * W + ((col + cs) & (W - 1));
+            if (w.f.dirs[d] != c) continue;
+            float v;
+            if (settled_as_of(w, d, rc, n, &v)) {
+                patched[np] = d;
+                kept[np++] = w.f.settled[d];
+                w.f.settled[d] = v;
+            }
+        }
+    }
+    double carried = arriving(w, c);
+    bool used;
+    double incised = 0.0, deposited = 0.0;
+    own_walk(w.p, w.f, c, carried, &used, &incised, &deposited);
+    w.handoff[c] = carried;
+    for (int i = 0; i < np; ++i) w.f.settled[patched[i]] = kept[i];
+    return true;
+}
+
+// Step C, on one thread: detect and make the repairs of the level [lo, hi) with events [0, n), whose
+// deposits are in the level's log in rank order. (a) a ponded cell of the level ranked after a fan
+// that laid into it has its settled height replayed in rank order; (b) a later cell of the level that
+// read, in its headroom, a donor such a fan raised is refitted (refit_cell), or, where it has a mouth
+// of its own, the level is restored and walked one cell after another.
 __device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int touch_n) {
     w.ev_touch[n] = touch_n;
     bool redo = false;
-    int replays = 0;
+    int replays = 0, refits = 0;
     const int gen = ++w.words[W_GEN];
-    for (int e = 0; e < n && !redo; ++e) {
+    for (int e = 0; e < n; ++e) {
         const int rank = w.events[e];
         for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
             const int x = w.touches[t].cell;
@@ -289,9 +437,11 @@ __device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int
                 w.replay[replays++] = x;
             }
             const int rr = w.f.dirs[x];
-            if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr]) {
-                redo = true;
-                break;
+            if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr] &&
+                w.mark[rr] != -gen) {
+                w.mark[rr] = -gen;   // a dry cell: never a replay's (those are ponded)
+                if (kind_of(w, rr) != ON) redo = true;
+                w.refit[refits++] = rr;
             }
         }
     }
@@ -307,6 +457,10 @@ __device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int
         }
         for (int k = lo; k < hi; ++k) walk_one(w, k);
         return;
+    }
+    for (int i = 0; i < refits; ++i) {
+        refit_cell(w, w.refit[i], n);
+        w.words[W_REFITTED]++;
     }
     for (int i = 0; i < replays; ++i) {
         // The cell's own subtraction and the fans' increments, in rank order.
@@ -402,11 +556,15 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         // B in chunks of `slots` mouths, in rank order.
         for (int e0 = 0; e0 < n; e0 += w.slots) {
             const int e1 = min(n, e0 + w.slots);
-            // The chunk's lake fans admitted at once, a thread each.
+            // The chunk's lake fans, their admissions taken from the round's pool.
             for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1; e += (int)(gridDim.x * blockDim.x)) {
                 const int k = w.events[e];
                 const bool lake = w.ev_kind[k] == LAKE;
-                if (lake) admit_lake(w, e - e0, k);
+                if (lake) {
+                    const int ci = w.cand_of[w.order[k]];
+                    w.slot_off[e - e0] = w.cand_off[ci];
+                    w.slot_n[e - e0] = w.cand_n[ci];
+                }
                 w.slot_state[e - e0] = lake ? 1 : 0;
                 w.slot_touch_n[e - e0] = 0;
             }
@@ -422,7 +580,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
                     if (!w.slot_state[sl]) continue;
                     const unsigned long long key = claim_key(wave, w.events[e0 + sl]);
-                    const int* cells = w.slot_sorted + (size_t)sl * w.cap;
+                    const int* cells = w.pool_cells + w.slot_off[sl];
                     for (int i = lane; i < w.slot_n[sl]; i += 32) atomicMax(&w.claim[cells[i]], key);
                 }
                 if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
@@ -431,7 +589,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     if (!w.slot_state[sl]) continue;
                     const int rank = w.events[e0 + sl];
                     const unsigned long long key = claim_key(wave, rank);
-                    const int* cells = w.slot_sorted + (size_t)sl * w.cap;
+                    const int* cells = w.pool_cells + w.slot_off[sl];
                     bool held = true;
                     for (int i = lane; i < w.slot_n[sl]; i += 32) held &= __ldcg(&w.claim[cells[i]]) == key;
                     if (__all_sync(0xFFFFFFFFu, held)) {
@@ -635,30 +793,85 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.seg_events = d_seg;
     w.events = d_events;
     w.ev_touch = d_evtouch;
-    // The heap's capacity (DeltaFan.Scratch) and the lake-admission slots.
+    // The heap's capacity (DeltaFan.Scratch), the round's lake fans admitted ahead of the walk, and the
+    // chunks' mouth slots.
     w.cap = heap_capacity(w.p);
     w.box_words = box_words(w.p);
     w.slots = 2048;
     const size_t S = (size_t)w.slots, cap = (size_t)w.cap;
-    CG_BUF(int, d_shc, ctx, S_DEPSLOT0, S * cap);
-    CG_BUF(float, d_shk, ctx, S_DEPSLOT1, S * cap);
-    CG_BUF(float, d_shp, ctx, S_DEPSLOT2, S * cap);
-    CG_BUF(int, d_sad, ctx, S_DEPSLOT3, S * cap);
-    CG_BUF(int, d_sso, ctx, S_DEPSLOT4, S * cap);
-    CG_BUF(double, d_sba, ctx, S_DEPSLOT5, S * cap);
-    CG_BUF(uint32_t, d_sbits, ctx, S_DEPSLOT6, S * (size_t)w.box_words);
+    CG_BUF(int, d_candof, ctx, S_DEPCANDOF, N);
+    CG_BUF(int, d_cand, ctx, S_DEPCAND, (size_t)n + 2);
+    int* d_ncand = d_cand + n;
+    CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
+    CG_CUDA(ctx, cudaMemsetAsync(d_ncand, 0, sizeof(int), sm));
+    CG_LAUNCH(ctx) k_lake_candidates<<<grid, 256, 0, sm>>>(w.p, w.f, (int)N, d_cand, d_ncand, d_candof);
+    CG_CHECK_LAUNCH(ctx);
+    int ncand = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&ncand, d_ncand, sizeof(int), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    CG_BUF(int, d_candn, ctx, S_DEPCANDN, (size_t)ncand + 1);
+    CG_BUF(long long, d_candoff, ctx, S_DEPCANDOFF, (size_t)ncand + 1);
+    long long pool_total = 0;
+    int* d_pool_cells = nullptr;
+    double* d_pool_base = nullptr;
+    if (ncand > 0) {
+        AdmitDev a;
+        a.p = w.p;
+        a.f = w.f;
+        a.cap = w.cap;
+        a.box_words = w.box_words;
+        a.cand = d_cand;
+        a.ncand = ncand;
+        a.cand_n = d_candn;
+        a.cand_off = d_candoff;
+        a.err = d_words + W_ERROR;
+        const int threads = ctx->num_sms * 128;
+        const size_t T = (size_t)threads;
+        CG_BUF(int, d_hc, ctx, S_DEPSLOT0, T * cap);
+        CG_BUF(float, d_hk, ctx, S_DEPSLOT1, T * cap);
+        CG_BUF(float, d_hp, ctx, S_DEPSLOT2, T * cap);
+        CG_BUF(int, d_ha, ctx, S_DEPSLOT3, T * cap);
+        CG_BUF(uint32_t, d_hb, ctx, S_DEPSLOT6, T * (size_t)w.box_words);
+        a.h_cells = d_hc;
+        a.h_keys = d_hk;
+        a.h_pens = d_hp;
+        a.h_admitted = d_ha;
+        a.h_bits = d_hb;
+        a.pool_cells = nullptr;
+        a.pool_base = nullptr;
+        a.fill = 0;
+        CG_LAUNCH(ctx) k_admit_lakes<<<ctx->num_sms, 128, 0, sm>>>(a);
+        CG_CHECK_LAUNCH(ctx);
+        // Offsets: an exclusive scan of the counts in 64 bits.
+        CG_BUF(long long, d_wide, ctx, S_DEPCANDW, (size_t)ncand + 1);
+        CG_LAUNCH(ctx) k_widen_counts<<<(ncand + 255) / 256, 256, 0, sm>>>(d_candn, ncand, d_wide);
+        CG_CHECK_LAUNCH(ctx);
+        CG_LAUNCH(ctx) k_scan64_one_block<<<1, 1024, 0, sm>>>(d_wide, d_candoff, ncand);
+        CG_CHECK_LAUNCH(ctx);
+        CG_CUDA(ctx, cudaMemcpyAsync(&pool_total, d_candoff + ncand, sizeof(long long), cudaMemcpyDeviceToHost, sm));
+        CG_CUDA(ctx, cudaStreamSynchronize(sm));
+        CG_BUF(int, d_pc, ctx, S_DEPSLOT4, (size_t)pool_total + 1);
+        CG_BUF(double, d_pb, ctx, S_DEPSLOT5, (size_t)pool_total + 1);
+        d_pool_cells = d_pc;
+        d_pool_base = d_pb;
+        a.pool_cells = d_pc;
+        a.pool_base = d_pb;
+        a.fill = 1;
+        CG_LAUNCH(ctx) k_admit_lakes<<<ctx->num_sms, 128, 0, sm>>>(a);
+        CG_CHECK_LAUNCH(ctx);
+    }
+    w.cand_of = d_candof;
+    w.cand_n = d_candn;
+    w.cand_off = d_candoff;
+    w.pool_cells = d_pool_cells;
+    w.pool_base = d_pool_base;
+    CG_BUF(long long, d_soff, ctx, S_DEPSLOTOFF, S);
     CG_BUF(int, d_sn, ctx, S_DEPSLOT7, 2 * S);
     CG_BUF(double, d_slaid, ctx, S_DEPSLOT8, S);
     CG_BUF(Touch, d_stouch, ctx, S_DEPSLOT9, S * cap);
     CG_BUF(int, d_stn, ctx, S_DEPSLOT10, S);
     CG_BUF(unsigned long long, d_claim, ctx, S_DEPCLAIM, N);
-    w.slot_heap_cells = d_shc;
-    w.slot_heap_keys = d_shk;
-    w.slot_heap_pens = d_shp;
-    w.slot_admitted = d_sad;
-    w.slot_sorted = d_sso;
-    w.slot_base = d_sba;
-    w.slot_bits = d_sbits;
+    w.slot_off = d_soff;
     w.slot_n = d_sn;
     w.slot_state = d_sn + S;
     w.slot_laid = d_slaid;
@@ -676,11 +889,14 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_BUF(Touch, d_touch, ctx, S_DEPTOUCH, (size_t)w.touch_cap);
     w.touches = d_touch;
     CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
-    CG_BUF(int, d_replay, ctx, S_DEPREPLAY, N);
+    CG_BUF(int, d_replay, ctx, S_DEPREPLAY, 2 * N);
     w.mark = d_mark;
     w.replay = d_replay;
-    CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
+    w.refit = d_replay + N;
     w.words = d_words;
+    // The round's own counts (the fan ids, generations and wave numbers carry on through the stage).
+    for (int word : {W_REDONE, W_REPLAYED, W_WAVES, W_REFITTED})
+        CG_CUDA(ctx, cudaMemsetAsync(d_words + word, 0, sizeof(int), sm));
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "deposition kernel cannot be resident");
@@ -700,6 +916,7 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
         counts->redone = words[W_REDONE];
         counts->replayed = words[W_REPLAYED];
         counts->waves = words[W_WAVES];
+        counts->refitted = words[W_REFITTED];
     }
     return CG_OK;
 }

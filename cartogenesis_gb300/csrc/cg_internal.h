@@ -141,6 +141,7 @@ struct DepositCounts {
     int redone;     // levels restored and walked one cell after another
     int replayed;   // ponded cells whose settled height was replayed in rank order
     int waves;      // the lake fans' laying waves, over all levels (counted over the stage so far)
+    int refitted;   // dry cells whose own walk was taken again with their donors as the walk saw them
 };
 // The deposition walk of one round (HydraulicErosion.kt:1068-1349), the sediment in the stage's buffer.
 cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& p, const DepositRound& r, DepositCounts* counts);

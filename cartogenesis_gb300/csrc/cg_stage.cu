@@ -293,7 +293,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia,
                           d_incised_at));
         mark(5);
-        DepositCounts dc{0, 0, 0};
+        DepositCounts dc{0, 0, 0, 0};
         if (deposition) {
             DepositRound dr;
             dr.recv = d_recv;
@@ -378,6 +378,8 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             s.ms_relax = ms[7];
             s.deposit_replayed = dc.replayed;
             s.deposit_redone = dc.redone;
+            s.deposit_refitted = dc.refitted;
+            s.deposit_waves = dc.waves;
         }
     }
     if (run.next_round >= p.hydraulic_rounds) run.done = true;
