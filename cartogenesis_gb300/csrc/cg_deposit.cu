@@ -19,10 +19,14 @@
 //     laid), a lake fan's laying as a scan of its sorted cells.
 //  C. a fan changes only sea cells and ponded land, which no own walk reads, except (a) a ponded cell
 //     of the fan's own level ranked after it, whose settled height took its own subtraction before
-//     the fan's addition instead of after: its settled height is replayed in rank order; and (b) a
-//     donor whose settled height a later cell of the level read in its headroom: the level is then
-//     restored and walked one cell after another. Both are rare; the same schedule is shown on the
-//     host to give the reference walk's bits (tests/native/deposit_host.cpp).
+//     the fan's addition instead of after: its settled height is replayed in rank order, in one pass
+//     over the level's log of deposits; and (b) a donor whose settled height a later (dry) cell of the
+//     level read in its headroom. Such a cell's own walk is taken again with its donors as the
+//     reference's walk shows them at its rank. Nothing else of the level reads that cell, so where its
+//     step hands everything on the fix is local; where it has a mouth, its fan changes with it: every
+//     fan from its rank on is undone, the cell refitted, and those fans laid again, and the check
+//     repeats past it. Both are rare; the level schedule itself is shown on the host to give the
+//     reference walk's bits (tests/native/deposit_host.cpp).
 // Settle is elementwise, and the mouths pass reads only each cell's receiver, so it runs receivers
 // first, level by level from the top, like the incision.
 #include <algorithm>
@@ -46,8 +50,8 @@ constexpr int kThreads = 256;
 
 // Control words of a walk.
 enum {
-    W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REDONE = 4, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
-    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_WORDS = 16
+    W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
+    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_WORDS = 16
 };
 
 struct WalkDev {
@@ -97,6 +101,8 @@ struct WalkDev {
     int* mark;              // per cell: the generation that listed it for a replay
     int* replay;            // cells to replay
     int* refit;             // cells to refit
+    float* acc;             // per cell: a replayed settled height
+    uint8_t* own_done;      // per cell: the replay has taken the cell's own subtraction
     int* words;             // W_* control words
 };
 
@@ -138,23 +144,6 @@ __device__ bool mouth_live(const WalkDev& w, int c, double carried, int kind) {
 
 __device__ Heap thread_heap(const WalkDev& w) {
     return Heap{w.heap_cells, w.heap_keys, w.heap_pens, w.heap_admitted, w.cap, 0, 0};
-}
-
-// One cell's whole step the reference's way, for a level walked one cell after another.
-__device__ void walk_one(const WalkDev& w, int k) {
-    const int c = w.order[k];
-    double carried = arriving(w, c);
-    bool used;
-    double incised = 0.0, deposited = 0.0;
-    const int kind = own_walk(w.p, w.f, c, carried, &used, &incised, &deposited);
-    if (kind == ON) {
-        w.handoff[c] = carried;
-    } else if (kind == SEA || kind == LAKE) {
-        Heap h = thread_heap(w);
-        const int id = ++w.words[W_MOUTH_ID];
-        const double laid = mouth(w.p, w.f, c, carried, kind, w.stamp, id, h, nullptr);
-        if (kind == LAKE) w.handoff[c] = __dsub_rn(carried, laid);
-    }
 }
 
 // The round's lake mouths and their fans' admissions, ahead of the walk. A lake fan's admission (its
@@ -417,16 +406,79 @@ __device__ bool refit_cell(const WalkDev& w, int c, int n) {
     return true;
 }
 
-// Step C, on one thread: detect and make the repairs of the level [lo, hi) with events [0, n), whose
-// deposits are in the level's log in rank order. (a) a ponded cell of the level ranked after a fan
-// that laid into it has its settled height replayed in rank order; (b) a later cell of the level that
-// read, in its headroom, a donor such a fan raised is refitted (refit_cell), or, where it has a mouth
-// of its own, the level is restored and walked one cell after another.
-__device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int touch_n) {
+// The earliest cell of level L, ranked after a fan of the level that raised one of its donors, whose
+// headroom read that donor and which has a mouth of its own (its step ends at the sea or in a lake):
+// its own walk, and so its fan, are not the reference's. Cells refitted already (mark = refit_gen)
+// are final and skipped. Returns its rank, or -1.
+__device__ int earliest_mouth_conflict(const WalkDev& w, int L, int n, int refit_gen) {
+    int best = -1;
+    for (int e = 0; e < n; ++e) {
+        const int rank = w.events[e];
+        if (best >= 0 && rank >= best) break;   // a conflict needs a fan ranked before the cell
+        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
+            const int x = w.touches[t].cell;
+            if (!w.f.land[x]) continue;
+            const int rr = w.f.dirs[x];
+            if (rr < 0 || !w.f.land[rr] || level_of_cell(w, rr) != L) continue;
+            const int r = w.rank_of[rr];
+            if (r > rank && w.used[rr] && kind_of(w, rr) != ON && w.mark[rr] != refit_gen && (best < 0 || r < best))
+                best = r;
+        }
+    }
+    return best;
+}
+
+// Makes the walk the reference's again from rank rc (the earliest mouth conflict): every fan ranked
+// at or after rc undone, latest first, and the level's log cut back to before them; the conflicted
+// cell's own walk taken again on the state the reference's walk shows it (its own state before the
+// walk, and its donors as every fan ranked before it left them, which is now the current state); its
+// mouth listed or unlisted as its new load decides. Returns the index of the first event to lay
+// again; *n and *touch_n are updated.
+__device__ int refit_mouth_cell(const WalkDev& w, int rc, int refit_gen, int* n, int* touch_n) {
+    int ec = 0;
+    while (ec < *n && w.events[ec] < rc) ++ec;
+    const int cut = ec < *n ? w.ev_touch[ec] : *touch_n;
+    for (int t = *touch_n - 1; t >= cut; --t) {
+        w.f.settled[w.touches[t].cell] = w.touches[t].settled_before;
+        w.f.sediment[w.touches[t].cell] = w.touches[t].sediment_before;
+    }
+    *touch_n = cut;
+    const int c = w.order[rc];
+    w.f.settled[c] = w.s0[rc];
+    w.f.sediment[c] = w.d0[rc];
+    double carried = arriving(w, c);
+    bool used;
+    double incised = 0.0, deposited = 0.0;
+    const int kind = own_walk(w.p, w.f, c, carried, &used, &incised, &deposited);
+    w.used[c] = used ? 1 : 0;
+    if (kind == LAKE) w.handoff[c] = carried;
+    w.mark[c] = refit_gen;
+    const bool listed = ec < *n && w.events[ec] == rc;
+    const bool live = (kind == SEA || kind == LAKE) && mouth_live(w, c, carried, kind);
+    if (live) {
+        w.ev_carried[rc] = carried;
+        w.ev_kind[rc] = (int8_t)kind;
+        if (!listed) {
+            for (int e = *n; e > ec; --e) w.events[e] = w.events[e - 1];
+            w.events[ec] = rc;
+            ++*n;
+        }
+    } else if (listed) {
+        for (int e = ec; e + 1 < *n; ++e) w.events[e] = w.events[e + 1];
+        --*n;
+    }
+    return ec;
+}
+
+// The last repairs of level L ([lo, hi)), with its final log of n events, on one thread:
+// (b) a dry cell whose step hands everything on (kind ON) and whose headroom read a donor an earlier
+// fan of the level raised is refitted with its donors as the reference's walk showed them; (a) a
+// ponded cell of the level ranked after a fan that laid into it has its settled height replayed, its
+// own subtraction and the fans' increments in rank order, in one pass over the log.
+__device__ void final_repairs(const WalkDev& w, int L, int n, int touch_n) {
     w.ev_touch[n] = touch_n;
-    bool redo = false;
-    int replays = 0, refits = 0;
     const int gen = ++w.words[W_GEN];
+    int replays = 0, refits = 0;
     for (int e = 0; e < n; ++e) {
         const int rank = w.events[e];
         for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
@@ -435,56 +487,42 @@ __device__ void repair_level(const WalkDev& w, int L, int lo, int hi, int n, int
             if (level_of_cell(w, x) == L && w.rank_of[x] > rank && w.mark[x] != gen) {
                 w.mark[x] = gen;
                 w.replay[replays++] = x;
+                w.acc[x] = w.s0[w.rank_of[x]];
+                w.own_done[x] = 0;
             }
             const int rr = w.f.dirs[x];
             if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr] &&
-                w.mark[rr] != -gen) {
+                kind_of(w, rr) == ON && w.mark[rr] != -gen) {
                 w.mark[rr] = -gen;   // a dry cell: never a replay's (those are ponded)
-                if (kind_of(w, rr) != ON) redo = true;
                 w.refit[refits++] = rr;
             }
         }
-    }
-    if (redo) {
-        w.words[W_REDONE]++;
-        for (int t = touch_n - 1; t >= 0; --t) {
-            w.f.settled[w.touches[t].cell] = w.touches[t].settled_before;
-            w.f.sediment[w.touches[t].cell] = w.touches[t].sediment_before;
-        }
-        for (int k = lo; k < hi; ++k) {
-            w.f.settled[w.order[k]] = w.s0[k];
-            w.f.sediment[w.order[k]] = w.d0[k];
-        }
-        for (int k = lo; k < hi; ++k) walk_one(w, k);
-        return;
     }
     for (int i = 0; i < refits; ++i) {
         refit_cell(w, w.refit[i], n);
         w.words[W_REFITTED]++;
     }
-    for (int i = 0; i < replays; ++i) {
-        // The cell's own subtraction and the fans' increments, in rank order.
-        const int x = w.replay[i];
-        const int rx = w.rank_of[x];
-        float v = w.s0[rx];
-        bool own_done = false;
-        for (int e = 0; e < n; ++e) {
-            const int rank = w.events[e];
-            for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
-                if (w.touches[t].cell != x) continue;
-                if (!own_done && rank > rx) {
-                    const double moved = w.f.incised_at[x];
-                    if (moved > 0.0) v -= (float)(moved * (double)w.p.to_relative);
-                    own_done = true;
-                }
-                v += w.touches[t].increment;
+    if (replays == 0) return;
+    for (int e = 0; e < n; ++e) {
+        const int rank = w.events[e];
+        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
+            const int x = w.touches[t].cell;
+            if (!w.f.land[x] || w.mark[x] != gen) continue;
+            if (!w.own_done[x] && rank > w.rank_of[x]) {
+                const double moved = w.f.incised_at[x];
+                if (moved > 0.0) w.acc[x] -= (float)(moved * (double)w.p.to_relative);
+                w.own_done[x] = 1;
             }
+            w.acc[x] += w.touches[t].increment;
         }
-        if (!own_done) {
+    }
+    for (int i = 0; i < replays; ++i) {
+        const int x = w.replay[i];
+        if (!w.own_done[x]) {
             const double moved = w.f.incised_at[x];
-            if (moved > 0.0) v -= (float)(moved * (double)w.p.to_relative);
+            if (moved > 0.0) w.acc[x] -= (float)(moved * (double)w.p.to_relative);
         }
-        w.f.settled[x] = v;
+        w.f.settled[x] = w.acc[x];
         w.words[W_REPLAYED]++;
     }
 }
@@ -552,73 +590,102 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         const int lane = threadIdx.x & 31;
         const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
         const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-        int touch_n = 0;
-        // B in chunks of `slots` mouths, in rank order.
-        for (int e0 = 0; e0 < n; e0 += w.slots) {
-            const int e1 = min(n, e0 + w.slots);
-            // The chunk's lake fans, their admissions taken from the round's pool.
-            for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1; e += (int)(gridDim.x * blockDim.x)) {
-                const int k = w.events[e];
-                const bool lake = w.ev_kind[k] == LAKE;
-                if (lake) {
-                    const int ci = w.cand_of[w.order[k]];
-                    w.slot_off[e - e0] = w.cand_off[ci];
-                    w.slot_n[e - e0] = w.cand_n[ci];
+        int touch_n = 0;   // the level's log length (kept by the one thread that writes the log)
+        int n_now = n, e_start = 0;
+        int refit_gen = 0;   // thread 0's mark for the level's refitted mouth cells (a fresh generation)
+        // B, and C's mouth conflicts: lay the events from e_start in rank order (chunks of `slots`); then
+        // if a cell with a mouth read a donor an earlier fan raised, make the walk the reference's again
+        // from that cell (refit_mouth_cell) and lay what follows it again. Each pass moves past at least
+        // one such cell, so there are at most as many passes as the level has cells, and one more.
+        const int passes = hi - lo + 1;
+        for (int pass = 0; pass <= passes; ++pass) {
+            for (int e0 = e_start; e0 < n_now; e0 += w.slots) {
+                const int e1 = min(n_now, e0 + w.slots);
+                // The chunk's lake fans, their admissions taken from the round's pool.
+                for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1;
+                     e += (int)(gridDim.x * blockDim.x)) {
+                    const int k = w.events[e];
+                    const bool lake = w.ev_kind[k] == LAKE;
+                    if (lake) {
+                        const int ci = w.cand_of[w.order[k]];
+                        w.slot_off[e - e0] = w.cand_off[ci];
+                        w.slot_n[e - e0] = w.cand_n[ci];
+                    }
+                    w.slot_state[e - e0] = lake ? 1 : 0;
+                    w.slot_touch_n[e - e0] = 0;
                 }
-                w.slot_state[e - e0] = lake ? 1 : 0;
-                w.slot_touch_n[e - e0] = 0;
+                grid.sync();
+                // The lake fans lay in waves, a warp each: a fan lays once no earlier waiting fan
+                // admitted any of its cells (its claims all hold), so overlapping fans lay in rank order
+                // and disjoint ones at once (their layings touch different cells). Bounded: the lowest
+                // waiting rank always holds its claims, so every wave lays at least one fan.
+                const unsigned wave0 = (unsigned)*(volatile int*)&w.words[W_WAVEBASE];
+                unsigned wave = wave0;
+                for (int guard = 0; guard <= e1 - e0; ++guard) {
+                    const int par = (int)(wave & 1u);
+                    for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
+                        if (!w.slot_state[sl]) continue;
+                        const unsigned long long key = claim_key(wave, w.events[e0 + sl]);
+                        const int* cells = w.pool_cells + w.slot_off[sl];
+                        for (int i = lane; i < w.slot_n[sl]; i += 32) atomicMax(&w.claim[cells[i]], key);
+                    }
+                    if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
+                    grid.sync();
+                    for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
+                        if (!w.slot_state[sl]) continue;
+                        const int rank = w.events[e0 + sl];
+                        const unsigned long long key = claim_key(wave, rank);
+                        const int* cells = w.pool_cells + w.slot_off[sl];
+                        bool held = true;
+                        for (int i = lane; i < w.slot_n[sl]; i += 32) held &= __ldcg(&w.claim[cells[i]]) == key;
+                        if (__all_sync(0xFFFFFFFFu, held)) {
+                            const int c = w.order[rank];
+                            const double carried = w.ev_carried[rank];
+                            lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
+                            if (lane == 0) {
+                                w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
+                                w.slot_state[sl] = 0;
+                            }
+                        } else if (lane == 0) {
+                            atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
+                        }
+                    }
+                    grid.sync();
+                    ++wave;
+                    if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
+                    if (guard == e1 - e0 && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
+                }
+                // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    w.words[W_WAVEBASE] = (int)wave;
+                    w.words[W_WAVES] += (int)(wave - wave0);
+                    log_and_run_seas(w, e0, e1, &touch_n);
+                }
+                grid.sync();
+            }
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                w.ev_touch[n_now] = touch_n;
+                if (pass == 0) refit_gen = ++w.words[W_GEN];
+                const int rc = earliest_mouth_conflict(w, L, n_now, refit_gen);
+                if (rc < 0) {
+                    w.words[W_DONE] = 1;
+                } else {
+                    if (pass == passes) w.words[W_ERROR] |= 8;
+                    int nn = n_now;
+                    w.words[W_ESTART] = refit_mouth_cell(w, rc, refit_gen, &nn, &touch_n);
+                    w.words[W_EVENTS] = nn;
+                    w.words[W_DONE] = 0;
+                    w.words[W_RELAID]++;
+                }
             }
             grid.sync();
-            // The lake fans lay in waves, a warp each: a fan lays once no earlier waiting fan admitted
-            // any of its cells (its claims all hold), so overlapping fans lay in rank order and
-            // disjoint ones at once (their layings touch different cells). Bounded: the lowest waiting
-            // rank always holds its claims, so every wave lays at least one fan.
-            const unsigned wave0 = (unsigned)*(volatile int*)&w.words[W_WAVEBASE];
-            unsigned wave = wave0;
-            for (int guard = 0; guard <= e1 - e0; ++guard) {
-                const int par = (int)(wave & 1u);
-                for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
-                    if (!w.slot_state[sl]) continue;
-                    const unsigned long long key = claim_key(wave, w.events[e0 + sl]);
-                    const int* cells = w.pool_cells + w.slot_off[sl];
-                    for (int i = lane; i < w.slot_n[sl]; i += 32) atomicMax(&w.claim[cells[i]], key);
-                }
-                if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
-                grid.sync();
-                for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
-                    if (!w.slot_state[sl]) continue;
-                    const int rank = w.events[e0 + sl];
-                    const unsigned long long key = claim_key(wave, rank);
-                    const int* cells = w.pool_cells + w.slot_off[sl];
-                    bool held = true;
-                    for (int i = lane; i < w.slot_n[sl]; i += 32) held &= __ldcg(&w.claim[cells[i]]) == key;
-                    if (__all_sync(0xFFFFFFFFu, held)) {
-                        const int c = w.order[rank];
-                        const double carried = w.ev_carried[rank];
-                        lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
-                        if (lane == 0) {
-                            w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
-                            w.slot_state[sl] = 0;
-                        }
-                    } else if (lane == 0) {
-                        atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
-                    }
-                }
-                grid.sync();
-                ++wave;
-                if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
-                if (guard == e1 - e0 && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
-            }
-            // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                w.words[W_WAVEBASE] = (int)wave;
-                w.words[W_WAVES] += (int)(wave - wave0);
-                log_and_run_seas(w, e0, e1, &touch_n);
-            }
+            if (*(volatile int*)&w.words[W_DONE]) break;
+            e_start = *(volatile int*)&w.words[W_ESTART];
+            n_now = *(volatile int*)&w.words[W_EVENTS];
             grid.sync();
         }
-        // C: the repairs, with every deposit of the level in its log.
-        if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) repair_level(w, L, lo, hi, n, touch_n);
+        // C: the last repairs, with every deposit of the level in its log.
+        if (blockIdx.x == 0 && threadIdx.x == 0 && n_now > 0) final_repairs(w, L, n_now, touch_n);
         grid.sync();
     }
 }
@@ -893,9 +960,13 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.mark = d_mark;
     w.replay = d_replay;
     w.refit = d_replay + N;
+    CG_BUF(float, d_acc, ctx, S_DEPACC, N);
+    CG_BUF(uint8_t, d_own, ctx, S_DEPOWN, N);
+    w.acc = d_acc;
+    w.own_done = d_own;
     w.words = d_words;
     // The round's own counts (the fan ids, generations and wave numbers carry on through the stage).
-    for (int word : {W_REDONE, W_REPLAYED, W_WAVES, W_REFITTED})
+    for (int word : {W_REPLAYED, W_WAVES, W_REFITTED, W_RELAID})
         CG_CUDA(ctx, cudaMemsetAsync(d_words + word, 0, sizeof(int), sm));
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
@@ -912,11 +983,12 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     if (words[W_ERROR] & 1) return fail(ctx, CG_INEXACT, "deposition: a level's fan deposits overflowed the repair log");
     if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
     if (words[W_ERROR] & 4) return fail(ctx, CG_INEXACT, "deposition: the lake fans' laying waves did not converge");
+    if (words[W_ERROR] & 8) return fail(ctx, CG_INEXACT, "deposition: a level's mouth refits did not converge");
     if (counts) {
-        counts->redone = words[W_REDONE];
         counts->replayed = words[W_REPLAYED];
         counts->waves = words[W_WAVES];
         counts->refitted = words[W_REFITTED];
+        counts->redone = words[W_RELAID];
     }
     return CG_OK;
 }

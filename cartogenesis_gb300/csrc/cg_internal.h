@@ -138,7 +138,7 @@ struct DepositRound {
     const double* incised_at;
 };
 struct DepositCounts {
-    int redone;     // levels restored and walked one cell after another
+    int redone;     // cells with a mouth refitted, the later fans of their level laid again
     int replayed;   // ponded cells whose settled height was replayed in rank order
     int waves;      // the lake fans' laying waves, over all levels (counted over the stage so far)
     int refitted;   // dry cells whose own walk was taken again with their donors as the walk saw them

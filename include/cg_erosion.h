@@ -170,7 +170,7 @@ typedef struct cg_round_stats {
     double  ms_deposit;         /* P2's deposition walk and, in the last round, settle, the closing
                                    breach (P1, P2: its cut, fill, routing and notch) and the mouths pass */
     int32_t deposit_replayed;   /* P2: ponded cells whose settled height the level schedule replayed */
-    int32_t deposit_redone;     /* P2: levels the schedule restored and walked one cell after another */
+    int32_t deposit_redone;     /* P2: cells with a mouth refitted, the later fans of their level laid again */
     int32_t deposit_refitted;   /* P2: dry cells whose own walk was taken again with their donors as
                                    the reference's walk showed them */
     int32_t deposit_waves;      /* P2: the lake fans' laying waves over the round's levels */
