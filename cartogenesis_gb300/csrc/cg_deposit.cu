@@ -51,7 +51,7 @@ constexpr int kThreads = 256;
 // Control words of a walk.
 enum {
     W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
-    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_WORDS = 16
+    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15, W_WORDS = 16
 };
 
 struct WalkDev {
@@ -87,7 +87,20 @@ struct WalkDev {
     double* slot_laid;      // per slot: what its fan laid
     Touch* slot_touch;      // per slot: its fan's deposits, `cap` entries
     int* slot_touch_n;
-    unsigned long long* claim;   // per cell: the (wave, rank) of the fan holding it
+    // A chunk's laying schedule: each (fan, admitted cell) pair, grouped by cell, knows the fan that
+    // follows it on that cell in rank order; a fan lays once every fan before it on its cells has.
+    int pair_cap;
+    int* poff;              // per slot + 1: its first pair
+    int* pair_fan;          // per pair: its slot
+    int* pair_cell;
+    int* pair_pos;          // per pair: its place in its cell's group (arrival order)
+    int* pair_succ;         // per pair: the slot of the next fan on its cell, or -1
+    int* group;             // pairs grouped by cell
+    int* dcell;             // the chunk's distinct cells
+    int* doff;              // per distinct cell + 1: its group's first entry
+    int* cell_cnt;          // per cell: pairs on it (0 outside a chunk's scheduling)
+    int* cell_d;            // per cell: its distinct index (valid for the chunk's cells)
+    int* blockers;          // per slot: earlier fans still to lay on its cells
     // The sequential thread's heap (sea lobes, a redone level).
     int* heap_cells;
     float* heap_keys;
@@ -261,10 +274,29 @@ __global__ void k_widen_counts(const int* __restrict__ n, int count, long long* 
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) out[i] = n[i];
 }
 
-// A claim on a cell for a fan of rank `rank` in wave `wave`: later waves outrank earlier ones, and in
-// a wave the lowest rank holds the cell.
-__device__ __forceinline__ unsigned long long claim_key(unsigned wave, int rank) {
-    return ((unsigned long long)wave << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)rank);
+// An exclusive prefix sum by one CTA (every thread of it calls this), chunk after chunk; out[n]
+// receives the total. get(i) gives element i.
+template <class Get>
+__device__ void cta_exclusive_scan(Get get, int n, int* __restrict__ out, int* __restrict__ sh) {
+    int carry = 0;
+    for (int base = 0; base < n; base += kThreads) {
+        const int i = base + (int)threadIdx.x;
+        const int v = i < n ? get(i) : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kThreads; o <<= 1) {
+            const int t = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n) out[i] = carry + sh[threadIdx.x] - v;
+        const int chunk = sh[kThreads - 1];
+        __syncthreads();
+        carry += chunk;
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+    __syncthreads();
 }
 
 // A lake fan's laying by one warp (lay_admitted's loop over the distance-sorted admitted cells). A
@@ -285,7 +317,7 @@ __device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) 
         double need = 0.0;
         if (i < n) {
             x = sorted[i];
-            need = __dsub_rn(base[i], (double)w.f.sediment[x]);
+            need = __dsub_rn(base[i], (double)__ldcg(&w.f.sediment[x]));
         }
         unsigned live = __ballot_sync(FULL, i < n && need > 0.0);
         while (live && remaining > 0.0) {
@@ -293,11 +325,15 @@ __device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) 
             live &= live - 1;
             double moved = 0.0;
             if (lane == j) {
-                log[logged] = Touch{x, w.f.settled[x], w.f.sediment[x], 0.0f};
-                moved = raise(w.f.sediment, x, need < remaining ? need : remaining);
+                // HydraulicErosion.raise and the settled height's rise, through L2: an earlier fan on
+                // this cell may have laid on another SM in this same wave.
+                const float prior = __ldcg(&w.f.sediment[x]), settled = __ldcg(&w.f.settled[x]);
+                const float now = (float)((double)prior + (need < remaining ? need : remaining));
+                __stcg(&w.f.sediment[x], now);
+                moved = (double)now - (double)prior;
                 const float increment = (float)(moved * (double)w.p.to_relative);
-                w.f.settled[x] += increment;
-                log[logged].increment = increment;
+                __stcg(&w.f.settled[x], settled + increment);
+                log[logged] = Touch{x, settled, prior, increment};
             }
             moved = __shfl_sync(FULL, moved, j);
             ++logged;
@@ -531,6 +567,7 @@ __device__ void final_repairs(const WalkDev& w, int L, int n, int touch_n) {
 __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
     cgr::grid_group grid = cgr::this_grid();
     __shared__ int warp_counts[kThreads / 32];
+    __shared__ int sh_scan[kThreads];
     __shared__ int block_base;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int L = 0; L < w.levels; ++L) {
@@ -613,52 +650,106 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     }
                     w.slot_state[e - e0] = lake ? 1 : 0;
                     w.slot_touch_n[e - e0] = 0;
+                    w.blockers[e - e0] = 0;
                 }
                 grid.sync();
-                // The lake fans lay in waves, a warp each: a fan lays once no earlier waiting fan
-                // admitted any of its cells (its claims all hold), so overlapping fans lay in rank order
-                // and disjoint ones at once (their layings touch different cells). Bounded: the lowest
-                // waiting rank always holds its claims, so every wave lays at least one fan.
-                const unsigned wave0 = (unsigned)*(volatile int*)&w.words[W_WAVEBASE];
-                unsigned wave = wave0;
-                for (int guard = 0; guard <= e1 - e0; ++guard) {
-                    const int par = (int)(wave & 1u);
-                    for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
-                        if (!w.slot_state[sl]) continue;
-                        const unsigned long long key = claim_key(wave, w.events[e0 + sl]);
-                        const int* cells = w.pool_cells + w.slot_off[sl];
-                        for (int i = lane; i < w.slot_n[sl]; i += 32) atomicMax(&w.claim[cells[i]], key);
+                // The lake fans lay in waves, a warp each, in rank order wherever they share a cell: the
+                // chunk's (fan, cell) pairs are grouped by cell, each pair learning whether an earlier
+                // fan is on its cell (the fan's blocker count) and which fan follows it there. A fan lays
+                // once its count is 0 and then releases its followers; disjoint fans lay at once (their
+                // layings touch different cells). Bounded: the lowest waiting rank is never blocked, so
+                // every wave lays at least one fan.
+                const int S = e1 - e0;
+                if (blockIdx.x == 0) {
+                    cta_exclusive_scan([&](int i) { return w.slot_state[i] ? w.slot_n[i] : 0; }, S, w.poff, sh_scan);
+                    if (threadIdx.x == 0) {
+                        w.words[W_PAIRS] = w.poff[S];
+                        w.words[W_DISTINCT] = 0;
+                        if (w.poff[S] > w.pair_cap) w.words[W_ERROR] |= 16;
                     }
+                }
+                grid.sync();
+                const int P = min(*(volatile int*)&w.words[W_PAIRS], w.pair_cap);
+                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x)) {
+                    int a = 0, b = S;   // the slot whose pairs hold q: poff[a] <= q < poff[a + 1]
+                    while (b - a > 1) {
+                        const int m = (a + b) >> 1;
+                        if (w.poff[m] <= q) a = m;
+                        else b = m;
+                    }
+                    const int x = w.pool_cells[w.slot_off[a] + (q - w.poff[a])];
+                    w.pair_fan[q] = a;
+                    w.pair_cell[q] = x;
+                    const int pos = atomicAdd(&w.cell_cnt[x], 1);
+                    w.pair_pos[q] = pos;
+                    if (pos == 0) {
+                        const int d = atomicAdd(&w.words[W_DISTINCT], 1);
+                        w.dcell[d] = x;
+                        w.cell_d[x] = d;
+                    }
+                }
+                grid.sync();
+                const int D = *(volatile int*)&w.words[W_DISTINCT];
+                if (blockIdx.x == 0) cta_exclusive_scan([&](int i) { return __ldcg(&w.cell_cnt[w.dcell[i]]); }, D, w.doff, sh_scan);
+                grid.sync();
+                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x))
+                    w.group[w.doff[w.cell_d[w.pair_cell[q]]] + w.pair_pos[q]] = q;
+                grid.sync();
+                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x)) {
+                    const int x = w.pair_cell[q];
+                    const int* g = w.group + w.doff[w.cell_d[x]];
+                    const int m = __ldcg(&w.cell_cnt[x]);
+                    const int r = w.events[e0 + w.pair_fan[q]];
+                    bool pred = false;
+                    int succ = -1, rs = 0;
+                    for (int j = 0; j < m; ++j) {
+                        const int f = w.pair_fan[g[j]];
+                        const int rf = w.events[e0 + f];
+                        if (rf < r) pred = true;
+                        else if (rf > r && (succ < 0 || rf < rs)) {
+                            succ = f;
+                            rs = rf;
+                        }
+                    }
+                    w.pair_succ[q] = succ;
+                    if (pred) atomicAdd(&w.blockers[w.pair_fan[q]], 1);
+                }
+                grid.sync();
+                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x))
+                    w.cell_cnt[w.pair_cell[q]] = 0;   // every cell's count back to 0 for the next chunk
+                int waves = 0;
+                for (int guard = 0; guard <= S; ++guard) {
+                    const int par = guard & 1;
                     if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
                     grid.sync();
-                    for (int sl = gwarp; sl < e1 - e0; sl += nwarps) {
+                    for (int sl = gwarp; sl < S; sl += nwarps) {
                         if (!w.slot_state[sl]) continue;
+                        if (*(volatile int*)&w.blockers[sl] != 0) {
+                            if (lane == 0) atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
+                            continue;
+                        }
+                        __threadfence();
                         const int rank = w.events[e0 + sl];
-                        const unsigned long long key = claim_key(wave, rank);
-                        const int* cells = w.pool_cells + w.slot_off[sl];
-                        bool held = true;
-                        for (int i = lane; i < w.slot_n[sl]; i += 32) held &= __ldcg(&w.claim[cells[i]]) == key;
-                        if (__all_sync(0xFFFFFFFFu, held)) {
-                            const int c = w.order[rank];
-                            const double carried = w.ev_carried[rank];
-                            lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
-                            if (lane == 0) {
-                                w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
-                                w.slot_state[sl] = 0;
-                            }
-                        } else if (lane == 0) {
-                            atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
+                        const int c = w.order[rank];
+                        const double carried = w.ev_carried[rank];
+                        lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
+                        __syncwarp();
+                        __threadfence();
+                        for (int q = w.poff[sl] + lane; q < w.poff[sl + 1]; q += 32)
+                            if (w.pair_succ[q] >= 0) atomicSub(&w.blockers[w.pair_succ[q]], 1);
+                        if (lane == 0) {
+                            w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
+                            w.slot_state[sl] = 0;
                         }
                     }
                     grid.sync();
-                    ++wave;
+                    ++waves;
                     if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
-                    if (guard == e1 - e0 && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
+                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
                 }
                 // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
-                    w.words[W_WAVEBASE] = (int)wave;
-                    w.words[W_WAVES] += (int)(wave - wave0);
+                    w.words[W_WAVES] += waves;
                     log_and_run_seas(w, e0, e1, &touch_n);
                 }
                 grid.sync();
@@ -789,14 +880,15 @@ cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
     CG_BUF(int, d_stamp, ctx, S_STAMP, N);
     CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
-    CG_BUF(unsigned long long, d_claim, ctx, S_DEPCLAIM, N);
+    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * N);
     CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
     CG_LAUNCH(ctx) k_zero_float<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_sediment, N);
     CG_CHECK_LAUNCH(ctx);
-    // Fan ids, replay generations and laying waves restart at 0, so every stamp, mark and claim must too.
+    // Fan ids and replay generations restart at 0, so every stamp and mark must too; the laying
+    // schedule's per-cell counts start at 0 (each chunk leaves them at 0).
     CG_CUDA(ctx, cudaMemsetAsync(d_stamp, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), ctx->stream));
-    CG_CUDA(ctx, cudaMemsetAsync(d_claim, 0, N * sizeof(unsigned long long), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_cellcnt, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_words, 0, W_WORDS * sizeof(int), ctx->stream));
     return CG_OK;
 }
@@ -937,14 +1029,27 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_BUF(double, d_slaid, ctx, S_DEPSLOT8, S);
     CG_BUF(Touch, d_stouch, ctx, S_DEPSLOT9, S * cap);
     CG_BUF(int, d_stn, ctx, S_DEPSLOT10, S);
-    CG_BUF(unsigned long long, d_claim, ctx, S_DEPCLAIM, N);
+    w.pair_cap = (int)std::min<size_t>(S * cap, (size_t)1 << 30);
+    const size_t PC = (size_t)w.pair_cap;
+    CG_BUF(int, d_sched, ctx, S_DEPCLAIM, 6 * PC + 2 * S + 4);
+    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * N);
+    w.poff = d_sched;
+    w.blockers = d_sched + S + 1;
+    w.pair_fan = w.blockers + S + 1;
+    w.pair_cell = w.pair_fan + PC;
+    w.pair_pos = w.pair_cell + PC;
+    w.pair_succ = w.pair_pos + PC;
+    w.group = w.pair_succ + PC;
+    w.dcell = w.group + PC;
+    w.doff = w.dcell + PC;
+    w.cell_cnt = d_cellcnt;
+    w.cell_d = d_cellcnt + N;
     w.slot_off = d_soff;
     w.slot_n = d_sn;
     w.slot_state = d_sn + S;
     w.slot_laid = d_slaid;
     w.slot_touch = d_stouch;
     w.slot_touch_n = d_stn;
-    w.claim = d_claim;
     CG_BUF(int, d_hc, ctx, S_DEPHEAP, 4 * cap);
     w.heap_cells = d_hc;
     w.heap_keys = (float*)(d_hc + cap);
@@ -984,6 +1089,7 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
     if (words[W_ERROR] & 4) return fail(ctx, CG_INEXACT, "deposition: the lake fans' laying waves did not converge");
     if (words[W_ERROR] & 8) return fail(ctx, CG_INEXACT, "deposition: a level's mouth refits did not converge");
+    if (words[W_ERROR] & 16) return fail(ctx, CG_INEXACT, "deposition: a chunk's fan cells overflowed the schedule");
     if (counts) {
         counts->replayed = words[W_REPLAYED];
         counts->waves = words[W_WAVES];
