@@ -661,7 +661,9 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 // every wave lays at least one fan.
                 const int S = e1 - e0;
                 if (blockIdx.x == 0) {
-                    cta_exclusive_scan([&](int i) { return w.slot_state[i] ? w.slot_n[i] : 0; }, S, w.poff, sh_scan);
+                    const int* st = w.slot_state;
+                    const int* sn = w.slot_n;
+                    cta_exclusive_scan([=](int i) { return st[i] ? sn[i] : 0; }, S, w.poff, sh_scan);
                     if (threadIdx.x == 0) {
                         w.words[W_PAIRS] = w.poff[S];
                         w.words[W_DISTINCT] = 0;
@@ -690,7 +692,11 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 }
                 grid.sync();
                 const int D = *(volatile int*)&w.words[W_DISTINCT];
-                if (blockIdx.x == 0) cta_exclusive_scan([&](int i) { return __ldcg(&w.cell_cnt[w.dcell[i]]); }, D, w.doff, sh_scan);
+                if (blockIdx.x == 0) {
+                    const int* cnt = w.cell_cnt;
+                    const int* dc = w.dcell;
+                    cta_exclusive_scan([=](int i) { return __ldcg(&cnt[dc[i]]); }, D, w.doff, sh_scan);
+                }
                 grid.sync();
                 for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x))
                     w.group[w.doff[w.cell_d[w.pair_cell[q]]] + w.pair_pos[q]] = q;
@@ -735,7 +741,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                         lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
                         __syncwarp();
                         __threadfence();
-                        for (int q = w.poff[sl] + lane; q < w.poff[sl + 1]; q += 32)
+                        for (int q = w.poff[sl] + lane; q < min(w.poff[sl + 1], P); q += 32)   // P: past an overflow
                             if (w.pair_succ[q] >= 0) atomicSub(&w.blockers[w.pair_succ[q]], 1);
                         if (lane == 0) {
                             w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
@@ -1031,7 +1037,9 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_BUF(int, d_stn, ctx, S_DEPSLOT10, S);
     w.pair_cap = (int)std::min<size_t>(S * cap, (size_t)1 << 30);
     const size_t PC = (size_t)w.pair_cap;
-    CG_BUF(int, d_sched, ctx, S_DEPCLAIM, 6 * PC + 2 * S + 4);
+    // poff (S + 1), blockers (S + 1), then seven arrays of PC: pair_fan, pair_cell, pair_pos,
+    // pair_succ, group, dcell, and doff (its D + 1 <= PC + 1 entries run into the spare 2).
+    CG_BUF(int, d_sched, ctx, S_DEPCLAIM, 7 * PC + 2 * S + 4);
     CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * N);
     w.poff = d_sched;
     w.blockers = d_sched + S + 1;
