@@ -51,7 +51,8 @@ constexpr int kThreads = 256;
 // Control words of a walk.
 enum {
     W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
-    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15, W_WORDS = 16
+    W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15,
+    W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18, W_WORDS = 20
 };
 
 struct WalkDev {
@@ -79,6 +80,8 @@ struct WalkDev {
     const long long* cand_off;   // per candidate: first pool entry
     const int* pool_cells;
     const double* pool_base;
+    int ncand;
+    long long pool_total;
     // The mouths of a chunk, `slots` of them at a time.
     int slots, cap, box_words;
     long long* slot_off;    // per slot: its fan's first pool entry
@@ -275,9 +278,11 @@ __global__ void k_widen_counts(const int* __restrict__ n, int count, long long* 
 }
 
 // An exclusive prefix sum by one CTA (every thread of it calls this), chunk after chunk; out[n]
-// receives the total. get(i) gives element i.
+// receives the total. get(i) gives element i. sh is the CTA's shared scratch: no __restrict__ on it,
+// which would let the compiler keep a thread's own sh entry in a register across the barriers that
+// publish it to the other threads.
 template <class Get>
-__device__ void cta_exclusive_scan(Get get, int n, int* __restrict__ out, int* __restrict__ sh) {
+__device__ void cta_exclusive_scan(Get get, int n, int* out, int* sh) {
     int carry = 0;
     for (int base = 0; base < n; base += kThreads) {
         const int i = base + (int)threadIdx.x;
@@ -299,6 +304,21 @@ __device__ void cta_exclusive_scan(Get get, int n, int* __restrict__ out, int* _
     __syncthreads();
 }
 
+// An index check of the laying schedule: v must lie in [0, hi). A failure records its site, value and
+// bound (the first one only), raises error bit 32, and the caller skips the access.
+__device__ __noinline__ void check_failed(const WalkDev& w, long long v, long long hi, int site) {
+    if (atomicCAS(&w.words[W_CHECK_SITE], 0, site) == 0) {
+        w.words[W_CHECK_VALUE] = (int)v;
+        w.words[W_CHECK_BOUND] = (int)hi;
+    }
+    atomicOr(&w.words[W_ERROR], 32);
+}
+__device__ __forceinline__ bool index_ok(const WalkDev& w, long long v, long long hi, int site) {
+    if (v >= 0 && v < hi) return true;
+    check_failed(w, v, hi, site);
+    return false;
+}
+
 // A lake fan's laying by one warp (lay_admitted's loop over the distance-sorted admitted cells). A
 // fan's cells are distinct, so laying into one changes no other's need: the warp reads 32 needs at
 // once and lays into the ones above zero one after another, in order, while the budget lasts. The
@@ -317,7 +337,7 @@ __device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) 
         double need = 0.0;
         if (i < n) {
             x = sorted[i];
-            need = __dsub_rn(base[i], (double)__ldcg(&w.f.sediment[x]));
+            if (index_ok(w, x, (long long)w.p.W * w.p.H, 9)) need = __dsub_rn(base[i], (double)__ldcg(&w.f.sediment[x]));
         }
         unsigned live = __ballot_sync(FULL, i < n && need > 0.0);
         while (live && remaining > 0.0) {
@@ -356,7 +376,7 @@ __device__ void log_and_run_seas(const WalkDev& w, int e0, int e1, int* touch_n)
         w.ev_touch[e] = *touch_n;
         if (w.ev_kind[k] == LAKE) {
             const Touch* t = w.slot_touch + (size_t)(e - e0) * w.cap;
-            const int nt = w.slot_touch_n[e - e0];
+            const int nt = index_ok(w, w.slot_touch_n[e - e0], (long long)w.cap + 1, 10) ? w.slot_touch_n[e - e0] : 0;
             for (int i = 0; i < nt; ++i) {
                 if (*touch_n < w.touch_cap) w.touches[(*touch_n)++] = t[i];
                 else w.words[W_ERROR] |= 1;
@@ -643,12 +663,18 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                      e += (int)(gridDim.x * blockDim.x)) {
                     const int k = w.events[e];
                     const bool lake = w.ev_kind[k] == LAKE;
+                    bool ok = lake;
                     if (lake) {
                         const int ci = w.cand_of[w.order[k]];
-                        w.slot_off[e - e0] = w.cand_off[ci];
-                        w.slot_n[e - e0] = w.cand_n[ci];
+                        ok = index_ok(w, ci, w.ncand, 1);
+                        if (ok) ok = index_ok(w, w.cand_n[ci], (long long)w.cap + 1, 3);
+                        if (ok) ok = index_ok(w, w.cand_off[ci] + w.cand_n[ci], w.pool_total + 1, 2);
+                        if (ok) {
+                            w.slot_off[e - e0] = w.cand_off[ci];
+                            w.slot_n[e - e0] = w.cand_n[ci];
+                        }
                     }
-                    w.slot_state[e - e0] = lake ? 1 : 0;
+                    w.slot_state[e - e0] = ok ? 1 : 0;
                     w.slot_touch_n[e - e0] = 0;
                     w.blockers[e - e0] = 0;
                 }
@@ -679,7 +705,9 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                         if (w.poff[m] <= q) a = m;
                         else b = m;
                     }
-                    const int x = w.pool_cells[w.slot_off[a] + (q - w.poff[a])];
+                    int x = 0;
+                    if (index_ok(w, q - w.poff[a], w.slot_n[a], 12)) x = w.pool_cells[w.slot_off[a] + (q - w.poff[a])];
+                    if (!index_ok(w, x, (long long)w.p.W * w.p.H, 4)) x = 0;
                     w.pair_fan[q] = a;
                     w.pair_cell[q] = x;
                     const int pos = atomicAdd(&w.cell_cnt[x], 1);
@@ -696,19 +724,29 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     const int* cnt = w.cell_cnt;
                     const int* dc = w.dcell;
                     cta_exclusive_scan([=](int i) { return __ldcg(&cnt[dc[i]]); }, D, w.doff, sh_scan);
+                    // Every pair is counted on exactly one distinct cell.
+                    if (threadIdx.x == 0 && w.doff[D] != P) check_failed(w, w.doff[D], P, 13);
                 }
                 grid.sync();
-                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x))
-                    w.group[w.doff[w.cell_d[w.pair_cell[q]]] + w.pair_pos[q]] = q;
+                for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x)) {
+                    const int d = w.cell_d[w.pair_cell[q]];
+                    if (!index_ok(w, d, D, 5)) continue;
+                    const int at = w.doff[d] + w.pair_pos[q];
+                    if (index_ok(w, at, P, 6)) w.group[at] = q;
+                }
                 grid.sync();
                 for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x)) {
                     const int x = w.pair_cell[q];
-                    const int* g = w.group + w.doff[w.cell_d[x]];
+                    const int d = w.cell_d[x];
+                    if (!index_ok(w, d, D, 5)) continue;
+                    const int* g = w.group + w.doff[d];
                     const int m = __ldcg(&w.cell_cnt[x]);
+                    if (!index_ok(w, w.doff[d] + m, (long long)P + 1, 7)) continue;
                     const int r = w.events[e0 + w.pair_fan[q]];
                     bool pred = false;
                     int succ = -1, rs = 0;
                     for (int j = 0; j < m; ++j) {
+                        if (!index_ok(w, g[j], P, 8)) continue;
                         const int f = w.pair_fan[g[j]];
                         const int rf = w.events[e0 + f];
                         if (rf < r) pred = true;
@@ -742,7 +780,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                         __syncwarp();
                         __threadfence();
                         for (int q = w.poff[sl] + lane; q < min(w.poff[sl + 1], P); q += 32)   // P: past an overflow
-                            if (w.pair_succ[q] >= 0) atomicSub(&w.blockers[w.pair_succ[q]], 1);
+                            if (w.pair_succ[q] >= 0 && index_ok(w, w.pair_succ[q], S, 11)) atomicSub(&w.blockers[w.pair_succ[q]], 1);
                         if (lane == 0) {
                             w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
                             w.slot_state[sl] = 0;
@@ -751,7 +789,14 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     grid.sync();
                     ++waves;
                     if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
-                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
+                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) {
+                        w.words[W_ERROR] |= 4;
+                        for (int sl = 0; sl < S; ++sl)   // the lowest waiting fan, which nothing should block
+                            if (w.slot_state[sl]) {
+                                check_failed(w, *(volatile int*)&w.blockers[sl], sl, 14);
+                                break;
+                            }
+                    }
                 }
                 // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1028,6 +1073,8 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.cand_of = d_candof;
     w.cand_n = d_candn;
     w.cand_off = d_candoff;
+    w.ncand = ncand;
+    w.pool_total = pool_total;
     w.pool_cells = d_pool_cells;
     w.pool_base = d_pool_base;
     CG_BUF(long long, d_soff, ctx, S_DEPSLOTOFF, S);
@@ -1093,6 +1140,9 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     int words[W_WORDS];
     CG_CUDA(ctx, cudaMemcpyAsync(words, d_words, sizeof(words), cudaMemcpyDeviceToHost, sm));
     CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    if (words[W_ERROR] & 32)
+        return fail(ctx, CG_INEXACT, "deposition: laying-schedule index check %d failed (value %d, bound %d)",
+                    words[W_CHECK_SITE], words[W_CHECK_VALUE], words[W_CHECK_BOUND]);
     if (words[W_ERROR] & 1) return fail(ctx, CG_INEXACT, "deposition: a level's fan deposits overflowed the repair log");
     if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
     if (words[W_ERROR] & 4) return fail(ctx, CG_INEXACT, "deposition: the lake fans' laying waves did not converge");
