@@ -283,7 +283,10 @@ def run_ours(args):
     per_round = [{"land": s.land_cells, "flats": s.flats, "raised": s.raised_cells, "levels": s.levels,
                   "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2),
                   **({"replayed": s.deposit_replayed, "redone": s.deposit_redone, "refitted": s.deposit_refitted,
-                      "waves": s.deposit_waves, "ms_deposit": round(s.ms_deposit, 2)} if args.profile == 2 else {})}
+                      "waves": s.deposit_waves, "ms_deposit": round(s.ms_deposit, 2),
+                      "ms_deposit_parts": {k: round(getattr(s, "ms_deposit_" + k), 2)
+                                           for k in ("walks", "schedule", "lakes", "seas", "repairs")}}
+                     if args.profile == 2 else {})}
                  for s in stats]
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0

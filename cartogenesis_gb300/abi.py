@@ -13,7 +13,7 @@ STATUS_NAMES = {
     CG_OOM: "OOM", CG_CUDA: "CUDA", CG_UNSUPPORTED: "UNSUPPORTED", CG_INEXACT: "INEXACT",
 }
 CG_MODE_REF32 = 0
-CG_PROFILE_P0, CG_PROFILE_P1, CG_PROFILE_P2 = 0, 1, 2
+CG_PROFILE_P0, CG_PROFILE_P1, CG_PROFILE_P2, CG_PROFILE_P3 = 0, 1, 2, 3
 
 
 class ThermalLimits(C.Structure):
@@ -45,6 +45,14 @@ class ErosionParams(C.Structure):
         ("shield_cut", C.c_int32),
         ("profile", C.c_int32),
         ("climate_feed", C.c_int32),
+        ("mantle_density", C.c_float),
+        ("deflection_fill_density", C.c_float),
+        ("gravity", C.c_float),
+        ("continental_crust_density", C.c_float),
+        ("elastic_thickness_km", C.c_float),
+        ("youngs_modulus_gpa", C.c_float),
+        ("poisson_ratio", C.c_float),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -118,6 +126,11 @@ class RoundStats(C.Structure):
         ("deposit_redone", C.c_int32),
         ("deposit_refitted", C.c_int32),
         ("deposit_waves", C.c_int32),
+        ("ms_deposit_walks", C.c_double),
+        ("ms_deposit_schedule", C.c_double),
+        ("ms_deposit_lakes", C.c_double),
+        ("ms_deposit_seas", C.c_double),
+        ("ms_deposit_repairs", C.c_double),
     ]
 
 

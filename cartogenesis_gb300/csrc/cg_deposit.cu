@@ -120,7 +120,17 @@ struct WalkDev {
     float* acc;             // per cell: a replayed settled height
     uint8_t* own_done;      // per cell: the replay has taken the cell's own subtraction
     int* words;             // W_* control words
+    unsigned long long* timers;   // T_*: nanoseconds of the walk's parts, kept by CTA 0's thread 0
 };
+
+// The walk's parts that CTA 0's thread 0 times (it runs every serial part and meets every grid barrier).
+enum { T_WALKS = 0, T_SCHEDULE = 1, T_LAKES = 2, T_SEAS = 3, T_REPAIRS = 4, T_COUNT = 5 };
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ int level_of_cell(const WalkDev& w, int c) { return (int)(w.key[c] >> 32); }
 
@@ -590,7 +600,11 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
     __shared__ int sh_scan[kThreads];
     __shared__ int block_base;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+    unsigned long long tm[T_COUNT] = {0, 0, 0, 0, 0};
+    unsigned long long t0 = 0;
     for (int L = 0; L < w.levels; ++L) {
+        if (timer) t0 = now_ns();
         const int lo = w.level_start[L], hi = w.level_start[L + 1];
         // A: own walks over this CTA's segment of the level, listing live mouths in rank order.
         const int seg = (hi - lo + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -643,6 +657,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
             w.words[W_EVENTS] = n;
         }
         grid.sync();
+        if (timer) tm[T_WALKS] += now_ns() - t0;
         const int n = *(volatile int*)&w.words[W_EVENTS];
         const int lane = threadIdx.x & 31;
         const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -657,6 +672,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         const int passes = hi - lo + 1;
         for (int pass = 0; pass <= passes; ++pass) {
             for (int e0 = e_start; e0 < n_now; e0 += w.slots) {
+                if (timer) t0 = now_ns();
                 const int e1 = min(n_now, e0 + w.slots);
                 // The chunk's lake fans, their admissions taken from the round's pool.
                 for (int e = e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); e < e1;
@@ -762,6 +778,11 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x))
                     w.cell_cnt[w.pair_cell[q]] = 0;   // every cell's count back to 0 for the next chunk
                 int waves = 0;
+                if (timer) {
+                    const unsigned long long t = now_ns();
+                    tm[T_SCHEDULE] += t - t0;
+                    t0 = t;
+                }
                 for (int guard = 0; guard <= S; ++guard) {
                     const int par = guard & 1;
                     if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
@@ -800,11 +821,15 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 }
                 // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
                 if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    const unsigned long long t = now_ns();
+                    tm[T_LAKES] += t - t0;
                     w.words[W_WAVES] += waves;
                     log_and_run_seas(w, e0, e1, &touch_n);
+                    tm[T_SEAS] += now_ns() - t;
                 }
                 grid.sync();
             }
+            if (timer) t0 = now_ns();
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 w.ev_touch[n_now] = touch_n;
                 if (pass == 0) refit_gen = ++w.words[W_GEN];
@@ -821,15 +846,20 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 }
             }
             grid.sync();
+            if (timer) tm[T_REPAIRS] += now_ns() - t0;
             if (*(volatile int*)&w.words[W_DONE]) break;
             e_start = *(volatile int*)&w.words[W_ESTART];
             n_now = *(volatile int*)&w.words[W_EVENTS];
             grid.sync();
         }
         // C: the last repairs, with every deposit of the level in its log.
+        if (timer) t0 = now_ns();
         if (blockIdx.x == 0 && threadIdx.x == 0 && n_now > 0) final_repairs(w, L, n_now, touch_n);
         grid.sync();
+        if (timer) tm[T_REPAIRS] += now_ns() - t0;
     }
+    if (timer)
+        for (int i = 0; i < T_COUNT; ++i) w.timers[i] = tm[i];
 }
 
 // settled = relative + sediment * toRelative, with no load and nothing incised yet
@@ -1125,6 +1155,8 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.acc = d_acc;
     w.own_done = d_own;
     w.words = d_words;
+    CG_BUF(unsigned long long, d_timers, ctx, S_DEPTIMERS, T_COUNT);
+    w.timers = d_timers;
     // The round's own counts (the fan ids, generations and wave numbers carry on through the stage).
     for (int word : {W_REPLAYED, W_WAVES, W_REFITTED, W_RELAID})
         CG_CUDA(ctx, cudaMemsetAsync(d_words + word, 0, sizeof(int), sm));
@@ -1138,7 +1170,9 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     ctx->launches++;
     CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_deposit_levels, cgrid, kThreads, kargs, 0, sm));
     int words[W_WORDS];
+    unsigned long long timers[T_COUNT];
     CG_CUDA(ctx, cudaMemcpyAsync(words, d_words, sizeof(words), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaMemcpyAsync(timers, d_timers, sizeof(timers), cudaMemcpyDeviceToHost, sm));
     CG_CUDA(ctx, cudaStreamSynchronize(sm));
     if (words[W_ERROR] & 32)
         return fail(ctx, CG_INEXACT, "deposition: laying-schedule index check %d failed (value %d, bound %d)",
@@ -1153,6 +1187,11 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
         counts->waves = words[W_WAVES];
         counts->refitted = words[W_REFITTED];
         counts->redone = words[W_RELAID];
+        counts->ms_walks = timers[T_WALKS] * 1e-6;
+        counts->ms_schedule = timers[T_SCHEDULE] * 1e-6;
+        counts->ms_lakes = timers[T_LAKES] * 1e-6;
+        counts->ms_seas = timers[T_SEAS] * 1e-6;
+        counts->ms_repairs = timers[T_REPAIRS] * 1e-6;
     }
     return CG_OK;
 }

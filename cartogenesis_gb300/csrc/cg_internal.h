@@ -142,6 +142,9 @@ struct DepositCounts {
     int replayed;   // ponded cells whose settled height was replayed in rank order
     int waves;      // the lake fans' laying waves, over all levels (counted over the stage so far)
     int refitted;   // dry cells whose own walk was taken again with their donors as the walk saw them
+    // Device-clock milliseconds of the walk's parts: own walks and listing, laying schedules, laying
+    // waves, sea lobes and logs, mouth refits and last repairs.
+    double ms_walks, ms_schedule, ms_lakes, ms_seas, ms_repairs;
 };
 // The deposition walk of one round (HydraulicErosion.kt:1068-1349), the sediment in the stage's buffer.
 cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& p, const DepositRound& r, DepositCounts* counts);

@@ -55,6 +55,13 @@ inline void default_params(cg_erosion_params* p, int width, int height, int64_t 
     p->receiver_clamp = 1;
     p->shield_cut = 1;
     p->profile = CG_PROFILE_P0;
+    p->mantle_density = 3300.0f;
+    p->deflection_fill_density = 0.0f;
+    p->gravity = 9.81f;
+    p->continental_crust_density = 2835.0f;
+    p->elastic_thickness_km = 30.0f;
+    p->youngs_modulus_gpa = 70.0f;
+    p->poisson_ratio = 0.25f;
 }
 
 // WorldGenConfig.wholeCellsFor: kotlin.math.round rounds half to even (nearbyint).

@@ -293,7 +293,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         CG_TRY(incise_dev(ctx, W, H, d_land, d_recv, d_key, levels, d_filled, d_rel, d_area, d_erod, cur, ia,
                           d_incised_at));
         mark(5);
-        DepositCounts dc{0, 0, 0, 0};
+        DepositCounts dc{};
         if (deposition) {
             DepositRound dr;
             dr.recv = d_recv;
@@ -380,6 +380,11 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             s.deposit_redone = dc.redone;
             s.deposit_refitted = dc.refitted;
             s.deposit_waves = dc.waves;
+            s.ms_deposit_walks = dc.ms_walks;
+            s.ms_deposit_schedule = dc.ms_schedule;
+            s.ms_deposit_lakes = dc.ms_lakes;
+            s.ms_deposit_seas = dc.ms_seas;
+            s.ms_deposit_repairs = dc.ms_repairs;
         }
     }
     if (run.next_round >= p.hydraulic_rounds) run.done = true;

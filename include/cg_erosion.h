@@ -57,9 +57,13 @@ typedef enum cg_mode { CG_MODE_REF32 = 0 } cg_mode;
  * (the closing mouths pass belongs to P2). P2: P1 with ErosionConfig.deposition, deltaLobe,
  * deltaOutline and gradedAggradation (the reference's default round tail): each round's deposition
  * walk with its sea lobes and lake fans, settle and the closing mouths pass (HydraulicErosion.kt:
- * 1068-1349, 1351-1364, 1451-1462, 1804-1892; DeltaFan.kt).
+ * 1068-1349, 1351-1364, 1451-1462, 1804-1892; DeltaFan.kt). P3: P2 with IsostasyConfig.flexure (the
+ * reference's default): at the top of every round, after the uplift, the plate bends under the load
+ * the rounds have put on it, a mirrored 2D FFT low-pass of the column change (Isostasy.Flexure,
+ * Isostasy.kt:277-411; HydraulicErosion.kt:707-725, 856-880). P3 needs width <= 8192 and
+ * height <= 4096 (a transform line in one CTA's shared memory).
  */
-typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2 } cg_profile;
+typedef enum cg_profile { CG_PROFILE_P0 = 0, CG_PROFILE_P1 = 1, CG_PROFILE_P2 = 2, CG_PROFILE_P3 = 3 } cg_profile;
 
 /* ThermalLimits (.../pipeline/ErosionAccelerator.kt:58-65): steepest drop per neighbour kind. */
 typedef struct cg_thermal_limits {
@@ -107,6 +111,16 @@ typedef struct cg_erosion_params {
        it set runs through cg_stage_begin / cg_erode_rounds, which stop where the weather is asked;
        cg_erode_stage refuses it. 0 in the P0-P2 profiles. */
     int32_t  climate_feed;
+    /* IsostasyConfig, the plate flexure of profile P3 (Isostasy.Flexure, .../pipeline/Isostasy.kt:
+       277-411; M:WorldGenConfig.kt:1348-1476) */
+    float    mantle_density;              /* 3300 */
+    float    deflection_fill_density;     /* 0 */
+    float    gravity;                     /* 9.81 */
+    float    continental_crust_density;   /* 2835: the load's density */
+    float    elastic_thickness_km;        /* 30 */
+    float    youngs_modulus_gpa;          /* 70 */
+    float    poisson_ratio;               /* 0.25 */
+    int32_t  reserved;
 } cg_erosion_params;
 
 /* Per-cell inputs of one world (ErosionTectonics + the weather the rounds cut with). */
@@ -174,6 +188,14 @@ typedef struct cg_round_stats {
     int32_t deposit_refitted;   /* P2: dry cells whose own walk was taken again with their donors as
                                    the reference's walk showed them */
     int32_t deposit_waves;      /* P2: the lake fans' laying waves over the round's levels */
+    /* P2: where the deposition walk's time went (device clock, milliseconds): the own walks and the
+       mouths' listing, the lake fans' laying schedules, their laying waves, the sea lobes and the
+       level logs (one thread), and the mouth refits and last repairs (one thread). */
+    double  ms_deposit_walks;
+    double  ms_deposit_schedule;
+    double  ms_deposit_lakes;
+    double  ms_deposit_seas;
+    double  ms_deposit_repairs;
 } cg_round_stats;
 
 typedef struct cg_ctx cg_ctx;
