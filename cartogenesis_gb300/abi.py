@@ -131,6 +131,7 @@ class RoundStats(C.Structure):
         ("ms_deposit_lakes", C.c_double),
         ("ms_deposit_seas", C.c_double),
         ("ms_deposit_repairs", C.c_double),
+        ("ms_flexure", C.c_double),
     ]
 
 

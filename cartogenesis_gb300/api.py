@@ -272,6 +272,29 @@ class SeaLevelStage:
         return s.value, is_land, rel, n.value
 
 
+class Isostasy:
+    class Flexure:
+        """Isostasy.Flexure (P/Isostasy.kt:277-411): the plate's bend under a load, on the device."""
+
+        def __init__(self, config, ctx=None):
+            self.config = config
+            self.ctx = ctx or default_context()
+            self.rigidity = None
+            self.restoring = None
+
+        def deflection_metres(self, load_pascals):
+            """deflectionMetres(loadPascals, deflection): the bend in metres, positive down."""
+            H, W = self.config.params.height, self.config.params.width
+            ld = _f32(load_pascals, (H, W))
+            out = np.empty((H, W), np.float32)
+            d, r = C.c_double(), C.c_double()
+            with self.ctx.lock:
+                self.ctx.check(self.ctx.lib.cg_flexure_deflection(self.ctx.handle, C.byref(self.config.params), P(ld),
+                                                                  P(out), C.byref(d), C.byref(r)))
+            self.rigidity, self.restoring = d.value, r.value
+            return out
+
+
 class FlowRouting:
     @staticmethod
     def fill_depressions(is_land, elevation, ctx=None, with_ties=False):

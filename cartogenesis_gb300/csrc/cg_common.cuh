@@ -70,7 +70,7 @@ struct cg_ctx {
     std::atomic<int> cancel{0};
     char error[512] = {0};
     // Named scratch buffers, grown on demand and reused across calls.
-    cg::DevBuf bufs[128];
+    cg::DevBuf bufs[160];
     // Pinned host staging.
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -78,6 +78,10 @@ struct cg_ctx {
     // Row-weight table of the sea-level cut, cached for the last grid shape.
     int rw_w = 0, rw_h = 0;
     double rw_total = 0.0;
+    // The plate flexure's twiddle tables, cached for the last line lengths; its line kernel's
+    // shared-memory limit, raised once.
+    int flex_tw_w = 0, flex_tw_h2 = 0;
+    bool flex_attr = false;
     // Kernels launched on this context (every launch site counts itself with CG_LAUNCH).
     long long launches = 0;
     // The resident world of the round-range entry points (inactive otherwise).
@@ -105,6 +109,7 @@ enum Slot {
     S_OM_LAND, S_OM_REL, S_OM_FILLED, S_OM_RECV, S_OM_KEY, S_OM_AREA, S_OM_RUNOFF, S_OM_DONORS,
     S_FILLEB, S_THERMERR, S_SL_MASK, S_SL_LABEL, S_SL_SIZE, S_SL_WORDS, S_DEPSLOT8, S_DEPSLOT9, S_DEPSLOT10,
     S_DEPCLAIM, S_DEPCANDOF, S_DEPCAND, S_DEPCANDN, S_DEPCANDOFF, S_DEPCANDW, S_DEPSLOTOFF, S_DEPACC, S_DEPOWN, S_DEPCELLCNT, S_DEPTIMERS,
+    S_FX_TW, S_FX_A, S_FX_B, S_FX_MEAN, S_FX_REF, S_FX_DEFL, S_FX_UPL, S_FX_LOAD,
     S_COUNT
 };
 static_assert(S_COUNT <= (int)(sizeof(((cg_ctx*)nullptr)->bufs) / sizeof(DevBuf)), "a slot past the context's buffers");

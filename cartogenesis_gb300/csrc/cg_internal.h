@@ -146,6 +146,15 @@ struct DepositCounts {
     // waves, sea lobes and logs, mouth refits and last repairs.
     double ms_walks, ms_schedule, ms_lakes, ms_seas, ms_repairs;
 };
+// The plate flexure of profile P3 (cg_flexure.cu). flexure_check refuses grids whose transform lines
+// do not fit a CTA's shared memory; flexure_stage_begin_dev records the field before the rounds and
+// clears the bend (and the uplift record when the world has uplift); flexure_uplifted_dev is that
+// record, for k_uplift; flexure_round_dev bends the surface under the rounds' load so far.
+cg_status flexure_check(cg_ctx* ctx, int W, int H);
+cg_status flexure_stage_begin_dev(cg_ctx* ctx, const cg_erosion_params& p, const float* d_work, bool uplift);
+float* flexure_uplifted_dev(cg_ctx* ctx, const cg_erosion_params& p);
+cg_status flexure_round_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_work, const float* d_sediment,
+                            bool uplift);
 // The deposition walk of one round (HydraulicErosion.kt:1068-1349), the sediment in the stage's buffer.
 cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& p, const DepositRound& r, DepositCounts* counts);
 // settle() (HydraulicErosion.kt:1351-1364): the sediment laid on d_h; the sediment is kept as the spoil.

@@ -20,11 +20,13 @@ namespace {
 
 // HydraulicErosion.kt:824-837: h += rate * upliftMetresPerRoundPerMm / metresPerFieldUnit where rate > 0.
 __global__ void k_uplift(float* __restrict__ h, const float* __restrict__ rate, size_t N, float per_mm,
-                         float metres_per_field) {
+                         float metres_per_field, float* __restrict__ uplifted) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         float r = rate[i];
         if (r <= 0.0f) continue;
-        h[i] = __fadd_rn(h[i], __fdiv_rn(__fmul_rn(r, per_mm), metres_per_field));
+        const float metres = __fmul_rn(r, per_mm);
+        h[i] = __fadd_rn(h[i], __fdiv_rn(metres, metres_per_field));
+        if (uplifted) uplifted[i] = __fadd_rn(uplifted[i], metres);   // the plate flexure's record (P3)
     }
 }
 
@@ -158,6 +160,8 @@ cg_status stage_begin_dev(cg_ctx* ctx, StageRun& run) {
         CG_TRY(thermal_sweeps_dev(ctx, p.width, p.height, run.cur, run.other, thermal_limits(p), sweeps, p.rate, &res));
         if (res != run.cur) std::swap(run.cur, run.other);
     }
+    // HydraulicErosion.kt:707-725: the plate flexure's field before the rounds (P3).
+    if (p.profile >= CG_PROFILE_P3) CG_TRY(flexure_stage_begin_dev(ctx, p, run.cur, run.uplift != nullptr));
     if (p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) run.done = true;
     return CG_OK;
 }
@@ -207,8 +211,17 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
     CG_BUF(float, d_erod, ctx, S_ERODE, N);
     CG_BUF(double, d_sum, ctx, S_CG3, 2);
 
-    // Phase boundaries of a round, for the per-phase device times of cg_round_stats.
-    cudaEvent_t ev[8] = {};
+    const bool flexure = p.profile >= CG_PROFILE_P3;
+    float* d_uplifted = flexure && d_uplift ? flexure_uplifted_dev(ctx, p) : nullptr;
+    float* d_sediment_now = nullptr;
+    if (flexure) {
+        CG_BUF(float, sed, ctx, S_SEDIMENT, N);
+        d_sediment_now = sed;
+    }
+
+    // Phase boundaries of a round, for the per-phase device times of cg_round_stats (ev[8]: the end
+    // of the uplift and the plate flexure).
+    cudaEvent_t ev[9] = {};
     if (stats)
         for (auto& e : ev) CG_CUDA(ctx, cudaEventCreate(&e));
     struct Events {
@@ -216,7 +229,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         bool on;
         ~Events() {
             if (on)
-                for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+                for (int i = 0; i < 9; ++i) cudaEventDestroy(ev[i]);
         }
     } guard{ev, stats != nullptr};
     auto mark = [&](int i) {
@@ -228,7 +241,11 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
         float* cur = run.cur;
         const long long launches0 = ctx->launches;
         mark(0);
-        if (d_uplift) CG_LAUNCH(ctx) k_uplift<<<grid, 256, 0, sm>>>(cur, d_uplift, N, per_mm, sc.relief_span());
+        if (d_uplift)
+            CG_LAUNCH(ctx) k_uplift<<<grid, 256, 0, sm>>>(cur, d_uplift, N, per_mm, sc.relief_span(), d_uplifted);
+        // HydraulicErosion.kt:856-884: the plate answers the whole load so far (P3).
+        if (flexure) CG_TRY(flexure_round_dev(ctx, p, cur, d_sediment_now, d_uplift != nullptr));
+        mark(8);
         float shoreline;
         int land_cells;
         CG_TRY(percentile_cut_dev(ctx, W, H, cur, p.sea_level, land_half, sea_half, stand_below_today(p, round),
@@ -354,6 +371,11 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             CG_CUDA(ctx, cudaEventSynchronize(ev[7]));
             float ms[8] = {0};
             for (int i = 1; i < 8; ++i) cudaEventElapsedTime(&ms[i], ev[i - 1], ev[i]);
+            float ms_flexure = 0.0f;
+            if (flexure) {
+                cudaEventElapsedTime(&ms_flexure, ev[0], ev[8]);
+                cudaEventElapsedTime(&ms[1], ev[8], ev[1]);
+            }
             float total = 0.0f;
             cudaEventElapsedTime(&total, ev[0], ev[7]);
             cg_round_stats& s = stats[round - first_round];
@@ -376,6 +398,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             s.ms_incise = ms[5];
             s.ms_deposit = ms[6];
             s.ms_relax = ms[7];
+            s.ms_flexure = ms_flexure;
             s.deposit_replayed = dc.replayed;
             s.deposit_redone = dc.redone;
             s.deposit_refitted = dc.refitted;
@@ -463,8 +486,9 @@ cg_status check_params(cg_ctx* ctx, const cg_erosion_params* p, bool fed_ok) {
                     CG_ABI_VERSION);
     CG_TRY(check_grid(ctx, p->width, p->height));
     if (p->mode != CG_MODE_REF32) return fail(ctx, CG_UNSUPPORTED, "only the REF32 mode is built");
-    if (p->profile < CG_PROFILE_P0 || p->profile > CG_PROFILE_P2)
-        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0, P1 and P2)", p->profile);
+    if (p->profile < CG_PROFILE_P0 || p->profile > CG_PROFILE_P3)
+        return fail(ctx, CG_UNSUPPORTED, "profile P%d is not built (P0 to P3)", p->profile);
+    if (p->profile >= CG_PROFILE_P3) CG_TRY(flexure_check(ctx, p->width, p->height));
     if (p->climate_feed && !fed_ok)
         return fail(ctx, CG_UNSUPPORTED,
                     "climate_feed asks for the caller's weather halfway through the rounds: run the stage with "

@@ -196,6 +196,8 @@ typedef struct cg_round_stats {
     double  ms_deposit_lakes;
     double  ms_deposit_seas;
     double  ms_deposit_repairs;
+    double  ms_flexure;         /* P3: the uplift and the plate flexure at the top of the round (ms_cut then
+                                   holds the cut and the weights alone); 0 below P3 */
 } cg_round_stats;
 
 typedef struct cg_ctx cg_ctx;
@@ -354,6 +356,16 @@ cg_status cg_percentile_cut(cg_ctx* ctx, int32_t width, int32_t height, const fl
 cg_status cg_sea_level_cut(cg_ctx* ctx, const cg_erosion_params* params, const float* height,
                            double enclosed_sea_max_share, int32_t post_cut_outlet, float* shoreline,
                            uint8_t* is_land, float* relative, int32_t* land_cells, int32_t* passes);
+
+/*
+ * Isostasy.Flexure(config).deflectionMetres(load, out) (.../pipeline/Isostasy.kt:277-372, over
+ * math/Fft.kt's Fft2D): the plate's bend, in metres (positive down), under `load` pascals (host memory,
+ * width x height of `params`), bit-exact to the reference's transform: the load less its mean, mirrored
+ * about each pole to 2 x height rows, the low-pass 1 / (dRho g + D k^4) with the zero-frequency term
+ * dropped. `rigidity` (D) and `restoring` (dRho g) may be NULL. Needs width <= 8192 and height <= 4096.
+ */
+cg_status cg_flexure_deflection(cg_ctx* ctx, const cg_erosion_params* params, const float* load,
+                                float* deflection, double* rigidity, double* restoring);
 
 /* FlowRouting.fillDepressions (.../pipeline/FlowRouting.kt:52-111). */
 cg_status cg_fill_depressions(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,

@@ -86,6 +86,8 @@ def lib():
         L.or_sea_level_drained_cut.argtypes = [C.POINTER(abi.ErosionParams), vp, f64, i32, C.POINTER(f32), vp, vp,
                                                C.POINTER(i32), C.POINTER(i32)]
         L.or_sea_level_drained_cut.restype = i32
+        L.or_flexure_deflection.argtypes = [C.POINTER(abi.ErosionParams), vp, vp, C.POINTER(f64), C.POINTER(f64)]
+        L.or_flexure_deflection.restype = i32
         _lib = L
     return _lib
 
@@ -383,3 +385,13 @@ def sea_level_drained_cut(params, height, enclosed_max_share=0.00073, post_cut_o
                                         P(land), P(rel), C.byref(n), C.byref(passes))
     assert st == 0, st
     return s.value, land, rel, n.value, passes.value
+
+
+def flexure_deflection(params, load):
+    """Isostasy.Flexure.deflectionMetres: (deflection in metres, rigidity D, restoring dRho g)."""
+    H, W = params.height, params.width
+    ld = np.ascontiguousarray(load, dtype=np.float32).reshape(H, W)
+    out = np.empty((H, W), np.float32)
+    d, r = C.c_double(), C.c_double()
+    assert lib().or_flexure_deflection(C.byref(params), P(ld), P(out), C.byref(d), C.byref(r)) == 0
+    return out, d.value, r.value

@@ -1291,6 +1291,7 @@ struct Switches {
     double delta_min_catchment_km2 = 70000.0;   // ErosionConfig.deltaMinCatchmentKm2
     double delta_reach_km = 140.625;         // ErosionConfig.deltaReachKm
     float delta_freeboard_metres = 48.0f;    // ErosionConfig.deltaFreeboardMetres
+    bool flexure = false;             // IsostasyConfig.flexure (with IsostasyConfig.enabled)
 };
 
 // P0: the plain core; P1 adds the outlet notch; P2 adds deposition with the lobed, outlined and
@@ -1299,6 +1300,7 @@ Switches switches_of(const cg_erosion_params& p) {
     Switches s;
     s.outlet_incision = p.profile >= CG_PROFILE_P1;
     s.deposition = s.delta_lobe = s.delta_outline = s.graded_aggradation = p.profile >= CG_PROFILE_P2;
+    s.flexure = p.profile >= CG_PROFILE_P3;
     return s;
 }
 
@@ -2139,6 +2141,133 @@ double open_mouths(const cg_erosion_params& p, float* working, const float* spoi
     return removed;
 }
 
+// ---------------------------------------------------------------- plate flexure (profile P3)
+
+// Fft1D (math/Fft.kt:12-97): in-place radix-2 decimation in time over a strided line, twiddles
+// tabulated once per length; `inverse` flips the sign of the twiddles' imaginary parts only.
+struct Fft1D {
+    int n;
+    std::vector<double> cos_t, sin_t;
+    explicit Fft1D(int length) : n(length), cos_t(length / 2), sin_t(length / 2) {
+        for (int i = 0; i < length / 2; ++i) {
+            cos_t[i] = std::cos(2.0 * M_PI * (double)i / (double)length);
+            sin_t[i] = std::sin(2.0 * M_PI * (double)i / (double)length);
+        }
+    }
+    void transform(double* re, double* im, size_t offset, size_t stride, bool inverse) const {
+        int reversed = 0;
+        for (int index = 1; index < n; ++index) {
+            int bit = n >> 1;
+            while (reversed & bit) {
+                reversed ^= bit;
+                bit >>= 1;
+            }
+            reversed |= bit;
+            if (index < reversed) {
+                const size_t a = offset + (size_t)index * stride, b = offset + (size_t)reversed * stride;
+                std::swap(re[a], re[b]);
+                std::swap(im[a], im[b]);
+            }
+        }
+        for (int block = 2; block <= n; block <<= 1) {
+            const int half = block >> 1, tw_stride = n / block;
+            for (int start = 0; start < n; start += block)
+                for (int pair = 0; pair < half; ++pair) {
+                    const int t = pair * tw_stride;
+                    const double wr = cos_t[t], wi = inverse ? sin_t[t] : -sin_t[t];
+                    const size_t e = offset + (size_t)(start + pair) * stride;
+                    const size_t o = offset + (size_t)(start + pair + half) * stride;
+                    const double rr = re[o] * wr - im[o] * wi;
+                    const double ri = re[o] * wi + im[o] * wr;
+                    const double er = re[e], ei = im[e];
+                    re[e] = er + rr;
+                    im[e] = ei + ri;
+                    re[o] = er - rr;
+                    im[o] = ei - ri;
+                }
+        }
+    }
+};
+
+// Fft2D (math/Fft.kt:99-152): every row, then every column; the inverse scaled by 1 / (width height).
+struct Fft2D {
+    int w, h;
+    Fft1D rows, cols;
+    Fft2D(int width, int height) : w(width), h(height), rows(width), cols(height) {}
+    void run(double* re, double* im, bool inverse) const {
+        for (int r = 0; r < h; ++r) rows.transform(re, im, (size_t)r * w, 1, inverse);
+        for (int c = 0; c < w; ++c) cols.transform(re, im, (size_t)c, (size_t)w, inverse);
+    }
+    void forward(double* re, double* im) const { run(re, im, false); }
+    void inverse(double* re, double* im) const {
+        run(re, im, true);
+        const double scale = 1.0 / ((double)w * (double)h);
+        for (size_t c = 0; c < (size_t)w * h; ++c) {
+            re[c] *= scale;
+            im[c] *= scale;
+        }
+    }
+};
+
+// Isostasy.Flexure (Isostasy.kt:277-411): the plate's deflection under a load, a low-pass filter
+// 1 / (dRho g + D k^4) over a grid mirrored about each pole to twice the map's height, the load's
+// mean removed and the zero-frequency term left at zero.
+struct Flexure {
+    int W, H, rows2;
+    double restoring, rigidity, per_cycle_across, per_cycle_down;
+    Fft2D fft;
+    std::vector<double> re, im;
+    explicit Flexure(const cg_erosion_params& p)
+        : W(p.width), H(p.height), rows2(p.height * 2), fft(p.width, p.height * 2),
+          re((size_t)p.width * p.height * 2), im((size_t)p.width * p.height * 2) {
+        const float metres_per_km = 1000.0f;
+        restoring = (double)(p.mantle_density - p.deflection_fill_density) * (double)p.gravity;
+        const double te = (double)p.elastic_thickness_km * (double)metres_per_km;
+        const double e = (double)p.youngs_modulus_gpa * 1e9;
+        const double nu = (double)p.poisson_ratio;
+        rigidity = e * te * te * te / (12.0 * (1.0 - nu * nu));
+        const Scale sc = scale_of(p);
+        per_cycle_across = 2.0 * M_PI / ((double)W * sc.cell_width_km(W) * (double)metres_per_km);
+        per_cycle_down = 2.0 * M_PI / ((double)rows2 * sc.cell_height_km(H) * (double)metres_per_km);
+    }
+    // deflectionMetres(load, out): `out` may be `load`.
+    void deflection(const float* load, float* out) {
+        const size_t cells = (size_t)W * H;
+        double sum = 0.0;
+        for (size_t c = 0; c < cells; ++c) sum += (double)load[c];
+        const double mean = sum / (double)cells;
+        for (int r = 0; r < H; ++r)
+            for (int c = 0; c < W; ++c) {
+                const double v = (double)load[(size_t)r * W + c] - mean;
+                re[(size_t)r * W + c] = v;
+                re[(size_t)(rows2 - 1 - r) * W + c] = v;
+                im[(size_t)r * W + c] = 0.0;
+                im[(size_t)(rows2 - 1 - r) * W + c] = 0.0;
+            }
+        fft.forward(re.data(), im.data());
+        for (int r = 0; r < rows2; ++r) {
+            const int cycles_down = r <= rows2 / 2 ? r : r - rows2;
+            const double kd = (double)cycles_down * per_cycle_down;
+            for (int c = 0; c < W; ++c) {
+                const int cycles_across = c <= W / 2 ? c : c - W;
+                const double ka = (double)cycles_across * per_cycle_across;
+                const size_t i = (size_t)r * W + c;
+                const double k2 = ka * ka + kd * kd;
+                if (k2 == 0.0) {
+                    re[i] = 0.0;
+                    im[i] = 0.0;
+                    continue;
+                }
+                const double response = 1.0 / (restoring + rigidity * k2 * k2);
+                re[i] *= response;
+                im[i] *= response;
+            }
+        }
+        fft.inverse(re.data(), im.data());
+        for (size_t c = 0; c < cells; ++c) out[c] = (float)re[c];
+    }
+};
+
 struct StageOut {
     std::vector<float> height;
     Cut cut;
@@ -2211,6 +2340,17 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
         for (float v : f) sum += (double)v;
         return sum;
     };
+    // The plate flexure's state (HydraulicErosion.kt:707-725): the field before the rounds, the bend
+    // applied so far, and the uplift so far (which arrives compensated, so is no load).
+    std::unique_ptr<Flexure> flexure;
+    std::vector<float> reference, deflection, load_pa, uplifted;
+    if (sw.flexure) {
+        flexure.reset(new Flexure(p));
+        reference = working;
+        deflection.assign(N, 0.0f);
+        load_pa.assign(N, 0.0f);
+        if (in.uplift_mm_per_year) uplifted.assign(N, 0.0f);
+    }
     std::vector<float> ones(N, 1.0f), zeros(N, 0.0f);
     const float* rain = in.rainfall_mm ? in.rainfall_mm : ones.data();
     const float* veg = in.vegetation_density ? in.vegetation_density : zeros.data();
@@ -2236,6 +2376,22 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
                 if (rate[c] <= 0.0f) continue;
                 float metres = rate[c] * uplift_per_mm;
                 working[c] += metres / metres_per_field;
+                if (!uplifted.empty()) uplifted[c] += metres;
+            }
+        }
+        if (flexure) {   // HydraulicErosion.kt:856-880: the plate answers the whole load so far
+            const float density = p.continental_crust_density, gravity = p.gravity;
+            for (size_t c = 0; c < N; ++c) {
+                float column = (working[c] - reference[c]) * metres_per_field + deflection[c] -
+                               (uplifted.empty() ? 0.0f : uplifted[c]) +
+                               (sediment.empty() ? 0.0f : sediment[c] * metres_per_field);
+                load_pa[c] = column * density * gravity;
+            }
+            flexure->deflection(load_pa.data(), load_pa.data());
+            for (size_t c = 0; c < N; ++c) {
+                const float bend = load_pa[c];
+                working[c] += (deflection[c] - bend) / metres_per_field;
+                deflection[c] = bend;
             }
         }
         percentile_cut(W, H, working.data(), p.sea_level, sc, stand_below_today(p, round), cut);
@@ -2440,6 +2596,13 @@ void or_default_params(cg_erosion_params* p, int32_t width, int32_t height, int6
     p->receiver_clamp = 1;
     p->shield_cut = 1;
     p->profile = CG_PROFILE_P0;
+    p->mantle_density = 3300.0f;
+    p->deflection_fill_density = 0.0f;
+    p->gravity = 9.81f;
+    p->continental_crust_density = 2835.0f;
+    p->elastic_thickness_km = 30.0f;
+    p->youngs_modulus_gpa = 70.0f;
+    p->poisson_ratio = 0.25f;
 }
 
 void or_thermal_limits(const cg_erosion_params* p, cg_thermal_limits* lim, int32_t* sweeps) {
@@ -2694,6 +2857,16 @@ int32_t or_sea_level_drained_cut(const cg_erosion_params* p, const float* height
     std::memcpy(relative, cut.relative.data(), N * 4);
     *land_cells = cut.land_cells;
     *passes = run;
+    return 0;
+}
+
+// Isostasy.Flexure(config).deflectionMetres(load, out) (Isostasy.kt:327-372), and its two scalars.
+int32_t or_flexure_deflection(const cg_erosion_params* p, const float* load, float* out, double* rigidity,
+                              double* restoring) {
+    Flexure f(*p);
+    f.deflection(load, out);
+    if (rigidity) *rigidity = f.rigidity;
+    if (restoring) *restoring = f.restoring;
     return 0;
 }
 

@@ -91,7 +91,7 @@ def test_stage_rejects_bad_arguments():
     with pytest.raises(CgError):
         ErosionStage.apply(ErosionConfig(48, 32, 1), h)
     with pytest.raises(CgError):
-        ErosionStage.apply(ErosionConfig(64, 32, 1, profile=3), np.zeros((32, 64), np.float32))
+        ErosionStage.apply(ErosionConfig(64, 32, 1, profile=4), np.zeros((32, 64), np.float32))
     with pytest.raises(CgError):
         ErosionStage.apply(ErosionConfig(64, 32, 1, mode=1), np.zeros((32, 64), np.float32))
 

@@ -1,0 +1,70 @@
+"""The oracle's restatement of the plate flexure (Isostasy.Flexure over Fft2D; Isostasy.kt:277-411,
+math/Fft.kt), pinned by the reference's own IsostasyTest (T/IsostasyTest.kt:219-362, rebuilt from its
+constants): a broad load sinks to Airy's answer, a narrow one is held up, the bend carries no mean,
+the flexural parameter is a continent's, and a load on one pole does not bend the other."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+KM_PER_METRE = 1e-3
+
+
+def params(W, H):
+    return oracle.default_params(W, H, 1)
+
+
+def test_broad_load_sinks_to_airy_and_a_narrow_one_is_held_up():
+    W = H = 256
+    p = params(W, H)
+    load_metres = np.float32(1000.0)
+    pascals = np.float32(load_metres * np.float32(p.continental_crust_density) * np.float32(p.gravity))
+    airy = float(load_metres * np.float32(p.continental_crust_density) /
+                 (np.float32(p.mantle_density) - np.float32(p.deflection_fill_density)))
+
+    def deflection_under(half):
+        load = np.zeros((H, W), np.float32)
+        rows = np.abs(np.arange(H) - H // 2) <= half
+        cols = np.abs(np.arange(W) - W // 2) <= half
+        load[np.ix_(rows, cols)] = pascals
+        out, rigidity, restoring = oracle.flexure_deflection(p, load)
+        assert abs(float(out.astype(np.float64).mean())) <= 1e-6   # no mean: the datum is not the plate's
+        return float(out[H // 2, W // 2]), rigidity, restoring
+
+    broad, rigidity, restoring = deflection_under(16)
+    narrow, _, _ = deflection_under(0)
+    alpha_km = math.sqrt(math.sqrt(4.0 * rigidity / restoring)) * KM_PER_METRE
+    assert 50.0 <= alpha_km <= 200.0
+    assert broad == pytest.approx(airy, abs=airy * 0.05)
+    assert narrow < airy * 0.5
+
+
+def test_a_load_on_one_pole_does_not_bend_the_other():
+    H = 512
+    W = 2 * H
+    p = params(W, H)
+    load = np.zeros((H, W), np.float32)
+    load[0, :] = np.float32(np.float32(1000.0) * np.float32(p.continental_crust_density) * np.float32(p.gravity))
+    out, _, _ = oracle.flexure_deflection(p, load)
+    middle = float(out[H // 2, 0])
+    near = float(out[1, 0]) - middle
+    far = float(out[H - 1, 0]) - middle
+    assert abs(near) > 10.0                 # MIN_STRIPE_DEFLECTION_METRES
+    assert abs(far) / abs(near) < 1e-6      # FAR_POLE_SHARE_OF_NEAR_ROW
+
+
+def test_fft_round_trip():
+    """Fft2D.inverse(forward(f)) is f to rounding (the transform and its 1 / (w h))."""
+    p = params(64, 32)
+    rng = np.random.default_rng(1)
+    load = rng.standard_normal((32, 64)).astype(np.float32) * np.float32(1e6)
+    # A flexure with no stiffness and unit restoring force is the identity less the mean.
+    p.elastic_thickness_km = 0.0
+    p.mantle_density = 1.0
+    p.deflection_fill_density = 0.0
+    p.gravity = 1.0
+    out, _, _ = oracle.flexure_deflection(p, load)
+    want = load.astype(np.float64) - load.astype(np.float64).mean()
+    assert np.allclose(out, want, rtol=1e-5, atol=1e-3 * np.abs(want).max())
