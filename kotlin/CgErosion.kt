@@ -98,29 +98,35 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     }
 
     // cg_profile: P0 without the outlet notch; P1 with it (HydraulicErosion.breach and the closing
-    // breach); P2 with deposition and its lobed, outlined and graded deltas too (the reference's
-    // default). Any other mix of those switches is not a profile the library runs: -1.
+    // breach); P2 with deposition and its lobed, outlined and graded deltas too; P3 is P2 with the
+    // plate flexure (the reference's default). Any other mix of those switches is not a profile the
+    // library runs: -1.
     private fun profileOf(config: WorldGenConfig): Int {
         val e = config.erosion
         val deltas = e.deltaLobe && e.deltaOutline && e.gradedAggradation
+        val flexure = config.isostasy.enabled && config.isostasy.flexure
         return when {
-            e.deposition && e.outletIncision && deltas -> 2
+            e.deposition && e.outletIncision && deltas -> if (flexure) 3 else 2
+            flexure -> -1
             !e.deposition && !e.deltaLobe && e.outletIncision -> 1
             !e.deposition && !e.deltaLobe && !e.outletIncision -> 0
             else -> -1
         }
     }
 
-    // The parts of the stage the library does not run: the belts' replay (needs the plate history),
-    // the plate flexure, and the relief finer than the grid.
-    override fun supports(config: WorldGenConfig): Boolean =
-        profileOf(config) >= 0 && !config.isostasy.flexure
+    // The parts of the stage the library does not run: the belts' replay (needs the plate history)
+    // and the relief finer than the grid. The flexure's transform lines must fit a CTA: width <= 8192,
+    // height <= 4096.
+    override fun supports(config: WorldGenConfig): Boolean {
+        val profile = profileOf(config)
+        return profile >= 0 && (profile < 3 || (config.width <= 8192 && config.height <= 4096))
+    }
 
     override fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
                             rockErodibility: FloatField?, weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField =
         Arena.ofConfined().use { a ->
-            // cg_erosion_params, 112 bytes (offsets as in cg_erosion.h, checked by the C tests).
-            val p = a.allocate(112, 8)
+            // cg_erosion_params, 144 bytes (offsets as in cg_erosion.h, checked by the C tests).
+            val p = a.allocate(144, 8)
             defaults.invokeExact(p, config.width, config.height, config.seed)
             p.set(JAVA_DOUBLE, 24, config.scale.worldWidthKm)
             p.set(JAVA_FLOAT, 32, config.scale.highestLandMetres)
@@ -139,6 +145,14 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
             p.set(JAVA_INT, 100, profileOf(config))
             val fed = config.erosion.climateFeed && weather != null
             p.set(JAVA_INT, 104, if (fed) 1 else 0)   // climate_feed
+            val iso = config.isostasy   // IsostasyConfig, read by P3's flexure
+            p.set(JAVA_FLOAT, 108, iso.mantleDensity)
+            p.set(JAVA_FLOAT, 112, iso.deflectionFillDensity)
+            p.set(JAVA_FLOAT, 116, iso.gravity)
+            p.set(JAVA_FLOAT, 120, iso.continentalCrustDensity)
+            p.set(JAVA_FLOAT, 124, iso.elasticThicknessKm)
+            p.set(JAVA_FLOAT, 128, iso.youngsModulusGPa)
+            p.set(JAVA_FLOAT, 132, iso.poissonRatio)
             fun field(f: FloatArray?) = if (f == null) MemorySegment.NULL else a.allocateFrom(JAVA_FLOAT, *f)
             val inputs = a.allocate(40, 8)
             inputs.set(ADDRESS, 0, field(height.data))
@@ -176,7 +190,7 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
      */
     fun drainedCut(config: WorldGenConfig, height: FloatField, enclosedSeaMaxShare: Double,
                    postCutOutlet: Boolean): SeaLevelResult = Arena.ofConfined().use { a ->
-        val p = a.allocate(112, 8)
+        val p = a.allocate(144, 8)
         defaults.invokeExact(p, config.width, config.height, config.seed)
         p.set(JAVA_DOUBLE, 24, config.scale.worldWidthKm)
         p.set(JAVA_FLOAT, 32, config.scale.highestLandMetres)
