@@ -30,6 +30,7 @@
 // Settle is elementwise, and the mouths pass reads only each cell's receiver, so it runs receivers
 // first, level by level from the top, like the incision.
 #include <algorithm>
+#include <climits>
 #include <cooperative_groups.h>
 #include <vector>
 
@@ -52,7 +53,8 @@ constexpr int kThreads = 256;
 enum {
     W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
     W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15,
-    W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18, W_WORDS = 20
+    W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18,
+    W_REFITGEN = 20, W_BEST = 21, W_TOUCHN = 22, W_NREPLAY = 23, W_NREFIT = 24, W_FGEN = 25, W_WORDS = 28
 };
 
 struct WalkDev {
@@ -117,6 +119,8 @@ struct WalkDev {
     int* mark;              // per cell: the generation that listed it for a replay
     int* replay;            // cells to replay
     int* refit;             // cells to refit
+    int* rlist;             // the log's entries on the cells to replay, grouped by cell (touch_cap)
+    int* roff;              // per cell to replay + 1: its group's first entry
     float* acc;             // per cell: a replayed settled height
     uint8_t* own_done;      // per cell: the replay has taken the cell's own subtraction
     int* words;             // W_* control words
@@ -472,28 +476,6 @@ __device__ bool refit_cell(const WalkDev& w, int c, int n) {
     return true;
 }
 
-// The earliest cell of level L, ranked after a fan of the level that raised one of its donors, whose
-// headroom read that donor and which has a mouth of its own (its step ends at the sea or in a lake):
-// its own walk, and so its fan, are not the reference's. Cells refitted already (mark = refit_gen)
-// are final and skipped. Returns its rank, or -1.
-__device__ int earliest_mouth_conflict(const WalkDev& w, int L, int n, int refit_gen) {
-    int best = -1;
-    for (int e = 0; e < n; ++e) {
-        const int rank = w.events[e];
-        if (best >= 0 && rank >= best) break;   // a conflict needs a fan ranked before the cell
-        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
-            const int x = w.touches[t].cell;
-            if (!w.f.land[x]) continue;
-            const int rr = w.f.dirs[x];
-            if (rr < 0 || !w.f.land[rr] || level_of_cell(w, rr) != L) continue;
-            const int r = w.rank_of[rr];
-            if (r > rank && w.used[rr] && kind_of(w, rr) != ON && w.mark[rr] != refit_gen && (best < 0 || r < best))
-                best = r;
-        }
-    }
-    return best;
-}
-
 // Makes the walk the reference's again from rank rc (the earliest mouth conflict): every fan ranked
 // at or after rc undone, latest first, and the level's log cut back to before them; the conflicted
 // cell's own walk taken again on the state the reference's walk shows it (its own state before the
@@ -536,61 +518,136 @@ __device__ int refit_mouth_cell(const WalkDev& w, int rc, int refit_gen, int* n,
     return ec;
 }
 
-// The last repairs of level L ([lo, hi)), with its final log of n events, on one thread:
+// The level-log entry t's event: the last e with ev_touch[e] <= t (events without entries share
+// their successor's offset).
+__device__ __forceinline__ int event_of(const WalkDev& w, int t, int n) {
+    int a = 0, b = n;
+    while (b - a > 1) {
+        const int m = (a + b) >> 1;
+        if (w.ev_touch[m] <= t) a = m;
+        else b = m;
+    }
+    return a;
+}
+
+// The earliest cell of level L, ranked after a fan of the level that raised one of its donors, whose
+// headroom read that donor and which has a mouth of its own (its step ends at the sea or in a lake):
+// its own walk, and so its fan, are not the reference's. Cells refitted already (mark = the level's
+// refit generation) are final and skipped. Over the grid: each thread takes log entries and the
+// lowest rank found wins (atomicMin into W_BEST, INT_MAX when there is none).
+__device__ void mouth_conflicts_grid(const WalkDev& w, int L, int n) {
+    const int T = *(volatile int*)&w.words[W_TOUCHN];
+    const int refit_gen = *(volatile int*)&w.words[W_REFITGEN];
+    int best = INT_MAX;
+    for (int t = (int)(blockIdx.x * blockDim.x + threadIdx.x); t < T; t += (int)(gridDim.x * blockDim.x)) {
+        const int x = w.touches[t].cell;
+        if (!w.f.land[x]) continue;
+        const int rr = w.f.dirs[x];
+        if (rr < 0 || !w.f.land[rr] || level_of_cell(w, rr) != L) continue;
+        const int r = w.rank_of[rr];
+        if (r >= best) continue;
+        const int rank = w.events[event_of(w, t, n)];
+        if (r > rank && w.used[rr] && kind_of(w, rr) != ON && w.mark[rr] != refit_gen) best = r;
+    }
+    if (best != INT_MAX) atomicMin(&w.words[W_BEST], best);
+}
+
+// The last repairs of level L, with its final log of n events, called by every thread of the grid:
 // (b) a dry cell whose step hands everything on (kind ON) and whose headroom read a donor an earlier
 // fan of the level raised is refitted with its donors as the reference's walk showed them; (a) a
 // ponded cell of the level ranked after a fan that laid into it has its settled height replayed, its
-// own subtraction and the fans' increments in rank order, in one pass over the log.
-__device__ void final_repairs(const WalkDev& w, int L, int n, int touch_n) {
-    w.ev_touch[n] = touch_n;
-    const int gen = ++w.words[W_GEN];
-    int replays = 0, refits = 0;
-    for (int e = 0; e < n; ++e) {
-        const int rank = w.events[e];
-        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
-            const int x = w.touches[t].cell;
-            if (!w.f.land[x]) continue;
-            if (level_of_cell(w, x) == L && w.rank_of[x] > rank && w.mark[x] != gen) {
-                w.mark[x] = gen;
-                w.replay[replays++] = x;
-                w.acc[x] = w.s0[w.rank_of[x]];
-                w.own_done[x] = 0;
-            }
-            const int rr = w.f.dirs[x];
-            if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr] &&
-                kind_of(w, rr) == ON && w.mark[rr] != -gen) {
-                w.mark[rr] = -gen;   // a dry cell: never a replay's (those are ponded)
-                w.refit[refits++] = rr;
-            }
+// own subtraction and the fans' increments in rank order. Steps: (1) the cells to replay and to refit
+// listed from the log (each once: atomicExch on its mark); (2) the refits, a thread each (a donor has
+// one receiver and cells of a level never read one another, so they share nothing), and the log's
+// entries counted per cell to replay; (3) offsets; (4) the entries scattered into per-cell groups;
+// (5) each group put back in log order and replayed by one thread: the additions of a walk over the
+// whole log, in its order.
+__device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, int* sh_scan) {
+    cgr::grid_group grid = cgr::this_grid();
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x), stride = (int)(gridDim.x * blockDim.x);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.ev_touch[n] = touch_n;
+        w.words[W_TOUCHN] = touch_n;
+        w.words[W_FGEN] = ++w.words[W_GEN];
+        w.words[W_NREPLAY] = 0;
+        w.words[W_NREFIT] = 0;
+    }
+    grid.sync();
+    const int T = *(volatile int*)&w.words[W_TOUCHN];
+    const int gen = *(volatile int*)&w.words[W_FGEN];
+    for (int t = tid; t < T; t += stride) {
+        const int x = w.touches[t].cell;
+        if (!w.f.land[x]) continue;
+        const int rank = w.events[event_of(w, t, n)];
+        if (level_of_cell(w, x) == L && w.rank_of[x] > rank && atomicExch(&w.mark[x], gen) != gen) {
+            const int i = atomicAdd(&w.words[W_NREPLAY], 1);
+            w.replay[i] = x;
+            w.cell_d[x] = i;
+        }
+        const int rr = w.f.dirs[x];
+        if (rr >= 0 && w.f.land[rr] && level_of_cell(w, rr) == L && w.rank_of[rr] > rank && w.used[rr] &&
+            kind_of(w, rr) == ON && atomicExch(&w.mark[rr], -gen) != -gen) {   // a dry cell: never a replay's
+            const int j = atomicAdd(&w.words[W_NREFIT], 1);
+            w.refit[j] = rr;
         }
     }
-    for (int i = 0; i < refits; ++i) {
-        refit_cell(w, w.refit[i], n);
-        w.words[W_REFITTED]++;
+    grid.sync();
+    const int R = *(volatile int*)&w.words[W_NREPLAY], F = *(volatile int*)&w.words[W_NREFIT];
+    for (int j = tid; j < F; j += stride) {
+        refit_cell(w, w.refit[j], n);
+        atomicAdd(&w.words[W_REFITTED], 1);
     }
-    if (replays == 0) return;
-    for (int e = 0; e < n; ++e) {
-        const int rank = w.events[e];
-        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
-            const int x = w.touches[t].cell;
-            if (!w.f.land[x] || w.mark[x] != gen) continue;
-            if (!w.own_done[x] && rank > w.rank_of[x]) {
-                const double moved = w.f.incised_at[x];
-                if (moved > 0.0) w.acc[x] -= (float)(moved * (double)w.p.to_relative);
-                w.own_done[x] = 1;
-            }
-            w.acc[x] += w.touches[t].increment;
-        }
+    if (R == 0) return;   // every thread reads the same R: the grid leaves together
+    for (int t = tid; t < T; t += stride) {
+        const int x = w.touches[t].cell;
+        if (w.f.land[x] && __ldcg(&w.mark[x]) == gen) atomicAdd(&w.cell_cnt[x], 1);
     }
-    for (int i = 0; i < replays; ++i) {
+    grid.sync();
+    if (blockIdx.x == 0) {
+        const int* cnt = w.cell_cnt;
+        const int* rp = w.replay;
+        cta_exclusive_scan([=](int i) { return __ldcg(&cnt[rp[i]]); }, R, w.roff, sh_scan);
+    }
+    grid.sync();
+    for (int t = tid; t < T; t += stride) {
+        const int x = w.touches[t].cell;
+        if (!w.f.land[x] || __ldcg(&w.mark[x]) != gen) continue;
+        const int p = atomicSub(&w.cell_cnt[x], 1) - 1;   // the counts return to 0
+        w.rlist[w.roff[w.cell_d[x]] + p] = t;
+    }
+    grid.sync();
+    for (int i = tid; i < R; i += stride) {
         const int x = w.replay[i];
-        if (!w.own_done[x]) {
-            const double moved = w.f.incised_at[x];
-            if (moved > 0.0) w.acc[x] -= (float)(moved * (double)w.p.to_relative);
+        int* g = w.rlist + w.roff[i];
+        const int m = w.roff[i + 1] - w.roff[i];
+        for (int a = 1; a < m; ++a) {   // log order (groups are short)
+            const int v = g[a];
+            int b = a - 1;
+            while (b >= 0 && g[b] > v) {
+                g[b + 1] = g[b];
+                --b;
+            }
+            g[b + 1] = v;
         }
-        w.f.settled[x] = w.acc[x];
-        w.words[W_REPLAYED]++;
+        const int rx = w.rank_of[x];
+        float acc = w.s0[rx];
+        bool own = false;
+        for (int a = 0; a < m; ++a) {
+            const int t = g[a];
+            if (!own && w.events[event_of(w, t, n)] > rx) {
+                const double moved = w.f.incised_at[x];
+                if (moved > 0.0) acc -= (float)(moved * (double)w.p.to_relative);
+                own = true;
+            }
+            acc += w.touches[t].increment;
+        }
+        if (!own) {
+            const double moved = w.f.incised_at[x];
+            if (moved > 0.0) acc -= (float)(moved * (double)w.p.to_relative);
+        }
+        w.f.settled[x] = acc;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_REPLAYED] += R;
 }
 
 // The round's walk, level by level (steps A, B, C above), in one cooperative launch.
@@ -833,7 +890,16 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 w.ev_touch[n_now] = touch_n;
                 if (pass == 0) refit_gen = ++w.words[W_GEN];
-                const int rc = earliest_mouth_conflict(w, L, n_now, refit_gen);
+                w.words[W_REFITGEN] = refit_gen;
+                w.words[W_BEST] = INT_MAX;
+                w.words[W_TOUCHN] = touch_n;
+            }
+            grid.sync();
+            mouth_conflicts_grid(w, L, n_now);
+            grid.sync();
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                const int best = *(volatile int*)&w.words[W_BEST];
+                const int rc = best == INT_MAX ? -1 : best;
                 if (rc < 0) {
                     w.words[W_DONE] = 1;
                 } else {
@@ -854,7 +920,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         }
         // C: the last repairs, with every deposit of the level in its log.
         if (timer) t0 = now_ns();
-        if (blockIdx.x == 0 && threadIdx.x == 0 && n_now > 0) final_repairs(w, L, n_now, touch_n);
+        if (n_now > 0) final_repairs_grid(w, L, n_now, touch_n, sh_scan);
         grid.sync();
         if (timer) tm[T_REPAIRS] += now_ns() - t0;
     }
@@ -1150,6 +1216,9 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.mark = d_mark;
     w.replay = d_replay;
     w.refit = d_replay + N;
+    CG_BUF(int, d_rlist, ctx, S_DEPRLIST, (size_t)w.touch_cap + (size_t)N + 1);
+    w.rlist = d_rlist;
+    w.roff = d_rlist + w.touch_cap;
     CG_BUF(float, d_acc, ctx, S_DEPACC, N);
     CG_BUF(uint8_t, d_own, ctx, S_DEPOWN, N);
     w.acc = d_acc;
