@@ -48,13 +48,15 @@ using namespace dep;
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kTile = 16;   // a sea lobe's box is scheduled in tiles of kTile x kTile cells
 
 // Control words of a walk.
 enum {
     W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
     W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15,
     W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18,
-    W_REFITGEN = 20, W_BEST = 21, W_TOUCHN = 22, W_NREPLAY = 23, W_NREFIT = 24, W_FGEN = 25, W_WORDS = 28
+    W_REFITGEN = 20, W_BEST = 21, W_TOUCHN = 22, W_NREPLAY = 23, W_NREFIT = 24, W_FGEN = 25, W_NLAKE = 26,
+    W_NSEA = 27, W_SEAWAIT0 = 28, W_SEAWAIT1 = 29, W_WORDS = 32
 };
 
 struct WalkDev {
@@ -87,8 +89,9 @@ struct WalkDev {
     // The mouths of a chunk, `slots` of them at a time.
     int slots, cap, box_words;
     long long* slot_off;    // per slot: its fan's first pool entry
-    int* slot_n;            // per slot: admitted cells
-    int* slot_state;        // per slot: 1 while a lake fan waits to lay, else 0
+    int* slot_n;            // per slot: admitted cells (a lake fan) or box tiles (a sea lobe)
+    int* slot_box;          // per slot, a sea lobe's box in tiles: first column (may be < 0), first row, columns, rows
+    int* slot_state;        // per slot: 1 while a lake fan waits to lay, 2 while a sea lobe waits, 3 once it may run
     double* slot_laid;      // per slot: what its fan laid
     Touch* slot_touch;      // per slot: its fan's deposits, `cap` entries
     int* slot_touch_n;
@@ -106,7 +109,10 @@ struct WalkDev {
     int* cell_cnt;          // per cell: pairs on it (0 outside a chunk's scheduling)
     int* cell_d;            // per cell: its distinct index (valid for the chunk's cells)
     int* blockers;          // per slot: earlier fans still to lay on its cells
-    // The sequential thread's heap (sea lobes, a redone level).
+    // The sea lobes' boxes in tiles of kTile x kTile cells (a tile's schedule id is N + its index), and
+    // each warp's heap (a sea lobe runs on its warp's lane 0): heap_warps heaps of `cap` entries.
+    int tiles_x, tiles_y, box_x, box_y, heap_warps;
+    uint32_t* warp_bits;    // per warp: a sea lobe's visited bits over its box (box_words)
     int* heap_cells;
     float* heap_keys;
     float* heap_pens;
@@ -172,8 +178,9 @@ __device__ bool mouth_live(const WalkDev& w, int c, double carried, int kind) {
     return budget > 0.0 && mouth_accepts(w.p, w.f, kind == SEA, w.f.dirs[c]);
 }
 
-__device__ Heap thread_heap(const WalkDev& w) {
-    return Heap{w.heap_cells, w.heap_keys, w.heap_pens, w.heap_admitted, w.cap, 0, 0};
+__device__ Heap warp_heap(const WalkDev& w, int gwarp) {
+    const size_t o = (size_t)gwarp * w.cap;
+    return Heap{w.heap_cells + o, w.heap_keys + o, w.heap_pens + o, w.heap_admitted + o, w.cap, 0, 0};
 }
 
 // The round's lake mouths and their fans' admissions, ahead of the walk. A lake fan's admission (its
@@ -378,32 +385,6 @@ __device__ void lay_lake_warp(const WalkDev& w, int s, double budget, int lane) 
     if (lane == 0) {
         w.slot_laid[s] = laid;
         w.slot_touch_n[s] = logged;
-    }
-}
-
-// The mouths of events [e0, e1) in rank order on one thread, into the level's log: a lake fan's
-// deposits (already laid in the waves) copied from its slot, a sea lobe run whole (its admission
-// reads what earlier lobes laid). ev_touch[e] receives each event's first entry.
-__device__ void log_and_run_seas(const WalkDev& w, int e0, int e1, int* touch_n) {
-    for (int e = e0; e < e1; ++e) {
-        const int k = w.events[e];
-        w.ev_touch[e] = *touch_n;
-        if (w.ev_kind[k] == LAKE) {
-            const Touch* t = w.slot_touch + (size_t)(e - e0) * w.cap;
-            const int nt = index_ok(w, w.slot_touch_n[e - e0], (long long)w.cap + 1, 10) ? w.slot_touch_n[e - e0] : 0;
-            for (int i = 0; i < nt; ++i) {
-                if (*touch_n < w.touch_cap) w.touches[(*touch_n)++] = t[i];
-                else w.words[W_ERROR] |= 1;
-            }
-        } else {
-            const int c = w.order[k];
-            Heap h = thread_heap(w);
-            TouchLog log{w.touches + *touch_n, w.touch_cap - *touch_n, 0, 0};
-            const int id = ++w.words[W_MOUTH_ID];
-            mouth(w.p, w.f, c, w.ev_carried[k], SEA, w.stamp, id, h, &log);
-            if (log.overflow) w.words[W_ERROR] |= 1;
-            *touch_n += log.count;
-        }
     }
 }
 
@@ -747,7 +728,24 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                             w.slot_n[e - e0] = w.cand_n[ci];
                         }
                     }
-                    w.slot_state[e - e0] = ok ? 1 : 0;
+                    int state = ok ? 1 : 0;
+                    if (w.ev_kind[k] == SEA) {   // the tiles of the box its lobe can read or write
+                        const int apex = w.f.dirs[w.order[k]];
+                        const int acol = apex % w.p.W, arow = apex / w.p.W;
+                        const int c0 = acol - w.box_x, c1 = acol + w.box_x;
+                        const int r0 = max(0, arow - w.box_y), r1 = min(w.p.H - 1, arow + w.box_y);
+                        const int tx0 = c0 >= 0 ? c0 / kTile : -((-c0 + kTile - 1) / kTile);
+                        const int tx1 = c1 >= 0 ? c1 / kTile : -((-c1 + kTile - 1) / kTile);
+                        const int ntx = min(tx1 - tx0 + 1, w.tiles_x), nty = r1 / kTile - r0 / kTile + 1;
+                        int* box = w.slot_box + 4 * (e - e0);
+                        box[0] = tx0;
+                        box[1] = r0 / kTile;
+                        box[2] = ntx;
+                        box[3] = nty;
+                        w.slot_n[e - e0] = ntx * nty;
+                        state = 2;
+                    }
+                    w.slot_state[e - e0] = state;
                     w.slot_touch_n[e - e0] = 0;
                     w.blockers[e - e0] = 0;
                 }
@@ -763,9 +761,17 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     const int* st = w.slot_state;
                     const int* sn = w.slot_n;
                     cta_exclusive_scan([=](int i) { return st[i] ? sn[i] : 0; }, S, w.poff, sh_scan);
+                    int lakes = 0, seas = 0;
+                    for (int base = 0; base < S; base += kThreads) {
+                        const int i = base + (int)threadIdx.x;
+                        lakes += __syncthreads_count(i < S && st[i] == 1);
+                        seas += __syncthreads_count(i < S && st[i] == 2);
+                    }
                     if (threadIdx.x == 0) {
                         w.words[W_PAIRS] = w.poff[S];
                         w.words[W_DISTINCT] = 0;
+                        w.words[W_NLAKE] = lakes;
+                        w.words[W_NSEA] = seas;
                         if (w.poff[S] > w.pair_cap) w.words[W_ERROR] |= 16;
                     }
                 }
@@ -779,8 +785,19 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                         else b = m;
                     }
                     int x = 0;
-                    if (index_ok(w, q - w.poff[a], w.slot_n[a], 12)) x = w.pool_cells[w.slot_off[a] + (q - w.poff[a])];
-                    if (!index_ok(w, x, (long long)w.p.W * w.p.H, 4)) x = 0;
+                    const int k = q - w.poff[a];
+                    if (index_ok(w, k, w.slot_n[a], 12)) {
+                        if (w.slot_state[a] == 2) {   // a sea lobe's tile
+                            const int* box = w.slot_box + 4 * a;
+                            const int ntx = box[2];
+                            int tx = (box[0] + k % ntx) % w.tiles_x;
+                            if (tx < 0) tx += w.tiles_x;
+                            x = w.p.W * w.p.H + (box[1] + k / ntx) * w.tiles_x + tx;
+                        } else {
+                            x = w.pool_cells[w.slot_off[a] + k];
+                        }
+                    }
+                    if (!index_ok(w, x, (long long)w.p.W * w.p.H + (long long)w.tiles_x * w.tiles_y, 4)) x = 0;
                     w.pair_fan[q] = a;
                     w.pair_cell[q] = x;
                     const int pos = atomicAdd(&w.cell_cnt[x], 1);
@@ -840,12 +857,13 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     tm[T_SCHEDULE] += t - t0;
                     t0 = t;
                 }
-                for (int guard = 0; guard <= S; ++guard) {
+                const int n_lakes = *(volatile int*)&w.words[W_NLAKE], n_seas = *(volatile int*)&w.words[W_NSEA];
+                for (int guard = 0; n_lakes > 0 && guard <= S; ++guard) {
                     const int par = guard & 1;
                     if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
                     grid.sync();
                     for (int sl = gwarp; sl < S; sl += nwarps) {
-                        if (!w.slot_state[sl]) continue;
+                        if (w.slot_state[sl] != 1) continue;
                         if (*(volatile int*)&w.blockers[sl] != 0) {
                             if (lane == 0) atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
                             continue;
@@ -870,20 +888,99 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) {
                         w.words[W_ERROR] |= 4;
                         for (int sl = 0; sl < S; ++sl)   // the lowest waiting fan, which nothing should block
-                            if (w.slot_state[sl]) {
+                            if (w.slot_state[sl] == 1) {
                                 check_failed(w, *(volatile int*)&w.blockers[sl], sl, 14);
                                 break;
                             }
                     }
                 }
-                // The chunk's deposits into the level's log in rank order, the sea lobes run in turn.
-                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                if (timer) {
                     const unsigned long long t = now_ns();
                     tm[T_LAKES] += t - t0;
-                    w.words[W_WAVES] += waves;
-                    log_and_run_seas(w, e0, e1, &touch_n);
-                    tm[T_SEAS] += now_ns() - t;
+                    t0 = t;
                 }
+                // The sea lobes (after the lake fans: a lobe touches only sea cells, a fan only land),
+                // a warp each on its lane 0, in rank order wherever their boxes share a tile. A lobe runs
+                // in a wave only if nothing blocked it when the wave began, so whatever an earlier lobe
+                // laid reaches it across a grid barrier. The lowest waiting rank is never blocked.
+                for (int guard = 0; n_seas > 0 && guard <= S; ++guard) {
+                    // This wave's count of waiting lobes; the other word is the last wave's, which a
+                    // slower thread may still be reading.
+                    const int wait_word = W_SEAWAIT0 + (guard & 1);
+                    if (blockIdx.x == 0 && threadIdx.x == 0) w.words[wait_word] = 0;
+                    grid.sync();
+                    for (int sl = gwarp; sl < S; sl += nwarps) {
+                        if (w.slot_state[sl] != 2) continue;
+                        if (*(volatile int*)&w.blockers[sl] == 0) {
+                            if (lane == 0) w.slot_state[sl] = 3;
+                        } else if (lane == 0) {
+                            atomicAdd(&w.words[wait_word], 1);
+                        }
+                    }
+                    grid.sync();
+                    for (int sl = gwarp; sl < S; sl += nwarps) {
+                        if (w.slot_state[sl] != 3) continue;
+                        uint32_t* bits = w.warp_bits + (size_t)gwarp * w.box_words;
+                        for (int j = lane; j < w.box_words; j += 32) bits[j] = 0u;
+                        __syncwarp();
+                        if (lane == 0) {
+                            const int rank = w.events[e0 + sl];
+                            Heap h = warp_heap(w, gwarp);
+                            TouchLog log{w.slot_touch + (size_t)sl * w.cap, w.cap, 0, 0};
+                            int outside = 0;
+                            const int bx = w.box_x, by = w.box_y, W = w.p.W;
+                            mouth_with(w.p, w.f, w.order[rank], w.ev_carried[rank], SEA,
+                                       [=, &outside](const Rim& m) {
+                                           return BoxVisited{bits, W, m.apex_column, m.apex_row, bx, by, &outside};
+                                       },
+                                       h, &log);
+                            if (log.overflow) atomicOr(&w.words[W_ERROR], 1);
+                            if (outside) atomicOr(&w.words[W_ERROR], 2);   // past the box its tiles cover
+                            w.slot_touch_n[sl] = log.count;
+                            w.slot_state[sl] = 0;
+                        }
+                        __syncwarp();
+                        __threadfence();
+                        for (int q = w.poff[sl] + lane; q < min(w.poff[sl + 1], P); q += 32)
+                            if (w.pair_succ[q] >= 0 && index_ok(w, w.pair_succ[q], S, 11))
+                                atomicSub(&w.blockers[w.pair_succ[q]], 1);
+                    }
+                    grid.sync();
+                    ++waves;
+                    if (*(volatile int*)&w.words[wait_word] == 0) break;
+                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
+                }
+                // The chunk's deposits into the level's log in rank order: each event's entries at the
+                // offset of the events before it.
+                if (blockIdx.x == 0) {
+                    const int* tn = w.slot_touch_n;
+                    cta_exclusive_scan([=](int i) { return tn[i]; }, S, w.poff, sh_scan);
+                    if (threadIdx.x == 0) {
+                        w.words[W_WAVES] += waves;
+                        w.words[W_TOUCHN] = touch_n;
+                    }
+                }
+                grid.sync();
+                {
+                    const int base = *(volatile int*)&w.words[W_TOUCHN];
+                    const int total = w.poff[S];
+                    const int room = w.touch_cap - base;
+                    const int copied = total < room ? total : room;
+                    if (total > room && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 1;
+                    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x), stride = (int)(gridDim.x * blockDim.x);
+                    for (int e = tid; e < S; e += stride) w.ev_touch[e0 + e] = base + min(w.poff[e], copied);
+                    for (int q = tid; q < copied; q += stride) {
+                        int a = 0, b = S;
+                        while (b - a > 1) {
+                            const int m = (a + b) >> 1;
+                            if (w.poff[m] <= q) a = m;
+                            else b = m;
+                        }
+                        w.touches[base + q] = w.slot_touch[(size_t)a * w.cap + (q - w.poff[a])];
+                    }
+                    if (blockIdx.x == 0 && threadIdx.x == 0) touch_n = base + copied;
+                }
+                if (timer) tm[T_SEAS] += now_ns() - t0;
                 grid.sync();
             }
             if (timer) t0 = now_ns();
@@ -1022,12 +1119,18 @@ __global__ void k_zero_float(float* __restrict__ a, size_t N) {
 
 }  // namespace
 
+// The laying schedule's ids: the cells, then the sea lobes' box tiles.
+size_t schedule_ids(int W, int H) {
+    return (size_t)W * H + (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+}
+
 cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     const size_t N = (size_t)W * H;
+    const size_t ids = schedule_ids(W, H);
     CG_BUF(float, d_sediment, ctx, S_SEDIMENT, N);
     CG_BUF(int, d_stamp, ctx, S_STAMP, N);
     CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
-    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * N);
+    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * ids);
     CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
     CG_LAUNCH(ctx) k_zero_float<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_sediment, N);
     CG_CHECK_LAUNCH(ctx);
@@ -1035,7 +1138,7 @@ cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     // schedule's per-cell counts start at 0 (each chunk leaves them at 0).
     CG_CUDA(ctx, cudaMemsetAsync(d_stamp, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), ctx->stream));
-    CG_CUDA(ctx, cudaMemsetAsync(d_cellcnt, 0, N * sizeof(int), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_cellcnt, 0, ids * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_words, 0, W_WORDS * sizeof(int), ctx->stream));
     return CG_OK;
 }
@@ -1174,7 +1277,7 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.pool_cells = d_pool_cells;
     w.pool_base = d_pool_base;
     CG_BUF(long long, d_soff, ctx, S_DEPSLOTOFF, S);
-    CG_BUF(int, d_sn, ctx, S_DEPSLOT7, 2 * S);
+    CG_BUF(int, d_sn, ctx, S_DEPSLOT7, 6 * S);
     CG_BUF(double, d_slaid, ctx, S_DEPSLOT8, S);
     CG_BUF(Touch, d_stouch, ctx, S_DEPSLOT9, S * cap);
     CG_BUF(int, d_stn, ctx, S_DEPSLOT10, S);
@@ -1183,7 +1286,12 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     // poff (S + 1), blockers (S + 1), then seven arrays of PC: pair_fan, pair_cell, pair_pos,
     // pair_succ, group, dcell, and doff (its D + 1 <= PC + 1 entries run into the spare 2).
     CG_BUF(int, d_sched, ctx, S_DEPCLAIM, 7 * PC + 2 * S + 4);
-    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * N);
+    const size_t ids = schedule_ids(W, H);
+    CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * ids);
+    w.tiles_x = (W + kTile - 1) / kTile;
+    w.tiles_y = (H + kTile - 1) / kTile;
+    w.box_x = box_bx(w.p);
+    w.box_y = box_by(w.p);
     w.poff = d_sched;
     w.blockers = d_sched + S + 1;
     w.pair_fan = w.blockers + S + 1;
@@ -1194,18 +1302,14 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.dcell = w.group + PC;
     w.doff = w.dcell + PC;
     w.cell_cnt = d_cellcnt;
-    w.cell_d = d_cellcnt + N;
+    w.cell_d = d_cellcnt + ids;
     w.slot_off = d_soff;
     w.slot_n = d_sn;
     w.slot_state = d_sn + S;
+    w.slot_box = d_sn + 2 * S;
     w.slot_laid = d_slaid;
     w.slot_touch = d_stouch;
     w.slot_touch_n = d_stn;
-    CG_BUF(int, d_hc, ctx, S_DEPHEAP, 4 * cap);
-    w.heap_cells = d_hc;
-    w.heap_keys = (float*)(d_hc + cap);
-    w.heap_pens = (float*)(d_hc + 2 * cap);
-    w.heap_admitted = d_hc + 3 * cap;
     CG_BUF(int, d_stamp, ctx, S_STAMP, N);
     w.stamp = d_stamp;
     w.touch_cap = (int)std::min<size_t>(N, (size_t)1 << 26);
@@ -1235,6 +1339,16 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
     CG_BUF(int, d_segc, ctx, S_DEPSEGC, (size_t)cgrid);
     w.seg_count = d_segc;
+    // A heap per warp, for the sea lobes.
+    w.heap_warps = cgrid * (kThreads / 32);
+    const size_t HC = (size_t)w.heap_warps * cap;
+    CG_BUF(int, d_hc, ctx, S_DEPHEAP, 4 * HC);
+    w.heap_cells = d_hc;
+    w.heap_keys = (float*)(d_hc + HC);
+    w.heap_pens = (float*)(d_hc + 2 * HC);
+    w.heap_admitted = d_hc + 3 * HC;
+    CG_BUF(uint32_t, d_wbits, ctx, S_DEPWBITS, (size_t)w.heap_warps * w.box_words);
+    w.warp_bits = d_wbits;
     void* kargs[] = {&w};
     ctx->launches++;
     CG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_deposit_levels, cgrid, kThreads, kargs, 0, sm));
@@ -1247,7 +1361,7 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
         return fail(ctx, CG_INEXACT, "deposition: laying-schedule index check %d failed (value %d, bound %d)",
                     words[W_CHECK_SITE], words[W_CHECK_VALUE], words[W_CHECK_BOUND]);
     if (words[W_ERROR] & 1) return fail(ctx, CG_INEXACT, "deposition: a level's fan deposits overflowed the repair log");
-    if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a lake fan's admission left its box");
+    if (words[W_ERROR] & 2) return fail(ctx, CG_INEXACT, "deposition: a fan's or lobe's admission left its box");
     if (words[W_ERROR] & 4) return fail(ctx, CG_INEXACT, "deposition: the lake fans' laying waves did not converge");
     if (words[W_ERROR] & 8) return fail(ctx, CG_INEXACT, "deposition: a level's mouth refits did not converge");
     if (words[W_ERROR] & 16) return fail(ctx, CG_INEXACT, "deposition: a chunk's fan cells overflowed the schedule");

@@ -607,17 +607,24 @@ CG_HD double lay_admitted(const Params& p, const Fields& f, const Rim& m, bool s
     return laid;
 }
 
-// The whole mouth. Returns what it laid.
-CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, int kind, int* stamp, int id,
-                   Heap& heap, TouchLog* log) {
+// The whole mouth, its admission's visited cells kept by `make_visited(rim)`. Returns what it laid.
+template <class MakeVisited>
+CG_HD double mouth_with(const Params& p, const Fields& f, int cell, double carried, int kind, MakeVisited make_visited,
+                        Heap& heap, TouchLog* log) {
     const bool sea = kind == SEA;
     const double budget = mouth_budget(p, f, cell, carried, kind);
     Rim m;
     mouth_rim(p, f, cell, kind, m);
     if (budget <= 0.0 || !mouth_accepts(p, f, sea, m.apex)) return 0.0;
-    StampVisited visited{stamp, id};
+    auto visited = make_visited(m);
     const int count = admit(p, f, m, sea, visited, heap);
     return lay_admitted(p, f, m, sea, heap.admitted, count, budget, heap, log);
+}
+
+// The whole mouth with the stage's stamps. Returns what it laid.
+CG_HD double mouth(const Params& p, const Fields& f, int cell, double carried, int kind, int* stamp, int id,
+                   Heap& heap, TouchLog* log) {
+    return mouth_with(p, f, cell, carried, kind, [=](const Rim&) { return StampVisited{stamp, id}; }, heap, log);
 }
 
 }  // namespace dep
