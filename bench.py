@@ -50,10 +50,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=8192)
     ap.add_argument("--height", type=int, default=4096)
-    ap.add_argument("--profile", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--profile", type=int, default=0, choices=[0, 1, 2, 3],
                     help="round-tail profile: 0 = P0 (the plain stage), 1 = P1 (P0 with the outlet notch and the "
                          "closing breach), 2 = P2 (P1 with deposition, its lobed and outlined deltas and the "
-                         "closing mouths pass: the reference's default)")
+                         "closing mouths pass), 3 = P3 (P2 with the plate flexure: the reference's default)")
     ap.add_argument("--case", default=None, choices=["thermal", "stage"],
                     help="one public call on the bench world for a profiler, then exit: `thermal` runs the sweeps "
                          "(--passes of them), `stage` the stage with --rounds rounds; prints nothing to parse")
@@ -266,7 +266,8 @@ def run_ours(args):
     # The timed steps also fill cg_round_stats: the library records CUDA events on its stream around
     # each phase of each round, which gives the per-phase device times (and the sweep kernel's
     # launch durations for the roofline) over the timed region itself.
-    PHASES = ("ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_deposit", "ms_relax", "ms_total")
+    PHASES = ("ms_flexure", "ms_cut", "ms_fill", "ms_route", "ms_tree", "ms_incise", "ms_deposit", "ms_relax",
+              "ms_total")
     phase = {k: 0.0 for k in PHASES}
     clocks = ClockSampler(local)
     barrier()
@@ -286,7 +287,7 @@ def run_ours(args):
                       "waves": s.deposit_waves, "ms_deposit": round(s.ms_deposit, 2),
                       "ms_deposit_parts": {k: round(getattr(s, "ms_deposit_" + k), 2)
                                            for k in ("walks", "schedule", "lakes", "seas", "repairs")}}
-                     if args.profile == 2 else {})}
+                     if args.profile >= 2 else {})}
                  for s in stats]
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
@@ -311,7 +312,13 @@ def run_ours(args):
     # and a write of the height field per sweep (8 B per cell-sweep); with two sweeps fused per
     # launch the kernel moves less than that (the traffic key, from ncu).
     from cartogenesis_gb300.perf import roofline_entry
-    roof = roofline_entry(cfg, phase, ROOT, traffic=SWEEP_TRAFFIC_PER_LAUNCH if (W, H) == (8192, 4096) else None)
+    fp64 = None
+    if args.profile >= 3:   # the flexure's transform runs in FP64: its ceiling, measured on this GPU now
+        rate = C.c_double()
+        ctx.check(lib.cg_probe_fp64_rate(ctx.handle, C.byref(rate)))
+        fp64 = rate.value
+    roof = roofline_entry(cfg, phase, ROOT, traffic=SWEEP_TRAFFIC_PER_LAUNCH if (W, H) == (8192, 4096) else None,
+                          fp64_gflops=fp64)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,

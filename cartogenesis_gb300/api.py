@@ -272,6 +272,23 @@ class SeaLevelStage:
         return s.value, is_land, rel, n.value
 
 
+def sequential_sum(values, mask=None, mode=0, ctx=None):
+    """The reference's `var s = 0.0; for (c in cells) s += v[c]` over the cells where mask is set (all when
+    mask is None), v = values (mode 0) or 1 - 0.5 values (mode 1), bit for bit, on the device. Returns
+    (sum, counts): blocks of 8192 values taken whole, pieces of 1024 reduced, pieces added one by one."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(values, dtype=np.float32).ravel()
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).ravel()
+    if m is not None and m.size != x.size:
+        raise ValueError("mask and values differ in size")
+    s = C.c_double()
+    counts = np.zeros(3, np.int64)
+    with ctx.lock:
+        ctx.check(ctx.lib.cg_sequential_sum(ctx.handle, P(x) if x.size else None, None if m is None else P(m), mode,
+                                            x.size, C.byref(s), P(counts)))
+    return s.value, counts
+
+
 class Isostasy:
     class Flexure:
         """Isostasy.Flexure (P/Isostasy.kt:277-411): the plate's bend under a load, on the device."""

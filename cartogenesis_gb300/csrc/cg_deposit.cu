@@ -76,6 +76,7 @@ struct WalkDev {
     int8_t* ev_kind;        // per rank: SEA or LAKE
     int* seg_events;        // per rank: listed ranks, compacted within each CTA's segment
     int* seg_count;         // per CTA
+    int* seg_off;           // per CTA + 1: its listed mouths' first place in `events`
     int* events;            // the level's listed ranks, dense, in rank order
     // The round's lake fans, admitted before the walk (k_admit_lakes): per candidate mouth cell its
     // admitted cells sorted by distance and each one's level less its terrain, in a pool.
@@ -685,15 +686,14 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
         }
         if (threadIdx.x == 0) w.seg_count[blockIdx.x] = block_base;
         grid.sync();
-        // The listed mouths, dense and in rank order.
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            int n = 0;
-            for (int b = 0; b < (int)gridDim.x; ++b) {
-                const int b_lo = lo + b * seg;
-                for (int i = 0; i < w.seg_count[b]; ++i) w.events[n++] = w.seg_events[b_lo + i];
-            }
-            w.words[W_EVENTS] = n;
+        // The listed mouths, dense and in rank order: each CTA's segment at the offset of the ones before.
+        if (blockIdx.x == 0) {
+            const int* sc = w.seg_count;
+            cta_exclusive_scan([=](int i) { return sc[i]; }, (int)gridDim.x, w.seg_off, sh_scan);
+            if (threadIdx.x == 0) w.words[W_EVENTS] = w.seg_off[gridDim.x];
         }
+        grid.sync();
+        for (int i = threadIdx.x; i < block_base; i += blockDim.x) w.events[w.seg_off[blockIdx.x] + i] = w.seg_events[s_lo + i];
         grid.sync();
         if (timer) tm[T_WALKS] += now_ns() - t0;
         const int n = *(volatile int*)&w.words[W_EVENTS];
@@ -1337,8 +1337,9 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "deposition kernel cannot be resident");
     const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
-    CG_BUF(int, d_segc, ctx, S_DEPSEGC, (size_t)cgrid);
+    CG_BUF(int, d_segc, ctx, S_DEPSEGC, 2 * (size_t)cgrid + 1);
     w.seg_count = d_segc;
+    w.seg_off = d_segc + cgrid;
     // A heap per warp, for the sea lobes.
     w.heap_warps = cgrid * (kThreads / 32);
     const size_t HC = (size_t)w.heap_warps * cap;

@@ -12,8 +12,8 @@
 // is applied in the forward column pass and the inverse's 1 / (W 2H) in the inverse column pass, each
 // after the pass's last butterfly, where the reference applies them.
 //
-// The load's mean is the reference's sequential double sum in cell order; one thread adds while the
-// CTA stages the next chunk. Everything else is elementwise or per line.
+// The load's mean is the reference's sequential double sum in cell order (seq_sum_dev, bit for bit).
+// Everything else is elementwise or per line.
 #include <cmath>
 #include <vector>
 
@@ -79,24 +79,6 @@ __global__ void k_flex_load(const float* __restrict__ work, const float* __restr
         column = __fadd_rn(column, sed ? __fmul_rn(sed[i], mpf) : 0.0f);
         load[i] = __fmul_rn(__fmul_rn(column, density), gravity);
     }
-}
-
-// deflectionMetres' mean (Isostasy.kt:337-339): loadSum += load[c] in cell order, then / cells. One
-// CTA: the threads stage chunks in shared memory (two buffers) and one thread adds them in order.
-__global__ void __launch_bounds__(1024) k_flex_mean(const float* __restrict__ load, size_t N, double* __restrict__ mean) {
-    constexpr size_t C = 4096;
-    __shared__ float chunk[2][C];
-    double s = 0.0;
-    for (size_t base = 0; base < N; base += C) {
-        const int b = (int)((base / C) & 1);
-        for (size_t i = threadIdx.x; i < C && base + i < N; i += blockDim.x) chunk[b][i] = load[base + i];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const size_t n = N - base < C ? N - base : C;
-            for (size_t i = 0; i < n; ++i) s = __dadd_rn(s, (double)chunk[b][i]);
-        }
-    }
-    if (threadIdx.x == 0) *mean = __ddiv_rn(s, (double)N);
 }
 
 enum { SRC_GRID = 0, SRC_LOAD = 1 };
@@ -258,8 +240,8 @@ cg_status flexure_dev(cg_ctx* ctx, const cg_erosion_params& p, const float* d_lo
     CG_BUF(double2, d_b, ctx, S_FX_B, N2);
     CG_BUF(double, d_mean, ctx, S_FX_MEAN, 1);
     const FlexConsts k = flex_consts(p);
-    CG_LAUNCH(ctx) k_flex_mean<<<1, 1024, 0, sm>>>(d_load, N, d_mean);
-    CG_CHECK_LAUNCH(ctx);
+    // deflectionMetres' mean (Isostasy.kt:337-339): loadSum += load[c] in cell order, then / cells.
+    CG_TRY_ST(seq_sum_dev(ctx, d_load, nullptr, 0, N, (double)N, d_mean, nullptr));
     LineArgs a{};
     a.k = k;
     a.W = W;

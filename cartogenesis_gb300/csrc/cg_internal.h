@@ -146,6 +146,13 @@ struct DepositCounts {
     // waves, sea lobes and logs, mouth refits and last repairs.
     double ms_walks, ms_schedule, ms_lakes, ms_seas, ms_repairs;
 };
+// The reference's sequential double sum (`s += v` in cell order, s from 0.0) of v = x (mode 0) or
+// v = 1 - 0.5 x (mode 1) over the cells of d_mask (all cells when null), into *d_out on the device,
+// divided by `divisor` unless it is 0; bit for bit, in parallel (cg_seqsum.cu). d_counts (3, may be
+// null) receives how the sum went: blocks of 8192 values taken whole, pieces of 1024 reduced on the
+// spot, pieces added one value at a time.
+cg_status seq_sum_dev(cg_ctx* ctx, const float* d_x, const uint8_t* d_mask, int mode, size_t n, double divisor,
+                      double* d_out, long long* d_counts);
 // The plate flexure of profile P3 (cg_flexure.cu). flexure_check refuses grids whose transform lines
 // do not fit a CTA's shared memory; flexure_stage_begin_dev records the field before the rounds and
 // clears the bend (and the uplift record when the world has uplift); flexure_uplifted_dev is that

@@ -40,35 +40,6 @@ __global__ void k_unit_weights(const float* __restrict__ rock, size_t N, float* 
     }
 }
 
-// The reference's sequential double sum over land cells, in cell order (HydraulicErosion.kt:557,
-// 476-478): one CTA; the threads stage chunks in shared memory and one thread adds them in order.
-// mode 0: sum of x; mode 1: sum of (1 - 0.5 x).
-__global__ void __launch_bounds__(1024) k_seq_land_sum(const float* __restrict__ x, const uint8_t* __restrict__ land,
-                                                       size_t N, int mode, double* __restrict__ out) {
-    __shared__ float chunk[2][4096];
-    __shared__ uint8_t lchunk[2][4096];
-    double s = 0.0;
-    const size_t C = 4096;
-    for (size_t base = 0; base < N; base += C) {
-        int b = (int)((base / C) & 1);
-        for (size_t i = threadIdx.x; i < C && base + i < N; i += blockDim.x) {
-            chunk[b][i] = x[base + i];
-            lchunk[b][i] = land[base + i];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            size_t n = N - base < C ? N - base : C;
-            for (size_t i = 0; i < n; ++i) {
-                if (!lchunk[b][i]) continue;
-                float v = chunk[b][i];
-                if (mode == 1) v = __fsub_rn(1.0f, __fmul_rn(0.5f, v));
-                s = __dadd_rn(s, (double)v);
-            }
-        }
-    }
-    if (threadIdx.x == 0) *out = s;
-}
-
 // weights[c] = rain[c] / mean, or 0 when mean <= 0 (HydraulicErosion.kt:558-567).
 __global__ void k_normalise(const float* __restrict__ rain, const double* __restrict__ sum, int land_cells, size_t N,
                             float* __restrict__ w) {
@@ -132,7 +103,7 @@ cg_status runoff_weights_dev(cg_ctx* ctx, int W, int H, const float* d_rain, con
     const int grid = ctx->num_sms * 8;
     if (d_rain) {
         CG_BUF(double, d_sum, ctx, S_CG3, 2);
-        CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, ctx->stream>>>(d_rain, d_land, N, 0, d_sum);
+        CG_TRY(seq_sum_dev(ctx, d_rain, d_land, 0, N, 0.0, d_sum, nullptr));
         CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, ctx->stream>>>(d_rain, d_sum, land_cells, N, d_runoff);
     } else {
         CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, ctx->stream>>>(d_runoff, N, 1.0f);
@@ -262,13 +233,13 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             CG_LAUNCH(ctx) k_unit_weights<<<grid, 256, 0, sm>>>(d_rock, N, d_runoff, d_erod);
         } else {
             if (d_rain) {
-                CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_rain, d_land, N, 0, d_sum);
+                CG_TRY(seq_sum_dev(ctx, d_rain, d_land, 0, N, 0.0, d_sum, nullptr));
                 CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, sm>>>(d_rain, d_sum, land_cells, N, d_runoff);
             } else {
                 CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_runoff, N, 1.0f);
             }
             if (p.shield_cut && d_veg) {
-                CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_veg, d_land, N, 1, d_sum + 1);
+                CG_TRY(seq_sum_dev(ctx, d_veg, d_land, 1, N, 0.0, d_sum + 1, nullptr));
                 CG_LAUNCH(ctx) k_shield<<<grid, 256, 0, sm>>>(d_veg, d_sum + 1, land_cells, d_rock, N, d_erod);
             } else {
                 CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_erod, N, 1.0f);
@@ -342,7 +313,7 @@ cg_status stage_rounds_dev(cg_ctx* ctx, StageRun& run, int end_round, cg_round_s
             run.land_cells = closing_land;
             if (closing_land > 0) {
                 if (d_rain) {
-                    CG_LAUNCH(ctx) k_seq_land_sum<<<1, 1024, 0, sm>>>(d_rain, d_land, N, 0, d_sum);
+                    CG_TRY(seq_sum_dev(ctx, d_rain, d_land, 0, N, 0.0, d_sum, nullptr));
                     CG_LAUNCH(ctx) k_normalise<<<grid, 256, 0, sm>>>(d_rain, d_sum, closing_land, N, d_runoff);
                 } else {
                     CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, sm>>>(d_runoff, N, 1.0f);

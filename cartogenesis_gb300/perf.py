@@ -10,6 +10,9 @@ B = 4 bytes per height (the REF32 field):
   deposit (P2's walk: routing, cut and load inputs 33, incisedAt 8, load 8, settled and sediment
            read and written 16, hand-off 8, order and rank 8)     81
   relax (s sweeps, a read and a write of the field each: 2B s)   8 s
+The plate flexure (P3) is bound by the FP64 pipe instead: its two 2D transforms over the W x 2H
+mirrored grid take 5 flops per point per radix-2 stage, 20 (log2 W + log2 2H) flops per map cell
+and round, against the FP64 rate the bench measures on the GPU it runs on (cg_probe_fp64_rate).
 The peak is the measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json, written by
 the pool's driver), else the recipe's fallback of 6.8 TB/s.
 """
@@ -27,6 +30,7 @@ PHASE_KERNELS = {
     "ms_deposit": "k_round_begin, k_rank_of, k_level_bounds, k_deposit_levels, k_settle, k_mouths_levels "
                   "(last round: the closing breach's cut, fill, routing and notch)",
     "ms_relax": "thermal_sweeps_kernel",
+    "ms_flexure": "k_uplift, k_flex_load, k_flex_mean, k_fft_lines, k_transpose, k_flex_apply",
 }
 FALLBACK_HBM_GBS = 6800.0
 
@@ -51,7 +55,11 @@ def sweep_launches(sweeps):
     return (sweeps + 1) // 2
 
 
-def roofline_entry(cfg, phase_ms_per_stage, root, traffic=None):
+def flexure_flops_per_cell(W, H):
+    return 20.0 * ((W.bit_length() - 1) + ((2 * H).bit_length() - 1))
+
+
+def roofline_entry(cfg, phase_ms_per_stage, root, traffic=None, fp64_gflops=None):
     """The roofline object for the dominant kernel, the thermal sweeps of the relax phase.
 
     phase_ms_per_stage maps ms_* to that phase's device milliseconds summed over a stage's rounds
@@ -75,6 +83,13 @@ def roofline_entry(cfg, phase_ms_per_stage, root, traffic=None):
     phases = {}
     for k, v in phase_ms_per_stage.items():
         if k == "ms_total" or v <= 0:
+            continue
+        if k == "ms_flexure":
+            gfs = flexure_flops_per_cell(p.width, p.height) * N / (v / rounds / 1000.0) / 1e9
+            phases["flexure"] = {"achieved": round(gfs, 1), "unit": "GFLOP/s (FP64)",
+                                 "frac": round(gfs / fp64_gflops, 4) if fp64_gflops else None,
+                                 "peak": round(fp64_gflops, 1) if fp64_gflops else None,
+                                 "ms_per_round": round(v / rounds, 3), "kernels": PHASE_KERNELS[k]}
             continue
         gbs = phase_bytes_per_cell(k, per_round) * N / (v / rounds / 1000.0) / 1e9
         phases[k[3:]] = {"achieved": round(gbs, 1), "frac": round(gbs / peak, 4),

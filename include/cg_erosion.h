@@ -367,6 +367,21 @@ cg_status cg_sea_level_cut(cg_ctx* ctx, const cg_erosion_params* params, const f
 cg_status cg_flexure_deflection(cg_ctx* ctx, const cg_erosion_params* params, const float* load,
                                 float* deflection, double* rigidity, double* restoring);
 
+/*
+ * The reference's sequential double sum of a float field, `var s = 0.0; for (c in cells) s += v[c]`,
+ * bit for bit: the sums behind normaliseOverLand's rain mean and shieldingOverLand's cover mean
+ * (.../pipeline/HydraulicErosion.kt:476-486, 557-567; mode 1 sums 1 - 0.5 x, the cover's factor) and
+ * deflectionMetres' load mean (.../pipeline/Isostasy.kt:337-339). Cells with mask[c] == 0 are skipped
+ * (mask may be NULL). Host buffers. The stage computes these sums on the device the same way; this entry
+ * point exposes the primitive on its own. The sum is not a chain of n double additions: blocks of values
+ * are reduced in parallel to integer walks inside the running sum's binade (the one state a walk carries
+ * is the parity of the sum's mantissa, which decides ties), and only where the sum crosses a binade are
+ * values added one at a time. `counts` (3 entries, may be NULL) receives blocks of 8192 values taken
+ * whole, pieces of 1024 reduced on the spot, and pieces added one value at a time.
+ */
+cg_status cg_sequential_sum(cg_ctx* ctx, const float* x, const uint8_t* mask, int32_t mode, int64_t n,
+                            double* sum, int64_t* counts);
+
 /* FlowRouting.fillDepressions (.../pipeline/FlowRouting.kt:52-111). */
 cg_status cg_fill_depressions(cg_ctx* ctx, int32_t width, int32_t height, const uint8_t* is_land,
                               const float* relative, float* filled, int64_t* ties,
