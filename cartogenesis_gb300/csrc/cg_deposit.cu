@@ -49,14 +49,16 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTile = 16;   // a sea lobe's box is scheduled in tiles of kTile x kTile cells
+constexpr int kNoTouch = 0x7F7F7F7F;   // `first`'s resting value (a byte-wise memset)
+constexpr long long kSpinLimit = 1LL << 24;   // a lake fan's wait for its turn, in polls (seconds)
 
 // Control words of a walk.
 enum {
-    W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
+    W_EVENTS = 0, W_ERROR = 1, W_MOUTH_ID = 2, W_GEN = 3, W_ABORT = 4, W_REPLAYED = 5, W_WAVEBASE = 6, W_WAVES = 7,
     W_WAIT0 = 8, W_WAIT1 = 9, W_REFITTED = 10, W_ESTART = 11, W_DONE = 12, W_RELAID = 13, W_PAIRS = 14, W_DISTINCT = 15,
-    W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18,
+    W_CHECK_SITE = 16, W_CHECK_VALUE = 17, W_CHECK_BOUND = 18, W_NDONOR = 19,
     W_REFITGEN = 20, W_BEST = 21, W_TOUCHN = 22, W_NREPLAY = 23, W_NREFIT = 24, W_FGEN = 25, W_NLAKE = 26,
-    W_NSEA = 27, W_SEAWAIT0 = 28, W_SEAWAIT1 = 29, W_WORDS = 32
+    W_NSEA = 27, W_SEAWAIT0 = 28, W_SEAWAIT1 = 29, W_CUT = 30, W_RC = 31, W_WORDS = 32
 };
 
 struct WalkDev {
@@ -127,6 +129,8 @@ struct WalkDev {
     int* replay;            // cells to replay
     int* refit;             // cells to refit
     int* rlist;             // the log's entries on the cells to replay, grouped by cell (touch_cap)
+    int* first;             // per cell: its earliest log entry being undone (kNoTouch at rest)
+    int* touch_ev;          // per level-log entry: its event's index
     int* roff;              // per cell to replay + 1: its group's first entry
     float* acc;             // per cell: a replayed settled height
     uint8_t* own_done;      // per cell: the replay has taken the cell's own subtraction
@@ -400,23 +404,19 @@ __device__ __forceinline__ int kind_of(const WalkDev& w, int c) {
 
 // Cell d's settled height as the reference's walk shows it to the cell of rank `rc` of this level:
 // its value before the level's fans, plus the increments of the level's fans ranked before rc, in
-// order. False when no fan of the level touched d (its current value is then the answer).
-__device__ bool settled_as_of(const WalkDev& w, int d, int rc, int n, float* out) {
-    bool seen = false;
-    float v = 0.0f;
-    for (int e = 0; e < n; ++e) {
-        const int rank = w.events[e];
-        for (int t = w.ev_touch[e]; t < w.ev_touch[e + 1]; ++t) {
-            if (w.touches[t].cell != d) continue;
-            if (!seen) {
-                seen = true;
-                v = w.touches[t].settled_before;
-            }
-            if (rank < rc) v += w.touches[t].increment;
-        }
-    }
+// order. False when no fan of the level touched d (its current value is then the answer). Reads d's
+// group of log entries (in log order), which the last repairs build for the donors of the cells they
+// refit.
+__device__ bool settled_as_of(const WalkDev& w, int d, int rc, float* out) {
+    const int i = w.cell_d[d];
+    const int* g = w.rlist + w.roff[i];
+    const int m = w.roff[i + 1] - w.roff[i];
+    if (m == 0) return false;
+    float v = w.touches[g[0]].settled_before;
+    for (int a = 0; a < m; ++a)
+        if (w.events[w.touch_ev[g[a]]] < rc) v += w.touches[g[a]].increment;
     *out = v;
-    return seen;
+    return true;
 }
 
 // A dry cell of the level whose headroom read a donor that an earlier fan of the level raised, when
@@ -425,7 +425,7 @@ __device__ bool settled_as_of(const WalkDev& w, int d, int rc, int n, float* out
 // rank. Nothing else of the level reads such a cell (fans touch only ponded land and sea, and cells of
 // one level never read one another), so the fix is local. Returns false (a whole redo is needed)
 // where the cell has a mouth, whose fan would change with it.
-__device__ bool refit_cell(const WalkDev& w, int c, int n) {
+__device__ bool refit_cell(const WalkDev& w, int c) {
     if (kind_of(w, c) != ON) return false;
     const int rc = w.rank_of[c];
     w.f.settled[c] = w.s0[rc];
@@ -442,7 +442,7 @@ __device__ bool refit_cell(const WalkDev& w, int c, int n) {
             const int d = nr * W + ((col + cs) & (W - 1));
             if (w.f.dirs[d] != c) continue;
             float v;
-            if (settled_as_of(w, d, rc, n, &v)) {
+            if (settled_as_of(w, d, rc, &v)) {
                 patched[np] = d;
                 kept[np++] = w.f.settled[d];
                 w.f.settled[d] = v;
@@ -458,21 +458,13 @@ __device__ bool refit_cell(const WalkDev& w, int c, int n) {
     return true;
 }
 
-// Makes the walk the reference's again from rank rc (the earliest mouth conflict): every fan ranked
-// at or after rc undone, latest first, and the level's log cut back to before them; the conflicted
-// cell's own walk taken again on the state the reference's walk shows it (its own state before the
-// walk, and its donors as every fan ranked before it left them, which is now the current state); its
-// mouth listed or unlisted as its new load decides. Returns the index of the first event to lay
-// again; *n and *touch_n are updated.
-__device__ int refit_mouth_cell(const WalkDev& w, int rc, int refit_gen, int* n, int* touch_n) {
-    int ec = 0;
-    while (ec < *n && w.events[ec] < rc) ++ec;
-    const int cut = ec < *n ? w.ev_touch[ec] : *touch_n;
-    for (int t = *touch_n - 1; t >= cut; --t) {
-        w.f.settled[w.touches[t].cell] = w.touches[t].settled_before;
-        w.f.sediment[w.touches[t].cell] = w.touches[t].sediment_before;
-    }
-    *touch_n = cut;
+// The walk made the reference's again from rank rc (the earliest mouth conflict), once every fan
+// ranked at or after rc is undone (undo_from_grid) and the level's log cut back to before them: the
+// conflicted cell's own walk taken again on the state the reference's walk shows it (its own state
+// before the walk, and its donors as every fan ranked before it left them, which is now the current
+// state); its mouth listed or unlisted as its new load decides. ec is the index of the first event
+// ranked at or after rc, the first to lay again; *n is updated.
+__device__ void refit_mouth_cell(const WalkDev& w, int rc, int ec, int refit_gen, int* n) {
     const int c = w.order[rc];
     w.f.settled[c] = w.s0[rc];
     w.f.sediment[c] = w.d0[rc];
@@ -497,20 +489,27 @@ __device__ int refit_mouth_cell(const WalkDev& w, int rc, int refit_gen, int* n,
         for (int e = ec; e + 1 < *n; ++e) w.events[e] = w.events[e + 1];
         --*n;
     }
-    return ec;
 }
 
-// The level-log entry t's event: the last e with ev_touch[e] <= t (events without entries share
-// their successor's offset).
-__device__ __forceinline__ int event_of(const WalkDev& w, int t, int n) {
-    int a = 0, b = n;
-    while (b - a > 1) {
-        const int m = (a + b) >> 1;
-        if (w.ev_touch[m] <= t) a = m;
-        else b = m;
+// The level log's entries [cut, T) undone over the grid, called by every thread: a cell takes back
+// the state before its earliest entry in the range (what undoing the entries latest first leaves).
+// `first` holds kNoTouch outside this call.
+__device__ void undo_from_grid(const WalkDev& w, int cut, int T) {
+    cgr::grid_group grid = cgr::this_grid();
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x), stride = (int)(gridDim.x * blockDim.x);
+    for (int t = cut + tid; t < T; t += stride) atomicMin(&w.first[w.touches[t].cell], t);
+    grid.sync();
+    for (int t = cut + tid; t < T; t += stride) {
+        const Touch tt = w.touches[t];
+        if (__ldcg(&w.first[tt.cell]) != t) continue;
+        w.f.settled[tt.cell] = tt.settled_before;
+        w.f.sediment[tt.cell] = tt.sediment_before;
+        w.first[tt.cell] = kNoTouch;
     }
-    return a;
 }
+
+// The level-log entry t's event (recorded as the log is assembled).
+__device__ __forceinline__ int event_of(const WalkDev& w, int t, int) { return w.touch_ev[t]; }
 
 // The earliest cell of level L, ranked after a fan of the level that raised one of its donors, whose
 // headroom read that donor and which has a mouth of its own (its step ends at the sea or in a lake):
@@ -527,9 +526,8 @@ __device__ void mouth_conflicts_grid(const WalkDev& w, int L, int n) {
         const int rr = w.f.dirs[x];
         if (rr < 0 || !w.f.land[rr] || level_of_cell(w, rr) != L) continue;
         const int r = w.rank_of[rr];
-        if (r >= best) continue;
-        const int rank = w.events[event_of(w, t, n)];
-        if (r > rank && w.used[rr] && kind_of(w, rr) != ON && w.mark[rr] != refit_gen) best = r;
+        if (r >= best || !w.used[rr] || w.mark[rr] == refit_gen || kind_of(w, rr) == ON) continue;
+        if (r > w.events[event_of(w, t, n)]) best = r;
     }
     if (best != INT_MAX) atomicMin(&w.words[W_BEST], best);
 }
@@ -553,6 +551,7 @@ __device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, 
         w.words[W_FGEN] = ++w.words[W_GEN];
         w.words[W_NREPLAY] = 0;
         w.words[W_NREFIT] = 0;
+        w.words[W_NDONOR] = 0;
     }
     grid.sync();
     const int T = *(volatile int*)&w.words[W_TOUCHN];
@@ -575,11 +574,27 @@ __device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, 
     }
     grid.sync();
     const int R = *(volatile int*)&w.words[W_NREPLAY], F = *(volatile int*)&w.words[W_NREFIT];
+    if (R == 0 && F == 0) return;   // every thread reads the same counts: the grid leaves together
+    // The refitted cells' donors join the groups, after the cells to replay (a donor sits on a lower
+    // level, so it is never one of those, and it has one receiver, so it joins once).
+    const int W = w.p.W, H = w.p.H;
     for (int j = tid; j < F; j += stride) {
-        refit_cell(w, w.refit[j], n);
-        atomicAdd(&w.words[W_REFITTED], 1);
+        const int c = w.refit[j], col = c % W, row = c / W;
+        for (int rs = -1; rs <= 1; ++rs) {
+            const int nr = row + rs;
+            if (nr < 0 || nr >= H) continue;
+            for (int cs = -1; cs <= 1; ++cs) {
+                if (rs == 0 && cs == 0) continue;
+                const int d = nr * W + ((col + cs) & (W - 1));
+                if (w.f.dirs[d] != c || atomicExch(&w.mark[d], gen) == gen) continue;
+                const int k = R + atomicAdd(&w.words[W_NDONOR], 1);
+                w.replay[k] = d;
+                w.cell_d[d] = k;
+            }
+        }
     }
-    if (R == 0) return;   // every thread reads the same R: the grid leaves together
+    grid.sync();
+    const int G = R + *(volatile int*)&w.words[W_NDONOR];
     for (int t = tid; t < T; t += stride) {
         const int x = w.touches[t].cell;
         if (w.f.land[x] && __ldcg(&w.mark[x]) == gen) atomicAdd(&w.cell_cnt[x], 1);
@@ -588,7 +603,7 @@ __device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, 
     if (blockIdx.x == 0) {
         const int* cnt = w.cell_cnt;
         const int* rp = w.replay;
-        cta_exclusive_scan([=](int i) { return __ldcg(&cnt[rp[i]]); }, R, w.roff, sh_scan);
+        cta_exclusive_scan([=](int i) { return __ldcg(&cnt[rp[i]]); }, G, w.roff, sh_scan);
     }
     grid.sync();
     for (int t = tid; t < T; t += stride) {
@@ -598,11 +613,10 @@ __device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, 
         w.rlist[w.roff[w.cell_d[x]] + p] = t;
     }
     grid.sync();
-    for (int i = tid; i < R; i += stride) {
-        const int x = w.replay[i];
+    for (int i = tid; i < G; i += stride) {   // each group back in log order (groups are short)
         int* g = w.rlist + w.roff[i];
         const int m = w.roff[i + 1] - w.roff[i];
-        for (int a = 1; a < m; ++a) {   // log order (groups are short)
+        for (int a = 1; a < m; ++a) {
             const int v = g[a];
             int b = a - 1;
             while (b >= 0 && g[b] > v) {
@@ -611,6 +625,16 @@ __device__ void final_repairs_grid(const WalkDev& w, int L, int n, int touch_n, 
             }
             g[b + 1] = v;
         }
+    }
+    grid.sync();
+    for (int j = tid; j < F; j += stride) {
+        refit_cell(w, w.refit[j]);
+        atomicAdd(&w.words[W_REFITTED], 1);
+    }
+    for (int i = tid; i < R; i += stride) {
+        const int x = w.replay[i];
+        const int* g = w.rlist + w.roff[i];
+        const int m = w.roff[i + 1] - w.roff[i];
         const int rx = w.rank_of[x];
         float acc = w.s0[rx];
         bool own = false;
@@ -858,16 +882,28 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     t0 = t;
                 }
                 const int n_lakes = *(volatile int*)&w.words[W_NLAKE], n_seas = *(volatile int*)&w.words[W_NSEA];
-                for (int guard = 0; n_lakes > 0 && guard <= S; ++guard) {
-                    const int par = guard & 1;
-                    if (blockIdx.x == 0 && threadIdx.x == 0) w.words[W_WAIT0 + (par ^ 1)] = 0;
-                    grid.sync();
+                // A fan's warp waits for its count to reach 0 (the fans before it on its cells laid), inside
+                // the cooperative launch: every CTA is resident, each warp takes its slots in rank order and
+                // a count only waits on lower ranks, so the lowest waiting fan always runs. The wait is
+                // bounded; a warp that gives up raises the abort word, which every other waiter also
+                // heeds, and the walk reports the error.
+                if (n_lakes > 0) {
                     for (int sl = gwarp; sl < S; sl += nwarps) {
                         if (w.slot_state[sl] != 1) continue;
-                        if (*(volatile int*)&w.blockers[sl] != 0) {
-                            if (lane == 0) atomicAdd(&w.words[W_WAIT0 + (par ^ 1)], 1);
-                            continue;
+                        int go = 1;
+                        if (lane == 0) {
+                            long long spins = 0;
+                            while (*(volatile int*)&w.blockers[sl] != 0) {
+                                if (*(volatile int*)&w.words[W_ABORT] || ++spins > kSpinLimit) {
+                                    atomicOr(&w.words[W_ERROR], 4);
+                                    atomicExch(&w.words[W_ABORT], 1);
+                                    go = 0;
+                                    break;
+                                }
+                                __nanosleep(64);
+                            }
                         }
+                        if (!__shfl_sync(0xFFFFFFFFu, go, 0)) continue;
                         __threadfence();
                         const int rank = w.events[e0 + sl];
                         const int c = w.order[rank];
@@ -884,15 +920,6 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     }
                     grid.sync();
                     ++waves;
-                    if (*(volatile int*)&w.words[W_WAIT0 + (par ^ 1)] == 0) break;
-                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) {
-                        w.words[W_ERROR] |= 4;
-                        for (int sl = 0; sl < S; ++sl)   // the lowest waiting fan, which nothing should block
-                            if (w.slot_state[sl] == 1) {
-                                check_failed(w, *(volatile int*)&w.blockers[sl], sl, 14);
-                                break;
-                            }
-                    }
                 }
                 if (timer) {
                     const unsigned long long t = now_ns();
@@ -977,6 +1004,7 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                             else b = m;
                         }
                         w.touches[base + q] = w.slot_touch[(size_t)a * w.cap + (q - w.poff[a])];
+                        w.touch_ev[base + q] = e0 + a;
                     }
                     if (blockIdx.x == 0 && threadIdx.x == 0) touch_n = base + copied;
                 }
@@ -1001,10 +1029,29 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     w.words[W_DONE] = 1;
                 } else {
                     if (pass == passes) w.words[W_ERROR] |= 8;
-                    int nn = n_now;
-                    w.words[W_ESTART] = refit_mouth_cell(w, rc, refit_gen, &nn, &touch_n);
-                    w.words[W_EVENTS] = nn;
+                    int a = 0, b = n_now;   // the first event ranked at or after rc (events are in rank order)
+                    while (a < b) {
+                        const int m = (a + b) >> 1;
+                        if (w.events[m] < rc) a = m + 1;
+                        else b = m;
+                    }
+                    w.words[W_ESTART] = a;
+                    w.words[W_CUT] = a < n_now ? w.ev_touch[a] : touch_n;
+                    w.words[W_RC] = rc;
                     w.words[W_DONE] = 0;
+                }
+            }
+            grid.sync();
+            if (!*(volatile int*)&w.words[W_DONE]) {
+                // Every fan ranked at or after rc undone, the log cut back to before them, the cell refitted.
+                const int cut = *(volatile int*)&w.words[W_CUT];
+                undo_from_grid(w, cut, *(volatile int*)&w.words[W_TOUCHN]);
+                grid.sync();
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    touch_n = cut;
+                    int nn = n_now;
+                    refit_mouth_cell(w, w.words[W_RC], w.words[W_ESTART], refit_gen, &nn);
+                    w.words[W_EVENTS] = nn;
                     w.words[W_RELAID]++;
                 }
             }
@@ -1131,6 +1178,7 @@ cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     CG_BUF(int, d_stamp, ctx, S_STAMP, N);
     CG_BUF(int, d_mark, ctx, S_DEPMARK, N);
     CG_BUF(int, d_cellcnt, ctx, S_DEPCELLCNT, 2 * ids);
+    CG_BUF(int, d_first, ctx, S_DEPFIRST, N);
     CG_BUF(int, d_words, ctx, S_DEPWORDS, W_WORDS);
     CG_LAUNCH(ctx) k_zero_float<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(d_sediment, N);
     CG_CHECK_LAUNCH(ctx);
@@ -1139,6 +1187,7 @@ cg_status deposit_stage_reset_dev(cg_ctx* ctx, int W, int H) {
     CG_CUDA(ctx, cudaMemsetAsync(d_stamp, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_mark, 0, N * sizeof(int), ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(d_cellcnt, 0, ids * sizeof(int), ctx->stream));
+    CG_CUDA(ctx, cudaMemsetAsync(d_first, 0x7F, N * sizeof(int), ctx->stream));   // kNoTouch
     CG_CUDA(ctx, cudaMemsetAsync(d_words, 0, W_WORDS * sizeof(int), ctx->stream));
     return CG_OK;
 }
@@ -1322,6 +1371,10 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     w.refit = d_replay + N;
     CG_BUF(int, d_rlist, ctx, S_DEPRLIST, (size_t)w.touch_cap + (size_t)N + 1);
     w.rlist = d_rlist;
+    CG_BUF(int, d_first, ctx, S_DEPFIRST, N);
+    w.first = d_first;
+    CG_BUF(int, d_tev, ctx, S_DEPTOUCHEV, (size_t)w.touch_cap);
+    w.touch_ev = d_tev;
     w.roff = d_rlist + w.touch_cap;
     CG_BUF(float, d_acc, ctx, S_DEPACC, N);
     CG_BUF(uint8_t, d_own, ctx, S_DEPOWN, N);
@@ -1331,7 +1384,7 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_BUF(unsigned long long, d_timers, ctx, S_DEPTIMERS, T_COUNT);
     w.timers = d_timers;
     // The round's own counts (the fan ids, generations and wave numbers carry on through the stage).
-    for (int word : {W_REPLAYED, W_WAVES, W_REFITTED, W_RELAID})
+    for (int word : {W_REPLAYED, W_WAVES, W_REFITTED, W_RELAID, W_ABORT})
         CG_CUDA(ctx, cudaMemsetAsync(d_words + word, 0, sizeof(int), sm));
     int per_sm = 0;
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
