@@ -285,8 +285,10 @@ def run_ours(args):
                   "fill_ties": s.fill_ties, "fill_unresolved": s.fill_unresolved, "ms": round(s.ms_total, 2),
                   **({"replayed": s.deposit_replayed, "redone": s.deposit_redone, "refitted": s.deposit_refitted,
                       "waves": s.deposit_waves, "ms_deposit": round(s.ms_deposit, 2),
-                      "ms_deposit_parts": {k: round(getattr(s, "ms_deposit_" + k), 2)
-                                           for k in ("walks", "schedule", "lakes", "seas", "repairs")}}
+                      "ms_deposit_parts": {name: round(getattr(s, "ms_deposit_" + k), 2)
+                                           for name, k in (("walks", "walks"), ("schedule", "schedule"),
+                                                           ("laying", "lakes"), ("log", "seas"),
+                                                           ("repairs", "repairs"))}}
                      if args.profile >= 2 else {})}
                  for s in stats]
     clk = clocks.stop()

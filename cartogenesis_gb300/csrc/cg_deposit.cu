@@ -94,7 +94,7 @@ struct WalkDev {
     long long* slot_off;    // per slot: its fan's first pool entry
     int* slot_n;            // per slot: admitted cells (a lake fan) or box tiles (a sea lobe)
     int* slot_box;          // per slot, a sea lobe's box in tiles: first column (may be < 0), first row, columns, rows
-    int* slot_state;        // per slot: 1 while a lake fan waits to lay, 2 while a sea lobe waits, 3 once it may run
+    int* slot_state;        // per slot: 1 while a lake fan waits to lay, 2 while a sea lobe waits, else 0
     double* slot_laid;      // per slot: what its fan laid
     Touch* slot_touch;      // per slot: its fan's deposits, `cap` entries
     int* slot_touch_n;
@@ -138,7 +138,8 @@ struct WalkDev {
     unsigned long long* timers;   // T_*: nanoseconds of the walk's parts, kept by CTA 0's thread 0
 };
 
-// The walk's parts that CTA 0's thread 0 times (it runs every serial part and meets every grid barrier).
+// The walk's parts that CTA 0's thread 0 times (it runs every serial part and meets every grid barrier):
+// own walks and listing, schedules, the laying of lake fans and sea lobes, the logs, the repairs.
 enum { T_WALKS = 0, T_SCHEDULE = 1, T_LAKES = 2, T_SEAS = 3, T_REPAIRS = 4, T_COUNT = 5 };
 
 __device__ __forceinline__ unsigned long long now_ns() {
@@ -887,9 +888,13 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 // a count only waits on lower ranks, so the lowest waiting fan always runs. The wait is
                 // bounded; a warp that gives up raises the abort word, which every other waiter also
                 // heeds, and the walk reports the error.
-                if (n_lakes > 0) {
+                // A lake fan touches only ponded land and a sea lobe only sea cells, so the two kinds wait
+                // only on their own (their schedule ids are cells and tiles, apart) and lay in one pass. A
+                // sea lobe runs whole on its warp's lane 0, reading and writing the fields through L2.
+                if (n_lakes + n_seas > 0) {
                     for (int sl = gwarp; sl < S; sl += nwarps) {
-                        if (w.slot_state[sl] != 1) continue;
+                        const int kind_slot = w.slot_state[sl];
+                        if (kind_slot != 1 && kind_slot != 2) continue;
                         int go = 1;
                         if (lane == 0) {
                             long long spins = 0;
@@ -908,13 +913,33 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                         const int rank = w.events[e0 + sl];
                         const int c = w.order[rank];
                         const double carried = w.ev_carried[rank];
-                        lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
+                        if (kind_slot == 1) {
+                            lay_lake_warp(w, sl, mouth_budget(w.p, w.f, c, carried, LAKE), lane);
+                        } else {
+                            uint32_t* bits = w.warp_bits + (size_t)gwarp * w.box_words;
+                            for (int j = lane; j < w.box_words; j += 32) bits[j] = 0u;
+                            __syncwarp();
+                            if (lane == 0) {
+                                Heap h = warp_heap(w, gwarp);
+                                TouchLog log{w.slot_touch + (size_t)sl * w.cap, w.cap, 0, 0};
+                                int outside = 0;
+                                const int bx = w.box_x, by = w.box_y, W = w.p.W;
+                                mouth_with(w.p, w.f, c, carried, SEA,
+                                           [=, &outside](const Rim& m) {
+                                               return BoxVisited{bits, W, m.apex_column, m.apex_row, bx, by, &outside};
+                                           },
+                                           h, &log);
+                                if (log.overflow) atomicOr(&w.words[W_ERROR], 1);
+                                if (outside) atomicOr(&w.words[W_ERROR], 2);   // past the box its tiles cover
+                                w.slot_touch_n[sl] = log.count;
+                            }
+                        }
                         __syncwarp();
                         __threadfence();
                         for (int q = w.poff[sl] + lane; q < min(w.poff[sl + 1], P); q += 32)   // P: past an overflow
                             if (w.pair_succ[q] >= 0 && index_ok(w, w.pair_succ[q], S, 11)) atomicSub(&w.blockers[w.pair_succ[q]], 1);
                         if (lane == 0) {
-                            w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
+                            if (kind_slot == 1) w.handoff[c] = __dsub_rn(carried, w.slot_laid[sl]);
                             w.slot_state[sl] = 0;
                         }
                     }
@@ -925,57 +950,6 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                     const unsigned long long t = now_ns();
                     tm[T_LAKES] += t - t0;
                     t0 = t;
-                }
-                // The sea lobes (after the lake fans: a lobe touches only sea cells, a fan only land),
-                // a warp each on its lane 0, in rank order wherever their boxes share a tile. A lobe runs
-                // in a wave only if nothing blocked it when the wave began, so whatever an earlier lobe
-                // laid reaches it across a grid barrier. The lowest waiting rank is never blocked.
-                for (int guard = 0; n_seas > 0 && guard <= S; ++guard) {
-                    // This wave's count of waiting lobes; the other word is the last wave's, which a
-                    // slower thread may still be reading.
-                    const int wait_word = W_SEAWAIT0 + (guard & 1);
-                    if (blockIdx.x == 0 && threadIdx.x == 0) w.words[wait_word] = 0;
-                    grid.sync();
-                    for (int sl = gwarp; sl < S; sl += nwarps) {
-                        if (w.slot_state[sl] != 2) continue;
-                        if (*(volatile int*)&w.blockers[sl] == 0) {
-                            if (lane == 0) w.slot_state[sl] = 3;
-                        } else if (lane == 0) {
-                            atomicAdd(&w.words[wait_word], 1);
-                        }
-                    }
-                    grid.sync();
-                    for (int sl = gwarp; sl < S; sl += nwarps) {
-                        if (w.slot_state[sl] != 3) continue;
-                        uint32_t* bits = w.warp_bits + (size_t)gwarp * w.box_words;
-                        for (int j = lane; j < w.box_words; j += 32) bits[j] = 0u;
-                        __syncwarp();
-                        if (lane == 0) {
-                            const int rank = w.events[e0 + sl];
-                            Heap h = warp_heap(w, gwarp);
-                            TouchLog log{w.slot_touch + (size_t)sl * w.cap, w.cap, 0, 0};
-                            int outside = 0;
-                            const int bx = w.box_x, by = w.box_y, W = w.p.W;
-                            mouth_with(w.p, w.f, w.order[rank], w.ev_carried[rank], SEA,
-                                       [=, &outside](const Rim& m) {
-                                           return BoxVisited{bits, W, m.apex_column, m.apex_row, bx, by, &outside};
-                                       },
-                                       h, &log);
-                            if (log.overflow) atomicOr(&w.words[W_ERROR], 1);
-                            if (outside) atomicOr(&w.words[W_ERROR], 2);   // past the box its tiles cover
-                            w.slot_touch_n[sl] = log.count;
-                            w.slot_state[sl] = 0;
-                        }
-                        __syncwarp();
-                        __threadfence();
-                        for (int q = w.poff[sl] + lane; q < min(w.poff[sl + 1], P); q += 32)
-                            if (w.pair_succ[q] >= 0 && index_ok(w, w.pair_succ[q], S, 11))
-                                atomicSub(&w.blockers[w.pair_succ[q]], 1);
-                    }
-                    grid.sync();
-                    ++waves;
-                    if (*(volatile int*)&w.words[wait_word] == 0) break;
-                    if (guard == S && blockIdx.x == 0 && threadIdx.x == 0) w.words[W_ERROR] |= 4;
                 }
                 // The chunk's deposits into the level's log in rank order: each event's entries at the
                 // offset of the events before it.

@@ -174,11 +174,31 @@ CG_HD float fan_draw(int32_t hash, int slot) {
     return (float)((mixed >> 8) & 0xFFFFu) / 65535.0f;
 }
 
+// Reads and writes of the sediment and settled heights a fan or lobe may share with one laid just
+// before it. On the device they go through L2: the earlier one may have run on another SM of the same
+// launch and handed over through a flag rather than a grid barrier, and L1 is not coherent. On the host
+// they are plain accesses.
+CG_HD float ld_l2(const float* p) {
+#ifdef __CUDA_ARCH__
+    return __ldcg(p);
+#else
+    return *p;
+#endif
+}
+CG_HD void st_l2(float* p, float v) {
+#ifdef __CUDA_ARCH__
+    __stcg(p, v);
+#else
+    *p = v;
+#endif
+}
+
 // HydraulicErosion.raise: the change the float field actually took, in double.
 CG_HD double raise(float* field, int cell, double amount) {
-    float prior = field[cell];
-    field[cell] = (float)((double)prior + amount);
-    return (double)field[cell] - (double)prior;
+    const float prior = ld_l2(&field[cell]);
+    const float now = (float)((double)prior + amount);
+    st_l2(&field[cell], now);
+    return (double)now - (double)prior;
 }
 
 // HydraulicErosion.headroom.
@@ -551,7 +571,7 @@ CG_HD int admit(const Params& p, const Fields& f, const Rim& m, bool sea, Visite
                 if (visited.seen(n) || !mouth_accepts(p, f, sea, n)) continue;
                 float co = rim_column_offset(m, n), ro = rim_row_offset(m, n);
                 float distance = sqrt_rn(co * co + ro * ro);
-                float depth = sea ? p.shoreline - (f.surface[n] + f.sediment[n])
+                float depth = sea ? p.shoreline - (f.surface[n] + ld_l2(&f.sediment[n]))
                                   : (f.ground[n] - f.relative[n]) * p.land_range;
                 float advance = 1.0f + kDepthCost * (depth > 0.0f ? depth : 0.0f) / p.shelf_depth;
                 float np = penalty + step_of(p, sx, sy) * (advance - 1.0f);
@@ -590,16 +610,17 @@ CG_HD double lay_admitted(const Params& p, const Fields& f, const Rim& m, bool s
             float depth = 2.0f * p.pond_depth * (1.0f + kLakeFanSlope * fraction) * (0.9f + 0.35f * cell_wobble(cur));
             level = p.shoreline + (f.ground[cur] - depth) * p.land_range;
         }
-        double need = (double)level - (double)f.surface[cur] - (double)f.sediment[cur];
+        double need = (double)level - (double)f.surface[cur] - (double)ld_l2(&f.sediment[cur]);
         if (need <= 0.0) continue;
         if (sea && need > remaining) break;   // a sea lobe lays whole cells
         if (log) {
-            if (log->count < log->capacity) log->touches[log->count] = {cur, f.settled[cur], f.sediment[cur], 0.0f};
+            if (log->count < log->capacity)
+                log->touches[log->count] = {cur, ld_l2(&f.settled[cur]), ld_l2(&f.sediment[cur]), 0.0f};
             else log->overflow = 1;
         }
         double moved = raise(f.sediment, cur, need < remaining ? need : remaining);
         float increment = (float)(moved * (double)p.to_relative);
-        f.settled[cur] += increment;
+        st_l2(&f.settled[cur], ld_l2(&f.settled[cur]) + increment);
         if (log && log->count < log->capacity) log->touches[log->count++].increment = increment;
         remaining -= moved;
         laid += moved;

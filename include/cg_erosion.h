@@ -189,12 +189,13 @@ typedef struct cg_round_stats {
                                    the reference's walk showed them */
     int32_t deposit_waves;      /* P2: the lake fans' laying waves over the round's levels */
     /* P2: where the deposition walk's time went (device clock, milliseconds): the own walks and the
-       mouths' listing, the lake fans' laying schedules, their laying waves, the sea lobes and the
-       level logs (one thread), and the mouth refits and last repairs (one thread). */
+       mouths' listing; the laying schedules; the lake fans and sea lobes laid (each waiting on the
+       earlier ones that share its cells or tiles); the level logs' assembly; and the mouth-conflict
+       searches, relays and last repairs. */
     double  ms_deposit_walks;
     double  ms_deposit_schedule;
-    double  ms_deposit_lakes;
-    double  ms_deposit_seas;
+    double  ms_deposit_lakes;           /* the lake fans and sea lobes laid */
+    double  ms_deposit_seas;            /* the level logs assembled */
     double  ms_deposit_repairs;
     double  ms_flexure;         /* P3: the uplift and the plate flexure at the top of the round (ms_cut then
                                    holds the cut and the weights alone); 0 below P3 */
