@@ -209,6 +209,140 @@ __device__ int facet_receiver(int W, int H, const double* __restrict__ rs, int c
     return dkey(draw) < dkey(share) ? fdiag : fcard;
 }
 
+// facet_receiver<true> for the 32 cells a warp holds (cell < 0: an idle lane), with the expensive
+// FP64 operations taken densely. An FP64 warp instruction holds the pipe whatever its active lanes, and
+// in the per-lane form each facet's division and square root run under a branch that only some lanes
+// take. Here every lane first settles each facet's case (cardinal, diagonal, inside) from the falls,
+// which are dense FP64 subtractions and integer comparisons; the warp then takes the diagonal
+// divisions and the inside square roots as two compacted lists, every lane one request; then each
+// lane compares its facets' slopes in the reference's order. The early outs of the per-lane form only
+// skipped slopes that could not win, so computing every slope changes no comparison's outcome.
+struct DenseFacets {
+    double sq[32 * 8];    // per lane and facet: an inside facet's squared slope, then its slope
+    double dv[32 * 4];    // per lane and diagonal: the fall, then the slope
+    int idx[32 * 8];      // the compacted requests
+};
+
+__device__ __forceinline__ int warp_exclusive_sum(int v, int lane, int* total) {
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    *total = __shfl_sync(0xFFFFFFFFu, x, 31);
+    return x - v;
+}
+
+__device__ int facet_receiver_dense(int W, int H, const double* __restrict__ rs, int cell, Steps st, long long seed,
+                                    DenseFacets& sh) {
+    const int lane = threadIdx.x & 31;
+    const int ccs_t[4] = {1, 0, -1, 0};
+    const int crs_t[4] = {0, -1, 0, 1};
+    const bool live = cell >= 0;
+    const int row = live ? pdiv(cell, W) : 0, col = live ? pmod(cell, W) : 0;
+    const double here = live ? rs[cell] : 0.0;
+    const double dg = (double)st.diag;
+    int dcell[4];
+    double dfall[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int dcs = (k & 1) ? 1 : -1, drs = (k & 2) ? 1 : -1;
+        dcell[k] = live ? neighbour_at(W, H, col + dcs, row + drs) : -1;
+        dfall[k] = dcell[k] >= 0 ? __dsub_rn(here, rs[dcell[k]]) : 0.0;
+    }
+    int card[4];
+    double cdrop[4];
+    unsigned modes = 0;     // 2 bits per facet: 0 cardinal, 1 diagonal, 2 inside, 3 none
+    unsigned need_div = 0, need_sq = 0;
+#pragma unroll
+    for (int side = 0; side < 4; ++side) {
+        card[side] = live ? neighbour_at(W, H, col + ccs_t[side], row + crs_t[side]) : -1;
+        cdrop[side] = card[side] >= 0 ? __dsub_rn(here, rs[card[side]]) : 0.0;
+        const bool cdown = dpos(cdrop[side]);
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const int turn = t ? 1 : -1, f = side * 2 + t;
+            const int dcs = ccs_t[side] == 0 ? turn : ccs_t[side];
+            const int drs = crs_t[side] == 0 ? turn : crs_t[side];
+            const int k = (dcs > 0 ? 1 : 0) | (drs > 0 ? 2 : 0);
+            unsigned m = 3;
+            if (card[side] >= 0 && dcell[k] >= 0) {
+                const double outward = __dsub_rn(dfall[k], cdrop[side]);
+                if (cdown && !dpos(outward)) {
+                    m = 0;
+                } else if (!cdown || dkey(outward) >= dkey(cdrop[side])) {   // a >= b, with unit legs
+                    m = 1;
+                    need_div |= 1u << k;
+                } else {
+                    m = 2;
+                    need_sq |= 1u << f;
+                    sh.sq[lane * 8 + f] = __dadd_rn(__dmul_rn(cdrop[side], cdrop[side]), __dmul_rn(outward, outward));
+                }
+            }
+            modes |= m << (2 * f);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (need_div & (1u << k)) sh.dv[lane * 4 + k] = dfall[k];
+    // The diagonal divisions, densely.
+    int total;
+    int off = warp_exclusive_sum(__popc(need_div), lane, &total);
+    for (int k = 0, j = 0; k < 4; ++k)
+        if (need_div & (1u << k)) sh.idx[off + j++] = lane * 4 + k;
+    __syncwarp();
+    for (int base = 0; base < total; base += 32)
+        if (base + lane < total) {
+            const int i = sh.idx[base + lane];
+            sh.dv[i] = __ddiv_rn(sh.dv[i], dg);
+        }
+    __syncwarp();
+    // The inside facets' square roots, densely.
+    off = warp_exclusive_sum(__popc(need_sq), lane, &total);
+    for (int f = 0, j = 0; f < 8; ++f)
+        if (need_sq & (1u << f)) sh.idx[off + j++] = lane * 8 + f;
+    __syncwarp();
+    for (int base = 0; base < total; base += 32)
+        if (base + lane < total) {
+            const int i = sh.idx[base + lane];
+            sh.sq[i] = __dsqrt_rn(sh.sq[i]);
+        }
+    __syncwarp();
+    // The facets in the reference's order; the winner's cells and falls kept as it wins.
+    double steepest = 0.0;
+    unsigned wmode = 3;
+    int fcard = -1, fdiag = -1;
+    double wout = 0.0, wdrop = 0.0;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const unsigned m = (modes >> (2 * f)) & 3u;
+        const int side = f >> 1, turn = (f & 1) ? 1 : -1;
+        const int dcs = ccs_t[side] == 0 ? turn : ccs_t[side];
+        const int drs = crs_t[side] == 0 ? turn : crs_t[side];
+        const int k = (dcs > 0 ? 1 : 0) | (drs > 0 ? 2 : 0);
+        if (m == 3) continue;
+        const double v = m == 0 ? cdrop[side] : m == 1 ? sh.dv[lane * 4 + k] : sh.sq[lane * 8 + f];
+        if (dkey(v) > dkey(steepest)) {
+            steepest = v;
+            wmode = m;
+            fcard = card[side];
+            fdiag = dcell[k];
+            wout = dfall[k];
+            wdrop = cdrop[side];
+        }
+    }
+    __syncwarp();   // the buffers are the warp's next call's
+    if (!live || wmode == 3 || !dpos(steepest)) return -1;
+    if (wmode == 0) return fcard;
+    if (wmode == 1) return fdiag;
+    const double share = __ddiv_rn(__dsub_rn(wout, wdrop), wdrop);
+    if (!dpos(share)) return fcard;
+    // FlowRouting.subGridDraw (FlowRouting.kt:355-356).
+    const double draw = (double)__fmul_rn(__fadd_rn(seeded_noise(col, row, seed ^ kSubGridDrawSalt), 1.0f), 0.5f);
+    return dkey(draw) < dkey(share) ? fdiag : fcard;
+}
+
 // FlowRouting.steepestNeighbourOf (FlowRouting.kt:320-343).
 __device__ int steepest_neighbour(int W, int H, const double* __restrict__ rs, int col, int row, Steps st) {
     int best = -1;
@@ -267,9 +401,11 @@ __global__ void __launch_bounds__(RECV_THREADS) k_receivers(const uint8_t* __res
                                                             int32_t* __restrict__ recv) {
     const unsigned FULL = 0xFFFFFFFFu;
     __shared__ int queue[RECV_THREADS / 32][64];
+    __shared__ DenseFacets dense[RECV_THREADS / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int* q = queue[warp];
     const bool unit = st.ew == 1.0f && st.ns == 1.0f;
+    const bool warp_dense = by_facet && unit;   // square cells: the facet rule with dense FP64 requests
     const size_t N = (size_t)W * H;
     const size_t warps = (size_t)gridDim.x * (RECV_THREADS / 32);
     int n = 0;   // queued land cells (the same in every lane)
@@ -284,14 +420,19 @@ __global__ void __launch_bounds__(RECV_THREADS) k_receivers(const uint8_t* __res
         __syncwarp();
         if (n >= 32) {
             const int cell = q[lane];
-            recv[cell] = receiver_of(cell, surface, W, H, st, seed, by_facet, unit);
+            recv[cell] = warp_dense ? facet_receiver_dense(W, H, surface, cell, st, seed, dense[warp])
+                                    : receiver_of(cell, surface, W, H, st, seed, by_facet, unit);
             __syncwarp();
             if (lane < n - 32) q[lane] = q[32 + lane];
             n -= 32;
             __syncwarp();
         }
     }
-    if (lane < n) {
+    if (warp_dense) {
+        const int cell = lane < n ? q[lane] : -1;
+        const int r = facet_receiver_dense(W, H, surface, cell, st, seed, dense[warp]);
+        if (lane < n) recv[cell] = r;
+    } else if (lane < n) {
         const int cell = q[lane];
         recv[cell] = receiver_of(cell, surface, W, H, st, seed, by_facet, unit);
     }
