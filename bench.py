@@ -39,7 +39,7 @@ ROUNDS = 12
 # DRAM bytes (read + write) of one two-sweep launch of thermal_sweeps_kernel on the 8192 x 4096
 # field, read from an ncu capture of that launch (ncu cannot run inside the timed bench); the
 # roofline's traffic at that size, null at other sizes.
-SWEEP_TRAFFIC_PER_LAUNCH = 228.1e6
+SWEEP_TRAFFIC_PER_LAUNCH = 227.5e6
 
 
 def parse():
