@@ -68,3 +68,28 @@ def test_fft_round_trip():
     out, _, _ = oracle.flexure_deflection(p, load)
     want = load.astype(np.float64) - load.astype(np.float64).mean()
     assert np.allclose(out, want, rtol=1e-5, atol=1e-3 * np.abs(want).max())
+
+
+def test_stripped_ground_rebounds_in_the_stage():
+    """IsostasyTest's `a stripped range rebounds and its foreland sinks` (T/IsostasyTest.kt:790-850) in
+    the form this stage can show without the plate history: the same world with the flexure on
+    (profile P3) and off (P2). The first round's load is nothing, so its bend is nothing (the
+    reference says so: HydraulicErosion.kt:853-854); after twelve rounds the ground the rounds cut
+    most stands higher with the flexure on, since a loss is a negative load and the plate answers it
+    upward, by a good share of what was cut (on cells of 156 km the plate answers almost locally, so
+    the share approaches Airy's 2835 / 3300 for a loss as broad as a cell)."""
+    from cartogenesis_gb300 import synthetic
+    W, H, seed = 256, 128, 4
+    h, up, rk = synthetic.world(W, H, seed)
+
+    def heights(profile, rounds):
+        p = oracle.default_params(W, H, seed, sea_level=0.70, profile=profile, hydraulic_rounds=rounds)
+        return oracle.erode_stage(p, h, up, rk)["height"].astype(np.float64)
+
+    one2, one3 = heights(2, 1), heights(3, 1)
+    assert np.abs(one3 - one2).max() * 16000.0 < 1e-3   # no bend after the first round
+    p2, p3 = heights(2, 12), heights(3, 12)
+    cut = (h.astype(np.float64) - p2) * 16000.0
+    stripped = cut > np.quantile(cut, 0.99)             # the most eroded cells
+    rebound = float(((p3 - p2) * 16000.0)[stripped].mean())
+    assert rebound > 0.1 * float(cut[stripped].mean()), (rebound, float(cut[stripped].mean()))
