@@ -11,22 +11,28 @@
 //     hand-off plus the donors' hand-offs added in rank order, the reference's double additions in
 //     the reference's order. A cell whose mouth has something to lay (a sea lobe or a lake fan with a
 //     budget and an open apex) is listed, in rank order per CTA segment.
-//  B. the listed mouths run in rank order. A lake fan's admission (its best-first growth inside the
-//     rim) reads only fixed fields (the land, the lake's depth), so every lake fan of the level is
-//     admitted at once, a thread each with its own visited bits over the box its rim can reach, and
-//     its admitted cells are sorted by distance (the laying heap's pop order). One thread then takes
-//     the mouths in rank order: a sea lobe whole (its admission reads the sediment earlier lobes
-//     laid), a lake fan's laying as a scan of its sorted cells.
+//  B. the listed mouths lay in rank order wherever two of them could see each other. A lake fan's
+//     admission (its best-first growth inside the rim) reads only fixed fields (the land, the lake's
+//     depth), so every lake fan of the round is admitted before the walk, a thread each with its own
+//     visited bits over the box its rim can reach, and its admitted cells sorted by distance (the
+//     laying heap's pop order) into a pool. A chunk of mouths gets a laying schedule: the lake fans'
+//     (fan, cell) pairs and the sea lobes' (lobe, box tile) pairs grouped by cell or tile, each mouth
+//     counting the earlier mouths on its cells or tiles and learning the next ones. A mouth's warp
+//     waits for its count to reach 0 (a bounded poll inside the cooperative launch), lays (a lake fan
+//     as a scan of its sorted cells, 32 needs at a time; a sea lobe whole on lane 0, its admission
+//     reading the sediment earlier lobes laid), and releases the next ones. Every deposit is logged,
+//     and the level's log is assembled in rank order from the mouths' own logs.
 //  C. a fan changes only sea cells and ponded land, which no own walk reads, except (a) a ponded cell
 //     of the fan's own level ranked after it, whose settled height took its own subtraction before
-//     the fan's addition instead of after: its settled height is replayed in rank order, in one pass
-//     over the level's log of deposits; and (b) a donor whose settled height a later (dry) cell of the
-//     level read in its headroom. Such a cell's own walk is taken again with its donors as the
-//     reference's walk shows them at its rank. Nothing else of the level reads that cell, so where its
-//     step hands everything on the fix is local; where it has a mouth, its fan changes with it: every
-//     fan from its rank on is undone, the cell refitted, and those fans laid again, and the check
-//     repeats past it. Both are rare; the level schedule itself is shown on the host to give the
-//     reference walk's bits (tests/native/deposit_host.cpp).
+//     the fan's addition instead of after: its settled height is replayed in rank order from its
+//     group of log entries; and (b) a donor whose settled height a later (dry) cell of the level read
+//     in its headroom. Such a cell's own walk is taken again with its donors as the reference's walk
+//     shows them at its rank. Nothing else of the level reads that cell, so where its step hands
+//     everything on the fix is local; where it has a mouth, its fan changes with it: every fan from
+//     its rank on is undone (over the grid, from the log), the cell refitted, and those fans laid
+//     again, and the search, an atomic minimum over the log, repeats past it. Both are rare; the
+//     level schedule itself is shown on the host to give the reference walk's bits
+//     (tests/native/deposit_host.cpp).
 // Settle is elementwise, and the mouths pass reads only each cell's receiver, so it runs receivers
 // first, level by level from the top, like the incision.
 #include <algorithm>
