@@ -85,6 +85,7 @@ struct WalkDev {
     int* seg_events;        // per rank: listed ranks, compacted within each CTA's segment
     int* seg_count;         // per CTA
     int* seg_off;           // per CTA + 1: its listed mouths' first place in `events`
+    int* seg_part;          // per CTA + 1: a grid-wide scan's slice sums
     int* events;            // the level's listed ranks, dense, in rank order
     // The round's lake fans, admitted before the walk (k_admit_lakes): per candidate mouth cell its
     // admitted cells sorted by distance and each one's level less its terrain, in a pool.
@@ -335,6 +336,51 @@ __device__ void cta_exclusive_scan(Get get, int n, int* out, int* sh) {
     }
     if (threadIdx.x == 0) out[n] = carry;
     __syncthreads();
+}
+
+// An exclusive prefix sum over the whole grid, called by every thread: each CTA sums a slice, one CTA
+// scans the slices' sums, then each CTA scans its slice from its offset; out[n] receives the total.
+// For long arrays, where one CTA stepping through them would hold the grid. `part` holds gridDim.x + 1
+// ints.
+template <class Get>
+__device__ void grid_exclusive_scan(Get get, int n, int* out, int* part, int* sh) {
+    cgr::grid_group grid = cgr::this_grid();
+    const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int lo = min(n, (int)blockIdx.x * per), hi = min(n, lo + per);
+    int sum = 0;
+    for (int i = lo + (int)threadIdx.x; i < hi; i += kThreads) sum += get(i);
+    sh[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+    __syncthreads();
+    grid.sync();
+    if (blockIdx.x == 0) {
+        const int* pp = part;
+        cta_exclusive_scan([=](int i) { return __ldcg(&pp[i]); }, (int)gridDim.x, part, sh);
+    }
+    grid.sync();
+    int carry = __ldcg(&part[blockIdx.x]);
+    for (int base = lo; base < hi; base += kThreads) {
+        const int i = base + (int)threadIdx.x;
+        const int v = i < hi ? get(i) : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kThreads; o <<= 1) {
+            const int t = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < hi) out[i] = carry + sh[threadIdx.x] - v;
+        const int chunk = sh[kThreads - 1];
+        __syncthreads();
+        carry += chunk;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = __ldcg(&part[gridDim.x]);
 }
 
 // An index check of the laying schedule: v must lie in [0, hi). A failure records its site, value and
@@ -841,14 +887,18 @@ __global__ void __launch_bounds__(kThreads) k_deposit_levels(WalkDev w) {
                 }
                 grid.sync();
                 const int D = *(volatile int*)&w.words[W_DISTINCT];
-                if (blockIdx.x == 0) {
+                {
                     const int* cnt = w.cell_cnt;
                     const int* dc = w.dcell;
-                    cta_exclusive_scan([=](int i) { return __ldcg(&cnt[dc[i]]); }, D, w.doff, sh_scan);
-                    // Every pair is counted on exactly one distinct cell.
-                    if (threadIdx.x == 0 && w.doff[D] != P) check_failed(w, w.doff[D], P, 13);
+                    if (D > 4 * kThreads) {   // long: over the grid
+                        grid_exclusive_scan([=](int i) { return __ldcg(&cnt[dc[i]]); }, D, w.doff, w.seg_part, sh_scan);
+                    } else if (blockIdx.x == 0) {
+                        cta_exclusive_scan([=](int i) { return __ldcg(&cnt[dc[i]]); }, D, w.doff, sh_scan);
+                    }
                 }
                 grid.sync();
+                // Every pair is counted on exactly one distinct cell.
+                if (blockIdx.x == 0 && threadIdx.x == 0 && __ldcg(&w.doff[D]) != P) check_failed(w, w.doff[D], P, 13);
                 for (int q = (int)(blockIdx.x * blockDim.x + threadIdx.x); q < P; q += (int)(gridDim.x * blockDim.x)) {
                     const int d = w.cell_d[w.pair_cell[q]];
                     if (!index_ok(w, d, D, 5)) continue;
@@ -1370,9 +1420,10 @@ cg_status deposit_walk_dev(cg_ctx* ctx, const cg_erosion_params& cp, const Depos
     CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_levels, kThreads, 0));
     if (per_sm < 1) return fail(ctx, CG_CUDA, "deposition kernel cannot be resident");
     const int cgrid = ctx->num_sms * (per_sm < 2 ? per_sm : 2);
-    CG_BUF(int, d_segc, ctx, S_DEPSEGC, 2 * (size_t)cgrid + 1);
+    CG_BUF(int, d_segc, ctx, S_DEPSEGC, 3 * (size_t)cgrid + 2);
     w.seg_count = d_segc;
     w.seg_off = d_segc + cgrid;
+    w.seg_part = d_segc + 2 * (size_t)cgrid + 1;
     // A heap per warp, for the sea lobes.
     w.heap_warps = cgrid * (kThreads / 32);
     const size_t HC = (size_t)w.heap_warps * cap;
