@@ -108,7 +108,7 @@ enum Slot {
     S_DEPHEAP, S_DEPTOUCH, S_DEPREPLAY, S_DEPSEGC,
     S_OM_LAND, S_OM_REL, S_OM_FILLED, S_OM_RECV, S_OM_KEY, S_OM_AREA, S_OM_RUNOFF, S_OM_DONORS,
     S_FILLEB, S_THERMERR, S_SL_MASK, S_SL_LABEL, S_SL_SIZE, S_SL_WORDS, S_DEPSLOT8, S_DEPSLOT9, S_DEPSLOT10,
-    S_DEPCLAIM, S_DEPCANDOF, S_DEPCAND, S_DEPCANDN, S_DEPCANDOFF, S_DEPCANDW, S_DEPSLOTOFF, S_DEPACC, S_DEPOWN, S_DEPCELLCNT, S_DEPTIMERS, S_DEPRLIST, S_DEPWBITS, S_SS_EST, S_SS_SPEC, S_SS_WALK, S_SS_X, S_SS_MASK, S_SS_OUT, S_DEPFIRST, S_DEPTOUCHEV,
+    S_DEPCLAIM, S_DEPCANDOF, S_DEPCAND, S_DEPCANDN, S_DEPCANDOFF, S_DEPCANDW, S_DEPSLOTOFF, S_DEPACC, S_DEPOWN, S_DEPCELLCNT, S_DEPTIMERS, S_DEPRLIST, S_DEPWBITS, S_SS_EST, S_SS_SPEC, S_SS_WALK, S_SS_X, S_SS_MASK, S_SS_OUT, S_DEPFIRST, S_DEPTOUCHEV, S_RS_KEYS, S_RS_VALS, S_RS_HIST,
     S_FX_TW, S_FX_A, S_FX_B, S_FX_MEAN, S_FX_REF, S_FX_DEFL, S_FX_UPL, S_FX_LOAD,
     S_COUNT
 };

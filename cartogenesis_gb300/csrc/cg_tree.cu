@@ -22,6 +22,7 @@
 
 #include <cfloat>
 #include <climits>
+#include <utility>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -225,44 +226,88 @@ __global__ void k_area_sea(const uint8_t* __restrict__ land, size_t N, float* __
         if (!land[i]) area[i] = 0.0f;
 }
 
-// Key-value bitonic stage over P2 slots padded with the largest key. Used only to hand the
-// explicit order back to a caller that asked for it.
-__global__ void k_bitonic_kv(long long* keys, int* vals, int P2, int k, int j) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
-        int l = i ^ j;
-        if (l <= i) continue;
-        long long ka = keys[i], kb = keys[l];
-        bool up = (i & k) == 0;
-        if ((ka > kb) == up) {
-            keys[i] = kb;
-            keys[l] = ka;
-            int t = vals[i];
-            vals[i] = vals[l];
-            vals[l] = t;
-        }
-    }
-}
-
-__global__ void k_pad_kv(long long* keys, int* vals, int n, int P2) {
-    for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < P2; i += gridDim.x * blockDim.x) {
-        keys[i] = LLONG_MAX;
-        vals[i] = -1;
-    }
-}
-
 __global__ void k_land_flags(const uint8_t* __restrict__ land, size_t N, int* __restrict__ flag) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
         flag[i] = land[i] ? 1 : 0;
 }
 
-__global__ void k_land_compact(const uint8_t* __restrict__ land, const int* __restrict__ pos,
-                               const long long* __restrict__ key, size_t N, long long* __restrict__ okeys,
-                               int* __restrict__ ovals) {
+// The drainage order as a stable LSD radix sort of the land cells' compact keys, level N + deepest
+// source (distinct, ordered as the drainage keys are), 8 bits a pass over the bits they use. A CTA
+// takes a tile of kRsTile cells: it counts its digits, the counts are scanned digit-major over the
+// tiles, and the CTA scatters its tile in order, 256 cells at a time, each cell's place among the
+// chunk's cells of its digit found with __match_any_sync within its warp and per-warp counts across
+// warps, so cells of one digit keep their order.
+constexpr int kRsTile = 4096;
+
+__global__ void k_land_compact_ck(const uint8_t* __restrict__ land, const int* __restrict__ pos,
+                                  const long long* __restrict__ key, size_t N, unsigned long long* __restrict__ ck,
+                                  int* __restrict__ vals, unsigned long long* __restrict__ kmax) {
+    unsigned long long m = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
         if (land[i]) {
-            okeys[pos[i]] = key[i];
-            ovals[pos[i]] = (int)i;
+            const unsigned long long k = (unsigned long long)key[i];
+            const unsigned long long c = (k >> 32) * (unsigned long long)N + (k & 0xFFFFFFFFull);
+            ck[pos[i]] = c;
+            vals[pos[i]] = (int)i;
+            m = c > m ? c : m;
         }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(0xFFFFFFFFu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(kmax, m);
+}
+
+__global__ void __launch_bounds__(256) k_rs_hist(const unsigned long long* __restrict__ keys, int n, int shift,
+                                                 int tiles, int* __restrict__ hist) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int lo = blockIdx.x * kRsTile, hi = min(n, lo + kRsTile);
+    for (int i = lo + (int)threadIdx.x; i < hi; i += 256) atomicAdd(&h[(int)((keys[i] >> shift) & 255ull)], 1);
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_rs_scatter(const unsigned long long* __restrict__ kin,
+                                                    const int* __restrict__ vin, int n, int shift, int tiles,
+                                                    const int* __restrict__ off, unsigned long long* __restrict__ kout,
+                                                    int* __restrict__ vout) {
+    __shared__ int base[256];
+    __shared__ int wcnt[8][256];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    base[tid] = off[tid * tiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+    const int lo = blockIdx.x * kRsTile, hi = min(n, lo + kRsTile);
+    for (int c = lo; c < hi; c += 256) {
+        const int i = c + tid;
+        const bool valid = i < hi;
+        const unsigned long long k = valid ? kin[i] : 0ull;
+        const int v = valid ? vin[i] : 0;
+        const int d = valid ? (int)((k >> shift) & 255ull) : 256;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            int before = 0;
+            for (int w = 0; w < warp; ++w) before += wcnt[w][d];
+            const int p = base[d] + before + rank;
+            kout[p] = k;
+            vout[p] = v;
+        }
+        __syncthreads();
+        int sum = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) {
+            sum += wcnt[w][tid];
+            wcnt[w][tid] = 0;
+        }
+        base[tid] += sum;
+        __syncthreads();
+    }
 }
 
 // ---- incise
@@ -575,22 +620,40 @@ cg_status order_from_keys_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
     if (land_cells <= 0) return CG_OK;
     CG_BUF(int, d_flag, ctx, S_SCRATCH0, N);
     CG_BUF(int, d_pos, ctx, S_SCRATCH1, N);
-    int P2 = 1;
-    while (P2 < land_cells) P2 <<= 1;
-    CG_BUF(long long, d_okeys, ctx, S_BRACKET2, P2);
-    CG_BUF(int, d_ovals, ctx, S_SCRATCH3, P2);
+    const int n = land_cells;
+    const int tiles = (n + kRsTile - 1) / kRsTile;
+    CG_BUF(unsigned long long, d_keys, ctx, S_RS_KEYS, 2 * (size_t)n + 1);
+    CG_BUF(int, d_vals, ctx, S_RS_VALS, 2 * (size_t)n);
+    CG_BUF(int, d_hist, ctx, S_RS_HIST, 2 * (size_t)tiles * 256);
+    unsigned long long* kmax = d_keys + 2 * (size_t)n;
+    unsigned long long* ka = d_keys;
+    unsigned long long* kb = d_keys + n;
+    int* va = d_vals;
+    int* vb = d_vals + n;
+    int* d_off = d_hist + (size_t)tiles * 256;
     CG_LAUNCH(ctx) k_land_flags<<<grid, 256, 0, sm>>>(d_land, N, d_flag);
     CG_CHECK_LAUNCH(ctx);
     cg_status st = exclusive_scan(ctx, d_flag, d_pos, (int)N, nullptr);
     if (st != CG_OK) return st;
-    CG_LAUNCH(ctx) k_land_compact<<<grid, 256, 0, sm>>>(d_land, d_pos, d_key, N, d_okeys, d_ovals);
-    int blocks = (P2 / 2 + 255) / 256;
-    if (blocks > grid) blocks = grid;
-    CG_LAUNCH(ctx) k_pad_kv<<<blocks, 256, 0, sm>>>(d_okeys, d_ovals, land_cells, P2);
-    for (int k = 2; k <= P2; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) CG_LAUNCH(ctx) k_bitonic_kv<<<blocks, 256, 0, sm>>>(d_okeys, d_ovals, P2, k, j);
-    CG_CUDA(ctx, cudaMemcpyAsync(d_order, d_ovals, sizeof(int) * land_cells, cudaMemcpyDeviceToDevice, sm));
+    CG_CUDA(ctx, cudaMemsetAsync(kmax, 0, sizeof(unsigned long long), sm));
+    CG_LAUNCH(ctx) k_land_compact_ck<<<grid, 256, 0, sm>>>(d_land, d_pos, d_key, N, ka, va, kmax);
     CG_CHECK_LAUNCH(ctx);
+    unsigned long long hmax = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&hmax, kmax, sizeof(hmax), cudaMemcpyDeviceToHost, sm));
+    CG_CUDA(ctx, cudaStreamSynchronize(sm));
+    int bits = 0;
+    while (bits < 64 && (hmax >> bits) != 0) ++bits;
+    for (int shift = 0; shift < bits; shift += 8) {
+        CG_LAUNCH(ctx) k_rs_hist<<<tiles, 256, 0, sm>>>(ka, n, shift, tiles, d_hist);
+        CG_CHECK_LAUNCH(ctx);
+        st = exclusive_scan(ctx, d_hist, d_off, tiles * 256, nullptr);
+        if (st != CG_OK) return st;
+        CG_LAUNCH(ctx) k_rs_scatter<<<tiles, 256, 0, sm>>>(ka, va, n, shift, tiles, d_off, kb, vb);
+        CG_CHECK_LAUNCH(ctx);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    CG_CUDA(ctx, cudaMemcpyAsync(d_order, va, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, sm));
     return CG_OK;
 }
 
