@@ -6,5 +6,6 @@ include/cg_erosion.h). This package loads it and mirrors the reference's own ent
 top of it. There is no CPU fallback: if the library or the device is missing, calls raise.
 """
 from .runtime import (CgError, Context, library, load_library)  # noqa: F401
-from .api import (ErosionStage, ErosionConfig, GpuErosionAccelerator, FlowRouting, HydraulicErosion, Isostasy, SeaLevelStage,  # noqa: F401
-                  StageRounds, ThermalLimits)
+from .api import (BeltErosion, BeltReplay, BeltWindow, ErosionStage, ErosionConfig, GaussianBlur,  # noqa: F401
+                  GpuErosionAccelerator, FlowRouting, HydraulicErosion, Isostasy, SeaLevelStage, StageRounds,
+                  ThermalLimits)

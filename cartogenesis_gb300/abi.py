@@ -144,6 +144,44 @@ class World(C.Structure):
     ]
 
 
+class BeltWindow(C.Structure):
+    """cg_belt_window: BeltWindow, the belts' history over the exposure window."""
+    _fields_ = [
+        ("tectonic_km", C.c_void_p),
+        ("wear_km", C.c_void_p),
+        ("onset_myr_ago", C.c_void_p),
+        ("window_myr", C.c_double),
+    ]
+
+
+class BeltInputs(C.Structure):
+    """cg_belt_inputs: the rest of BeltErosion.replay's arguments."""
+    _fields_ = [
+        ("uplift_mm_per_year", C.c_void_p),
+        ("rainfall_mm", C.c_void_p),
+        ("cover_density", C.c_void_p),
+        ("rock_erodibility", C.c_void_p),
+        ("unresolved_relief", C.c_void_p),
+        ("provisional_sea_level", C.c_float),
+        ("shield_cut", C.c_int32),
+        ("rebound", C.c_int32),
+        ("history_cell_km", C.c_double),
+    ]
+
+
+class BeltBooks(C.Structure):
+    """cg_belt_books: BeltReplay's figures."""
+    _fields_ = [
+        ("rounds", C.c_int32),
+        ("belt_cells", C.c_int32),
+        ("uplifted_cubic_meters", C.c_double),
+        ("cut_cubic_meters", C.c_double),
+        ("exported_to_sea_cubic_meters", C.c_double),
+        ("exported_to_land_cubic_meters", C.c_double),
+        ("shed_beside_cubic_meters", C.c_double),
+    ]
+
+
 def ptr(a):
     """Address of a numpy array's data, or None."""
     return None if a is None else a.ctypes.data

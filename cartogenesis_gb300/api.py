@@ -1,13 +1,15 @@
 """Python mirror of the reference's entry points for the erosion stage, on libcg_erosion.so.
 
 Names, argument meanings and units follow the Kotlin (P = worldgen/src/commonMain/kotlin/com/
-cartogenesis/worldgen/pipeline):
+cartogenesis/worldgen/pipeline, MA = .../worldgen/math):
   GpuErosionAccelerator.erode  -> ErosionAccelerator.erode   (P/ErosionAccelerator.kt:38-45)
   ErosionStage.apply           -> ErosionStage.apply         (P/ErosionStage.kt:110-183)
   SeaLevelStage.percentile_cut -> SeaLevelStage.percentileCut (P/SeaLevelStage.kt:146-200)
   FlowRouting.*                -> FlowRouting.fillDepressions, flowDirections, drainageOrder,
                                   accumulate, spillways (P/FlowRouting.kt)
   HydraulicErosion.breach      -> HydraulicErosion.breach    (P/HydraulicErosion.kt:1931-2171)
+  BeltErosion.replay           -> BeltErosion.replay         (P/BeltErosion.kt:96-425)
+  GaussianBlur.apply           -> GaussianBlur.apply         (MA/GaussianBlur.kt:44-111)
 Arrays are numpy, row-major [height, width]. Every call runs on the GPU; none falls back to a CPU.
 """
 import ctypes as C
@@ -310,6 +312,88 @@ class Isostasy:
                                                                   P(out), C.byref(d), C.byref(r)))
             self.rigidity, self.restoring = d.value, r.value
             return out
+
+
+def sequential_sum_f64(terms, ctx=None):
+    """`var s = 0.0; for (v in terms) s += v` over double terms in the order given, bit for bit, on the
+    device (the belts' replay keeps its books with it)."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(terms, dtype=np.float64).ravel()
+    s = C.c_double()
+    with ctx.lock:
+        ctx.check(ctx.lib.cg_sequential_sum_f64(ctx.handle, P(x) if x.size else None, x.size, C.byref(s)))
+    return s.value
+
+
+class GaussianBlur:
+    """GaussianBlur (MA/GaussianBlur.kt): a Gaussian of a spread on the ground, x wrapping, y clamped."""
+
+    @staticmethod
+    def apply(field, sigma_across_cells, sigma_down_cells, ctx=None):
+        """Blurs `field` (float32 [H, W]) in place, as GaussianBlur.apply does."""
+        ctx = ctx or default_context()
+        f = np.ascontiguousarray(field, dtype=np.float32).copy()
+        H, W = f.shape
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_gaussian_blur(ctx.handle, W, H, P(f), float(sigma_across_cells),
+                                               float(sigma_down_cells)))
+        field[...] = f
+        return field
+
+
+@dataclass
+class BeltWindow:
+    """BeltWindow (P/BeltErosion.kt:19-24): per cell, km thickened and worn over the window and when the
+    thickening began (Myr ago, negative where none did); the window's length in Myr."""
+    tectonic_km: np.ndarray
+    wear_km: np.ndarray
+    onset_myr_ago: np.ndarray
+    window_myr: float
+
+
+@dataclass
+class BeltReplay:
+    """BeltReplay (P/BeltErosion.kt:35-47)."""
+    rounds: int
+    belt_cells: int
+    uplifted_cubic_meters: float
+    cut_cubic_meters: float
+    exported_to_sea_cubic_meters: float
+    exported_to_land_cubic_meters: float
+    shed_beside_cubic_meters: float
+    eroded_meters: np.ndarray
+
+
+class BeltErosion:
+    @staticmethod
+    def replay(config, surface, window, present_uplift_mm_per_year=None, rainfall_mm=None, cover_density=None,
+               rock_erodibility=None, provisional_sea_level=None, shield_cut=True, unresolved_relief=None,
+               rebound=True, history_cell_km=80.0, ctx=None):
+        """BeltErosion.replay (P/BeltErosion.kt:96-425) on the device: `surface` (the height field,
+        [H, W]) is replayed in place, as the reference's array is. `rebound` is IsostasyConfig.enabled,
+        `history_cell_km` TectonicsConfig.historyCellKm; the provisional sea level defaults to the
+        config's sea_level. Returns the BeltReplay, its eroded_meters a new [H, W] array."""
+        ctx = ctx or default_context()
+        p = config.params
+        H, W = p.height, p.width
+        h = _f32(surface, (H, W)).copy()
+        fields = [_f32(a, (H, W)) if a is not None else None
+                  for a in (window.tectonic_km, window.wear_km, window.onset_myr_ago, present_uplift_mm_per_year,
+                            rainfall_mm, cover_density, rock_erodibility, unresolved_relief)]
+        tect, wear, onset, upl, rain, cover, rock, unres = fields
+        win = abi.BeltWindow(P(tect), P(wear), P(onset), float(window.window_myr))
+        sea = p.sea_level if provisional_sea_level is None else provisional_sea_level
+        ins = abi.BeltInputs(P(upl), P(rain), P(cover), P(rock), P(unres), float(sea), int(bool(shield_cut)),
+                             int(bool(rebound)), float(history_cell_km))
+        eroded = np.empty((H, W), np.float32)
+        books = abi.BeltBooks()
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_belt_replay(ctx.handle, C.byref(p), P(h), C.byref(win), C.byref(ins), P(eroded),
+                                             C.byref(books)))
+        surface[...] = h
+        return BeltReplay(books.rounds, books.belt_cells, books.uplifted_cubic_meters, books.cut_cubic_meters,
+                          books.exported_to_sea_cubic_meters, books.exported_to_land_cubic_meters,
+                          books.shed_beside_cubic_meters, eroded)
 
 
 class FlowRouting:

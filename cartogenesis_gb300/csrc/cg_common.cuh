@@ -70,7 +70,7 @@ struct cg_ctx {
     std::atomic<int> cancel{0};
     char error[512] = {0};
     // Named scratch buffers, grown on demand and reused across calls.
-    cg::DevBuf bufs[160];
+    cg::DevBuf bufs[200];
     // Pinned host staging.
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -110,6 +110,13 @@ enum Slot {
     S_FILLEB, S_THERMERR, S_SL_MASK, S_SL_LABEL, S_SL_SIZE, S_SL_WORDS, S_DEPSLOT8, S_DEPSLOT9, S_DEPSLOT10,
     S_DEPCLAIM, S_DEPCANDOF, S_DEPCAND, S_DEPCANDN, S_DEPCANDOFF, S_DEPCANDW, S_DEPSLOTOFF, S_DEPACC, S_DEPOWN, S_DEPCELLCNT, S_DEPTIMERS, S_DEPRLIST, S_DEPWBITS, S_SS_EST, S_SS_SPEC, S_SS_WALK, S_SS_X, S_SS_MASK, S_SS_OUT, S_DEPFIRST, S_DEPTOUCHEV, S_RS_KEYS, S_RS_VALS, S_RS_HIST,
     S_FX_TW, S_FX_A, S_FX_B, S_FX_MEAN, S_FX_REF, S_FX_DEFL, S_FX_UPL, S_FX_LOAD,
+    // the belts' replay: its inputs, the belt and its frontier, the opening's routing, a round's state
+    S_BT_H, S_BT_TECT, S_BT_WEAR, S_BT_ONSET, S_BT_UPLIFT, S_BT_RAIN, S_BT_COVER, S_BT_ROCK, S_BT_UNRES,
+    S_BT_BELT, S_BT_INNER, S_BT_ROUTED, S_BT_LAND, S_BT_REL, S_BT_FLAG, S_BT_POS, S_BT_LIST, S_BT_LOCAL,
+    S_BT_FIRST, S_BT_RISE, S_BT_WEIGHTS, S_BT_FACTOR, S_BT_FILLED, S_BT_SURF, S_BT_RECV, S_BT_KEY,
+    S_BT_DONORS, S_BT_AREA, S_BT_INFLOW, S_BT_ROUTING, S_BT_DISC, S_BT_FLUX, S_BT_CUTV, S_BT_GIVE,
+    S_BT_NEXT, S_BT_ORDER, S_BT_XS, S_BT_REF, S_BT_UPLM, S_BT_RBM, S_BT_LOSS, S_BT_TMP, S_BT_TAPS,
+    S_BT_SMALL, S_BT_ERODED,
     S_COUNT
 };
 static_assert(S_COUNT <= (int)(sizeof(((cg_ctx*)nullptr)->bufs) / sizeof(DevBuf)), "a slot past the context's buffers");

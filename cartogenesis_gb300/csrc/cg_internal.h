@@ -46,6 +46,10 @@ cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, 
                               const float* d_filled, int64_t seed, double r, int lattice, bool by_facet,
                               bool over_potential, int32_t* d_recv, double* d_surface, FlatCounts* counts);
 
+// FlowRouting.facetReceiver at every cell of d_mask over the routing surface d_surface (-1 elsewhere).
+cg_status facet_receivers_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_mask, const double* d_surface,
+                              int64_t seed, double r, int32_t* d_recv);
+
 // ---- drainage tree (cg_tree.cu)
 // Donor counts, the Kahn queue keys (level << 32 | deepest source) of FlowRouting.drainageOrder and,
 // if d_weights is given, FlowRouting.accumulate's areas, in one last-arriver walk. *h_levels
@@ -153,6 +157,9 @@ struct DepositCounts {
 // spot, pieces added one value at a time.
 cg_status seq_sum_dev(cg_ctx* ctx, const float* d_x, const uint8_t* d_mask, int mode, size_t n, double divisor,
                       double* d_out, long long* d_counts);
+// The same sequential sum (`s += v`, s from 0.0) over n double terms already laid out in the order the
+// reference adds them, bit for bit; a running total is carried by laying it first.
+cg_status seq_sum_f64_dev(cg_ctx* ctx, const double* d_x, size_t n, double* d_out);
 // The plate flexure of profile P3 (cg_flexure.cu). flexure_check refuses grids whose transform lines
 // do not fit a CTA's shared memory; flexure_stage_begin_dev records the field before the rounds and
 // clears the bend (and the uplift record when the world has uplift); flexure_uplifted_dev is that

@@ -1585,6 +1585,21 @@ __global__ void k_flat_lists(const int* __restrict__ count, int flats, int* __re
 
 }  // namespace
 
+// FlowRouting.facetReceiver over a caller's routing surface (FlowRouting.kt:218-310, the rule
+// BeltErosion's rounds route the belts by): the facet receiver of every cell of d_mask, -1 elsewhere.
+cg_status facet_receivers_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_mask, const double* d_surface,
+                              int64_t seed, double r, int32_t* d_recv) {
+    Steps steps;
+    steps.ew = 1.0f;
+    steps.ns = (float)r;
+    steps.diag = (float)std::sqrt(1.0 + r * r);
+    CG_LAUNCH(ctx) k_receivers<<<ctx->num_sms * 8, RECV_THREADS, 0, ctx->stream>>>(d_mask, d_surface, W, H, steps,
+                                                                                  (long long)seed, 1, nullptr, 0,
+                                                                                  d_recv);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
 cg_status flow_directions_dev(cg_ctx* ctx, int W, int H, const uint8_t* d_land, const float* d_rel,
                               const float* d_filled, int64_t seed, double r, int lattice, bool by_facet,
                               bool over_potential, int32_t* d_recv, double* d_surface, FlatCounts* counts) {

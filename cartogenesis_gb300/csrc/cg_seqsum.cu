@@ -29,10 +29,12 @@ constexpr int kSSBlock = kSSThreads * kSSPer;    // values per block
 constexpr long long kM0 = 1LL << 52, kM1 = 1LL << 53;
 constexpr long long kBig = 1LL << 58;            // a partial step this large leaves any binade: give up
 
+// The values summed: float fields (widened exactly), or double terms already in summation order.
+template <typename T>
 struct SumIn {
-    const float* x;
-    const uint8_t* mask;   // may be null: every cell
-    int mode;              // 0: x, 1: 1 - 0.5 x (the cover's shielding factor)
+    const T* x;
+    const uint8_t* mask;   // may be null: every value (float fields only)
+    int mode;              // 0: x, 1: 1 - 0.5 x (the cover's shielding factor; float fields only)
     size_t n;
 };
 
@@ -71,11 +73,17 @@ __device__ __forceinline__ Walk walk_then(const Walk& a, const Walk& b) {
     return w;
 }
 
-__device__ __forceinline__ bool value_at(const SumIn& in, size_t i, float* v) {
+__device__ __forceinline__ bool value_at(const SumIn<float>& in, size_t i, float* v) {
     if (i >= in.n) return false;
     if (in.mask && !in.mask[i]) return false;
     const float x = in.x[i];
     *v = in.mode == 1 ? __fsub_rn(1.0f, __fmul_rn(0.5f, x)) : x;
+    return true;
+}
+
+__device__ __forceinline__ bool value_at(const SumIn<double>& in, size_t i, double* v) {
+    if (i >= in.n) return false;
+    *v = in.x[i];
     return true;
 }
 
@@ -115,6 +123,42 @@ __device__ __forceinline__ Step step_of(float v, int ef, int neg) {
     if (frac == half) {
         s.tie = 1;
         s.r = negative ? -(a + 1) : a;   // floor(y)
+    } else {
+        const long long r = a + (frac > half ? 1 : 0);
+        s.r = negative ? -r : r;
+    }
+    return s;
+}
+
+// The same for a double value: y = M 2^k with M < 2^53 and k = max(fe, 1) - ef. A value of 2^58 u or
+// more, or NaN or infinity, is left to the serial additions; below u / 4 it adds nothing.
+__device__ __forceinline__ Step step_of(double v, int ef, int neg) {
+    Step s{0, 0, 0};
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int fe = (int)((b >> 52) & 0x7FF);
+    if (fe == 0x7FF) {
+        s.fail = 1;
+        return s;
+    }
+    long long M = (long long)(b & ((1ULL << 52) - 1));
+    if (fe != 0) M |= 1LL << 52;
+    if (M == 0) return s;
+    const bool negative = ((b >> 63) != 0) != (neg != 0);
+    const int k = (fe == 0 ? 1 : fe) - ef;
+    if (k >= 0) {
+        if (k > 5) {
+            s.fail = 1;
+            return s;
+        }
+        s.r = negative ? -(M << k) : (M << k);
+        return s;
+    }
+    const int sh = -k;
+    if (sh >= 55) return s;   // |y| < 2^-2: rounds to 0
+    const long long a = M >> sh, frac = M & ((1LL << sh) - 1), half = 1LL << (sh - 1);
+    if (frac == half) {
+        s.tie = 1;
+        s.r = negative ? -(a + 1) : a;
     } else {
         const long long r = a + (frac > half ? 1 : 0);
         s.r = negative ? -r : r;
@@ -171,12 +215,13 @@ __device__ Walk cta_walk(const Walk& mine, Walk* sh_warps) {
 }
 
 // A cheap estimate of each block's sum (any order): it only picks the binade each block is reduced for.
-__global__ void __launch_bounds__(kSSThreads) k_ss_estimate(SumIn in, double* __restrict__ est) {
+template <typename T>
+__global__ void __launch_bounds__(kSSThreads) k_ss_estimate(SumIn<T> in, double* __restrict__ est) {
     __shared__ double part[kSSThreads / 32];
     const size_t base = (size_t)blockIdx.x * kSSBlock;
     double s = 0.0;
     for (int t = 0; t < kSSPer; ++t) {
-        float v;
+        T v;
         if (value_at(in, base + (size_t)t * kSSThreads + threadIdx.x, &v)) s += (double)v;
     }
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
@@ -217,7 +262,9 @@ __global__ void __launch_bounds__(1024) k_ss_spec(const double* __restrict__ est
 }
 
 // Each block's walk under the binade it is expected to begin in. A thread's values are consecutive.
-__global__ void __launch_bounds__(kSSThreads) k_ss_walks(SumIn in, const int* __restrict__ spec, Walk* __restrict__ walks) {
+template <typename T>
+__global__ void __launch_bounds__(kSSThreads) k_ss_walks(SumIn<T> in, const int* __restrict__ spec,
+                                                        Walk* __restrict__ walks) {
     __shared__ Walk sh_warps[kSSThreads / 32];
     const int sp = spec[blockIdx.x];
     LocalWalk lw;
@@ -225,7 +272,7 @@ __global__ void __launch_bounds__(kSSThreads) k_ss_walks(SumIn in, const int* __
     if (sp >= 0) {
         const size_t base = (size_t)blockIdx.x * kSSBlock + (size_t)threadIdx.x * kSSPer;
         for (int t = 0; t < kSSPer; ++t) {
-            float v;
+            T v;
             if (value_at(in, base + t, &v)) lw.add(step_of(v, sp & 0x7FF, sp >> 11));
         }
     }
@@ -257,7 +304,8 @@ __device__ __forceinline__ bool apply_walk(double* s, const Walk& w, int ef, int
 
 // The walk over the blocks, one CTA. Thread 0 keeps the sum; the CTA reduces a piece on the spot, or
 // stages it for thread 0's serial additions.
-__global__ void __launch_bounds__(kSSThreads) k_ss_chain(SumIn in, const int* __restrict__ spec,
+template <typename T>
+__global__ void __launch_bounds__(kSSThreads) k_ss_chain(SumIn<T> in, const int* __restrict__ spec,
                                                         const Walk* __restrict__ walks, int blocks,
                                                         double* __restrict__ out, double divisor,
                                                         long long* __restrict__ counts) {
@@ -265,7 +313,7 @@ __global__ void __launch_bounds__(kSSThreads) k_ss_chain(SumIn in, const int* __
     __shared__ Walk sh_warps[kSSThreads / 32];
     __shared__ Walk sh_walks[kBatch];
     __shared__ int sh_spec[kBatch];
-    __shared__ float vals[kSSThreads];
+    __shared__ T vals[kSSThreads];
     __shared__ uint8_t present[kSSThreads];
     __shared__ double s_sh;
     double s = 0.0;   // thread 0's
@@ -291,7 +339,7 @@ __global__ void __launch_bounds__(kSSThreads) k_ss_chain(SumIn in, const int* __
         // The block in pieces of 1024, each reduced for the binade the sum is in when it begins.
         for (int piece = 0; piece < kSSPer; ++piece) {
             const size_t i = (size_t)j * kSSBlock + (size_t)piece * kSSThreads + threadIdx.x;
-            float v = 0.0f;
+            T v = 0;
             const bool has = value_at(in, i, &v);
             vals[threadIdx.x] = v;
             present[threadIdx.x] = has ? 1 : 0;
@@ -326,16 +374,11 @@ __global__ void __launch_bounds__(kSSThreads) k_ss_chain(SumIn in, const int* __
     }
 }
 
-}  // namespace
-
-// The reference's sequential double sum of (mode 0) x or (mode 1) 1 - 0.5 x over the cells of `mask`
-// (every cell when null), in cell order, into *d_out on the device; divided by `divisor` when it is
-// not 0 (the mean's one division, in double).
-cg_status seq_sum_dev(cg_ctx* ctx, const float* d_x, const uint8_t* d_mask, int mode, size_t n, double divisor,
-                      double* d_out, long long* d_counts) {
+template <typename T>
+cg_status seq_sum_run(cg_ctx* ctx, const SumIn<T>& in, double divisor, double* d_out, long long* d_counts) {
+    const size_t n = in.n;
     const int blocks = (int)((n + kSSBlock - 1) / kSSBlock);
     cudaStream_t sm = ctx->stream;
-    SumIn in{d_x, d_mask, mode, n};
     if (blocks == 0) {
         CG_CUDA(ctx, cudaMemsetAsync(d_out, 0, sizeof(double), sm));
         if (d_counts) CG_CUDA(ctx, cudaMemsetAsync(d_counts, 0, 3 * sizeof(long long), sm));
@@ -344,12 +387,27 @@ cg_status seq_sum_dev(cg_ctx* ctx, const float* d_x, const uint8_t* d_mask, int 
     CG_BUF(double, d_est, ctx, S_SS_EST, (size_t)blocks);
     CG_BUF(int, d_spec, ctx, S_SS_SPEC, (size_t)blocks);
     CG_BUF(Walk, d_walks, ctx, S_SS_WALK, (size_t)blocks);
-    CG_LAUNCH(ctx) k_ss_estimate<<<blocks, kSSThreads, 0, sm>>>(in, d_est);
+    CG_LAUNCH(ctx) k_ss_estimate<T><<<blocks, kSSThreads, 0, sm>>>(in, d_est);
     CG_LAUNCH(ctx) k_ss_spec<<<1, 1024, 0, sm>>>(d_est, blocks, d_spec);
-    CG_LAUNCH(ctx) k_ss_walks<<<blocks, kSSThreads, 0, sm>>>(in, d_spec, d_walks);
-    CG_LAUNCH(ctx) k_ss_chain<<<1, kSSThreads, 0, sm>>>(in, d_spec, d_walks, blocks, d_out, divisor, d_counts);
+    CG_LAUNCH(ctx) k_ss_walks<T><<<blocks, kSSThreads, 0, sm>>>(in, d_spec, d_walks);
+    CG_LAUNCH(ctx) k_ss_chain<T><<<1, kSSThreads, 0, sm>>>(in, d_spec, d_walks, blocks, d_out, divisor, d_counts);
     CG_CHECK_LAUNCH(ctx);
     return CG_OK;
+}
+
+}  // namespace
+
+// The reference's sequential double sum of (mode 0) x or (mode 1) 1 - 0.5 x over the cells of `mask`
+// (every cell when null), in cell order, into *d_out on the device; divided by `divisor` when it is
+// not 0 (the mean's one division, in double).
+cg_status seq_sum_dev(cg_ctx* ctx, const float* d_x, const uint8_t* d_mask, int mode, size_t n, double divisor,
+                      double* d_out, long long* d_counts) {
+    return seq_sum_run(ctx, SumIn<float>{d_x, d_mask, mode, n}, divisor, d_out, d_counts);
+}
+
+// `s = 0.0; for (v in x) s += v` over n double terms, into *d_out on the device.
+cg_status seq_sum_f64_dev(cg_ctx* ctx, const double* d_x, size_t n, double* d_out) {
+    return seq_sum_run(ctx, SumIn<double>{d_x, nullptr, 0, n}, 0.0, d_out, nullptr);
 }
 
 }  // namespace cg

@@ -15,7 +15,7 @@ EXPORTS = [
     "cg_thermal_sweeps", "cg_thermal_sweeps_noalloc", "cg_erode_stage", "cg_erode_stage_dev", "cg_erode_batch", "cg_percentile_cut", "cg_fill_depressions", "cg_flow_directions",
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
     "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish", "cg_sea_level_cut",
-    "cg_flexure_deflection", "cg_sequential_sum",
+    "cg_flexure_deflection", "cg_sequential_sum", "cg_sequential_sum_f64", "cg_belt_replay", "cg_gaussian_blur",
 ]
 
 
@@ -77,6 +77,10 @@ def load_library(path=LIB_PATH):
                                            C.POINTER(i32)]
             L.cg_flexure_deflection.argtypes = [vp, PP, vp, vp, C.POINTER(f64), C.POINTER(f64)]
             L.cg_sequential_sum.argtypes = [vp, vp, vp, i32, C.c_int64, C.POINTER(f64), vp]
+            L.cg_sequential_sum_f64.argtypes = [vp, vp, C.c_int64, C.POINTER(f64)]
+            L.cg_belt_replay.argtypes = [vp, PP, vp, C.POINTER(abi.BeltWindow), C.POINTER(abi.BeltInputs), vp,
+                                         C.POINTER(abi.BeltBooks)]
+            L.cg_gaussian_blur.argtypes = [vp, i32, i32, vp, f64, f64]
         _lib = L
         return _lib
 

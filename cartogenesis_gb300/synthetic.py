@@ -8,7 +8,8 @@ cannot run without a JVM, so worlds here are project-written and fully determine
   mapped to the height field's units, (m + 10000) / 16000 (WorldScale.fieldAtAltitude);
 - uplift: millimetres a year, >= 0, in 100-300 km bands along plate boundaries (a seeded
   Voronoi partition of the sphere), or Gaussian ridges along great-circle segments;
-- rock erodibility: a smooth lognormal factor, median 1, log-sigma 0.5.
+- rock erodibility: a smooth lognormal factor, median 1, log-sigma 0.5;
+- the belts' exposure-window history: thickening, wear and onset under the active uplift bands.
 """
 import numpy as np
 
@@ -110,6 +111,22 @@ def world(width, height, seed=1, uplift="bands"):
     up = uplift_bands(width, height, seed) if uplift == "bands" else uplift_ridges(width, height, seed)
     rk = rock_erodibility(width, height, seed)
     return h, up, rk
+
+
+def belt_window(width, height, seed=1, window_myr=40.0, threshold_mm=0.05):
+    """A seeded stand-in for the plate stage's exposure-window history (BeltWindow): the cells under
+    uplift_bands' active bands thickened by 40 km per mm/yr of today's uplift (so the window's rise
+    outruns the rounds' share of today's rate, as a young belt's does), worn by 20-50% of that,
+    beginning 40-100% of the window ago (a smooth field); -1 onset, no thickening and no wear
+    elsewhere. Returns (tectonic_km, wear_km, onset_myr_ago, window_myr), float32 [H, W] and a float."""
+    up = uplift_bands(width, height, seed)
+    belt = up > threshold_mm
+    wear_share = 0.2 + 0.3 * (0.5 + 0.5 * np.tanh(fbm(width, height, beta=3.0, seed=seed, salt=11)))
+    start = 0.4 + 0.6 * (0.5 + 0.5 * np.tanh(fbm(width, height, beta=3.0, seed=seed, salt=12)))
+    tectonic = np.where(belt, 40.0 * up, 0.0).astype(np.float32)
+    wear = np.where(belt, tectonic * wear_share, 0.0).astype(np.float32)
+    onset = np.where(belt, window_myr * start, -1.0).astype(np.float32)
+    return tectonic, wear, onset, float(window_myr)
 
 
 def batch_shapes(n, seed=1, max_rows=2048):

@@ -423,6 +423,65 @@ cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* params, const uint8_t*
                     float* relative, float* ground, const int32_t* receivers, const float* area,
                     float land_cells, float land_range, float* surface, int32_t* cells_cut);
 
+/*
+ * The sequential double sum over n double terms given in the order they are added, `var s = 0.0;
+ * for (v in x) s += v`, bit for bit, by the same parallel walks (host buffers). The belts' replay keeps
+ * its books with it; a running total is carried by laying it first. No counterpart in the reference.
+ */
+cg_status cg_sequential_sum_f64(cg_ctx* ctx, const double* x, int64_t n, double* sum);
+/* ---- The belts' replay (BeltErosion.replay, .../pipeline/BeltErosion.kt:96-425) ----
+ *
+ * Before the hydraulic rounds, when the plate stage hands the erosion the belts' recent history
+ * (ErosionTectonics.window; HydraulicErosion.kt:680-688), each young belt is lowered to where its crust
+ * stood when the exposure window opened, raised again round by round at the rate its own thickening
+ * came at, and cut as it rises: about a hundred rounds over the belt cells alone, each with a priority
+ * flood over the belts, the facet rule, the Kahn order, the implicit incision, the spoil carried to the
+ * belts' outlets and the rounds' thermal sweeps, and every ten rounds the crust's Airy rebound of the
+ * rock taken (a Gaussian of GaussianBlur, .../math/GaussianBlur.kt, at the crust map's spread). */
+/* BeltWindow (BeltErosion.kt:19-24): per cell, what tectonics did to the crust over the window. */
+typedef struct cg_belt_window {
+    const float* tectonic_km;      /* N: km of thickness thickened over the window */
+    const float* wear_km;          /* N: km the orogens' wear took over it */
+    const float* onset_myr_ago;    /* N: when the thickening began, Myr ago; < 0 where none did */
+    double       window_myr;       /* the window's length, Myr (PlateResult.exposureWindowMyr, 40) */
+} cg_belt_window;
+/* The rest of BeltErosion.replay's arguments (host buffers, N floats each where given). */
+typedef struct cg_belt_inputs {
+    const float* uplift_mm_per_year;   /* or NULL: presentUpliftMmPerYear */
+    const float* rainfall_mm;          /* or NULL (all 1): the opening weather's rain */
+    const float* cover_density;        /* or NULL (all 0): the opening weather's cover */
+    const float* rock_erodibility;     /* or NULL */
+    const float* unresolved_relief;    /* or NULL: UnresolvedRelief in the height field's units */
+    float        provisional_sea_level;/* the sea fraction the opening cut takes (WorldGenConfig.seaLevel) */
+    int32_t      shield_cut;           /* 1: the cover's shielding in the incision's factor */
+    int32_t      rebound;              /* IsostasyConfig.enabled: the crust answers the rock taken */
+    double       history_cell_km;      /* TectonicsConfig.historyCellKm (80): the rebound's spread is 0.6 of it */
+} cg_belt_inputs;
+/* BeltReplay (BeltErosion.kt:35-47) without erodedMeters, which the call writes to its own buffer. */
+typedef struct cg_belt_books {
+    int32_t rounds;                         /* 0 where the replay does nothing (BeltReplay.NOTHING) */
+    int32_t belt_cells;
+    double  uplifted_cubic_meters;
+    double  cut_cubic_meters;
+    double  exported_to_sea_cubic_meters;
+    double  exported_to_land_cubic_meters;
+    double  shed_beside_cubic_meters;
+} cg_belt_books;
+/*
+ * BeltErosion.replay on host buffers: `height` (N, the height field) is replayed in place, `eroded_meters`
+ * (N, may be NULL) receives the metres each cell lost, `books` the replay's figures. Reads params' grid,
+ * seed, WorldScale, ErosionConfig (rounds, erodibility, rate, critical fall, debris travel), facet_routing
+ * and flat_potential (the opening's routing) and the isostasy densities. Bit-identical to the reference's
+ * arithmetic; CG_INEXACT if a belt flood's quantised-key ties cannot be ordered exactly.
+ */
+cg_status cg_belt_replay(cg_ctx* ctx, const cg_erosion_params* params, float* height, const cg_belt_window* window,
+                         const cg_belt_inputs* inputs, float* eroded_meters, cg_belt_books* books);
+/* GaussianBlur.apply (.../math/GaussianBlur.kt:44-111) in place on a host field: x wraps, y clamps; a
+ * sigma of zero or less leaves that axis alone. The taps are the Gaussian at cell centres to 4 sigma,
+ * normalised, computed on the host. */
+cg_status cg_gaussian_blur(cg_ctx* ctx, int32_t width, int32_t height, float* field, double sigma_across,
+                           double sigma_down);
+
 #ifdef __cplusplus
 }
 #endif

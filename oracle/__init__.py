@@ -88,6 +88,10 @@ def lib():
         L.or_sea_level_drained_cut.restype = i32
         L.or_flexure_deflection.argtypes = [C.POINTER(abi.ErosionParams), vp, vp, C.POINTER(f64), C.POINTER(f64)]
         L.or_flexure_deflection.restype = i32
+        L.or_belt_replay.argtypes = [C.POINTER(abi.ErosionParams), vp, vp, vp, vp, f64, vp, vp, vp, vp, f32, i32, vp,
+                                     i32, f64, vp, vp, vp]
+        L.or_belt_replay.restype = i32
+        L.or_gaussian_blur.argtypes = [i32, i32, vp, f64, f64]
         _lib = L
     return _lib
 
@@ -395,3 +399,39 @@ def flexure_deflection(params, load):
     d, r = C.c_double(), C.c_double()
     assert lib().or_flexure_deflection(C.byref(params), P(ld), P(out), C.byref(d), C.byref(r)) == 0
     return out, d.value, r.value
+
+
+BELT_BOOKS = ("uplifted_cubic_meters", "cut_cubic_meters", "exported_to_sea_cubic_meters",
+              "exported_to_land_cubic_meters", "shed_beside_cubic_meters")
+
+
+def belt_replay(params, height, tectonic_km, wear_km, onset_myr_ago, window_myr, uplift=None, rain=None, cover=None,
+                rock=None, provisional_sea_level=None, shield_cut=True, unresolved=None, rebound=True,
+                history_cell_km=80.0):
+    """BeltErosion.replay: (height after, eroded metres, dict of the BeltReplay figures)."""
+    H, W = params.height, params.width
+
+    def f32(a):
+        return None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+
+    h = f32(height).copy()
+    t, w, o, u, ra, cv, rk, ur = (f32(a) for a in (tectonic_km, wear_km, onset_myr_ago, uplift, rain, cover, rock,
+                                                  unresolved))
+    eroded = np.zeros((H, W), np.float32)
+    counts = np.zeros(2, np.int32)
+    books = np.zeros(5, np.float64)
+    sea = params.sea_level if provisional_sea_level is None else provisional_sea_level
+    assert lib().or_belt_replay(C.byref(params), P(h), P(t), P(w), P(o), float(window_myr), P(u), P(ra), P(cv), P(rk),
+                                float(sea), int(bool(shield_cut)), P(ur), int(bool(rebound)),
+                                float(history_cell_km), P(eroded), P(counts), P(books)) == 0
+    out = {"rounds": int(counts[0]), "belt_cells": int(counts[1])}
+    out.update({k: float(v) for k, v in zip(BELT_BOOKS, books)})
+    return h, eroded, out
+
+
+def gaussian_blur(field, sigma_across, sigma_down):
+    """GaussianBlur.apply on a copy of `field`."""
+    f = np.ascontiguousarray(field, dtype=np.float32).copy()
+    H, W = f.shape
+    lib().or_gaussian_blur(W, H, P(f), float(sigma_across), float(sigma_down))
+    return f

@@ -2566,6 +2566,406 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     return CG_OK;
 }
 
+// ---------------------------------------------------------------- the belts' replay (P/BeltErosion.kt)
+
+// Kotlin's Double.toInt(): toward zero, NaN to 0, saturating at the Int range.
+int jvm_d2i(double x) {
+    if (std::isnan(x)) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return (int)x;
+}
+
+// GaussianBlur.weights (MA/GaussianBlur.kt:53-65): the continuous Gaussian sampled at cell centres
+// out to 4 standard deviations, normalised to one.
+std::vector<double> gaussian_taps(double sigma) {
+    int radius = std::max(jvm_d2i(std::ceil(4.0 * sigma)), 1);
+    std::vector<double> taps(2 * (size_t)radius + 1);
+    double total = 0.0;
+    for (int off = -radius; off <= radius; ++off) {
+        double z = off / sigma;
+        double w = std::exp(-0.5 * z * z);
+        taps[off + radius] = w;
+        total += w;
+    }
+    for (double& t : taps) t /= total;
+    return taps;
+}
+
+// GaussianBlur.apply (MA/GaussianBlur.kt:44-47, 67-111): across (x wraps) then down (y clamps), each
+// output cell a double sum over the taps in order, rounded to float.
+void gaussian_blur(int W, int H, float* data, double sigma_across, double sigma_down) {
+    const size_t N = (size_t)W * H;
+    std::vector<float> blurred(N);
+    if (sigma_across > 0.0) {
+        std::vector<double> taps = gaussian_taps(sigma_across);
+        const int radius = (int)taps.size() / 2;
+        std::vector<double> padded(W + 2 * (size_t)radius);
+        for (int row = 0; row < H; ++row) {
+            const size_t rs = (size_t)row * W;
+            for (size_t slot = 0; slot < padded.size(); ++slot) {
+                int col = ((int)slot - radius) % W;
+                if (col < 0) col += W;
+                padded[slot] = (double)data[rs + col];
+            }
+            for (int col = 0; col < W; ++col) {
+                double sum = 0.0;
+                for (size_t t = 0; t < taps.size(); ++t) sum += taps[t] * padded[col + t];
+                blurred[rs + col] = (float)sum;
+            }
+        }
+        std::memcpy(data, blurred.data(), N * sizeof(float));
+    }
+    if (sigma_down > 0.0) {
+        std::vector<double> taps = gaussian_taps(sigma_down);
+        const int radius = (int)taps.size() / 2;
+        std::vector<double> sums(W);
+        for (int row = 0; row < H; ++row) {
+            std::fill(sums.begin(), sums.end(), 0.0);
+            for (size_t t = 0; t < taps.size(); ++t) {
+                int src = std::min(std::max(row + (int)t - radius, 0), H - 1);
+                const double w = taps[t];
+                for (int col = 0; col < W; ++col) sums[col] += w * (double)data[(size_t)src * W + col];
+            }
+            for (int col = 0; col < W; ++col) blurred[(size_t)row * W + col] = (float)sums[col];
+        }
+        std::memcpy(data, blurred.data(), N * sizeof(float));
+    }
+}
+
+const double kCrustKernelSpreadSpacings = 0.6;   // CrustMap.KERNEL_SPREAD_SPACINGS (P/CrustMap.kt:521)
+const int kReboundRounds = 10;                   // BeltErosion.REBOUND_ROUNDS
+
+// What BeltErosion.replay hands back (BeltReplay, P/BeltErosion.kt:35-47), erodedMeters aside.
+struct BeltBooks {
+    int rounds = 0, belt_cells = 0;
+    double uplifted = 0.0, cut = 0.0, to_sea = 0.0, to_land = 0.0, shed = 0.0;
+};
+
+// BeltErosion.replay (P/BeltErosion.kt:96-425), statement by statement. `surface` is the height field,
+// changed in place; `eroded` (N) receives the metres each cell lost. rain and cover are required
+// here (the entry point fills the defaults); uplift, rock and unresolved may be null.
+BeltBooks belt_replay(const cg_erosion_params& p, float* surface, const float* tectonic, const float* wear,
+                      const float* onset, double window_myr, const float* uplift, const float* rain,
+                      const float* cover, const float* rock, float provisional_sea_level, bool shield_cut,
+                      const float* unresolved, bool rebounding, double history_cell_km, float* eroded) {
+    BeltBooks books;
+    const int W = p.width, H = p.height;
+    const size_t N = (size_t)W * H;
+    std::fill(eroded, eroded + N, 0.0f);
+    const Scale sc = scale_of(p);
+    const double round_years = sc.years_per_round;
+    const double round_myr = round_years / 1e6;
+    const double main_myr = p.hydraulic_rounds * round_myr;
+    const int rounds = jvm_d2i((window_myr - main_myr) / round_myr + 1e-9);   // ROUND_ROUNDING
+    if (rounds <= 0 || p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) return books;
+
+    const float freeboard = (p.mantle_density - p.continental_crust_density) / p.mantle_density * 1000.0f;
+    const float mpfu = sc.relief_span();   // metersPerFieldUnit
+
+    // The belts, and each one's rise (BeltErosion.kt:127-144).
+    std::vector<int> belt;
+    std::vector<int> local_of(N, -1);
+    for (size_t c = 0; c < N; ++c)
+        if (onset[c] >= 0.0f) {
+            local_of[c] = (int)belt.size();
+            belt.push_back((int)c);
+        }
+    if (belt.empty()) return books;
+    const int B = (int)belt.size();
+    std::vector<float> rise_per(B);
+    std::vector<int> first_round(B);
+    for (int l = 0; l < B; ++l) {
+        const int c = belt[l];
+        surface[c] = surface[c] - freeboard * (tectonic[c] - wear[c]) / mpfu;
+        const double rounds_share =
+            uplift ? (double)(uplift[c] * (float)p.hydraulic_rounds) * round_years / 1000.0 : 0.0;
+        const double rise_m = (double)(freeboard * tectonic[c]) - rounds_share;
+        int f = jvm_d2i(std::ceil((window_myr - (double)onset[c]) / round_myr - 1e-9));
+        f = std::min(std::max(f, 0), rounds - 1);
+        first_round[l] = f;
+        rise_per[l] = (float)(rise_m / (double)(rounds - f) / (double)mpfu);
+    }
+
+    // The sea the belts' rivers reach, cut once as the window opens (BeltErosion.kt:147-163).
+    Cut opening;
+    percentile_cut(W, H, surface, provisional_sea_level, sc, 0.0f, opening);
+    const u8* is_land = opening.is_land.data();
+    const float shoreline = opening.shoreline;
+    const float land_cells = std::max((float)opening.land_cells, 1.0f);
+    std::vector<float> weights(N), factor(N);
+    double rain_sum = 0.0;
+    for (size_t c = 0; c < N; ++c)
+        if (is_land[c]) rain_sum += (double)rain[c];
+    const float rain_mean = (float)(rain_sum / (double)land_cells);
+    for (size_t c = 0; c < N; ++c) weights[c] = rain_mean > 0.0f ? rain[c] / rain_mean : 1.0f;
+    double cover_sum = 0.0;
+    for (size_t c = 0; c < N; ++c)
+        if (is_land[c]) cover_sum += (double)(1.0f - kVegetationShielding * cover[c]);
+    const float cover_mean = (float)(cover_sum / (double)land_cells);
+    for (size_t c = 0; c < N; ++c) {
+        const float cv = (shield_cut && cover_mean > 0.0f) ? (1.0f - kVegetationShielding * cover[c]) / cover_mean : 1.0f;
+        factor[c] = cv * (rock ? rock[c] : 1.0f);
+    }
+
+    // The water reaching the belts from beyond them, routed once over the opening ground
+    // (BeltErosion.kt:166-181).
+    const double r = sc.cell_height_km(H) / sc.cell_width_km(W);
+    std::vector<double> inflow(B, 0.0);
+    {
+        std::vector<float> filled0(N), area(N);
+        std::vector<int32_t> dirs(N);
+        fill_depressions(W, H, is_land, opening.relative.data(), filled0.data());
+        flow_directions(W, H, is_land, opening.relative.data(), filled0.data(), p.seed, r,
+                        smooth_field_lattice_columns(sc.world_width_km), p.facet_routing != 0, p.flat_potential != 0,
+                        dirs.data(), nullptr, nullptr);
+        accumulate(W, H, is_land, dirs.data(), opening.land_cells, weights.data(), area.data());
+        for (size_t c = 0; c < N; ++c) {
+            const int rc = dirs[c];
+            if (rc < 0 || local_of[c] >= 0) continue;
+            const int l = local_of[rc];
+            if (l >= 0) inflow[l] += (double)area[c];
+        }
+    }
+
+    // The ground just beyond the belts (BeltErosion.kt:184-195).
+    std::vector<int> frontier;
+    std::vector<u8> on_frontier(N, 0);
+    for (int c : belt)
+        for_each_neighbour(W, H, c % W, c / W, [&](int n, int, int) {
+            if (local_of[n] < 0 && !on_frontier[n]) {
+                on_frontier[n] = 1;
+                frontier.push_back(n);
+            }
+        });
+    std::sort(frontier.begin(), frontier.end());
+    std::vector<int> swept(belt);
+    swept.insert(swept.end(), frontier.begin(), frontier.end());
+
+    const Rates rates(p);
+    const GroundSteps steps(r);
+    const float pond_depth_field = kPondDepthMetres / mpfu;
+    const int sweeps_per_round = std::max(sweeps_for(p) / std::max(p.hydraulic_rounds, 1), 1);
+    const cg_thermal_limits lim = thermal_limits(p);
+    const float courant = rates.courant_coefficient;
+
+    std::vector<double> routing(N);
+    for (size_t c = 0; c < N; ++c) routing[c] = (double)surface[c];
+    std::vector<float> filled(B, 0.0f), give(B, 0.0f), next(swept.size());
+    std::vector<int> receiver(B), donors(B), run_order(B);
+    std::vector<double> discharge(B), flux(B);
+    std::vector<u8> visited(B);
+    const double cell_area = sc.cell_width_km(W) * sc.cell_height_km(H) * 1e6;
+
+    std::vector<float> reference, uplifted_m, rebound_m, loss(N);
+    if (rebounding) {
+        reference.assign(surface, surface + N);
+        uplifted_m.assign(N, 0.0f);
+        rebound_m.assign(N, 0.0f);
+    }
+    const float rebound_share = p.continental_crust_density / p.mantle_density;
+    const double crust_spread_km = kCrustKernelSpreadSpacings * history_cell_km;
+
+    // forEachNeighborWithLimit's limit by step (BeltErosion.kt:445-466).
+    auto limit_of = [&](int rs, int cs) {
+        return (rs != 0 && cs != 0) ? lim.diagonal : (rs != 0 ? lim.north_south : lim.east_west);
+    };
+    auto at_sea = [&](int c) { return !is_land[c] || surface[c] <= shoreline; };
+
+    for (int round = 0; round < rounds; ++round) {
+        // The rock rises where the belt has begun to (BeltErosion.kt:240-248).
+        for (int l = 0; l < B; ++l) {
+            if (round < first_round[l]) continue;
+            const float rise = rise_per[l];
+            const int c = belt[l];
+            surface[c] = surface[c] + rise;
+            if (rebounding) uplifted_m[c] = uplifted_m[c] + rise * mpfu;
+            books.uplifted += (double)rise * (double)mpfu * cell_area;
+        }
+        for (int c : swept) routing[c] = (double)surface[c];
+
+        // Every belt cell's spill level, by a priority flood (BeltErosion.kt:253-284).
+        std::fill(visited.begin(), visited.end(), 0);
+        std::priority_queue<int64_t, std::vector<int64_t>, std::greater<int64_t>> heap;
+        for (int l = 0; l < B; ++l) {
+            const int c = belt[l];
+            if (at_sea(c)) {
+                filled[l] = surface[c];
+                visited[l] = 1;
+                heap.push(encode(surface[c], l));
+                continue;
+            }
+            bool edge = false;
+            for_each_neighbour(W, H, c % W, c / W, [&](int n, int, int) {
+                if (local_of[n] < 0) edge = true;
+            });
+            if (c / W == 0 || c / W == H - 1) edge = true;
+            if (edge) {
+                filled[l] = surface[c];
+                visited[l] = 1;
+                heap.push(encode(surface[c], l));
+            }
+        }
+        while (!heap.empty()) {
+            const int l = decode_index(heap.top());
+            heap.pop();
+            const float level = filled[l];
+            const int c = belt[l];
+            for_each_neighbour(W, H, c % W, c / W, [&](int n, int, int) {
+                const int o = local_of[n];
+                if (o >= 0 && !visited[o]) {
+                    visited[o] = 1;
+                    filled[o] = surface[n] <= level ? level + kFlatGradientStep : surface[n];
+                    heap.push(encode(filled[o], o));
+                }
+            });
+        }
+        for (int l = 0; l < B; ++l) {
+            const int c = belt[l];
+            if (is_land[c] && surface[c] > shoreline) routing[c] = (double)filled[l];
+        }
+        // The facet rule over the filled ground (BeltErosion.kt:286-292).
+        for (int l = 0; l < B; ++l) {
+            const int c = belt[l];
+            receiver[l] = at_sea(c) ? -1 : facet_receiver(W, H, routing.data(), c % W, c / W, steps, p.seed);
+        }
+        // The order the water runs in (BeltErosion.kt:296-311).
+        std::fill(donors.begin(), donors.end(), 0);
+        for (int l = 0; l < B; ++l) {
+            const int d = receiver[l];
+            if (d < 0) continue;
+            const int dl = local_of[d];
+            if (dl >= 0) donors[dl]++;
+        }
+        int downstream = 0;
+        for (int l = 0; l < B; ++l)
+            if (donors[l] == 0) run_order[downstream++] = l;
+        int walked = 0;
+        while (walked < downstream) {
+            const int d = receiver[run_order[walked++]];
+            if (d < 0) continue;
+            const int dl = local_of[d];
+            if (dl >= 0 && --donors[dl] == 0) run_order[downstream++] = dl;
+        }
+        // Water gathered from the top down (BeltErosion.kt:313-323).
+        for (int l = 0; l < B; ++l) {
+            discharge[l] = (double)weights[belt[l]] + inflow[l];
+            flux[l] = 0.0;
+        }
+        for (int i = 0; i < downstream; ++i) {
+            const int l = run_order[i];
+            const int d = receiver[l];
+            if (d < 0) continue;
+            const int dl = local_of[d];
+            if (dl >= 0) discharge[dl] += discharge[l];
+        }
+        // The cut, from the outlets up (BeltErosion.kt:325-351).
+        for (int i = downstream - 1; i >= 0; --i) {
+            const int l = run_order[i];
+            const int c = belt[l];
+            const int d = receiver[l];
+            if (d < 0) continue;
+            if (filled[l] - surface[c] > pond_depth_field) continue;
+            const int dl = local_of[d];
+            const float own = unresolved ? unresolved[c] : 0.0f;
+            float base;
+            if (at_sea(d)) base = shoreline + own;
+            else if (dl >= 0 && filled[dl] - surface[d] > pond_depth_field) base = filled[dl] + own;
+            else base = surface[d] + own - (unresolved ? unresolved[d] : 0.0f);
+            const float height = surface[c];
+            if (height <= base) continue;
+            const double share = discharge[l] / (double)land_cells;
+            const double cn = (double)courant * std::sqrt(share) * (double)factor[c] / (double)steps.between(c, d, W);
+            const float after = (float)((double)base + (double)(height - base) / (1.0 + cn));
+            surface[c] = after;
+            const float lost = (height - after) * mpfu;
+            eroded[c] = eroded[c] + lost;
+            books.cut += (double)lost * cell_area;
+            flux[l] += (double)lost * cell_area;
+        }
+        // The spoil carried down to where it leaves the belts (BeltErosion.kt:354-370).
+        for (int i = 0; i < downstream; ++i) {
+            const int l = run_order[i];
+            const int d = receiver[l];
+            if (d < 0) {
+                if (at_sea(belt[l])) books.to_sea += flux[l];
+                else books.to_land += flux[l];
+                continue;
+            }
+            const int dl = local_of[d];
+            if (dl >= 0) flux[dl] += flux[l];
+            else if (at_sea(d)) books.to_sea += flux[l];
+            else books.to_land += flux[l];
+        }
+
+        // The slopes, relaxed by the rounds' own sweeps (BeltErosion.kt:373-408).
+        for (int s = 0; s < sweeps_per_round; ++s) {
+            for (int l = 0; l < B; ++l) {
+                const int c = belt[l], col = c % W, row = c / W;
+                const float here = surface[c];
+                float excess = 0.0f, steepest = 0.0f;
+                for (int rs = -1; rs <= 1; ++rs) {
+                    const int nr = row + rs;
+                    if (nr < 0 || nr >= H) continue;
+                    for (int cs = -1; cs <= 1; ++cs) {
+                        if (rs == 0 && cs == 0) continue;
+                        const int n = nr * W + (col + cs + W) % W;
+                        const float drop = here - surface[n];
+                        if (drop > 0.0f) {
+                            if (drop > steepest) steepest = drop;
+                            const float limit = limit_of(rs, cs);
+                            if (drop > limit) excess += drop - limit;
+                        }
+                    }
+                }
+                give[l] = excess <= lim.east_west * 1e-3f
+                              ? 0.0f
+                              : jvm_min(p.rate * excess, steepest * 0.5f) / excess;
+            }
+            for (size_t k = 0; k < swept.size(); ++k) {
+                const int c = swept[k], col = c % W, row = c / W;
+                const float here = surface[c];
+                const int own = local_of[c];
+                float received = 0.0f, given = 0.0f;
+                for (int rs = -1; rs <= 1; ++rs) {
+                    const int nr = row + rs;
+                    if (nr < 0 || nr >= H) continue;
+                    for (int cs = -1; cs <= 1; ++cs) {
+                        if (rs == 0 && cs == 0) continue;
+                        const int n = nr * W + (col + cs + W) % W;
+                        const float limit = limit_of(rs, cs);
+                        const float incoming = surface[n] - here;
+                        const int giver = local_of[n];
+                        if (incoming > limit && giver >= 0) received += give[giver] * (incoming - limit);
+                        else if (-incoming > limit && own >= 0) given += give[own] * (-incoming - limit);
+                    }
+                }
+                next[k] = here - given + received;
+            }
+            for (size_t k = 0; k < swept.size(); ++k) {
+                const int c = swept[k];
+                if (local_of[c] < 0) books.shed += (double)(next[k] - surface[c]) * (double)mpfu * cell_area;
+                surface[c] = next[k];
+            }
+        }
+
+        // The crust answering the rock taken so far (BeltErosion.kt:413-423).
+        if (rebounding && ((round + 1) % kReboundRounds == 0 || round == rounds - 1)) {
+            for (size_t c = 0; c < N; ++c)
+                loss[c] = uplifted_m[c] + rebound_m[c] - (surface[c] - reference[c]) * mpfu;
+            gaussian_blur(W, H, loss.data(), crust_spread_km / sc.cell_width_km(W), crust_spread_km / sc.cell_height_km(H));
+            for (size_t c = 0; c < N; ++c) {
+                const float rebound = rebound_share * loss[c];
+                surface[c] = surface[c] + (rebound - rebound_m[c]) / mpfu;
+                rebound_m[c] = rebound;
+            }
+        }
+    }
+    books.rounds = rounds;
+    books.belt_cells = B;
+    return books;
+}
+
 }  // namespace
 
 // ================================================================ C entry points (ctypes)
@@ -2872,6 +3272,43 @@ int32_t or_flexure_deflection(const cg_erosion_params* p, const float* load, flo
 
 int32_t or_stage_rounds(const cg_erosion_params* p, const cg_inputs* in, cg_outputs* out, int32_t rounds) {
     return erode_stage(*p, *in, out, nullptr, true, false, rounds);
+}
+
+// BeltErosion.replay (BeltErosion.kt:96-425) on host buffers: `height` is changed in place, `eroded`
+// (N) receives the metres each cell lost, counts[2] the rounds and belt cells, books[5] the cubic
+// metres uplifted, cut, exported to the sea and to the land, and shed beside. rain and cover may be
+// null (all 1, all 0).
+int32_t or_belt_replay(const cg_erosion_params* p, float* height, const float* tectonic, const float* wear,
+                       const float* onset, double window_myr, const float* uplift, const float* rain,
+                       const float* cover, const float* rock, float provisional_sea_level, int32_t shield_cut,
+                       const float* unresolved, int32_t rebounding, double history_cell_km, float* eroded,
+                       int32_t* counts, double* books) {
+    const size_t N = (size_t)p->width * p->height;
+    std::vector<float> ones, zeros;
+    if (!rain) {
+        ones.assign(N, 1.0f);
+        rain = ones.data();
+    }
+    if (!cover) {
+        zeros.assign(N, 0.0f);
+        cover = zeros.data();
+    }
+    BeltBooks b = belt_replay(*p, height, tectonic, wear, onset, window_myr, uplift, rain, cover, rock,
+                              provisional_sea_level, shield_cut != 0, unresolved, rebounding != 0, history_cell_km,
+                              eroded);
+    counts[0] = b.rounds;
+    counts[1] = b.belt_cells;
+    books[0] = b.uplifted;
+    books[1] = b.cut;
+    books[2] = b.to_sea;
+    books[3] = b.to_land;
+    books[4] = b.shed;
+    return 0;
+}
+
+// GaussianBlur.apply (MA/GaussianBlur.kt:44-111) in place.
+void or_gaussian_blur(int32_t W, int32_t H, float* data, double sigma_across, double sigma_down) {
+    gaussian_blur(W, H, data, sigma_across, sigma_down);
 }
 
 }  // extern "C"

@@ -47,6 +47,8 @@ int main(void) {
   O(cg_erosion_params, seed) O(cg_erosion_params, world_width_km) O(cg_erosion_params, years_per_hydraulic_round)
   O(cg_erosion_params, debris_travel_km) O(cg_erosion_params, sea_level) O(cg_erosion_params, profile)
   O(cg_outputs, basins) O(cg_basins, largest) O(cg_round_stats, fill_ties) O(cg_round_stats, ms_total) O(cg_round_stats, ms_relax)
+  S(cg_belt_window) S(cg_belt_inputs) S(cg_belt_books) O(cg_belt_window, window_myr)
+  O(cg_belt_inputs, provisional_sea_level) O(cg_belt_inputs, history_cell_km) O(cg_belt_books, uplifted_cubic_meters)
   return 0;
 }
 """
@@ -58,7 +60,8 @@ int main(void) {
     got = dict(line.rsplit(" ", 1) for line in out if line)
     types = {"cg_erosion_params": abi.ErosionParams, "cg_inputs": abi.Inputs, "cg_outputs": abi.Outputs,
              "cg_basins": abi.Basins, "cg_round_stats": abi.RoundStats, "cg_thermal_limits": abi.ThermalLimits,
-             "cg_world": abi.World}
+             "cg_world": abi.World, "cg_belt_window": abi.BeltWindow, "cg_belt_inputs": abi.BeltInputs,
+             "cg_belt_books": abi.BeltBooks}
     for k, v in got.items():
         if "." in k:
             t, f = k.split(".")
