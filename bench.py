@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--batched", type=int, default=0, metavar="WORLDS",
                     help="the batched workload instead: WORLDS planets of radius U(0.25, 2.0) Earth radii (grids "
                          "512 x 256 to 4096 x 2048, each its own seed) through cg_erode_batch, one batch per step")
+    ap.add_argument("--belt", action="store_true",
+                    help="the belts' replay instead (BeltErosion.replay, about a hundred rounds over the young "
+                         "belts of a 40 Myr exposure window) on the --width x --height world, through "
+                         "cg_belt_replay; the line reports belt cell-rounds per second")
     ap.add_argument("--passes", type=int, default=4, help="--case thermal: sweeps")
     ap.add_argument("--rounds", type=int, default=2, help="--case stage: hydraulic rounds")
     ap.add_argument("--cpu-sample", type=int, default=1,
@@ -420,10 +424,67 @@ def run_batched(args):
     return 0
 
 
+def run_belt(args):
+    """The belts' replay (BeltErosion.replay) through its public host-buffer call: the world's heights,
+    window and factors in, the replayed heights and eroded depths out, every copy inside the timing.
+    The unit is Mcell-rounds/s over the belt's cells: belt cells x replayed rounds / seconds. The CPU
+    leg runs the oracle's replay of the same world over a window cut to --cpu-sample replayed rounds."""
+    import numpy as np
+    import oracle
+    from cartogenesis_gb300 import BeltErosion, BeltWindow, ErosionConfig, synthetic
+    from cartogenesis_gb300.api import default_context
+    W, H, seed = args.width, args.height, 3
+    h, up, rk = synthetic.world(W, H, seed)
+    t, w, o, win = synthetic.belt_window(W, H, seed)
+    cfg = ErosionConfig(W, H, seed)
+    window = BeltWindow(t, w, o, win)
+    ctx = default_context()
+    for _ in range(args.warmup):
+        r = BeltErosion.replay(cfg, h.copy(), window, up, None, None, rk, ctx=ctx)
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = ctx.kernel_launches
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = BeltErosion.replay(cfg, h.copy(), window, up, None, None, rk, ctx=ctx)
+    dt = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    units = r.belt_cells * r.rounds
+    value = units / dt / 1e6
+    cpu = None
+    if args.cpu_sample > 0:
+        p = oracle.default_params(W, H, seed)
+        round_myr = p.years_per_hydraulic_round / 1e6
+        short = (ROUNDS + args.cpu_sample + 0.5) * round_myr
+        tc = time.perf_counter()
+        _, _, b = oracle.belt_replay(p, h, t, w, o, short, uplift=up, rock=rk)
+        tc = time.perf_counter() - tc
+        cpu = {"value": round(b["belt_cells"] * b["rounds"] / tc / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"the oracle's replay of the same world over a window of {b['rounds']} replayed rounds"}
+    n = W * H
+    line = {
+        "metric": "belt replay Mcell-rounds/s (belt cells x replayed rounds)", "value": round(value, 3), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * dt, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"BeltErosion.replay over {r.belt_cells} belt cells of the {W}x{H} world, "
+                               f"{r.rounds} rounds of a 40 Myr window, through the host-buffer call (value = e2e)",
+                   "grid": [W, H], "belt_cells": r.belt_cells, "rounds": r.rounds, "l2": "the world's fields exceed L2"
+                   if n * 4 > 129e6 else "fits L2"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 4 * n * 6, "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": int(ctx.kernel_launches - launches0),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.case:
         return run_case(args)
+    if args.belt:
+        return run_belt(args)
     if args.batched:
         return run_batched(args)
     if args.impl == "reference":

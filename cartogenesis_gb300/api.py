@@ -206,6 +206,29 @@ class StageRounds:
         self.next_round = end_round
         return [{f: getattr(s, f) for f, _ in abi.RoundStats._fields_} for s in stats[:max(end_round - first, 0)]]
 
+    def replay_belts(self, window, rainfall_mm=None, vegetation_density=None, rebound=True, history_cell_km=80.0):
+        """BeltErosion.replay on the resident swept terrain before round 0 (cg_stage_replay_belts), as
+        HydraulicErosion.apply runs it (P/HydraulicErosion.kt:680-688): the stage's uplift, rock, sea
+        level and shield_cut, the given opening weather (or, with neither field given, the weather the
+        world was begun with), no sub-grid relief. Returns the BeltReplay."""
+        H, W = self.shape
+        fields = [_f32(a, (H, W)) for a in (window.tectonic_km, window.wear_km, window.onset_myr_ago)]
+        win = abi.BeltWindow(*[P(a) for a in fields], float(window.window_myr))
+        weather = None
+        if rainfall_mm is not None or vegetation_density is not None:
+            wk = [_f32(a, (H, W)) for a in (rainfall_mm, vegetation_density)]
+            weather = abi.Weather(*[P(a) for a in wk])
+        eroded = np.empty((H, W), np.float32)
+        books = abi.BeltBooks()
+        with self.ctx.lock:
+            self.ctx.check(self.ctx.lib.cg_stage_replay_belts(self.ctx.handle, C.byref(win),
+                                                              C.byref(weather) if weather is not None else None,
+                                                              int(bool(rebound)), float(history_cell_km), P(eroded),
+                                                              C.byref(books)))
+        return BeltReplay(books.rounds, books.belt_cells, books.uplifted_cubic_meters, books.cut_cubic_meters,
+                          books.exported_to_sea_cubic_meters, books.exported_to_land_cubic_meters,
+                          books.shed_beside_cubic_meters, eroded)
+
     def height(self):
         out = np.empty(self.shape, np.float32)
         with self.ctx.lock:

@@ -560,17 +560,7 @@ cg_status gaussian_blur_dev(cg_ctx* ctx, int W, int H, float* d_field, float* d_
     return CG_OK;
 }
 
-// Device copies of the replay's per-cell inputs; rain and cover always present, the rest may be null.
-struct BeltInputsDev {
-    const float* tectonic;
-    const float* wear;
-    const float* onset;
-    const float* uplift;
-    const float* rain;
-    const float* cover;
-    const float* rock;
-    const float* unresolved;
-};
+}  // namespace
 
 cg_status belt_replay_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, const BeltInputsDev& in,
                           double window_myr, const cg_belt_inputs& opt, float* d_eroded, cg_belt_books* books) {
@@ -808,6 +798,42 @@ cg_status belt_replay_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, c
     return CG_OK;
 }
 
+cg_status belt_window_dev(cg_ctx* ctx, const cg_erosion_params& p, const cg_belt_window& w, BeltInputsDev* in) {
+    const size_t N = (size_t)p.width * p.height;
+    const float** dst[3] = {&in->tectonic, &in->wear, &in->onset};
+    const float* src[3] = {w.tectonic_km, w.wear_km, w.onset_myr_ago};
+    const int slots[3] = {S_BT_TECT, S_BT_WEAR, S_BT_ONSET};
+    for (int i = 0; i < 3; ++i) {
+        cg_status st = CG_OK;
+        float* d = (float*)buf(ctx, slots[i], N * 4, &st);
+        if (st != CG_OK) return st;
+        CG_CUDA(ctx, cudaMemcpyAsync(d, src[i], N * 4, cudaMemcpyHostToDevice, ctx->stream));
+        *dst[i] = d;
+    }
+    return CG_OK;
+}
+
+cg_status belt_weather_dev(cg_ctx* ctx, int W, int H, const float* d_rain, const float* d_cover, BeltInputsDev* in) {
+    const size_t N = (size_t)W * H;
+    const int grid = ctx->num_sms * 8;
+    in->rain = d_rain;
+    in->cover = d_cover;
+    if (!in->rain) {
+        CG_BUF(float, d, ctx, S_BT_RAIN, N);
+        CG_LAUNCH(ctx) k_fill_f<<<grid, 256, 0, ctx->stream>>>(d, N, 1.0f);
+        in->rain = d;
+    }
+    if (!in->cover) {
+        CG_BUF(float, d, ctx, S_BT_COVER, N);
+        CG_LAUNCH(ctx) k_fill_f<<<grid, 256, 0, ctx->stream>>>(d, N, 0.0f);
+        in->cover = d;
+    }
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+namespace {
+
 // Uploads one optional host field into its slot (null stays null).
 cg_status upload_optional(cg_ctx* ctx, int slot, const float* host, size_t N, const float** d) {
     *d = nullptr;
@@ -841,29 +867,17 @@ extern "C" cg_status cg_belt_replay(cg_ctx* ctx, const cg_erosion_params* params
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t N = (size_t)params->width * params->height;
     cudaStream_t sm = ctx->stream;
-    const int grid = ctx->num_sms * 8;
     CG_BUF(float, d_h, ctx, S_BT_H, N);
     CG_CUDA(ctx, cudaMemcpyAsync(d_h, height, N * 4, cudaMemcpyHostToDevice, sm));
     BeltInputsDev in{};
-    CG_TRY_ST(upload_optional(ctx, S_BT_TECT, window->tectonic_km, N, &in.tectonic));
-    CG_TRY_ST(upload_optional(ctx, S_BT_WEAR, window->wear_km, N, &in.wear));
-    CG_TRY_ST(upload_optional(ctx, S_BT_ONSET, window->onset_myr_ago, N, &in.onset));
+    const float *d_rain, *d_cover;
+    CG_TRY_ST(belt_window_dev(ctx, *params, *window, &in));
     CG_TRY_ST(upload_optional(ctx, S_BT_UPLIFT, inputs->uplift_mm_per_year, N, &in.uplift));
     CG_TRY_ST(upload_optional(ctx, S_BT_ROCK, inputs->rock_erodibility, N, &in.rock));
     CG_TRY_ST(upload_optional(ctx, S_BT_UNRES, inputs->unresolved_relief, N, &in.unresolved));
-    CG_TRY_ST(upload_optional(ctx, S_BT_RAIN, inputs->rainfall_mm, N, &in.rain));
-    CG_TRY_ST(upload_optional(ctx, S_BT_COVER, inputs->cover_density, N, &in.cover));
-    if (!in.rain) {
-        CG_BUF(float, d, ctx, S_BT_RAIN, N);
-        CG_LAUNCH(ctx) k_fill_f<<<grid, 256, 0, sm>>>(d, N, 1.0f);
-        in.rain = d;
-    }
-    if (!in.cover) {
-        CG_BUF(float, d, ctx, S_BT_COVER, N);
-        CG_LAUNCH(ctx) k_fill_f<<<grid, 256, 0, sm>>>(d, N, 0.0f);
-        in.cover = d;
-    }
-    CG_CHECK_LAUNCH(ctx);
+    CG_TRY_ST(upload_optional(ctx, S_BT_RAIN, inputs->rainfall_mm, N, &d_rain));
+    CG_TRY_ST(upload_optional(ctx, S_BT_COVER, inputs->cover_density, N, &d_cover));
+    CG_TRY_ST(belt_weather_dev(ctx, params->width, params->height, d_rain, d_cover, &in));
     CG_BUF(float, d_eroded, ctx, S_BT_ERODED, N);
     CG_TRY_ST(belt_replay_dev(ctx, *params, d_h, in, window->window_myr, *inputs, d_eroded, books));
     CG_CUDA(ctx, cudaMemcpyAsync(height, d_h, N * 4, cudaMemcpyDeviceToHost, sm));

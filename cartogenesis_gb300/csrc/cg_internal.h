@@ -177,6 +177,29 @@ cg_status deposit_settle_dev(cg_ctx* ctx, int W, int H, float* d_h);
 // buffers of its own: the stage's last routing is left as it was.
 cg_status open_mouths_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, const float* d_rain);
 
+// ---- the belts' replay (cg_belt.cu)
+// The replay's per-cell inputs on the device: the window (tectonic, wear, onset) required, rain and
+// cover always present (belt_weather_dev fills ones and zeros for null), the rest may be null.
+struct BeltInputsDev {
+    const float* tectonic;
+    const float* wear;
+    const float* onset;
+    const float* uplift;
+    const float* rain;
+    const float* cover;
+    const float* rock;
+    const float* unresolved;
+};
+// Uploads the window's three fields into the replay's slots.
+cg_status belt_window_dev(cg_ctx* ctx, const cg_erosion_params& p, const cg_belt_window& w, BeltInputsDev* in);
+// Sets the replay's rain and cover to the given device fields, or to ones and zeros where null.
+cg_status belt_weather_dev(cg_ctx* ctx, int W, int H, const float* d_rain, const float* d_cover, BeltInputsDev* in);
+// BeltErosion.replay (BeltErosion.kt:96-425) on the device field d_h (replayed in place); d_eroded
+// (N) receives the metres each cell lost. Of `opt` it reads the sea level, shield_cut, rebound and
+// history_cell_km (its pointers are the host call's, unused here). Synchronises before it returns.
+cg_status belt_replay_dev(cg_ctx* ctx, const cg_erosion_params& p, float* d_h, const BeltInputsDev& in,
+                          double window_myr, const cg_belt_inputs& opt, float* d_eroded, cg_belt_books* books);
+
 // ---- small helpers (cg_api.cu)
 cg_status sync(cg_ctx* ctx);
 

@@ -622,6 +622,57 @@ cg_status cg_erode_rounds(cg_ctx* ctx, int32_t first_round, int32_t end_round, c
     return sync(ctx);
 }
 
+cg_status cg_stage_replay_belts(cg_ctx* ctx, const cg_belt_window* window, const cg_weather* weather,
+                                int32_t rebound, double history_cell_km, float* eroded_meters,
+                                cg_belt_books* books) {
+    if (!ctx || !window || !books || !window->tectonic_km || !window->wear_km || !window->onset_myr_ago)
+        return CG_BAD_ARG;
+    StageRun& run = ctx->run;
+    if (!run.active) return fail(ctx, CG_BAD_ARG, "no resident world: call cg_stage_begin first");
+    if (run.next_round != 0) return fail(ctx, CG_BAD_ARG, "the belts replay before round 0, not after round %d",
+                                         run.next_round);
+    const cg_erosion_params& p = run.p;
+    const size_t N = (size_t)p.width * p.height;
+    *books = cg_belt_books{};
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cancel.store(0);
+    // HydraulicErosion.apply returns before the replay when the stage erodes nothing
+    // (HydraulicErosion.kt:632): run.done is set then, and the terrain is left as the sweeps left it.
+    if (run.done) {
+        if (eroded_meters) std::memset(eroded_meters, 0, N * 4);
+        return CG_OK;
+    }
+    BeltInputsDev in{};
+    CG_TRY(belt_window_dev(ctx, p, *window, &in));
+    in.uplift = run.uplift;
+    in.rock = run.rock;
+    const float* d_rain = run.rain;
+    const float* d_veg = run.veg;
+    if (weather) {   // the opening weather, when the caller solves it (climate_feed); NULL fields are the defaults
+        float *r = nullptr, *v = nullptr;
+        CG_TRY(upload_optional(ctx, S_BT_RAIN, weather->rainfall_mm, N, &r));
+        CG_TRY(upload_optional(ctx, S_BT_COVER, weather->vegetation_density, N, &v));
+        d_rain = r;
+        d_veg = v;
+    }
+    CG_TRY(belt_weather_dev(ctx, p.width, p.height, d_rain, d_veg, &in));
+    cg_belt_inputs opt{};
+    opt.provisional_sea_level = p.sea_level;   // ErosionStage.apply hands config.seaLevel (ErosionStage.kt:174)
+    opt.shield_cut = p.shield_cut;
+    opt.rebound = rebound;
+    opt.history_cell_km = history_cell_km;
+    CG_BUF(float, d_eroded, ctx, S_BT_ERODED, N);
+    cg_status st = belt_replay_dev(ctx, p, run.cur, in, window->window_myr, opt, d_eroded, books);
+    if (st != CG_OK) {
+        run.active = false;   // the replay stopped part way: the world is no longer a whole terrain
+        return st;
+    }
+    // HydraulicErosion.kt:707-725: the flexure's field before the rounds is the replayed one (P3).
+    if (p.profile >= CG_PROFILE_P3) CG_TRY(flexure_stage_begin_dev(ctx, p, run.cur, run.uplift != nullptr));
+    if (eroded_meters) CG_TRY(down(ctx, eroded_meters, d_eroded, N * 4));
+    return sync(ctx);
+}
+
 cg_status cg_stage_height(cg_ctx* ctx, float* height) {
     if (!ctx || !height) return CG_BAD_ARG;
     if (!ctx->run.active) return fail(ctx, CG_BAD_ARG, "no resident world: call cg_stage_begin first");

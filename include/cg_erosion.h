@@ -276,6 +276,44 @@ cg_status cg_erode_stage(cg_ctx* ctx, const cg_erosion_params* params, const cg_
 cg_status cg_erode_stage_dev(cg_ctx* ctx, const cg_erosion_params* params, const cg_inputs* inputs_dev,
                              float* height_out_dev, cg_round_stats* stats, int32_t* land_cells);
 
+/* ---- The belts' replay (BeltErosion.replay, .../pipeline/BeltErosion.kt:96-425) ----
+ *
+ * Before the hydraulic rounds, when the plate stage hands the erosion the belts' recent history
+ * (ErosionTectonics.window; HydraulicErosion.kt:680-688), each young belt is lowered to where its crust
+ * stood when the exposure window opened, raised again round by round at the rate its own thickening
+ * came at, and cut as it rises: about a hundred rounds over the belt cells alone, each with a priority
+ * flood over the belts, the facet rule, the Kahn order, the implicit incision, the spoil carried to the
+ * belts' outlets and the rounds' thermal sweeps, and every ten rounds the crust's Airy rebound of the
+ * rock taken (a Gaussian of GaussianBlur, .../math/GaussianBlur.kt, at the crust map's spread). */
+/* BeltWindow (BeltErosion.kt:19-24): per cell, what tectonics did to the crust over the window. */
+typedef struct cg_belt_window {
+    const float* tectonic_km;      /* N: km of thickness thickened over the window */
+    const float* wear_km;          /* N: km the orogens' wear took over it */
+    const float* onset_myr_ago;    /* N: when the thickening began, Myr ago; < 0 where none did */
+    double       window_myr;       /* the window's length, Myr (PlateResult.exposureWindowMyr, 40) */
+} cg_belt_window;
+/* The rest of BeltErosion.replay's arguments (host buffers, N floats each where given). */
+typedef struct cg_belt_inputs {
+    const float* uplift_mm_per_year;   /* or NULL: presentUpliftMmPerYear */
+    const float* rainfall_mm;          /* or NULL (all 1): the opening weather's rain */
+    const float* cover_density;        /* or NULL (all 0): the opening weather's cover */
+    const float* rock_erodibility;     /* or NULL */
+    const float* unresolved_relief;    /* or NULL: UnresolvedRelief in the height field's units */
+    float        provisional_sea_level;/* the sea fraction the opening cut takes (WorldGenConfig.seaLevel) */
+    int32_t      shield_cut;           /* 1: the cover's shielding in the incision's factor */
+    int32_t      rebound;              /* IsostasyConfig.enabled: the crust answers the rock taken */
+    double       history_cell_km;      /* TectonicsConfig.historyCellKm (80): the rebound's spread is 0.6 of it */
+} cg_belt_inputs;
+/* BeltReplay (BeltErosion.kt:35-47) without erodedMeters, which the call writes to its own buffer. */
+typedef struct cg_belt_books {
+    int32_t rounds;                         /* 0 where the replay does nothing (BeltReplay.NOTHING) */
+    int32_t belt_cells;
+    double  uplifted_cubic_meters;
+    double  cut_cubic_meters;
+    double  exported_to_sea_cubic_meters;
+    double  exported_to_land_cubic_meters;
+    double  shed_beside_cubic_meters;
+} cg_belt_books;
 /* ---- The stage round by round, its world resident on the context between calls ----
  *
  * HydraulicErosion.apply asks for the weather twice when ErosionConfig.climateFeed is on: on the
@@ -310,6 +348,20 @@ cg_status cg_stage_begin(cg_ctx* ctx, const cg_erosion_params* params, const cg_
 cg_status cg_erode_rounds(cg_ctx* ctx, int32_t first_round, int32_t end_round, const cg_weather* weather,
                           cg_round_stats* stats);
 
+/*
+ * The belts' replay (BeltErosion.replay, see cg_belt_replay below) on the resident world, where
+ * HydraulicErosion.apply runs it: after the initial sweeps and the opening weather, before round 0
+ * (HydraulicErosion.kt:680-688). It reads the stage's uplift and rock, `weather` (may be NULL: the
+ * weather the world was begun with; with climate_feed, the opening weather the caller solved), the
+ * stage's sea level and shield_cut, and no sub-grid relief (the rounds take none). `rebound` is
+ * IsostasyConfig.enabled and `history_cell_km` TectonicsConfig.historyCellKm (80). With profile P3 the
+ * flexure's field before the rounds becomes the replayed one, as in the reference. `eroded_meters`
+ * (N, host, may be NULL) and `books` receive the replay's results; a stage that erodes nothing
+ * (no rounds or no erodibility) replays nothing, as the reference returns before the replay.
+ */
+cg_status cg_stage_replay_belts(cg_ctx* ctx, const cg_belt_window* window, const cg_weather* weather,
+                                int32_t rebound, double history_cell_km, float* eroded_meters,
+                                cg_belt_books* books);
 /* The resident world's current height field (N floats, host), e.g. for the caller's weather solve. */
 cg_status cg_stage_height(cg_ctx* ctx, float* height);
 
@@ -429,44 +481,6 @@ cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* params, const uint8_t*
  * its books with it; a running total is carried by laying it first. No counterpart in the reference.
  */
 cg_status cg_sequential_sum_f64(cg_ctx* ctx, const double* x, int64_t n, double* sum);
-/* ---- The belts' replay (BeltErosion.replay, .../pipeline/BeltErosion.kt:96-425) ----
- *
- * Before the hydraulic rounds, when the plate stage hands the erosion the belts' recent history
- * (ErosionTectonics.window; HydraulicErosion.kt:680-688), each young belt is lowered to where its crust
- * stood when the exposure window opened, raised again round by round at the rate its own thickening
- * came at, and cut as it rises: about a hundred rounds over the belt cells alone, each with a priority
- * flood over the belts, the facet rule, the Kahn order, the implicit incision, the spoil carried to the
- * belts' outlets and the rounds' thermal sweeps, and every ten rounds the crust's Airy rebound of the
- * rock taken (a Gaussian of GaussianBlur, .../math/GaussianBlur.kt, at the crust map's spread). */
-/* BeltWindow (BeltErosion.kt:19-24): per cell, what tectonics did to the crust over the window. */
-typedef struct cg_belt_window {
-    const float* tectonic_km;      /* N: km of thickness thickened over the window */
-    const float* wear_km;          /* N: km the orogens' wear took over it */
-    const float* onset_myr_ago;    /* N: when the thickening began, Myr ago; < 0 where none did */
-    double       window_myr;       /* the window's length, Myr (PlateResult.exposureWindowMyr, 40) */
-} cg_belt_window;
-/* The rest of BeltErosion.replay's arguments (host buffers, N floats each where given). */
-typedef struct cg_belt_inputs {
-    const float* uplift_mm_per_year;   /* or NULL: presentUpliftMmPerYear */
-    const float* rainfall_mm;          /* or NULL (all 1): the opening weather's rain */
-    const float* cover_density;        /* or NULL (all 0): the opening weather's cover */
-    const float* rock_erodibility;     /* or NULL */
-    const float* unresolved_relief;    /* or NULL: UnresolvedRelief in the height field's units */
-    float        provisional_sea_level;/* the sea fraction the opening cut takes (WorldGenConfig.seaLevel) */
-    int32_t      shield_cut;           /* 1: the cover's shielding in the incision's factor */
-    int32_t      rebound;              /* IsostasyConfig.enabled: the crust answers the rock taken */
-    double       history_cell_km;      /* TectonicsConfig.historyCellKm (80): the rebound's spread is 0.6 of it */
-} cg_belt_inputs;
-/* BeltReplay (BeltErosion.kt:35-47) without erodedMeters, which the call writes to its own buffer. */
-typedef struct cg_belt_books {
-    int32_t rounds;                         /* 0 where the replay does nothing (BeltReplay.NOTHING) */
-    int32_t belt_cells;
-    double  uplifted_cubic_meters;
-    double  cut_cubic_meters;
-    double  exported_to_sea_cubic_meters;
-    double  exported_to_land_cubic_meters;
-    double  shed_beside_cubic_meters;
-} cg_belt_books;
 /*
  * BeltErosion.replay on host buffers: `height` (N, the height field) is replayed in place, `eroded_meters`
  * (N, may be NULL) receives the metres each cell lost, `books` the replay's figures. Reads params' grid,

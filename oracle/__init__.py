@@ -92,6 +92,9 @@ def lib():
                                      i32, f64, vp, vp, vp]
         L.or_belt_replay.restype = i32
         L.or_gaussian_blur.argtypes = [i32, i32, vp, f64, f64]
+        L.or_erode_stage_belts.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), vp, vp, vp, f64, i32,
+                                           f64, C.POINTER(abi.Outputs)]
+        L.or_erode_stage_belts.restype = i32
         _lib = L
     return _lib
 
@@ -435,3 +438,31 @@ def gaussian_blur(field, sigma_across, sigma_down):
     H, W = f.shape
     lib().or_gaussian_blur(W, H, P(f), float(sigma_across), float(sigma_down))
     return f
+
+
+def erode_stage_belts(params, height, window, uplift=None, rock=None, rain=None, veg=None, rebound=True,
+                      history_cell_km=80.0, want=("receivers",)):
+    """ErosionStage.apply with the belts' window: window = (tectonic_km, wear_km, onset_myr_ago,
+    window_myr); the replay runs on the swept terrain with the opening weather (rain, veg) before
+    round 0. Returns the outputs as erode_stage does (height plus `want`)."""
+    H, W = params.height, params.width
+    keep = []
+
+    def f32(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float32).reshape(H, W)
+        keep.append(a)
+        return a
+
+    h, up, rk, rn, vg, t, w, o = map(f32, (height, uplift, rock, rain, veg) + tuple(window[:3]))
+    inputs = abi.Inputs(P(h), P(up), P(rk), P(rn), P(vg))
+    kinds = {"receivers": np.int32, "area": np.float32, "filled": np.float32, "relative": np.float32,
+             "is_land": np.uint8, "order": np.int32, "donors": np.int32}
+    outs = {"height": np.empty((H, W), np.float32)}
+    for k in want:
+        outs[k] = np.empty((H, W), kinds[k])
+    o_ = abi.Outputs(**{k: P(v) for k, v in outs.items()})
+    assert lib().or_erode_stage_belts(C.byref(params), C.byref(inputs), P(t), P(w), P(o), float(window[3]),
+                                      int(bool(rebound)), float(history_cell_km), C.byref(o_)) == 0
+    return outs

@@ -2276,9 +2276,31 @@ struct StageOut {
     FlatCounts flats;
 };
 
+// What BeltErosion.replay hands back (BeltReplay, P/BeltErosion.kt:35-47), erodedMeters aside.
+struct BeltBooks {
+    int rounds = 0, belt_cells = 0;
+    double uplifted = 0.0, cut = 0.0, to_sea = 0.0, to_land = 0.0, shed = 0.0;
+};
+
+BeltBooks belt_replay(const cg_erosion_params& p, float* surface, const float* tectonic, const float* wear,
+                      const float* onset, double window_myr, const float* uplift, const float* rain,
+                      const float* cover, const float* rock, float provisional_sea_level, bool shield_cut,
+                      const float* unresolved, bool rebounding, double history_cell_km, float* eroded);
+
+// The belts' window for the stage's replay (ErosionTectonics.window), with IsostasyConfig.enabled and
+// TectonicsConfig.historyCellKm.
+struct BeltStage {
+    const float* tectonic;
+    const float* wear;
+    const float* onset;
+    double window_myr;
+    bool rebound;
+    double history_cell_km;
+};
+
 // ErosionStage.apply (ErosionStage.kt:133-183) with HydraulicErosion.apply (HydraulicErosion.kt:596-1506)
-// for profiles P0 and P1: no provisional climate (the given weather is held), no belt replay, no
-// flexure, no deposition; P1 adds the outlet notch (ErosionConfig.outletIncision): each round's breach
+// for profiles P0 and P1: no provisional climate (the given weather is held), no flexure, no
+// deposition; P1 adds the outlet notch (ErosionConfig.outletIncision): each round's breach
 // before the incision (HydraulicErosion.kt:1002-1028) and the closing breach before the last
 // relaxation (HydraulicErosion.kt:1404-1442). P1's routing outputs are the closing pass's, as its
 // breach left them.
@@ -2287,11 +2309,13 @@ struct StageOut {
 // refreshed (may be NULL) is the weather the provisional climate gives halfway down when
 // params.climate_feed is set (HydraulicErosion.kt:655-661, 809-813): it replaces the given weather
 // from round hydraulic_rounds / 2 on. The climate itself is not this path's: the caller solves it.
+// belts (may be NULL) is the belts' window: BeltErosion.replay runs on the swept terrain with the
+// opening weather before round 0 (HydraulicErosion.kt:680-688), with no sub-grid relief.
 int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out, cg_round_stats* stats,
                 bool with_thermal = true, bool initial = true, int run_rounds = -1,
                 const Switches* switches = nullptr, Tally* tallies = nullptr,
                 LevelRepairs* level_repairs = nullptr, WalkCapture* capture = nullptr,
-                const cg_inputs* refreshed = nullptr) {
+                const cg_inputs* refreshed = nullptr, const BeltStage* belts = nullptr) {
     int W = p.width, H = p.height;
     size_t N = (size_t)W * H;
     Scale sc = scale_of(p);
@@ -2312,6 +2336,16 @@ int erode_stage(const cg_erosion_params& p, const cg_inputs& in, cg_outputs* out
     if (p.hydraulic_rounds <= 0 || p.bedrock_erodibility_per_year <= 0.0f) {
         std::memcpy(out->height, working.data(), N * sizeof(float));
         return CG_OK;
+    }
+    // The belts' replay on the swept terrain, with the opening weather (HydraulicErosion.kt:680-688).
+    if (belts) {
+        std::vector<float> ones_b, zeros_b, eroded_b(N);
+        if (!in.rainfall_mm) ones_b.assign(N, 1.0f);
+        if (!in.vegetation_density) zeros_b.assign(N, 0.0f);
+        belt_replay(p, working.data(), belts->tectonic, belts->wear, belts->onset, belts->window_myr,
+                    in.uplift_mm_per_year, in.rainfall_mm ? in.rainfall_mm : ones_b.data(),
+                    in.vegetation_density ? in.vegetation_density : zeros_b.data(), in.rock_erodibility, p.sea_level,
+                    p.shield_cut != 0, nullptr, belts->rebound, belts->history_cell_km, eroded_b.data());
     }
     Rates rates(p);
     const Switches sw = switches ? *switches : switches_of(p);
@@ -2635,12 +2669,6 @@ void gaussian_blur(int W, int H, float* data, double sigma_across, double sigma_
 
 const double kCrustKernelSpreadSpacings = 0.6;   // CrustMap.KERNEL_SPREAD_SPACINGS (P/CrustMap.kt:521)
 const int kReboundRounds = 10;                   // BeltErosion.REBOUND_ROUNDS
-
-// What BeltErosion.replay hands back (BeltReplay, P/BeltErosion.kt:35-47), erodedMeters aside.
-struct BeltBooks {
-    int rounds = 0, belt_cells = 0;
-    double uplifted = 0.0, cut = 0.0, to_sea = 0.0, to_land = 0.0, shed = 0.0;
-};
 
 // BeltErosion.replay (P/BeltErosion.kt:96-425), statement by statement. `surface` is the height field,
 // changed in place; `eroded` (N) receives the metres each cell lost. rain and cover are required
@@ -3304,6 +3332,14 @@ int32_t or_belt_replay(const cg_erosion_params* p, float* height, const float* t
     books[3] = b.to_land;
     books[4] = b.shed;
     return 0;
+}
+
+// ErosionStage.apply with the belts' window (the stage above with `belts`).
+int32_t or_erode_stage_belts(const cg_erosion_params* p, const cg_inputs* in, const float* tectonic, const float* wear,
+                             const float* onset, double window_myr, int32_t rebound, double history_cell_km,
+                             cg_outputs* out) {
+    BeltStage b{tectonic, wear, onset, window_myr, rebound != 0, history_cell_km};
+    return erode_stage(*p, *in, out, nullptr, true, true, -1, nullptr, nullptr, nullptr, nullptr, nullptr, &b);
 }
 
 // GaussianBlur.apply (MA/GaussianBlur.kt:44-111) in place.

@@ -137,3 +137,29 @@ def test_books_close_on_the_device():
     exported = got.exported_to_sea_cubic_meters + got.exported_to_land_cubic_meters
     assert got.cut_cubic_meters > 0.0
     assert abs(got.cut_cubic_meters - exported) / got.cut_cubic_meters <= 1e-6
+
+
+@pytest.mark.parametrize("W,H,seed,profile", [(256, 128, 5, 0), (128, 64, 3, 2), (128, 64, 7, 3)])
+def test_stage_with_the_window_matches_the_oracle(W, H, seed, profile):
+    # ErosionStage.apply with ErosionTectonics.window: the initial sweeps, the replay on the resident
+    # swept terrain (cg_stage_replay_belts), then the rounds, bit-identical to the oracle's stage; the
+    # replay's books are the standalone replay's on the same swept terrain.
+    from cartogenesis_gb300 import StageRounds
+    h, up, rk = synthetic.world(W, H, seed)
+    t, w, o, win = synthetic.belt_window(W, H, seed)
+    cfg = ErosionConfig(W, H, seed, profile=profile)
+    run = StageRounds(cfg, h, up, rk)
+    swept = run.height()
+    rep = run.replay_belts(BeltWindow(t, w, o, win))
+    run.rounds(cfg.params.hydraulic_rounds)
+    got = run.finish(want=("receivers",))
+    want = oracle.erode_stage_belts(oracle.default_params(W, H, seed, profile=profile), h, (t, w, o, win), uplift=up,
+                                    rock=rk)
+    assert np.array_equal(got.height.view(np.uint32), want["height"].view(np.uint32))
+    assert np.array_equal(got.receivers, want["receivers"])
+    alone = BeltErosion.replay(ErosionConfig(W, H, seed, profile=profile), swept.copy(), BeltWindow(t, w, o, win), up,
+                               None, None, rk)
+    assert rep.rounds == alone.rounds == 106
+    for k in BOOKS:
+        assert same(getattr(rep, k), getattr(alone, k)), k
+    assert np.array_equal(rep.eroded_meters.view(np.uint32), alone.eroded_meters.view(np.uint32))

@@ -138,3 +138,21 @@ def test_gaussian_blur_keeps_a_constant_and_spreads_a_point_evenly(sigma):
     assert np.allclose(b[64 - 3, 10], b[64 + 3, 10], rtol=0, atol=1e-7)
     # Zero spread leaves an axis alone.
     assert np.array_equal(oracle.gaussian_blur(d, 0.0, 0.0), d)
+
+
+@pytest.mark.parametrize("profile", [0, 2, 3])
+def test_stage_with_the_window_is_sweeps_then_replay_then_rounds(profile):
+    # HydraulicErosion.kt:680-688: the replay runs on the swept terrain before round 0, with the stage's
+    # uplift, rock, sea level and shield_cut and the opening weather; the rounds (the flexure's field
+    # before them included) start from the replayed terrain.
+    W, H = 128, 64
+    h, up, rk, t, w, o, win = world(W, H)
+    p = oracle.default_params(W, H, seed=SEED, profile=profile)
+    whole = oracle.erode_stage_belts(p, h, (t, w, o, win), uplift=up, rock=rk)["height"]
+    swept = oracle.thermal_sweep(h, oracle.thermal_limits(p)[0], oracle.thermal_limits(p)[1])
+    replayed, _, books = oracle.belt_replay(p, swept, t, w, o, win, uplift=up, rock=rk)
+    assert books["rounds"] == 106
+    parts = oracle.stage_rounds(p, replayed, up, rk, rounds=p.hydraulic_rounds)
+    assert np.array_equal(whole.view(np.uint32), parts.view(np.uint32))
+    plain = oracle.erode_stage(p, h, up, rk, want=())["height"]
+    assert not np.array_equal(whole, plain)
