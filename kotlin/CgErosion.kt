@@ -6,6 +6,7 @@ package com.cartogenesis.desktop
 
 import com.cartogenesis.worldgen.model.FloatField
 import com.cartogenesis.worldgen.model.WorldGenConfig
+import com.cartogenesis.worldgen.pipeline.BeltWindow
 import com.cartogenesis.worldgen.pipeline.ErosionAccelerator
 import com.cartogenesis.worldgen.pipeline.SeaLevelResult
 import com.cartogenesis.worldgen.pipeline.ThermalLimits
@@ -37,9 +38,12 @@ interface HydraulicAccelerator {
      * (HydraulicErosion.kt:655-661, 809-813): with climateFeed on, on the swept terrain before round 0
      * and again before round hydraulicRounds / 2, each time with the terrain as it stands and the
      * round about to cut; with it off it is never called and the rounds cut with no weather.
+     * `window` (ErosionTectonics.window, or null) is the belts' history: the belts are replayed on the
+     * swept terrain with the opening weather before round 0 (BeltErosion.replay, HydraulicErosion.kt:680-688).
      */
     fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
-                   rockErodibility: FloatField?, weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField
+                   rockErodibility: FloatField?, window: BeltWindow?,
+                   weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField
 }
 
 /** cg_erosion.h's status codes. */
@@ -70,6 +74,8 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     private val rounds = fn("cg_erode_rounds", FunctionDescriptor.of(JAVA_INT, ADDRESS, JAVA_INT, JAVA_INT, ADDRESS, ADDRESS))
     private val current = fn("cg_stage_height", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
     private val finish = fn("cg_stage_finish", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
+    private val replayBelts = fn("cg_stage_replay_belts", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS,
+        JAVA_INT, JAVA_DOUBLE, ADDRESS, ADDRESS))
     private val seaCut = fn("cg_sea_level_cut", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS, JAVA_DOUBLE,
         JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS, ADDRESS))
     private val ctx: MemorySegment
@@ -114,16 +120,17 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
         }
     }
 
-    // The parts of the stage the library does not run: the belts' replay (needs the plate history)
-    // and the relief finer than the grid. The flexure's transform lines must fit a CTA: width <= 8192,
-    // height <= 4096.
+    // The part of the stage the library does not run is the relief finer than the grid
+    // (orogenicExcessKm), which the engine checks beside this. The flexure's transform lines must fit a
+    // CTA: width <= 8192, height <= 4096.
     override fun supports(config: WorldGenConfig): Boolean {
         val profile = profileOf(config)
         return profile >= 0 && (profile < 3 || (config.width <= 8192 && config.height <= 4096))
     }
 
     override fun erodeStage(config: WorldGenConfig, height: FloatField, upliftMmPerYear: FloatField?,
-                            rockErodibility: FloatField?, weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField =
+                            rockErodibility: FloatField?, window: BeltWindow?,
+                            weather: ((FloatField, Int) -> Pair<FloatArray, FloatArray>)?): FloatField =
         Arena.ofConfined().use { a ->
             // cg_erosion_params, 144 bytes (offsets as in cg_erosion.h, checked by the C tests).
             val p = a.allocate(144, 8)
@@ -161,20 +168,37 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
             val result = a.allocate(JAVA_FLOAT, height.data.size.toLong())
             val outputs = a.allocate(80, 8)   // cg_outputs: height, then nine optional pointers
             outputs.set(ADDRESS, 0, result)
-            if (!fed) {
+            if (!fed && window == null) {
                 check(stage.invokeExact(ctx, p, inputs, outputs, MemorySegment.NULL) as Int, ctx, lastError)
             } else {
-                // climateFeed: stop where HydraulicErosion.apply asks the weather, ask it, go on.
+                // Stop where HydraulicErosion.apply asks the weather (climateFeed) or replays the belts.
                 check(begin.invokeExact(ctx, p, inputs) as Int, ctx, lastError)
                 val total = config.erosion.hydraulicRounds
                 val half = if (total > 1) total / 2 else total
-                var done = 0
-                for (end in listOf(half, total).distinct()) {
+                fun askWeather(round: Int): MemorySegment {
+                    if (!fed) return MemorySegment.NULL
                     check(current.invokeExact(ctx, result) as Int, ctx, lastError)
-                    val (rain, cover) = weather!!(FloatField(config.width, config.height, result.toArray(JAVA_FLOAT)), done)
+                    val (rain, cover) = weather!!(FloatField(config.width, config.height, result.toArray(JAVA_FLOAT)), round)
                     val w = a.allocate(16, 8)   // cg_weather
                     w.set(ADDRESS, 0, field(rain))
                     w.set(ADDRESS, 8, field(cover))
+                    return w
+                }
+                val opening = askWeather(0)
+                if (window != null) {
+                    val win = a.allocate(32, 8)   // cg_belt_window
+                    win.set(ADDRESS, 0, field(window.tectonicKm.data))
+                    win.set(ADDRESS, 8, field(window.wearKm.data))
+                    win.set(ADDRESS, 16, field(window.onsetMyrAgo.data))
+                    win.set(JAVA_DOUBLE, 24, window.windowMyr)
+                    val books = a.allocate(48, 8)   // cg_belt_books
+                    check(replayBelts.invokeExact(ctx, win, opening, if (config.isostasy.enabled) 1 else 0,
+                                                  config.tectonics.historyCellKm, MemorySegment.NULL, books) as Int,
+                          ctx, lastError)
+                }
+                var done = 0
+                for (end in (if (fed) listOf(half, total) else listOf(total)).distinct()) {
+                    val w = if (done == 0) opening else askWeather(done)
                     check(rounds.invokeExact(ctx, done, end, w, MemorySegment.NULL) as Int, ctx, lastError)
                     done = end
                 }
