@@ -421,6 +421,26 @@ class BeltErosion:
 
 class FlowRouting:
     @staticmethod
+    def route_cut(config, is_land, relative, land_cells, weights=None, ctx=None):
+        """fillDepressions, flowDirections, accumulate (weights, or all ones) and drainageOrder of one
+        cut in a single device call, as DrownedValleys, RiverStage and GlaciationStage run them on their
+        own cut (cg_route_cut). Returns (filled, receivers, area, order)."""
+        ctx = ctx or default_context()
+        p = config.params
+        H, W = p.height, p.width
+        il = np.ascontiguousarray(is_land, dtype=np.uint8).reshape(H, W)
+        rel = _f32(relative, (H, W))
+        w = _f32(weights, (H, W))
+        filled = np.empty((H, W), np.float32)
+        recv = np.empty((H, W), np.int32)
+        area = np.empty((H, W), np.float32)
+        order = np.empty(max(int(land_cells), 1), np.int32)
+        with ctx.lock:
+            ctx.check(ctx.lib.cg_route_cut(ctx.handle, C.byref(p), P(il), P(rel), int(land_cells), P(w), P(filled),
+                                           P(recv), P(area), P(order)))
+        return filled, recv, area, order[:int(land_cells)]
+
+    @staticmethod
     def fill_depressions(is_land, elevation, ctx=None, with_ties=False):
         ctx = ctx or default_context()
         rel = np.ascontiguousarray(elevation, dtype=np.float32)

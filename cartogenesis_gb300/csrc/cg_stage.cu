@@ -807,6 +807,60 @@ cg_status cg_accumulate(cg_ctx* ctx, int32_t W, int32_t H, const uint8_t* is_lan
     return sync(ctx);
 }
 
+cg_status cg_route_cut(cg_ctx* ctx, const cg_erosion_params* p, const uint8_t* is_land, const float* relative,
+                       int32_t land_cells, const float* weights, float* filled, int32_t* receivers, float* area,
+                       int32_t* order) {
+    if (!ctx || !p || !is_land || !relative || !receivers || land_cells < 0) return CG_BAD_ARG;
+    ctx->run.active = false;   // this call reuses the resident world's buffers
+    if (p->abi_version != CG_ABI_VERSION)
+        return fail(ctx, CG_BAD_ARG, "params carry ABI version %u, this library is %u", p->abi_version,
+                    CG_ABI_VERSION);
+    const int W = p->width, H = p->height;
+    CG_TRY(check_grid(ctx, W, H));
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t N = (size_t)W * H;
+    const int grid = ctx->num_sms * 8;
+    CG_BUF(uint8_t, d_land, ctx, S_LAND, N);
+    CG_BUF(float, d_rel, ctx, S_REL, N);
+    CG_BUF(float, d_filled, ctx, S_FILLED, N);
+    CG_BUF(double, d_surface, ctx, S_SURFACE, N);
+    CG_BUF(int32_t, d_recv, ctx, S_RECV, N);
+    CG_TRY(up(ctx, d_land, is_land, N));
+    CG_TRY(up(ctx, d_rel, relative, N * 4));
+    // FlowRouting.fillDepressions, then flowDirections over it (FlowRouting.kt:52-111, 179-216).
+    CG_TRY(fill_depressions_dev(ctx, W, H, d_land, d_rel, d_filled, nullptr, nullptr));
+    const ScaleF sc = scale_of(*p);
+    FlatCounts fc{0, 0, 0};
+    CG_TRY(flow_directions_dev(ctx, W, H, d_land, d_rel, d_filled, p->seed, sc.cell_height_km(H) / sc.cell_width_km(W),
+                               smooth_field_lattice_columns(p->world_width_km), p->facet_routing != 0,
+                               p->flat_potential != 0, d_recv, d_surface, &fc));
+    // accumulate (weights, or { 1f }) and drainageOrder over those receivers (FlowRouting.kt:485-511, 695-729).
+    if (area || order) {
+        CG_BUF(int32_t, d_donors, ctx, S_DONORS, N);
+        CG_BUF(long long, d_key, ctx, S_KEY, N);
+        float *d_w = nullptr, *d_area = nullptr;
+        if (area) {
+            CG_BUF(float, w, ctx, S_RUNOFF, N);
+            CG_BUF(float, a, ctx, S_AREA, N);
+            d_w = w;
+            d_area = a;
+            if (weights) CG_TRY(up(ctx, d_w, weights, N * 4));
+            else CG_LAUNCH(ctx) k_fill_value<<<grid, 256, 0, ctx->stream>>>(d_w, N, 1.0f);
+            CG_CHECK_LAUNCH(ctx);
+        }
+        CG_TRY(tree_walk_dev(ctx, W, H, d_land, d_recv, d_w, d_key, d_donors, d_area, nullptr));
+        if (order) {
+            CG_BUF(int32_t, d_order, ctx, S_ORDER, N);
+            CG_TRY(order_from_keys_dev(ctx, W, H, d_land, d_key, land_cells, d_order));
+            if (land_cells > 0) CG_TRY(down(ctx, order, d_order, (size_t)land_cells * 4));
+        }
+        if (area) CG_TRY(down(ctx, area, d_area, N * 4));
+    }
+    if (filled) CG_TRY(down(ctx, filled, d_filled, N * 4));
+    CG_TRY(down(ctx, receivers, d_recv, N * 4));
+    return sync(ctx);
+}
+
 cg_status cg_breach(cg_ctx* ctx, const cg_erosion_params* p, const uint8_t* is_land, float* relative, float* ground,
                     const int32_t* receivers, const float* area, float land_cells, float land_range, float* surface,
                     int32_t* cells_cut) {

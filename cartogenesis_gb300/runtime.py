@@ -16,7 +16,7 @@ EXPORTS = [
     "cg_drainage_order", "cg_accumulate", "cg_spillways", "cg_breach",
     "cg_stage_begin", "cg_erode_rounds", "cg_stage_height", "cg_stage_finish", "cg_sea_level_cut",
     "cg_flexure_deflection", "cg_sequential_sum", "cg_sequential_sum_f64", "cg_belt_replay", "cg_gaussian_blur",
-    "cg_stage_replay_belts",
+    "cg_stage_replay_belts", "cg_route_cut",
 ]
 
 
@@ -82,6 +82,7 @@ def load_library(path=LIB_PATH):
             L.cg_belt_replay.argtypes = [vp, PP, vp, C.POINTER(abi.BeltWindow), C.POINTER(abi.BeltInputs), vp,
                                          C.POINTER(abi.BeltBooks)]
             L.cg_gaussian_blur.argtypes = [vp, i32, i32, vp, f64, f64]
+            L.cg_route_cut.argtypes = [vp, PP, vp, vp, i32, vp, vp, vp, vp, vp]
             L.cg_stage_replay_belts.argtypes = [vp, C.POINTER(abi.BeltWindow), C.POINTER(abi.Weather), i32, f64, vp,
                                                 C.POINTER(abi.BeltBooks)]
         _lib = L

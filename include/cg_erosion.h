@@ -387,6 +387,17 @@ cg_status cg_erode_batch(cg_ctx* ctx, int32_t n_worlds, const cg_world* worlds, 
 
 /* ---- The stage's routing functions, each run alone on host buffers (FlowRouting, SeaLevelStage) ---- */
 
+/*
+ * FlowRouting's routing of one sea-level cut in one call, as the stages after the erosion run it on
+ * their own cut: fillDepressions, flowDirections (params' seed, cell aspect, lattice, facet_routing and
+ * flat_potential), accumulate with `weights` (all ones when NULL, the `{ 1f }` of DrownedValleys) and
+ * drainageOrder (land cells first, land_cells entries). DrownedValleys.kt:411-421, RiverStage.kt:228-240
+ * and 306-308 (with the runoff as weights), GlaciationStage.kt:371-385 (the order for its ice walk).
+ * Host buffers; `receivers` is required, `filled`, `area` and `order` may be NULL.
+ */
+cg_status cg_route_cut(cg_ctx* ctx, const cg_erosion_params* params, const uint8_t* is_land, const float* relative,
+                       int32_t land_cells, const float* weights, float* filled, int32_t* receivers, float* area,
+                       int32_t* order);
 /* SeaLevelStage.percentileCut (.../pipeline/SeaLevelStage.kt:146-200, 579-651). */
 cg_status cg_percentile_cut(cg_ctx* ctx, int32_t width, int32_t height, const float* heights,
                             float sea_level_fraction, float highest_land_metres,

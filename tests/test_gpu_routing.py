@@ -249,3 +249,23 @@ def test_drainage_order_accumulate_spillways(W, H, seed):
         assert np.array_equal(bits(sw_got[k]), bits(sw_want[k])), k
     for k in ("largest", "largest_cells", "largest_depth", "deepest"):
         assert sw_got[k] == sw_want[k], k
+
+
+@pytest.mark.parametrize("W,H,seed", [(128, 64, 3), (512, 256, 7), (256, 256, 5)])
+def test_route_cut_is_the_downstream_stages_routing(W, H, seed):
+    # cg_route_cut: fillDepressions, flowDirections, accumulate and drainageOrder of one cut in one call,
+    # as DrownedValleys.kt:411-421, RiverStage.kt:228-240 and GlaciationStage.kt:371-385 run them.
+    from cartogenesis_gb300 import ErosionConfig
+    _, (s, land, rel, n) = world_cut(W, H, seed)
+    cfg = ErosionConfig(W, H, seed)
+    r = (cfg.params.world_width_km * 0.5 / H) / (cfg.params.world_width_km / W)
+    filled_w = oracle.fill_depressions(land, rel)
+    rec_w, _ = oracle.flow_directions(land, rel, filled_w, seed, r, 214)
+    filled, rec, area, order = FlowRouting.route_cut(cfg, land, rel, n)
+    assert np.array_equal(bits(filled), bits(filled_w))
+    assert np.array_equal(rec, rec_w)
+    assert np.array_equal(bits(area), bits(oracle.accumulate(land, rec_w, n, np.ones((H, W), np.float32))))
+    assert np.array_equal(order, oracle.drainage_order(land, rec_w, n))
+    w = np.random.default_rng(seed).uniform(0.3, 3.0, (H, W)).astype(np.float32)
+    _, _, area_w, _ = FlowRouting.route_cut(cfg, land, rel, n, weights=w)
+    assert np.array_equal(bits(area_w), bits(oracle.accumulate(land, rec_w, n, w)))
