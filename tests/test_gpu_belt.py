@@ -163,3 +163,13 @@ def test_stage_with_the_window_matches_the_oracle(W, H, seed, profile):
     for k in BOOKS:
         assert same(getattr(rep, k), getattr(alone, k)), k
     assert np.array_equal(rep.eroded_meters.view(np.uint32), alone.eroded_meters.view(np.uint32))
+
+
+def test_replay_matches_the_oracle_at_2048x1024():
+    # 158,795 belt cells, 106 rounds, with the rebound's blur at a spread of 2.5 cells; the books close.
+    W, H, seed = 2048, 1024, 21
+    surface, got, want_h, want_e, want, o = run_both(W, H, seed)
+    assert got.belt_cells > 100000
+    check(surface, got, want_h, want_e, want)
+    exported = got.exported_to_sea_cubic_meters + got.exported_to_land_cubic_meters
+    assert abs(got.cut_cubic_meters - exported) / got.cut_cubic_meters <= 1e-6
