@@ -156,3 +156,31 @@ def test_stage_with_the_window_is_sweeps_then_replay_then_rounds(profile):
     assert np.array_equal(whole.view(np.uint32), parts.view(np.uint32))
     plain = oracle.erode_stage(p, h, up, rk, want=())["height"]
     assert not np.array_equal(whole, plain)
+
+
+@pytest.mark.parametrize("W,H", [(512, 512), (512, 256)])
+def test_a_point_spreads_as_far_on_the_ground_whichever_way_it_goes(W, H):
+    # T:GaussianBlurTest.kt:26-58: a point blurred by 93.75 km, handed over as that many columns and
+    # rows, keeps its mass to 1e-5, spreads 93.75 km each way on the ground to a hundredth, and does not
+    # lean along a diagonal.
+    spread_km = 93.75
+    cw, ch = 40075.0 / W, 40075.0 * 0.5 / H
+    f = np.zeros((H, W), np.float32)
+    f[H // 2, W // 2] = 1.0
+    b = oracle.gaussian_blur(f, spread_km / cw, spread_km / ch).astype(np.float64)
+    east = (np.arange(W) - W // 2) * cw
+    south = (np.arange(H) - H // 2) * ch
+    total = b.sum()
+    ew = (b * east[None, :] ** 2).sum()
+    ns = (b * south[:, None] ** 2).sum()
+    across = (b * east[None, :] * south[:, None]).sum()
+    assert abs(total - 1.0) < 1e-5
+    assert abs(np.sqrt(ew / total) / spread_km - 1.0) < 0.01
+    assert abs(np.sqrt(ns / total) / spread_km - 1.0) < 0.01
+    assert abs(across / np.sqrt(ew * ns)) < 0.01
+
+
+def test_a_constant_stays_that_constant():
+    # T:GaussianBlurTest.kt:60-66.
+    f = np.full((64, 64), 0.625, np.float32)
+    assert np.abs(oracle.gaussian_blur(f, 3.0, 6.0) - np.float32(0.625)).max() < 1e-6
