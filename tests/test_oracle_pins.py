@@ -294,3 +294,50 @@ def test_accumulate_sums_weights_down_the_forest():
     il = is_land.ravel().astype(bool)
     mouths = [c for c in np.flatnonzero(il) if flat_rec[c] < 0 or not il[flat_rec[c]]]
     assert abs(sum(float(area.ravel()[m]) for m in mouths) - land) < 1e-3
+
+
+def test_one_round_asks_what_the_stream_power_law_and_the_clock_say():
+    """T:ErosionUnitsTest.kt:163-247: a 32-column plane falling due west at 1 m/km into a deep sea on a
+    128 x 128 map a quarter land, one round, no climate, deposition, notch, flexure or relaxation. The
+    law's rate the pass spends on a cell k cells below the crest, F times the drop to its receiver as
+    the pass found it, is K T sqrt(k A) S to a thousandth, with F from 0.24 at one cell to 1.3 at
+    thirty. F is read back from the cut: after = base + (h - base) / (1 + F), the base the receiver's
+    height after the pass."""
+    import math
+    W = H = 128
+    land_cols = W // 4
+    p = oracle.default_params(W, H, seed=7, sea_level=np.float32(1.0 - land_cols / W), hydraulic_rounds=1,
+                              climate_feed=0, profile=0, lowstand_metres=0.0)
+    f32 = np.float32
+    span = f32(6000.0) + f32(10000.0)
+
+    def field_at(m):   # WorldScale.fieldAtAltitude
+        return f32((f32(m) + f32(10000.0)) / span)
+
+    fall = f32(1.0 * 40075.0 / W)
+    first = (W - land_cols) // 2
+    g = np.empty((H, W), np.float32)
+    for r in range(H):
+        for c in range(W):
+            up = c - first + 1
+            g[r, c] = (field_at(f32(up) * fall) if 1 <= up <= land_cols
+                       else field_at(f32(-4000.0) - f32(r * W + c) * f32(0.01)))
+    _, _, _, n = oracle.percentile_cut(g, p.sea_level, 0.0)
+    assert 0 <= n - land_cols * H <= 1   # SEA_CELLS_READ_AS_LAND
+    out = oracle.erode_stage(p, g, thermal=False, want=("receivers",))
+    after, rec = out["height"].ravel(), out["receivers"].ravel()
+    crest = first + land_cols - 1
+    cell_area = (1.0 - float(p.sea_level)) * 40075.0 ** 2 * 0.5 / n * 1e6
+    worst, fs = 0.0, []
+    for k in range(1, 31):
+        law = float(p.bedrock_erodibility_per_year) * p.years_per_hydraulic_round * math.sqrt(k * cell_area) * 1e-3
+        for row in (H // 4, H // 2, 3 * H // 4):
+            c = row * W + crest - k
+            r = rec[c]
+            assert r == c - 1   # due west
+            h0, a, b, b0 = float(g.ravel()[c]), float(after[c]), float(after[r]), float(g.ravel()[r])
+            F = (h0 - b) / (a - b) - 1.0
+            worst = max(worst, abs(F * (h0 - b0) * float(span) / law - 1.0))
+            fs.append(F)
+    assert worst <= 1e-3, worst
+    assert abs(min(fs) - 0.24) < 0.01 and abs(max(fs) - 1.3) < 0.01
