@@ -341,3 +341,115 @@ def test_one_round_asks_what_the_stream_power_law_and_the_clock_say():
             fs.append(F)
     assert worst <= 1e-3, worst
     assert abs(min(fs) - 0.24) < 0.01 and abs(max(fs) - 1.3) < 0.01
+
+
+STEADY_SIDE = 64
+
+
+def _steady_state(uplift_mm, zone_of, rock_of, rain_of):
+    """ImplicitIncisionTest.steadyState (T:ImplicitIncisionTest.kt:640-752): a 64 x 64 island lifted
+    every round and cut by the routing and the incision (no thermal pass, deposition or notch) until
+    no land cell moves by more than 1e-3 of a round's uplift, the routing taken afresh for 1000 rounds
+    and then held. Returns (rounds, {zone: (channel cells, concavity, median steepness in m)})."""
+    import math
+    f32 = np.float32
+    side = STEADY_SIDE
+    p = oracle.default_params(side, side, seed=11, climate_feed=0, profile=0)
+    N = side * side
+    span = f32(16000.0)
+    land_range, sea_half = f32(6000.0) / span, f32(10000.0) / span
+    shoreline = f32((f32(0.0) + f32(10000.0)) / span)   # WorldScale.fieldAtAltitude(0)
+    cell = np.arange(N)
+    row, col = cell // side, cell % side
+    land = ((row >= 2) & (row < side - 2) & (col >= 3) & (col < side - 3)).astype(np.uint8)
+    n = int(land.sum())
+    zones = np.array([zone_of(r) for r in row])
+    erod = np.array([rock_of(z) for z in zones], np.float32)
+    rain = np.array([rain_of(z) for z in zones], np.float32)
+    rain_sum = 0.0
+    for c in range(N):   # the stage's sequential double sum over the land
+        if land[c]:
+            rain_sum += float(rain[c])
+    weight = (rain / f32(rain_sum / n)).astype(np.float32)
+    up = f32(f32(uplift_mm / 1000.0 * p.years_per_hydraulic_round) / span)
+    rough = ((cell.astype(np.int64) * 2654435761) >> 7) % 1000
+    metres = (f32(1.0) + (f32(5.0) * rough.astype(np.float32)) / f32(1000.0)).astype(np.float32)
+    surface = np.where(land == 1, ((metres + f32(10000.0)) / span).astype(np.float32),
+                       f32((f32(-100.0) + f32(10000.0)) / span)).astype(np.float32)
+    lm = land.reshape(side, side)
+    r = 0.5   # cellHeightInCellWidths of a square grid
+    rounds = 0
+    while True:
+        rounds += 1
+        assert rounds <= 20000, "no balance in 20000 rounds"
+        prev = surface.copy()
+        surface[land == 1] = (surface[land == 1] + up).astype(np.float32)
+        rel = np.where(land == 1, (surface - shoreline) / land_range,
+                       (surface - shoreline) / sea_half).astype(np.float32).reshape(side, side)
+        filled = oracle.fill_depressions(lm, rel)
+        if rounds <= 1000:
+            rec, _ = oracle.flow_directions(lm, rel, filled, 11, r, 214)
+            disc = oracle.accumulate(lm, rec, n, weight.reshape(side, side))
+            order = oracle.drainage_order(lm, rec, n)
+        oracle.incise(p, order, rec, land, filled, rel, disc, f32(n), land_range, shoreline, erod, surface)
+        if rounds > 1000 and np.abs(surface[land == 1] - prev[land == 1]).max() < f32(1e-3) * up:
+            break
+    upstream = oracle.accumulate(lm, rec, n, np.ones((side, side), np.float32)).ravel()
+    land_area = (1.0 - float(f32(0.71))) * 40075.0 ** 2 * 0.5 * 1e6
+    cell_m = 40075.0 / side * 1000.0
+    step_ns, step_diag = float(f32(r)), float(f32(math.sqrt(1.0 + r * r)))
+    recf = rec.ravel()
+    out = {}
+    for z in sorted(set(zones)):
+        in_zone = oracle.accumulate(lm, rec, n, (zones == z).astype(np.float32).reshape(side, side)).ravel()
+        la, ls, steep = [], [], []
+        for c in range(N):
+            if not land[c] or zones[c] != z or upstream[c] < 4 or in_zone[c] != upstream[c]:
+                continue
+            d = recf[c]
+            if d < 0:
+                continue
+            fall = float(f32(surface[c] - (surface[d] if land[d] else shoreline))) * 16000.0
+            if fall <= 0.0:
+                continue
+            same_row, same_col = c // side == d // side, c % side == d % side
+            step = step_diag if not same_row and not same_col else (step_ns if not same_row else 1.0)
+            slope = fall / (step * cell_m)
+            area = float(upstream[c]) / n * land_area
+            la.append(math.log(area))
+            ls.append(math.log(slope))
+            steep.append(slope * math.sqrt(area))
+        la, ls = np.array(la), np.array(ls)
+        theta = -np.sum((la - la.mean()) * (ls - ls.mean())) / np.sum((la - la.mean()) ** 2)
+        steep.sort()
+        out[z] = (len(la), float(theta), steep[len(steep) // 2])
+    return rounds, out
+
+
+def test_at_balance_the_profiles_are_the_laws_across_rock_and_uplift():
+    """T:ImplicitIncisionTest.kt:763-820: under uniform uplift the concavity at balance is m / n = 0.5
+    and the steepness U / (K e) in each of two rocks (e 0.5 and 2), and doubles with the uplift, each
+    to a hundredth."""
+    rock = {"hard": 0.5, "soft": 2.0}
+    res = {}
+    for uplift in (0.1, 0.2):
+        _, out = _steady_state(uplift, lambda r: "hard" if r < STEADY_SIDE // 2 else "soft", rock.get, lambda z: 1.0)
+        res[uplift] = out
+        for z, e in rock.items():
+            cells, theta, steep = out[z]
+            assert cells > 50
+            assert abs(theta - 0.5) <= 0.01, (uplift, z, theta)
+            assert abs(steep / (uplift / 1000.0 / (1e-6 * e)) - 1.0) <= 0.01, (uplift, z, steep)
+    for z in rock:
+        assert abs(res[0.2][z][2] / res[0.1][z][2] / 2.0 - 1.0) <= 0.01
+    assert abs(res[0.1]["hard"][2] / res[0.1]["soft"][2] / 4.0 - 1.0) <= 0.01
+
+
+def test_at_balance_the_steepness_falls_as_the_square_root_of_the_rain():
+    """T:ImplicitIncisionTest.kt:822-857: a wet zone with four times the dry zone's rain, one rock: the
+    concavity stays 0.5 in both and the wet steepness is half the dry, each to a hundredth."""
+    _, out = _steady_state(0.1, lambda r: "wet" if r < STEADY_SIDE // 2 else "dry", lambda z: 1.0,
+                           lambda z: 4.0 if z == "wet" else 1.0)
+    for z in ("wet", "dry"):
+        assert abs(out[z][1] - 0.5) <= 0.01, (z, out[z])
+    assert abs(out["wet"][2] / out["dry"][2] / 0.5 - 1.0) <= 0.01, out
