@@ -453,3 +453,78 @@ def test_at_balance_the_steepness_falls_as_the_square_root_of_the_rain():
     for z in ("wet", "dry"):
         assert abs(out[z][1] - 0.5) <= 0.01, (z, out[z])
     assert abs(out["wet"][2] / out["dry"][2] / 0.5 - 1.0) <= 0.01, out
+
+
+def _knickpoint(southward, rounds, share):
+    """ImplicitIncisionTest.knickpoint (T:ImplicitIncisionTest.kt:870-935): a 40-cell-width profile
+    into the sea along a row or down a column of a 128 x 128 grid, a break in slope (60 m a cell width
+    below, 20 above) 12 cell widths from the sea, the same F = 2 along a row on both bearings, the sea
+    lowered each round with the lower reach, cut by the incision for `rounds` rounds of `share` of the
+    clock. Returns (sharp-break distance, steepest-change point, smear) in cell widths."""
+    f32 = np.float32
+    lower, upper, knick, length, courant_ew = 60.0, 20.0, 12.0, 40, 2.0
+    span = f32(16000.0)
+
+    def field_at(m):
+        return f32((f32(m) + f32(10000.0)) / span)
+
+    side = 128
+    p = oracle.default_params(side, side, seed=3)
+    p.years_per_hydraulic_round = p.years_per_hydraulic_round * share
+    courant = oracle.rates(p)[1]
+    step = float(f32(0.5)) if southward else 1.0
+    cells = int(length / step)
+    N = side * side
+    start = 20 * side + 64 if southward else 64 * side + 4
+    stride = side if southward else 1
+    prof = [start + (i + 1) * stride for i in range(cells)]
+    land = np.zeros(N, np.uint8)
+    dirs = np.full(N, -1, np.int32)
+    for i, c in enumerate(prof):
+        land[c] = 1
+        dirs[c] = start if i == 0 else prof[i - 1]
+    surface = np.full(N, field_at(0.0), np.float32)
+    for i, c in enumerate(prof):
+        g = (i + 1) * step
+        m = 1000.0 + lower * g if g <= knick else 1000.0 + lower * knick + upper * (g - knick)
+        surface[c] = field_at(f32(m))
+    root = courant_ew / (float(courant) / share)
+    disc = np.full(N, f32(root * root), np.float32)
+    erod = np.ones(N, np.float32)
+    order = np.array(prof[::-1], np.int32)
+    land_half = f32(6000.0) / span
+    sea = 1000.0
+    for _ in range(rounds):
+        sea -= courant_ew * share * lower
+        rel = ((surface - field_at(0.0)) / land_half).astype(np.float32)
+        oracle.incise(p, order, dirs, land, rel, rel, disc, f32(1.0), land_half, field_at(f32(sea)), erod, surface)
+    h = np.array([float(f32(surface[c] * span - f32(10000.0))) for c in prof])   # altitudeAtField
+    sharp = ((h[-1] - sea) - upper * cells * step) / (lower - upper)
+    slopes = np.array([(h[i] - (sea if i == 0 else h[i - 1])) / step for i in range(cells)])
+    mids = (np.arange(cells) + 0.5) * step
+
+    def crossing(s):
+        level = upper + (lower - upper) * s
+        for i in range(1, cells):
+            if slopes[i - 1] >= level > slopes[i]:
+                a = (slopes[i - 1] - level) / (slopes[i - 1] - slopes[i])
+                return mids[i - 1] + a * (mids[i] - mids[i - 1])
+        return float("nan")
+
+    return sharp, crossing(0.5), crossing(0.1) - crossing(0.9)
+
+
+def test_a_knickpoint_retreats_as_far_north_south_as_east_west_and_in_two_half_rounds():
+    """T:ImplicitIncisionTest.kt:937-996: the break, read as a sharp break of equal relief, retreats the
+    law's F = 2 cell widths a round along a row, to 1e-3, and as far down a column and in two half
+    rounds; read as the steepest-change point, the four retreats agree to a cell width."""
+    start, ns_start = _knickpoint(False, 0, 1.0), _knickpoint(True, 0, 1.0)
+    ew, ns = _knickpoint(False, 1, 1.0), _knickpoint(True, 1, 1.0)
+    ewh, nsh = _knickpoint(False, 2, 0.5), _knickpoint(True, 2, 0.5)
+    retreat = ew[0] - start[0]
+    assert retreat > 0.0 and abs(retreat - 2.0) <= 1e-3, retreat
+    for other in (ns[0] - ns_start[0], ewh[0] - start[0], nsh[0] - ns_start[0]):
+        assert abs(other - retreat) <= 1e-3, (other, retreat)
+    mid = ew[1] - start[1]
+    for other in (ns[1] - ns_start[1], ewh[1] - start[1], nsh[1] - ns_start[1]):
+        assert abs(other - mid) <= 1.0, (other, mid)
