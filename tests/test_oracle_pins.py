@@ -528,3 +528,64 @@ def test_a_knickpoint_retreats_as_far_north_south_as_east_west_and_in_two_half_r
     mid = ew[1] - start[1]
     for other in (ns[1] - ns_start[1], ewh[1] - start[1], nsh[1] - ns_start[1]):
         assert abs(other - mid) <= 1.0, (other, mid)
+
+
+def _facet_share(fall, rs):
+    """RoutingGroundTest.facetShare (T:RoutingGroundTest.kt:214-228): the share of a plane's steps the
+    facet rule sends to the diagonal, and whether that facet's cardinal is a column step."""
+    import math
+    off = math.atan2(abs(math.sin(fall)), abs(math.cos(fall)))
+    if off <= math.atan2(rs, 1.0):
+        return math.tan(off) / rs, False
+    return rs * math.tan(math.pi / 2 - off), True
+
+
+@pytest.mark.parametrize("rs,want", [(0.5, (44.87, 15.31, 39.82)), (1.0, (27.94, 27.94, 44.13))])
+def test_the_facet_rule_takes_each_bearing_as_often_as_its_geometry_says(rs, want):
+    """T:RoutingGroundTest.kt:84-213: on 128 x 128 planes at 360 bearings and three seeds, the facet
+    rule's Rho8 draws take a column, a row and a diagonal as often as the facets' geometry says (44.87,
+    15.31 and 39.82% on cells half as tall as wide; 27.94, 27.94 and 44.13% on square ones), each
+    within four standard errors, and each plane's mean step points down it within 4.5."""
+    import math
+    side, margin, bearings, seeds = 128, 16, 360, (7, 42, 1234)
+    taken, expected = np.zeros(3), np.zeros(3)
+    per = np.zeros((len(seeds), 3, side * side))
+    worst = 0.0
+    land = np.ones((side, side), np.uint8)
+    cols = np.arange(side)[None, :].astype(np.float64)
+    rows = np.arange(side)[:, None].astype(np.float64)
+    inner = np.zeros((side, side), bool)
+    inner[margin:side - margin, margin:side - margin] = True
+    index = np.arange(side * side).reshape(side, side)[inner]
+    for si, seed in enumerate(seeds):
+        for i in range(bearings):
+            deg = (i + 0.5) * 360.0 / bearings
+            fall = math.radians(deg)
+            plane = (0.5 - 1e-3 * (cols * math.cos(fall) + rows * rs * math.sin(fall))).astype(np.float32)
+            rec, _ = oracle.flow_directions(land, plane, plane, seed, rs, 8)
+            share, colwise = _facet_share(fall, rs)
+            t = rec[inner]
+            ok = t >= 0
+            t, c = t[ok], index[ok]
+            dc, dr = (t % side) - (c % side), (t // side) - (c // side)
+            way = np.where(dc == 0, 0, np.where(dr == 0, 1, 2))
+            for k in range(3):
+                taken[k] += (way == k).sum()
+            np.add.at(per[si], (way, c), 1.0)
+            per[si, 2, c] -= share
+            per[si, 0 if colwise else 1, c] -= 1 - share
+            expected[2] += len(t) * share
+            expected[0 if colwise else 1] += len(t) * (1 - share)
+            x, y = dc.astype(np.float64), dr * rs
+            mx, my = x.mean(), y.mean()
+            err = (math.degrees(math.atan2(my, mx)) - deg + 180.0) % 360.0 - 180.0
+            ax, ay = -math.sin(fall), math.cos(fall)
+            var = (ax * ax * ((x * x).mean() - mx * mx) + ay * ay * ((y * y).mean() - my * my)
+                   + 2 * ax * ay * ((x * y).mean() - mx * my))
+            sigma = math.sqrt(max(var, 0.0) / len(t)) / math.hypot(mx, my) * 180.0 / math.pi
+            worst = max(worst, abs(err) / sigma if sigma > 0 else (0.0 if abs(err) < 1e-9 else math.inf))
+    cells = taken.sum()
+    for k in range(3):
+        assert abs(100.0 * expected[k] / cells - want[k]) < 0.01
+        assert abs(taken[k] - expected[k]) <= 4.0 * math.sqrt((per[:, k, :] ** 2).sum()), k
+    assert worst <= 4.5, worst
