@@ -92,6 +92,7 @@ def lib():
                                      i32, f64, vp, vp, vp]
         L.or_belt_replay.restype = i32
         L.or_gaussian_blur.argtypes = [i32, i32, vp, f64, f64]
+        L.or_flat_stencil.argtypes = [f64, vp]
         L.or_erode_stage_belts.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), vp, vp, vp, f64, i32,
                                            f64, C.POINTER(abi.Outputs)]
         L.or_erode_stage_belts.restype = i32
@@ -466,3 +467,10 @@ def erode_stage_belts(params, height, window, uplift=None, rock=None, rain=None,
     assert lib().or_erode_stage_belts(C.byref(params), C.byref(inputs), P(t), P(w), P(o), float(window[3]),
                                       int(bool(rebound)), float(history_cell_km), C.byref(o_)) == 0
     return outs
+
+
+def flat_stencil(r):
+    """FlatRouting.stencil: (east-west, north-south, diagonal) weights on cells r as tall as wide."""
+    w = np.zeros(3, np.float64)
+    lib().or_flat_stencil(float(r), P(w))
+    return tuple(float(x) for x in w)

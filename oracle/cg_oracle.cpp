@@ -3342,6 +3342,15 @@ int32_t or_erode_stage_belts(const cg_erosion_params* p, const cg_inputs* in, co
     return erode_stage(*p, *in, out, nullptr, true, true, -1, nullptr, nullptr, nullptr, nullptr, nullptr, &b);
 }
 
+// FlatRouting.stencil (FlatRouting.kt:177-186): the flat Laplacian's east-west, north-south and
+// diagonal weights on cells r as tall as they are wide.
+void or_flat_stencil(double r, double* weights) {
+    Stencil s = stencil_of(r);
+    weights[0] = s.ew;
+    weights[1] = s.ns;
+    weights[2] = s.diag;
+}
+
 // GaussianBlur.apply (MA/GaussianBlur.kt:44-111) in place.
 void or_gaussian_blur(int32_t W, int32_t H, float* data, double sigma_across, double sigma_down) {
     gaussian_blur(W, H, data, sigma_across, sigma_down);

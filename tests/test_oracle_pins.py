@@ -589,3 +589,42 @@ def test_the_facet_rule_takes_each_bearing_as_often_as_its_geometry_says(rs, wan
         assert abs(100.0 * expected[k] / cells - want[k]) < 0.01
         assert abs(taken[k] - expected[k]) <= 4.0 * math.sqrt((per[:, k, :] ** 2).sum()), k
     assert worst <= 4.5, worst
+
+
+@pytest.mark.parametrize("aspect", [0.25, 0.5, 1.0, 2.0])
+def test_the_potential_across_a_flat_is_round_on_the_ground(aspect):
+    """T:RoutingGroundTest.kt:239-300: a flat of radius 50 cell widths, one flat-gradient step of fill
+    over its floor, its outlet one lower cell at the centre and a rim far above: laid (one flat, none
+    kept), and at 10, 20, 30 and 40 cell widths from the outlet the north-south quarters' mean
+    potential is the east-west quarters' within a tenth, on cells a quarter to twice as tall as wide."""
+    import math
+    columns = 128
+    rows = int(math.ceil(128 / aspect))
+    cc, cr = columns // 2, rows // 2
+    across = (np.arange(columns)[None, :] - cc).astype(np.float64)
+    down = (np.arange(rows)[:, None] - cr) * aspect
+    dist = np.sqrt(across ** 2 + down ** 2)
+    ground = np.where(dist <= 50.0, np.float32(0.0), np.float32(10.0)).astype(np.float32)
+    filled = np.where(dist <= 50.0, np.float32(1e-3), np.float32(10.0)).astype(np.float32)
+    ground[cr, cc] = filled[cr, cc] = np.float32(-1.0)
+    land = np.ones((rows, columns), np.uint8)
+    _, surf, counts = oracle.flow_directions(land, ground, filled, 1, aspect, 8, want_surface=True)
+    assert counts[0] == 1 and counts[1] == 0, counts   # one flat, laid
+    floor = surf[cr, cc + 1]
+    for radius in (10.0, 20.0, 30.0, 40.0):
+        ring = np.abs(dist - radius) <= 0.75 * max(1.0, aspect)
+        ew = ring & (np.abs(across) > np.abs(down))
+        ns = ring & ~(np.abs(across) > np.abs(down))
+        ratio = (surf[ns] - floor).mean() / (surf[ew] - floor).mean()
+        assert abs(ratio - 1.0) <= 0.10, (aspect, radius, ratio)
+
+
+def test_the_flats_weights_are_positive_and_isotropic_on_cells_of_every_shape():
+    """T:RoutingGroundTest.kt:313-332: for r = 2^k, k from -8 to 8, every weight of the flat Laplacian
+    is positive and e + 2d = r^2 (n + 2d) to 1e-9."""
+    for k in range(-8, 9):
+        r = 2.0 ** k
+        ew, ns, d = oracle.flat_stencil(r)
+        assert ew > 0 and ns > 0 and d > 0, (r, ew, ns, d)
+        a, b = ew + 2.0 * d, r * r * (ns + 2.0 * d)
+        assert abs(a - b) <= 1e-9 * a, (r, a, b)
