@@ -628,3 +628,23 @@ def test_the_flats_weights_are_positive_and_isotropic_on_cells_of_every_shape():
         assert ew > 0 and ns > 0 and d > 0, (r, ew, ns, d)
         a, b = ew + 2.0 * d, r * r * (ns + 2.0 * d)
         assert abs(a - b) <= 1e-9 * a, (r, a, b)
+
+
+def test_the_sea_covers_the_share_of_the_planet_the_slider_asks_for():
+    """T:SeaShareTest.kt:26-58: ground falling from the equator to both poles on a 512 x 256 map, half
+    the planet asked for: the percentile cut drowns half the planet's area (the ground poleward of 30
+    degrees) to 1e-3, where a cut by the map's cells would drown 0.29 of it."""
+    import math
+    cols, rows = 512, 256
+    lat = 90.0 - (np.arange(rows) + 0.5) * 180.0 / rows
+    h = (-np.abs(lat)[:, None] + np.arange(cols)[None, :] * 1e-4).astype(np.float32)
+    shoreline, _, _, _ = oracle.percentile_cut(h, 0.5, 0.0)
+    weight = np.cos(np.radians(lat))[:, None] * np.ones((1, cols))
+
+    def share(mask):
+        return float((weight * mask).sum() / weight.sum())
+
+    drowned = share(h < np.float32(shoreline))
+    by_cells = np.sort(h.ravel())[int(h.size * 0.5)]
+    assert abs(drowned - 0.5) <= 1e-3, drowned
+    assert abs(share(h < by_cells) - 0.5) > 0.1
