@@ -76,6 +76,8 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
     private val finish = fn("cg_stage_finish", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS))
     private val replayBelts = fn("cg_stage_replay_belts", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS,
         JAVA_INT, JAVA_DOUBLE, ADDRESS, ADDRESS))
+    private val routeCutFn = fn("cg_route_cut", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS,
+        JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS, ADDRESS))
     private val seaCut = fn("cg_sea_level_cut", FunctionDescriptor.of(JAVA_INT, ADDRESS, ADDRESS, ADDRESS, JAVA_DOUBLE,
         JAVA_INT, ADDRESS, ADDRESS, ADDRESS, ADDRESS, ADDRESS))
     private val ctx: MemorySegment
@@ -233,6 +235,36 @@ class GbErosion(library: Path, device: Int = 0) : ErosionAccelerator, HydraulicA
         val isLand = BooleanArray(cells.toInt()) { land.get(java.lang.foreign.ValueLayout.JAVA_BYTE, it.toLong()) != 0.toByte() }
         SeaLevelResult(shoreline.get(JAVA_FLOAT, 0), isLand,
                        FloatField(config.width, config.height, relative.toArray(JAVA_FLOAT)), count.get(JAVA_INT, 0))
+    }
+
+    /** What [routeCut] hands back: FlowRouting's fill, receivers, accumulation and drainage order. */
+    class RoutedCut(val filled: FloatField, val receivers: IntArray, val area: FloatField, val order: IntArray)
+
+    /**
+     * The routing the stages after the erosion run on their own cut (DrownedValleys.kt:411-421,
+     * RiverStage.kt:228-240 and 306-308, GlaciationStage.kt:371-385), in one call: fillDepressions,
+     * flowDirections, accumulate with `weights` (null: the `{ 1f }` weights) and drainageOrder.
+     */
+    fun routeCut(config: WorldGenConfig, isLand: BooleanArray, relative: FloatField, landCells: Int,
+                 weights: FloatArray?): RoutedCut = Arena.ofConfined().use { a ->
+        val p = a.allocate(144, 8)
+        defaults.invokeExact(p, config.width, config.height, config.seed)
+        p.set(JAVA_DOUBLE, 24, config.scale.worldWidthKm)
+        p.set(JAVA_INT, 76, if (config.facetRouting) 1 else 0)
+        p.set(JAVA_INT, 80, if (config.flatPotential) 1 else 0)
+        val cells = relative.data.size.toLong()
+        val land = a.allocate(cells)
+        for (i in 0 until cells.toInt()) land.set(java.lang.foreign.ValueLayout.JAVA_BYTE, i.toLong(), if (isLand[i]) 1 else 0)
+        val rel = a.allocateFrom(JAVA_FLOAT, *relative.data)
+        val w = if (weights == null) MemorySegment.NULL else a.allocateFrom(JAVA_FLOAT, *weights)
+        val filled = a.allocate(JAVA_FLOAT, cells)
+        val receivers = a.allocate(JAVA_INT, cells)
+        val area = a.allocate(JAVA_FLOAT, cells)
+        val order = a.allocate(JAVA_INT, maxOf(landCells, 1).toLong())
+        check(routeCutFn.invokeExact(ctx, p, land, rel, landCells, w, filled, receivers, area, order) as Int, ctx, lastError)
+        RoutedCut(FloatField(config.width, config.height, filled.toArray(JAVA_FLOAT)), receivers.toArray(JAVA_INT),
+                  FloatField(config.width, config.height, area.toArray(JAVA_FLOAT)),
+                  order.toArray(JAVA_INT).copyOf(landCells))
     }
 
     override fun close() {
