@@ -93,6 +93,7 @@ def lib():
         L.or_belt_replay.restype = i32
         L.or_gaussian_blur.argtypes = [i32, i32, vp, f64, f64]
         L.or_flat_stencil.argtypes = [f64, vp]
+        L.or_facet_flip_delta.argtypes = [i32, i32, vp, vp, vp, i64, f64, vp]
         L.or_erode_stage_belts.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), vp, vp, vp, f64, i32,
                                            f64, C.POINTER(abi.Outputs)]
         L.or_erode_stage_belts.restype = i32
@@ -474,3 +475,16 @@ def flat_stencil(r):
     w = np.zeros(3, np.float64)
     lib().or_flat_stencil(float(r), P(w))
     return tuple(float(x) for x in w)
+
+
+def facet_flip_delta(surface, mask, raised, seed, r):
+    """Per cell of `mask`, the relative change of the routing surface at the `raised` cells (the flats'
+    potentials; the rest is exact) that could change its facet receiver, to first order; +inf where
+    none could."""
+    rs = np.ascontiguousarray(surface, dtype=np.float64)
+    H, W = rs.shape
+    m = np.ascontiguousarray(mask, dtype=np.uint8)
+    rz = np.ascontiguousarray(raised, dtype=np.uint8)
+    out = np.empty((H, W), np.float64)
+    lib().or_facet_flip_delta(W, H, P(rs), P(m), P(rz), int(seed), float(r), P(out))
+    return out

@@ -3342,6 +3342,91 @@ int32_t or_erode_stage_belts(const cg_erosion_params* p, const cg_inputs* in, co
     return erode_stage(*p, *in, out, nullptr, true, true, -1, nullptr, nullptr, nullptr, nullptr, nullptr, &b);
 }
 
+// How far the flats' potentials must move before FlowRouting.facetReceiver's answer can change, per
+// cell of `mask`: the relative change delta of the routing surface at the cells of `raised` (each such
+// value v moving by up to delta |v|; the other values are the filled field widened, exact) that
+// could close the gap between the steepest facet and a facet whose receiver (its draw included) is
+// another cell, or carry the winning facet's diagonal share across the cell's Rho8 draw. To first order: a facet
+// slope moves by at most 2 delta (the sum of its moving values' |v|) / (its shortest leg), a share by
+// share (|d outward| / outward + |d cdrop| / cdrop). Cells outside the mask, with no facet falling, or
+// whose deciding values are all exact, get +inf.
+void or_facet_flip_delta(int32_t W, int32_t H, const double* rs, const uint8_t* mask, const uint8_t* raised,
+                         int64_t seed, double r, double* out) {
+    GroundSteps steps(r);
+    for (int row = 0; row < H; ++row)
+        for (int col = 0; col < W; ++col) {
+            const int cell = row * W + col;
+            out[cell] = INFINITY;
+            if (!mask[cell]) continue;
+            const double here = rs[cell];
+            const double e_here = raised[cell] ? std::fabs(here) : 0.0;
+            struct Facet {
+                double slope, moves, share, outward, cdrop, m_out, m_drop;
+                int kind, card, diag;
+            } f[8];
+            int nf = 0, win = -1;
+            double best = 0.0;
+            for (int side = 0; side < 4; ++side) {
+                int ccs = kCardColStep[side], crs = kCardRowStep[side];
+                int card = neighbour_at(W, H, col + ccs, row + crs);
+                if (card < 0) continue;
+                const double e_card = raised[card] ? std::fabs(rs[card]) : 0.0;
+                double cdrop = here - rs[card];
+                double to_card = (double)steps.of(ccs, crs);
+                double on_to_diag = (double)(ccs == 0 ? steps.east_west : steps.north_south);
+                for (int turn = -1; turn <= 1; turn += 2) {
+                    int dcs = ccs == 0 ? turn : ccs;
+                    int drs = crs == 0 ? turn : crs;
+                    int diag = neighbour_at(W, H, col + dcs, row + drs);
+                    if (diag < 0) continue;
+                    const double e_diag = raised[diag] ? std::fabs(rs[diag]) : 0.0;
+                    double dfall = here - rs[diag];
+                    double dslope = dfall / (double)steps.diagonal;
+                    double outward = dfall - cdrop;
+                    double cslope = cdrop / to_card;
+                    double oslope = outward / on_to_diag;
+                    double share_edge =
+                        cdrop > 0.0 ? outward * to_card * to_card / (cdrop * on_to_diag * on_to_diag) : 1.0;
+                    bool to_cardinal = cdrop > 0.0 && outward <= 0.0;
+                    bool to_diagonal = !to_cardinal && share_edge >= 1.0;
+                    double fslope = to_cardinal ? cslope
+                                                : (to_diagonal ? dslope : std::sqrt(cslope * cslope + oslope * oslope));
+                    double share = to_cardinal ? 0.0 : (to_diagonal ? 1.0 : share_edge);
+                    const double leg = std::min({to_card, on_to_diag, (double)steps.diagonal});
+                    const int kind = share <= 0.0 ? 1 : (share >= 1.0 ? 2 : 3);
+                    f[nf] = Facet{fslope, 2.0 * (e_here + e_card + e_diag) / leg, share, outward, cdrop,
+                                  e_here + e_diag + e_card, e_here + e_card, kind, card, diag};
+                    if (fslope > best) {
+                        best = fslope;
+                        win = nf;
+                    }
+                    ++nf;
+                }
+            }
+            if (win < 0) continue;
+            const Facet& w = f[win];
+            // Each facet's receiver as the rule would take it, the draw included.
+            const double draw = sub_grid_draw(col, row, seed);
+            auto taken = [&](const Facet& g) {
+                return g.kind == 1 ? g.card : (g.kind == 2 ? g.diag : (draw < g.share ? g.diag : g.card));
+            };
+            double delta = INFINITY;
+            for (int i = 0; i < nf; ++i) {
+                const Facet& g = f[i];
+                if (i == win) continue;
+                if (taken(g) == taken(w) || w.moves + g.moves <= 0.0) continue;
+                delta = std::min(delta, (w.slope - g.slope) / (w.moves + g.moves));
+            }
+            // The no-receiver threshold: the winner's slope against zero.
+            if (w.moves > 0.0) delta = std::min(delta, w.slope / w.moves);
+            if (w.kind == 3 && (w.m_out > 0.0 || w.m_drop > 0.0)) {
+                const double d_share = w.share * (2.0 * w.m_out / w.outward + 2.0 * w.m_drop / w.cdrop);
+                if (d_share > 0.0) delta = std::min(delta, std::fabs(draw - w.share) / d_share);
+            }
+            out[cell] = delta;
+        }
+}
+
 // FlatRouting.stencil (FlatRouting.kt:177-186): the flat Laplacian's east-west, north-south and
 // diagonal weights on cells r as tall as they are wide.
 void or_flat_stencil(double r, double* weights) {
