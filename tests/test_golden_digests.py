@@ -22,3 +22,8 @@ def test_oracle_stage_matches_committed_digests(W, H, seed, profile):
     want = TABLE[f"{W}x{H}-seed{seed}-P{profile}"]
     got = golden.digests(W, H, seed, profile)
     assert got == want
+
+
+@pytest.mark.parametrize("W,H,seed", golden.WORLDS)
+def test_oracle_belt_replay_matches_committed_digests(W, H, seed):
+    assert golden.belt_digests(W, H, seed) == TABLE[f"{W}x{H}-seed{seed}-belt"]
