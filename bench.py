@@ -429,7 +429,6 @@ def run_belt(args):
     window and factors in, the replayed heights and eroded depths out, every copy inside the timing.
     The unit is Mcell-rounds/s over the belt's cells: belt cells x replayed rounds / seconds. The CPU
     leg runs the oracle's replay of the same world over a window cut to --cpu-sample replayed rounds."""
-    import numpy as np
     import oracle
     from cartogenesis_gb300 import BeltErosion, BeltWindow, ErosionConfig, synthetic
     from cartogenesis_gb300.api import default_context
