@@ -93,6 +93,10 @@ def lib():
         L.or_belt_replay.restype = i32
         L.or_gaussian_blur.argtypes = [i32, i32, vp, f64, f64]
         L.or_flat_stencil.argtypes = [f64, vp]
+        L.or_grow_fan_fixture.argtypes = [i32, i32, i32, f64, f32, f32, f32, i32, i32, f32, vp, i32, vp]
+        L.or_grow_fan_fixture.restype = f64
+        L.or_fan_hash.argtypes = [i64, i32]
+        L.or_fan_hash.restype = i32
         L.or_facet_flip_delta.argtypes = [i32, i32, vp, vp, vp, i64, f64, vp]
         L.or_erode_stage_belts.argtypes = [C.POINTER(abi.ErosionParams), C.POINTER(abi.Inputs), vp, vp, vp, f64, i32,
                                            f64, C.POINTER(abi.Outputs)]
@@ -488,3 +492,19 @@ def facet_flip_delta(surface, mask, raised, seed, r):
     out = np.empty((H, W), np.float64)
     lib().or_facet_flip_delta(W, H, P(rs), P(m), P(rz), int(seed), float(r), P(out))
     return out
+
+
+def fan_hash(seed, index):
+    """DeltaFan.hash(seed, index)."""
+    return lib().or_fan_hash(int(seed), int(index))
+
+
+def grow_fan_fixture(surface, apex, r, reach, out_x, out_y, hash_, grooved=False, wobble=0.30, bent=False):
+    """DeltaFan.growFan on `surface` as DeltaOutlineTest drives it: every cell accepted, the distance bent
+    by 1 - surface when `bent`, every level 0. Returns (sediment laid per cell, volume laid)."""
+    s = np.ascontiguousarray(surface, dtype=np.float32)
+    H, W = s.shape
+    sed = np.empty((H, W), np.float32)
+    laid = lib().or_grow_fan_fixture(W, H, int(apex), float(r), float(reach), float(out_x), float(out_y), int(hash_),
+                                     int(bool(grooved)), float(wobble), P(s), int(bool(bent)), P(sed))
+    return sed, laid

@@ -1446,6 +1446,7 @@ struct Rim {
     float groove_half_width;
     GroundSteps steps;
     float row_scale;
+    float wobble = kFanWobble;   // DeltaFan.Rim's wobble (DeltaFan.WOBBLE unless a caller sets it)
 
     static void phase(int32_t hash, int slot, float& x, float& y) {
         float hx = fan_draw(hash, slot * 2) * 2.0f - 1.0f;
@@ -1508,7 +1509,7 @@ struct Rim {
         float term = (kWobbleW2 * (c2 * ph2x - s2 * ph2y) + kWobbleW3 * (c3 * ph3x - s3 * ph3y) +
                       kWobbleW5 * (c5 * ph5x - s5 * ph5y) + kWobbleW7 * (c7 * ph7x - s7 * ph7y)) *
                      kWobbleTotalInverse;
-        return reach_cells * nose * (1.0f + kFanWobble * term);
+        return reach_cells * nose * (1.0f + wobble * term);
     }
 
     bool grooved(float column_offset, float row_offset) const {
@@ -3426,6 +3427,26 @@ void or_facet_flip_delta(int32_t W, int32_t H, const double* rs, const uint8_t* 
             out[cell] = delta;
         }
 }
+
+// DeltaFan.growFan driven straight, as DeltaOutlineTest drives it (T:DeltaOutlineTest.kt:556-688): a rim
+// at `apex` with the given reach, bearing, hash, grooves and wobble, every cell accepted, its distance
+// bent by 1 - surface when `bent` (else 1), every level 0, a budget of 1e9. `sediment` (N, zeroed
+// here) receives what the fan laid; returns the volume laid.
+double or_grow_fan_fixture(int32_t W, int32_t H, int32_t apex, double r, float reach, float out_x, float out_y,
+                           int32_t hash, int32_t grooved, float wobble, const float* surface, int32_t bent,
+                           float* sediment) {
+    const size_t N = (size_t)W * H;
+    std::fill(sediment, sediment + N, 0.0f);
+    std::vector<float> settled(N, 0.0f);
+    FanScratch scratch(N, (int)reach, r);
+    Rim rim(apex, W, r, reach, out_x, out_y, hash, grooved != 0);
+    rim.wobble = wobble;
+    return grow_fan(
+        W, H, 1e9, rim, scratch, 1, surface, sediment, settled.data(), 1.0f, false, nullptr, [](int) { return true; },
+        [&](int c) { return bent ? 1.0f - surface[c] : 1.0f; }, [](int, float) { return 0.0f; });
+}
+
+int32_t or_fan_hash(int64_t seed, int32_t index) { return fan_hash(seed, index); }
 
 // FlatRouting.stencil (FlatRouting.kt:177-186): the flat Laplacian's east-west, north-south and
 // diagonal weights on cells r as tall as they are wide.

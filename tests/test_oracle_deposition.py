@@ -100,3 +100,43 @@ def test_level_schedule_reproduces_the_walk(W, H, seed, uplift, replays, redos):
     levels, (replayed, redone) = oracle.erode_stage_levels(p, h, up, rk)
     assert np.array_equal(bits(levels), bits(walk))
     assert replayed >= replays and redone >= redos
+
+
+@pytest.mark.parametrize("r", [1.0, 0.5])
+def test_a_lobe_reaches_as_far_north_as_east_on_the_ground(r):
+    """T:DeltaOutlineTest.kt:546-597: a directionless lobe of 40 cell widths, no wobble, grown on open flat
+    water at the centre of a 256 x 256 grid reaches as far east-west as north-south on the ground, to a
+    cell width (the project's 2:1 grids have square cells; half-height cells are read too)."""
+    W = H = 256
+    apex = (H // 2) * W + W // 2
+    sed, laid = oracle.grow_fan_fixture(np.full((H, W), -1.0, np.float32), apex, r, 40.0, 0.0, 0.0,
+                                        oracle.fan_hash(42, 1), grooved=False, wobble=0.0)
+    assert laid > 0
+    rows, cols = np.nonzero(sed > 0)
+    east_west = np.abs(cols[rows == H // 2] - W // 2).max()
+    north_south = (np.abs(rows[cols == W // 2] - H // 2) * r).max()
+    assert abs(east_west - north_south) <= 1.0, (east_west, north_south)
+
+
+def test_a_fan_reaches_further_over_a_shelf_than_into_deep_water():
+    """T:DeltaOutlineTest.kt:599-688: a lobe of 24 cells aimed east from the edge between a 0.2-deep shelf
+    and 6-deep water, over 24 mouths: with the depth term (the distance bent by 1 - surface) it
+    reaches on average at least 1.5 times as far over the shelf as into the deep water; without it,
+    not."""
+    W = H = 96
+    ax, ay = 32, 48
+    surface = np.where(np.arange(H)[:, None] < ay, np.float32(-0.2), np.float32(-6.0)) * np.ones((1, W), np.float32)
+    ratios = {True: [], False: []}
+    for trial in range(24):
+        h = oracle.fan_hash(9001, trial)
+        for bent in (True, False):
+            sed, _ = oracle.grow_fan_fixture(surface, ay * W + ax, 1.0, 24.0, 1.0, 0.0, h, grooved=False,
+                                             wobble=0.30, bent=bent)
+            rows, cols = np.nonzero(sed > 0)
+            dx, dy = (cols - ax).astype(np.float64), (rows - ay).astype(np.float64)
+            rr = np.sqrt(dx * dx + dy * dy)
+            shelf = rr[dy < 0].max() if (dy < 0).any() else 0.0
+            deep = rr[dy > 0].max() if (dy > 0).any() else 0.0
+            ratios[bent].append(shelf / max(deep, 1e-9))
+    assert np.mean(ratios[False]) < 1.5
+    assert np.mean(ratios[True]) >= 1.5, np.mean(ratios[True])
