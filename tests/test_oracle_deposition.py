@@ -140,3 +140,68 @@ def test_a_fan_reaches_further_over_a_shelf_than_into_deep_water():
             ratios[bent].append(shelf / max(deep, 1e-9))
     assert np.mean(ratios[False]) < 1.5
     assert np.mean(ratios[True]) >= 1.5, np.mean(ratios[True])
+
+
+def _rim_shape(w, h, apex, mask, bins=32):
+    """DeltaOutlineTest.rimOf (T:DeltaOutlineTest.kt:454-532): per angle bin the farthest cell laid;
+    the rim's max / min radius, its RMS departure from a fitted a0 + a1 cos + b1 sin over the mean, and
+    its RMS difference from its reflection about the fitted axis (snapped to a half bin) over the mean."""
+    import math
+    ax, ay = apex % w, apex // w
+    radius = np.full(bins, -1.0)
+    for c in np.flatnonzero(mask.ravel()):
+        dx = c % w - ax
+        dx = dx - w if dx > w // 2 else (dx + w if dx < -(w // 2) else dx)
+        dy = c // w - ay
+        r = math.hypot(dx, dy)
+        if r <= 0:
+            continue
+        a = math.atan2(dy, dx) / (2 * math.pi)
+        a = a + 1.0 if a < 0 else a
+        b = min(max(int(a * bins), 0), bins - 1)
+        radius[b] = max(radius[b], r)
+    filled = [b for b in range(bins) if radius[b] > 0]
+    if len(filled) < bins // 4:
+        return None
+    pos = radius[radius > 0]
+    ratio = pos.max() / pos.min()
+    t = np.array([2 * math.pi * (b + 0.5) / bins for b in filled])
+    A = np.stack([np.ones_like(t), np.cos(t), np.sin(t)], axis=1)
+    fit = np.linalg.solve(A.T @ A, A.T @ radius[filled])
+    mean = radius[filled].mean()
+    residual = math.sqrt(((radius[filled] - A @ fit) ** 2).mean()) / mean
+    k = math.floor(math.atan2(fit[2], fit[1]) / (math.pi / bins) + 0.5)   # Math.round
+    asq, pairs = 0.0, 0
+    for b in filled:
+        m = (k - b - 1) % bins
+        if radius[m] <= 0:
+            continue
+        asq += (radius[b] - radius[m]) ** 2
+        pairs += 1
+    asymmetry = 0.0 if pairs < bins // 4 else math.sqrt(asq / pairs) / mean
+    return ratio, residual, asymmetry
+
+
+def test_a_lobe_is_not_a_disc_and_not_a_cosine():
+    """T:DeltaOutlineTest.kt:286-383: over 24 mouths on open water, a lobe of 24 cells with its wobble has
+    a rim whose radius varies by at least 1.5 and differs by at least 6% from its reflection about its
+    own axis; the compass-drawn controls (a half-disc with no direction, a cosine lobe with no wobble)
+    fail those bars."""
+    W = H = 128
+    apex = 64 * W + 64
+    shapes = {"shaped": (1.0, 0.0, 0.30), "cosine lobe": (1.0, 0.0, 0.0), "half-disc": (0.0, 0.0, 0.0)}
+    worst = {}
+    for trial in range(24):
+        h = oracle.fan_hash(4242, trial)
+        for name, (ox, oy, wob) in shapes.items():
+            sed, _ = oracle.grow_fan_fixture(np.full((H, W), -1.0, np.float32), apex, 1.0, 24.0, ox, oy, h,
+                                             grooved=False, wobble=wob)
+            shape = _rim_shape(W, H, apex, sed > 0)
+            if shape is None:
+                continue
+            pick = min if name == "shaped" else max
+            worst[name] = tuple(pick(a, b) for a, b in zip(worst.get(name, shape), shape))
+    assert worst["half-disc"][0] < 1.5
+    assert worst["cosine lobe"][2] < 0.06 and worst["half-disc"][2] < 0.06
+    assert worst["shaped"][0] >= 1.5, worst
+    assert worst["shaped"][2] >= 0.06, worst
